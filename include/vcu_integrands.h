@@ -1,0 +1,424 @@
+/*
+ * vcu_integrands.h -- built-in integrands of libviltrum_cuda, compiled identically for the host
+ * (g++, -ffp-contract=off) and the device (nvcc).
+ *
+ * An integrand cannot cross a C ABI as code, so every integrand the library can run is a
+ * trivially-copyable functor defined here and selected by a VCU_F_* tag (vcu_integrand::kind).
+ * The functor is built on the host from a flat float parameter array and handed to the kernels
+ * BY VALUE (a __grid_constant__ kernel parameter), exactly as viltrum passes its integrand
+ * functor by const reference into Integrator::integrate (src/integrate.h:72-79).
+ *
+ * Every operation is spelled out with explicit rounding (vmul/vadd/vsub/vfma below): on the
+ * device they map to the __f*_rn intrinsics, which the compiler never contracts; on the host
+ * the file is compiled with -ffp-contract=off.  The transcendental functions are the
+ * project's own (vexp, vsin, vcos: Cody-Waite range reduction + Taylor polynomials), not the
+ * platform's, so a host evaluation and a device evaluation of the same point return the same
+ * bits.  This is what lets the adaptive-quadrature split decisions of the GPU be compared
+ * one-to-one with the CPU reference path.
+ */
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define VCU_HD __host__ __device__ __forceinline__
+#else
+#define VCU_HD inline
+#include <cmath>
+#include <cstring>
+#endif
+
+namespace vcu {
+
+/* ---------------------------------------------------------------- explicit-rounding ops */
+VCU_HD float vmul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+VCU_HD float vadd(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+VCU_HD float vsub(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+VCU_HD float vdiv(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+VCU_HD float vfma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fmaf(a, b, c);
+#endif
+}
+VCU_HD float vrint(float a) {
+#if defined(__CUDA_ARCH__)
+    return rintf(a);
+#else
+    return std::rint(a);
+#endif
+}
+VCU_HD float vabs(float a) {
+#if defined(__CUDA_ARCH__)
+    return fabsf(a);
+#else
+    return std::fabs(a);
+#endif
+}
+VCU_HD float bits_to_float(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f; std::memcpy(&f, &u, 4); return f;
+#endif
+}
+
+/* ---------------------------------------------------------------- portable transcendentals
+ * Constants are exact splits of ln 2 and pi/2 into float parts with 12 significant bits in
+ * the high and middle parts (so k*hi and k*mid are exact for |k| < 2^12), and the Taylor
+ * coefficients 1/n! rounded to float.  Both were computed from exact decimal arithmetic.   */
+constexpr float kLog2e = 1.4426950216293335f;
+constexpr float kLn2Hi = 0.693115234375f;
+constexpr float kLn2Mi = 3.193318843841553e-05f;
+constexpr float kLn2Lo = 1.2996506981721723e-08f;
+constexpr float kTwoOverPi = 0.6366197466850281f;
+constexpr float kPio2Hi = 1.5703125f;
+constexpr float kPio2Mi = 0.0004837512969970703f;
+constexpr float kPio2Lo = 7.549790126404332e-08f;
+constexpr float kInvFact2 = 0.5f;
+constexpr float kInvFact3 = 0.1666666716337204f;
+constexpr float kInvFact4 = 0.0416666679084301f;
+constexpr float kInvFact5 = 0.008333333767950535f;
+constexpr float kInvFact6 = 0.0013888889225199819f;
+constexpr float kInvFact7 = 0.00019841270113829523f;
+constexpr float kInvFact8 = 2.4801587642286904e-05f;
+constexpr float kInvFact9 = 2.7557318844628753e-06f;
+constexpr float kInvFact10 = 2.755731998149713e-07f;
+
+/* e^x: x = k ln2 + r, |r| <= ln2/2, e^r by its degree-7 Taylor polynomial (truncation error
+ * < 6e-9 relative), times 2^k assembled in the exponent field.  Results below 2^-126 are
+ * returned as 0 (no denormals), results above FLT_MAX as +inf.                              */
+VCU_HD float vexp(float x) {
+    if (!(x > -87.0f)) return (x != x) ? x : 0.0f;
+    if (x > 88.5f) return bits_to_float(0x7f800000u);
+    const float k = vrint(vmul(x, kLog2e));
+    float r = vfma(-k, kLn2Hi, x);
+    r = vfma(-k, kLn2Mi, r);
+    r = vfma(-k, kLn2Lo, r);
+    float p = kInvFact7;
+    p = vfma(p, r, kInvFact6);
+    p = vfma(p, r, kInvFact5);
+    p = vfma(p, r, kInvFact4);
+    p = vfma(p, r, kInvFact3);
+    p = vfma(p, r, kInvFact2);
+    p = vfma(p, r, 1.0f);
+    p = vfma(p, r, 1.0f);
+    /* k in [-126, 128): split 2^k in two factors so k = 128 never appears as an exponent */
+    const int ki = (int)k;
+    const int k1 = ki / 2, k2 = ki - k1;
+    const float s1 = bits_to_float((uint32_t)(k1 + 127) << 23);
+    const float s2 = bits_to_float((uint32_t)(k2 + 127) << 23);
+    return vmul(vmul(p, s1), s2);
+}
+
+/* sin and cos of the reduced argument |r| <= pi/4 (Taylor to degree 9 and 10). */
+VCU_HD float sin_kernel(float r) {
+    const float r2 = vmul(r, r);
+    float p = kInvFact9;
+    p = vfma(p, r2, -kInvFact7);
+    p = vfma(p, r2, kInvFact5);
+    p = vfma(p, r2, -kInvFact3);
+    p = vmul(p, r2);
+    return vfma(p, r, r);
+}
+VCU_HD float cos_kernel(float r) {
+    const float r2 = vmul(r, r);
+    float p = -kInvFact10;
+    p = vfma(p, r2, kInvFact8);
+    p = vfma(p, r2, -kInvFact6);
+    p = vfma(p, r2, kInvFact4);
+    p = vfma(p, r2, -kInvFact2);
+    return vfma(p, r2, 1.0f);
+}
+/* Quadrant reduction x = k pi/2 + r; accurate for |x| < 4000 (k*hi exact).                 */
+VCU_HD float vsincos_q(float x, int add_quadrant) {
+    const float k = vrint(vmul(x, kTwoOverPi));
+    float r = vfma(-k, kPio2Hi, x);
+    r = vfma(-k, kPio2Mi, r);
+    r = vfma(-k, kPio2Lo, r);
+    const int q = ((int)k + add_quadrant) & 3;
+    const float s = (q & 1) ? cos_kernel(r) : sin_kernel(r);
+    return (q & 2) ? -s : s;
+}
+VCU_HD float vsin(float x) { return vsincos_q(x, 0); }
+VCU_HD float vcos(float x) { return vsincos_q(x, 1); }
+
+/* ---------------------------------------------------------------- integrand tags */
+enum IntegrandKind : int32_t {
+    VCU_F_POLY2 = 1,          /* x^2 + y^2 on 2-D (main/doc/integrators.cc:6-11)                */
+    VCU_F_SIN1 = 2,           /* sin(x) on 1-D (main/doc/montecarlo-1d.cc:6-12)                 */
+    VCU_F_SPHERE3 = 3,        /* indicator x^2+y^2+z^2 <= 1 on 3-D (main/doc/integrands.cc:3-5)  */
+    VCU_F_WAVE2 = 4,          /* sin(8x) e^-y + x^2 + y^2 on 2-D (per-bin Monte Carlo workload)   */
+    VCU_F_SCENE2 = 5,         /* Gaussian bumps + hard-edged disks on 2-D                          */
+    VCU_F_MOVING_SCENE3 = 6,  /* bumps + disks moving over t, RGB, on 3-D (x, y, t)                */
+    VCU_F_HALFSPACE = 7,      /* prod_d e^{-a_d x_d} cos(b_d x_d) [n.x < c], 2..6-D                */
+    VCU_F_OCCLUDED_SCENE5 = 8 /* SCENE2(x,y) times box visibility of a segment, 5-D                */
+};
+
+constexpr int kMaxGauss = 64;
+constexpr int kMaxDisk = 32;
+constexpr int kMaxBox = 128;
+constexpr int kMaxHalfspaceDim = 6;
+
+/* ---------------------------------------------------------------- functors
+ * Each functor: static DIM (compile-time arity) and CH (value channels), a host-side
+ * build(params, n) returning 0 on success, and operator()(const float* x, float* out).      */
+
+struct Poly2 {
+    static constexpr int DIM = 2, CH = 1;
+    int32_t dummy;
+    VCU_HD void operator()(const float* x, float* out) const {
+        out[0] = vadd(vmul(x[0], x[0]), vmul(x[1], x[1]));
+    }
+};
+
+struct Sin1 {
+    static constexpr int DIM = 1, CH = 1;
+    int32_t dummy;
+    VCU_HD void operator()(const float* x, float* out) const { out[0] = vsin(x[0]); }
+};
+
+struct Sphere3 {
+    static constexpr int DIM = 3, CH = 1;
+    int32_t dummy;
+    VCU_HD void operator()(const float* x, float* out) const {
+        const float r2 = vadd(vadd(vmul(x[0], x[0]), vmul(x[1], x[1])), vmul(x[2], x[2]));
+        out[0] = (r2 <= 1.0f) ? 1.0f : 0.0f;
+    }
+};
+
+struct Wave2 {
+    static constexpr int DIM = 2, CH = 1;
+    int32_t dummy;
+    VCU_HD void operator()(const float* x, float* out) const {
+        float t = vmul(vsin(vmul(8.0f, x[0])), vexp(-x[1]));
+        t = vadd(t, vmul(x[0], x[0]));
+        out[0] = vadd(t, vmul(x[1], x[1]));
+    }
+};
+
+/* Scene parameters (flat float array, as produced by viltrum_gb300.scenes):
+ *   [0] n_gauss, [1] n_disk,
+ *   n_gauss x (cx, cy, sigma, amplitude), n_disk x (cx, cy, radius, value)
+ * The functor stores the exponent factor -1/(2 sigma^2) and the squared radius, computed once
+ * here with explicit float rounding.                                                          */
+struct Scene2 {
+    static constexpr int DIM = 2, CH = 1;
+    int32_t ng, nd;
+    float g[kMaxGauss][4]; /* cx, cy, -1/(2 s^2), amplitude */
+    float d[kMaxDisk][4];  /* cx, cy, r^2, value           */
+
+    int build(const float* p, int n) {
+        if (n < 2) return 1;
+        ng = (int32_t)p[0];
+        nd = (int32_t)p[1];
+        if (ng < 0 || nd < 0 || ng > kMaxGauss || nd > kMaxDisk) return 1;
+        if (n < 2 + 4 * ng + 4 * nd) return 1;
+        const float* q = p + 2;
+        for (int i = 0; i < ng; ++i, q += 4) {
+            g[i][0] = q[0];
+            g[i][1] = q[1];
+            g[i][2] = vdiv(-0.5f, vmul(q[2], q[2]));
+            g[i][3] = q[3];
+        }
+        for (int i = 0; i < nd; ++i, q += 4) {
+            d[i][0] = q[0];
+            d[i][1] = q[1];
+            d[i][2] = vmul(q[2], q[2]);
+            d[i][3] = q[3];
+        }
+        return 0;
+    }
+    VCU_HD float eval(float x, float y) const {
+        float acc = 0.0f;
+        for (int i = 0; i < ng; ++i) {
+            const float dx = vsub(x, g[i][0]);
+            const float dy = vsub(y, g[i][1]);
+            const float r2 = vfma(dx, dx, vmul(dy, dy));
+            acc = vfma(g[i][3], vexp(vmul(r2, g[i][2])), acc);
+        }
+        for (int i = 0; i < nd; ++i) {
+            const float dx = vsub(x, d[i][0]);
+            const float dy = vsub(y, d[i][1]);
+            const float r2 = vfma(dx, dx, vmul(dy, dy));
+            if (r2 <= d[i][2]) acc = vadd(acc, d[i][3]);
+        }
+        return acc;
+    }
+    VCU_HD void operator()(const float* x, float* out) const { out[0] = eval(x[0], x[1]); }
+};
+
+/* Moving scene, 3 channels, on (x, y, t):
+ *   [0] n_gauss, [1] n_disk,
+ *   n_gauss x (cx, cy, sigma, amplitude)                   -- static, grey
+ *   n_disk  x (cx, cy, vx, vy, radius, r, g, b)            -- centre (cx + t vx, cy + t vy)
+ */
+struct MovingScene3 {
+    static constexpr int DIM = 3, CH = 3;
+    int32_t ng, nd;
+    float g[kMaxGauss][4];
+    float d[kMaxDisk][8]; /* cx, cy, vx, vy, r^2, r, g, b */
+
+    int build(const float* p, int n) {
+        if (n < 2) return 1;
+        ng = (int32_t)p[0];
+        nd = (int32_t)p[1];
+        if (ng < 0 || nd < 0 || ng > kMaxGauss || nd > kMaxDisk) return 1;
+        if (n < 2 + 4 * ng + 8 * nd) return 1;
+        const float* q = p + 2;
+        for (int i = 0; i < ng; ++i, q += 4) {
+            g[i][0] = q[0];
+            g[i][1] = q[1];
+            g[i][2] = vdiv(-0.5f, vmul(q[2], q[2]));
+            g[i][3] = q[3];
+        }
+        for (int i = 0; i < nd; ++i, q += 8) {
+            d[i][0] = q[0];
+            d[i][1] = q[1];
+            d[i][2] = q[2];
+            d[i][3] = q[3];
+            d[i][4] = vmul(q[4], q[4]);
+            d[i][5] = q[5];
+            d[i][6] = q[6];
+            d[i][7] = q[7];
+        }
+        return 0;
+    }
+    VCU_HD void operator()(const float* x, float* out) const {
+        float grey = 0.0f;
+        for (int i = 0; i < ng; ++i) {
+            const float dx = vsub(x[0], g[i][0]);
+            const float dy = vsub(x[1], g[i][1]);
+            const float r2 = vfma(dx, dx, vmul(dy, dy));
+            grey = vfma(g[i][3], vexp(vmul(r2, g[i][2])), grey);
+        }
+        float c0 = grey, c1 = grey, c2 = grey;
+        for (int i = 0; i < nd; ++i) {
+            const float cx = vfma(x[2], d[i][2], d[i][0]);
+            const float cy = vfma(x[2], d[i][3], d[i][1]);
+            const float dx = vsub(x[0], cx);
+            const float dy = vsub(x[1], cy);
+            const float r2 = vfma(dx, dx, vmul(dy, dy));
+            if (r2 <= d[i][4]) {
+                c0 = vadd(c0, d[i][5]);
+                c1 = vadd(c1, d[i][6]);
+                c2 = vadd(c2, d[i][7]);
+            }
+        }
+        out[0] = c0;
+        out[1] = c1;
+        out[2] = c2;
+    }
+};
+
+/* Separable smooth product times a half-space indicator, dimension dim (2..6):
+ *   [0] dim, [1..6] a_d, [7..12] b_d, [13..18] n_d, [19] c
+ *   f(x) = prod_d e^{-a_d x_d} cos(b_d x_d)  if  sum_d n_d x_d < c,  else 0
+ * The functor's DIM is the maximum; the kernels use dim() at run time for the arity.        */
+struct Halfspace {
+    static constexpr int DIM = kMaxHalfspaceDim, CH = 1;
+    int32_t dim;
+    float a[kMaxHalfspaceDim], b[kMaxHalfspaceDim], nrm[kMaxHalfspaceDim], c;
+
+    int build(const float* p, int n) {
+        if (n < 20) return 1;
+        dim = (int32_t)p[0];
+        if (dim < 1 || dim > kMaxHalfspaceDim) return 1;
+        for (int i = 0; i < kMaxHalfspaceDim; ++i) {
+            a[i] = p[1 + i];
+            b[i] = p[7 + i];
+            nrm[i] = p[13 + i];
+        }
+        c = p[19];
+        return 0;
+    }
+    VCU_HD void operator()(const float* x, float* out) const {
+        float dot = 0.0f;
+        for (int i = 0; i < dim; ++i) dot = vfma(nrm[i], x[i], dot);
+        if (!(dot < c)) {
+            out[0] = 0.0f;
+            return;
+        }
+        float v = 1.0f;
+        for (int i = 0; i < dim; ++i)
+            v = vmul(v, vmul(vexp(-vmul(a[i], x[i])), vcos(vmul(b[i], x[i]))));
+        out[0] = v;
+    }
+};
+
+/* Scene2 on (x, y) times the visibility of the segment from (x, y, 0) to (u, v, h) with
+ * h = 0.25 + 0.75 w, against axis-aligned boxes (slab test):
+ *   scene parameters as Scene2, then [k] n_box, n_box x (cx, cy, cz, hx, hy, hz)            */
+struct OccludedScene5 {
+    static constexpr int DIM = 5, CH = 1;
+    Scene2 scene;
+    int32_t nb;
+    float lo[kMaxBox][3], hi[kMaxBox][3];
+
+    int build(const float* p, int n) {
+        if (scene.build(p, n)) return 1;
+        const int off = 2 + 4 * scene.ng + 4 * scene.nd;
+        if (n < off + 1) return 1;
+        nb = (int32_t)p[off];
+        if (nb < 0 || nb > kMaxBox || n < off + 1 + 6 * nb) return 1;
+        const float* q = p + off + 1;
+        for (int i = 0; i < nb; ++i, q += 6)
+            for (int k = 0; k < 3; ++k) {
+                lo[i][k] = vsub(q[k], q[3 + k]);
+                hi[i][k] = vadd(q[k], q[3 + k]);
+            }
+        return 0;
+    }
+    VCU_HD float visibility(const float* x) const {
+        const float o[3] = {x[0], x[1], 0.0f};
+        const float e[3] = {x[2], x[3], vfma(0.75f, x[4], 0.25f)};
+        float dir[3], inv[3];
+        for (int k = 0; k < 3; ++k) {
+            dir[k] = vsub(e[k], o[k]);
+            inv[k] = vdiv(1.0f, dir[k]);
+        }
+        for (int i = 0; i < nb; ++i) {
+            float t0 = 0.0f, t1 = 1.0f;
+            for (int k = 0; k < 3; ++k) {
+                float ta = vmul(vsub(lo[i][k], o[k]), inv[k]);
+                float tb = vmul(vsub(hi[i][k], o[k]), inv[k]);
+                if (ta > tb) { const float s = ta; ta = tb; tb = s; }
+                /* a NaN (0 * inf on a face) leaves the interval unchanged */
+                t0 = (ta > t0) ? ta : t0;
+                t1 = (tb < t1) ? tb : t1;
+            }
+            if (t0 <= t1) return 0.0f;
+        }
+        return 1.0f;
+    }
+    VCU_HD void operator()(const float* x, float* out) const {
+        const float s = scene.eval(x[0], x[1]);
+        out[0] = (s == 0.0f) ? 0.0f : vmul(s, visibility(x));
+    }
+};
+
+}  // namespace vcu

@@ -1,0 +1,91 @@
+/*
+ * oracle.h -- C interface of the CPU oracle (test infrastructure, NOT the product).
+ *
+ * liboracle.so is a plain-C++ restatement of viltrum's per-bin integration path, written to
+ * reproduce the reference's results bit for bit (same float/double promotions, same libstdc++
+ * std::mt19937 / uniform distributions / push_heap / pop_heap).  Only tests/, bench.py's
+ * cpu_baseline leg and __graft_entry__.smoke() use it, and only as the checker.
+ *
+ * The same symbols with an "ref_" prefix instead of "orc_" are exported by oracle/_ref/
+ * libvref.so, built (where the reference sources are available) from ref_driver.cc, which
+ * calls the unmodified reference headers; the goldens under tests/golden/ come from it.
+ *
+ * Conventions shared by every entry point:
+ *   kind, params, n_params   integrand (vcu_integrands.h VCU_F_* tag + flat parameters)
+ *   dim, rmin[dim], rmax[dim] integration range (viltrum::Range<float,dim>)
+ *   dimbins, res[dimbins]    bin resolution; bins are written dim-0-fastest, channels
+ *                            interleaved (out[bin*channels + c])
+ *   return 0 on success, non-zero on a bad argument.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* rule ids (Nested<H,L> pairs of src/nested/nested.h:7-34) */
+enum { ORC_RULE_TRAPEZOIDAL = 2, ORC_RULE_SIMPSON = 3, ORC_RULE_BOOLE = 5 };
+/* error heuristics (src/nested/error-heuristic.h) and metrics (src/nested/error-metric.h) */
+enum { ORC_HEUR_DEFAULT = 0, ORC_HEUR_SIZE = 1 };
+enum { ORC_METRIC_ABSOLUTE = 0, ORC_METRIC_RELATIVE = 1 };
+/* control-variate weight strategies (src/control-variates/weight-strategy.h) */
+enum { ORC_CV_OPTIMIZE = 0, ORC_CV_FIXED = 1 };
+/* Monte Carlo flavours */
+enum {
+    ORC_MC_PER_BIN_PARALLEL = 0, /* integrator_per_bin_parallel(monte_carlo(spp, seed))    */
+    ORC_MC_PER_BIN_PARALLEL_SINGLE = 1 /* monte_carlo_per_bin_parallel(spp, seed), += into bins */
+};
+
+typedef struct orc_nested {
+    int32_t rule_hi, rule_lo;
+    int32_t heuristic, metric;
+    double size_weight; /* error_heuristic_size: 1e-5 by default   */
+    double min_size;    /* error_heuristic_size: 1e-37 by default  */
+    double min_val;     /* error_metric_relative: 1e-37 by default */
+} orc_nested;
+
+int orc_channels(int32_t kind);
+/* f at npts points (row-major npts x dim) -> out[npts*channels] */
+int orc_eval(int32_t kind, const float* params, int32_t n_params, int32_t dim, const float* x,
+             int64_t npts, float* out);
+
+/* Per-bin Monte Carlo.  points_out (nullable) receives every sample point in the order the
+ * reference draws them: bin-major (dim-0-fastest bins), then sample, then coordinate.      */
+int orc_per_bin_monte_carlo(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                            const float* rmin, const float* rmax, int32_t dimbins,
+                            const uint64_t* res, uint64_t spp, uint64_t seed, int32_t flavour,
+                            float* out, float* points_out);
+
+/* integrator_per_bin_parallel(integrator_adaptive_iterations(nested(H,L), heuristic, iters)).
+ * trace (nullable) receives, per bin, iterations x (split dimension, popped error bits).   */
+int orc_per_bin_adaptive_nested(int32_t kind, const float* params, int32_t n_params,
+                                int32_t dim, const float* rmin, const float* rmax,
+                                int32_t dimbins, const uint64_t* res, const orc_nested* nested,
+                                uint64_t iterations, float* out, int32_t* trace);
+
+/* integrator_region_based(regions_generator_adaptive_heap(nested, heuristic, iters),
+ *   regions_integrator_parallel_variance_reduction(rr_uniform_region(), cv, region_sampling_uniform(),
+ *   std::mt19937(seed), spp))  -- crespo2021 when nested = (simpson, trapezoidal, size, relative).
+ * approx_out (nullable): per-bin control-variate integral (the "approximation").
+ * regions_out (nullable): (iters+1) x (2*dim) float ranges in heap order.
+ * replay_out (nullable): per bin, spp x (chosen list index, dim coordinates) as floats.      */
+int orc_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                         const float* rmin, const float* rmax, int32_t dimbins,
+                         const uint64_t* res, const orc_nested* nested, uint64_t iterations,
+                         uint64_t spp, uint64_t seed, int32_t weight, double alpha, float* out,
+                         float* approx_out, float* regions_out, float* replay_out);
+
+/* Same per-bin Monte Carlo arithmetic over a contiguous slice of bins [bin_begin, bin_end),
+ * on nthreads host threads (bins are independent once their seeds are drawn in bin order, as
+ * integrator-per-bin-parallel.h:24 draws them).  Used to time the CPU path on all host cores. */
+int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* params, int32_t n_params,
+                                        int32_t dim, const float* rmin, const float* rmax,
+                                        int32_t dimbins, const uint64_t* res,
+                                        const orc_nested* nested, uint64_t iterations,
+                                        uint64_t bin_begin, uint64_t bin_end, int32_t nthreads,
+                                        float* out);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,199 @@
+"""ctypes access to the CPU oracle -- TEST INFRASTRUCTURE, not the product.
+
+`port()` loads oracle/liboracle.so, the C++ restatement of viltrum's per-bin integration path
+(oracle.cc); `reference()` loads oracle/_ref/libvref.so, the driver over the unmodified reference
+headers, which exists only where the reference sources were available to build it.
+
+Only tests/, bench.py's cpu_baseline leg and __graft_entry__.smoke() use this module, and only as
+the checker the CUDA library is compared against.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libvref.so")
+
+RULE = {"trapezoidal": 2, "simpson": 3, "boole": 5}
+HEUR = {"default": 0, "size": 1}
+METRIC = {"absolute": 0, "relative": 1}
+CV_OPTIMIZE, CV_FIXED = 0, 1
+MC_PER_BIN_PARALLEL, MC_PER_BIN_PARALLEL_SINGLE = 0, 1
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+class Nested(ctypes.Structure):
+    """orc_nested: a Nested<H,L> rule with its error heuristic and metric."""
+
+    _fields_ = [
+        ("rule_hi", ctypes.c_int32),
+        ("rule_lo", ctypes.c_int32),
+        ("heuristic", ctypes.c_int32),
+        ("metric", ctypes.c_int32),
+        ("size_weight", ctypes.c_double),
+        ("min_size", ctypes.c_double),
+        ("min_val", ctypes.c_double),
+    ]
+
+    @classmethod
+    def make(cls, hi="boole", lo="simpson", heuristic="default", metric="absolute", size_weight=1e-5,
+             min_size=1e-37, min_val=1e-37):
+        return cls(RULE[hi], RULE[lo], HEUR[heuristic], METRIC[metric], size_weight, min_size, min_val)
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so from oracle.cc with the flags of oracle/Makefile."""
+    src = os.path.join(HERE, "oracle.cc")
+    if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(
+            os.path.getmtime(os.path.join(HERE, f)) for f in ("oracle.cc", "oracle.h", "vrgb.h")):
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+               "-o", PORT_SO, src, "-lpthread"]
+        subprocess.check_call(cmd)
+    return PORT_SO
+
+
+def _ptr(a, t=_f32p):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class Oracle:
+    def __init__(self, path: str, prefix: str):
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        self.kind = "reference" if prefix == "ref_" else "port"
+        L = self.lib
+        if prefix == "orc_":
+            L.orc_channels.restype = ctypes.c_int
+            L.orc_channels.argtypes = [ctypes.c_int32]
+            L.orc_eval.restype = ctypes.c_int
+            L.orc_eval.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, ctypes.c_int64,
+                                   _f32p]
+            L.orc_per_bin_adaptive_nested_threads.restype = ctypes.c_int
+            L.orc_per_bin_adaptive_nested_threads.argtypes = [
+                ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, _f32p]
+        f = getattr(L, prefix + "per_bin_monte_carlo")
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                      ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, _f32p, _f32p]
+        f = getattr(L, prefix + "per_bin_adaptive_nested")
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                      ctypes.POINTER(Nested), ctypes.c_uint64, _f32p, _i32p]
+        f = getattr(L, prefix + "control_variates")
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                      ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32,
+                      ctypes.c_double, _f32p, _f32p, _f32p, _f32p]
+
+    # ------------------------------------------------------------------ helpers
+    @staticmethod
+    def _problem(params, rmin, rmax, res):
+        params = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float32)
+        rmin = np.ascontiguousarray(rmin, dtype=np.float32)
+        rmax = np.ascontiguousarray(rmax, dtype=np.float32)
+        res = np.ascontiguousarray(res, dtype=np.uint64)
+        return params, rmin, rmax, res
+
+    @staticmethod
+    def channels(kind: int) -> int:
+        return 3 if kind == 6 else 1
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}{what} failed with status {rc}")
+
+    # ------------------------------------------------------------------ API
+    def eval(self, kind, params, x):
+        params = np.ascontiguousarray(params if params is not None else np.zeros(1), dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n, dim = x.shape
+        out = np.zeros((n, self.channels(kind)), dtype=np.float32)
+        self._check(self.lib.orc_eval(kind, _ptr(params), params.size, dim, _ptr(x), n, _ptr(out)), "eval")
+        return out
+
+    def per_bin_monte_carlo(self, kind, params, rmin, rmax, res, spp, seed, flavour=MC_PER_BIN_PARALLEL,
+                            record=False, initial=None):
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        out = np.zeros(nb * ch, dtype=np.float32) if initial is None else np.array(initial, dtype=np.float32).ravel()
+        pts = np.zeros(nb * spp * rmin.size, dtype=np.float32) if record else None
+        rc = getattr(self.lib, self.prefix + "per_bin_monte_carlo")(
+            kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p), spp,
+            seed, flavour, _ptr(out), _ptr(pts))
+        self._check(rc, "per_bin_monte_carlo")
+        return out.reshape(nb, ch), (pts.reshape(nb, spp, rmin.size) if record else None)
+
+    def per_bin_adaptive_nested(self, kind, params, rmin, rmax, res, nested: Nested, iterations, trace=False):
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        out = np.zeros(nb * ch, dtype=np.float32)
+        tr = np.zeros(nb * iterations * 2, dtype=np.int32) if trace else None
+        rc = getattr(self.lib, self.prefix + "per_bin_adaptive_nested")(
+            kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
+            ctypes.byref(nested), iterations, _ptr(out), _ptr(tr, _i32p))
+        self._check(rc, "per_bin_adaptive_nested")
+        return out.reshape(nb, ch), (tr.reshape(nb, iterations, 2) if trace else None)
+
+    def per_bin_adaptive_nested_threads(self, kind, params, rmin, rmax, res, nested, iterations, bin_begin,
+                                        bin_end, nthreads):
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        out = np.zeros(nb * ch, dtype=np.float32)
+        rc = self.lib.orc_per_bin_adaptive_nested_threads(
+            kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
+            ctypes.byref(nested), iterations, bin_begin, bin_end, nthreads, _ptr(out))
+        self._check(rc, "per_bin_adaptive_nested_threads")
+        return out.reshape(nb, ch)[bin_begin:bin_end]
+
+    def control_variates(self, kind, params, rmin, rmax, res, nested: Nested, iterations, spp, seed,
+                         weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False):
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        dim = rmin.size
+        out = np.zeros(nb * ch, dtype=np.float32)
+        ap = np.zeros(nb * ch, dtype=np.float32) if approx else None
+        rg = np.zeros((iterations + 1) * 2 * dim, dtype=np.float32) if regions else None
+        width = (1 + dim) if self.prefix == "orc_" else dim
+        rp = np.zeros(nb * spp * width, dtype=np.float32) if replay else None
+        rc = getattr(self.lib, self.prefix + "control_variates")(
+            kind, _ptr(params), params.size, dim, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
+            ctypes.byref(nested), iterations, spp, seed, weight, alpha, _ptr(out), _ptr(ap), _ptr(rg), _ptr(rp))
+        self._check(rc, "control_variates")
+        return {
+            "bins": out.reshape(nb, ch),
+            "approximation": None if ap is None else ap.reshape(nb, ch),
+            "regions": None if rg is None else rg.reshape(iterations + 1, 2, dim),
+            "replay": None if rp is None else rp.reshape(nb, spp, width),
+        }
+
+
+_port = None
+
+
+def port() -> Oracle:
+    """The C++ restatement (built on demand)."""
+    global _port
+    if _port is None:
+        build()
+        _port = Oracle(PORT_SO, "orc_")
+    return _port
+
+
+def reference() -> Oracle | None:
+    """The unmodified reference driver, if it was built here (oracle/Makefile `ref`)."""
+    if not os.path.exists(REF_SO):
+        return None
+    return Oracle(REF_SO, "ref_")

@@ -1,0 +1,303 @@
+/*
+ * ref_driver.cc -- runs the UNMODIFIED viltrum reference headers on the built-in integrands.
+ *
+ * Test infrastructure only.  Compiled by oracle/Makefile (target `ref`) against the reference
+ * sources where they lie (-I <reference root>) into oracle/_ref/libvref.so, which exports the
+ * oracle.h entry points with a "ref_" prefix.  tests/golden/make_golden.py calls it to produce
+ * the golden fixtures that pin the CPU restatement (oracle.cc) to the reference.
+ *
+ * Only the configurations the fixtures use are instantiated (the reference composes integrators
+ * as compile-time types); anything else returns 9.
+ */
+#include "viltrum.h"
+
+#include <array>
+#include <cstring>
+#include <vector>
+
+#include "../include/vcu_integrands.h"
+#include "oracle.h"
+#include "vrgb.h"
+
+namespace {
+
+template <class T> struct VT;
+template <> struct VT<float> {
+    static constexpr int CH = 1;
+    static float from(const float* o) { return o[0]; }
+    static void to(const float& v, float* o) { o[0] = v; }
+};
+template <> struct VT<vrgb> {
+    static constexpr int CH = 3;
+    static vrgb from(const float* o) { return vrgb(o[0], o[1], o[2]); }
+    static void to(const vrgb& v, float* o) { o[0] = v.c[0]; o[1] = v.c[1]; o[2] = v.c[2]; }
+};
+
+/* integrand as viltrum sees it: std::array<float,DIM> -> value; records points if asked */
+struct Recorder {
+    float* next = nullptr;
+};
+template <class Fun, std::size_t DIM, class T> struct RefF {
+    const Fun* f;
+    Recorder* rec;
+    T operator()(const std::array<float, DIM>& x) const {
+        if (rec && rec->next)
+            for (std::size_t i = 0; i < DIM; ++i) *rec->next++ = x[i];
+        float o[3];
+        (*f)(x.data(), o);
+        return VT<T>::from(o);
+    }
+};
+
+template <std::size_t DIM> viltrum::Range<float, DIM> mk_range(const float* a, const float* b) {
+    std::array<float, DIM> x, y;
+    for (std::size_t i = 0; i < DIM; ++i) {
+        x[i] = a[i];
+        y[i] = b[i];
+    }
+    return viltrum::Range<float, DIM>(x, y);
+}
+
+template <std::size_t DB> std::array<std::size_t, DB> mk_res(const uint64_t* r) {
+    std::array<std::size_t, DB> a;
+    for (std::size_t i = 0; i < DB; ++i) a[i] = r[i];
+    return a;
+}
+
+template <std::size_t DB, class T> struct BinStore {
+    std::array<std::size_t, DB> res;
+    std::vector<T> v;
+    std::size_t lin(const std::array<std::size_t, DB>& p) const {
+        std::size_t l = 0, m = 1;
+        for (std::size_t i = 0; i < DB; ++i) {
+            l += p[i] * m;
+            m *= res[i];
+        }
+        return l;
+    }
+};
+
+/* logger that captures the region list handed to Logger::log by IntegratorRegionBased
+ * (src/newton-cotes/integrator-region-based.h:13-22) */
+struct RegionLogger {
+    float* regions_out = nullptr;
+    Recorder* arm = nullptr; /* recording starts once the regions are built */
+    float* arm_at = nullptr;
+    std::string n;
+    RegionLogger() = default;
+    std::string name() const { return n; }
+    void set_name(const std::string& s) { n = s; }
+    template <typename Number> void log_progress(const Number&, const Number& = Number(1)) {}
+    template <typename Data> void log(const Data& data) {
+        if (arm) arm->next = arm_at;
+        if (!regions_out) return;
+        std::size_t k = 0;
+        for (const auto& r : data) {
+            constexpr std::size_t D = std::decay_t<decltype(r.range())>::size;
+            for (std::size_t d = 0; d < D; ++d) {
+                regions_out[k * 2 * D + d] = r.range().min(d);
+                regions_out[k * 2 * D + D + d] = r.range().max(d);
+            }
+            ++k;
+        }
+    }
+};
+
+template <class Fun, std::size_t DIM, std::size_t DB, class T>
+int run_mc(const Fun& fun, const float* rmin, const float* rmax, const uint64_t* res, uint64_t spp, uint64_t seed,
+           int flavour, float* out, float* points) {
+    Recorder rec{points};
+    RefF<Fun, DIM, T> f{&fun, &rec};
+    auto range = mk_range<DIM>(rmin, rmax);
+    BinStore<DB, T> bs{mk_res<DB>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.resize(nb);
+    for (std::size_t i = 0; i < nb; ++i) bs.v[i] = VT<T>::from(out + i * VT<T>::CH);
+    auto bins = [&bs](const std::array<std::size_t, DB>& p) -> T& { return bs.v[bs.lin(p)]; };
+    if (flavour == ORC_MC_PER_BIN_PARALLEL)
+        viltrum::integrate(viltrum::integrator_per_bin_parallel(viltrum::monte_carlo(spp, seed)), bins, bs.res, f, range);
+    else
+        viltrum::integrate(viltrum::monte_carlo_per_bin_parallel(spp, seed), bins, bs.res, f, range);
+    for (std::size_t i = 0; i < nb; ++i) VT<T>::to(bs.v[i], out + i * VT<T>::CH);
+    return 0;
+}
+
+template <class Fun, std::size_t DIM, std::size_t DB, class T, class Rule, class Heur>
+int run_nested(const Fun& fun, const float* rmin, const float* rmax, const uint64_t* res, const Rule& rule,
+               const Heur& heur, uint64_t iters, float* out) {
+    RefF<Fun, DIM, T> f{&fun, nullptr};
+    auto range = mk_range<DIM>(rmin, rmax);
+    BinStore<DB, T> bs{mk_res<DB>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.assign(nb, T(0.0));
+    auto bins = [&bs](const std::array<std::size_t, DB>& p) -> T& { return bs.v[bs.lin(p)]; };
+    viltrum::integrate(viltrum::integrator_per_bin_parallel(viltrum::integrator_adaptive_iterations(rule, heur, iters)),
+                       bins, bs.res, f, range);
+    for (std::size_t i = 0; i < nb; ++i) VT<T>::to(bs.v[i], out + i * VT<T>::CH);
+    return 0;
+}
+
+template <class Fun, std::size_t DIM, std::size_t DB, class T, class Rule, class Heur, class CV>
+int run_cv(const Fun& fun, const float* rmin, const float* rmax, const uint64_t* res, const Rule& rule,
+           const Heur& heur, uint64_t iters, uint64_t spp, uint64_t seed, CV cv, float* out, float* regions_out,
+           float* points) {
+    Recorder rec{nullptr};
+    RefF<Fun, DIM, T> f{&fun, &rec};
+    auto range = mk_range<DIM>(rmin, rmax);
+    BinStore<DB, T> bs{mk_res<DB>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.assign(nb, T(0.0));
+    auto bins = [&bs](const std::array<std::size_t, DB>& p) -> T& { return bs.v[bs.lin(p)]; };
+    auto integrator = viltrum::integrator_region_based(
+        viltrum::regions_generator_adaptive_heap(rule, heur, iters),
+        viltrum::regions_integrator_parallel_variance_reduction(viltrum::rr_uniform_region(), std::move(cv),
+                                                                viltrum::region_sampling_uniform(), std::mt19937(seed),
+                                                                spp));
+    RegionLogger logger;
+    logger.regions_out = regions_out;
+    if (points) {
+        logger.arm = &rec;
+        logger.arm_at = points;
+    }
+    viltrum::integrate(integrator, bins, bs.res, f, range, logger);
+    for (std::size_t i = 0; i < nb; ++i) VT<T>::to(bs.v[i], out + i * VT<T>::CH);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int ref_per_bin_monte_carlo(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                                       const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                                       uint64_t spp, uint64_t seed, int32_t flavour, float* out, float* points_out) {
+    if (kind == vcu::VCU_F_WAVE2 && dim == 2 && dimbins == 1) {
+        vcu::Wave2 f{};
+        return run_mc<vcu::Wave2, 2, 1, float>(f, rmin, rmax, res, spp, seed, flavour, out, points_out);
+    }
+    if (kind == vcu::VCU_F_POLY2 && dim == 2 && dimbins == 2) {
+        vcu::Poly2 f{};
+        return run_mc<vcu::Poly2, 2, 2, float>(f, rmin, rmax, res, spp, seed, flavour, out, points_out);
+    }
+    if (kind == vcu::VCU_F_SIN1 && dim == 1 && dimbins == 1) {
+        vcu::Sin1 f{};
+        return run_mc<vcu::Sin1, 1, 1, float>(f, rmin, rmax, res, spp, seed, flavour, out, points_out);
+    }
+    if (kind == vcu::VCU_F_SPHERE3 && dim == 3 && dimbins == 1) {
+        vcu::Sphere3 f{};
+        return run_mc<vcu::Sphere3, 3, 1, float>(f, rmin, rmax, res, spp, seed, flavour, out, points_out);
+    }
+    if (kind == vcu::VCU_F_MOVING_SCENE3 && dim == 3 && dimbins == 2) {
+        auto* f = new vcu::MovingScene3;
+        int r = f->build(params, n_params) ? 3
+                                           : run_mc<vcu::MovingScene3, 3, 2, vrgb>(*f, rmin, rmax, res, spp, seed,
+                                                                                   flavour, out, points_out);
+        delete f;
+        return r;
+    }
+    return 9;
+}
+
+extern "C" int ref_per_bin_adaptive_nested(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                                           const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                                           const orc_nested* nc, uint64_t iterations, float* out, int32_t* trace) {
+    (void)trace;
+    using namespace viltrum;
+    const bool bs_da = nc->rule_hi == ORC_RULE_BOOLE && nc->rule_lo == ORC_RULE_SIMPSON &&
+                       nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_ABSOLUTE;
+    const bool bs_dr = nc->rule_hi == ORC_RULE_BOOLE && nc->rule_lo == ORC_RULE_SIMPSON &&
+                       nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_RELATIVE;
+    const bool st_sr = nc->rule_hi == ORC_RULE_SIMPSON && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
+                       nc->heuristic == ORC_HEUR_SIZE && nc->metric == ORC_METRIC_RELATIVE;
+    const bool bt_da = nc->rule_hi == ORC_RULE_BOOLE && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
+                       nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_ABSOLUTE;
+    const bool st_da = nc->rule_hi == ORC_RULE_SIMPSON && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
+                       nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_ABSOLUTE;
+    auto hda = error_heuristic_default(error_metric_absolute());
+    auto hdr = error_heuristic_default(error_metric_relative(nc->min_val));
+    auto hsr = error_heuristic_size(error_metric_relative(nc->min_val), nc->size_weight, nc->min_size);
+    if (kind == vcu::VCU_F_SCENE2 && dim == 2 && dimbins == 2) {
+        auto* f = new vcu::Scene2;
+        int r = 9;
+        if (f->build(params, n_params)) r = 3;
+        else if (bs_da) r = run_nested<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(boole, simpson), hda, iterations, out);
+        else if (bs_dr) r = run_nested<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(boole, simpson), hdr, iterations, out);
+        else if (st_sr) r = run_nested<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr, iterations, out);
+        delete f;
+        return r;
+    }
+    if (kind == vcu::VCU_F_POLY2 && dim == 2 && dimbins == 1 && bs_da) {
+        vcu::Poly2 f{};
+        return run_nested<vcu::Poly2, 2, 1, float>(f, rmin, rmax, res, nested(boole, simpson), hda, iterations, out);
+    }
+    if (kind == vcu::VCU_F_WAVE2 && dim == 2 && dimbins == 1 && bs_da) {
+        vcu::Wave2 f{};
+        return run_nested<vcu::Wave2, 2, 1, float>(f, rmin, rmax, res, nested(boole, simpson), hda, iterations, out);
+    }
+    if (kind == vcu::VCU_F_WAVE2 && dim == 2 && dimbins == 2 && bt_da) {
+        vcu::Wave2 f{};
+        return run_nested<vcu::Wave2, 2, 2, float>(f, rmin, rmax, res, nested(boole, trapezoidal), hda, iterations, out);
+    }
+    if (kind == vcu::VCU_F_HALFSPACE && dim == 3 && dimbins == 1 && st_da) {
+        vcu::Halfspace f{};
+        if (f.build(params, n_params) || f.dim != 3) return 3;
+        return run_nested<vcu::Halfspace, 3, 1, float>(f, rmin, rmax, res, nested(simpson, trapezoidal),
+                                                        error_heuristic_default(error_metric_absolute()), iterations, out);
+    }
+    if (kind == vcu::VCU_F_MOVING_SCENE3 && dim == 3 && dimbins == 2 && st_sr) {
+        auto* f = new vcu::MovingScene3;
+        int r = f->build(params, n_params)
+                    ? 3
+                    : run_nested<vcu::MovingScene3, 3, 2, vrgb>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr,
+                                                                 iterations, out);
+        delete f;
+        return r;
+    }
+    return 9;
+}
+
+extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                                    const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                                    const orc_nested* nc, uint64_t iterations, uint64_t spp, uint64_t seed,
+                                    int32_t weight, double alpha, float* out, float* approx_out, float* regions_out,
+                                    float* replay_out) {
+    (void)approx_out;
+    using namespace viltrum;
+    const bool st_sr = nc->rule_hi == ORC_RULE_SIMPSON && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
+                       nc->heuristic == ORC_HEUR_SIZE && nc->metric == ORC_METRIC_RELATIVE;
+    if (!st_sr) return 9;
+    auto hsr = error_heuristic_size(error_metric_relative(nc->min_val), nc->size_weight, nc->min_size);
+    /* replay_out receives the recorded sample points only (spp x dim per bin); the chosen
+     * region indices are internal to the reference */
+    if (kind == vcu::VCU_F_MOVING_SCENE3 && dim == 3 && dimbins == 2 && weight == ORC_CV_OPTIMIZE) {
+        auto* f = new vcu::MovingScene3;
+        int r = f->build(params, n_params)
+                    ? 3
+                    : run_cv<vcu::MovingScene3, 3, 2, vrgb>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr,
+                                                             iterations, spp, seed, cv_optimize_weight(), out,
+                                                             regions_out, replay_out);
+        delete f;
+        return r;
+    }
+    if (kind == vcu::VCU_F_SCENE2 && dim == 2 && dimbins == 2) {
+        auto* f = new vcu::Scene2;
+        int r = 3;
+        if (!f->build(params, n_params)) {
+            if (weight == ORC_CV_OPTIMIZE)
+                r = run_cv<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr, iterations,
+                                                      spp, seed, cv_optimize_weight(), out, regions_out, replay_out);
+            else
+                r = run_cv<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr, iterations,
+                                                      spp, seed, cv_fixed_weight(alpha), out, regions_out, replay_out);
+        }
+        delete f;
+        return r;
+    }
+    if (kind == vcu::VCU_F_POLY2 && dim == 2 && dimbins == 1 && weight == ORC_CV_OPTIMIZE) {
+        vcu::Poly2 f{};
+        return run_cv<vcu::Poly2, 2, 1, float>(f, rmin, rmax, res, nested(simpson, trapezoidal), hsr, iterations, spp,
+                                                seed, cv_optimize_weight(), out, regions_out, replay_out);
+    }
+    return 9;
+}

@@ -1,0 +1,177 @@
+"""Generate the golden fixtures that pin the CPU oracle to the viltrum reference.
+
+Run where the reference sources are available (the fixtures are committed; the GPU machine never
+runs this):
+
+    make -C oracle ref          # builds oracle/_ref/libvref.so from the unmodified headers
+    python tests/golden/make_golden.py
+
+Each case is executed by the reference driver (oracle/_ref) and its outputs are stored in
+tests/golden/<name>.npz.  The script also runs the C++ restatement (oracle/liboracle.so) on the
+same case and refuses to write a fixture the restatement does not reproduce bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as orc  # noqa: E402
+from viltrum_gb300 import scenes  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+SCENE_SMALL = scenes.scene2(seed=7)
+MOVING_SMALL = scenes.moving_scene3(seed=7, n_gauss=8, n_disk=8)
+HALF3 = scenes.halfspace(seed=11, dim=3)
+
+# (name, method, kwargs)
+CASES = [
+    ("mc_wave2_bins16_spp64_seed1", "mc", dict(kind=scenes.WAVE2, params=None, rmin=[0, 0], rmax=[1, 1], res=[16],
+                                             spp=64, seed=1, flavour=0, record=True)),
+    ("mc_wave2_bins1024_spp1024_seed1", "mc", dict(kind=scenes.WAVE2, params=None, rmin=[0, 0], rmax=[1, 1],
+                                                 res=[1024], spp=1024, seed=1, flavour=0, record=False)),
+    ("mc_poly2_bins4x3_spp16_seed2_single", "mc", dict(kind=scenes.POLY2, params=None, rmin=[0, 0], rmax=[1, 1],
+                                                     res=[4, 3], spp=16, seed=2, flavour=1, record=True)),
+    ("mc_sin1_pi_spp64_seed5", "mc", dict(kind=scenes.SIN1, params=None, rmin=[0.0], rmax=[3.14159265], res=[1],
+                                        spp=64, seed=5, flavour=0, record=True)),
+    ("mc_sphere3_spp1024_seed3", "mc", dict(kind=scenes.SPHERE3, params=None, rmin=[-1, -1, -1], rmax=[1, 1, 1],
+                                          res=[1], spp=1024, seed=3, flavour=0, record=False)),
+    ("mc_moving3_rgb_bins4x4_spp8_seed9", "mc", dict(kind=scenes.MOVING_SCENE3, params=MOVING_SMALL, rmin=[0, 0, 0],
+                                                   rmax=[1, 1, 1], res=[4, 4], spp=8, seed=9, flavour=0,
+                                                   record=True)),
+    ("nc_scene2_bins16x16_bs_abs_it15", "nc", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1],
+                                                  res=[16, 16], nested=("boole", "simpson", "default", "absolute"),
+                                                  iterations=15)),
+    ("nc_scene2_bins8x8_bs_rel_it15", "nc", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1],
+                                                res=[8, 8], nested=("boole", "simpson", "default", "relative"),
+                                                iterations=15)),
+    ("nc_scene2_bins8x8_st_size_rel_it7", "nc", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0],
+                                                    rmax=[1, 1], res=[8, 8],
+                                                    nested=("simpson", "trapezoidal", "size", "relative"),
+                                                    iterations=7)),
+    ("nc_poly2_bins5_bs_abs_it4", "nc", dict(kind=scenes.POLY2, params=None, rmin=[0, 0], rmax=[1, 1], res=[5],
+                                            nested=("boole", "simpson", "default", "absolute"), iterations=4)),
+    ("nc_wave2_bins32_bs_abs_it15", "nc", dict(kind=scenes.WAVE2, params=None, rmin=[0, 0], rmax=[1, 1], res=[32],
+                                              nested=("boole", "simpson", "default", "absolute"), iterations=15)),
+    ("nc_wave2_bins4x4_bt_abs_it5", "nc", dict(kind=scenes.WAVE2, params=None, rmin=[0, 0], rmax=[1, 1],
+                                              res=[4, 4], nested=("boole", "trapezoidal", "default", "absolute"),
+                                              iterations=5)),
+    ("nc_halfspace3_bins4_st_abs_it10", "nc", dict(kind=scenes.HALFSPACE, params=HALF3, rmin=[0, 0, 0],
+                                                  rmax=[1, 1, 1], res=[4],
+                                                  nested=("simpson", "trapezoidal", "default", "absolute"),
+                                                  iterations=10)),
+    ("nc_moving3_rgb_bins4x4_st_size_rel_it7", "nc", dict(kind=scenes.MOVING_SCENE3, params=MOVING_SMALL,
+                                                         rmin=[0, 0, 0], rmax=[1, 1, 1], res=[4, 4],
+                                                         nested=("simpson", "trapezoidal", "size", "relative"),
+                                                         iterations=7)),
+    ("cv_moving3_rgb_bins16x16_it255_spp16_seed3", "cv", dict(kind=scenes.MOVING_SCENE3, params=MOVING_SMALL,
+                                                             rmin=[0, 0, 0], rmax=[1, 1, 1], res=[16, 16],
+                                                             iterations=255, spp=16, seed=3, weight=0, alpha=1.0)),
+    ("cv_scene2_bins16x16_it127_spp8_seed4", "cv", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0],
+                                                       rmax=[1, 1], res=[16, 16], iterations=127, spp=8, seed=4,
+                                                       weight=0, alpha=1.0)),
+    ("cv_scene2_fixed_bins8x8_it63_spp4_seed6", "cv", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0],
+                                                          rmax=[1, 1], res=[8, 8], iterations=63, spp=4, seed=6,
+                                                          weight=1, alpha=0.75)),
+    ("cv_poly2_crespo_bins1_it16_spp64_seed0", "cv", dict(kind=scenes.POLY2, params=None, rmin=[0, 0], rmax=[1, 1],
+                                                         res=[1], iterations=16, spp=64, seed=0, weight=0,
+                                                         alpha=1.0)),
+]
+
+CRESPO = ("simpson", "trapezoidal", "size", "relative")
+
+
+def visit_to_linear(res, parallel: bool) -> np.ndarray:
+    """Bin (dim-0-fastest linear index) visited at each step of the reference's bin loop.
+
+    for_each(parallel, ...) walks dim 0 in the outer loop and the remaining dims, dim 1 fastest,
+    inside it (src/foreach.h:98-120); for_each(sequential, ...) walks dim-0 fastest."""
+    res = [int(r) for r in res]
+    nb = int(np.prod(res))
+    lin = np.arange(nb)
+    if not parallel or len(res) == 1:
+        return lin
+    idx = np.array(np.unravel_index(lin, res[::-1]))[::-1]  # idx[d] for linear order
+    # visit key: dims 1..D-1 dim-1 fastest, then dim 0 slowest
+    key = np.zeros(nb, dtype=np.int64)
+    mul = 1
+    for d in list(range(1, len(res))) + [0]:
+        key += idx[d] * mul
+        mul *= res[d]
+    order = np.empty(nb, dtype=np.int64)
+    order[key] = lin
+    return order
+
+
+def run(lib: orc.Oracle, method: str, kw: dict) -> dict:
+    kw = dict(kw)
+    if method == "mc":
+        bins, pts = lib.per_bin_monte_carlo(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"], kw["spp"],
+                                            kw["seed"], kw["flavour"], record=kw["record"])
+        out = {"bins": bins}
+        if pts is not None:
+            if lib.kind == "reference":
+                fixed = np.empty_like(pts)
+                fixed[visit_to_linear(kw["res"], True)] = pts
+                pts = fixed
+            out["points"] = pts
+        return out
+    if method == "nc":
+        hi, lo, heur, met = kw["nested"]
+        nested = orc.Nested.make(hi, lo, heur, met)
+        bins, _ = lib.per_bin_adaptive_nested(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"], nested,
+                                              kw["iterations"])
+        return {"bins": bins}
+    if method == "cv":
+        nested = orc.Nested.make(*CRESPO)
+        r = lib.control_variates(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"], nested,
+                                 kw["iterations"], kw["spp"], kw["seed"], kw["weight"], kw["alpha"], regions=True,
+                                 replay=True)
+        pts = r["replay"]
+        if lib.kind == "port":
+            pts = pts[:, :, 1:]
+        else:
+            fixed = np.empty_like(pts)
+            fixed[visit_to_linear(kw["res"], int(kw["res"][0]) >= 4)] = pts
+            pts = fixed
+        return {"bins": r["bins"], "regions": r["regions"], "points": pts}
+    raise ValueError(method)
+
+
+def main() -> int:
+    ref = orc.reference()
+    if ref is None:
+        print("oracle/_ref/libvref.so is missing: run `make -C oracle ref` where the reference exists")
+        return 1
+    port = orc.port()
+    bad = 0
+    for name, method, kw in CASES:
+        r = run(ref, method, kw)
+        p = run(port, method, kw)
+        same = all(np.array_equal(r[k].view(np.uint32), p[k].view(np.uint32)) for k in r)
+        if not same:
+            bad += 1
+            for k in r:
+                if not np.array_equal(r[k], p[k]):
+                    diff = np.abs(r[k].astype(np.float64) - p[k].astype(np.float64))
+                    print(f"MISMATCH {name}.{k}: max |diff| {diff.max():.3e} at {np.unravel_index(diff.argmax(), diff.shape)}"
+                          f" ({int((diff > 0).sum())} of {diff.size} differ)")
+            continue
+        meta = {k: np.asarray(v) for k, v in kw.items() if v is not None and k not in ("params",)}
+        if kw.get("params") is not None:
+            meta["params"] = np.asarray(kw["params"], dtype=np.float32)
+        if method == "nc":
+            meta["nested"] = np.array(kw["nested"])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), method=method, **meta, **{"out_" + k: v for k, v in r.items()})
+        print(f"ok {name}")
+    print(f"{len(CASES) - bad} of {len(CASES)} cases bit-identical")
+    return 1 if bad else 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
