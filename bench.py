@@ -1,0 +1,344 @@
+"""Benchmark of viltrum's per-bin integration path on GB300.
+
+Workload (one "step"): per-bin adaptive nested Newton-Cotes, nested(boole, simpson) with the default
+absolute-error heuristic and 15 splits per bin (16 regions per bin), over 512x512 bins of the
+synthetic scene "64 Gaussian bumps + 32 hard-edged disks" (SplitMix64 seed 7) on [0,1]^2 --
+integrator_per_bin_parallel(integrator_adaptive_iterations(nested(boole,simpson), 15)).
+
+Metric: integrand evaluations per second (Gsamples/s) of the whole step, kernel-only with the
+scene resident on the device (`value`), and end to end through the public API with host buffers
+(`e2e`: the step's input -- the scene parameters -- copied from pinned host memory, and the 512x512
+bin image read back to pinned host memory, inside the timed region).  The bin RMSE of the result
+against the FP64 closed-form bin integrals is reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU path (the oracle's restatement, which
+reproduces the reference bit for bit; the reference itself cannot be built on the GPU host) on all
+host cores over a bounded sample of bins per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms to bin RMSE 1e-3 vs FP64 oracle (learned-CV vs plain GPU); Gsamples/s"
+RES = [512, 512]
+ITERS = 15
+SEED = 7
+# integrand cost per evaluation of the scene, in FP32 flops (FMA = 2): per Gaussian bump
+# 2 sub + mul + fma + mul + exp(mul + 3 fma + 7 fma + 2 mul) + fma = 31; per disk sub, sub, mul,
+# fma, compare (+ add) = 6
+FLOPS_PER_EVAL = 64 * 31 + 32 * 6
+
+
+def _peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def stripe(rank: int, world: int):
+    """rank r integrates the horizontal stripe y in [r/world, (r+1)/world] with its own RES bins
+    (weak scaling: every rank does one full workload, no data exchange)."""
+    return [0.0, rank / world], [1.0, (rank + 1) / world]
+
+
+def run_ours(args) -> dict | None:
+    import torch
+
+    import viltrum_gb300 as v
+    from viltrum_gb300 import _lib, scenes
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    ctx = v.Context(local, stream=stream.cuda_stream)
+    params = scenes.scene2(SEED)
+    rmin, rmax = stripe(rank, ws)
+    nb = RES[0] * RES[1]
+    nested = _lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37)
+    dev_bins = torch.empty(nb, dtype=torch.float32, device="cuda")
+    p_dev = ctx.problem(scenes.SCENE2, params, rmin, rmax, RES, mem=_lib.MEM_DEVICE)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step():
+        return ctx.per_bin_adaptive_nested(p_dev, nested, ITERS, dev_bins)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    evals = 0
+    launches = 0
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)  # evict the previous step's bins from L2 (outside the timed events)
+            starts[i].record(stream)
+            st = step()
+            stops[i].record(stream)
+            evals += st.evaluations
+            launches += st.kernel_launches
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = evals * ws / (total_ms * 1e-3) / 1e9
+
+    # accuracy of this step's result against the FP64 closed-form bin integrals
+    out = dev_bins.cpu().numpy()
+    exact = scenes.exact_bins(scenes.SCENE2, params, rmin, rmax, RES)
+    rmse = scenes.bin_rmse(out.reshape(-1, 1), exact)
+
+    # end to end through the public API: pinned host input and output buffers
+    params_host = torch.from_numpy(params).pin_memory()
+    bins_host = torch.empty(nb, dtype=torch.float32).pin_memory()
+    bins_np = bins_host.numpy()
+    integrator = v.integrator_per_bin_parallel(v.integrator_adaptive_iterations(
+        v.nested(v.boole, v.simpson), v.error_heuristic_default(v.error_metric_absolute()), ITERS))
+    rng = v.Range(rmin, rmax)
+    e2e_value = None
+    if not args.no_e2e:
+        for _ in range(max(1, args.warmup)):
+            v.integrate_into(integrator, bins_np, RES, v.Integrand.scene2(params_host.numpy()), rng, ctx=ctx,
+                             device_bins=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            v.integrate_into(integrator, bins_np, RES, v.Integrand.scene2(params_host.numpy()), rng, ctx=ctx,
+                             device_bins=False)
+        e2e_s = time.perf_counter() - t0
+        e2e_value = round(evals * ws / e2e_s / 1e9, 4)
+
+    # roofline of the dominant kernel (the nested-quadrature kernel is the only kernel of a step)
+    peaks = _peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s
+    per_launch_ms = total_ms / args.steps
+    achieved = (evals / args.steps) * FLOPS_PER_EVAL / (per_launch_ms * 1e-3) / 1e12
+    traffic = _traffic_from_profile(nb)
+    line = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "Gsamples/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: 64 Gaussian bumps + 32 disks drawn by SplitMix64 (seed 7); FP64 truth from closed forms",
+        "config": {
+            "workload": "per-bin adaptive nested Newton-Cotes: nested(boole,simpson), default absolute heuristic, "
+                        f"15 splits (16 regions) per bin, {RES[0]}x{RES[1]} bins of the 2-D scene",
+            "bins": RES, "regions_per_bin": ITERS + 1, "evaluations_per_step": evals // args.steps,
+            "l2": "flushed between timed steps by a 256 MiB device write outside the timed events",
+            "parallelism": f"replicas: {ws} rank(s), one stripe of the image each",
+        },
+        "rmse_vs_fp64": rmse,
+        "rel_rmse_vs_fp64": rmse / float(np.sqrt(np.mean(exact ** 2))),
+        "roofline": {
+            "bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_peak, 3), "unit": "TFLOP/s",
+            "frac": round(achieved / fp32_peak, 4), "traffic": traffic,
+            "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json "
+                           "(that file holds no FP32 figure; the kernel moves ~1 MB per launch, so HBM is not its bound)",
+            "flops_per_evaluation": FLOPS_PER_EVAL,
+        },
+        "e2e": {"value": e2e_value, "unit": "Gsamples/s", "h2d_bytes_per_step": int(params.nbytes),
+                "d2h_bytes_per_step": int(nb * 4)},
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    ctx.close()
+    if ws > 1:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def _traffic_from_profile(nbins: int):
+    """DRAM bytes per launch of the nested kernel: the per-bin figure of the committed ncu summary
+    (captured on a 128x128 case) times this launch's bins (traffic grows with the bins written)."""
+    path = os.path.join(ROOT, "profiles", "k_per_bin_nested_scene128.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_bin:"):
+                return round(float(ln.split(":")[1].split()[0]) * nbins)
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(args, sample_rows: int | None = None) -> dict:
+    """The reference algorithm on the host cores (oracle restatement, bit-identical to the
+    reference), over a bounded sample: the first `sample_rows` rows of bins."""
+    from oracle import oracle as orc
+    from viltrum_gb300 import scenes
+
+    port = orc.port()
+    params = scenes.scene2(SEED)
+    threads = os.cpu_count() or 1
+    rows = sample_rows or args.cpu_rows
+    nbins = rows * RES[0]
+    t0 = time.perf_counter()
+    port.per_bin_adaptive_nested_threads(scenes.SCENE2, params, [0, 0], [1, 1], RES, orc.Nested.make(), ITERS, 0,
+                                         nbins, threads)
+    dt = time.perf_counter() - t0
+    evals = nbins * (25 + ITERS * 20)
+    return {"value": round(evals / dt / 1e9, 6), "unit": "Gsamples/s", "cores": threads, "kind": "port",
+            "sample": f"first {rows} of {RES[1]} rows of bins ({nbins} bins, {evals} evaluations) in {dt:.2f} s"}
+
+
+def run_reference(args) -> dict | None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    samples = []
+    for _ in range(args.warmup):
+        cpu_baseline(args, sample_rows=max(1, args.cpu_rows // 8))
+    t_total = 0.0
+    evals_total = 0
+    for _ in range(args.steps):
+        b = cpu_baseline(args)
+        samples.append(b)
+        nb = args.cpu_rows * RES[0]
+        evals = nb * (25 + ITERS * 20)
+        evals_total += evals
+        t_total += evals / (b["value"] * 1e9)
+    value = evals_total / t_total / 1e9
+    base = samples[-1]
+    return {
+        "metric": METRIC, "value": round(value, 6), "unit": "Gsamples/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_total / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+        "data": "synthetic: 64 Gaussian bumps + 32 disks drawn by SplitMix64 (seed 7)",
+        "config": {"workload": "per-bin adaptive nested Newton-Cotes: nested(boole,simpson), default absolute "
+                               "heuristic, 15 splits (16 regions) per bin, 512x512 bins of the 2-D scene",
+                   "bins": RES, "regions_per_bin": ITERS + 1,
+                   "sample_per_step": f"first {args.cpu_rows} rows of bins",
+                   "implementation": "the reference algorithm's CPU path restated in C++ (oracle/oracle.cc), "
+                                     "bit-identical to the reference headers on the golden fixtures; "
+                                     "bins split over all host threads"},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gsamples/s", "cores": base["cores"], "kind": "port",
+                         "sample": base["sample"]},
+        "e2e": {"value": round(value, 6), "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-rows", type=int, default=64, help="rows of bins in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--res", type=int, default=512, help="bins per side (512 is the benchmark workload)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    args = ap.parse_args(argv)
+    global RES
+    RES = [args.res, args.res]
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        line = run_reference(args)
+    else:
+        from viltrum_gb300 import build
+        build.build()
+        line = run_ours(args)
+    if line is not None:
+        print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

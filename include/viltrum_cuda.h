@@ -1,0 +1,147 @@
+/*
+ * viltrum_cuda.h -- C ABI of libviltrum_cuda.so, the GB300 (sm_103a) per-bin integration path of
+ * viltrum.
+ *
+ * In viltrum every integrator is a value type whose
+ *     template<class Bins, size_t DIMBINS, class F, class Float, size_t DIM, class Logger>
+ *     void integrate(Bins& bins, const std::array<size_t,DIMBINS>& resolution, const F& f,
+ *                    const Range<Float,DIM>& range, Logger& logger) const;
+ * is called by viltrum::integrate (src/integrate.h:72-79).  Each entry point below replaces one
+ * such call for one family of per-bin integrators; the header-side integrator types of
+ * viltrum_cuda.hpp (and the Python package viltrum_gb300) turn the bins/resolution/functor/range
+ * arguments into a vcu_problem, call the entry point, and write the result back through the
+ * caller's bins(pos) accessor with the assign/accumulate semantics of the integrator replaced.
+ *
+ * Conventions
+ *   - Bins are returned as floats, dim-0-fastest (the order of viltrum's
+ *     multidimensional_range, src/multidimensional-range.h:33-40), channels interleaved:
+ *     bins[linear_bin * channels + c].  Bin values use viltrum's normalisation,
+ *     (prod of the resolution) x integral over the bin (src/integrator-per-bin.h:26).
+ *   - Pointers are host pointers when vcu_problem::mem is VCU_MEM_HOST (the library copies
+ *     through its own device buffers) and device pointers when it is VCU_MEM_DEVICE.
+ *   - Every call returns a vcu_status; no exception crosses the ABI.  vcu_last_error() gives the
+ *     message of the last failure on a context.
+ *   - A context owns one CUDA stream and its device buffers; calls on one context must not
+ *     overlap (one context per host thread).  All calls are synchronous with respect to the
+ *     host: they return after the results are written.
+ *   - Integrands are the built-in functors of vcu_integrands.h selected by tag (a functor's
+ *     code cannot cross a C ABI); the parameters are copied into the kernel launch.
+ */
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VCU_ABI_VERSION 1
+#define VCU_MAX_DIM 6     /* viltrum's VILTRUM_MAX_DIMENSIONS_REGION (src/newton-cotes/region.h:16-18) */
+#define VCU_MAX_DIMBINS 4
+
+typedef enum vcu_status {
+    VCU_OK = 0,
+    VCU_INVALID_ARG = 1,
+    VCU_OOM = 2,
+    VCU_QUEUE_OVERFLOW = 3,
+    VCU_DEVICE_TIMEOUT = 4, /* a bounded device-side wait expired                    */
+    VCU_NAN_DETECTED = 5,   /* the integrand produced NaN in at least one bin        */
+    VCU_CUDA_ERROR = 6,
+    VCU_NO_DEVICE = 7,
+    VCU_UNSUPPORTED = 8     /* valid request outside what this build instantiates    */
+} vcu_status;
+
+enum { VCU_MEM_HOST = 0, VCU_MEM_DEVICE = 1 };
+/* Newton-Cotes rules by node count (src/newton-cotes/rules.h): trapezoidal, simpson, boole */
+enum { VCU_RULE_TRAPEZOIDAL = 2, VCU_RULE_SIMPSON = 3, VCU_RULE_BOOLE = 5 };
+/* error heuristics (src/nested/error-heuristic.h) and metrics (src/nested/error-metric.h) */
+enum { VCU_HEUR_DEFAULT = 0, VCU_HEUR_SIZE = 1 };
+enum { VCU_METRIC_ABSOLUTE = 0, VCU_METRIC_RELATIVE = 1 };
+/* control-variate weights (src/control-variates/weight-strategy.h) */
+enum { VCU_CV_OPTIMIZE = 0, VCU_CV_FIXED = 1 };
+
+typedef struct vcu_ctx vcu_ctx;
+
+typedef struct vcu_opts {
+    int32_t device;   /* CUDA device ordinal                                        */
+    int32_t flags;    /* reserved, 0                                               */
+    void* stream;     /* cudaStream_t to run on, or NULL for a stream of the context */
+} vcu_opts;
+
+typedef struct vcu_integrand {
+    int32_t kind;          /* VCU_F_* of vcu_integrands.h          */
+    int32_t n_params;      /* number of floats in params            */
+    const float* params;   /* host pointer, may be NULL if n_params==0 */
+} vcu_integrand;
+
+typedef struct vcu_problem {
+    vcu_integrand f;
+    int32_t dim;                         /* dimension of the integration range      */
+    int32_t dimbins;                     /* leading dimensions that are binned      */
+    float range_min[VCU_MAX_DIM];
+    float range_max[VCU_MAX_DIM];
+    uint64_t resolution[VCU_MAX_DIMBINS];
+    int32_t mem;                         /* VCU_MEM_HOST or VCU_MEM_DEVICE          */
+    int32_t reserved;
+} vcu_problem;
+
+typedef struct vcu_nested {
+    int32_t rule_hi, rule_lo;  /* Nested<H,L> (src/nested/nested.h:7-34)                     */
+    int32_t heuristic, metric; /* VCU_HEUR_*, VCU_METRIC_*                                   */
+    double size_weight;        /* error_heuristic_size weight, 1e-5 (error-heuristic.h:129) */
+    double min_size;           /* error_heuristic_size minimum size, 1e-37                  */
+    double min_val;            /* error_metric_relative minimum value, 1e-37 (error-metric.h:79) */
+} vcu_nested;
+
+typedef struct vcu_stats {
+    double device_ms;          /* device time of the call's kernels (CUDA events)     */
+    uint64_t evaluations;      /* integrand evaluations performed                      */
+    uint64_t regions;          /* regions built (adaptive methods)                     */
+    uint32_t kernel_launches;  /* kernels of this library launched by the call         */
+    uint32_t flags;            /* device status bits (1: NaN seen, 2: timeout, 4: overflow) */
+} vcu_stats;
+
+/* ------------------------------------------------------------------ context */
+int vcu_abi_version(void);
+int vcu_create(vcu_ctx** ctx, const vcu_opts* opts);
+int vcu_destroy(vcu_ctx* ctx);
+int vcu_last_error(const vcu_ctx* ctx, char* buf, size_t len);
+/* value channels of a built-in integrand (1 or 3), or a negative vcu_status */
+int vcu_channels(int32_t kind);
+
+/* Device evaluation of a built-in integrand at npts points (row-major npts x dim); out receives
+ * npts x channels floats.  Pointers follow mem.  No reference counterpart: it exposes the
+ * device functor so callers can check it against a host evaluation of the same functor. */
+int vcu_eval(vcu_ctx* ctx, const vcu_integrand* f, int32_t dim, const float* x, int64_t npts,
+             float* out, int32_t mem);
+
+/* ------------------------------------------------------------------ per-bin Monte Carlo
+ * Replaces integrator_per_bin_parallel(monte_carlo(samples, seed))
+ * (src/integrator-per-bin-parallel.h:17-35 with src/monte-carlo/monte-carlo.h:39-63) and
+ * monte_carlo_per_bin_parallel(samples, seed) (src/monte-carlo/monte-carlo-per-bin-parallel.h:40-71).
+ * Sample j of bin b draws its coordinates from Philox4x32-10 with key = seed and counter
+ * (j, b_lo, b_hi, block), in place of the reference's per-bin std::mt19937 copies.
+ * bins receives the per-bin estimate (prod(res) x volume(bin)/samples x sum f).            */
+int vcu_per_bin_monte_carlo(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
+                            uint64_t seed, float* bins, vcu_stats* stats);
+
+/* Same estimator over caller-supplied sample points (bin-major, then sample, then coordinate:
+ * nbins x samples x dim floats), e.g. the points the reference drew for the same call. */
+int vcu_per_bin_monte_carlo_replay(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
+                                   const float* points, float* bins, vcu_stats* stats);
+
+/* ------------------------------------------------------------------ per-bin adaptive nested NC
+ * Replaces integrator_per_bin_parallel(integrator_adaptive_iterations(nested(H,L), heuristic,
+ * iterations)) (src/nested/integrator-adaptive-iterations.h:12-30,
+ * src/nested/regions-generator-adaptive-heap.h:18-45,
+ * src/newton-cotes/regions-integrator-sequential.h:37-58): per bin, a max-error heap of
+ * regions is split `iterations` times and the iterations+1 regions are integrated into the bin.
+ * trace (nullable, follows mem) receives per bin and iteration (split dimension, float bits of
+ * the popped region's error): nbins x iterations x 2 int32.                                 */
+int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
+                                uint64_t iterations, float* bins, int32_t* trace,
+                                vcu_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,265 @@
+/*
+ * viltrum_cuda.hpp -- drop-in CUDA integrators for viltrum's integrate() (header-only host C++).
+ *
+ * Each type below satisfies viltrum's Integrator concept (src/integrate.h:72-79):
+ *
+ *     template<class Bins, size_t DIMBINS, class F, class R, class Logger>
+ *     void integrate(Bins& bins, const std::array<size_t,DIMBINS>& resolution, const F& f,
+ *                    const R& range, Logger& logger) const;
+ *
+ * so it can be passed wherever a CPU per-bin integrator was:
+ *
+ *     #include "viltrum.h"
+ *     #include "viltrum_cuda.hpp"
+ *     std::vector<std::vector<float>> image(512, std::vector<float>(512));
+ *     auto scene = viltrum::cuda::builtin_integrand::scene2(params);
+ *     viltrum::integrate(viltrum::cuda::per_bin_adaptive_nested(viltrum::cuda::boole_simpson(), 15),
+ *                        image, scene, viltrum::range_primary<2>());
+ *
+ * The integrand must be a viltrum::cuda::builtin_integrand (a built-in functor of the CUDA
+ * library, selected by tag: functor code cannot cross the C ABI).  It is also callable on the host
+ * with std::array<float,DIM> (the same functor, bit-identical to the device), which is what
+ * viltrum's integrate() checks its result type against.
+ *
+ * Results are written back through the caller's bins(pos) accessor in viltrum's
+ * multidimensional_range order (dim 0 fastest) with the semantics of the integrator replaced:
+ * per_bin_monte_carlo and per_bin_adaptive_nested ASSIGN, like integrator_per_bin_parallel
+ * (src/integrator-per-bin-parallel.h:33); per_bin_monte_carlo_accumulate ADDS, like
+ * monte_carlo_per_bin_parallel (src/monte-carlo/monte-carlo-per-bin-parallel.h:70).
+ * Failures throw viltrum::cuda::error with the library's message; there is no CPU fallback.
+ * The context (one CUDA stream and the library's device buffers) is per host thread.
+ */
+#pragma once
+#include <array>
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "vcu_integrands.h"
+#include "viltrum_cuda.h"
+
+namespace viltrum {
+namespace cuda {
+
+class error : public std::runtime_error {
+public:
+    int code;
+    error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+/* RAII owner of a vcu_ctx */
+class context {
+    vcu_ctx* ctx_ = nullptr;
+
+public:
+    explicit context(int device = 0, void* stream = nullptr) {
+        vcu_opts o{device, 0, stream};
+        const int rc = vcu_create(&ctx_, &o);
+        if (rc != VCU_OK) throw error(rc, "vcu_create failed (status " + std::to_string(rc) + ")");
+    }
+    context(const context&) = delete;
+    context& operator=(const context&) = delete;
+    ~context() { vcu_destroy(ctx_); }
+    vcu_ctx* get() const { return ctx_; }
+    void check(int rc) const {
+        if (rc == VCU_OK) return;
+        char buf[512];
+        vcu_last_error(ctx_, buf, sizeof(buf));
+        throw error(rc, buf);
+    }
+};
+
+inline context& thread_context() {
+    thread_local context ctx(0);
+    return ctx;
+}
+
+/* A built-in integrand: tag + flat parameters (include/vcu_integrands.h). */
+class builtin_integrand {
+public:
+    int32_t kind = 0;
+    std::vector<float> params;
+
+    builtin_integrand() = default;
+    builtin_integrand(int32_t k, std::vector<float> p) : kind(k), params(std::move(p)) {}
+    static builtin_integrand poly2() { return {vcu::VCU_F_POLY2, {}}; }
+    static builtin_integrand sin1() { return {vcu::VCU_F_SIN1, {}}; }
+    static builtin_integrand sphere3() { return {vcu::VCU_F_SPHERE3, {}}; }
+    static builtin_integrand wave2() { return {vcu::VCU_F_WAVE2, {}}; }
+    static builtin_integrand scene2(std::vector<float> p) { return {vcu::VCU_F_SCENE2, std::move(p)}; }
+    static builtin_integrand moving_scene3(std::vector<float> p) { return {vcu::VCU_F_MOVING_SCENE3, std::move(p)}; }
+    static builtin_integrand halfspace(std::vector<float> p) { return {vcu::VCU_F_HALFSPACE, std::move(p)}; }
+    static builtin_integrand occluded_scene5(std::vector<float> p) {
+        return {vcu::VCU_F_OCCLUDED_SCENE5, std::move(p)};
+    }
+    int channels() const { return vcu_channels(kind); }
+
+    /* host evaluation of the same functor (first channel); only std::array arguments, so
+     * viltrum's detail::adapt passes this object through unchanged (src/integrate.h:11-16) */
+    template <std::size_t DIM> float operator()(const std::array<float, DIM>& x) const {
+        float out[3] = {0, 0, 0};
+        float xx[vcu::kMaxHalfspaceDim > 5 ? 6 : 6] = {0, 0, 0, 0, 0, 0};
+        for (std::size_t i = 0; i < DIM && i < 6; ++i) xx[i] = x[i];
+        eval(xx, out);
+        return out[0];
+    }
+    void eval(const float* x, float* out) const {
+        switch (kind) {
+        case vcu::VCU_F_POLY2: vcu::Poly2{}(x, out); break;
+        case vcu::VCU_F_SIN1: vcu::Sin1{}(x, out); break;
+        case vcu::VCU_F_SPHERE3: vcu::Sphere3{}(x, out); break;
+        case vcu::VCU_F_WAVE2: vcu::Wave2{}(x, out); break;
+        case vcu::VCU_F_SCENE2: { vcu::Scene2 f{}; if (!f.build(params.data(), (int)params.size())) f(x, out); break; }
+        case vcu::VCU_F_MOVING_SCENE3: {
+            vcu::MovingScene3 f{};
+            if (!f.build(params.data(), (int)params.size())) f(x, out);
+            break;
+        }
+        case vcu::VCU_F_HALFSPACE: { vcu::Halfspace f{}; if (!f.build(params.data(), (int)params.size())) f(x, out); break; }
+        default: throw error(VCU_INVALID_ARG, "host evaluation not available for this integrand");
+        }
+    }
+};
+
+namespace detail {
+
+template <class R> constexpr std::size_t range_dim() { return R::size; }
+
+template <std::size_t DIMBINS, class R>
+vcu_problem make_problem(const builtin_integrand& f, const std::array<std::size_t, DIMBINS>& res, const R& range) {
+    static_assert(DIMBINS >= 1 && DIMBINS <= VCU_MAX_DIMBINS, "1..4 binned dimensions");
+    constexpr std::size_t DIM = range_dim<R>();
+    static_assert(DIM >= DIMBINS && DIM <= VCU_MAX_DIM, "range dimension must be DIMBINS..6");
+    vcu_problem p{};
+    p.f.kind = f.kind;
+    p.f.n_params = (int32_t)f.params.size();
+    p.f.params = f.params.empty() ? nullptr : f.params.data();
+    p.dim = (int32_t)DIM;
+    p.dimbins = (int32_t)DIMBINS;
+    for (std::size_t d = 0; d < DIM; ++d) {
+        p.range_min[d] = (float)range.min(d);
+        p.range_max[d] = (float)range.max(d);
+    }
+    for (std::size_t d = 0; d < DIMBINS; ++d) p.resolution[d] = res[d];
+    p.mem = VCU_MEM_HOST;
+    return p;
+}
+
+/* write channel values into whatever bins(pos) returns: a float&/double& or an indexable value */
+template <class T> void store(T& dst, const float* v, int ch, bool accumulate) {
+    if constexpr (std::is_arithmetic_v<T>) {
+        if (accumulate) dst += v[0];
+        else dst = v[0];
+    } else {
+        for (int c = 0; c < ch; ++c) {
+            if (accumulate) dst[c] += v[c];
+            else dst[c] = v[c];
+        }
+    }
+}
+
+template <class Bins, std::size_t DIMBINS>
+void write_back(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const std::vector<float>& out, int ch,
+                bool accumulate) {
+    std::array<std::size_t, DIMBINS> pos{};
+    const std::size_t n = out.size() / ch;
+    for (std::size_t lin = 0; lin < n; ++lin) {
+        store(bins(pos), &out[lin * ch], ch, accumulate);
+        for (std::size_t d = 0; d < DIMBINS; ++d) {
+            if (++pos[d] < res[d]) break;
+            pos[d] = 0;
+        }
+    }
+}
+
+template <class F> const builtin_integrand& as_builtin(const F& f) {
+    static_assert(std::is_same_v<std::decay_t<F>, builtin_integrand>,
+                  "CUDA integrators take a viltrum::cuda::builtin_integrand (integrand code cannot cross the C ABI)");
+    return f;
+}
+
+template <std::size_t DIMBINS> std::size_t bin_count(const std::array<std::size_t, DIMBINS>& res) {
+    std::size_t n = 1;
+    for (auto r : res) n *= r;
+    return n;
+}
+
+}  // namespace detail
+
+/* ---------------------------------------------------------------- per-bin Monte Carlo */
+/* drop-in for integrator_per_bin_parallel(monte_carlo(samples, seed)) (assigns), or with
+ * accumulate=true for monte_carlo_per_bin_parallel(samples, seed) (adds into the bins) */
+class per_bin_monte_carlo {
+    unsigned long samples_;
+    std::uint64_t seed_;
+    bool accumulate_;
+
+public:
+    per_bin_monte_carlo(unsigned long samples, std::uint64_t seed, bool accumulate = false)
+        : samples_(samples), seed_(seed), accumulate_(accumulate) {}
+
+    template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
+    void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
+                   Logger& logger) const {
+        const builtin_integrand& fi = detail::as_builtin(f);
+        context& ctx = thread_context();
+        logger.log_progress(std::size_t(0), std::size_t(1));
+        vcu_problem p = detail::make_problem(fi, res, range);
+        const int ch = fi.channels();
+        std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
+        vcu_stats st{};
+        ctx.check(vcu_per_bin_monte_carlo(ctx.get(), &p, samples_, seed_, out.data(), &st));
+        detail::write_back(bins, res, out, ch, accumulate_);
+        logger.log_progress(std::size_t(1), std::size_t(1));
+    }
+};
+
+inline per_bin_monte_carlo per_bin_monte_carlo_accumulate(unsigned long samples, std::uint64_t seed) {
+    return per_bin_monte_carlo(samples, seed, true);
+}
+
+/* ---------------------------------------------------------------- per-bin adaptive nested */
+struct nested_rule {
+    vcu_nested n;
+};
+inline nested_rule boole_simpson(int heuristic = VCU_HEUR_DEFAULT, int metric = VCU_METRIC_ABSOLUTE) {
+    return {{VCU_RULE_BOOLE, VCU_RULE_SIMPSON, heuristic, metric, 1e-5, 1e-37, 1e-37}};
+}
+inline nested_rule boole_trapezoidal(int heuristic = VCU_HEUR_DEFAULT, int metric = VCU_METRIC_ABSOLUTE) {
+    return {{VCU_RULE_BOOLE, VCU_RULE_TRAPEZOIDAL, heuristic, metric, 1e-5, 1e-37, 1e-37}};
+}
+inline nested_rule simpson_trapezoidal(int heuristic = VCU_HEUR_DEFAULT, int metric = VCU_METRIC_ABSOLUTE) {
+    return {{VCU_RULE_SIMPSON, VCU_RULE_TRAPEZOIDAL, heuristic, metric, 1e-5, 1e-37, 1e-37}};
+}
+
+/* drop-in for integrator_per_bin_parallel(integrator_adaptive_iterations(nested(H,L), heuristic,
+ * iterations)) (assigns) */
+class per_bin_adaptive_nested {
+    nested_rule rule_;
+    unsigned long iterations_;
+
+public:
+    per_bin_adaptive_nested(nested_rule r, unsigned long iterations) : rule_(r), iterations_(iterations) {}
+
+    template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
+    void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
+                   Logger& logger) const {
+        const builtin_integrand& fi = detail::as_builtin(f);
+        context& ctx = thread_context();
+        logger.log_progress(std::size_t(0), std::size_t(1));
+        vcu_problem p = detail::make_problem(fi, res, range);
+        const int ch = fi.channels();
+        std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
+        vcu_stats st{};
+        ctx.check(vcu_per_bin_adaptive_nested(ctx.get(), &p, &rule_.n, iterations_, out.data(), nullptr, &st));
+        detail::write_back(bins, res, out, ch, false);
+        logger.log_progress(std::size_t(1), std::size_t(1));
+    }
+};
+
+}  // namespace cuda
+}  // namespace viltrum

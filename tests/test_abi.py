@@ -1,0 +1,46 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point include/*.h declares.
+No compute call is made here (no GPU is needed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_symbols() -> set[str]:
+    names = set()
+    for h in ("viltrum_cuda.h",):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\bint\s+(vcu_\w+)\s*\(", text))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    from viltrum_gb300 import build
+    return build.build()
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    declared = _declared_symbols()
+    assert {"vcu_create", "vcu_destroy", "vcu_per_bin_monte_carlo", "vcu_per_bin_adaptive_nested"} <= declared
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (vcu_\w+)", out))
+    missing = declared - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    lib = ctypes.CDLL(lib_path)
+    for name in declared:
+        getattr(lib, name)
+
+
+def test_host_logic_without_device(lib_path):
+    """ABI version, channel table, and argument validation that happens before any device use."""
+    lib = ctypes.CDLL(lib_path)
+    assert lib.vcu_abi_version() == 1
+    assert lib.vcu_channels(5) == 1 and lib.vcu_channels(6) == 3 and lib.vcu_channels(99) < 0
+    assert lib.vcu_per_bin_monte_carlo(None, None, 1, 1, None, None) == 1  # null context -> INVALID_ARG
+    assert lib.vcu_destroy(None) == 0

@@ -1,0 +1,55 @@
+"""The CPU oracle reproduces every golden fixture of the reference bit for bit.
+
+The fixtures were produced by the unmodified reference headers (oracle/_ref, see
+tests/golden/make_golden.py); this pins the C++ restatement the GPU is later compared to."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import oracle as orc
+
+
+def _nested(g):
+    hi, lo, heur, met = [str(x) for x in g["nested"]]
+    return orc.Nested.make(hi, lo, heur, met)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_matches_reference_golden(port, name):
+    g = load_golden(name)
+    method = str(g["method"])
+    params = g.get("params")
+    if method == "mc":
+        bins, pts = port.per_bin_monte_carlo(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"], int(g["spp"]),
+                                             int(g["seed"]), int(g["flavour"]), record="out_points" in g)
+        assert np.array_equal(bins.view(np.uint32), g["out_bins"].view(np.uint32))
+        if "out_points" in g:
+            assert np.array_equal(pts.view(np.uint32), g["out_points"].view(np.uint32))
+    elif method == "nc":
+        bins, _ = port.per_bin_adaptive_nested(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"], _nested(g),
+                                               int(g["iterations"]))
+        assert np.array_equal(bins.view(np.uint32), g["out_bins"].view(np.uint32))
+    elif method == "cv":
+        r = port.control_variates(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"],
+                                  orc.Nested.make("simpson", "trapezoidal", "size", "relative"), int(g["iterations"]),
+                                  int(g["spp"]), int(g["seed"]), int(g["weight"]), float(g["alpha"]), regions=True,
+                                  replay=True)
+        assert np.array_equal(r["bins"].view(np.uint32), g["out_bins"].view(np.uint32))
+        assert np.array_equal(r["regions"].view(np.uint32), g["out_regions"].view(np.uint32))
+        assert np.array_equal(r["replay"][:, :, 1:].view(np.uint32), g["out_points"].view(np.uint32))
+    else:
+        pytest.fail(method)
+
+
+def test_known_answers(port):
+    """Known answers printed by the reference's examples (main/doc/*.cc)."""
+    # Boole reproduces x^2+y^2 exactly: 5 bins of 5*int x^2 dx + 1/3 (main/doc/integrators.cc:57-63)
+    bins, _ = port.per_bin_adaptive_nested(1, None, [0, 0], [1, 1], [5], orc.Nested.make(), 0)
+    exact = np.array([5 * ((i + 1) ** 3 - i ** 3) / 375.0 + 1.0 / 3.0 for i in range(5)])
+    assert np.allclose(bins[:, 0], exact, rtol=1e-5)  # float coefficient rounding of the reference
+    # sin over [0, pi] = 2 (main/doc/montecarlo-1d.cc:6-12), 4096 samples
+    b, _ = port.per_bin_monte_carlo(2, None, [0.0], [3.14159265], [1], 4096, 5)
+    assert abs(b[0, 0] - 2.0) < 0.05
+    # sphere volume 4pi/3 (main/doc/integrands.cc:34)
+    b, _ = port.per_bin_monte_carlo(3, None, [-1, -1, -1], [1, 1, 1], [1], 1 << 15, 3)
+    assert abs(b[0, 0] - 4 * np.pi / 3) < 0.05

@@ -1,0 +1,304 @@
+"""viltrum_gb300 -- viltrum's per-bin integration path on GB300 (sm_103a).
+
+The names mirror viltrum's C++ API so a per-bin integration reads the same:
+
+    import viltrum_gb300 as v
+    bins = np.zeros(1024, np.float32)
+    v.integrate(v.integrator_per_bin_parallel(v.monte_carlo(1024, seed=1)), bins,
+                v.Integrand.wave2(), v.range_primary(2))
+
+integrate(integrator, bins, f, range[, logger]) mirrors src/integrate.h:72-79/132-176 (bins is a
+numpy array of shape `resolution` [+ (channels,)], indexed bins[pos0, pos1, ...] like viltrum's
+bins(pos) accessor), and integrate(integrator, f, range) mirrors the single-value form
+(src/integrate.h:105-113).  Each integrator keeps the write semantics of the reference one it
+replaces: per-bin wrappers assign (src/integrator-per-bin-parallel.h:33), monte_carlo_per_bin_parallel
+accumulates (src/monte-carlo/monte-carlo-per-bin-parallel.h:70).
+
+Every integrator runs on the GPU through libviltrum_cuda.so; there is no CPU fallback, and a
+combination the CUDA library does not implement raises NotImplementedError.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import scenes
+from ._lib import MEM_DEVICE, MEM_HOST, Context, Nested, VcuError, default_context, load
+
+__all__ = [
+    "Context", "VcuError", "Integrand", "Range", "integrate", "range_", "range_all", "range_primary",
+    "trapezoidal", "simpson", "boole", "nested", "error_metric_absolute", "error_metric_relative",
+    "error_heuristic_default", "error_heuristic_size", "monte_carlo", "monte_carlo_per_bin_parallel",
+    "integrator_per_bin_parallel", "integrator_adaptive_iterations", "scenes", "load",
+]
+
+
+# ------------------------------------------------------------------------------------ ranges
+@dataclass
+class Range:
+    """viltrum::Range<float,DIM> (src/range.h:17-139)."""
+    min: np.ndarray
+    max: np.ndarray
+
+    def __post_init__(self):
+        self.min = np.asarray(self.min, dtype=np.float32).ravel()
+        self.max = np.asarray(self.max, dtype=np.float32).ravel()
+        if self.min.shape != self.max.shape or not 1 <= self.min.size <= 6:
+            raise ValueError("range bounds must have the same dimension, 1..6")
+
+    @property
+    def dim(self) -> int:
+        return int(self.min.size)
+
+
+def range_(a, b) -> Range:
+    return Range(np.atleast_1d(a), np.atleast_1d(b))
+
+
+def range_all(n: int, a: float, b: float) -> Range:
+    return Range(np.full(n, a), np.full(n, b))
+
+
+def range_primary(n: int) -> Range:
+    """range_primary<N>(): [0,1]^N (src/range.h:196-199)."""
+    return range_all(n, 0.0, 1.0)
+
+
+# ------------------------------------------------------------------------------------ integrands
+@dataclass
+class Integrand:
+    """A built-in integrand of libviltrum_cuda (include/vcu_integrands.h) with its parameters."""
+    kind: int
+    params: np.ndarray | None = None
+    dim: int = 0
+
+    @property
+    def channels(self) -> int:
+        return scenes.CHANNELS.get(self.kind, 1)
+
+    @classmethod
+    def poly2(cls):
+        return cls(scenes.POLY2, None, 2)
+
+    @classmethod
+    def sin1(cls):
+        return cls(scenes.SIN1, None, 1)
+
+    @classmethod
+    def sphere3(cls):
+        return cls(scenes.SPHERE3, None, 3)
+
+    @classmethod
+    def wave2(cls):
+        return cls(scenes.WAVE2, None, 2)
+
+    @classmethod
+    def scene2(cls, params=None, seed: int = 7):
+        return cls(scenes.SCENE2, scenes.scene2(seed) if params is None else np.asarray(params, np.float32), 2)
+
+    @classmethod
+    def moving_scene3(cls, params=None, seed: int = 7):
+        p = scenes.moving_scene3(seed) if params is None else np.asarray(params, np.float32)
+        return cls(scenes.MOVING_SCENE3, p, 3)
+
+    @classmethod
+    def halfspace(cls, params):
+        p = np.asarray(params, np.float32)
+        return cls(scenes.HALFSPACE, p, int(p[0]))
+
+    @classmethod
+    def occluded_scene5(cls, params=None, seed: int = 7):
+        p = scenes.occluded_scene5(seed) if params is None else np.asarray(params, np.float32)
+        return cls(scenes.OCCLUDED_SCENE5, p, 5)
+
+
+# ------------------------------------------------------------------------------------ rules
+@dataclass(frozen=True)
+class Rule:
+    name: str
+    samples: int
+
+
+trapezoidal = Rule("trapezoidal", 2)
+simpson = Rule("simpson", 3)
+boole = Rule("boole", 5)
+
+
+@dataclass(frozen=True)
+class NestedRule:
+    """nested(H, L) (src/nested/nested.h:42-45)."""
+    high: Rule
+    low: Rule
+
+    def __post_init__(self):
+        if (self.high.samples - 1) % (self.low.samples - 1) != 0:
+            raise ValueError("Quadrature rules are not compatible for a nested rule")
+
+
+def nested(high: Rule, low: Rule) -> NestedRule:
+    return NestedRule(high, low)
+
+
+@dataclass(frozen=True)
+class error_metric_absolute:  # noqa: N801  (reference name)
+    relative = False
+    min_val = 1e-37
+
+
+@dataclass(frozen=True)
+class error_metric_relative:  # noqa: N801
+    min_val: float = 1e-37
+    relative = True
+
+
+@dataclass(frozen=True)
+class error_heuristic_default:  # noqa: N801
+    metric: object = field(default_factory=error_metric_absolute)
+    size = False
+    size_weight = 1e-5
+    min_size = 1e-37
+
+
+@dataclass(frozen=True)
+class error_heuristic_size:  # noqa: N801
+    metric: object = field(default_factory=error_metric_absolute)
+    size_weight: float = 1e-5
+    min_size: float = 1e-37
+    size = True
+
+
+def _nested_struct(rule: NestedRule, heur) -> Nested:
+    m = heur.metric
+    return Nested(rule.high.samples, rule.low.samples, 1 if heur.size else 0, 1 if m.relative else 0,
+                  float(heur.size_weight), float(heur.min_size), float(m.min_val))
+
+
+# ------------------------------------------------------------------------------------ integrators
+@dataclass
+class MonteCarlo:
+    """monte_carlo(samples, seed) (src/monte-carlo/monte-carlo.h:88-95)."""
+    samples: int
+    seed: int
+
+
+@dataclass
+class MonteCarloPerBinParallel:
+    """monte_carlo_per_bin_parallel(samples, seed): per-bin samples, accumulated into the bins."""
+    samples: int
+    seed: int
+
+    def integrate(self, bins, res, f, rng, logger=None, ctx=None, device_bins=False):
+        return _run(self, bins, res, f, rng, logger, ctx, device_bins, accumulate=True)
+
+
+@dataclass
+class AdaptiveIterations:
+    """integrator_adaptive_iterations(nested, heuristic, iterations)."""
+    rule: NestedRule
+    heuristic: object
+    iterations: int
+
+
+@dataclass
+class PerBinParallel:
+    """integrator_per_bin_parallel(inner) (src/integrator-per-bin-parallel.h:11-47)."""
+    inner: object
+
+    def integrate(self, bins, res, f, rng, logger=None, ctx=None, device_bins=False):
+        return _run(self, bins, res, f, rng, logger, ctx, device_bins, accumulate=False)
+
+
+def monte_carlo(samples: int, seed: int = 0) -> MonteCarlo:
+    return MonteCarlo(int(samples), int(seed))
+
+
+def monte_carlo_per_bin_parallel(samples: int, seed: int = 0) -> MonteCarloPerBinParallel:
+    return MonteCarloPerBinParallel(int(samples), int(seed))
+
+
+def integrator_adaptive_iterations(rule: NestedRule, heuristic_or_iterations, iterations: int | None = None):
+    if iterations is None:
+        return AdaptiveIterations(rule, error_heuristic_default(error_metric_absolute()), int(heuristic_or_iterations))
+    return AdaptiveIterations(rule, heuristic_or_iterations, int(iterations))
+
+
+def integrator_per_bin_parallel(inner) -> PerBinParallel:
+    return PerBinParallel(inner)
+
+
+# ------------------------------------------------------------------------------------ integrate
+def _as_integrand(f) -> Integrand:
+    if isinstance(f, Integrand):
+        return f
+    raise TypeError("integrands are built-in functors of the CUDA library: pass a viltrum_gb300.Integrand")
+
+
+def _run(integrator, bins, res, f, rng, logger, ctx, device_bins, accumulate):
+    f = _as_integrand(f)
+    ctx = ctx or default_context()
+    res = [int(r) for r in res]
+    if f.dim and f.dim != rng.dim:
+        raise ValueError(f"integrand dimension {f.dim} does not match range dimension {rng.dim}")
+    ch = f.channels
+    nb = int(np.prod(res))
+    if logger is not None:
+        logger.log_progress(0, 1)
+    mem = MEM_DEVICE if device_bins else MEM_HOST
+    p = Context.problem(f.kind, f.params, rng.min, rng.max, res, mem)
+    # a flat float32 buffer in viltrum's linear order is written in place (assign semantics)
+    flat = (not device_bins and not accumulate and isinstance(bins, np.ndarray) and bins.ndim == 1
+            and bins.dtype == np.float32 and bins.size == nb * ch and bins.flags.c_contiguous)
+    out = bins if (device_bins or flat) else np.empty(nb * ch, dtype=np.float32)
+    inner = integrator.inner if isinstance(integrator, PerBinParallel) else integrator
+    if isinstance(inner, (MonteCarlo, MonteCarloPerBinParallel)):
+        stats = ctx.per_bin_monte_carlo(p, inner.samples, inner.seed, out)
+    elif isinstance(inner, AdaptiveIterations):
+        stats = ctx.per_bin_adaptive_nested(p, _nested_struct(inner.rule, inner.heuristic), inner.iterations, out)
+    else:
+        raise NotImplementedError(f"no CUDA implementation of per-bin {type(inner).__name__}")
+    if not device_bins and not flat:
+        vals = out.reshape(tuple(reversed(res)) + (ch,)).transpose(tuple(range(len(res) - 1, -1, -1)) + (len(res),))
+        if ch == 1:
+            vals = vals[..., 0]
+        target = bins
+        if accumulate:
+            target += vals.astype(target.dtype).reshape(target.shape)
+        else:
+            target[...] = vals.reshape(target.shape)
+    if logger is not None:
+        logger.log_progress(1, 1)
+    return stats
+
+
+def integrate(integrator, *args, logger=None, ctx=None, device_bins=False):
+    """integrate(integrator, bins, f, range) or integrate(integrator, f, range) (single value).
+
+    bins: numpy array of shape `resolution` (+ (channels,) for multi-channel integrands), or,
+    with device_bins=True, a CUDA buffer (torch tensor or pointer) of prod(resolution)*channels
+    floats in viltrum's linear order (dim 0 fastest, channels interleaved).
+    Returns the call's vcu_stats as a dict (single-value form: the value)."""
+    if len(args) == 2:
+        f, rng = args
+        f = _as_integrand(f)
+        sol = np.zeros((1, f.channels) if f.channels > 1 else (1,), dtype=np.float32)
+        integrator.integrate(sol, [1], f, rng, logger, ctx, False) if hasattr(integrator, "integrate") \
+            else _run(integrator, sol, [1], f, rng, logger, ctx, False, False)
+        return sol[0]
+    bins, f, rng = args
+    f = _as_integrand(f)
+    if device_bins:
+        raise ValueError("device bins need an explicit resolution: use integrate_into(...)")
+    res = list(bins.shape[:-1] if f.channels > 1 else bins.shape)
+    if hasattr(integrator, "integrate"):
+        st = integrator.integrate(bins, res, f, rng, logger, ctx, False)
+    else:
+        raise NotImplementedError(f"{type(integrator).__name__} is not a per-bin integrator")
+    return st.as_dict()
+
+
+def integrate_into(integrator, bins, resolution, f, rng, logger=None, ctx=None, device_bins=True):
+    """integrate with an explicit resolution (viltrum's integrate(I, bins, res, f, range) form,
+    src/integrate.h:72-79); with device_bins=True `bins` is a device buffer."""
+    st = integrator.integrate(bins, list(resolution), _as_integrand(f), rng, logger, ctx, device_bins)
+    return st.as_dict()

@@ -1,0 +1,206 @@
+"""ctypes binding of libviltrum_cuda.so (include/viltrum_cuda.h).
+
+The library is built in-tree (viltrum_gb300/build.py).  There is no CPU fallback: if the library
+is missing or no CUDA device is present, loading or creating a context raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libviltrum_cuda.so")
+
+VCU_MAX_DIM = 6
+VCU_MAX_DIMBINS = 4
+MEM_HOST, MEM_DEVICE = 0, 1
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "QUEUE_OVERFLOW", 4: "DEVICE_TIMEOUT", 5: "NAN_DETECTED",
+          6: "CUDA_ERROR", 7: "NO_DEVICE", 8: "UNSUPPORTED"}
+FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
+
+EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
+           "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested"]
+
+
+class VcuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS.get(code, code)}: {message}")
+        self.code = code
+
+
+class Integrand(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("n_params", ctypes.c_int32), ("params", ctypes.POINTER(ctypes.c_float))]
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("f", Integrand), ("dim", ctypes.c_int32), ("dimbins", ctypes.c_int32),
+                ("range_min", ctypes.c_float * VCU_MAX_DIM), ("range_max", ctypes.c_float * VCU_MAX_DIM),
+                ("resolution", ctypes.c_uint64 * VCU_MAX_DIMBINS), ("mem", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class Nested(ctypes.Structure):
+    _fields_ = [("rule_hi", ctypes.c_int32), ("rule_lo", ctypes.c_int32), ("heuristic", ctypes.c_int32),
+                ("metric", ctypes.c_int32), ("size_weight", ctypes.c_double), ("min_size", ctypes.c_double),
+                ("min_val", ctypes.c_double)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("evaluations", ctypes.c_uint64), ("regions", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("flags", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with `python -m viltrum_gb300.build` "
+                               "(there is no CPU fallback)")
+        L = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        f32p = ctypes.POINTER(ctypes.c_float)
+        L.vcu_abi_version.restype = ctypes.c_int
+        L.vcu_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Opts)]
+        L.vcu_destroy.argtypes = [vp]
+        L.vcu_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+        L.vcu_channels.argtypes = [ctypes.c_int32]
+        L.vcu_eval.argtypes = [vp, ctypes.POINTER(Integrand), ctypes.c_int32, vp, ctypes.c_int64, vp, ctypes.c_int32]
+        L.vcu_per_bin_monte_carlo.argtypes = [vp, ctypes.POINTER(Problem), ctypes.c_uint64, ctypes.c_uint64, vp,
+                                              ctypes.POINTER(Stats)]
+        L.vcu_per_bin_monte_carlo_replay.argtypes = [vp, ctypes.POINTER(Problem), ctypes.c_uint64, vp, vp,
+                                                     ctypes.POINTER(Stats)]
+        L.vcu_per_bin_adaptive_nested.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested),
+                                                  ctypes.c_uint64, vp, vp, ctypes.POINTER(Stats)]
+        for name in EXPORTS:
+            getattr(L, name).restype = ctypes.c_int
+        del f32p
+        _lib = L
+        return L
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array, torch tensor or raw integer pointer."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+class Context:
+    """One vcu_ctx: a CUDA stream plus the library's device buffers on one device."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        opts = Opts(device, 0, stream)
+        rc = self.lib.vcu_create(ctypes.byref(h), ctypes.byref(opts))
+        if rc != 0:
+            raise VcuError(rc, "vcu_create failed (no CUDA device or driver?)")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.vcu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        self.lib.vcu_last_error(self.handle, buf, 512)
+        return buf.value.decode()
+
+    def check(self, rc: int):
+        if rc != 0:
+            raise VcuError(rc, self.last_error())
+
+    # ----------------------------------------------------------------- entry points
+    @staticmethod
+    def problem(kind, params, rmin, rmax, res, mem=MEM_HOST):
+        params = np.ascontiguousarray(params if params is not None else np.zeros(0), dtype=np.float32)
+        p = Problem()
+        p.f = Integrand(int(kind), int(params.size),
+                        params.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if params.size else None)
+        p.dim = len(rmin)
+        p.dimbins = len(res)
+        for d in range(len(rmin)):
+            p.range_min[d] = float(rmin[d])
+            p.range_max[d] = float(rmax[d])
+        for d in range(len(res)):
+            p.resolution[d] = int(res[d])
+        p.mem = mem
+        p._keep = params  # keep the parameter array alive with the struct
+        return p
+
+    def channels(self, kind: int) -> int:
+        c = self.lib.vcu_channels(int(kind))
+        if c < 0:
+            raise VcuError(-c, f"unknown integrand kind {kind}")
+        return c
+
+    def eval(self, kind, params, x, mem=MEM_HOST, out=None):
+        params = np.ascontiguousarray(params if params is not None else np.zeros(0), dtype=np.float32)
+        f = Integrand(int(kind), int(params.size),
+                      params.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if params.size else None)
+        if mem == MEM_HOST:
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            npts, dim = x.shape
+            out = np.empty((npts, self.channels(kind)), dtype=np.float32)
+        else:
+            npts, dim = x.shape
+        self.check(self.lib.vcu_eval(self.handle, ctypes.byref(f), dim, _ptr(x), npts, _ptr(out), mem))
+        return out
+
+    def per_bin_monte_carlo(self, p: Problem, spp: int, seed: int, bins) -> Stats:
+        st = Stats()
+        self.check(self.lib.vcu_per_bin_monte_carlo(self.handle, ctypes.byref(p), spp, seed, _ptr(bins),
+                                                    ctypes.byref(st)))
+        return st
+
+    def per_bin_monte_carlo_replay(self, p: Problem, spp: int, points, bins) -> Stats:
+        st = Stats()
+        self.check(self.lib.vcu_per_bin_monte_carlo_replay(self.handle, ctypes.byref(p), spp, _ptr(points),
+                                                           _ptr(bins), ctypes.byref(st)))
+        return st
+
+    def per_bin_adaptive_nested(self, p: Problem, nested: Nested, iterations: int, bins, trace=None) -> Stats:
+        st = Stats()
+        self.check(self.lib.vcu_per_bin_adaptive_nested(self.handle, ctypes.byref(p), ctypes.byref(nested),
+                                                        iterations, _ptr(bins), _ptr(trace), ctypes.byref(st)))
+        return st
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx

@@ -1,0 +1,531 @@
+/*
+ * k_nested.cu -- per-bin adaptive nested Newton-Cotes on the device.
+ *
+ * Replaces integrator_per_bin_parallel(integrator_adaptive_iterations(nested(H,L), heuristic,
+ * iterations)): for every bin, the reference builds a root region over the bin
+ * (src/newton-cotes/region.h:74-78), then `iterations` times pops the region of largest error
+ * estimate from a std heap, splits it in two along its worst dimension re-using the parent's
+ * even nodes (region.h:345-359, src/multiarray/split.h:13-49), estimates the children's errors
+ * (region.h:387-418, src/nested/error-heuristic.h) and pushes them
+ * (src/nested/regions-generator-adaptive-heap.h:18-45); finally it integrates every region over
+ * its intersection with the bin, in heap order (src/newton-cotes/regions-integrator-sequential.h:37-58),
+ * and scales by prod(res) (src/integrator-per-bin-parallel.h:33).
+ *
+ * GB300 mapping: a group of G lanes of a warp owns one bin at a time (grid-stride over bins, a
+ * persistent grid sized by occupancy).  All node values of the bin's live regions, their ranges,
+ * the heap and the scratch of the error folds live in the group's slice of shared memory; the
+ * group evaluates the integrand at a region's new nodes in parallel (Boole 2-D: 20 new nodes per
+ * split, 5 rounds of 4 lanes), folds the per-line error metrics in parallel, and one lane keeps
+ * the heap.  Nothing touches global memory but the integrand parameters (kernel parameter space)
+ * and the bin writes.
+ */
+#pragma once
+#include "vcu_heap.h"
+#include "vcu_internal.cuh"
+#include "vcu_rules.cuh"
+
+namespace vcu {
+
+namespace nc_detail {
+
+constexpr int NC_THREADS = 128;
+
+__host__ __device__ constexpr int ipow(int b, int e) { return e <= 0 ? 1 : b * ipow(b, e - 1); }
+
+struct NcCfg {
+    int32_t iters;
+    int32_t nslot;
+    int32_t nheap;
+    int32_t words_per_group;
+    int32_t heuristic, relative;
+    float min_val_f;  /* smallest float >= error_metric_relative's min_val */
+    double size_weight;
+    double min_size;
+};
+
+template <int DIM, int S, int CH> struct Layout {
+    static constexpr int SD = ipow(S, DIM);
+    static constexpr int NL = ipow(S, DIM - 1);
+    /* words of one group's slice for a given slot/heap count */
+    static __host__ __device__ int words(int nslot, int nheap) {
+        return nslot * SD * CH          /* node values            */
+               + nslot * (2 * DIM + 1)  /* ranges + volume        */
+               + 2 * nheap              /* heap keys + payloads   */
+               + 2 * DIM * NL           /* line metrics           */
+               + 2 * DIM                /* per-dimension errors   */
+               + DIM * S + (S - 1)      /* node coordinates       */
+               + nheap * CH;            /* region contributions   */
+    }
+};
+
+/* index of the node with coordinate `pos` along dimension d and the other coordinates given by J
+ * (J enumerates the remaining dimensions, dim-0 fastest) */
+template <int DIM, int S> __device__ __forceinline__ int node_index(int d, int J, int pos) {
+    int idx = 0, rem = J;
+#pragma unroll
+    for (int e = 0; e < DIM; ++e) {
+        if (e == d) {
+            idx += pos * ipow(S, e);
+        } else {
+            idx += (rem % S) * ipow(S, e);
+            rem /= S;
+        }
+    }
+    return idx;
+}
+
+template <int DIM, int S>
+__device__ float fold_all_errors(const float* lines) {
+    /* lines: S^(DIM-1) metric values, dim-0 fastest; fold dimension 0 repeatedly with the high
+     * rule (the reference's fold_all(quadrature)) */
+    constexpr int NL = ipow(S, DIM - 1);
+    if constexpr (DIM == 1) {
+        return lines[0];
+    } else {
+        float buf[NL];
+#pragma unroll
+        for (int i = 0; i < NL; ++i) buf[i] = lines[i];
+        int n = NL;
+#pragma unroll
+        for (int level = 0; level < DIM - 1; ++level) {
+            n /= S;
+            for (int i = 0; i < n; ++i) buf[i] = RefRule<S>::scalar(buf + i * S);
+        }
+        return buf[0];
+    }
+}
+
+/* integral of one region's polynomial over its intersection [A,B] (normalised), folding the
+ * last dimension first (region.h:141-150); values of channel c */
+template <int DIM, int S, int CH>
+__device__ float region_subrange(const float* V, int c, const float* A, const float* B) {
+    constexpr int SD = ipow(S, DIM);
+    float buf[SD / S];
+    /* first level: fold dimension DIM-1 straight from shared memory */
+    constexpr int inner = SD / S;
+#pragma unroll
+    for (int i = 0; i < inner; ++i) {
+        float line[S];
+#pragma unroll
+        for (int j = 0; j < S; ++j) line[j] = V[(i + j * inner) * CH + c];
+        buf[i] = Rule<S>::subrange(A[DIM - 1], B[DIM - 1], line);
+    }
+    int n = inner;
+#pragma unroll
+    for (int d = DIM - 2; d >= 0; --d) {
+        const int m = n / S;
+        for (int i = 0; i < m; ++i) {
+            float line[S];
+#pragma unroll
+            for (int j = 0; j < S; ++j) line[j] = buf[i + j * m];
+            buf[i] = Rule<S>::subrange(A[d], B[d], line);
+        }
+        n = m;
+    }
+    return buf[0];
+}
+
+template <class F, int DIM, int SH, int SL, int G>
+__global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_constant__ F f, const BinGrid g,
+                                                               const NcCfg cfg, float* __restrict__ bins,
+                                                               int32_t* __restrict__ trace,
+                                                               uint32_t* __restrict__ status) {
+    constexpr int S = SH;
+    constexpr int CH = F::CH;
+    constexpr int SD = ipow(S, DIM);
+    constexpr int NL = ipow(S, DIM - 1);
+    constexpr int NNEW = (S - 1) * NL;
+    extern __shared__ float smem[];
+
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const int gib = threadIdx.x / G;
+    const int gpb = blockDim.x / G;
+
+    float* V = smem + (size_t)gib * cfg.words_per_group;
+    float* RMIN = V + cfg.nslot * SD * CH;
+    float* RMAX = RMIN + cfg.nslot * DIM;
+    float* VOL = RMAX + cfg.nslot * DIM;
+    float* HE = VOL + cfg.nslot;
+    int* HS = reinterpret_cast<int*>(HE + cfg.nheap);
+    float* LN = reinterpret_cast<float*>(HS + cfg.nheap);
+    float* EC = LN + 2 * DIM * NL;
+    float* CO = EC + 2 * DIM;
+    float* CN = CO + DIM * S;
+    float* CT = CN + (S - 1);
+
+    const uint64_t ngroups = (uint64_t)gridDim.x * gpb;
+    const int iters = cfg.iters;
+
+    for (uint64_t bin = (uint64_t)blockIdx.x * gpb + gib; bin < g.nbins; bin += ngroups) {
+        /* ---- bin sub-range (integrator-per-bin-parallel.h:30-32) */
+        float bmin[DIM], bmax[DIM];
+        {
+            uint64_t rem = bin;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                if (d < g.dimbins) {
+                    const uint32_t pos = (uint32_t)(rem % g.res[d]);
+                    rem /= g.res[d];
+                    bmin[d] = vadd(g.rmin[d], vmul((float)pos, g.drange[d]));
+                    bmax[d] = vadd(g.rmin[d], vmul((float)(pos + 1), g.drange[d]));
+                } else {
+                    bmin[d] = g.rmin[d];
+                    bmax[d] = g.rmax[d];
+                }
+            }
+        }
+        /* ---- root region in slot 0 */
+        if (gl == 0) {
+            float vol = 1.0f;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                RMIN[d] = bmin[d];
+                RMAX[d] = bmax[d];
+                vol = vmul(vol, vsub(bmax[d], bmin[d]));
+            }
+            VOL[0] = vol;
+        }
+        for (int t = gl; t < DIM * S; t += G) {
+            const int d = t / S, j = t % S;
+            CO[t] = node_coord((double)j / (double)(S - 1), vsub(bmax[d], bmin[d]), bmin[d]);
+        }
+        __syncwarp(gmask);
+        for (int t = gl; t < SD; t += G) {
+            float x[F::DIM];
+#pragma unroll
+            for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+            int rem = t;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                x[d] = CO[d * S + rem % S];
+                rem /= S;
+            }
+            float v[CH];
+            f(x, v);
+#pragma unroll
+            for (int c = 0; c < CH; ++c) V[t * CH + c] = v[c];
+        }
+        __syncwarp(gmask);
+
+        /* ---- error estimates of `nreg` regions (slots sl[0..nreg)) into EC[r*DIM + d] */
+        auto region_errors = [&](int nreg, int s0, int s1) {
+            for (int t = gl; t < nreg * DIM * NL; t += G) {
+                const int r = t / (DIM * NL), rr = t % (DIM * NL);
+                const int d = rr / NL, J = rr % NL;
+                const float* RV = V + (size_t)(r ? s1 : s0) * SD * CH;
+                float m = 0.0f;
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    float line[S], low[SL];
+#pragma unroll
+                    for (int i = 0; i < S; ++i) line[i] = RV[node_index<DIM, S>(d, J, i) * CH + c];
+#pragma unroll
+                    for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+                    float H, L;
+                    if constexpr (CH == 1) {
+                        H = RefRule<S>::scalar(line);
+                        L = RefRule<SL>::scalar(low);
+                    } else {
+                        H = RefRule<S>::rgb(line);
+                        L = RefRule<SL>::rgb(low);
+                    }
+                    const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
+                    m = (c == 0) ? mv : vadd(m, mv);
+                }
+                LN[t] = m;
+            }
+            __syncwarp(gmask);
+            for (int t = gl; t < nreg * DIM; t += G) {
+                const int r = t / DIM;
+                const float folded = fold_all_errors<DIM, S>(LN + t * NL);
+                EC[t] = vmul(VOL[r ? s1 : s0], folded);
+            }
+            __syncwarp(gmask);
+        };
+        /* heuristic over EC[r*DIM ..] for the region in slot s (lane 0 only) */
+        auto heuristic = [&](int r, int s, float& err_out, int& dim_out) {
+            const float* e = EC + r * DIM;
+            if (cfg.heuristic == VCU_HEUR_DEFAULT) {
+                float max_err = 0.0f;
+                int max_dim = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    if (e[d] > max_err) {
+                        max_err = e[d];
+                        max_dim = d;
+                    }
+                err_out = max_err;
+                dim_out = max_dim;
+                return;
+            }
+            float w = vsub(RMAX[s * DIM], RMIN[s * DIM]);
+            float max_err;
+            if ((double)w < cfg.min_size || isnan(w)) max_err = 0.0f;
+            else max_err = __double2float_rn(__dadd_rn((double)e[0], __dmul_rn(cfg.size_weight, (double)fabsf(w))));
+            int max_dim = 0;
+#pragma unroll
+            for (int d = 1; d < DIM; ++d) {
+                w = vsub(RMAX[s * DIM + d], RMIN[s * DIM + d]);
+                float err = __double2float_rn(__dadd_rn((double)e[d], __dmul_rn(cfg.size_weight, (double)fabsf(w))));
+                if ((double)w < cfg.min_size) err = 0.0f;
+                if (err >= max_err) {
+                    max_err = err;
+                    max_dim = d;
+                }
+            }
+            err_out = max_err;
+            dim_out = max_dim;
+        };
+
+        region_errors(1, 0, 0);
+        if (gl == 0) {
+            float e;
+            int dm;
+            heuristic(0, 0, e, dm);
+            HE[0] = e;
+            HS[0] = 0 | (dm << 8);
+        }
+        uint64_t freemask = (cfg.nslot >= 64 ? ~0ull : ((1ull << cfg.nslot) - 1ull)) & ~1ull;
+
+        for (int it = 0; it < iters; ++it) {
+            __syncwarp(gmask);
+            const int top = HS[0];
+            const int P = top & 0xff, dd = top >> 8;
+            const int C0 = __ffsll((long long)freemask) - 1;
+            freemask &= freemask - 1;
+            const int C1 = __ffsll((long long)freemask) - 1;
+            freemask &= freemask - 1;
+            /* node coordinates of the parent (other dimensions) and of the new nodes along dd */
+            for (int t = gl; t < DIM * S + (S - 1); t += G) {
+                if (t < DIM * S) {
+                    const int d = t / S, j = t % S;
+                    const float mn = RMIN[P * DIM + d];
+                    CO[t] = node_coord((double)j / (double)(S - 1), vsub(RMAX[P * DIM + d], mn), mn);
+                } else {
+                    const int k = t - DIM * S;
+                    const float mn = RMIN[P * DIM + dd];
+                    CN[k] = node_coord((double)(2 * k + 1) / (double)(2 * (S - 1)), vsub(RMAX[P * DIM + dd], mn), mn);
+                }
+            }
+            __syncwarp(gmask);
+            float* VP = V + (size_t)P * SD * CH;
+            float* V0 = V + (size_t)C0 * SD * CH;
+            float* V1 = V + (size_t)C1 * SD * CH;
+            /* new nodes: odd positions of the 2(S-1)+1 grid along dd */
+            for (int t = gl; t < NNEW; t += G) {
+                const int k = t / NL, J = t % NL;
+                float x[F::DIM];
+#pragma unroll
+                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+                int rem = J;
+#pragma unroll
+                for (int e = 0; e < DIM; ++e) {
+                    if (e == dd) continue;
+                    x[e] = CO[e * S + rem % S];
+                    rem /= S;
+                }
+                x[dd] = CN[k];
+                float v[CH];
+                f(x, v);
+                const int i = 2 * k + 1;
+                if (i <= S - 1) {
+                    const int n0 = node_index<DIM, S>(dd, J, i);
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) V0[n0 * CH + c] = v[c];
+                }
+                if (i >= S - 1) {
+                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = v[c];
+                }
+            }
+            /* parent nodes re-used at the even positions */
+            for (int t = gl; t < S * NL; t += G) {
+                const int m = t / NL, J = t % NL;
+                const int i = 2 * m;
+                const int src = node_index<DIM, S>(dd, J, m);
+                if (i <= S - 1) {
+                    const int n0 = node_index<DIM, S>(dd, J, i);
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) V0[n0 * CH + c] = VP[src * CH + c];
+                }
+                if (i >= S - 1) {
+                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = VP[src * CH + c];
+                }
+            }
+            if (gl == 0) {
+                const float pmn = RMIN[P * DIM + dd], pmx = RMAX[P * DIM + dd];
+                const float half = vdiv(vsub(pmx, pmn), 2.0f);
+                const float mid = vadd(pmn, vmul(half, 1.0f));
+                float vol0 = 1.0f, vol1 = 1.0f;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const float mn = RMIN[P * DIM + d], mx = RMAX[P * DIM + d];
+                    const float mx0 = (d == dd) ? mid : mx;
+                    const float mn1 = (d == dd) ? mid : mn;
+                    RMIN[C0 * DIM + d] = mn;
+                    RMAX[C0 * DIM + d] = mx0;
+                    RMIN[C1 * DIM + d] = mn1;
+                    RMAX[C1 * DIM + d] = mx;
+                    vol0 = vmul(vol0, vsub(mx0, mn));
+                    vol1 = vmul(vol1, vsub(mx, mn1));
+                }
+                VOL[C0] = vol0;
+                VOL[C1] = vol1;
+            }
+            __syncwarp(gmask);
+            region_errors(2, C0, C1);
+            if (gl == 0) {
+                float e0, e1;
+                int d0, d1;
+                heuristic(0, C0, e0, d0);
+                heuristic(1, C1, e1, d1);
+                if (trace) {
+                    trace[((size_t)bin * iters + it) * 2] = dd;
+                    trace[((size_t)bin * iters + it) * 2 + 1] = __float_as_int(HE[0]);
+                }
+                const int n = it + 1; /* heap size before this split */
+                heap_pop(HE, HS, n);
+                HE[n - 1] = e0;
+                HS[n - 1] = C0 | (d0 << 8);
+                heap_push(HE, HS, n);
+                HE[n] = e1;
+                HS[n] = C1 | (d1 << 8);
+                heap_push(HE, HS, n + 1);
+            }
+            freemask |= 1ull << P;
+        }
+        __syncwarp(gmask);
+        /* ---- integrate each region over its intersection with the bin
+         * (regions-integrator-sequential.h:37-58 with a single bin: the bin range is the bin's
+         * sub-range with dimension 0 rebuilt as min + 1*(max-min)) */
+        const int nreg = iters + 1;
+        for (int k = gl; k < nreg; k += G) {
+            const int s = HS[k] & 0xff;
+            float A[DIM], B[DIM];
+            bool empty = false;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const float blo = bmin[d];
+                const float bhi = (d == 0) ? vadd(bmin[0], vmul(1.0f, vdiv(vsub(bmax[0], bmin[0]), 1.0f))) : bmax[d];
+                const float rmn = RMIN[s * DIM + d], rmx = RMAX[s * DIM + d];
+                const float a = smax(blo, rmn);
+                const float b = smax(a, smin(bhi, rmx));
+                empty = empty || (a >= b);
+                A[d] = (rmn >= rmx) ? rmn : vdiv(vsub(a, rmn), vsub(rmx, rmn));
+                B[d] = (rmn >= rmx) ? rmn : vdiv(vsub(b, rmn), vsub(rmx, rmn));
+            }
+#pragma unroll
+            for (int c = 0; c < CH; ++c)
+                CT[k * CH + c] = empty ? 0.0f : vmul(VOL[s], region_subrange<DIM, S, CH>(V + (size_t)s * SD * CH, c, A, B));
+            if (empty) CT[k * CH] = __int_as_float(0x7fc00001); /* marker: skipped region */
+        }
+        __syncwarp(gmask);
+        if (gl == 0) {
+            float sol[CH];
+#pragma unroll
+            for (int c = 0; c < CH; ++c) sol[c] = 0.0f;
+            for (int k = 0; k < nreg; ++k) {
+                if (__float_as_int(CT[k * CH]) == 0x7fc00001) continue;
+#pragma unroll
+                for (int c = 0; c < CH; ++c) sol[c] = vadd(sol[c], CT[k * CH + c]);
+            }
+            bool nan = false;
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                const float v = vmul(g.factor, sol[c]);
+                nan = nan || isnan(v);
+                bins[bin * CH + c] = v;
+            }
+            if (nan) atomicOr(status, VCU_FLAG_NAN);
+        }
+        __syncwarp(gmask);
+    }
+}
+
+template <int DIM, int S> constexpr int lanes_per_bin() {
+    /* lanes sharing one bin: enough to cover one split's new nodes in a few rounds */
+    return ((S - 1) * ipow(S, DIM - 1) <= 24) ? 4 : (((S - 1) * ipow(S, DIM - 1) <= 64) ? 8 : 32);
+}
+
+template <int DIM, int SH, int SL, class F>
+int launch(vcu_ctx* ctx, const F& f, const BinGrid& g, const vcu_nested& n, int iterations, float* d_bins,
+           int32_t* d_trace, uint32_t& launches) {
+    constexpr int G = lanes_per_bin<DIM, SH>();
+    using Lay = Layout<DIM, SH, F::CH>;
+    NcCfg cfg{};
+    cfg.iters = iterations;
+    cfg.nslot = iterations + 2;
+    cfg.nheap = iterations + 1;
+    int w = Lay::words(cfg.nslot, cfg.nheap);
+    /* pad so that consecutive groups start G banks apart: conflict-free same-offset accesses */
+    while ((w & 31) != (G & 31)) ++w;
+    cfg.words_per_group = w;
+    cfg.heuristic = n.heuristic;
+    cfg.relative = n.metric == VCU_METRIC_RELATIVE;
+    float mv = (float)n.min_val;
+    if ((double)mv < n.min_val) mv = nextafterf(mv, INFINITY);
+    cfg.min_val_f = mv;
+    cfg.size_weight = n.size_weight;
+    cfg.min_size = n.min_size;
+    /* bins per block: as many as fit in shared memory, up to NC_THREADS / G */
+    int gpb = NC_THREADS / G;
+    while (gpb > 1 && (size_t)gpb * (size_t)w * 4 > ctx->smem_optin) gpb /= 2;
+    const size_t smem = (size_t)gpb * (size_t)w * 4;
+    if (smem > ctx->smem_optin)
+        return fail(ctx, VCU_UNSUPPORTED,
+                    "per-bin region storage of " + std::to_string(smem) + " bytes exceeds shared memory");
+    const int threads = gpb * G;
+    auto kern = k_per_bin_nested<F, DIM, SH, SL, G>;
+    VCU_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+    if (per_sm < 1) per_sm = 1;
+    const uint64_t need = (g.nbins + gpb - 1) / gpb;
+    const uint64_t cap = (uint64_t)ctx->sm_count * per_sm;
+    const unsigned blocks = (unsigned)(need < cap ? need : cap);
+    kern<<<blocks, threads, smem, ctx->stream>>>(f, g, cfg, d_bins, d_trace, ctx->d_status);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+    return VCU_OK;
+}
+
+}  // namespace nc_detail
+using namespace nc_detail;
+
+/* per-bin nested quadrature for one rule pair; region storage is limited to S^dim <= 125
+ * nodes (Boole up to 3-D, Simpson up to 4-D) */
+template <int SH, int SL>
+int run_nested_pair(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+                    float* d_bins, int32_t* d_trace, uint32_t& launches) {
+    return with_integrand(ctx, p->f, p->dim, [&](const auto& f) -> int {
+        using F = std::decay_t<decltype(f)>;
+        auto by_dim = [&](auto dimc) -> int {
+            constexpr int DIM = decltype(dimc)::value;
+            if constexpr (ipow(SH, DIM) <= 125)
+                return launch<DIM, SH, SL>(ctx, f, g, n, iterations, d_bins, d_trace, launches);
+            else
+                return fail(ctx, VCU_UNSUPPORTED, "per-bin nested regions are limited to 125 nodes (S^dim)");
+        };
+        if constexpr (F::DIM == 6) {
+            /* the half-space functor takes its arity at run time */
+            switch (p->dim) {
+            case 2: return by_dim(std::integral_constant<int, 2>{});
+            case 3: return by_dim(std::integral_constant<int, 3>{});
+            default:
+                return fail(ctx, VCU_UNSUPPORTED,
+                            "per-bin nested quadrature of the half-space integrand is built for 2-3 dimensions");
+            }
+        } else if constexpr (F::DIM <= 4) {
+            return by_dim(std::integral_constant<int, F::DIM>{});
+        } else {
+            return fail(ctx, VCU_UNSUPPORTED, "per-bin nested quadrature is built for up to 4 dimensions");
+        }
+    });
+}
+
+}  // namespace vcu

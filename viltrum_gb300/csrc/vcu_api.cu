@@ -1,0 +1,272 @@
+/*
+ * vcu_api.cu -- the extern "C" entry points of libviltrum_cuda.so (declared in
+ * include/viltrum_cuda.h): context lifetime, argument validation, host<->device staging of the
+ * caller's buffers, timing and device status.  The kernels live in k_*.cu.
+ */
+#include <cmath>
+#include <new>
+
+#include "vcu_internal.cuh"
+
+namespace vcu {
+
+int make_grid(vcu_ctx* ctx, const vcu_problem* p, BinGrid& g) {
+    if (!p) return fail(ctx, VCU_INVALID_ARG, "null problem");
+    if (p->dim < 1 || p->dim > VCU_MAX_DIM) return fail(ctx, VCU_INVALID_ARG, "dim must be 1..6");
+    if (p->dimbins < 1 || p->dimbins > VCU_MAX_DIMBINS || p->dimbins > p->dim)
+        return fail(ctx, VCU_INVALID_ARG, "dimbins must be 1..min(dim,4)");
+    if (p->mem != VCU_MEM_HOST && p->mem != VCU_MEM_DEVICE) return fail(ctx, VCU_INVALID_ARG, "mem must be host or device");
+    std::memset(&g, 0, sizeof(g));
+    g.dim = p->dim;
+    g.dimbins = p->dimbins;
+    for (int d = 0; d < p->dim; ++d) {
+        if (!std::isfinite(p->range_min[d]) || !std::isfinite(p->range_max[d]))
+            return fail(ctx, VCU_INVALID_ARG, "range bounds must be finite");
+        g.rmin[d] = p->range_min[d];
+        g.rmax[d] = p->range_max[d];
+    }
+    uint64_t nb = 1;
+    double prod = 1.0;
+    for (int d = 0; d < p->dimbins; ++d) {
+        const uint64_t r = p->resolution[d];
+        if (r == 0 || r > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "resolution must be 1..2^32-1");
+        if (nb > (1ull << 40) / r) return fail(ctx, VCU_INVALID_ARG, "too many bins");
+        nb *= r;
+        prod *= (double)r;
+        g.res[d] = (uint32_t)r;
+        /* (range.max(i) - range.min(i)) / Float(res[i]) in float (integrator-per-bin-parallel.h:22) */
+        volatile float w = p->range_max[d] - p->range_min[d];
+        g.drange[d] = w / (float)r;
+    }
+    g.nbins = nb;
+    g.factor = (float)prod;
+    return VCU_OK;
+}
+
+int CallScope::begin() {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    VCU_CUDA(ctx, cudaSetDevice(ctx->device));
+    VCU_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
+    VCU_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    return VCU_OK;
+}
+
+int CallScope::end(uint64_t evaluations, uint64_t regions) {
+    VCU_CUDA(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    uint32_t flags = 0;
+    VCU_CUDA(ctx, cudaMemcpyAsync(&flags, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    VCU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+    if (stats) {
+        stats->device_ms = ms;
+        stats->evaluations = evaluations;
+        stats->regions = regions;
+        stats->kernel_launches = launches;
+        stats->flags = flags;
+    }
+    if (flags & VCU_FLAG_TIMEOUT) return fail(ctx, VCU_DEVICE_TIMEOUT, "a device-side wait expired");
+    if (flags & VCU_FLAG_OVERFLOW) return fail(ctx, VCU_QUEUE_OVERFLOW, "a device queue overflowed");
+    return VCU_OK;
+}
+
+/* output buffer: the caller's device pointer, or the context's staging buffer */
+static int out_buffer(vcu_ctx* ctx, const vcu_problem* p, float* user, size_t bytes, float** dev) {
+    if (p->mem == VCU_MEM_DEVICE) {
+        *dev = user;
+        return VCU_OK;
+    }
+    int rc = ensure(ctx, ctx->out, bytes);
+    if (rc) return rc;
+    *dev = static_cast<float*>(ctx->out.ptr);
+    return VCU_OK;
+}
+
+}  // namespace vcu
+
+using namespace vcu;
+
+extern "C" int vcu_abi_version(void) { return VCU_ABI_VERSION; }
+
+extern "C" int vcu_create(vcu_ctx** out, const vcu_opts* opts) {
+    if (!out) return VCU_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return VCU_NO_DEVICE;
+    }
+    vcu_ctx* ctx = new (std::nothrow) vcu_ctx();
+    if (!ctx) return VCU_OOM;
+    ctx->device = opts ? opts->device : 0;
+    if (ctx->device < 0 || ctx->device >= ndev) {
+        delete ctx;
+        return VCU_INVALID_ARG;
+    }
+    auto bail = [&](cudaError_t e) {
+        (void)e;
+        cudaGetLastError();
+        vcu_destroy(ctx);
+        return VCU_CUDA_ERROR;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(ctx->device)) != cudaSuccess) return bail(e);
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, ctx->device)) != cudaSuccess) return bail(e);
+    ctx->sm_count = prop.multiProcessorCount;
+    ctx->smem_optin = prop.sharedMemPerBlockOptin;
+    if (opts && opts->stream) {
+        ctx->stream = static_cast<cudaStream_t>(opts->stream);
+        ctx->own_stream = false;
+    } else {
+        if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+        ctx->own_stream = true;
+    }
+    if ((e = cudaEventCreate(&ctx->ev_start)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&ctx->d_status, 256)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(ctx->d_status, 0, 256)) != cudaSuccess) return bail(e);
+    *out = ctx;
+    return VCU_OK;
+}
+
+extern "C" int vcu_destroy(vcu_ctx* ctx) {
+    if (!ctx) return VCU_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (vcu_buffer* b : {&ctx->out, &ctx->aux, &ctx->in, &ctx->scratch})
+        if (b->ptr) cudaFree(b->ptr);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    cudaGetLastError();
+    delete ctx;
+    return VCU_OK;
+}
+
+extern "C" int vcu_last_error(const vcu_ctx* ctx, char* buf, size_t len) {
+    if (!ctx || !buf || len == 0) return VCU_INVALID_ARG;
+    std::snprintf(buf, len, "%s", ctx->last_error.c_str());
+    return VCU_OK;
+}
+
+extern "C" int vcu_channels(int32_t kind) {
+    switch (kind) {
+    case VCU_F_POLY2: case VCU_F_SIN1: case VCU_F_SPHERE3: case VCU_F_WAVE2: case VCU_F_SCENE2:
+    case VCU_F_HALFSPACE: case VCU_F_OCCLUDED_SCENE5:
+        return 1;
+    case VCU_F_MOVING_SCENE3:
+        return 3;
+    default:
+        return -VCU_INVALID_ARG;
+    }
+}
+
+extern "C" int vcu_eval(vcu_ctx* ctx, const vcu_integrand* f, int32_t dim, const float* x, int64_t npts, float* out,
+                        int32_t mem) {
+    if (!ctx) return VCU_INVALID_ARG;
+    if (!f || npts < 0 || (npts > 0 && (!x || !out))) return fail(ctx, VCU_INVALID_ARG, "bad vcu_eval arguments");
+    const int ch = vcu_channels(f->kind);
+    if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
+    CallScope scope{ctx, nullptr};
+    int rc = scope.begin();
+    if (rc) return rc;
+    const float* dx = x;
+    float* dout = out;
+    if (mem == VCU_MEM_HOST && npts > 0) {
+        if ((rc = ensure(ctx, ctx->in, (size_t)npts * dim * 4))) return rc;
+        if ((rc = ensure(ctx, ctx->out, (size_t)npts * ch * 4))) return rc;
+        VCU_CUDA(ctx, cudaMemcpyAsync(ctx->in.ptr, x, (size_t)npts * dim * 4, cudaMemcpyHostToDevice, ctx->stream));
+        dx = static_cast<float*>(ctx->in.ptr);
+        dout = static_cast<float*>(ctx->out.ptr);
+    }
+    if ((rc = run_eval(ctx, *f, dim, dx, npts, dout, scope.launches))) return rc;
+    if (mem == VCU_MEM_HOST && npts > 0)
+        VCU_CUDA(ctx, cudaMemcpyAsync(out, dout, (size_t)npts * ch * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    return scope.end((uint64_t)npts, 0);
+}
+
+static int per_bin_mc(vcu_ctx* ctx, const vcu_problem* p, uint64_t spp, uint64_t seed, const float* points, float* bins,
+                      vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    BinGrid g;
+    int rc = make_grid(ctx, p, g);
+    if (rc) return rc;
+    if (spp == 0 || spp > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "samples per bin must be 1..2^32-1");
+    if (!bins) return fail(ctx, VCU_INVALID_ARG, "null bins");
+    const int ch = vcu_channels(p->f.kind);
+    if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
+    CallScope scope{ctx, stats};
+    if ((rc = scope.begin())) return rc;
+    float* dbins = nullptr;
+    if ((rc = out_buffer(ctx, p, bins, g.nbins * ch * 4, &dbins))) return rc;
+    const float* dpts = points;
+    if (points && p->mem == VCU_MEM_HOST) {
+        const size_t bytes = g.nbins * spp * p->dim * 4;
+        if ((rc = ensure(ctx, ctx->in, bytes))) return rc;
+        VCU_CUDA(ctx, cudaMemcpyAsync(ctx->in.ptr, points, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        dpts = static_cast<const float*>(ctx->in.ptr);
+    }
+    if ((rc = run_mc(ctx, p, g, spp, seed, dpts, dbins, scope.launches))) return rc;
+    if (p->mem == VCU_MEM_HOST)
+        VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, g.nbins * ch * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    return scope.end(g.nbins * spp, 0);
+}
+
+extern "C" int vcu_per_bin_monte_carlo(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin, uint64_t seed,
+                                       float* bins, vcu_stats* stats) {
+    return per_bin_mc(ctx, p, samples_per_bin, seed, nullptr, bins, stats);
+}
+
+extern "C" int vcu_per_bin_monte_carlo_replay(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
+                                              const float* points, float* bins, vcu_stats* stats) {
+    if (ctx && !points) return fail(ctx, VCU_INVALID_ARG, "null points");
+    return per_bin_mc(ctx, p, samples_per_bin, 0, points, bins, stats);
+}
+
+extern "C" int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
+                                           uint64_t iterations, float* bins, int32_t* trace, vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    BinGrid g;
+    int rc = make_grid(ctx, p, g);
+    if (rc) return rc;
+    if (!nested || !bins) return fail(ctx, VCU_INVALID_ARG, "null nested rule or bins");
+    if (iterations > 62) return fail(ctx, VCU_UNSUPPORTED, "per-bin region budget is limited to 62 splits (63 regions)");
+    if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
+    if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    const int ch = vcu_channels(p->f.kind);
+    if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
+    CallScope scope{ctx, stats};
+    if ((rc = scope.begin())) return rc;
+    float* dbins = nullptr;
+    if ((rc = out_buffer(ctx, p, bins, g.nbins * ch * 4, &dbins))) return rc;
+    int32_t* dtrace = trace;
+    const size_t tbytes = g.nbins * iterations * 2 * 4;
+    if (trace && p->mem == VCU_MEM_HOST) {
+        if ((rc = ensure(ctx, ctx->aux, tbytes))) return rc;
+        dtrace = static_cast<int32_t*>(ctx->aux.ptr);
+    }
+    if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_SIMPSON)
+        rc = run_nested_bs(ctx, p, g, *nested, (int)iterations, dbins, dtrace, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_nested_bt(ctx, p, g, *nested, (int)iterations, dbins, dtrace, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_nested_st(ctx, p, g, *nested, (int)iterations, dbins, dtrace, scope.launches);
+    else
+        rc = fail(ctx, VCU_INVALID_ARG, "unsupported nested rule pair (boole/simpson, boole/trapezoidal, simpson/trapezoidal)");
+    if (rc) return rc;
+    if (p->mem == VCU_MEM_HOST) {
+        VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, g.nbins * ch * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        if (trace) VCU_CUDA(ctx, cudaMemcpyAsync(trace, dtrace, tbytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    /* evaluations: root S^dim + iterations x (S-1) S^(dim-1) per bin */
+    const int S = nested->rule_hi;
+    double sd = 1.0, sd1 = 1.0;
+    for (int d = 0; d < p->dim; ++d) sd *= S;
+    for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
+    const uint64_t evals = (uint64_t)((double)g.nbins * (sd + (double)iterations * (S - 1) * sd1));
+    return scope.end(evals, g.nbins * (iterations + 1));
+}

@@ -1,0 +1,179 @@
+/*
+ * vcu_internal.cuh -- runtime shared by the translation units of libviltrum_cuda.so:
+ * the context (stream, grow-only device buffers, status word, timing events), error plumbing,
+ * the Philox4x32-10 counter generator and the integrand dispatcher.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/vcu_integrands.h"
+#include "../../include/viltrum_cuda.h"
+
+/* status bits written by kernels into the context's status word */
+#define VCU_FLAG_NAN 1u
+#define VCU_FLAG_TIMEOUT 2u
+#define VCU_FLAG_OVERFLOW 4u
+
+struct vcu_buffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct vcu_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    uint32_t* d_status = nullptr; /* one word of device status flags */
+    vcu_buffer out, aux, in, scratch;
+    std::string last_error;
+};
+
+namespace vcu {
+
+inline int fail(vcu_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+inline int cuda_fail(vcu_ctx* ctx, cudaError_t e, const char* where) {
+    return fail(ctx, VCU_CUDA_ERROR, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define VCU_CUDA(ctx, call)                                      \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return vcu::cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+/* grow-only device buffer owned by the context */
+inline int ensure(vcu_ctx* ctx, vcu_buffer& b, size_t bytes) {
+    if (b.bytes >= bytes) return VCU_OK;
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes < 256 ? 256 : bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, VCU_OOM, std::string("device allocation of ") + std::to_string(bytes) + " bytes failed");
+    }
+    b.bytes = bytes;
+    return VCU_OK;
+}
+
+/* Problem geometry shared by the per-bin kernels (plain data, passed by value). */
+struct BinGrid {
+    float rmin[VCU_MAX_DIM], rmax[VCU_MAX_DIM];
+    float drange[VCU_MAX_DIMBINS]; /* (max-min)/float(res), float arithmetic */
+    uint32_t res[VCU_MAX_DIMBINS];
+    int32_t dim, dimbins;
+    uint64_t nbins;
+    float factor; /* prod(res) as float (exact below 2^24) */
+};
+
+int make_grid(vcu_ctx* ctx, const vcu_problem* p, BinGrid& g);
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the multiply-xor bijection
+ * with the published multipliers and Weyl key increments. */
+struct U4 {
+    uint32_t x, y, z, w;
+};
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+/* top 24 bits -> float in [0,1), exact */
+__device__ __forceinline__ float u01(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-08f; }
+
+/* Calls v(functor, channels) with the built-in functor selected by kind.  The functor object is
+ * built on the host (vcu_integrands.h build()); its size decides the kernel parameter size. */
+template <class V> int with_integrand(vcu_ctx* ctx, const vcu_integrand& f, int dim, V&& v) {
+    switch (f.kind) {
+    case VCU_F_POLY2: {
+        if (dim != 2) break;
+        Poly2 fn{};
+        return v(fn);
+    }
+    case VCU_F_SIN1: {
+        if (dim != 1) break;
+        Sin1 fn{};
+        return v(fn);
+    }
+    case VCU_F_SPHERE3: {
+        if (dim != 3) break;
+        Sphere3 fn{};
+        return v(fn);
+    }
+    case VCU_F_WAVE2: {
+        if (dim != 2) break;
+        Wave2 fn{};
+        return v(fn);
+    }
+    case VCU_F_SCENE2: {
+        if (dim != 2) break;
+        Scene2 fn{};
+        if (fn.build(f.params, f.n_params)) return fail(ctx, VCU_INVALID_ARG, "bad scene parameters");
+        return v(fn);
+    }
+    case VCU_F_MOVING_SCENE3: {
+        if (dim != 3) break;
+        MovingScene3 fn{};
+        if (fn.build(f.params, f.n_params)) return fail(ctx, VCU_INVALID_ARG, "bad moving-scene parameters");
+        return v(fn);
+    }
+    case VCU_F_HALFSPACE: {
+        Halfspace fn{};
+        if (fn.build(f.params, f.n_params)) return fail(ctx, VCU_INVALID_ARG, "bad half-space parameters");
+        if (fn.dim != dim) break;
+        return v(fn);
+    }
+    case VCU_F_OCCLUDED_SCENE5: {
+        if (dim != 5) break;
+        /* ~5 KB: keep it off the host stack of deep call chains */
+        static thread_local OccludedScene5 fn;
+        if (fn.build(f.params, f.n_params)) return fail(ctx, VCU_INVALID_ARG, "bad occluded-scene parameters");
+        return v(fn);
+    }
+    default:
+        return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind " + std::to_string(f.kind));
+    }
+    return fail(ctx, VCU_INVALID_ARG,
+                "integrand kind " + std::to_string(f.kind) + " does not take dimension " + std::to_string(dim));
+}
+
+/* timing + status helpers around a call */
+struct CallScope {
+    vcu_ctx* ctx;
+    vcu_stats* stats;
+    uint32_t launches = 0;
+    int begin();
+    int end(uint64_t evaluations, uint64_t regions);
+};
+
+}  // namespace vcu
+
+/* entry points implemented by the method translation units */
+namespace vcu {
+int run_mc(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, uint64_t spp, uint64_t seed, const float* points,
+           float* d_bins, uint32_t& launches);
+int run_nested_bs(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+                  float* d_bins, int32_t* d_trace, uint32_t& launches);
+int run_nested_bt(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+                  float* d_bins, int32_t* d_trace, uint32_t& launches);
+int run_nested_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+                  float* d_bins, int32_t* d_trace, uint32_t& launches);
+int run_eval(vcu_ctx* ctx, const vcu_integrand& f, int dim, const float* d_x, int64_t npts, float* d_out,
+             uint32_t& launches);
+}  // namespace vcu

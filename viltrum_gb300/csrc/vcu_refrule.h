@@ -1,0 +1,125 @@
+/*
+ * vcu_refrule.h -- Newton-Cotes rule values rounded exactly as the reference rounds them.
+ * Host and device compile the same code (tests/test_refrule.py checks it on the host against
+ * the reference's double-promoted expressions).
+ */
+#pragma once
+#include "../../include/vcu_integrands.h"
+#if !defined(__CUDACC__)
+#include <cmath>
+#include <cstring>
+#endif
+
+namespace vcu {
+
+/* ---------------------------------------------------------------------------------------------
+ * The rule VALUE as the reference computes it, used for the nested error estimate that decides
+ * every split.  For float node values the reference evaluates e.g. Boole's
+ *     (7.0*p0 + 32.0*p1 + 12.0*p2 + 32.0*p3 + 7.0*p4) / 90.0
+ * in double and rounds once to float (rules.h:254-257): the products are exact, the double sum is
+ * exact whenever the nodes span fewer than ~2^23 in magnitude, and the result is the float nearest
+ * to sum/90.  ref_scalar() reproduces that on the FP32 pipe: the weighted sum is accumulated
+ * error-free as a float-float pair (two-product / two-sum), then divided with a correctly rounded
+ * FP32 division plus one residual correction.  It differs from the reference only where the
+ * reference itself double-rounds (result within 2^-29 ulp of a float rounding boundary).
+ * ref_rgb() is the same expression for the 3-channel value type, whose operators round every
+ * step to float (oracle/vrgb.h semantics).
+ * ------------------------------------------------------------------------------------------- */
+VCU_HD void two_sum(float a, float b, float& s, float& e) {
+    s = vadd(a, b);
+    const float bb = vsub(s, a);
+    e = vadd(vsub(a, vsub(s, bb)), vsub(b, bb));
+}
+VCU_HD void two_prod(float a, float b, float& p, float& e) {
+    p = vmul(a, b);
+    e = vfma(a, b, -p);
+}
+VCU_HD float next_up(float x) {
+#if defined(__CUDA_ARCH__)
+    return nextafterf(x, __int_as_float(0x7f800000));
+#else
+    return std::nextafter(x, INFINITY);
+#endif
+}
+VCU_HD float next_down(float x) {
+#if defined(__CUDA_ARCH__)
+    return nextafterf(x, -__int_as_float(0x7f800000));
+#else
+    return std::nextafter(x, -INFINITY);
+#endif
+}
+VCU_HD bool even_bits(float x) {
+#if defined(__CUDA_ARCH__)
+    return (__float_as_uint(x) & 1u) == 0u;
+#else
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    return (u & 1u) == 0u;
+#endif
+}
+/* RN_f(RN_d((h + l) / D)) for the float-float pair (h, l) and a small positive integer D, as the
+ * reference's "double sum / double constant, assigned to float" rounds it.  q0 (a corrected
+ * RN(h/D)) is within one float of the result; the exact remainder R = h + l - q0*D (two_sum of the
+ * exact fma residual and l) decides: R/D beyond half the gap to the neighbour moves to it, exactly half (or within the
+ * 2^-30-ulp band where the reference's intermediate double lands on the midpoint) ties to even. */
+VCU_HD float ff_div(float h, float l, float D) {
+    /* q0 = RN(h/D) can be two floats away when l is a full ulp of h; one approximate correction
+     * step brings it within one float of the result */
+    const float q00 = vdiv(h, D);
+    const float q0 = vfma(vadd(vfma(-q00, D, h), l), vdiv(1.0f, D), q00);
+    float s, e;
+    two_sum(vfma(-q0, D, h), l, s, e);
+    const float up = next_up(q0), dn = next_down(q0);
+    const float tu = vmul(D, vmul(vsub(up, q0), 0.5f)); /* exact: D * half gap above */
+    const float td = vmul(D, vmul(vsub(q0, dn), 0.5f)); /* exact: D * half gap below */
+    const float band = vmul(tu, 9.313225746154785e-10f); /* 2^-30 of the half gap */
+    /* distance of R above +tu and below -td, each as (float + small float) */
+    const float du = vadd(vsub(s, tu), e);
+    const float dd = vadd(vsub(-s, td), -e);
+    if (vabs(du) <= band) return even_bits(q0) ? q0 : up;
+    if (vabs(dd) <= band) return even_bits(q0) ? q0 : dn;
+    if (du > 0.0f) return up;
+    if (dd > 0.0f) return dn;
+    return q0;
+}
+
+template <int S> struct RefRule;
+template <> struct RefRule<2> { /* (p0+p1)/2.0: float sum, exact halving */
+    static VCU_HD float scalar(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
+    static VCU_HD float rgb(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
+};
+template <> struct RefRule<3> { /* (p0 + 4.0*p1 + p2)/6.0 */
+    static VCU_HD float scalar(const float* p) {
+        float h, e1, h2, e2;
+        two_sum(p[0], vmul(4.0f, p[1]), h, e1);
+        two_sum(h, p[2], h2, e2);
+        return ff_div(h2, vadd(e1, e2), 6.0f);
+    }
+    static VCU_HD float rgb(const float* p) {
+        return vdiv(vadd(vadd(p[0], vmul(4.0f, p[1])), p[2]), 6.0f);
+    }
+};
+template <> struct RefRule<5> { /* (7.0*p0 + 32.0*p1 + 12.0*p2 + 32.0*p3 + 7.0*p4)/90.0 */
+    static VCU_HD float scalar(const float* p) {
+        float h, l, ph, pl, e;
+        two_prod(7.0f, p[0], h, l);
+        two_sum(h, vmul(32.0f, p[1]), h, e);
+        l = vadd(l, e);
+        two_prod(12.0f, p[2], ph, pl);
+        two_sum(h, ph, h, e);
+        l = vadd(l, vadd(pl, e));
+        two_sum(h, vmul(32.0f, p[3]), h, e);
+        l = vadd(l, e);
+        two_prod(7.0f, p[4], ph, pl);
+        two_sum(h, ph, h, e);
+        l = vadd(l, vadd(pl, e));
+        return ff_div(h, l, 90.0f);
+    }
+    static VCU_HD float rgb(const float* p) {
+        const float s = vadd(vadd(vadd(vadd(vmul(7.0f, p[0]), vmul(32.0f, p[1])), vmul(12.0f, p[2])), vmul(32.0f, p[3])),
+                             vmul(7.0f, p[4]));
+        return vdiv(s, 90.0f);
+    }
+};
+
+}  // namespace vcu

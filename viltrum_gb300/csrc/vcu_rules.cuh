@@ -1,0 +1,130 @@
+/*
+ * vcu_rules.cuh -- Newton-Cotes rule arithmetic on the device, in FP32.
+ *
+ * The coefficient formulas and evaluation order follow src/newton-cotes/rules.h:9-319 (power-basis
+ * coefficients in float, Horner at(), exact sub-range integral subrange()); every operation is an
+ * explicitly rounded FP32 operation (vmul/vadd/vsub/vdiv), where the reference promotes the outer
+ * Horner steps to double.
+ *
+ * Nested error (src/nested/nested.h:25-33): the error metric of the two rule values H(p), L(p)
+ * decides every split, so the rule values are reproduced exactly as the reference rounds them
+ * (RefRule below), without the FP64 pipe (GB300's FP64 rate is 1/64 of FP32).
+ */
+#pragma once
+#include "../../include/vcu_integrands.h"
+#include "vcu_refrule.h"
+
+namespace vcu {
+
+template <int S> struct Rule;
+
+template <> struct Rule<2> { /* trapezoidal */
+    static __device__ __forceinline__ float rule(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
+    static __device__ __forceinline__ void coefficients(const float* p, float* c) {
+        c[0] = p[0];
+        c[1] = vsub(p[1], p[0]);
+    }
+    static __device__ __forceinline__ float at(float t, const float* p) {
+        float c[2];
+        coefficients(p, c);
+        return vadd(vmul(c[1], t), c[0]);
+    }
+    static __device__ __forceinline__ float horner_int(const float* c, float t) {
+        return vmul(vadd(vdiv(vmul(c[1], t), 2.0f), c[0]), t);
+    }
+    static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
+        float c[2];
+        coefficients(p, c);
+        return vsub(horner_int(c, b), horner_int(c, a));
+    }
+};
+
+template <> struct Rule<3> { /* simpson */
+    static __device__ __forceinline__ float rule(const float* p) {
+        return vdiv(vadd(vadd(p[0], vmul(4.0f, p[1])), p[2]), 6.0f);
+    }
+    static __device__ __forceinline__ void coefficients(const float* p, float* c) {
+        c[0] = p[0];
+        c[1] = vsub(vadd(vmul(-3.0f, p[0]), vmul(4.0f, p[1])), p[2]);
+        c[2] = vadd(vsub(vmul(2.0f, p[0]), vmul(4.0f, p[1])), vmul(2.0f, p[2]));
+    }
+    static __device__ __forceinline__ float at(float t, const float* p) {
+        float c[3];
+        coefficients(p, c);
+        return vadd(vmul(vadd(vmul(c[2], t), c[1]), t), c[0]);
+    }
+    static __device__ __forceinline__ float horner_int(const float* c, float t) {
+        float r = vadd(vdiv(vmul(c[2], t), 3.0f), vdiv(c[1], 2.0f));
+        r = vadd(vmul(r, t), c[0]);
+        return vmul(r, t);
+    }
+    static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
+        float c[3];
+        coefficients(p, c);
+        return vsub(horner_int(c, b), horner_int(c, a));
+    }
+};
+
+template <> struct Rule<5> { /* boole */
+    static __device__ __forceinline__ float rule(const float* p) {
+        const float s = vadd(vadd(vmul(7.0f, vadd(p[0], p[4])), vmul(32.0f, vadd(p[1], p[3]))), vmul(12.0f, p[2]));
+        return vdiv(s, 90.0f);
+    }
+    static __device__ __forceinline__ void coefficients(const float* p, float* c) {
+        c[0] = p[0];
+        c[1] = vsub(vadd(vsub(vadd(vdiv(vmul(-25.0f, p[0]), 3.0f), vmul(16.0f, p[1])), vmul(12.0f, p[2])),
+                         vdiv(vmul(16.0f, p[3]), 3.0f)),
+                    p[4]);
+        c[2] = vadd(vsub(vadd(vsub(vdiv(vmul(70.0f, p[0]), 3.0f), vdiv(vmul(208.0f, p[1]), 3.0f)), vmul(76.0f, p[2])),
+                         vdiv(vmul(112.0f, p[3]), 3.0f)),
+                    vdiv(vmul(22.0f, p[4]), 3.0f));
+        c[3] = vsub(vadd(vsub(vadd(vdiv(vmul(-80.0f, p[0]), 3.0f), vmul(96.0f, p[1])), vmul(128.0f, p[2])),
+                         vdiv(vmul(224.0f, p[3]), 3.0f)),
+                    vmul(16.0f, p[4]));
+        c[4] = vadd(vsub(vadd(vsub(vdiv(vmul(32.0f, p[0]), 3.0f), vdiv(vmul(128.0f, p[1]), 3.0f)), vmul(64.0f, p[2])),
+                         vdiv(vmul(128.0f, p[3]), 3.0f)),
+                    vdiv(vmul(32.0f, p[4]), 3.0f));
+    }
+    static __device__ __forceinline__ float at(float t, const float* p) {
+        float c[5];
+        coefficients(p, c);
+        float r = vadd(vmul(c[4], t), c[3]);
+        r = vadd(vmul(r, t), c[2]);
+        r = vadd(vmul(r, t), c[1]);
+        return vadd(vmul(r, t), c[0]);
+    }
+    static __device__ __forceinline__ float horner_int(const float* c, float t) {
+        float r = vadd(vdiv(vmul(c[4], t), 5.0f), vdiv(c[3], 4.0f));
+        r = vadd(vmul(r, t), vdiv(c[2], 3.0f));
+        r = vadd(vmul(r, t), vdiv(c[1], 2.0f));
+        r = vadd(vmul(r, t), c[0]);
+        return vmul(r, t);
+    }
+    static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
+        float c[5];
+        coefficients(p, c);
+        return vsub(horner_int(c, b), horner_int(c, a));
+    }
+};
+
+/* error metrics (src/nested/error-metric.h): absolute |L-H|, relative |L-H|/max(|H|,|L|) unless
+ * max(|H|,|L|) < min_val */
+__device__ __forceinline__ float metric_value(int relative, float min_val, float H, float L) {
+    const float ad = vabs(vsub(L, H));
+    if (!relative) return ad;
+    const float aH = vabs(H), aL = vabs(L);
+    const float m = (aH < aL) ? aL : aH;
+    return (m < min_val) ? ad : vdiv(ad, m);
+}
+
+/* exact node coordinate float(p*w + m) with p a dyadic fraction, computed as the reference does
+ * it in double (src/newton-cotes/region.h:39-47) */
+__device__ __forceinline__ float node_coord(double p, float w, float m) {
+    return __double2float_rn(__dadd_rn(__dmul_rn(p, (double)w), (double)m));
+}
+
+/* std::max / std::min semantics: (a < b) ? b : a */
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+
+}  // namespace vcu
