@@ -142,6 +142,27 @@ int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_ne
                                 uint64_t iterations, float* bins, int32_t* trace,
                                 vcu_stats* stats);
 
+/* ------------------------------------------------------------------ allocation-free variant
+ * No counterpart in the reference.  For host programs that must not allocate device memory -- a
+ * plugin inside a process whose GPU memory belongs to another allocator, code running while the
+ * caller builds a CUDA graph, or a service with a fixed memory budget -- this runs the same per-bin
+ * adaptive nested quadrature as vcu_per_bin_adaptive_nested without a context and without any
+ * cudaMalloc/cudaFree or allocating library call.  Its device scratch is a fixed array compiled
+ * into the library (the status word plus a staging area of VCU_STATIC_MAX_BIN_VALUES floats for
+ * host-memory bins, about 4 MiB), held by every GPU that loads the library until the process exits.
+ *   - p->mem == VCU_MEM_HOST: bins is a host buffer, staged through the array; at most
+ *     VCU_STATIC_MAX_BIN_VALUES bins x channels, larger requests return VCU_UNSUPPORTED.
+ *     p->mem == VCU_MEM_DEVICE: bins is the caller's device buffer (no size limit).
+ *   - Runs on the current device and on `stream` (a cudaStream_t, NULL = legacy default stream),
+ *     and returns after the results are written.  Returns VCU_NAN_DETECTED if a bin is NaN.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress); make
+ *     that first call before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU race and must be serialised.
+ *   - No trace, no stats, no message: only the status code. */
+#define VCU_STATIC_MAX_BIN_VALUES (1u << 20)
+int vcu_per_bin_adaptive_nested_static(const vcu_problem* p, const vcu_nested* nested,
+                                       uint64_t iterations, float* bins, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
