@@ -79,6 +79,13 @@ VCU_HD float vabs(float a) {
     return std::fabs(a);
 #endif
 }
+VCU_HD uint32_t float_to_bits(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u; std::memcpy(&u, &f, 4); return u;
+#endif
+}
 VCU_HD float bits_to_float(uint32_t u) {
 #if defined(__CUDA_ARCH__)
     return __uint_as_float(u);
@@ -115,7 +122,10 @@ constexpr float kInvFact10 = 2.755731998149713e-07f;
 VCU_HD float vexp(float x) {
     if (!(x > -87.0f)) return (x != x) ? x : 0.0f;
     if (x > 88.5f) return bits_to_float(0x7f800000u);
-    const float k = vrint(vmul(x, kLog2e));
+    /* k = rint(x log2e) by the 1.5*2^23 shift (exact round-to-nearest-even for |t| < 2^22);
+     * the integer k is the difference of the two bit patterns, no float->int conversion */
+    const float t = vadd(vmul(x, kLog2e), 12582912.0f);
+    const float k = vsub(t, 12582912.0f);
     float r = vfma(-k, kLn2Hi, x);
     r = vfma(-k, kLn2Mi, r);
     r = vfma(-k, kLn2Lo, r);
@@ -127,8 +137,8 @@ VCU_HD float vexp(float x) {
     p = vfma(p, r, kInvFact2);
     p = vfma(p, r, 1.0f);
     p = vfma(p, r, 1.0f);
-    /* k in [-126, 128): split 2^k in two factors so k = 128 never appears as an exponent */
-    const int ki = (int)k;
+    /* k in [-126, 128]: 2^k as two factors so k = 128 never appears as an exponent */
+    const int ki = (int)(float_to_bits(t) - 0x4B400000u);
     const int k1 = ki / 2, k2 = ki - k1;
     const float s1 = bits_to_float((uint32_t)(k1 + 127) << 23);
     const float s2 = bits_to_float((uint32_t)(k2 + 127) << 23);
@@ -265,7 +275,7 @@ struct Scene2 {
             const float dx = vsub(x, d[i][0]);
             const float dy = vsub(y, d[i][1]);
             const float r2 = vfma(dx, dx, vmul(dy, dy));
-            if (r2 <= d[i][2]) acc = vadd(acc, d[i][3]);
+            acc = vadd(acc, (r2 <= d[i][2]) ? d[i][3] : 0.0f);
         }
         return acc;
     }

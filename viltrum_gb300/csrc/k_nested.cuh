@@ -20,6 +20,8 @@
  * and the bin writes.
  */
 #pragma once
+#include <cstdlib>
+
 #include "vcu_heap.h"
 #include "vcu_internal.cuh"
 #include "vcu_rules.cuh"
@@ -452,10 +454,9 @@ template <int DIM, int S> constexpr int lanes_per_bin() {
     return ((S - 1) * ipow(S, DIM - 1) <= 24) ? 4 : (((S - 1) * ipow(S, DIM - 1) <= 64) ? 8 : 32);
 }
 
-template <int DIM, int SH, int SL, class F>
-int launch(vcu_ctx* ctx, const F& f, const BinGrid& g, const vcu_nested& n, int iterations, float* d_bins,
-           int32_t* d_trace, uint32_t& launches) {
-    constexpr int G = lanes_per_bin<DIM, SH>();
+template <int DIM, int SH, int SL, int G, class F>
+int launch_g(vcu_ctx* ctx, const F& f, const BinGrid& g, const vcu_nested& n, int iterations, float* d_bins,
+             int32_t* d_trace, uint32_t& launches) {
     using Lay = Layout<DIM, SH, F::CH>;
     NcCfg cfg{};
     cfg.iters = iterations;
@@ -492,6 +493,53 @@ int launch(vcu_ctx* ctx, const F& f, const BinGrid& g, const vcu_nested& n, int 
     ++launches;
     VCU_CUDA(ctx, cudaGetLastError());
     return VCU_OK;
+}
+
+/* Lanes per bin (G) does not change any result -- every value is computed by one lane with the
+ * same arithmetic -- only occupancy and lane utilisation.  For 2-D regions three variants are built
+ * and the context's autotuner times each once on the caller's problem (first use of a
+ * configuration), then reuses the fastest.  VCU_NESTED_LANES=4|8|16 forces a variant. */
+template <int DIM, int SH, int SL, class F>
+int launch(vcu_ctx* ctx, const F& f, const BinGrid& g, const vcu_nested& n, int iterations, float* d_bins,
+           int32_t* d_trace, uint32_t& launches) {
+    if constexpr (DIM == 2 && (SH - 1) * SH <= 24) {
+        auto run = [&](int G) -> int {
+            switch (G) {
+            case 4: return launch_g<DIM, SH, SL, 4>(ctx, f, g, n, iterations, d_bins, d_trace, launches);
+            case 16: return launch_g<DIM, SH, SL, 16>(ctx, f, g, n, iterations, d_bins, d_trace, launches);
+            default: return launch_g<DIM, SH, SL, 8>(ctx, f, g, n, iterations, d_bins, d_trace, launches);
+            }
+        };
+        if (const char* env = std::getenv("VCU_NESTED_LANES")) {
+            const int G = std::atoi(env);
+            if (G == 4 || G == 8 || G == 16) return run(G);
+        }
+        if (!ctx->tune || g.nbins < 4096 || d_trace) return run(8);
+        /* key: integrand functor size and arity, rules, iterations, bins (coarse) */
+        const uint64_t key = ((uint64_t)sizeof(F) << 40) ^ ((uint64_t)F::DIM << 36) ^ ((uint64_t)SH << 32) ^
+                             ((uint64_t)SL << 28) ^ ((uint64_t)iterations << 20) ^ (uint64_t)(63 - __builtin_clzll(g.nbins));
+        for (int i = 0; i < ctx->ntuned; ++i)
+            if (ctx->tuned[i].key == key) return run(ctx->tuned[i].value);
+        int best = 8;
+        float best_ms = 1e30f;
+        for (int G : {4, 8, 16}) {
+            VCU_CUDA(ctx, cudaEventRecord(ctx->ev_tune[0], ctx->stream));
+            const int rc = run(G);
+            if (rc) return rc;
+            VCU_CUDA(ctx, cudaEventRecord(ctx->ev_tune[1], ctx->stream));
+            VCU_CUDA(ctx, cudaEventSynchronize(ctx->ev_tune[1]));
+            float ms = 0.0f;
+            VCU_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev_tune[0], ctx->ev_tune[1]));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = G;
+            }
+        }
+        if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = vcu_tuned{key, best};
+        return VCU_OK; /* every timed launch wrote the same bins */
+    } else {
+        return launch_g<DIM, SH, SL, lanes_per_bin<DIM, SH>()>(ctx, f, g, n, iterations, d_bins, d_trace, launches);
+    }
 }
 
 }  // namespace nc_detail

@@ -124,6 +124,8 @@ extern "C" int vcu_create(vcu_ctx** out, const vcu_opts* opts) {
     }
     if ((e = cudaEventCreate(&ctx->ev_start)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&ctx->ev_tune[0])) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreate(&ctx->ev_tune[1])) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_status, 256)) != cudaSuccess) return bail(e);
     if ((e = cudaMemset(ctx->d_status, 0, 256)) != cudaSuccess) return bail(e);
     *out = ctx;
@@ -139,6 +141,8 @@ extern "C" int vcu_destroy(vcu_ctx* ctx) {
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    for (cudaEvent_t ev : ctx->ev_tune)
+        if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     cudaGetLastError();
     delete ctx;
@@ -269,4 +273,62 @@ extern "C" int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, c
     for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
     const uint64_t evals = (uint64_t)((double)g.nbins * (sd + (double)iterations * (S - 1) * sd1));
     return scope.end(evals, g.nbins * (iterations + 1));
+}
+
+extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested, uint64_t iterations,
+                                    const vcu_cv* cv, const float* replay, float* bins, float* approximation,
+                                    float* regions, vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    BinGrid g;
+    int rc = make_grid(ctx, p, g);
+    if (rc) return rc;
+    if (!nested || !cv || !bins) return fail(ctx, VCU_INVALID_ARG, "null nested rule, cv options or bins");
+    if (iterations >= (1ull << 23)) return fail(ctx, VCU_UNSUPPORTED, "control variates take at most 2^23-1 splits");
+    if (cv->samples_per_bin > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "samples per bin must be < 2^32");
+    if (cv->weight != VCU_CV_OPTIMIZE && cv->weight != VCU_CV_FIXED) return fail(ctx, VCU_INVALID_ARG, "unknown weight");
+    if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
+    if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    const int ch = vcu_channels(p->f.kind);
+    if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
+    CallScope scope{ctx, stats};
+    if ((rc = scope.begin())) return rc;
+    const size_t bbytes = g.nbins * ch * 4, rbytes = (iterations + 1) * 2 * p->dim * 4;
+    float *dbins = bins, *dapprox = approximation, *dregions = regions;
+    const float* dreplay = replay;
+    if (p->mem == VCU_MEM_HOST) {
+        if ((rc = ensure(ctx, ctx->out, 2 * bbytes + rbytes + 512))) return rc;
+        char* o = static_cast<char*>(ctx->out.ptr);
+        dbins = reinterpret_cast<float*>(o);
+        dapprox = approximation ? reinterpret_cast<float*>(o + ((bbytes + 255) & ~size_t(255))) : nullptr;
+        dregions = regions ? reinterpret_cast<float*>(o + 2 * ((bbytes + 255) & ~size_t(255))) : nullptr;
+        if (replay) {
+            const size_t pbytes = g.nbins * cv->samples_per_bin * (1 + p->dim) * 4;
+            if ((rc = ensure(ctx, ctx->in, pbytes))) return rc;
+            VCU_CUDA(ctx, cudaMemcpyAsync(ctx->in.ptr, replay, pbytes, cudaMemcpyHostToDevice, ctx->stream));
+            dreplay = static_cast<const float*>(ctx->in.ptr);
+        }
+    }
+    const int it = (int)iterations;
+    if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_cv_st(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_SIMPSON)
+        rc = run_cv_bs(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_cv_bt(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+    else
+        rc = fail(ctx, VCU_INVALID_ARG, "unsupported nested rule pair");
+    if (rc) return rc;
+    if (p->mem == VCU_MEM_HOST) {
+        VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (approximation) VCU_CUDA(ctx, cudaMemcpyAsync(approximation, dapprox, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (regions) VCU_CUDA(ctx, cudaMemcpyAsync(regions, dregions, rbytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    const int S = nested->rule_hi;
+    double sd = 1.0, sd1 = 1.0;
+    for (int d = 0; d < p->dim; ++d) sd *= S;
+    for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
+    const uint64_t evals = (uint64_t)(sd + (double)iterations * (S - 1) * sd1) + g.nbins * cv->samples_per_bin;
+    return scope.end(evals, iterations + 1);
 }

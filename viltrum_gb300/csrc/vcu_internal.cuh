@@ -24,8 +24,18 @@ struct vcu_buffer {
     size_t bytes = 0;
 };
 
+/* autotuner cache entry: launch configuration chosen for one kernel configuration */
+struct vcu_tuned {
+    uint64_t key;
+    int32_t value;
+};
+
 struct vcu_ctx {
     int device = 0;
+    int tune = 1;                 /* time launch-configuration candidates on first use */
+    vcu_tuned tuned[32] = {};     /* fixed-size autotuner cache (no allocation)         */
+    int ntuned = 0;
+    cudaEvent_t ev_tune[2] = {nullptr, nullptr};
     int sm_count = 0;
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
@@ -176,4 +186,13 @@ int run_nested_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vc
                   float* d_bins, int32_t* d_trace, uint32_t& launches);
 int run_eval(vcu_ctx* ctx, const vcu_integrand& f, int dim, const float* d_x, int64_t npts, float* d_out,
              uint32_t& launches);
+int run_cv_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+              const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+              uint32_t& launches);
+int run_cv_bs(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+              const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+              uint32_t& launches);
+int run_cv_bt(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+              const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+              uint32_t& launches);
 }  // namespace vcu

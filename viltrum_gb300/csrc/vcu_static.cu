@@ -65,6 +65,7 @@ extern "C" int vcu_per_bin_adaptive_nested_static(const vcu_problem* p, const vc
      * its buffers stay empty (nothing is allocated) */
     vcu_ctx ctx;
     ctx.device = device;
+    ctx.tune = 0; /* the autotuner would time extra launches: use the default configuration */
     ctx.stream = static_cast<cudaStream_t>(stream);
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return VCU_CUDA_ERROR;
