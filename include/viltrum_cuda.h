@@ -142,6 +142,33 @@ int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_ne
                                 uint64_t iterations, float* bins, int32_t* trace,
                                 vcu_stats* stats);
 
+/* ------------------------------------------------------------------ control variates
+ * Replaces integrator_region_based(regions_generator_adaptive_heap(nested(H,L), heuristic, iterations),
+ * regions_integrator_parallel_variance_reduction(rr_uniform_region(), cv_optimize_weight() or
+ * cv_fixed_weight(alpha), region_sampling_uniform(), std::mt19937(seed), samples))
+ * (src/control-variates/regions-integrator-parallel-variance-reduction.h:32-109,
+ * src/control-variates/integrator-crespo2021.h:7-22 for nested(simpson,trapezoidal) with
+ * error_heuristic_size(error_metric_relative(), 1e-5)): one max-error heap of regions over the whole
+ * range (iterations splits), per-bin lists of the regions overlapping each bin, the polynomial
+ * integral over bin n region as control variate, and `samples` residual samples per bin
+ * (region chosen uniformly, point uniform in bin n region).  The result is ASSIGNED to the bins.
+ * Residual sample j of bin b draws from Philox4x32-10 unless `replay` is given: nbins x samples x
+ * (1 + dim) floats (index of the chosen region in the bin's list, then the point), e.g. the
+ * reference's own draws.  approximation (nullable) receives the control-variate integral per bin,
+ * regions (nullable) the (iterations+1) x (min[dim], max[dim]) region ranges in heap order.  All
+ * pointers follow p->mem. */
+typedef struct vcu_cv {
+    uint64_t samples_per_bin; /* residual samples per bin (spp)                         */
+    uint64_t seed;            /* Philox key                                             */
+    int32_t weight;           /* VCU_CV_OPTIMIZE or VCU_CV_FIXED                        */
+    int32_t reserved;
+    double alpha;             /* cv_fixed_weight's alpha                                */
+} vcu_cv;
+
+int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
+                         uint64_t iterations, const vcu_cv* cv, const float* replay, float* bins,
+                         float* approximation, float* regions, vcu_stats* stats);
+
 /* ------------------------------------------------------------------ allocation-free variant
  * No counterpart in the reference.  For host programs that must not allocate device memory -- a
  * plugin inside a process whose GPU memory belongs to another allocator, code running while the

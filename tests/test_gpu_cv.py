@@ -1,0 +1,106 @@
+"""Control variates + residual Monte Carlo (crespo2021 configuration): the CUDA path against the
+reference.
+
+* Region construction is exact: the device builds the same regions in the same heap order as the
+  reference (bit-equal ranges).
+* The control-variate integral per bin (deterministic) matches the reference's within 1e-5
+  relative (floor 1e-3 of the largest bin).
+* Replaying the reference's own residual draws (chosen region index + point) gives the reference's
+  bins within 1e-5 of the scale of the combined terms (the reference sums its samples in float).
+* With Philox draws the estimator's error against the FP64 bin integrals matches the reference
+  estimator's at equal samples (mean squared error ratio in [0.7, 1.4] over seeds).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from oracle import oracle as orc
+import viltrum_gb300 as v
+from viltrum_gb300 import _lib, scenes
+
+pytestmark = pytest.mark.gpu
+CRESPO = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+
+
+def _gpu_cv(ctx, kind, params, rmin, rmax, res, iters, spp, seed, weight=0, alpha=1.0, replay=None, nested=CRESPO):
+    p = ctx.problem(kind, params, rmin, rmax, res)
+    nb = int(np.prod(res))
+    ch = 3 if kind == scenes.MOVING_SCENE3 else 1
+    dim = len(rmin)
+    out = np.empty(nb * ch, np.float32)
+    app = np.empty(nb * ch, np.float32)
+    reg = np.empty((iters + 1) * 2 * dim, np.float32)
+    rp = None if replay is None else np.ascontiguousarray(replay, np.float32)
+    st = ctx.control_variates(p, nested, iters, _lib.CvOpts(spp, seed, weight, 0, alpha), out, app, reg, rp)
+    return out.reshape(nb, ch), app.reshape(nb, ch), reg.reshape(iters + 1, 2, dim), st
+
+
+@pytest.mark.parametrize("name", golden_names("cv_"))
+def test_cv_matches_reference_golden(ctx, port, name):
+    g = load_golden(name)
+    kind, res, iters, spp, seed = int(g["kind"]), [int(r) for r in g["res"]], int(g["iterations"]), int(g["spp"]), \
+        int(g["seed"])
+    weight, alpha = int(g["weight"]), float(g["alpha"])
+    params = g.get("params")
+    ref = port.control_variates(kind, params, g["rmin"], g["rmax"], res,
+                                orc.Nested.make("simpson", "trapezoidal", "size", "relative"), iters, spp, seed,
+                                weight, alpha, replay=True, approx=True)
+    out, app, reg, st = _gpu_cv(ctx, kind, params, g["rmin"], g["rmax"], res, iters, spp, seed, weight, alpha,
+                                replay=ref["replay"])
+    # 1. the same regions, in the same heap order
+    assert np.array_equal(reg.view(np.uint32), g["out_regions"].view(np.uint32))
+    # 2. the control-variate integral
+    ra = ref["approximation"].astype(np.float64)
+    floor = 1e-3 * np.max(np.abs(ra))
+    assert np.all(np.abs(app - ra) <= 1e-5 * np.maximum(np.abs(ra), floor))
+    # 3. the residual estimator on the reference's own draws
+    rb = g["out_bins"].astype(np.float64)
+    scale = np.abs(rb) + np.abs(ra) + floor
+    err = np.abs(out - rb)
+    assert np.all(err <= 1e-5 * scale), f"max scaled err {np.max(err / scale):.3e}"
+    assert st.flags == 0
+
+
+def test_cv_statistics_against_fp64(ctx, port):
+    params = scenes.moving_scene3(7, n_gauss=16, n_disk=16)
+    res, iters, spp = [32, 32], 511, 16
+    exact = scenes.exact_bins(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, t_nodes=96)
+    gpu_sq, ref_sq = [], []
+    for seed in (1, 2, 3, 4):
+        out, app, _, _ = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, iters, spp, seed)
+        gpu_sq.append(np.mean((out - exact) ** 2))
+        ref = port.control_variates(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res,
+                                    orc.Nested.make("simpson", "trapezoidal", "size", "relative"), iters, spp, seed)
+        ref_sq.append(np.mean((ref["bins"] - exact) ** 2))
+    ratio = np.mean(gpu_sq) / np.mean(ref_sq)
+    assert 0.7 <= ratio <= 1.4, (gpu_sq, ref_sq)
+
+
+def test_cv_fullsize_crespo(ctx):
+    """512x512 bins, 2^14 regions, 64 residual samples on the moving RGB scene: deterministic,
+    finite, and far more accurate than plain Monte Carlo at the same samples."""
+    params = scenes.moving_scene3(7)
+    res = [512, 512]
+    a, app, reg, st = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, (1 << 14) - 1, 64, 3)
+    b, _, _, _ = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, (1 << 14) - 1, 64, 3)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.isfinite(a).all() and st.flags == 0
+    # regions tile the domain: their volumes sum to 1
+    vol = np.prod(reg[:, 1, :].astype(np.float64) - reg[:, 0, :], axis=1)
+    assert abs(vol.sum() - 1.0) < 1e-6
+    exact = scenes.exact_bins(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, t_nodes=64)
+    rmse_cv = scenes.bin_rmse(a, exact)
+    p = ctx.problem(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res)
+    mc = np.empty(512 * 512 * 3, np.float32)
+    ctx.per_bin_monte_carlo(p, 64, 3, mc)
+    rmse_mc = scenes.bin_rmse(mc.reshape(-1, 3), exact)
+    assert rmse_cv < 0.5 * rmse_mc, (rmse_cv, rmse_mc)
+
+
+def test_python_crespo2021_api(ctx):
+    bins = np.zeros((16, 16, 3), np.float32)
+    params = scenes.moving_scene3(7, n_gauss=8, n_disk=8)
+    v.integrate(v.integrator_crespo2021(255, 16, 3), bins, v.Integrand.moving_scene3(params), v.range_primary(3),
+                ctx=ctx)
+    out, _, _, _ = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], [16, 16], 255, 16, 3)
+    assert np.array_equal(bins.transpose(1, 0, 2).reshape(-1, 3), out)

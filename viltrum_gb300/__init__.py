@@ -31,6 +31,9 @@ __all__ = [
     "trapezoidal", "simpson", "boole", "nested", "error_metric_absolute", "error_metric_relative",
     "error_heuristic_default", "error_heuristic_size", "monte_carlo", "monte_carlo_per_bin_parallel",
     "integrator_per_bin_parallel", "integrator_adaptive_iterations", "scenes", "load",
+    "rr_uniform_region", "region_sampling_uniform", "cv_optimize_weight", "cv_fixed_weight",
+    "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction", "integrator_region_based",
+    "integrator_crespo2021",
 ]
 
 
@@ -227,6 +230,90 @@ def integrator_per_bin_parallel(inner) -> PerBinParallel:
     return PerBinParallel(inner)
 
 
+# control variates (src/control-variates/)
+@dataclass(frozen=True)
+class rr_uniform_region:  # noqa: N801  (reference name)
+    """Uniform choice of the residual's region, weight = number of regions (region-russian-roulette.h:9-28)."""
+
+
+@dataclass(frozen=True)
+class region_sampling_uniform:  # noqa: N801
+    """Uniform point in bin n region, weight = its volume (region-sampling.h:9-20)."""
+
+
+@dataclass(frozen=True)
+class cv_optimize_weight:  # noqa: N801
+    """Control-variate weight alpha = clamp(cov/var) from the samples (weight-strategy.h:171-241)."""
+    fixed = False
+    alpha = 1.0
+
+
+@dataclass(frozen=True)
+class cv_fixed_weight:  # noqa: N801
+    """Fixed control-variate weight (weight-strategy.h:7-35)."""
+    alpha: float = 1.0
+    fixed = True
+
+
+@dataclass
+class AdaptiveHeapGenerator:
+    """regions_generator_adaptive_heap(rule, heuristic, iterations) (regions-generator-adaptive-heap.h:8-51)."""
+    rule: NestedRule
+    heuristic: object
+    iterations: int
+
+
+@dataclass
+class VarianceReduction:
+    """regions_integrator_parallel_variance_reduction(rr, cv, sampling, seed, samples)."""
+    rr: object
+    cv: object
+    sampling: object
+    seed: int
+    samples: int
+
+
+@dataclass
+class RegionBased:
+    """integrator_region_based(generator, regions_integrator) (integrator-region-based.h:5-29)."""
+    generator: AdaptiveHeapGenerator
+    integrator: VarianceReduction
+
+    def integrate(self, bins, res, f, rng, logger=None, ctx=None, device_bins=False, replay=None,
+                  approximation=None, regions=None):
+        return _run_cv(self, bins, res, f, rng, logger, ctx, device_bins, replay, approximation, regions)
+
+
+def regions_generator_adaptive_heap(rule: NestedRule, heuristic, iterations: int) -> AdaptiveHeapGenerator:
+    return AdaptiveHeapGenerator(rule, heuristic, int(iterations))
+
+
+def regions_integrator_parallel_variance_reduction(rr, cv, *args) -> VarianceReduction:
+    """(rr, cv, sampling, seed, samples) or (rr, cv, samples, seed) as the reference's overloads."""
+    if len(args) == 3:
+        sampling, seed, samples = args
+    elif len(args) == 2:
+        sampling, (samples, seed) = region_sampling_uniform(), args
+    else:
+        raise TypeError("regions_integrator_parallel_variance_reduction(rr, cv, [sampling,] ...)")
+    if not isinstance(rr, rr_uniform_region) or not isinstance(sampling, region_sampling_uniform):
+        raise NotImplementedError("the CUDA control variates implement rr_uniform_region and region_sampling_uniform")
+    return VarianceReduction(rr, cv, sampling, int(seed), int(samples))
+
+
+def integrator_region_based(generator: AdaptiveHeapGenerator, integrator: VarianceReduction) -> RegionBased:
+    return RegionBased(generator, integrator)
+
+
+def integrator_crespo2021(iterations: int, spp: int, seed: int = 0) -> RegionBased:
+    """integrator_crespo2021(iterations, spp, seed) (src/control-variates/integrator-crespo2021.h:7-22)."""
+    return integrator_region_based(
+        regions_generator_adaptive_heap(nested(simpson, trapezoidal),
+                                        error_heuristic_size(error_metric_relative(), 1e-5), iterations),
+        regions_integrator_parallel_variance_reduction(rr_uniform_region(), cv_optimize_weight(),
+                                                       region_sampling_uniform(), seed, spp))
+
+
 # ------------------------------------------------------------------------------------ integrate
 def _as_integrand(f) -> Integrand:
     if isinstance(f, Integrand):
@@ -266,6 +353,34 @@ def _run(integrator, bins, res, f, rng, logger, ctx, device_bins, accumulate):
             target += vals.astype(target.dtype).reshape(target.shape)
         else:
             target[...] = vals.reshape(target.shape)
+    if logger is not None:
+        logger.log_progress(1, 1)
+    return stats
+
+
+def _run_cv(rb: RegionBased, bins, res, f, rng, logger, ctx, device_bins, replay, approximation, regions):
+    from ._lib import CvOpts
+    f = _as_integrand(f)
+    ctx = ctx or default_context()
+    res = [int(r) for r in res]
+    ch = f.channels
+    nb = int(np.prod(res))
+    if logger is not None:
+        logger.log_progress(0, 1)
+    g, vr = rb.generator, rb.integrator
+    mem = MEM_DEVICE if device_bins else MEM_HOST
+    p = Context.problem(f.kind, f.params, rng.min, rng.max, res, mem)
+    flat = (not device_bins and isinstance(bins, np.ndarray) and bins.ndim == 1 and bins.dtype == np.float32
+            and bins.size == nb * ch and bins.flags.c_contiguous)
+    out = bins if (device_bins or flat) else np.empty(nb * ch, dtype=np.float32)
+    opts = CvOpts(vr.samples, vr.seed, 1 if vr.cv.fixed else 0, 0, float(vr.cv.alpha))
+    stats = ctx.control_variates(p, _nested_struct(g.rule, g.heuristic), g.iterations, opts, out, approximation,
+                                 regions, replay)
+    if not device_bins and not flat:
+        vals = out.reshape(tuple(reversed(res)) + (ch,)).transpose(tuple(range(len(res) - 1, -1, -1)) + (len(res),))
+        if ch == 1:
+            vals = vals[..., 0]
+        bins[...] = vals.reshape(bins.shape)
     if logger is not None:
         logger.log_progress(1, 1)
     return stats

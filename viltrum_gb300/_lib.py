@@ -22,7 +22,8 @@ STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "QUEUE_OVERFLOW", 4: "DEVICE_T
 FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
 
 EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
-           "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested"]
+           "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested",
+           "vcu_control_variates"]
 
 
 class VcuError(RuntimeError):
@@ -54,6 +55,11 @@ class Stats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CvOpts(ctypes.Structure):
+    _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("weight", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double)]
 
 
 class Opts(ctypes.Structure):
@@ -88,6 +94,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                                                      ctypes.POINTER(Stats)]
         L.vcu_per_bin_adaptive_nested.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested),
                                                   ctypes.c_uint64, vp, vp, ctypes.POINTER(Stats)]
+        L.vcu_control_variates.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested), ctypes.c_uint64,
+                                           ctypes.POINTER(CvOpts), vp, vp, vp, vp, ctypes.POINTER(Stats)]
         for name in EXPORTS:
             getattr(L, name).restype = ctypes.c_int
         del f32p
@@ -195,6 +203,17 @@ class Context:
                                                         iterations, _ptr(bins), _ptr(trace), ctypes.byref(st)))
         return st
 
+
+def _cv_method(self, p: Problem, nested: Nested, iterations: int, cv: CvOpts, bins, approximation=None,
+               regions=None, replay=None) -> Stats:
+    st = Stats()
+    self.check(self.lib.vcu_control_variates(self.handle, ctypes.byref(p), ctypes.byref(nested), iterations,
+                                             ctypes.byref(cv), _ptr(replay), _ptr(bins), _ptr(approximation),
+                                             _ptr(regions), ctypes.byref(st)))
+    return st
+
+
+Context.control_variates = _cv_method
 
 _default_ctx: Context | None = None
 

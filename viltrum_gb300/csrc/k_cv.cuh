@@ -1,0 +1,846 @@
+/*
+ * k_cv.cuh -- piecewise-polynomial control variates with residual Monte Carlo on the device.
+ *
+ * Replaces integrator_region_based(regions_generator_adaptive_heap(nested(H,L), heuristic, iters),
+ * regions_integrator_parallel_variance_reduction(rr_uniform_region(), weight, region_sampling_uniform(),
+ * std::mt19937(seed), spp)) -- integrator_crespo2021 when nested = (simpson, trapezoidal) with
+ * error_heuristic_size(error_metric_relative(), 1e-5) (src/control-variates/integrator-crespo2021.h:7-22).
+ *
+ * Three stages:
+ *  1. k_cv_generate: ONE cooperative thread block builds the global region heap over the whole
+ *     range exactly as src/nested/regions-generator-adaptive-heap.h:18-45 does (same split choices:
+ *     error estimates with the reference's rounding, libstdc++ heap order).  The heap lives in shared
+ *     memory (up to ~28k regions) or global memory; node values, ranges and volumes of all
+ *     2*iters+1 regions ever built live in a global pool (region k of the pool is never moved, the
+ *     heap holds pool ids).  Splits are inherently sequential; the block evaluates each split's new
+ *     nodes and both children's error folds in parallel.
+ *  2. k_cv_count / k_cv_fill / k_cv_sort: per-bin region lists.  Every region, in heap order, is
+ *     appended to the bins pixels_in_region gives (src/newton-cotes/region.h:454-463, the 0.99 rule),
+ *     as the reference's stratification does (regions-integrator-parallel-variance-reduction.h:49-57):
+ *     count per bin, exclusive scan, fill, then sort each bin's list by heap position so the order
+ *     is the reference's sequential order.
+ *  3. k_cv_residual: one warp per bin computes the control-variate integral
+ *     sum_i prod(res) * integral over (bin n region_i) (:77-88), then the residual: sample j picks a
+ *     region uniformly (rr_uniform_region, weight n) and a uniform point in bin n region (weight
+ *     volume), pushes f*w and g*w (g = the region polynomial, region.h:103-112) into the
+ *     cv_optimize_weight / cv_fixed_weight estimator (weight-strategy.h:7-110); moments and the final
+ *     recombination (sum_f - a*sum_g)/n + a*approximation are in FP64.  Sample j of bin b draws from
+ *     Philox4x32-10 (key = seed, counter = (j, b_lo, b_hi, 0xC0DE0000 | block)), or replays given
+ *     (chosen list index, point) records.
+ */
+#pragma once
+#include <cstdlib>
+
+#include "vcu_heap.h"
+#include "vcu_internal.cuh"
+#include "vcu_rules.cuh"
+
+namespace vcu {
+namespace cv_detail {
+
+__host__ __device__ constexpr int ipow(int b, int e) { return e <= 0 ? 1 : b * ipow(b, e - 1); }
+
+constexpr int GEN_THREADS = 256;
+constexpr int RES_WARPS = 4;
+constexpr int RES_CHUNK = 128; /* region integrals staged per warp before the ordered sum */
+
+struct GenCfg {
+    float rmin[VCU_MAX_DIM], rmax[VCU_MAX_DIM];
+    int32_t iters;
+    int32_t heap_in_smem;
+    int32_t heuristic, relative;
+    float min_val_f;
+    double size_weight, min_size;
+};
+
+template <int DIM, int S>
+__device__ __forceinline__ int node_index(int d, int J, int pos) {
+    int idx = 0, rem = J;
+#pragma unroll
+    for (int e = 0; e < DIM; ++e) {
+        if (e == d) {
+            idx += pos * ipow(S, e);
+        } else {
+            idx += (rem % S) * ipow(S, e);
+            rem /= S;
+        }
+    }
+    return idx;
+}
+
+/* ---------------------------------------------------------------- stage 1: global region heap */
+template <class F, int DIM, int SH, int SL>
+__global__ void __launch_bounds__(GEN_THREADS, 1)
+    k_cv_generate(const __grid_constant__ F f, const GenCfg cfg, float* __restrict__ vals, float* __restrict__ rmin,
+                  float* __restrict__ rmax, float* __restrict__ vol, float* __restrict__ heap_key,
+                  int* __restrict__ heap_pay, uint32_t* __restrict__ status) {
+    constexpr int S = SH;
+    constexpr int CH = F::CH;
+    constexpr int SD = ipow(S, DIM);
+    constexpr int NL = ipow(S, DIM - 1);
+    constexpr int NNEW = (S - 1) * NL;
+    extern __shared__ float smem[];
+    __shared__ float CO[DIM * S], CN[S - 1];
+    __shared__ float LN[2 * DIM * NL];
+    __shared__ float EC[2 * DIM];
+    const int nheap = cfg.iters + 1;
+    float* HE = cfg.heap_in_smem ? smem : heap_key;
+    int* HS = cfg.heap_in_smem ? reinterpret_cast<int*>(smem + nheap) : heap_pay;
+    const int tid = threadIdx.x;
+
+    auto errors = [&](int nreg, int r0, int r1) {
+        for (int t = tid; t < nreg * DIM * NL; t += GEN_THREADS) {
+            const int r = t / (DIM * NL), rr = t % (DIM * NL);
+            const int d = rr / NL, J = rr % NL;
+            const float* RV = vals + (size_t)(r ? r1 : r0) * SD * CH;
+            float m = 0.0f;
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                float line[S], low[SL];
+#pragma unroll
+                for (int i = 0; i < S; ++i) line[i] = RV[node_index<DIM, S>(d, J, i) * CH + c];
+#pragma unroll
+                for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+                float H, L;
+                if constexpr (CH == 1) {
+                    H = RefRule<S>::scalar(line);
+                    L = RefRule<SL>::scalar(low);
+                } else {
+                    H = RefRule<S>::rgb(line);
+                    L = RefRule<SL>::rgb(low);
+                }
+                const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
+                m = (c == 0) ? mv : vadd(m, mv);
+            }
+            LN[t] = m;
+        }
+        __syncthreads();
+        for (int t = tid; t < nreg * DIM; t += GEN_THREADS) {
+            const int r = t / DIM;
+            float buf[NL];
+            for (int i = 0; i < NL; ++i) buf[i] = LN[t * NL + i];
+            int n = NL;
+            for (int level = 0; level < DIM - 1; ++level) {
+                n /= S;
+                for (int i = 0; i < n; ++i) buf[i] = RefRule<S>::scalar(buf + i * S);
+            }
+            EC[t] = vmul(vol[r ? r1 : r0], buf[0]);
+        }
+        __syncthreads();
+    };
+    auto heuristic = [&](int r, int id, float& err_out, int& dim_out) {
+        const float* e = EC + r * DIM;
+        if (cfg.heuristic == VCU_HEUR_DEFAULT) {
+            float max_err = 0.0f;
+            int max_dim = 0;
+            for (int d = 0; d < DIM; ++d)
+                if (e[d] > max_err) {
+                    max_err = e[d];
+                    max_dim = d;
+                }
+            err_out = max_err;
+            dim_out = max_dim;
+            return;
+        }
+        float w = vsub(rmax[id * DIM], rmin[id * DIM]);
+        float max_err;
+        if ((double)w < cfg.min_size || isnan(w)) max_err = 0.0f;
+        else max_err = __double2float_rn(__dadd_rn((double)e[0], __dmul_rn(cfg.size_weight, (double)fabsf(w))));
+        int max_dim = 0;
+        for (int d = 1; d < DIM; ++d) {
+            w = vsub(rmax[id * DIM + d], rmin[id * DIM + d]);
+            float err = __double2float_rn(__dadd_rn((double)e[d], __dmul_rn(cfg.size_weight, (double)fabsf(w))));
+            if ((double)w < cfg.min_size) err = 0.0f;
+            if (err >= max_err) {
+                max_err = err;
+                max_dim = d;
+            }
+        }
+        err_out = max_err;
+        dim_out = max_dim;
+    };
+
+    /* root region: the whole range (regions-generator-adaptive-heap.h:27) */
+    if (tid == 0) {
+        float v = 1.0f;
+        for (int d = 0; d < DIM; ++d) {
+            rmin[d] = cfg.rmin[d];
+            rmax[d] = cfg.rmax[d];
+            v = vmul(v, vsub(cfg.rmax[d], cfg.rmin[d]));
+        }
+        vol[0] = v;
+    }
+    for (int t = tid; t < DIM * S; t += GEN_THREADS) {
+        const int d = t / S, j = t % S;
+        CO[t] = node_coord((double)j / (double)(S - 1), vsub(cfg.rmax[d], cfg.rmin[d]), cfg.rmin[d]);
+    }
+    __syncthreads();
+    for (int t = tid; t < SD; t += GEN_THREADS) {
+        float x[F::DIM];
+        for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+        int rem = t;
+        for (int d = 0; d < DIM; ++d) {
+            x[d] = CO[d * S + rem % S];
+            rem /= S;
+        }
+        float v[CH];
+        f(x, v);
+        for (int c = 0; c < CH; ++c) vals[t * CH + c] = v[c];
+    }
+    __syncthreads();
+    errors(1, 0, 0);
+    if (tid == 0) {
+        float e;
+        int dm;
+        heuristic(0, 0, e, dm);
+        HE[0] = e;
+        HS[0] = 0 | (dm << 24);
+    }
+    for (int it = 0; it < cfg.iters; ++it) {
+        __syncthreads();
+        const int top = HS[0];
+        const int P = top & 0xffffff, dd = top >> 24;
+        const int C0 = 2 * it + 1, C1 = 2 * it + 2;
+        const float* pmin = rmin + (size_t)P * DIM;
+        const float* pmax = rmax + (size_t)P * DIM;
+        for (int t = tid; t < DIM * S + (S - 1); t += GEN_THREADS) {
+            if (t < DIM * S) {
+                const int d = t / S, j = t % S;
+                CO[t] = node_coord((double)j / (double)(S - 1), vsub(pmax[d], pmin[d]), pmin[d]);
+            } else {
+                const int k = t - DIM * S;
+                CN[k] = node_coord((double)(2 * k + 1) / (double)(2 * (S - 1)), vsub(pmax[dd], pmin[dd]), pmin[dd]);
+            }
+        }
+        __syncthreads();
+        const float* VP = vals + (size_t)P * SD * CH;
+        float* V0 = vals + (size_t)C0 * SD * CH;
+        float* V1 = vals + (size_t)C1 * SD * CH;
+        for (int t = tid; t < NNEW + S * NL; t += GEN_THREADS) {
+            if (t < NNEW) {
+                const int k = t / NL, J = t % NL;
+                float x[F::DIM];
+                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+                int rem = J;
+                for (int e = 0; e < DIM; ++e) {
+                    if (e == dd) continue;
+                    x[e] = CO[e * S + rem % S];
+                    rem /= S;
+                }
+                x[dd] = CN[k];
+                float v[CH];
+                f(x, v);
+                const int i = 2 * k + 1;
+                if (i <= S - 1) {
+                    const int n0 = node_index<DIM, S>(dd, J, i);
+                    for (int c = 0; c < CH; ++c) V0[n0 * CH + c] = v[c];
+                }
+                if (i >= S - 1) {
+                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
+                    for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = v[c];
+                }
+            } else {
+                const int u = t - NNEW;
+                const int m = u / NL, J = u % NL;
+                const int i = 2 * m;
+                const int src = node_index<DIM, S>(dd, J, m);
+                if (i <= S - 1) {
+                    const int n0 = node_index<DIM, S>(dd, J, i);
+                    for (int c = 0; c < CH; ++c) V0[n0 * CH + c] = VP[src * CH + c];
+                }
+                if (i >= S - 1) {
+                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
+                    for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = VP[src * CH + c];
+                }
+            }
+        }
+        if (tid == 0) {
+            const float pmn = pmin[dd], pmx = pmax[dd];
+            const float half = vdiv(vsub(pmx, pmn), 2.0f);
+            const float mid = vadd(pmn, vmul(half, 1.0f));
+            float v0 = 1.0f, v1 = 1.0f;
+            for (int d = 0; d < DIM; ++d) {
+                const float mn = pmin[d], mx = pmax[d];
+                const float mx0 = (d == dd) ? mid : mx;
+                const float mn1 = (d == dd) ? mid : mn;
+                rmin[(size_t)C0 * DIM + d] = mn;
+                rmax[(size_t)C0 * DIM + d] = mx0;
+                rmin[(size_t)C1 * DIM + d] = mn1;
+                rmax[(size_t)C1 * DIM + d] = mx;
+                v0 = vmul(v0, vsub(mx0, mn));
+                v1 = vmul(v1, vsub(mx, mn1));
+            }
+            vol[C0] = v0;
+            vol[C1] = v1;
+        }
+        __syncthreads();
+        errors(2, C0, C1);
+        if (tid == 0) {
+            float e0, e1;
+            int d0, d1;
+            heuristic(0, C0, e0, d0);
+            heuristic(1, C1, e1, d1);
+            const int n = it + 1;
+            heap_pop(HE, HS, n);
+            HE[n - 1] = e0;
+            HS[n - 1] = C0 | (d0 << 24);
+            heap_push(HE, HS, n);
+            HE[n] = e1;
+            HS[n] = C1 | (d1 << 24);
+            heap_push(HE, HS, n + 1);
+        }
+    }
+    __syncthreads();
+    if (cfg.heap_in_smem)
+        for (int t = tid; t < nheap; t += GEN_THREADS) {
+            heap_key[t] = HE[t];
+            heap_pay[t] = HS[t];
+        }
+}
+
+/* ---------------------------------------------------------------- stage 2: per-bin lists */
+struct ListCfg {
+    float rmin[VCU_MAX_DIMBINS], rmax[VCU_MAX_DIMBINS];
+    uint32_t res[VCU_MAX_DIMBINS];
+    int32_t dim, dimbins, nheap;
+};
+
+/* bins [st, en) a region covers along the binned dims (pixels_in_region, region.h:454-463) */
+__device__ __forceinline__ void region_bins(const ListCfg& c, const float* rmn, const float* rmx, uint32_t* st,
+                                            uint32_t* en) {
+    for (int i = 0; i < c.dimbins; ++i) {
+        const float w = vsub(c.rmax[i], c.rmin[i]);
+        const float a = vdiv(vmul((float)c.res[i], vsub(rmn[i], c.rmin[i])), w);
+        const float b = vadd(0.99f, vdiv(vmul((float)c.res[i], vsub(rmx[i], c.rmin[i])), w));
+        const uint32_t s = a > 0.0f ? (uint32_t)a : 0u;
+        uint32_t e = b > 0.0f ? (uint32_t)b : 0u;
+        if (e > c.res[i]) e = c.res[i];
+        if (e < s + 1) e = s + 1;
+        st[i] = s;
+        en[i] = e;
+    }
+}
+
+/* one warp per heap position: count (mode 0) or fill (mode 1) the bins of its region */
+static __global__ void k_cv_lists(const ListCfg c, const int* __restrict__ heap_pay, const float* __restrict__ rmin,
+                           const float* __restrict__ rmax, uint32_t* __restrict__ counts,
+                           const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursor,
+                           uint32_t* __restrict__ lists, int mode) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= c.nheap) return;
+    const int id = heap_pay[warp] & 0xffffff;
+    uint32_t st[VCU_MAX_DIMBINS], en[VCU_MAX_DIMBINS];
+    region_bins(c, rmin + (size_t)id * c.dim, rmax + (size_t)id * c.dim, st, en);
+    uint64_t area = 1;
+    for (int i = 0; i < c.dimbins; ++i) area *= (en[i] - st[i]);
+    for (uint64_t q = lane; q < area; q += 32) {
+        uint64_t rem = q, bin = 0, mul = 1;
+        for (int i = 0; i < c.dimbins; ++i) {
+            const uint32_t ext = en[i] - st[i];
+            bin += (st[i] + rem % ext) * mul;
+            rem /= ext;
+            mul *= c.res[i];
+        }
+        if (mode == 0) atomicAdd(&counts[bin], 1u);
+        else lists[offsets[bin] + atomicAdd(&cursor[bin], 1u)] = (uint32_t)warp;
+    }
+}
+
+/* exclusive scan of the bin counts by one block (counts are small; nbins up to ~1e7) */
+static __global__ void k_cv_scan(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets, uint64_t n,
+                          uint32_t* __restrict__ status) {
+    __shared__ uint64_t part[1024];
+    const int tid = threadIdx.x;
+    const uint64_t per = (n + 1023) / 1024;
+    const uint64_t a = tid * per, b = (a + per < n) ? a + per : n;
+    uint64_t s = 0;
+    for (uint64_t i = a; i < b; ++i) s += counts[i];
+    part[tid] = s;
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t acc = 0;
+        for (int i = 0; i < 1024; ++i) {
+            const uint64_t v = part[i];
+            part[i] = acc;
+            acc += v;
+        }
+        if (acc > 0xffffffffull) atomicOr(status, VCU_FLAG_OVERFLOW);
+        offsets[n] = (uint32_t)acc;
+    }
+    __syncthreads();
+    uint64_t acc = part[tid];
+    for (uint64_t i = a; i < b; ++i) {
+        offsets[i] = (uint32_t)acc;
+        acc += counts[i];
+    }
+}
+
+/* sort each bin's list by heap position (rank sort by one warp per bin) */
+static __global__ void k_cv_sort(const uint32_t* __restrict__ offsets, const uint32_t* __restrict__ in,
+                          uint32_t* __restrict__ out, uint64_t nbins) {
+    const uint64_t bin = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (bin >= nbins) return;
+    const uint32_t a = offsets[bin], n = offsets[bin + 1] - a;
+    for (uint32_t i = lane; i < n; i += 32) {
+        const uint32_t v = in[a + i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < n; ++j) rank += (in[a + j] < v) ? 1u : 0u;
+        out[a + rank] = v;
+    }
+}
+
+/* ---------------------------------------------------------------- stage 3: CV integral + residual */
+struct ResCfg {
+    float rmin[VCU_MAX_DIM], rmax[VCU_MAX_DIM];
+    float drange[VCU_MAX_DIMBINS];
+    uint32_t res[VCU_MAX_DIMBINS];
+    int32_t dimbins;
+    uint64_t nbins;
+    double factor; /* prod(res) */
+    uint64_t spp;
+    uint32_t k0, k1;
+    int32_t weight; /* VCU_CV_OPTIMIZE / VCU_CV_FIXED */
+    double alpha;
+};
+
+template <int DIM, int S, int CH>
+__device__ float poly_subrange(const float* V, int c, const float* A, const float* B) {
+    constexpr int SD = ipow(S, DIM);
+    constexpr int inner = SD / S;
+    float buf[inner > 0 ? inner : 1];
+    for (int i = 0; i < inner; ++i) {
+        float line[S];
+#pragma unroll
+        for (int j = 0; j < S; ++j) line[j] = V[(i + j * inner) * CH + c];
+        buf[i] = Rule<S>::subrange(A[DIM - 1], B[DIM - 1], line);
+    }
+    int n = inner;
+    for (int d = DIM - 2; d >= 0; --d) {
+        const int m = n / S;
+        for (int i = 0; i < m; ++i) {
+            float line[S];
+#pragma unroll
+            for (int j = 0; j < S; ++j) line[j] = buf[i + j * m];
+            buf[i] = Rule<S>::subrange(A[d], B[d], line);
+        }
+        n = m;
+    }
+    return buf[0];
+}
+
+/* the region polynomial at normalised position p, folding dimension 0 first (region.h:86-112) */
+template <int DIM, int S, int CH>
+__device__ float poly_at(const float* V, int c, const float* p) {
+    constexpr int SD = ipow(S, DIM);
+    float buf[SD / S > 0 ? SD / S : 1];
+    int n = SD / S;
+    for (int i = 0; i < n; ++i) {
+        float line[S];
+#pragma unroll
+        for (int j = 0; j < S; ++j) line[j] = V[(i * S + j) * CH + c];
+        buf[i] = Rule<S>::at(p[0], line);
+    }
+    for (int d = 1; d < DIM; ++d) {
+        const int m = n / S;
+        for (int i = 0; i < m; ++i) {
+            float line[S];
+#pragma unroll
+            for (int j = 0; j < S; ++j) line[j] = buf[i * S + j];
+            buf[i] = Rule<S>::at(p[d], line);
+        }
+        n = m;
+    }
+    return vmul(buf[0], 1.0f);
+}
+
+__device__ __forceinline__ float norm1(const float* v, int ch) {
+    float s = vabs(v[0]);
+    for (int c = 1; c < ch; ++c) s = vadd(s, vabs(v[c]));
+    return s;
+}
+
+template <class F, int DIM, int S>
+__global__ void __launch_bounds__(RES_WARPS * 32)
+    k_cv_residual(const __grid_constant__ F f, const ResCfg cfg, const uint32_t* __restrict__ offsets,
+                  const uint32_t* __restrict__ lists, const int* __restrict__ heap_pay, const float* __restrict__ vals,
+                  const float* __restrict__ rmin, const float* __restrict__ rmax, const float* __restrict__ rvol,
+                  const float* __restrict__ replay, float* __restrict__ bins, float* __restrict__ approx_out,
+                  uint32_t* __restrict__ status) {
+    constexpr int CH = F::CH;
+    constexpr int SD = ipow(S, DIM);
+    __shared__ float stage[RES_WARPS][RES_CHUNK][CH];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t bin = (uint64_t)blockIdx.x * RES_WARPS + warp;
+    if (bin >= cfg.nbins) return;
+    /* bin range (regions-integrator-parallel-variance-reduction.h:71-73) */
+    float bmin[DIM], bmax[DIM];
+    {
+        uint64_t rem = bin;
+        for (int d = 0; d < DIM; ++d) {
+            bmin[d] = cfg.rmin[d];
+            bmax[d] = cfg.rmax[d];
+            if (d < cfg.dimbins) {
+                const uint32_t pos = (uint32_t)(rem % cfg.res[d]);
+                rem /= cfg.res[d];
+                bmin[d] = vadd(cfg.rmin[d], vmul((float)pos, cfg.drange[d]));
+                bmax[d] = vadd(cfg.rmin[d], vmul((float)(pos + 1), cfg.drange[d]));
+            }
+        }
+    }
+    const uint32_t off = offsets[bin];
+    const uint32_t n = offsets[bin + 1] - off;
+    /* intersection bin n region (range.h:405-414) and its normalised bounds in the region */
+    auto isect = [&](int id, float* a, float* b, float* A, float* B, float& v, bool& empty) {
+        empty = false;
+        v = 1.0f;
+        for (int d = 0; d < DIM; ++d) {
+            const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
+            a[d] = smax(bmin[d], rmn);
+            b[d] = smax(a[d], smin(bmax[d], rmx));
+            empty = empty || (a[d] >= b[d]);
+            v = vmul(v, vsub(b[d], a[d]));
+            A[d] = (rmn >= rmx) ? rmn : vdiv(vsub(a[d], rmn), vsub(rmx, rmn));
+            B[d] = (rmn >= rmx) ? rmn : vdiv(vsub(b[d], rmn), vsub(rmx, rmn));
+        }
+    };
+    /* control-variate integral, summed in list order as the reference does */
+    float approx[CH];
+    double approx_d[CH];
+    for (int c = 0; c < CH; ++c) approx[c] = 0.0f;
+    for (uint32_t base = 0; base < n; base += RES_CHUNK) {
+        const uint32_t m = (n - base < RES_CHUNK) ? n - base : RES_CHUNK;
+        for (uint32_t i = lane; i < m; i += 32) {
+            const int id = heap_pay[lists[off + base + i]] & 0xffffff;
+            float a[DIM], b[DIM], A[DIM], B[DIM], v;
+            bool empty;
+            isect(id, a, b, A, B, v, empty);
+            for (int c = 0; c < CH; ++c)
+                stage[warp][i][c] = empty ? __int_as_float(0x7fc00001)
+                                          : vmul(rvol[id], poly_subrange<DIM, S, CH>(vals + (size_t)id * SD * CH, c, A, B));
+        }
+        __syncwarp();
+        if (lane == 0)
+            for (uint32_t i = 0; i < m; ++i) {
+                if (__float_as_int(stage[warp][i][0]) == 0x7fc00001) continue;
+                for (int c = 0; c < CH; ++c) {
+                    if (CH == 1) /* float += double(factor) * float */
+                        approx[c] = __double2float_rn((double)approx[c] + cfg.factor * (double)stage[warp][i][c]);
+                    else /* 3-channel value type: double scale rounded per channel, then float add */
+                        approx[c] = vadd(approx[c], __double2float_rn(cfg.factor * (double)stage[warp][i][c]));
+                }
+            }
+        __syncwarp();
+    }
+    for (int c = 0; c < CH; ++c) {
+        approx[c] = __shfl_sync(0xffffffffu, approx[c], 0);
+        approx_d[c] = (double)approx[c];
+    }
+    /* residual samples */
+    double sf[CH], sa[CH];
+    for (int c = 0; c < CH; ++c) sf[c] = sa[c] = 0.0;
+    /* covariance moments of the sample norms (weight-strategy.h:187-208): Welford per lane,
+     * merged across lanes with Chan's pairwise formulas -- stable, like the reference's shifted sums */
+    double wn = 0.0, mf = 0.0, ma = 0.0, m2a = 0.0, cfa = 0.0;
+    const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
+    for (uint64_t j = lane; j < cfg.spp && n > 0; j += 32) {
+        uint32_t chosen;
+        float x[F::DIM];
+        for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+        float a[DIM], b[DIM], A[DIM], B[DIM], v;
+        bool empty;
+        if (replay) {
+            const float* rec = replay + (bin * cfg.spp + j) * (1 + DIM);
+            chosen = (uint32_t)rec[0];
+            if (chosen >= n) {
+                atomicOr(status, VCU_FLAG_OVERFLOW);
+                chosen = n - 1;
+            }
+            const int id = heap_pay[lists[off + chosen]] & 0xffffff;
+            isect(id, a, b, A, B, v, empty);
+            for (int d = 0; d < DIM; ++d) x[d] = rec[1 + d];
+        } else {
+            const U4 r0 = philox4x32_10(U4{(uint32_t)j, blo, bhi, 0xC0DE0000u}, cfg.k0, cfg.k1);
+            chosen = (uint32_t)(((uint64_t)r0.x * n) >> 32); /* uniform index in [0, n) */
+            const int id = heap_pay[lists[off + chosen]] & 0xffffff;
+            isect(id, a, b, A, B, v, empty);
+            const uint32_t rr[3] = {r0.y, r0.z, r0.w};
+            for (int d = 0; d < DIM; ++d) {
+                uint32_t bits;
+                if (d < 3) bits = rr[d];
+                else {
+                    const U4 r1 = philox4x32_10(U4{(uint32_t)j, blo, bhi, 0xC0DE0001u + (uint32_t)((d - 3) / 4)},
+                                                cfg.k0, cfg.k1);
+                    const uint32_t q[4] = {r1.x, r1.y, r1.z, r1.w};
+                    bits = q[(d - 3) % 4];
+                }
+                x[d] = vadd(vmul(u01(bits), vsub(b[d], a[d])), a[d]);
+            }
+        }
+        const int id = heap_pay[lists[off + chosen]] & 0xffffff;
+        float fv[CH], gv[CH], p[DIM];
+        f(x, fv);
+        for (int d = 0; d < DIM; ++d) {
+            const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
+            p[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));
+        }
+        for (int c = 0; c < CH; ++c) gv[c] = poly_at<DIM, S, CH>(vals + (size_t)id * SD * CH, c, p);
+        /* sample weights: prod(res) * n (russian roulette) * volume(bin n region) */
+        float fs[CH], as[CH];
+        for (int c = 0; c < CH; ++c) {
+            if (CH == 1) {
+                fs[c] = __double2float_rn((double)fv[c] * cfg.factor * (double)n * (double)v);
+                as[c] = __double2float_rn((double)gv[c] * cfg.factor * (double)n * (double)v);
+            } else {
+                fs[c] = vmul(vmul(__double2float_rn((double)fv[c] * cfg.factor), (float)n), v);
+                as[c] = vmul(vmul(__double2float_rn((double)gv[c] * cfg.factor), (float)n), v);
+            }
+            sf[c] += (double)fs[c];
+            sa[c] += (double)as[c];
+        }
+        const double nf = (double)norm1(fs, CH), na = (double)norm1(as, CH);
+        wn += 1.0;
+        const double df = nf - mf;
+        mf += df / wn;
+        const double da = na - ma;
+        ma += da / wn;
+        const double da2 = na - ma;
+        m2a += da * da2;
+        cfa += df * da2;
+    }
+    for (int off2 = 16; off2 > 0; off2 >>= 1) {
+        for (int c = 0; c < CH; ++c) {
+            sf[c] += __shfl_down_sync(0xffffffffu, sf[c], off2);
+            sa[c] += __shfl_down_sync(0xffffffffu, sa[c], off2);
+        }
+        const double nb = __shfl_down_sync(0xffffffffu, wn, off2);
+        const double mfb = __shfl_down_sync(0xffffffffu, mf, off2);
+        const double mab = __shfl_down_sync(0xffffffffu, ma, off2);
+        const double m2b = __shfl_down_sync(0xffffffffu, m2a, off2);
+        const double cb = __shfl_down_sync(0xffffffffu, cfa, off2);
+        const double nt = wn + nb;
+        if (nb > 0.0 && nt > 0.0) {
+            const double dfm = mfb - mf, dam = mab - ma;
+            const double w = wn * nb / nt;
+            mf += dfm * nb / nt;
+            ma += dam * nb / nt;
+            m2a += m2b + dam * dam * w;
+            cfa += cb + dfm * dam * w;
+            wn = nt;
+        }
+    }
+    if (lane != 0) return;
+    const double N = (n > 0) ? (double)cfg.spp : 0.0;
+    double out[CH];
+    if (cfg.weight == VCU_CV_FIXED) {
+        for (int c = 0; c < CH; ++c)
+            out[c] = (N == 0.0) ? approx_d[c] : (sf[c] - cfg.alpha * sa[c]) / N + cfg.alpha * approx_d[c];
+    } else {
+        double alpha = 1.0;
+        if (N >= 2.0) {
+            const double cov = cfa / (N - 1.0);
+            const double var = m2a / (N - 1.0);
+            const double vv = var > 0.0 ? var : 0.0;
+            if (vv > 0.0) {
+                const double cc = cov > 0.0 ? cov : 0.0;
+                alpha = (cc < vv ? cc : vv) / vv;
+            }
+        }
+        for (int c = 0; c < CH; ++c)
+            out[c] = (N < 2.0) ? approx_d[c] : (sf[c] - alpha * sa[c]) / N + alpha * approx_d[c];
+    }
+    bool nan = false;
+    for (int c = 0; c < CH; ++c) {
+        const float o = (float)out[c];
+        nan = nan || isnan(o);
+        bins[bin * CH + c] = o;
+        if (approx_out) approx_out[bin * CH + c] = approx[c];
+    }
+    if (nan) atomicOr(status, VCU_FLAG_NAN);
+}
+
+}  // namespace cv_detail
+
+/* host driver for one rule pair */
+template <int SH, int SL>
+int run_cv_pair(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iterations,
+                const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+                uint32_t& launches);
+
+}  // namespace vcu
+
+namespace vcu {
+namespace cv_detail {
+
+static __global__ void k_cv_regions_out(const int* __restrict__ heap_pay, const float* __restrict__ rmin,
+                                 const float* __restrict__ rmax, int dim, int nheap, float* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nheap) return;
+    const int id = heap_pay[k] & 0xffffff;
+    for (int d = 0; d < dim; ++d) {
+        out[(size_t)k * 2 * dim + d] = rmin[(size_t)id * dim + d];
+        out[(size_t)k * 2 * dim + dim + d] = rmax[(size_t)id * dim + d];
+    }
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+template <int DIM, int SH, int SL, class F>
+int cv_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iters,
+              const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+              uint32_t& launches) {
+    constexpr int S = SH;
+    constexpr int CH = F::CH;
+    constexpr int SD = ipow(S, DIM);
+    const size_t npool = 2 * (size_t)iters + 1, nheap = (size_t)iters + 1;
+    /* scratch layout: region pool, heap, per-bin counts/offsets/cursors */
+    size_t o = 0;
+    const size_t o_vals = o;
+    o = align256(o + npool * SD * CH * 4);
+    const size_t o_rmin = o;
+    o = align256(o + npool * DIM * 4);
+    const size_t o_rmax = o;
+    o = align256(o + npool * DIM * 4);
+    const size_t o_vol = o;
+    o = align256(o + npool * 4);
+    const size_t o_hk = o;
+    o = align256(o + nheap * 4);
+    const size_t o_hp = o;
+    o = align256(o + nheap * 4);
+    const size_t o_cnt = o;
+    o = align256(o + g.nbins * 4);
+    const size_t o_off = o;
+    o = align256(o + (g.nbins + 1) * 4);
+    const size_t o_cur = o;
+    o = align256(o + g.nbins * 4);
+    int rc = ensure(ctx, ctx->scratch, o);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->scratch.ptr);
+    float* vals = reinterpret_cast<float*>(base + o_vals);
+    float* rmin = reinterpret_cast<float*>(base + o_rmin);
+    float* rmax = reinterpret_cast<float*>(base + o_rmax);
+    float* vol = reinterpret_cast<float*>(base + o_vol);
+    float* hk = reinterpret_cast<float*>(base + o_hk);
+    int* hp = reinterpret_cast<int*>(base + o_hp);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(base + o_cnt);
+    uint32_t* off = reinterpret_cast<uint32_t*>(base + o_off);
+    uint32_t* cur = reinterpret_cast<uint32_t*>(base + o_cur);
+
+    /* stage 1 */
+    GenCfg gc{};
+    for (int d = 0; d < DIM; ++d) {
+        gc.rmin[d] = p->range_min[d];
+        gc.rmax[d] = p->range_max[d];
+    }
+    gc.iters = iters;
+    gc.heuristic = nst.heuristic;
+    gc.relative = nst.metric == VCU_METRIC_RELATIVE;
+    float mv = (float)nst.min_val;
+    if ((double)mv < nst.min_val) mv = nextafterf(mv, INFINITY);
+    gc.min_val_f = mv;
+    gc.size_weight = nst.size_weight;
+    gc.min_size = nst.min_size;
+    auto gen = k_cv_generate<F, DIM, SH, SL>;
+    cudaFuncAttributes attr;
+    VCU_CUDA(ctx, cudaFuncGetAttributes(&attr, gen));
+    const size_t heap_bytes = nheap * 8;
+    gc.heap_in_smem = (heap_bytes + attr.sharedSizeBytes + 1024 <= ctx->smem_optin) ? 1 : 0;
+    const size_t dsmem = gc.heap_in_smem ? heap_bytes : 0;
+    if (dsmem) VCU_CUDA(ctx, cudaFuncSetAttribute(gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem));
+    gen<<<1, GEN_THREADS, dsmem, ctx->stream>>>(f, gc, vals, rmin, rmax, vol, hk, hp, ctx->d_status);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+
+    /* stage 2 */
+    ListCfg lc{};
+    for (int d = 0; d < p->dimbins; ++d) {
+        lc.rmin[d] = p->range_min[d];
+        lc.rmax[d] = p->range_max[d];
+        lc.res[d] = g.res[d];
+    }
+    lc.dim = DIM;
+    lc.dimbins = p->dimbins;
+    lc.nheap = (int)nheap;
+    VCU_CUDA(ctx, cudaMemsetAsync(cnt, 0, g.nbins * 4, ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(cur, 0, g.nbins * 4, ctx->stream));
+    const unsigned lblocks = (unsigned)((nheap * 32 + 255) / 256);
+    k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, cnt, nullptr, nullptr, nullptr, 0);
+    k_cv_scan<<<1, 1024, 0, ctx->stream>>>(cnt, off, g.nbins, ctx->d_status);
+    launches += 2;
+    VCU_CUDA(ctx, cudaGetLastError());
+    uint32_t total = 0;
+    VCU_CUDA(ctx, cudaMemcpyAsync(&total, off + g.nbins, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if ((rc = ensure(ctx, ctx->aux, (size_t)total * 8 + 512))) return rc;
+    uint32_t* lists_u = static_cast<uint32_t*>(ctx->aux.ptr);
+    uint32_t* lists = lists_u + total + 64;
+    k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, nullptr, off, cur, lists_u, 1);
+    k_cv_sort<<<(unsigned)((g.nbins * 32 + 255) / 256), 256, 0, ctx->stream>>>(off, lists_u, lists, g.nbins);
+    launches += 2;
+    VCU_CUDA(ctx, cudaGetLastError());
+
+    /* stage 3 */
+    ResCfg rcfg{};
+    for (int d = 0; d < DIM; ++d) {
+        rcfg.rmin[d] = p->range_min[d];
+        rcfg.rmax[d] = p->range_max[d];
+    }
+    for (int d = 0; d < p->dimbins; ++d) {
+        rcfg.res[d] = g.res[d];
+        rcfg.drange[d] = g.drange[d];
+    }
+    rcfg.dimbins = p->dimbins;
+    rcfg.nbins = g.nbins;
+    rcfg.factor = (double)g.factor;
+    rcfg.spp = cv.samples_per_bin;
+    rcfg.k0 = (uint32_t)cv.seed;
+    rcfg.k1 = (uint32_t)(cv.seed >> 32);
+    rcfg.weight = cv.weight;
+    rcfg.alpha = cv.alpha;
+    const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
+    k_cv_residual<F, DIM, S><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(f, rcfg, off, lists, hp, vals, rmin, rmax,
+                                                                          vol, d_replay, d_bins, d_approx,
+                                                                          ctx->d_status);
+    ++launches;
+    if (d_regions) {
+        k_cv_regions_out<<<(unsigned)((nheap + 255) / 256), 256, 0, ctx->stream>>>(hp, rmin, rmax, DIM, (int)nheap,
+                                                                                  d_regions);
+        ++launches;
+    }
+    VCU_CUDA(ctx, cudaGetLastError());
+    return VCU_OK;
+}
+
+}  // namespace cv_detail
+
+template <int SH, int SL>
+int run_cv_pair(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iterations,
+                const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+                uint32_t& launches) {
+    using cv_detail::ipow;
+    return with_integrand(ctx, p->f, p->dim, [&](const auto& f) -> int {
+        using F = std::decay_t<decltype(f)>;
+        auto by_dim = [&](auto dimc) -> int {
+            constexpr int DIM = decltype(dimc)::value;
+            if constexpr (ipow(SH, DIM) <= 243)
+                return cv_detail::cv_launch<DIM, SH, SL>(ctx, f, p, g, nst, iterations, cv, d_replay, d_bins, d_approx,
+                                                         d_regions, launches);
+            else
+                return fail(ctx, VCU_UNSUPPORTED, "control-variate regions are limited to 243 nodes (S^dim)");
+        };
+        if constexpr (F::DIM == 6) {
+            switch (p->dim) {
+            case 2: return by_dim(std::integral_constant<int, 2>{});
+            case 3: return by_dim(std::integral_constant<int, 3>{});
+            case 4: return by_dim(std::integral_constant<int, 4>{});
+            case 5: return by_dim(std::integral_constant<int, 5>{});
+            default: return fail(ctx, VCU_UNSUPPORTED, "half-space control variates are built for 2-5 dimensions");
+            }
+        } else {
+            return by_dim(std::integral_constant<int, F::DIM>{});
+        }
+    });
+}
+
+}  // namespace vcu

@@ -1,0 +1,10 @@
+/* control variates + residual Monte Carlo, rule pair (5 nodes, 2 nodes); see k_cv.cuh */
+#include "k_cv.cuh"
+
+namespace vcu {
+int run_cv_bt(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+              const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+              uint32_t& launches) {
+    return run_cv_pair<5, 2>(ctx, p, g, n, iterations, cv, d_replay, d_bins, d_approx, d_regions, launches);
+}
+}  // namespace vcu
