@@ -169,6 +169,91 @@ int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* n
                          uint64_t iterations, const vcu_cv* cv, const float* replay, float* bins,
                          float* approximation, float* regions, vcu_stats* stats);
 
+/* ------------------------------------------------------------------ learned control variate
+ * No reference counterpart: per-bin integration (the integrator_per_bin_parallel contract,
+ * src/integrator-per-bin-parallel.h:17-35, values ASSIGNED) with a small MLP control variate g --
+ * frequency encoding (6 bands), 4 hidden layers of 64, BF16 weights on the tensor cores, FP32
+ * accumulation -- trained online (Adam, mean squared error) on `batch` fresh Philox samples of the
+ * integrand per step for `train_steps` steps by the library's own forward/backward kernels.  Per
+ * bin, the integral of g is taken by Gauss-Legendre quadrature with `quad_nodes` (1..4) nodes per
+ * dimension and only f - g is Monte Carlo sampled (`samples_per_bin` Philox points); with
+ * `fallback` set, a bin keeps the plain Monte Carlo mean of the same samples when its sample
+ * variance is lower than the residual's.  Scalar integrands of dimension 2, 3 or 5.            */
+typedef struct vcu_learned {
+    uint64_t samples_per_bin;
+    uint64_t seed;
+    uint32_t train_steps;
+    uint32_t batch;           /* training samples per step (rounded up to whole blocks)        */
+    float learning_rate;
+    uint32_t quad_nodes;      /* Gauss-Legendre nodes per dimension for the integral of g, 1..4 */
+    int32_t fallback;         /* 1: per-bin fallback to plain Monte Carlo                       */
+    int32_t reserved;
+    float* theta_out;         /* nullable host buffer: receives the trained fp32 parameters
+                                 (vcu_mlp_eval layout), e.g. to checkpoint the network        */
+} vcu_learned;
+
+typedef struct vcu_learned_report {
+    double train_ms, integral_ms, residual_ms;
+    uint32_t fallback_bins;   /* bins that kept the plain Monte Carlo estimate */
+    uint32_t reserved;
+} vcu_learned_report;
+
+/* network_integral (nullable, follows p->mem): per bin, the mean of g over the bin */
+int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_learned* opt, float* bins,
+                                 float* network_integral, vcu_learned_report* report, vcu_stats* stats);
+
+/* The network alone, for checking the kernels: outputs g(u) at npts points u in [0,1]^dim (host
+ * arrays, row-major) for the fp32 parameter vector theta (layout: W0[FIN][64], b0, W1[64][64], b1,
+ * W2, b2, W3, b3, w4[64], b4 with FIN = 16*ceil(13*dim/16)); if y and grad are given, grad receives
+ * the gradient of mean((g - y)^2) computed by the training kernel.  dim 2, 3 or 5. */
+int vcu_mlp_eval(vcu_ctx* ctx, int32_t dim, const float* theta, const float* u, const float* y, int64_t npts,
+                 float* out, float* grad);
+
+/* ------------------------------------------------------------------ batched independent integrals
+ * Many calls of the reference's single-value form, viltrum::integrate(I, f, range)
+ * (src/integrate.h:105-113), each with its own dimension, range, integrand parameters, method and
+ * budget, run in one persistent launch captured in a CUDA graph.  Per item:
+ *   VCU_BATCH_MONTE_CARLO : I = monte_carlo(budget, seed) (src/monte-carlo/monte-carlo.h:39-63,
+ *                           89-95); Philox4x32-10 points keyed by (seed, sample, item position)
+ *                           replace the item's std::mt19937, so agreement is statistical;
+ *   VCU_BATCH_NESTED      : I = integrator_adaptive_iterations(nested(H,L), heuristic, budget - 1)
+ *                           (src/nested/integrator-adaptive-iterations.h:12-25): budget regions;
+ *                           the same value as the reference's.
+ * All items share the integrand family `kind` (each item has its own parameters) and, for the
+ * nested items, the rule pair / heuristic / metric of `nested` (NULL: simpson over trapezoidal,
+ * default heuristic, absolute metric).  Scalar integrands only.  Nested items are limited to
+ * S^dim <= 729 nodes per region (Simpson to 6-D, Boole to 4-D) and 2^24-2 regions. */
+enum { VCU_BATCH_MONTE_CARLO = 0, VCU_BATCH_NESTED = 1 };
+
+typedef struct vcu_batch_item {
+    int32_t dim;        /* 1..6 */
+    int32_t method;     /* VCU_BATCH_MONTE_CARLO or VCU_BATCH_NESTED */
+    uint64_t budget;    /* samples (Monte Carlo) or regions (nested), >= 1 */
+    uint64_t seed;      /* Monte Carlo stream */
+    float range_min[VCU_MAX_DIM];
+    float range_max[VCU_MAX_DIM];
+    int32_t n_params;   /* this item's integrand parameters (host array) */
+    int32_t reserved;
+    const float* params;
+} vcu_batch_item;
+
+typedef struct vcu_batch_report {
+    float* item_ms;       /* nullable host array [n_items]: each item's time on the device */
+    int32_t threads;      /* block size the autotuner chose */
+    uint32_t blocks;      /* resident blocks of the persistent launch */
+    uint64_t nested_regions;
+} vcu_batch_report;
+
+/* results[n_items] (host or device per results_mem): item i's integral, in item order.
+ * report and stats are nullable. */
+int vcu_integrate_batch(vcu_ctx* ctx, int32_t kind, const vcu_nested* nested, const vcu_batch_item* items,
+                        uint64_t n_items, float* results, int32_t results_mem, vcu_batch_report* report,
+                        vcu_stats* stats);
+/* Runs the batch last passed to vcu_integrate_batch on this context again from the copies already in
+ * device memory (no host->device traffic): for repeated evaluation of a fixed batch. */
+int vcu_integrate_batch_resident(vcu_ctx* ctx, float* results, int32_t results_mem, vcu_batch_report* report,
+                                 vcu_stats* stats);
+
 /* ------------------------------------------------------------------ allocation-free variant
  * No counterpart in the reference.  For host programs that must not allocate device memory -- a
  * plugin inside a process whose GPU memory belongs to another allocator, code running while the

@@ -533,6 +533,43 @@ void per_bin_nested_range(const Fun& fun, const Problem& p, const orc_nested& nc
     }
 }
 
+/* ------------------------------------------------------------------ single-value integrals */
+/* monte_carlo(budget, seed) through integrate(I, f, range): one bin of resolution {1}, the
+ * integrator's own std::mt19937(seed) (moved in, not reseeded), bins(pos) += f(x) * factor */
+template <int DIM, class Fun>
+float single_mc(const Fun& fun, const Range<DIM>& range, uint64_t budget, uint64_t seed) {
+    Fn<Fun, DIM, float> f{&fun};
+    std::mt19937 rng(seed);
+    const double factor = double(1) * range.volume() / double(budget);
+    float sol = 0.0f;
+    for (uint64_t s = 0; s < budget; ++s) {
+        std::array<float, DIM> x;
+        for (int i = 0; i < DIM; ++i) {
+            std::uniform_real_distribution<float> dis(range.min(i), range.max(i));
+            x[i] = dis(rng);
+        }
+        bool inside = true;
+        for (int i = 0; (i < DIM) && inside; ++i) inside = (x[i] >= range.min(i)) && (x[i] <= range.max(i));
+        if (inside) sol += f(x) * factor;
+    }
+    return sol;
+}
+
+/* integrator_adaptive_iterations(nested(H,L), heuristic, iters) through integrate(I, f, range) */
+template <class H, class L, int DIM, class Fun, class M>
+float single_nested(const Fun& fun, const Range<DIM>& range, const orc_nested& nc, const M& metric, uint64_t iters) {
+    Fn<Fun, DIM, float> f{&fun};
+    auto regions = generate<H, L, DIM, float>(f, range, iters, nc, metric, nullptr);
+    float sol = 0.0f;
+    const float drange0 = (range.max(0) - range.min(0)) / float(1);
+    const Range<DIM> binrange = range.subrange_dimension(0, range.min(0) + 0 * drange0, range.min(0) + 1 * drange0);
+    for (const auto& r : regions) {
+        const Range<DIM> rb = binrange.intersection(r.range);
+        if (!rb.empty()) sol += double(1) * r.integral_subrange(rb);
+    }
+    return sol;
+}
+
 /* ------------------------------------------------------------------ control variates */
 template <class T> struct CvOptimize {
     T sum_f, sum_app;
@@ -726,6 +763,7 @@ template <class Visitor> int with_integrand(int32_t kind, const float* params, i
         vcu::Halfspace f{};
         if (f.build(params, n) || f.dim != dim) return 3;
         switch (dim) {
+        case 1: return v(f, std::integral_constant<int, 1>{}, float{});
         case 2: return v(f, std::integral_constant<int, 2>{}, float{});
         case 3: return v(f, std::integral_constant<int, 3>{}, float{});
         case 4: return v(f, std::integral_constant<int, 4>{}, float{});
@@ -855,6 +893,30 @@ extern "C" int orc_control_variates(int32_t kind, const float* params, int32_t n
             return with_metric(*nested, [&](auto m) -> int {
                 control_variates<decltype(h), decltype(l), decltype(D)::value, decltype(t)>(
                     f, p, *nested, m, iterations, spp, seed, weight, alpha, out, approx_out, regions_out, replay_out);
+                return 0;
+            });
+        });
+    });
+}
+
+extern "C" int orc_integrate_single(int32_t kind, const float* params, int32_t n_params, int32_t dim, const float* rmin,
+                                    const float* rmax, int32_t method, uint64_t budget, uint64_t seed,
+                                    const orc_nested* nested, float* out) {
+    if (dim < 1 || dim > 6 || budget == 0 || !out || (method != 0 && method != 1)) return 1;
+    if (method == 1 && !nested) return 1;
+    if (orc_channels(kind) != 1) return 2;
+    Problem p{dim, 1, rmin, rmax, nullptr};
+    return with_integrand(kind, params, n_params, dim, [&](const auto& f, auto D, auto t) -> int {
+        (void)t;
+        constexpr int DIM = decltype(D)::value;
+        const auto range = make_range<DIM>(p);
+        if (method == 0) {
+            *out = single_mc<DIM>(f, range, budget, seed);
+            return 0;
+        }
+        return with_rules(*nested, [&](auto h, auto l) -> int {
+            return with_metric(*nested, [&](auto m) -> int {
+                *out = single_nested<decltype(h), decltype(l), DIM>(f, range, *nested, m, budget - 1);
                 return 0;
             });
         });

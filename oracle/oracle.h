@@ -86,6 +86,15 @@ int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* params, int32
                                         uint64_t bin_begin, uint64_t bin_end, int32_t nthreads,
                                         float* out);
 
+/* One single-value viltrum::integrate(I, f, range) (src/integrate.h:105-113):
+ *   method 0: I = monte_carlo(budget, seed)  (std::mt19937(seed), float accumulation,
+ *             src/monte-carlo/monte-carlo.h:39-63, 89-95)
+ *   method 1: I = integrator_adaptive_iterations(nested(H,L), heuristic, budget - 1)
+ * -> *out.  This is the shape of each item of a batch of independent integrals.           */
+int orc_integrate_single(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                         const float* rmin, const float* rmax, int32_t method, uint64_t budget,
+                         uint64_t seed, const orc_nested* nested, float* out);
+
 #ifdef __cplusplus
 }
 #endif

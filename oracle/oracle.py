@@ -88,6 +88,10 @@ class Oracle:
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
                       ctypes.POINTER(Nested), ctypes.c_uint64, _f32p, _i32p]
+        f = getattr(L, prefix + "integrate_single")
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32,
+                      ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(Nested), _f32p]
         f = getattr(L, prefix + "control_variates")
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
@@ -156,6 +160,17 @@ class Oracle:
             ctypes.byref(nested), iterations, bin_begin, bin_end, nthreads, _ptr(out))
         self._check(rc, "per_bin_adaptive_nested_threads")
         return out.reshape(nb, ch)[bin_begin:bin_end]
+
+    def integrate_single(self, kind, params, rmin, rmax, method, budget, seed=0, nested: Nested | None = None):
+        """One single-value integrate(I, f, range): method 0 = monte_carlo(budget, seed), 1 = adaptive
+        nested quadrature with `budget` regions."""
+        params, rmin, rmax, _ = self._problem(params, rmin, rmax, [1])
+        out = np.zeros(1, dtype=np.float32)
+        rc = getattr(self.lib, self.prefix + "integrate_single")(
+            kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), method, budget, seed,
+            ctypes.byref(nested) if nested is not None else None, _ptr(out))
+        self._check(rc, "integrate_single")
+        return float(out[0])
 
     def control_variates(self, kind, params, rmin, rmax, res, nested: Nested, iterations, spp, seed,
                          weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False):

@@ -301,3 +301,39 @@ extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n
     }
     return 9;
 }
+
+/* single-value integrate(I, f, range) of the half-space family: the items of a batch of
+ * independent integrals (monte_carlo(budget, seed), or adaptive nested(simpson, trapezoidal) with
+ * budget regions and the default heuristic / absolute metric) */
+template <std::size_t DIM>
+static int ref_single_halfspace(const vcu::Halfspace& f, const float* rmin, const float* rmax, int32_t method,
+                                uint64_t budget, uint64_t seed, float* out) {
+    using namespace viltrum;
+    RefF<vcu::Halfspace, DIM, float> F{&f, nullptr};
+    const auto range = mk_range<DIM>(rmin, rmax);
+    if (method == 0) {
+        *out = integrate(monte_carlo((unsigned long)budget, (std::size_t)seed), F, range);
+    } else {
+        *out = integrate(integrator_adaptive_iterations(nested(simpson, trapezoidal), (std::size_t)(budget - 1)), F, range);
+    }
+    return 0;
+}
+
+extern "C" int ref_integrate_single(int32_t kind, const float* params, int32_t n_params, int32_t dim, const float* rmin,
+                                    const float* rmax, int32_t method, uint64_t budget, uint64_t seed,
+                                    const orc_nested* nc, float* out) {
+    if (kind != vcu::VCU_F_HALFSPACE || budget == 0 || (method != 0 && method != 1)) return 9;
+    if (method == 1 && !(nc && nc->rule_hi == ORC_RULE_SIMPSON && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
+                         nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_ABSOLUTE))
+        return 9;
+    vcu::Halfspace f{};
+    if (f.build(params, n_params) || f.dim != dim) return 3;
+    switch (dim) {
+    case 2: return ref_single_halfspace<2>(f, rmin, rmax, method, budget, seed, out);
+    case 3: return ref_single_halfspace<3>(f, rmin, rmax, method, budget, seed, out);
+    case 4: return ref_single_halfspace<4>(f, rmin, rmax, method, budget, seed, out);
+    case 5: return ref_single_halfspace<5>(f, rmin, rmax, method, budget, seed, out);
+    case 6: return ref_single_halfspace<6>(f, rmin, rmax, method, budget, seed, out);
+    default: return 9;
+    }
+}

@@ -85,6 +85,19 @@ CASES = [
 
 CRESPO = ("simpson", "trapezoidal", "size", "relative")
 
+# independent single-value integrals (the batched-integrals workload at small budgets)
+BATCH_CASES = [
+    ("batch_halfspace_n64_seed5", dict(n=64, seed=5, budget_lo=1, budget_hi=400)),
+]
+
+
+def run_batch(lib: orc.Oracle, kw: dict) -> dict:
+    items = scenes.batch_items(kw["n"], kw["seed"], kw["budget_lo"], kw["budget_hi"])
+    nested = orc.Nested.make("simpson", "trapezoidal")
+    out = np.array([lib.integrate_single(scenes.HALFSPACE, it["params"], it["rmin"], it["rmax"], it["method"],
+                                         it["budget"], it["seed"], nested) for it in items], dtype=np.float32)
+    return {"values": out}
+
 
 def visit_to_linear(res, parallel: bool) -> np.ndarray:
     """Bin (dim-0-fastest linear index) visited at each step of the reference's bin loop.
@@ -169,7 +182,17 @@ def main() -> int:
             meta["nested"] = np.array(kw["nested"])
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method=method, **meta, **{"out_" + k: v for k, v in r.items()})
         print(f"ok {name}")
-    print(f"{len(CASES) - bad} of {len(CASES)} cases bit-identical")
+    for name, kw in BATCH_CASES:
+        r, p = run_batch(ref, kw), run_batch(port, kw)
+        if not np.array_equal(r["values"].view(np.uint32), p["values"].view(np.uint32)):
+            bad += 1
+            print(f"MISMATCH {name}: {int((r['values'] != p['values']).sum())} items differ")
+            continue
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), method="batch", **{k: np.asarray(v) for k, v in kw.items()},
+                            out_values=r["values"])
+        print(f"ok {name}")
+    total = len(CASES) + len(BATCH_CASES)
+    print(f"{total - bad} of {total} cases bit-identical")
     return 1 if bad else 0
 
 

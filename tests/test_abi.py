@@ -43,4 +43,6 @@ def test_host_logic_without_device(lib_path):
     assert lib.vcu_abi_version() == 1
     assert lib.vcu_channels(5) == 1 and lib.vcu_channels(6) == 3 and lib.vcu_channels(99) < 0
     assert lib.vcu_per_bin_monte_carlo(None, None, 1, 1, None, None) == 1  # null context -> INVALID_ARG
+    assert lib.vcu_integrate_batch(None, 7, None, None, 0, None, 0, None, None) == 1
+    assert lib.vcu_integrate_batch_resident(None, None, 0, None, None) == 1
     assert lib.vcu_destroy(None) == 0

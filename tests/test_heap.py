@@ -1,4 +1,6 @@
-"""The device heap (viltrum_gb300/csrc/vcu_heap.h) makes libstdc++'s choices.
+"""The device heap (viltrum_gb300/csrc/vcu_heap.h) makes libstdc++'s choices: the two-array form
+and the packed-entry form, over one array and split between two (as the batched kernel keeps its top
+levels in shared memory).
 
 A small host program drives vcu::heap_push / heap_pop and std::push_heap / std::pop_heap with
 the same random sequences (with many equal keys, which is where the two could disagree) and
@@ -21,6 +23,9 @@ int main() {
     for (int trial = 0; trial < 400; ++trial) {
         std::vector<E> ref;
         float key[128]; int pay[128]; int n = 0; int next = 0;
+        vcu::HeapEntry one[130], top[16], rest[130];
+        const vcu::HeapArray ha{one};
+        const vcu::HeapSplit hs{top, rest, 7};
         const int levels = 1 + trial % 7;
         for (int op = 0; op < 300; ++op) {
             const bool push = n == 0 || (n < 120 && (rng() % 3) != 0);
@@ -30,13 +35,21 @@ int main() {
                 std::push_heap(ref.begin(), ref.end(), [](const E& a, const E& b) { return a.k < b.k; });
                 key[n] = k; pay[n] = next; ++n; ++next;
                 vcu::heap_push(key, pay, n);
+                ha.set(n - 1, vcu::HeapEntry{k, next - 1});
+                vcu::heap_push_entries(ha, n);
+                hs.set(n - 1, vcu::HeapEntry{k, next - 1});
+                vcu::heap_push_entries(hs, n);
             } else {
                 std::pop_heap(ref.begin(), ref.end(), [](const E& a, const E& b) { return a.k < b.k; });
                 ref.pop_back();
-                vcu::heap_pop(key, pay, n); --n;
+                vcu::heap_pop(key, pay, n);
+                vcu::heap_pop_entries(ha, n);
+                vcu::heap_pop_entries(hs, n); --n;
             }
             for (int i = 0; i < n; ++i)
-                if (ref[i].k != key[i] || ref[i].p != pay[i]) { std::printf("mismatch trial %d op %d\n", trial, op); return 1; }
+                if (ref[i].k != key[i] || ref[i].p != pay[i] || ref[i].k != ha.get(i).key || ref[i].p != ha.get(i).pay ||
+                    ref[i].k != hs.get(i).key || ref[i].p != hs.get(i).pay) {
+                    std::printf("mismatch trial %d op %d\n", trial, op); return 1; }
         }
     }
     std::printf("ok\n");

@@ -37,6 +37,13 @@ def test_oracle_matches_reference_golden(port, name):
         assert np.array_equal(r["bins"].view(np.uint32), g["out_bins"].view(np.uint32))
         assert np.array_equal(r["regions"].view(np.uint32), g["out_regions"].view(np.uint32))
         assert np.array_equal(r["replay"][:, :, 1:].view(np.uint32), g["out_points"].view(np.uint32))
+    elif method == "batch":
+        from viltrum_gb300 import scenes
+        items = scenes.batch_items(int(g["n"]), int(g["seed"]), int(g["budget_lo"]), int(g["budget_hi"]))
+        nested = orc.Nested.make("simpson", "trapezoidal")
+        out = np.array([port.integrate_single(scenes.HALFSPACE, it["params"], it["rmin"], it["rmax"], it["method"],
+                                              it["budget"], it["seed"], nested) for it in items], dtype=np.float32)
+        assert np.array_equal(out.view(np.uint32), g["out_values"].view(np.uint32))
     else:
         pytest.fail(method)
 

@@ -23,7 +23,9 @@ FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
 
 EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
            "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested",
-           "vcu_control_variates"]
+           "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
+           "vcu_integrate_batch_resident"]
+BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
 
 
 class VcuError(RuntimeError):
@@ -62,6 +64,32 @@ class CvOpts(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double)]
 
 
+class LearnedOpts(ctypes.Structure):
+    _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("train_steps", ctypes.c_uint32),
+                ("batch", ctypes.c_uint32), ("learning_rate", ctypes.c_float), ("quad_nodes", ctypes.c_uint32),
+                ("fallback", ctypes.c_int32), ("reserved", ctypes.c_int32), ("theta_out", ctypes.c_void_p)]
+
+
+class LearnedReport(ctypes.Structure):
+    _fields_ = [("train_ms", ctypes.c_double), ("integral_ms", ctypes.c_double), ("residual_ms", ctypes.c_double),
+                ("fallback_bins", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("method", ctypes.c_int32), ("budget", ctypes.c_uint64),
+                ("seed", ctypes.c_uint64), ("range_min", ctypes.c_float * VCU_MAX_DIM),
+                ("range_max", ctypes.c_float * VCU_MAX_DIM), ("n_params", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("params", ctypes.c_void_p)]
+
+
+class BatchReport(ctypes.Structure):
+    _fields_ = [("item_ms", ctypes.c_void_p), ("threads", ctypes.c_int32), ("blocks", ctypes.c_uint32),
+                ("nested_regions", ctypes.c_uint64)]
+
+
 class Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("flags", ctypes.c_int32), ("stream", ctypes.c_void_p)]
 
@@ -96,6 +124,14 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                                                   ctypes.c_uint64, vp, vp, ctypes.POINTER(Stats)]
         L.vcu_control_variates.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested), ctypes.c_uint64,
                                            ctypes.POINTER(CvOpts), vp, vp, vp, vp, ctypes.POINTER(Stats)]
+        L.vcu_learned_control_variates.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(LearnedOpts), vp, vp,
+                                                   ctypes.POINTER(LearnedReport), ctypes.POINTER(Stats)]
+        L.vcu_mlp_eval.argtypes = [vp, ctypes.c_int32, vp, vp, vp, ctypes.c_int64, vp, vp]
+        L.vcu_integrate_batch.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Nested), ctypes.POINTER(BatchItem),
+                                          ctypes.c_uint64, vp, ctypes.c_int32, ctypes.POINTER(BatchReport),
+                                          ctypes.POINTER(Stats)]
+        L.vcu_integrate_batch_resident.argtypes = [vp, vp, ctypes.c_int32, ctypes.POINTER(BatchReport),
+                                                   ctypes.POINTER(Stats)]
         for name in EXPORTS:
             getattr(L, name).restype = ctypes.c_int
         del f32p
@@ -214,6 +250,76 @@ def _cv_method(self, p: Problem, nested: Nested, iterations: int, cv: CvOpts, bi
 
 
 Context.control_variates = _cv_method
+
+
+def _learned_method(self, p: Problem, opts: LearnedOpts, bins, network_integral=None):
+    st, rep = Stats(), LearnedReport()
+    self.check(self.lib.vcu_learned_control_variates(self.handle, ctypes.byref(p), ctypes.byref(opts), _ptr(bins),
+                                                     _ptr(network_integral), ctypes.byref(rep), ctypes.byref(st)))
+    return st, rep
+
+
+def _mlp_eval_method(self, dim: int, theta, u, y=None, grad=False):
+    theta = np.ascontiguousarray(theta, np.float32)
+    u = np.ascontiguousarray(u, np.float32)
+    n = u.shape[0]
+    out = np.empty(n, np.float32)
+    g = np.empty(theta.size, np.float32) if grad else None
+    yy = None if y is None else np.ascontiguousarray(y, np.float32)
+    self.check(self.lib.vcu_mlp_eval(self.handle, dim, _ptr(theta), _ptr(u), _ptr(yy), n, _ptr(out), _ptr(g)))
+    return out, g
+
+
+def batch_items(items) -> tuple:
+    """ctypes array of vcu_batch_item from dicts (dim, method, budget, seed, params, rmin, rmax); the
+    parameter arrays are returned too, since the items point into them."""
+    arr = (BatchItem * len(items))()
+    keep = []
+    for i, it in enumerate(items):
+        b = arr[i]
+        b.dim = int(it["dim"])
+        b.method = int(it["method"])
+        b.budget = int(it["budget"])
+        b.seed = int(it.get("seed", 0))
+        for d in range(b.dim):
+            b.range_min[d] = float(it["rmin"][d])
+            b.range_max[d] = float(it["rmax"][d])
+        prm = it.get("params")
+        if prm is not None:
+            prm = np.ascontiguousarray(prm, np.float32)
+            keep.append(prm)
+            b.params = prm.ctypes.data
+            b.n_params = prm.size
+    return arr, keep
+
+
+def _batch_method(self, kind: int, items, nested: Nested | None = None, results=None, mem=MEM_HOST,
+                  item_ms=None):
+    """vcu_integrate_batch over a list of item dicts (or a prepared (array, keep) pair)."""
+    arr, keep = items if isinstance(items, tuple) else batch_items(items)
+    n = len(arr)
+    if results is None:
+        results = np.empty(n, np.float32)
+    st, rep = Stats(), BatchReport()
+    rep.item_ms = _ptr(item_ms)
+    self.check(self.lib.vcu_integrate_batch(self.handle, kind, ctypes.byref(nested) if nested is not None else None,
+                                            arr, n, _ptr(results), mem, ctypes.byref(rep), ctypes.byref(st)))
+    del keep
+    return results, st, rep
+
+
+def _batch_resident_method(self, results, mem=MEM_HOST, item_ms=None):
+    st, rep = Stats(), BatchReport()
+    rep.item_ms = _ptr(item_ms)
+    self.check(self.lib.vcu_integrate_batch_resident(self.handle, _ptr(results), mem, ctypes.byref(rep),
+                                                     ctypes.byref(st)))
+    return st, rep
+
+
+Context.learned_control_variates = _learned_method
+Context.mlp_eval = _mlp_eval_method
+Context.integrate_batch = _batch_method
+Context.integrate_batch_resident = _batch_resident_method
 
 _default_ctx: Context | None = None
 

@@ -414,7 +414,7 @@ __device__ float poly_subrange(const float* V, int c, const float* A, const floa
         float line[S];
 #pragma unroll
         for (int j = 0; j < S; ++j) line[j] = V[(i + j * inner) * CH + c];
-        buf[i] = Rule<S>::subrange(A[DIM - 1], B[DIM - 1], line);
+        buf[i] = (CH == 1) ? subrange_ref<S>(A[DIM - 1], B[DIM - 1], line) : Rule<S>::subrange(A[DIM - 1], B[DIM - 1], line);
     }
     int n = inner;
     for (int d = DIM - 2; d >= 0; --d) {
@@ -423,7 +423,7 @@ __device__ float poly_subrange(const float* V, int c, const float* A, const floa
             float line[S];
 #pragma unroll
             for (int j = 0; j < S; ++j) line[j] = buf[i + j * m];
-            buf[i] = Rule<S>::subrange(A[d], B[d], line);
+            buf[i] = (CH == 1) ? subrange_ref<S>(A[d], B[d], line) : Rule<S>::subrange(A[d], B[d], line);
         }
         n = m;
     }

@@ -1,0 +1,839 @@
+/*
+ * k_mlp.cu -- learned control variate: online training, per-bin integral of the network, residual.
+ *
+ * No reference counterpart (the task's learned part; the per-bin wrapper it plugs into is
+ * src/integrator-per-bin-parallel.h:17-35).  Pipeline of vcu_learned_control_variates:
+ *  1. train: `train_steps` Adam steps on fresh samples of the integrand (Philox points over the
+ *     range, the integrand evaluated by the device) minimising mean (g - f)^2; each step is one
+ *     fused forward+backward kernel (k_mlp_train), one Adam kernel that also rewrites the BF16
+ *     shared-memory image of the weights, and one counter kernel -- captured once in a CUDA graph
+ *     and replayed for all steps;
+ *  2. k_mlp_integral: per bin, Gauss-Legendre quadrature (q nodes per dimension) of g over the bin;
+ *  3. k_mlp_residual: per bin, `samples` Philox points, estimate = integral of g + mean(f - g)
+ *     (control variate with weight 1: unbiased up to the quadrature error of the network's
+ *     integral); optionally the plain Monte Carlo mean of the same samples is kept instead when
+ *     its sample variance is lower (per-bin fallback).
+ */
+#include "k_mlp.cuh"
+
+namespace vcu {
+namespace mlp {
+
+constexpr int TRAIN_WARPS = 8;
+constexpr int FWD_WARPS = 4;
+constexpr int ZS = 16 + 8; /* row stride (bf16) of the transposed per-warp tiles */
+/* rows of the transposed activation tile: the widest layer input (features or a hidden layer) */
+__host__ __device__ constexpr int at_rows(int d) { return fin(d) > WIDTH ? fin(d) : WIDTH; }
+
+struct RangeCfg {
+    float rmin[VCU_MAX_DIM], rmax[VCU_MAX_DIM];
+};
+
+struct TrainCfg {
+    RangeCfg r;
+    uint32_t k0, k1;
+    uint32_t tiles_per_warp; /* 32-point chunks per warp */
+    float scale;             /* 2 / batch */
+    const float* u_in;       /* explicit points (gradient check) or null */
+    const float* y_in;
+    float* out;              /* outputs of explicit points, or null */
+    uint64_t npts;           /* explicit points: count */
+};
+
+template <int D> __host__ __device__ constexpr int train_smem_bytes() {
+    return pack_bytes(D) + (fin(D) * WIDTH + 3 * WIDTH * WIDTH + 4 * WIDTH + WIDTH + 4) * 4 +
+           TRAIN_WARPS * (at_rows(D) + WIDTH) * ZS * 2 + 64;
+}
+
+/* gradient of layer l's W, b accumulated into shared memory from one 16-point tile */
+template <int KT>
+__device__ __forceinline__ void accumulate_dW(__nv_bfloat16* AT, __nv_bfloat16* ZT, const uint32_t (*A)[4],
+                                              const float (*dZ)[4], float* gW, float* gb) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    /* store A (points x inputs) transposed: AT[input][point] */
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt) {
+        const int c = 16 * kt + 2 * t;
+        AT[(c)*ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][0] & 0xffff));
+        AT[(c + 1) * ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][0] >> 16));
+        AT[(c)*ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][1] & 0xffff));
+        AT[(c + 1) * ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][1] >> 16));
+        AT[(c + 8) * ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][2] & 0xffff));
+        AT[(c + 9) * ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][2] >> 16));
+        AT[(c + 8) * ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][3] & 0xffff));
+        AT[(c + 9) * ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][3] >> 16));
+    }
+    /* store dZ (points x 64) transposed, as BF16: ZT[unit][point]; db from the same BF16 values */
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        const int c = 8 * j + 2 * t;
+        const __nv_bfloat16 z00 = __float2bfloat16_rn(dZ[j][0]), z01 = __float2bfloat16_rn(dZ[j][1]);
+        const __nv_bfloat16 z10 = __float2bfloat16_rn(dZ[j][2]), z11 = __float2bfloat16_rn(dZ[j][3]);
+        ZT[c * ZS + g] = z00;
+        ZT[(c + 1) * ZS + g] = z01;
+        ZT[c * ZS + g + 8] = z10;
+        ZT[(c + 1) * ZS + g + 8] = z11;
+        float s0 = __bfloat162float(z00) + __bfloat162float(z10);
+        float s1 = __bfloat162float(z01) + __bfloat162float(z11);
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        }
+        if (g == 0) {
+            atomicAdd(&gb[c], s0);
+            atomicAdd(&gb[c + 1], s1);
+        }
+    }
+    __syncwarp();
+    /* dW[input][unit] += AT^T-tile x ZT-tile: M = inputs, N = 64 units, K = 16 points */
+#pragma unroll
+    for (int mt = 0; mt < KT; ++mt) {
+        uint32_t a[4];
+        const uint32_t* r0 = reinterpret_cast<const uint32_t*>(AT + (16 * mt + g) * ZS);
+        const uint32_t* r1 = reinterpret_cast<const uint32_t*>(AT + (16 * mt + g + 8) * ZS);
+        a[0] = r0[t];
+        a[1] = r1[t];
+        a[2] = r0[t + 4];
+        a[3] = r1[t + 4];
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+            const uint32_t* zb = reinterpret_cast<const uint32_t*>(ZT + (8 * j + g) * ZS);
+            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            mma16816(c, a, zb[t], zb[t + 4]);
+            float* row0 = gW + (16 * mt + g) * WIDTH + 8 * j + 2 * t;
+            float* row1 = gW + (16 * mt + g + 8) * WIDTH + 8 * j + 2 * t;
+            atomicAdd(row0, c[0]);
+            atomicAdd(row0 + 1, c[1]);
+            atomicAdd(row1, c[2]);
+            atomicAdd(row1 + 1, c[3]);
+        }
+    }
+    __syncwarp();
+}
+
+/* dh = dZ W^T for layer l (W in-major N_l: [in][64+PAD]), masked by relu'(previous z) */
+__device__ __forceinline__ void backprop_layer(const float (*dZ)[4], const __nv_bfloat16* N, const uint32_t (*Hprev)[4],
+                                               float (*dH)[4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    uint32_t AZ[KTH][4];
+#pragma unroll
+    for (int kt = 0; kt < KTH; ++kt) {
+        AZ[kt][0] = pack_bf16x2(dZ[2 * kt][0], dZ[2 * kt][1]);
+        AZ[kt][1] = pack_bf16x2(dZ[2 * kt][2], dZ[2 * kt][3]);
+        AZ[kt][2] = pack_bf16x2(dZ[2 * kt + 1][0], dZ[2 * kt + 1][1]);
+        AZ[kt][3] = pack_bf16x2(dZ[2 * kt + 1][2], dZ[2 * kt + 1][3]);
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        dH[j][0] = dH[j][1] = dH[j][2] = dH[j][3] = 0.0f;
+#pragma unroll
+        for (int kt = 0; kt < KTH; ++kt) {
+            const uint32_t* row = reinterpret_cast<const uint32_t*>(N + (8 * j + g) * (WIDTH + PAD) + 16 * kt);
+            mma16816(dH[j], AZ[kt], row[t], row[t + 4]);
+        }
+    }
+    /* relu' of the previous layer's pre-activation: its BF16 output is > 0 */
+#pragma unroll
+    for (int kt = 0; kt < KTH; ++kt) {
+        const uint32_t* h = Hprev[kt];
+        dH[2 * kt][0] = bf16_lo(h[0]) > 0.0f ? dH[2 * kt][0] : 0.0f;
+        dH[2 * kt][1] = bf16_hi(h[0]) > 0.0f ? dH[2 * kt][1] : 0.0f;
+        dH[2 * kt][2] = bf16_lo(h[1]) > 0.0f ? dH[2 * kt][2] : 0.0f;
+        dH[2 * kt][3] = bf16_hi(h[1]) > 0.0f ? dH[2 * kt][3] : 0.0f;
+        dH[2 * kt + 1][0] = bf16_lo(h[2]) > 0.0f ? dH[2 * kt + 1][0] : 0.0f;
+        dH[2 * kt + 1][1] = bf16_hi(h[2]) > 0.0f ? dH[2 * kt + 1][1] : 0.0f;
+        dH[2 * kt + 1][2] = bf16_lo(h[3]) > 0.0f ? dH[2 * kt + 1][2] : 0.0f;
+        dH[2 * kt + 1][3] = bf16_hi(h[3]) > 0.0f ? dH[2 * kt + 1][3] : 0.0f;
+    }
+    /* round through BF16 once, as the tensor cores will consume it */
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dH[j][i] = __bfloat162float(__float2bfloat16_rn(dH[j][i]));
+}
+
+/* forward + backward of one 16-point tile; y0/y1 targets of rows g, g+8 */
+template <int D>
+__device__ void train_tile(const SmemParams<D>& P, const float* u_g, const float* u_g8, float y0, float y1, bool v0,
+                           bool v1, float scale, float* gW[4], float* gb[4], float* gw4, float* gb4,
+                           __nv_bfloat16* AT, __nv_bfloat16* ZT, float* out_rows) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    Acts<D> a;
+    features_tile<D>(u_g, u_g8, a.F);
+    float out[2];
+    forward_tile<D>(P, a, out);
+    if (out_rows) {
+        out_rows[0] = out[0];
+        out_rows[1] = out[1];
+    }
+    const float d0 = v0 ? (out[0] - y0) * scale : 0.0f;
+    const float d1 = v1 ? (out[1] - y1) * scale : 0.0f;
+    /* output layer gradients */
+    {
+        float sb = (t == 0) ? d0 + d1 : 0.0f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
+        if (lane == 0) atomicAdd(gb4, sb);
+#pragma unroll
+        for (int kt = 0; kt < KTH; ++kt) {
+            const int c = 16 * kt + 2 * t;
+            float s[4] = {d0 * bf16_lo(a.H[3][kt][0]) + d1 * bf16_lo(a.H[3][kt][1]),
+                          d0 * bf16_hi(a.H[3][kt][0]) + d1 * bf16_hi(a.H[3][kt][1]),
+                          d0 * bf16_lo(a.H[3][kt][2]) + d1 * bf16_lo(a.H[3][kt][3]),
+                          d0 * bf16_hi(a.H[3][kt][2]) + d1 * bf16_hi(a.H[3][kt][3])};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) s[i] += __shfl_xor_sync(0xffffffffu, s[i], o);
+            if (g == 0) {
+                atomicAdd(&gw4[c], s[0]);
+                atomicAdd(&gw4[c + 1], s[1]);
+                atomicAdd(&gw4[c + 8], s[2]);
+                atomicAdd(&gw4[c + 9], s[3]);
+            }
+        }
+    }
+    /* dZ4 = dout * w4 * relu'(z4), rounded to BF16 */
+    float dZ[NT][4];
+#pragma unroll
+    for (int kt = 0; kt < KTH; ++kt) {
+        const int c = 16 * kt + 2 * t;
+        const uint32_t* h = a.H[3][kt];
+        dZ[2 * kt][0] = bf16_lo(h[0]) > 0.0f ? d0 * P.w4[c] : 0.0f;
+        dZ[2 * kt][1] = bf16_hi(h[0]) > 0.0f ? d0 * P.w4[c + 1] : 0.0f;
+        dZ[2 * kt][2] = bf16_lo(h[1]) > 0.0f ? d1 * P.w4[c] : 0.0f;
+        dZ[2 * kt][3] = bf16_hi(h[1]) > 0.0f ? d1 * P.w4[c + 1] : 0.0f;
+        dZ[2 * kt + 1][0] = bf16_lo(h[2]) > 0.0f ? d0 * P.w4[c + 8] : 0.0f;
+        dZ[2 * kt + 1][1] = bf16_hi(h[2]) > 0.0f ? d0 * P.w4[c + 9] : 0.0f;
+        dZ[2 * kt + 1][2] = bf16_lo(h[3]) > 0.0f ? d1 * P.w4[c + 8] : 0.0f;
+        dZ[2 * kt + 1][3] = bf16_hi(h[3]) > 0.0f ? d1 * P.w4[c + 9] : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dZ[j][i] = __bfloat162float(__float2bfloat16_rn(dZ[j][i]));
+    /* layers 3, 2, 1: dW from (input activations, dZ), then dZ of the layer below */
+    float dH[NT][4];
+    accumulate_dW<KTH>(AT, ZT, a.H[2], dZ, gW[3], gb[3]);
+    backprop_layer(dZ, P.N[3], a.H[2], dH);
+    accumulate_dW<KTH>(AT, ZT, a.H[1], dH, gW[2], gb[2]);
+    backprop_layer(dH, P.N[2], a.H[1], dZ);
+    accumulate_dW<KTH>(AT, ZT, a.H[0], dZ, gW[1], gb[1]);
+    backprop_layer(dZ, P.N[1], a.H[0], dH);
+    accumulate_dW<fin(D) / 16>(AT, ZT, a.F, dH, gW[0], gb[0]);
+}
+
+/* training points of one step: Philox points over the range and the integrand's values there */
+template <class F, int D>
+__global__ void k_mlp_samples(const __grid_constant__ F f, const TrainCfg cfg, uint64_t n, float* __restrict__ u_out,
+                              float* __restrict__ y_out, const uint32_t* __restrict__ step_ctr) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t step = *step_ctr;
+    float u[D], x[F::DIM];
+    for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+#pragma unroll
+    for (int blk = 0; blk < (D + 3) / 4; ++blk) {
+        const U4 r = philox4x32_10(U4{(uint32_t)s, (uint32_t)(s >> 32), step, 0x7EA10000u + blk}, cfg.k0, cfg.k1);
+        const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int d = blk * 4 + k;
+            if (d < D) u[d] = u01(rr[k]);
+        }
+    }
+    for (int d = 0; d < D; ++d) {
+        x[d] = vadd(vmul(u[d], vsub(cfg.r.rmax[d], cfg.r.rmin[d])), cfg.r.rmin[d]);
+        u_out[s * D + d] = u[d];
+    }
+    float v[1];
+    f(x, v);
+    y_out[s] = v[0];
+}
+
+template <int D>
+__global__ void __launch_bounds__(TRAIN_WARPS * 32, 1)
+    k_mlp_train(const TrainCfg cfg, const char* __restrict__ packed, float* __restrict__ grad) {
+    extern __shared__ __align__(16) char smem[];
+    load_params<D>(smem, packed, true);
+    const SmemParams<D> P = smem_params<D>(smem, true);
+    float* gsm = reinterpret_cast<float*>(smem + pack_bytes(D));
+    const int ng = fin(D) * WIDTH + 3 * WIDTH * WIDTH + 4 * WIDTH + WIDTH + 1;
+    for (int i = threadIdx.x; i < ng; i += blockDim.x) gsm[i] = 0.0f;
+    float* gW[4];
+    float* gb[4];
+    for (int l = 0; l < 4; ++l) {
+        gW[l] = gsm + (l == 0 ? 0 : fin(D) * WIDTH + (l - 1) * WIDTH * WIDTH);
+        gb[l] = gsm + fin(D) * WIDTH + 3 * WIDTH * WIDTH + l * WIDTH;
+    }
+    float* gw4 = gsm + fin(D) * WIDTH + 3 * WIDTH * WIDTH + 4 * WIDTH;
+    float* gb4 = gw4 + WIDTH;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
+    __nv_bfloat16* AT = reinterpret_cast<__nv_bfloat16*>(gsm + ng + 3) + warp * (at_rows(D) + WIDTH) * ZS;
+    AT = reinterpret_cast<__nv_bfloat16*>((reinterpret_cast<uintptr_t>(AT) + 15) & ~uintptr_t(15));
+    __nv_bfloat16* ZT = AT + at_rows(D) * ZS;
+    __syncthreads();
+    const uint64_t warp_global = (uint64_t)blockIdx.x * TRAIN_WARPS + warp;
+    for (uint32_t chunk = 0; chunk < cfg.tiles_per_warp; ++chunk) {
+        const uint64_t s = (warp_global * cfg.tiles_per_warp + chunk) * 32 + lane; /* this lane's point */
+        float u[D];
+        const bool valid = s < cfg.npts;
+        for (int d = 0; d < D; ++d) u[d] = valid ? cfg.u_in[s * D + d] : 0.5f;
+        const float y = valid ? cfg.y_in[s] : 0.0f;
+        /* two 16-point tiles: points 0..15 and 16..31 of this chunk */
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            float ug[D], ug8[D];
+            const int src0 = 16 * half + g, src1 = 16 * half + g + 8;
+            for (int d = 0; d < D; ++d) {
+                ug[d] = __shfl_sync(0xffffffffu, u[d], src0);
+                ug8[d] = __shfl_sync(0xffffffffu, u[d], src1);
+            }
+            const float y0 = __shfl_sync(0xffffffffu, y, src0), y1 = __shfl_sync(0xffffffffu, y, src1);
+            const bool v0 = __shfl_sync(0xffffffffu, valid, src0), v1 = __shfl_sync(0xffffffffu, valid, src1);
+            float outr[2];
+            train_tile<D>(P, ug, ug8, y0, y1, v0, v1, cfg.scale, gW, gb, gw4, gb4, AT, ZT, outr);
+            if (cfg.out && (lane & 3) == 0) {
+                const uint64_t base = (warp_global * cfg.tiles_per_warp + chunk) * 32 + 16 * half;
+                if (base + g < cfg.npts) cfg.out[base + g] = outr[0];
+                if (base + g + 8 < cfg.npts) cfg.out[base + g + 8] = outr[1];
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ng; i += blockDim.x) atomicAdd(&grad[i], gsm[i]);
+}
+
+/* gradient layout in shared memory / global: gW0..gW3 (W order), gb0..gb3, gw4, gb4 -> parameter index */
+template <int D> __device__ __forceinline__ int grad_to_param(int i) {
+    const int a = fin(D) * WIDTH, hid = WIDTH * WIDTH;
+    if (i < a) return w_off(0, D) + i;
+    if (i < a + 3 * hid) {
+        const int l = 1 + (i - a) / hid;
+        return w_off(l, D) + (i - a) % hid;
+    }
+    i -= a + 3 * hid;
+    if (i < 4 * WIDTH) return b_off(i / WIDTH, D) + i % WIDTH;
+    i -= 4 * WIDTH;
+    return w4_off(D) + i; /* w4[0..63], then b4 */
+}
+
+/* write parameter p (fp32) into the packed shared-memory image */
+template <int D> __device__ __forceinline__ void pack_param(char* packed, int p, float v) {
+    __nv_bfloat16* bf = reinterpret_cast<__nv_bfloat16*>(packed);
+    float* f32 = reinterpret_cast<float*>(packed + fp32_off_bytes(D));
+    for (int l = 0; l < 4; ++l) {
+        const int in = layer_in(l, D);
+        const int w0 = w_off(l, D);
+        if (p >= w0 && p < w0 + in * WIDTH) {
+            const int k = (p - w0) / WIDTH, n = (p - w0) % WIDTH;
+            const __nv_bfloat16 b = __float2bfloat16_rn(v);
+            bf[t_off(l, D) + n * (in + PAD) + k] = b;
+            bf[n_off(l, D) + k * (WIDTH + PAD) + n] = b;
+            return;
+        }
+        if (p >= b_off(l, D) && p < b_off(l, D) + WIDTH) {
+            f32[l * WIDTH + (p - b_off(l, D))] = v;
+            return;
+        }
+    }
+    f32[4 * WIDTH + (p - w4_off(D))] = v; /* w4 and b4 */
+}
+
+struct AdamCfg {
+    float lr, b1, b2, eps;
+    int n;
+};
+
+template <int D>
+__global__ void k_mlp_adam(const AdamCfg c, float* __restrict__ theta, float* __restrict__ m, float* __restrict__ v,
+                           float* __restrict__ grad, const uint32_t* __restrict__ step_ctr, char* __restrict__ packed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const int p = grad_to_param<D>(i);
+    const float gr = grad[i];
+    grad[i] = 0.0f;
+    const float t = (float)(*step_ctr + 1);
+    const float mi = c.b1 * m[p] + (1.0f - c.b1) * gr;
+    const float vi = c.b2 * v[p] + (1.0f - c.b2) * gr * gr;
+    m[p] = mi;
+    v[p] = vi;
+    const float mh = mi / (1.0f - powf(c.b1, t));
+    const float vh = vi / (1.0f - powf(c.b2, t));
+    const float w = theta[p] - c.lr * mh / (sqrtf(vh) + c.eps);
+    theta[p] = w;
+    pack_param<D>(packed, p, w);
+}
+
+__global__ void k_mlp_step_inc(uint32_t* step_ctr) { *step_ctr += 1u; }
+
+template <int D> __global__ void k_mlp_pack(const float* __restrict__ theta, char* __restrict__ packed) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n_params(D)) pack_param<D>(packed, p, theta[p]);
+}
+
+/* ---------------------------------------------------------------- per-bin integral of g */
+struct BinCfg {
+    RangeCfg r;
+    float drange[VCU_MAX_DIMBINS];
+    uint32_t res[VCU_MAX_DIMBINS];
+    int32_t dimbins;
+    uint64_t nbins;
+    int32_t q; /* Gauss-Legendre nodes per dimension */
+    float gl_x[4], gl_w[4];
+};
+
+template <int D>
+__device__ __forceinline__ void bin_box(const BinCfg& c, uint64_t bin, float* lo, float* hi) {
+    uint64_t rem = bin;
+    for (int d = 0; d < D; ++d) {
+        lo[d] = c.r.rmin[d];
+        hi[d] = c.r.rmax[d];
+        if (d < c.dimbins) {
+            const uint32_t pos = (uint32_t)(rem % c.res[d]);
+            rem /= c.res[d];
+            lo[d] = vadd(c.r.rmin[d], vmul((float)pos, c.drange[d]));
+            hi[d] = vadd(c.r.rmin[d], vmul((float)(pos + 1), c.drange[d]));
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(FWD_WARPS * 32)
+    k_mlp_integral(const BinCfg c, const char* __restrict__ packed, float* __restrict__ integral) {
+    extern __shared__ __align__(16) char smem[];
+    load_params<D>(smem, packed, false);
+    const SmemParams<D> P = smem_params<D>(smem, false);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
+    int nodes = 1;
+    for (int d = 0; d < D; ++d) nodes *= c.q;
+    for (uint64_t bin = (uint64_t)blockIdx.x * FWD_WARPS + warp; bin < c.nbins; bin += (uint64_t)gridDim.x * FWD_WARPS) {
+        float lo[D], hi[D];
+        bin_box<D>(c, bin, lo, hi);
+        float acc = 0.0f;
+        for (int base = 0; base < nodes; base += 16) {
+            float ug[D], ug8[D], w0 = 1.0f, w1 = 1.0f;
+            const int n0 = base + g, n1 = base + g + 8;
+            int r0 = n0, r1 = n1;
+            for (int d = 0; d < D; ++d) {
+                const int i0 = r0 % c.q, i1 = r1 % c.q;
+                r0 /= c.q;
+                r1 /= c.q;
+                const float x0 = lo[d] + (hi[d] - lo[d]) * 0.5f * (1.0f + c.gl_x[i0]);
+                const float x1 = lo[d] + (hi[d] - lo[d]) * 0.5f * (1.0f + c.gl_x[i1]);
+                const float span = c.r.rmax[d] - c.r.rmin[d];
+                ug[d] = (x0 - c.r.rmin[d]) / span;
+                ug8[d] = (x1 - c.r.rmin[d]) / span;
+                w0 *= 0.5f * c.gl_w[i0];
+                w1 *= 0.5f * c.gl_w[i1];
+            }
+            Acts<D> a;
+            features_tile<D>(ug, ug8, a.F);
+            float out[2];
+            forward_tile<D>(P, a, out);
+            if ((lane & 3) == 0) acc += (n0 < nodes ? w0 * out[0] : 0.0f) + (n1 < nodes ? w1 * out[1] : 0.0f);
+        }
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) integral[bin] = acc; /* mean of g over the bin */
+    }
+}
+
+/* ---------------------------------------------------------------- residual */
+struct ResidualCfg {
+    BinCfg b;
+    uint64_t spp;
+    uint32_t k0, k1;
+    int32_t fallback;
+    float factor; /* prod(res) */
+};
+
+template <class F, int D>
+__global__ void __launch_bounds__(FWD_WARPS * 32)
+    k_mlp_residual(const __grid_constant__ F f, const ResidualCfg c, const char* __restrict__ packed,
+                   const float* __restrict__ integral, float* __restrict__ bins, uint32_t* __restrict__ fallback_count,
+                   uint32_t* __restrict__ status) {
+    extern __shared__ __align__(16) char smem[];
+    load_params<D>(smem, packed, false);
+    const SmemParams<D> P = smem_params<D>(smem, false);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
+    for (uint64_t bin = (uint64_t)blockIdx.x * FWD_WARPS + warp; bin < c.b.nbins;
+         bin += (uint64_t)gridDim.x * FWD_WARPS) {
+        float lo[D], hi[D];
+        bin_box<D>(c.b, bin, lo, hi);
+        float vol = 1.0f;
+        for (int d = 0; d < D; ++d) vol = vmul(vol, vsub(hi[d], lo[d]));
+        double sf = 0.0, sf2 = 0.0, sr = 0.0, sr2 = 0.0;
+        for (uint64_t base = 0; base < c.spp; base += 32) {
+            const uint64_t s = base + lane;
+            const bool valid = s < c.spp;
+            float u[D], x[F::DIM];
+            for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+#pragma unroll
+            for (int blk = 0; blk < (D + 3) / 4; ++blk) {
+                const U4 r = philox4x32_10(U4{(uint32_t)s, (uint32_t)bin, (uint32_t)(bin >> 32), 0x5E5D0000u + blk},
+                                           c.k0, c.k1);
+                const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int d = blk * 4 + k;
+                    if (d < D) x[d] = vadd(vmul(u01(rr[k]), vsub(hi[d], lo[d])), lo[d]);
+                }
+            }
+            for (int d = 0; d < D; ++d) u[d] = (x[d] - c.b.r.rmin[d]) / (c.b.r.rmax[d] - c.b.r.rmin[d]);
+            float fv[1];
+            f(x, fv);
+            /* g at the 32 points: two 16-point tiles */
+            float gme = 0.0f;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                float ug[D], ug8[D];
+                for (int d = 0; d < D; ++d) {
+                    ug[d] = __shfl_sync(0xffffffffu, u[d], 16 * half + g);
+                    ug8[d] = __shfl_sync(0xffffffffu, u[d], 16 * half + g + 8);
+                }
+                Acts<D> a;
+                features_tile<D>(ug, ug8, a.F);
+                float out[2];
+                forward_tile<D>(P, a, out);
+                /* point p = 16*half + r lives in lanes 4*(r%8).. as out[r/8] */
+                const int r = lane - 16 * half;
+                const float o0 = __shfl_sync(0xffffffffu, out[0], 4 * (lane & 7));
+                const float o1 = __shfl_sync(0xffffffffu, out[1], 4 * (lane & 7));
+                if (r >= 0 && r < 16) gme = (r < 8) ? o0 : o1;
+            }
+            if (valid) {
+                const double fd = fv[0], rd = (double)fv[0] - (double)gme;
+                sf += fd;
+                sf2 += fd * fd;
+                sr += rd;
+                sr2 += rd * rd;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sf += __shfl_xor_sync(0xffffffffu, sf, o);
+            sf2 += __shfl_xor_sync(0xffffffffu, sf2, o);
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            sr2 += __shfl_xor_sync(0xffffffffu, sr2, o);
+        }
+        if (lane == 0) {
+            const double n = (double)c.spp;
+            const double scale = (double)c.factor * (double)vol;
+            const double est_cv = scale * ((double)integral[bin] + sr / n);
+            const double est_mc = scale * sf / n;
+            const double var_r = sr2 / n - (sr / n) * (sr / n), var_f = sf2 / n - (sf / n) * (sf / n);
+            const bool use_mc = c.fallback && var_f < var_r;
+            const float o = (float)(use_mc ? est_mc : est_cv);
+            bins[bin] = o;
+            if (use_mc) atomicAdd(fallback_count, 1u);
+            if (isnan(o)) atomicOr(status, VCU_FLAG_NAN);
+        }
+    }
+}
+
+}  // namespace mlp
+}  // namespace vcu
+
+/* ------------------------------------------------------------------------------------ host side */
+namespace vcu {
+namespace mlp {
+
+constexpr float kGLx[4][4] = {{0.0f, 0.0f, 0.0f, 0.0f},
+                              {-0.5773502691896258f, 0.5773502691896258f, 0.0f, 0.0f},
+                              {-0.7745966692414834f, 0.0f, 0.7745966692414834f, 0.0f},
+                              {-0.8611363115940526f, -0.3399810435848563f, 0.3399810435848563f, 0.8611363115940526f}};
+constexpr float kGLw[4][4] = {{2.0f, 0.0f, 0.0f, 0.0f},
+                              {1.0f, 1.0f, 0.0f, 0.0f},
+                              {0.5555555555555556f, 0.8888888888888888f, 0.5555555555555556f, 0.0f},
+                              {0.3478548451374538f, 0.6521451548625461f, 0.6521451548625461f, 0.3478548451374538f}};
+
+/* He-uniform initial weights from a SplitMix64 stream, zero biases */
+inline void init_params(int d, uint64_t seed, float* theta) {
+    uint64_t s = seed ^ 0x243F6A8885A308D3ull;
+    auto next = [&]() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int i = 0; i < n_params(d); ++i) theta[i] = 0.0f;
+    for (int l = 0; l < 4; ++l) {
+        const int in = layer_in(l, d);
+        const double lim = std::sqrt(6.0 / in);
+        for (int i = 0; i < in * WIDTH; ++i) theta[w_off(l, d) + i] = (float)((2.0 * next() - 1.0) * lim);
+    }
+    const double lim = std::sqrt(6.0 / WIDTH);
+    for (int i = 0; i < WIDTH; ++i) theta[w4_off(d) + i] = (float)((2.0 * next() - 1.0) * lim);
+}
+
+struct State {
+    float *theta, *m, *v, *grad;
+    char* packed;
+    uint32_t* step;
+    float* integral;
+    uint32_t* fallback;
+};
+
+template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, State& s) {
+    const size_t np = n_params(D), ng = np; /* gradient vector has one entry per parameter */
+    size_t o = 0;
+    auto a = [&](size_t bytes) {
+        const size_t at = o;
+        o = (o + bytes + 255) & ~size_t(255);
+        return at;
+    };
+    const size_t o_theta = a(np * 4), o_m = a(np * 4), o_v = a(np * 4), o_g = a(ng * 4), o_p = a(pack_bytes(D)),
+                 o_s = a(64), o_i = a(nbins * 4), o_f = a(64);
+    int rc = ensure(ctx, ctx->scratch, o);
+    if (rc) return rc;
+    char* b = static_cast<char*>(ctx->scratch.ptr);
+    s.theta = reinterpret_cast<float*>(b + o_theta);
+    s.m = reinterpret_cast<float*>(b + o_m);
+    s.v = reinterpret_cast<float*>(b + o_v);
+    s.grad = reinterpret_cast<float*>(b + o_g);
+    s.packed = b + o_p;
+    s.step = reinterpret_cast<uint32_t*>(b + o_s);
+    s.integral = reinterpret_cast<float*>(b + o_i);
+    s.fallback = reinterpret_cast<uint32_t*>(b + o_f);
+    return VCU_OK;
+}
+
+template <int D> int upload_params(vcu_ctx* ctx, const State& s, const float* theta_host, uint32_t& launches) {
+    const size_t np = n_params(D);
+    VCU_CUDA(ctx, cudaMemcpyAsync(s.theta, theta_host, np * 4, cudaMemcpyHostToDevice, ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.m, 0, np * 4, ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.v, 0, np * 4, ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.grad, 0, np * 4, ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.packed, 0, pack_bytes(D), ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.step, 0, 64, ctx->stream));
+    k_mlp_pack<D><<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(s.theta, s.packed);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+    return VCU_OK;
+}
+
+template <int D> int set_smem_train(vcu_ctx* ctx) {
+    const int tb = train_smem_bytes<D>();
+    if ((size_t)tb > ctx->smem_optin) return fail(ctx, VCU_UNSUPPORTED, "training block does not fit in shared memory");
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_train<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb));
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_integral<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem_fwd_bytes<D>()));
+    return VCU_OK;
+}
+
+template <class F, int D>
+int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_learned& opt, float* d_bins,
+            float* d_integral, vcu_learned_report* report, uint32_t& launches) {
+    State s;
+    int rc = alloc_state<D>(ctx, g.nbins, s);
+    if (rc) return rc;
+    if ((rc = set_smem_train<D>(ctx))) return rc;
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_residual<F, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem_fwd_bytes<D>()));
+    std::vector<float> theta(n_params(D));
+    init_params(D, opt.seed, theta.data());
+    if ((rc = upload_params<D>(ctx, s, theta.data(), launches))) return rc;
+    /* 1. training: one graph of (train, adam, step) replayed train_steps times */
+    TrainCfg tc{};
+    for (int d = 0; d < D; ++d) {
+        tc.r.rmin[d] = p->range_min[d];
+        tc.r.rmax[d] = p->range_max[d];
+    }
+    tc.k0 = (uint32_t)(opt.seed * 0x9E3779B97F4A7C15ull >> 32);
+    tc.k1 = (uint32_t)(opt.seed >> 32) ^ 0x51ED270Bu;
+    const unsigned train_blocks = (unsigned)ctx->sm_count;
+    const uint32_t per_block = TRAIN_WARPS * 32;
+    tc.tiles_per_warp = (opt.batch + train_blocks * per_block - 1) / (train_blocks * per_block);
+    const uint64_t batch = (uint64_t)tc.tiles_per_warp * train_blocks * per_block;
+    tc.scale = (float)(2.0 / (double)batch);
+    /* the step's training points live in the context's input buffer */
+    if ((rc = ensure(ctx, ctx->in, batch * (D + 1) * 4 + 1024))) return rc;
+    float* su = static_cast<float*>(ctx->in.ptr);
+    float* sy = su + batch * D;
+    tc.u_in = su;
+    tc.y_in = sy;
+    tc.npts = batch;
+    AdamCfg ac{opt.learning_rate, 0.9f, 0.999f, 1e-8f, n_params(D)};
+    cudaEvent_t e0 = ctx->ev_tune[0], e1 = ctx->ev_tune[1];
+    VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    if (opt.train_steps > 0) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        VCU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        k_mlp_samples<F, D><<<(unsigned)((batch + 255) / 256), 256, 0, ctx->stream>>>(f, tc, batch, su, sy, s.step);
+        k_mlp_train<D><<<train_blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.grad);
+        k_mlp_adam<D><<<(unsigned)((n_params(D) + 255) / 256), 256, 0, ctx->stream>>>(ac, s.theta, s.m, s.v, s.grad,
+                                                                                       s.step, s.packed);
+        k_mlp_step_inc<<<1, 1, 0, ctx->stream>>>(s.step);
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        if (ie != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+        }
+        for (uint32_t i = 0; i < opt.train_steps; ++i) {
+            const cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
+            if (le != cudaSuccess) {
+                cudaGraphExecDestroy(exec);
+                cudaGraphDestroy(graph);
+                return cuda_fail(ctx, le, "cudaGraphLaunch");
+            }
+        }
+        launches += 4 * opt.train_steps;
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+    }
+    VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+    float train_ms = 0.0f;
+    VCU_CUDA(ctx, cudaEventSynchronize(e1));
+    VCU_CUDA(ctx, cudaEventElapsedTime(&train_ms, e0, e1));
+    /* 2. per-bin integral of g */
+    BinCfg bc{};
+    for (int d = 0; d < D; ++d) {
+        bc.r.rmin[d] = p->range_min[d];
+        bc.r.rmax[d] = p->range_max[d];
+    }
+    for (int d = 0; d < p->dimbins; ++d) {
+        bc.drange[d] = g.drange[d];
+        bc.res[d] = g.res[d];
+    }
+    bc.dimbins = p->dimbins;
+    bc.nbins = g.nbins;
+    bc.q = (int)opt.quad_nodes;
+    for (int i = 0; i < 4; ++i) {
+        bc.gl_x[i] = kGLx[bc.q - 1][i];
+        bc.gl_w[i] = kGLw[bc.q - 1][i];
+    }
+    int per_sm = 0;
+    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_integral<D>, FWD_WARPS * 32,
+                                                                smem_fwd_bytes<D>()));
+    const uint64_t need = (g.nbins + FWD_WARPS - 1) / FWD_WARPS;
+    const uint64_t cap = (uint64_t)ctx->sm_count * (per_sm > 0 ? per_sm : 1) * 4;
+    const unsigned blocks = (unsigned)(need < cap ? need : cap);
+    float* integral = d_integral ? d_integral : s.integral;
+    VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    k_mlp_integral<D><<<blocks, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(bc, s.packed, integral);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+    VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+    float integral_ms = 0.0f;
+    VCU_CUDA(ctx, cudaEventSynchronize(e1));
+    VCU_CUDA(ctx, cudaEventElapsedTime(&integral_ms, e0, e1));
+    /* 3. residual */
+    ResidualCfg rcfg{};
+    rcfg.b = bc;
+    rcfg.spp = opt.samples_per_bin;
+    rcfg.k0 = (uint32_t)opt.seed;
+    rcfg.k1 = (uint32_t)(opt.seed >> 32);
+    rcfg.fallback = opt.fallback;
+    rcfg.factor = g.factor;
+    VCU_CUDA(ctx, cudaMemsetAsync(s.fallback, 0, 4, ctx->stream));
+    VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    k_mlp_residual<F, D><<<blocks, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(f, rcfg, s.packed, integral,
+                                                                                        d_bins, s.fallback,
+                                                                                        ctx->d_status);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+    VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+    float residual_ms = 0.0f;
+    VCU_CUDA(ctx, cudaEventSynchronize(e1));
+    VCU_CUDA(ctx, cudaEventElapsedTime(&residual_ms, e0, e1));
+    if (opt.theta_out)
+        VCU_CUDA(ctx, cudaMemcpyAsync(opt.theta_out, s.theta, n_params(D) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (report) {
+        uint32_t fb = 0;
+        VCU_CUDA(ctx, cudaMemcpy(&fb, s.fallback, 4, cudaMemcpyDeviceToHost));
+        report->fallback_bins = fb;
+        report->train_ms = train_ms;
+        report->integral_ms = integral_ms;
+        report->residual_ms = residual_ms;
+    }
+    return VCU_OK;
+}
+
+/* forward (and gradient) of given points with given parameters: the gradient check */
+template <int D>
+int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, int64_t npts, float* out, float* grad,
+              uint32_t& launches) {
+    State s;
+    int rc = alloc_state<D>(ctx, 1, s);
+    if (rc) return rc;
+    if ((rc = set_smem_train<D>(ctx))) return rc;
+    if ((rc = upload_params<D>(ctx, s, theta, launches))) return rc;
+    const size_t in_bytes = (size_t)npts * (D + 2) * 4;
+    if ((rc = ensure(ctx, ctx->in, in_bytes + 1024))) return rc;
+    float* du = static_cast<float*>(ctx->in.ptr);
+    float* dy = du + (size_t)npts * D;
+    float* dout = dy + npts;
+    VCU_CUDA(ctx, cudaMemcpyAsync(du, u, (size_t)npts * D * 4, cudaMemcpyHostToDevice, ctx->stream));
+    if (y) VCU_CUDA(ctx, cudaMemcpyAsync(dy, y, (size_t)npts * 4, cudaMemcpyHostToDevice, ctx->stream));
+    else VCU_CUDA(ctx, cudaMemsetAsync(dy, 0, (size_t)npts * 4, ctx->stream));
+    TrainCfg tc{};
+    tc.tiles_per_warp = 1;
+    tc.u_in = du;
+    tc.y_in = dy;
+    tc.out = dout;
+    tc.npts = (uint64_t)npts;
+    tc.scale = (float)(2.0 / (double)npts);
+    const unsigned blocks = (unsigned)((npts + TRAIN_WARPS * 32 - 1) / (TRAIN_WARPS * 32));
+    k_mlp_train<D><<<blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.grad);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+    VCU_CUDA(ctx, cudaMemcpyAsync(out, dout, (size_t)npts * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad) {
+        /* the kernel's gradient vector follows its own order (W0..W3, b0..b3, w4, b4): map to parameters */
+        std::vector<float> gk(n_params(D));
+        VCU_CUDA(ctx, cudaMemcpyAsync(gk.data(), s.grad, gk.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const int a = fin(D) * WIDTH, hid = WIDTH * WIDTH;
+        for (int i = 0; i < n_params(D); ++i) {
+            int pidx;
+            if (i < a) pidx = w_off(0, D) + i;
+            else if (i < a + 3 * hid) pidx = w_off(1 + (i - a) / hid, D) + (i - a) % hid;
+            else if (i < a + 3 * hid + 4 * WIDTH) pidx = b_off((i - a - 3 * hid) / WIDTH, D) + (i - a - 3 * hid) % WIDTH;
+            else pidx = w4_off(D) + (i - a - 3 * hid - 4 * WIDTH);
+            grad[pidx] = gk[i];
+        }
+    }
+    return VCU_OK;
+}
+
+}  // namespace mlp
+
+int run_learned(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_learned& opt, float* d_bins,
+                float* d_integral, vcu_learned_report* report, uint32_t& launches) {
+    return with_integrand(ctx, p->f, p->dim, [&](const auto& f) -> int {
+        using F = std::decay_t<decltype(f)>;
+        if constexpr (F::CH != 1) {
+            return fail(ctx, VCU_UNSUPPORTED, "the learned control variate is built for scalar integrands");
+        } else if constexpr (F::DIM == 6) {
+            switch (p->dim) {
+            case 2: return mlp::learned<F, 2>(ctx, f, p, g, opt, d_bins, d_integral, report, launches);
+            case 3: return mlp::learned<F, 3>(ctx, f, p, g, opt, d_bins, d_integral, report, launches);
+            case 5: return mlp::learned<F, 5>(ctx, f, p, g, opt, d_bins, d_integral, report, launches);
+            default: return fail(ctx, VCU_UNSUPPORTED, "the learned control variate is built for 2, 3 and 5 dimensions");
+            }
+        } else if constexpr (F::DIM == 2 || F::DIM == 3 || F::DIM == 5) {
+            return mlp::learned<F, F::DIM>(ctx, f, p, g, opt, d_bins, d_integral, report, launches);
+        } else {
+            return fail(ctx, VCU_UNSUPPORTED, "the learned control variate is built for 2, 3 and 5 dimensions");
+        }
+    });
+}
+
+int run_mlp_eval(vcu_ctx* ctx, int dim, const float* theta, const float* u, const float* y, int64_t npts, float* out,
+                 float* grad, uint32_t& launches) {
+    switch (dim) {
+    case 2: return mlp::eval_grad<2>(ctx, theta, u, y, npts, out, grad, launches);
+    case 3: return mlp::eval_grad<3>(ctx, theta, u, y, npts, out, grad, launches);
+    case 5: return mlp::eval_grad<5>(ctx, theta, u, y, npts, out, grad, launches);
+    default: return fail(ctx, VCU_UNSUPPORTED, "network dimension must be 2, 3 or 5");
+    }
+}
+
+}  // namespace vcu

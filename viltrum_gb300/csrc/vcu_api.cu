@@ -82,9 +82,126 @@ static int out_buffer(vcu_ctx* ctx, const vcu_problem* p, float* user, size_t by
     return VCU_OK;
 }
 
+int batch_launch(vcu_ctx* ctx, uint32_t& launches) {
+    vcu_batch_state& B = ctx->batch;
+    if (B.exec) {
+        VCU_CUDA(ctx, cudaGraphLaunch(B.exec, ctx->stream));
+    } else {
+        /* the legacy default stream cannot be captured: launch directly */
+        VCU_CUDA(ctx, cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), ctx->stream));
+        void* args[] = {&B.cfg, &B.items, &B.functors, &B.queue, &B.vals, &B.ranges,
+                        &B.vols, &B.heap, &B.results, &B.item_ns, &ctx->d_status};
+        VCU_CUDA(ctx, cudaLaunchKernel(B.kernel, dim3(B.blocks), dim3(B.threads), args, B.smem, ctx->stream));
+    }
+    ++launches;
+    return VCU_OK;
+}
+
+int batch_capture(vcu_ctx* ctx, uint32_t& launches) {
+    vcu_batch_state& B = ctx->batch;
+    if (B.exec) {
+        cudaGraphExecDestroy(B.exec);
+        B.exec = nullptr;
+    }
+    B.valid = true;
+    if (ctx->stream == nullptr) return batch_launch(ctx, launches);
+    VCU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    void* args[] = {&B.cfg, &B.items, &B.functors, &B.queue, &B.vals, &B.ranges,
+                    &B.vols, &B.heap, &B.results, &B.item_ns, &ctx->d_status};
+    cudaError_t e1 = cudaMemsetAsync(B.queue, 0, sizeof(uint32_t), ctx->stream);
+    cudaError_t e2 = cudaLaunchKernel(B.kernel, dim3(B.blocks), dim3(B.threads), args, B.smem, ctx->stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e3 = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        B.valid = false;
+        cudaGetLastError();
+        return cuda_fail(ctx, e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3), "batch graph capture");
+    }
+    cudaError_t e4 = cudaGraphInstantiate(&B.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e4 != cudaSuccess) {
+        B.exec = nullptr;
+        B.valid = false;
+        return cuda_fail(ctx, e4, "cudaGraphInstantiate");
+    }
+    return batch_launch(ctx, launches);
+}
+
+/* copy the batch results (and item times) out after a launch */
+static int batch_finish(vcu_ctx* ctx, CallScope& scope, float* results, int32_t results_mem, vcu_batch_report* report) {
+    vcu_batch_state& B = ctx->batch;
+    const size_t bytes = B.n * sizeof(float);
+    VCU_CUDA(ctx, cudaMemcpyAsync(results, B.results, bytes,
+                                  results_mem == VCU_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    std::vector<uint64_t> ns;
+    if (report && report->item_ms) {
+        ns.resize(B.n);
+        VCU_CUDA(ctx, cudaMemcpyAsync(ns.data(), B.item_ns, B.n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    const int rc = scope.end(B.evaluations, B.regions);
+    if (report) {
+        report->threads = B.threads;
+        report->blocks = B.blocks;
+        report->nested_regions = B.regions;
+        if (report->item_ms)
+            for (uint64_t i = 0; i < B.n; ++i) report->item_ms[i] = (float)((double)ns[i] * 1e-6);
+    }
+    return rc;
+}
+
 }  // namespace vcu
 
 using namespace vcu;
+
+extern "C" int vcu_integrate_batch(vcu_ctx* ctx, int32_t kind, const vcu_nested* nested, const vcu_batch_item* items,
+                                   uint64_t n_items, float* results, int32_t results_mem, vcu_batch_report* report,
+                                   vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    if (!items || !results || n_items == 0) return fail(ctx, VCU_INVALID_ARG, "empty batch or null results");
+    if (n_items > 0x7fffffffull) return fail(ctx, VCU_INVALID_ARG, "too many batch items");
+    if (results_mem != VCU_MEM_HOST && results_mem != VCU_MEM_DEVICE) return fail(ctx, VCU_INVALID_ARG, "bad results_mem");
+    vcu_nested n{};
+    if (nested) {
+        n = *nested;
+    } else {
+        n.rule_hi = VCU_RULE_SIMPSON;
+        n.rule_lo = VCU_RULE_TRAPEZOIDAL;
+        n.heuristic = VCU_HEUR_DEFAULT;
+        n.metric = VCU_METRIC_ABSOLUTE;
+        n.size_weight = 1e-5;
+        n.min_size = 1e-37;
+        n.min_val = 1e-37;
+    }
+    CallScope scope{ctx, stats};
+    int rc = scope.begin();
+    if (rc) return rc;
+    ctx->batch.valid = false;
+    if (n.rule_hi == VCU_RULE_SIMPSON && n.rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_batch_st(ctx, kind, n, items, n_items, scope.launches);
+    else if (n.rule_hi == VCU_RULE_BOOLE && n.rule_lo == VCU_RULE_SIMPSON)
+        rc = run_batch_bs(ctx, kind, n, items, n_items, scope.launches);
+    else if (n.rule_hi == VCU_RULE_BOOLE && n.rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_batch_bt(ctx, kind, n, items, n_items, scope.launches);
+    else
+        rc = fail(ctx, VCU_INVALID_ARG, "nested rules must be (simpson, trapezoidal), (boole, simpson) or (boole, trapezoidal)");
+    if (rc) return rc;
+    return batch_finish(ctx, scope, results, results_mem, report);
+}
+
+extern "C" int vcu_integrate_batch_resident(vcu_ctx* ctx, float* results, int32_t results_mem,
+                                            vcu_batch_report* report, vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    if (!ctx->batch.valid) return fail(ctx, VCU_INVALID_ARG, "no batch has been uploaded on this context");
+    if (!results) return fail(ctx, VCU_INVALID_ARG, "null results");
+    if (results_mem != VCU_MEM_HOST && results_mem != VCU_MEM_DEVICE) return fail(ctx, VCU_INVALID_ARG, "bad results_mem");
+    CallScope scope{ctx, stats};
+    int rc = scope.begin();
+    if (rc) return rc;
+    if ((rc = batch_launch(ctx, scope.launches))) return rc;
+    return batch_finish(ctx, scope, results, results_mem, report);
+}
 
 extern "C" int vcu_abi_version(void) { return VCU_ABI_VERSION; }
 
@@ -136,7 +253,8 @@ extern "C" int vcu_destroy(vcu_ctx* ctx) {
     if (!ctx) return VCU_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (vcu_buffer* b : {&ctx->out, &ctx->aux, &ctx->in, &ctx->scratch})
+    if (ctx->batch.exec) cudaGraphExecDestroy(ctx->batch.exec);
+    for (vcu_buffer* b : {&ctx->out, &ctx->aux, &ctx->in, &ctx->scratch, &ctx->batch_in, &ctx->batch_pool})
         if (b->ptr) cudaFree(b->ptr);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
@@ -331,4 +449,51 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
     const uint64_t evals = (uint64_t)(sd + (double)iterations * (S - 1) * sd1) + g.nbins * cv->samples_per_bin;
     return scope.end(evals, iterations + 1);
+}
+
+extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_learned* opt, float* bins,
+                                            float* network_integral, vcu_learned_report* report, vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    BinGrid g;
+    int rc = make_grid(ctx, p, g);
+    if (rc) return rc;
+    if (!opt || !bins) return fail(ctx, VCU_INVALID_ARG, "null options or bins");
+    if (opt->quad_nodes < 1 || opt->quad_nodes > 4) return fail(ctx, VCU_INVALID_ARG, "quad_nodes must be 1..4");
+    if (opt->samples_per_bin == 0 || opt->samples_per_bin > 0xffffffffull)
+        return fail(ctx, VCU_INVALID_ARG, "samples per bin must be 1..2^32-1");
+    if (opt->train_steps > 0 && opt->batch == 0) return fail(ctx, VCU_INVALID_ARG, "batch must be positive");
+    if (vcu_channels(p->f.kind) != 1) return fail(ctx, VCU_UNSUPPORTED, "learned control variates take scalar integrands");
+    CallScope scope{ctx, stats};
+    if ((rc = scope.begin())) return rc;
+    float *dbins = bins, *dint = network_integral;
+    const size_t bbytes = g.nbins * 4;
+    if (p->mem == VCU_MEM_HOST) {
+        if ((rc = ensure(ctx, ctx->out, 2 * bbytes + 512))) return rc;
+        dbins = static_cast<float*>(ctx->out.ptr);
+        dint = network_integral ? reinterpret_cast<float*>(static_cast<char*>(ctx->out.ptr) + ((bbytes + 255) & ~size_t(255)))
+                                : nullptr;
+    }
+    if ((rc = run_learned(ctx, p, g, *opt, dbins, dint, report, scope.launches))) return rc;
+    if (p->mem == VCU_MEM_HOST) {
+        VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (network_integral)
+            VCU_CUDA(ctx, cudaMemcpyAsync(network_integral, dint, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    double nodes = 1.0;
+    for (int d = 0; d < p->dim; ++d) nodes *= opt->quad_nodes;
+    (void)nodes;
+    const uint64_t evals = (uint64_t)opt->train_steps * opt->batch + g.nbins * opt->samples_per_bin;
+    return scope.end(evals, 0);
+}
+
+extern "C" int vcu_mlp_eval(vcu_ctx* ctx, int32_t dim, const float* theta, const float* u, const float* y,
+                            int64_t npts, float* out, float* grad) {
+    if (!ctx) return VCU_INVALID_ARG;
+    if (!theta || !u || !out || npts <= 0) return fail(ctx, VCU_INVALID_ARG, "bad vcu_mlp_eval arguments");
+    if (grad && !y) return fail(ctx, VCU_INVALID_ARG, "the gradient needs targets y");
+    CallScope scope{ctx, nullptr};
+    int rc = scope.begin();
+    if (rc) return rc;
+    if ((rc = run_mlp_eval(ctx, dim, theta, u, y, npts, out, grad, scope.launches))) return rc;
+    return scope.end((uint64_t)npts, 0);
 }

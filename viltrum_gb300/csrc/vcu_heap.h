@@ -66,4 +66,87 @@ template <class K, class P> VCU_HEAP_HD void heap_pop(K* key, P* pay, int len) {
     heap_sift_up(key, pay, hole, 0, vk, vp);
 }
 
+/* The same two algorithms on packed (key, payload) entries, for heaps too large for shared
+ * memory, through an accessor:
+ *   HeapArray: element i at h[i];
+ *   HeapSplit: elements below `cap` (odd) at top[i] (shared memory), the others at rest[i] (global).
+ * In both, the two children of any element (2i+1, 2i+2) form one 16-byte aligned pair (h + 1,
+ * top + 1 and rest + 1 are 16-byte aligned, and with an odd cap no pair straddles the two arrays),
+ * which the device reads with a single load. */
+struct HeapEntry {
+    float key;
+    int pay;
+};
+
+VCU_HEAP_HD void heap_load_pair(const HeapEntry* p, HeapEntry& l, HeapEntry& r) {
+#if defined(__CUDA_ARCH__)
+    const float4 pair = *reinterpret_cast<const float4*>(p);
+    l = HeapEntry{pair.x, __float_as_int(pair.y)};
+    r = HeapEntry{pair.z, __float_as_int(pair.w)};
+#else
+    l = p[0];
+    r = p[1];
+#endif
+}
+
+struct HeapArray {
+    HeapEntry* h;
+    VCU_HEAP_HD HeapEntry get(int i) const { return h[i]; }
+    VCU_HEAP_HD void set(int i, HeapEntry e) const { h[i] = e; }
+    VCU_HEAP_HD void pair(int left, HeapEntry& l, HeapEntry& r) const { heap_load_pair(h + left, l, r); }
+};
+
+struct HeapSplit {
+    HeapEntry* top;
+    HeapEntry* rest;
+    int cap;
+    VCU_HEAP_HD HeapEntry get(int i) const { return i < cap ? top[i] : rest[i]; }
+    VCU_HEAP_HD void set(int i, HeapEntry e) const {
+        if (i < cap) top[i] = e;
+        else rest[i] = e;
+    }
+    VCU_HEAP_HD void pair(int left, HeapEntry& l, HeapEntry& r) const {
+        heap_load_pair((left < cap ? top : rest) + left, l, r);
+    }
+};
+
+template <class A> VCU_HEAP_HD void heap_sift_up_entries(const A& h, int hole, HeapEntry v) {
+    int parent = (hole - 1) / 2;
+    while (hole > 0) {
+        const HeapEntry pe = h.get(parent);
+        if (!(pe.key < v.key)) break;
+        h.set(hole, pe);
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    h.set(hole, v);
+}
+
+template <class A> VCU_HEAP_HD void heap_push_entries(const A& h, int len) {
+    heap_sift_up_entries(h, len - 1, h.get(len - 1));
+}
+
+template <class A> VCU_HEAP_HD void heap_pop_entries(const A& h, int len) {
+    if (len <= 1) return;
+    const int n = len - 1;
+    const HeapEntry v = h.get(n);
+    h.set(n, h.get(0));
+    int hole = 0, child = 0;
+    while (child < (n - 1) / 2) {
+        child = 2 * (child + 1);
+        HeapEntry left, right;
+        h.pair(child - 1, left, right);
+        const bool take_left = right.key < left.key;
+        if (take_left) child--;
+        h.set(hole, take_left ? left : right);
+        hole = child;
+    }
+    if ((n & 1) == 0 && child == (n - 2) / 2) {
+        child = 2 * (child + 1);
+        h.set(hole, h.get(child - 1));
+        hole = child - 1;
+    }
+    heap_sift_up_entries(h, hole, v);
+}
+
 }  // namespace vcu

@@ -9,7 +9,9 @@
 
 #include <cstdio>
 #include <cstring>
+#include <cmath>
 #include <string>
+#include <vector>
 
 #include "../../include/vcu_integrands.h"
 #include "../../include/viltrum_cuda.h"
@@ -30,6 +32,39 @@ struct vcu_tuned {
     int32_t value;
 };
 
+namespace vcu {
+namespace batch {
+/* configuration of the batched-integral kernel shared by all its items */
+struct Cfg {
+    int32_t n_items;
+    int32_t heuristic, relative;
+    float min_val_f;
+    double size_weight, min_size;
+    int32_t hcap; /* heap elements kept in shared memory (odd) */
+    int32_t pad;
+};
+}  // namespace batch
+}  // namespace vcu
+
+/* device state of the batch last uploaded on a context: the kernel, its launch shape, the
+ * captured graph (queue reset + persistent launch) and the buffers it reads and writes */
+struct vcu_batch_state {
+    bool valid = false;
+    int kind = 0, sh = 0, sl = 0;
+    uint64_t n = 0;
+    vcu::batch::Cfg cfg{};
+    void* kernel = nullptr;
+    size_t smem = 0;
+    unsigned blocks = 0;
+    int threads = 0;
+    uint64_t evaluations = 0, regions = 0;
+    char *items = nullptr, *functors = nullptr, *vals = nullptr, *ranges = nullptr, *vols = nullptr, *heap = nullptr;
+    float* results = nullptr;
+    uint64_t* item_ns = nullptr;
+    uint32_t* queue = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
 struct vcu_ctx {
     int device = 0;
     int tune = 1;                 /* time launch-configuration candidates on first use */
@@ -43,6 +78,8 @@ struct vcu_ctx {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     uint32_t* d_status = nullptr; /* one word of device status flags */
     vcu_buffer out, aux, in, scratch;
+    vcu_buffer batch_in, batch_pool; /* owned by the batched-integral path only */
+    vcu_batch_state batch;
     std::string last_error;
 };
 
@@ -186,6 +223,19 @@ int run_nested_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vc
                   float* d_bins, int32_t* d_trace, uint32_t& launches);
 int run_eval(vcu_ctx* ctx, const vcu_integrand& f, int dim, const float* d_x, int64_t npts, float* d_out,
              uint32_t& launches);
+int run_learned(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_learned& opt, float* d_bins,
+                float* d_integral, vcu_learned_report* report, uint32_t& launches);
+int run_mlp_eval(vcu_ctx* ctx, int dim, const float* theta, const float* u, const float* y, int64_t npts, float* out,
+                 float* grad, uint32_t& launches);
+int run_batch_st(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_item* items, uint64_t count,
+                 uint32_t& launches);
+int run_batch_bs(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_item* items, uint64_t count,
+                 uint32_t& launches);
+int run_batch_bt(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_item* items, uint64_t count,
+                 uint32_t& launches);
+/* (re)capture the batch's queue reset + launch as a graph and launch it; launch it again */
+int batch_capture(vcu_ctx* ctx, uint32_t& launches);
+int batch_launch(vcu_ctx* ctx, uint32_t& launches);
 int run_cv_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
               const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
               uint32_t& launches);

@@ -107,6 +107,33 @@ template <> struct Rule<5> { /* boole */
     }
 };
 
+/* subrange() as the reference computes it for float nodes (rules.h:41-44, 96-100, 288-293): float
+ * coefficients, then the Horner steps in double ("c[k]*b/5.0" is a float product divided in double)
+ * and the difference of the two ends rounded once to float.  Used where bin n region can be a short
+ * piece of a large region (control variates), so the two Horner values nearly cancel. */
+template <int S> __device__ __forceinline__ double horner_int_ref(const float* c, float t);
+template <> __device__ __forceinline__ double horner_int_ref<2>(const float* c, float t) {
+    double r = __dadd_rn(__ddiv_rn((double)vmul(c[1], t), 2.0), (double)c[0]);
+    return __dmul_rn(r, (double)t);
+}
+template <> __device__ __forceinline__ double horner_int_ref<3>(const float* c, float t) {
+    double r = __dadd_rn(__ddiv_rn((double)vmul(c[2], t), 3.0), __ddiv_rn((double)c[1], 2.0));
+    r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
+    return __dmul_rn(r, (double)t);
+}
+template <> __device__ __forceinline__ double horner_int_ref<5>(const float* c, float t) {
+    double r = __dadd_rn(__ddiv_rn((double)vmul(c[4], t), 5.0), __ddiv_rn((double)c[3], 4.0));
+    r = __dadd_rn(__dmul_rn(r, (double)t), __ddiv_rn((double)c[2], 3.0));
+    r = __dadd_rn(__dmul_rn(r, (double)t), __ddiv_rn((double)c[1], 2.0));
+    r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
+    return __dmul_rn(r, (double)t);
+}
+template <int S> __device__ __forceinline__ float subrange_ref(float a, float b, const float* p) {
+    float c[S];
+    Rule<S>::coefficients(p, c);
+    return __double2float_rn(__dsub_rn(horner_int_ref<S>(c, b), horner_int_ref<S>(c, a)));
+}
+
 /* error metrics (src/nested/error-metric.h): absolute |L-H|, relative |L-H|/max(|H|,|L|) unless
  * max(|H|,|L|) < min_val */
 __device__ __forceinline__ float metric_value(int relative, float min_val, float H, float L) {

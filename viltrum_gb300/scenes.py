@@ -79,6 +79,26 @@ def halfspace(seed: int, dim: int) -> np.ndarray:
     return np.array([float(dim)] + a + b + list(n) + [c], dtype=np.float32)
 
 
+def batch_items(n: int, seed: int = 11, budget_lo: int = 256, budget_hi: int = 65536, dims=(2, 6),
+                methods=(0, 1)) -> list[dict]:
+    """The batched-integrals workload: n independent integrals over [0,1]^dim, dim uniform in
+    dims[0]..dims[1], integrand the half-space family (seeded per item), method drawn uniformly
+    from `methods` (0 Monte Carlo, 1 adaptive nested), budget log-uniform in [budget_lo, budget_hi]
+    (samples or regions), Monte Carlo seed per item."""
+    g = SplitMix64(seed)
+    items = []
+    lo, hi = np.log(budget_lo), np.log(budget_hi)
+    for i in range(n):
+        dim = dims[0] + min(int(g.uniform() * (dims[1] - dims[0] + 1)), dims[1] - dims[0])
+        method = methods[min(int(g.uniform() * len(methods)), len(methods) - 1)]
+        budget = int(round(float(np.exp(lo + (hi - lo) * g.uniform()))))
+        budget = max(budget_lo, min(budget_hi, budget))
+        item_seed = g.next_u64() & 0xFFFFFFFF
+        items.append(dict(dim=dim, method=method, budget=budget, seed=item_seed,
+                          params=halfspace(seed * 1000003 + i, dim), rmin=[0.0] * dim, rmax=[1.0] * dim))
+    return items
+
+
 def occluded_scene5(seed: int = 7, n_gauss: int = 64, n_disk: int = 32, n_box: int = 128) -> np.ndarray:
     """scene2 followed by n_box occluder boxes: centre ~ U[0,1]^3, half-size ~ U(0.01,0.08)^3."""
     s = list(scene2(seed, n_gauss, n_disk).astype(np.float64))
