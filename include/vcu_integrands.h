@@ -193,6 +193,11 @@ constexpr int kMaxGauss = 64;
 constexpr int kMaxDisk = 32;
 constexpr int kMaxBox = 128;
 constexpr int kMaxHalfspaceDim = 6;
+#if defined(__CUDA_ARCH__)
+#define VCU_UNROLL_HS _Pragma("unroll")
+#else
+#define VCU_UNROLL_HS
+#endif
 
 /* ---------------------------------------------------------------- functors
  * Each functor: static DIM (compile-time arity) and CH (value channels), a host-side
@@ -367,15 +372,19 @@ struct Halfspace {
         return 0;
     }
     VCU_HD void operator()(const float* x, float* out) const {
+        /* loops unrolled to the maximum arity and predicated, so that x[] stays in registers */
         float dot = 0.0f;
-        for (int i = 0; i < dim; ++i) dot = vfma(nrm[i], x[i], dot);
+        VCU_UNROLL_HS
+        for (int i = 0; i < kMaxHalfspaceDim; ++i)
+            if (i < dim) dot = vfma(nrm[i], x[i], dot);
         if (!(dot < c)) {
             out[0] = 0.0f;
             return;
         }
         float v = 1.0f;
-        for (int i = 0; i < dim; ++i)
-            v = vmul(v, vmul(vexp(-vmul(a[i], x[i])), vcos(vmul(b[i], x[i]))));
+        VCU_UNROLL_HS
+        for (int i = 0; i < kMaxHalfspaceDim; ++i)
+            if (i < dim) v = vmul(v, vmul(vexp(-vmul(a[i], x[i])), vcos(vmul(b[i], x[i]))));
         out[0] = v;
     }
 };

@@ -175,8 +175,10 @@ int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* n
  * frequency encoding (6 bands), 4 hidden layers of 64, BF16 weights on the tensor cores, FP32
  * accumulation -- trained online (Adam, mean squared error) on `batch` fresh Philox samples of the
  * integrand per step for `train_steps` steps by the library's own forward/backward kernels.  Per
- * bin, the integral of g is taken by Gauss-Legendre quadrature with `quad_nodes` (1..4) nodes per
- * dimension and only f - g is Monte Carlo sampled (`samples_per_bin` Philox points); with
+ * bin, the integral of g is taken by composite Gauss-Legendre quadrature (`quad_cells` equal cells
+ * per dimension, `quad_nodes` (1..4) nodes per cell and dimension) and only f - g is Monte Carlo
+ * sampled (`samples_per_bin` Philox points): the estimate is unbiased up to that quadrature's
+ * error on the network; with
  * `fallback` set, a bin keeps the plain Monte Carlo mean of the same samples when its sample
  * variance is lower than the residual's.  Scalar integrands of dimension 2, 3 or 5.            */
 typedef struct vcu_learned {
@@ -187,7 +189,7 @@ typedef struct vcu_learned {
     float learning_rate;
     uint32_t quad_nodes;      /* Gauss-Legendre nodes per dimension for the integral of g, 1..4 */
     int32_t fallback;         /* 1: per-bin fallback to plain Monte Carlo                       */
-    int32_t reserved;
+    int32_t quad_cells;       /* composite cells per dimension for the integral of g (0 = 1)    */
     float* theta_out;         /* nullable host buffer: receives the trained fp32 parameters
                                  (vcu_mlp_eval layout), e.g. to checkpoint the network        */
 } vcu_learned;

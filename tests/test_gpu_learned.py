@@ -37,12 +37,12 @@ def test_forward_backward_against_fp64_reference(ctx, dim):
         assert np.linalg.norm(gb - rb) <= 3e-2 * np.linalg.norm(rb) + 1e-7
 
 
-def _learned(ctx, kind, params, rmin, rmax, res, spp, seed, steps, fallback=0, q=3, lr=2e-3, batch=32768):
+def _learned(ctx, kind, params, rmin, rmax, res, spp, seed, steps, fallback=0, q=3, lr=2e-3, batch=32768, cells=1):
     p = ctx.problem(kind, params, rmin, rmax, res)
     nb = int(np.prod(res))
     out = np.empty(nb, np.float32)
     integ = np.empty(nb, np.float32)
-    opts = _lib.LearnedOpts(spp, seed, steps, batch, lr, q, fallback, 0)
+    opts = _lib.LearnedOpts(spp, seed, steps, batch, lr, q, fallback, cells)
     st, rep = ctx.learned_control_variates(p, opts, out, integ)
     return out, integ, st, rep
 
@@ -52,11 +52,14 @@ def test_training_gain_over_plain_monte_carlo(ctx):
     inside a bin, so plain per-bin Monte Carlo is noisy) the trained network removes most of the
     variance: the learned estimator's bin RMSE is several times lower than plain Monte Carlo's with
     the same residual samples, and than the untrained network's.  (On fine bins the integrand is
-    nearly constant inside a bin and the gain shrinks: 1.6x at 64x64 after 1600 steps.)"""
+    nearly constant inside a bin and the gain shrinks: 1.6x at 64x64 after 1600 steps.)  The network's
+    integral over a bin uses 4 cells x 4 Gauss-Legendre nodes per dimension: its frequency features
+    reach 32 pi, two periods per 1/8-wide bin."""
     res, spp = [8, 8], 32
     exact = scenes.exact_bins(scenes.WAVE2, None, [0, 0], [1, 1], res)[:, 0]
-    trained, integ, st, rep = _learned(ctx, scenes.WAVE2, None, [0, 0], [1, 1], res, spp, 5, steps=400, lr=3e-3)
-    untrained, _, _, _ = _learned(ctx, scenes.WAVE2, None, [0, 0], [1, 1], res, spp, 5, steps=0)
+    trained, integ, st, rep = _learned(ctx, scenes.WAVE2, None, [0, 0], [1, 1], res, spp, 5, steps=1000, lr=3e-3,
+                                       q=4, cells=4)
+    untrained, _, _, _ = _learned(ctx, scenes.WAVE2, None, [0, 0], [1, 1], res, spp, 5, steps=0, q=4, cells=4)
     p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], res)
     mc = np.empty(8 * 8, np.float32)
     ctx.per_bin_monte_carlo(p, spp, 5, mc)

@@ -104,6 +104,16 @@ __device__ float region_integral_ref(const float* __restrict__ V, const float* A
     return buf[0];
 }
 
+/* fn(integral_constant<int, 0>), ..., fn(integral_constant<int, N-1>): loops whose index must be a
+ * compile-time constant (strides, divisors) */
+template <class Fn, int... I>
+__device__ __forceinline__ void static_for_impl(Fn& fn, std::integer_sequence<int, I...>) {
+    (fn(std::integral_constant<int, I>{}), ...);
+}
+template <int N, class Fn> __device__ __forceinline__ void static_for(Fn fn) {
+    static_for_impl(fn, std::make_integer_sequence<int, N>{});
+}
+
 __device__ __forceinline__ uint64_t globaltimer() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -183,27 +193,32 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
     /* error estimates of the regions whose node values are in R0 (and R1) into EC[r*DIM + d]
      * (region.h:379-418); volumes of slots s0, s1 */
     auto region_errors = [&](int nreg, const float* R0, const float* R1, int s0, int s1) {
-        for (int t = tid; t < nreg * DIM * NL; t += nth) {
-            const int r = t / (DIM * NL), rr = t % (DIM * NL);
-            const int d = rr / NL, J = rr % NL;
-            const float* RV = r ? R1 : R0;
-            float line[S], low[SL];
+        /* line metrics LN[(r*DIM + d)*NL + J]: the line of region r along dimension d whose other
+         * coordinates are J's digits; its nodes are base + i*S^d */
+        static_for<DIM>([&](auto dc) {
+            constexpr int d = decltype(dc)::value;
+            constexpr int PD = ipow(S, d);
+            for (int t = tid; t < nreg * NL; t += nth) {
+                const int r = t >= NL ? 1 : 0;
+                const int J = t - r * NL;
+                const float* RV = (r ? R1 : R0) + (J % PD + (J / PD) * (PD * S));
+                float line[S], low[SL];
 #pragma unroll
-            for (int i = 0; i < S; ++i) line[i] = RV[node_index<DIM, S>(d, J, i)];
+                for (int i = 0; i < S; ++i) line[i] = RV[i * PD];
 #pragma unroll
-            for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
-            LN[t] = metric_value(cfg.relative, cfg.min_val_f, RefRule<S>::scalar(line), RefRule<SL>::scalar(low));
-        }
+                for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+                LN[(r * DIM + d) * NL + J] =
+                    metric_value(cfg.relative, cfg.min_val_f, RefRule<S>::scalar(line), RefRule<SL>::scalar(low));
+            }
+        });
         __syncthreads();
         /* fold dimension 0 of the remaining dimensions with the high rule, one level at a time */
         float* src = LN;
         float* dst = LF;
-        int n = NL;
-#pragma unroll 1
-        for (int level = 0; level < DIM - 1; ++level) {
-            const int m = n / S;
+        static_for<DIM - 1>([&](auto lc) {
+            constexpr int n = NL / ipow(S, decltype(lc)::value), m = n / S;
             for (int t = tid; t < nreg * DIM * m; t += nth) {
-                const int rd = t / m, i = t % m;
+                const int rd = t / m, i = t - rd * m;
                 float tmp[S];
 #pragma unroll
                 for (int j = 0; j < S; ++j) tmp[j] = src[rd * n + i * S + j];
@@ -213,8 +228,7 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
             float* sw = src;
             src = dst;
             dst = sw;
-            n = m;
-        }
+        });
         if (tid < nreg * DIM) EC[tid] = vmul(VOL[(tid / DIM) ? s1 : s0], src[tid]);
         __syncthreads();
     };
@@ -319,51 +333,51 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
         float* V0 = V + (size_t)C0 * SD;
         float* V1 = V + (size_t)C1 * SD;
         /* region.h:345-359 / split.h:13-49: new nodes at the odd positions, parent nodes at the even;
-         * the children are built on chip and copied to the pool for later splits and the final sum */
-        for (int t = tid; t < NNEW + S * NL; t += nth) {
-            if (t < NNEW) {
-                const int q = t / NL, J = t % NL;
-                float x[F::DIM];
+         * the children are built on chip and copied to the pool for later splits and the final sum.
+         * One instance per split dimension, so every stride and divisor is a constant. */
+        auto build_children = [&](auto ddc) {
+            constexpr int DD = decltype(ddc)::value;
+            constexpr int PD = ipow(S, DD);
+            for (int t = tid; t < NNEW + S * NL; t += nth) {
+                const bool fresh = t < NNEW;
+                const int u = fresh ? t : t - NNEW;
+                const int q = u / NL, J = u - q * NL;
+                const int base = J % PD + (J / PD) * (PD * S);
+                float v;
+                int i;
+                if (fresh) {
+                    float x[F::DIM];
 #pragma unroll
-                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
-                int rem = J;
-#pragma unroll
-                for (int e = 0; e < DIM; ++e) {
-                    if (e == dd) continue;
-                    x[e] = CO[e * S + rem % S];
-                    rem /= S;
+                    for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+                    static_for<DIM>([&](auto ec) {
+                        constexpr int e = decltype(ec)::value;
+                        if constexpr (e != DD) {
+                            constexpr int pe = e < DD ? ipow(S, e) : ipow(S, e - 1);
+                            x[e] = CO[e * S + (J / pe) % S];
+                        }
+                    });
+                    x[DD] = CN[q];
+                    float fv[1];
+                    f(x, fv);
+                    v = fv[0];
+                    i = 2 * q + 1;
+                } else {
+                    v = VP[base + q * PD];
+                    i = 2 * q;
                 }
-                x[dd] = CN[q];
-                float v[1];
-                f(x, v);
-                const int i = 2 * q + 1;
                 if (i <= S - 1) {
-                    const int n0 = node_index<DIM, S>(dd, J, i);
-                    VC0[n0] = v[0];
-                    V0[n0] = v[0];
+                    VC0[base + i * PD] = v;
+                    V0[base + i * PD] = v;
                 }
                 if (i >= S - 1) {
-                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
-                    VC1[n1] = v[0];
-                    V1[n1] = v[0];
-                }
-            } else {
-                const int u = t - NNEW;
-                const int m = u / NL, J = u % NL;
-                const int i = 2 * m;
-                const float src = VP[node_index<DIM, S>(dd, J, m)];
-                if (i <= S - 1) {
-                    const int n0 = node_index<DIM, S>(dd, J, i);
-                    VC0[n0] = src;
-                    V0[n0] = src;
-                }
-                if (i >= S - 1) {
-                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
-                    VC1[n1] = src;
-                    V1[n1] = src;
+                    VC1[base + (i - (S - 1)) * PD] = v;
+                    V1[base + (i - (S - 1)) * PD] = v;
                 }
             }
-        }
+        };
+        static_for<DIM>([&](auto dc) {
+            if (dd == decltype(dc)::value) build_children(dc);
+        });
         if (tid == 0) {
             const float pmn = pr[dd], pmx = pr[VCU_MAX_DIM + dd];
             const float half = vdiv(vsub(pmx, pmn), 2.0f);

@@ -5,9 +5,10 @@
  * src/integrator-per-bin-parallel.h:17-35).  Pipeline of vcu_learned_control_variates:
  *  1. train: `train_steps` Adam steps on fresh samples of the integrand (Philox points over the
  *     range, the integrand evaluated by the device) minimising mean (g - f)^2; each step is one
- *     fused forward+backward kernel (k_mlp_train), one Adam kernel that also rewrites the BF16
- *     shared-memory image of the weights, and one counter kernel -- captured once in a CUDA graph
- *     and replayed for all steps;
+ *     sampling kernel, one fused forward+backward kernel (k_mlp_train: every block writes its own
+ *     partial gradient, no atomics), one Adam kernel that sums the partials in a fixed order and
+ *     rewrites the BF16 image of the weights, and one counter kernel -- captured once in a CUDA
+ *     graph and replayed for all steps;
  *  2. k_mlp_integral: per bin, Gauss-Legendre quadrature (q nodes per dimension) of g over the bin;
  *  3. k_mlp_residual: per bin, `samples` Philox points, estimate = integral of g + mean(f - g)
  *     (control variate with weight 1: unbiased up to the quadrature error of the network's
@@ -21,9 +22,13 @@ namespace mlp {
 
 constexpr int TRAIN_WARPS = 8;
 constexpr int FWD_WARPS = 4;
-constexpr int ZS = 16 + 8; /* row stride (bf16) of the transposed per-warp tiles */
+constexpr int ROUND = TRAIN_WARPS * 16; /* points of one block round: a 16-point tile per warp      */
+constexpr int KS = ROUND + 8;           /* bf16 row stride of the block's transposed tiles (bank skew) */
+constexpr int GS = WIDTH + 8;           /* fp32 row stride of the block's dW accumulators            */
+constexpr int SLOT = 4 * WIDTH + WIDTH + 4; /* per-warp sums: db[4][64], dw4[64], db4, pad          */
 /* rows of the transposed activation tile: the widest layer input (features or a hidden layer) */
 __host__ __device__ constexpr int at_rows(int d) { return fin(d) > WIDTH ? fin(d) : WIDTH; }
+__host__ __device__ constexpr int gw_floats(int d) { return (fin(d) + 3 * WIDTH) * GS; }
 
 struct RangeCfg {
     float rmin[VCU_MAX_DIM], rmax[VCU_MAX_DIM];
@@ -32,7 +37,7 @@ struct RangeCfg {
 struct TrainCfg {
     RangeCfg r;
     uint32_t k0, k1;
-    uint32_t tiles_per_warp; /* 32-point chunks per warp */
+    uint32_t rounds;         /* ROUND-point rounds per block */
     float scale;             /* 2 / batch */
     const float* u_in;       /* explicit points (gradient check) or null */
     const float* y_in;
@@ -40,76 +45,80 @@ struct TrainCfg {
     uint64_t npts;           /* explicit points: count */
 };
 
+/* training block: parameter image | dW accumulators (fp32) | per-warp bias/output sums |
+ * transposed activation tile AT[in][ROUND] | transposed dZ tile ZT[64][ROUND] (bf16) */
 template <int D> __host__ __device__ constexpr int train_smem_bytes() {
-    return pack_bytes(D) + (fin(D) * WIDTH + 3 * WIDTH * WIDTH + 4 * WIDTH + WIDTH + 4) * 4 +
-           TRAIN_WARPS * (at_rows(D) + WIDTH) * ZS * 2 + 64;
+    return pack_bytes(D) + (gw_floats(D) + TRAIN_WARPS * SLOT) * 4 + (at_rows(D) + WIDTH) * KS * 2;
 }
 
-/* gradient of layer l's W, b accumulated into shared memory from one 16-point tile */
+/* a warp's 16-point tile of layer inputs (A fragments) -> columns col0..col0+15 of AT[input][point] */
 template <int KT>
-__device__ __forceinline__ void accumulate_dW(__nv_bfloat16* AT, __nv_bfloat16* ZT, const uint32_t (*A)[4],
-                                              const float (*dZ)[4], float* gW, float* gb) {
+__device__ __forceinline__ void stage_A(__nv_bfloat16* AT, const uint32_t (*A)[4], int col0) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    /* store A (points x inputs) transposed: AT[input][point] */
+    __nv_bfloat16* p = AT + col0 + g;
 #pragma unroll
     for (int kt = 0; kt < KT; ++kt) {
         const int c = 16 * kt + 2 * t;
-        AT[(c)*ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][0] & 0xffff));
-        AT[(c + 1) * ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][0] >> 16));
-        AT[(c)*ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][1] & 0xffff));
-        AT[(c + 1) * ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][1] >> 16));
-        AT[(c + 8) * ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][2] & 0xffff));
-        AT[(c + 9) * ZS + g] = __ushort_as_bfloat16((unsigned short)(A[kt][2] >> 16));
-        AT[(c + 8) * ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][3] & 0xffff));
-        AT[(c + 9) * ZS + g + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][3] >> 16));
+        p[c * KS] = __ushort_as_bfloat16((unsigned short)(A[kt][0] & 0xffff));
+        p[(c + 1) * KS] = __ushort_as_bfloat16((unsigned short)(A[kt][0] >> 16));
+        p[c * KS + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][1] & 0xffff));
+        p[(c + 1) * KS + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][1] >> 16));
+        p[(c + 8) * KS] = __ushort_as_bfloat16((unsigned short)(A[kt][2] & 0xffff));
+        p[(c + 9) * KS] = __ushort_as_bfloat16((unsigned short)(A[kt][2] >> 16));
+        p[(c + 8) * KS + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][3] & 0xffff));
+        p[(c + 9) * KS + 8] = __ushort_as_bfloat16((unsigned short)(A[kt][3] >> 16));
     }
-    /* store dZ (points x 64) transposed, as BF16: ZT[unit][point]; db from the same BF16 values */
+}
+
+/* a warp's dZ tile (C fragments, already BF16-valued) -> columns col0.. of ZT[unit][point]; its
+ * column sums (the bias gradient) are added to the warp's own slot db[64] */
+__device__ __forceinline__ void stage_Z(__nv_bfloat16* ZT, const float (*dZ)[4], int col0, float* db) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __nv_bfloat16* p = ZT + col0 + g;
 #pragma unroll
     for (int j = 0; j < NT; ++j) {
         const int c = 8 * j + 2 * t;
-        const __nv_bfloat16 z00 = __float2bfloat16_rn(dZ[j][0]), z01 = __float2bfloat16_rn(dZ[j][1]);
-        const __nv_bfloat16 z10 = __float2bfloat16_rn(dZ[j][2]), z11 = __float2bfloat16_rn(dZ[j][3]);
-        ZT[c * ZS + g] = z00;
-        ZT[(c + 1) * ZS + g] = z01;
-        ZT[c * ZS + g + 8] = z10;
-        ZT[(c + 1) * ZS + g + 8] = z11;
-        float s0 = __bfloat162float(z00) + __bfloat162float(z10);
-        float s1 = __bfloat162float(z01) + __bfloat162float(z11);
+        p[c * KS] = __float2bfloat16_rn(dZ[j][0]);
+        p[(c + 1) * KS] = __float2bfloat16_rn(dZ[j][1]);
+        p[c * KS + 8] = __float2bfloat16_rn(dZ[j][2]);
+        p[(c + 1) * KS + 8] = __float2bfloat16_rn(dZ[j][3]);
+        float s0 = dZ[j][0] + dZ[j][2], s1 = dZ[j][1] + dZ[j][3];
 #pragma unroll
         for (int o = 4; o < 32; o <<= 1) {
             s0 += __shfl_xor_sync(0xffffffffu, s0, o);
             s1 += __shfl_xor_sync(0xffffffffu, s1, o);
         }
         if (g == 0) {
-            atomicAdd(&gb[c], s0);
-            atomicAdd(&gb[c + 1], s1);
+            db[c] += s0;
+            db[c + 1] += s1;
         }
     }
-    __syncwarp();
-    /* dW[input][unit] += AT^T-tile x ZT-tile: M = inputs, N = 64 units, K = 16 points */
+}
+
+/* dW[in][64] += AT . ZT^T over the block's ROUND points (M = inputs, N = 64 units, K = points) on the
+ * tensor cores; each warp owns whole 16x8 output tiles, so the FP32 accumulators in shared memory
+ * are read and written by one warp only (no atomics, fixed summation order) */
+template <int MT>
+__device__ __forceinline__ void block_dW(const __nv_bfloat16* AT, const __nv_bfloat16* ZT, float* gw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int tile = warp; tile < MT * NT; tile += TRAIN_WARPS) {
+        const int mt = tile / NT, j = tile % NT;
+        float* r0 = gw + (16 * mt + g) * GS + 8 * j + 2 * t;
+        float* r1 = r0 + 8 * GS;
+        float c[4] = {r0[0], r0[1], r1[0], r1[1]};
+        const uint32_t* a0 = reinterpret_cast<const uint32_t*>(AT + (16 * mt + g) * KS);
+        const uint32_t* a1 = reinterpret_cast<const uint32_t*>(AT + (16 * mt + g + 8) * KS);
+        const uint32_t* zb = reinterpret_cast<const uint32_t*>(ZT + (8 * j + g) * KS);
 #pragma unroll
-    for (int mt = 0; mt < KT; ++mt) {
-        uint32_t a[4];
-        const uint32_t* r0 = reinterpret_cast<const uint32_t*>(AT + (16 * mt + g) * ZS);
-        const uint32_t* r1 = reinterpret_cast<const uint32_t*>(AT + (16 * mt + g + 8) * ZS);
-        a[0] = r0[t];
-        a[1] = r1[t];
-        a[2] = r0[t + 4];
-        a[3] = r1[t + 4];
-#pragma unroll
-        for (int j = 0; j < NT; ++j) {
-            const uint32_t* zb = reinterpret_cast<const uint32_t*>(ZT + (8 * j + g) * ZS);
-            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            mma16816(c, a, zb[t], zb[t + 4]);
-            float* row0 = gW + (16 * mt + g) * WIDTH + 8 * j + 2 * t;
-            float* row1 = gW + (16 * mt + g + 8) * WIDTH + 8 * j + 2 * t;
-            atomicAdd(row0, c[0]);
-            atomicAdd(row0 + 1, c[1]);
-            atomicAdd(row1, c[2]);
-            atomicAdd(row1 + 1, c[3]);
+        for (int ks = 0; ks < ROUND / 16; ++ks) {
+            const uint32_t a[4] = {a0[8 * ks + t], a1[8 * ks + t], a0[8 * ks + t + 4], a1[8 * ks + t + 4]};
+            mma16816(c, a, zb[8 * ks + t], zb[8 * ks + t + 4]);
         }
+        r0[0] = c[0];
+        r0[1] = c[1];
+        r1[0] = c[2];
+        r1[1] = c[3];
     }
-    __syncwarp();
 }
 
 /* dh = dZ W^T for layer l (W in-major N_l: [in][64+PAD]), masked by relu'(previous z) */
@@ -153,77 +162,6 @@ __device__ __forceinline__ void backprop_layer(const float (*dZ)[4], const __nv_
         for (int i = 0; i < 4; ++i) dH[j][i] = __bfloat162float(__float2bfloat16_rn(dH[j][i]));
 }
 
-/* forward + backward of one 16-point tile; y0/y1 targets of rows g, g+8 */
-template <int D>
-__device__ void train_tile(const SmemParams<D>& P, const float* u_g, const float* u_g8, float y0, float y1, bool v0,
-                           bool v1, float scale, float* gW[4], float* gb[4], float* gw4, float* gb4,
-                           __nv_bfloat16* AT, __nv_bfloat16* ZT, float* out_rows) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    Acts<D> a;
-    features_tile<D>(u_g, u_g8, a.F);
-    float out[2];
-    forward_tile<D>(P, a, out);
-    if (out_rows) {
-        out_rows[0] = out[0];
-        out_rows[1] = out[1];
-    }
-    const float d0 = v0 ? (out[0] - y0) * scale : 0.0f;
-    const float d1 = v1 ? (out[1] - y1) * scale : 0.0f;
-    /* output layer gradients */
-    {
-        float sb = (t == 0) ? d0 + d1 : 0.0f;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
-        if (lane == 0) atomicAdd(gb4, sb);
-#pragma unroll
-        for (int kt = 0; kt < KTH; ++kt) {
-            const int c = 16 * kt + 2 * t;
-            float s[4] = {d0 * bf16_lo(a.H[3][kt][0]) + d1 * bf16_lo(a.H[3][kt][1]),
-                          d0 * bf16_hi(a.H[3][kt][0]) + d1 * bf16_hi(a.H[3][kt][1]),
-                          d0 * bf16_lo(a.H[3][kt][2]) + d1 * bf16_lo(a.H[3][kt][3]),
-                          d0 * bf16_hi(a.H[3][kt][2]) + d1 * bf16_hi(a.H[3][kt][3])};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int o = 4; o < 32; o <<= 1) s[i] += __shfl_xor_sync(0xffffffffu, s[i], o);
-            if (g == 0) {
-                atomicAdd(&gw4[c], s[0]);
-                atomicAdd(&gw4[c + 1], s[1]);
-                atomicAdd(&gw4[c + 8], s[2]);
-                atomicAdd(&gw4[c + 9], s[3]);
-            }
-        }
-    }
-    /* dZ4 = dout * w4 * relu'(z4), rounded to BF16 */
-    float dZ[NT][4];
-#pragma unroll
-    for (int kt = 0; kt < KTH; ++kt) {
-        const int c = 16 * kt + 2 * t;
-        const uint32_t* h = a.H[3][kt];
-        dZ[2 * kt][0] = bf16_lo(h[0]) > 0.0f ? d0 * P.w4[c] : 0.0f;
-        dZ[2 * kt][1] = bf16_hi(h[0]) > 0.0f ? d0 * P.w4[c + 1] : 0.0f;
-        dZ[2 * kt][2] = bf16_lo(h[1]) > 0.0f ? d1 * P.w4[c] : 0.0f;
-        dZ[2 * kt][3] = bf16_hi(h[1]) > 0.0f ? d1 * P.w4[c + 1] : 0.0f;
-        dZ[2 * kt + 1][0] = bf16_lo(h[2]) > 0.0f ? d0 * P.w4[c + 8] : 0.0f;
-        dZ[2 * kt + 1][1] = bf16_hi(h[2]) > 0.0f ? d0 * P.w4[c + 9] : 0.0f;
-        dZ[2 * kt + 1][2] = bf16_lo(h[3]) > 0.0f ? d1 * P.w4[c + 8] : 0.0f;
-        dZ[2 * kt + 1][3] = bf16_hi(h[3]) > 0.0f ? d1 * P.w4[c + 9] : 0.0f;
-    }
-#pragma unroll
-    for (int j = 0; j < NT; ++j)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) dZ[j][i] = __bfloat162float(__float2bfloat16_rn(dZ[j][i]));
-    /* layers 3, 2, 1: dW from (input activations, dZ), then dZ of the layer below */
-    float dH[NT][4];
-    accumulate_dW<KTH>(AT, ZT, a.H[2], dZ, gW[3], gb[3]);
-    backprop_layer(dZ, P.N[3], a.H[2], dH);
-    accumulate_dW<KTH>(AT, ZT, a.H[1], dH, gW[2], gb[2]);
-    backprop_layer(dH, P.N[2], a.H[1], dZ);
-    accumulate_dW<KTH>(AT, ZT, a.H[0], dZ, gW[1], gb[1]);
-    backprop_layer(dZ, P.N[1], a.H[0], dH);
-    accumulate_dW<fin(D) / 16>(AT, ZT, a.F, dH, gW[0], gb[0]);
-}
-
 /* training points of one step: Philox points over the range and the integrand's values there */
 template <class F, int D>
 __global__ void k_mlp_samples(const __grid_constant__ F f, const TrainCfg cfg, uint64_t n, float* __restrict__ u_out,
@@ -252,57 +190,145 @@ __global__ void k_mlp_samples(const __grid_constant__ F f, const TrainCfg cfg, u
     y_out[s] = v[0];
 }
 
+/* One training step's forward and backward over cfg.rounds x ROUND points per block.  Each warp
+ * pushes a 16-point tile through the network in registers (activations stay in the A-fragment
+ * layout), then layer by layer from the top: the warp stages its tile's layer inputs and dZ
+ * (transposed, BF16) into the block's tiles and computes dh = dZ W^T for the layer below; after a
+ * barrier the block computes dW += AT . ZT^T over all its points on the tensor cores.  The block
+ * writes its summed gradient to partial[block] (kernel order: W0..W3, b0..b3, w4, b4). */
 template <int D>
 __global__ void __launch_bounds__(TRAIN_WARPS * 32, 1)
-    k_mlp_train(const TrainCfg cfg, const char* __restrict__ packed, float* __restrict__ grad) {
+    k_mlp_train(const TrainCfg cfg, const char* __restrict__ packed, float* __restrict__ partial) {
     extern __shared__ __align__(16) char smem[];
     load_params<D>(smem, packed, true);
     const SmemParams<D> P = smem_params<D>(smem, true);
-    float* gsm = reinterpret_cast<float*>(smem + pack_bytes(D));
-    const int ng = fin(D) * WIDTH + 3 * WIDTH * WIDTH + 4 * WIDTH + WIDTH + 1;
-    for (int i = threadIdx.x; i < ng; i += blockDim.x) gsm[i] = 0.0f;
-    float* gW[4];
-    float* gb[4];
-    for (int l = 0; l < 4; ++l) {
-        gW[l] = gsm + (l == 0 ? 0 : fin(D) * WIDTH + (l - 1) * WIDTH * WIDTH);
-        gb[l] = gsm + fin(D) * WIDTH + 3 * WIDTH * WIDTH + l * WIDTH;
-    }
-    float* gw4 = gsm + fin(D) * WIDTH + 3 * WIDTH * WIDTH + 4 * WIDTH;
-    float* gb4 = gw4 + WIDTH;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
-    __nv_bfloat16* AT = reinterpret_cast<__nv_bfloat16*>(gsm + ng + 3) + warp * (at_rows(D) + WIDTH) * ZS;
-    AT = reinterpret_cast<__nv_bfloat16*>((reinterpret_cast<uintptr_t>(AT) + 15) & ~uintptr_t(15));
-    __nv_bfloat16* ZT = AT + at_rows(D) * ZS;
+    float* gw = reinterpret_cast<float*>(smem + pack_bytes(D));
+    float* slots = gw + gw_floats(D);
+    __nv_bfloat16* AT = reinterpret_cast<__nv_bfloat16*>(slots + TRAIN_WARPS * SLOT);
+    __nv_bfloat16* ZT = AT + at_rows(D) * KS;
+    for (int i = threadIdx.x; i < gw_floats(D) + TRAIN_WARPS * SLOT; i += blockDim.x) gw[i] = 0.0f;
     __syncthreads();
-    const uint64_t warp_global = (uint64_t)blockIdx.x * TRAIN_WARPS + warp;
-    for (uint32_t chunk = 0; chunk < cfg.tiles_per_warp; ++chunk) {
-        const uint64_t s = (warp_global * cfg.tiles_per_warp + chunk) * 32 + lane; /* this lane's point */
-        float u[D];
-        const bool valid = s < cfg.npts;
-        for (int d = 0; d < D; ++d) u[d] = valid ? cfg.u_in[s * D + d] : 0.5f;
-        const float y = valid ? cfg.y_in[s] : 0.0f;
-        /* two 16-point tiles: points 0..15 and 16..31 of this chunk */
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float* my = slots + warp * SLOT; /* db[4][64] | dw4[64] | db4 */
+    const int col0 = warp * 16;
+    for (uint32_t round = 0; round < cfg.rounds; ++round) {
+        const uint64_t base = ((uint64_t)blockIdx.x * cfg.rounds + round) * ROUND + col0;
+        const uint64_t s0 = base + g, s1 = base + g + 8;
+        const bool v0 = s0 < cfg.npts, v1 = s1 < cfg.npts;
+        float ug[D], ug8[D];
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            float ug[D], ug8[D];
-            const int src0 = 16 * half + g, src1 = 16 * half + g + 8;
-            for (int d = 0; d < D; ++d) {
-                ug[d] = __shfl_sync(0xffffffffu, u[d], src0);
-                ug8[d] = __shfl_sync(0xffffffffu, u[d], src1);
-            }
-            const float y0 = __shfl_sync(0xffffffffu, y, src0), y1 = __shfl_sync(0xffffffffu, y, src1);
-            const bool v0 = __shfl_sync(0xffffffffu, valid, src0), v1 = __shfl_sync(0xffffffffu, valid, src1);
-            float outr[2];
-            train_tile<D>(P, ug, ug8, y0, y1, v0, v1, cfg.scale, gW, gb, gw4, gb4, AT, ZT, outr);
-            if (cfg.out && (lane & 3) == 0) {
-                const uint64_t base = (warp_global * cfg.tiles_per_warp + chunk) * 32 + 16 * half;
-                if (base + g < cfg.npts) cfg.out[base + g] = outr[0];
-                if (base + g + 8 < cfg.npts) cfg.out[base + g + 8] = outr[1];
+        for (int d = 0; d < D; ++d) {
+            ug[d] = v0 ? cfg.u_in[s0 * D + d] : 0.5f;
+            ug8[d] = v1 ? cfg.u_in[s1 * D + d] : 0.5f;
+        }
+        const float y0 = v0 ? cfg.y_in[s0] : 0.0f, y1 = v1 ? cfg.y_in[s1] : 0.0f;
+        Acts<D> a;
+        features_tile<D>(ug, ug8, a.F);
+        float out[2];
+        forward_tile<D>(P, a, out);
+        if (cfg.out && t == 0) {
+            if (v0) cfg.out[s0] = out[0];
+            if (v1) cfg.out[s1] = out[1];
+        }
+        const float d0 = v0 ? (out[0] - y0) * cfg.scale : 0.0f;
+        const float d1 = v1 ? (out[1] - y1) * cfg.scale : 0.0f;
+        /* output layer: dw4 = sum d * h4, db4 = sum d (the warp's own slot) */
+        {
+            float sb = (t == 0) ? d0 + d1 : 0.0f;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
+            if (lane == 0) my[5 * WIDTH] += sb;
+#pragma unroll
+            for (int kt = 0; kt < KTH; ++kt) {
+                const int c = 16 * kt + 2 * t;
+                float sw[4] = {d0 * bf16_lo(a.H[3][kt][0]) + d1 * bf16_lo(a.H[3][kt][1]),
+                               d0 * bf16_hi(a.H[3][kt][0]) + d1 * bf16_hi(a.H[3][kt][1]),
+                               d0 * bf16_lo(a.H[3][kt][2]) + d1 * bf16_lo(a.H[3][kt][3]),
+                               d0 * bf16_hi(a.H[3][kt][2]) + d1 * bf16_hi(a.H[3][kt][3])};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int o = 4; o < 32; o <<= 1) sw[i] += __shfl_xor_sync(0xffffffffu, sw[i], o);
+                if (g == 0) {
+                    my[4 * WIDTH + c] += sw[0];
+                    my[4 * WIDTH + c + 1] += sw[1];
+                    my[4 * WIDTH + c + 8] += sw[2];
+                    my[4 * WIDTH + c + 9] += sw[3];
+                }
             }
         }
+        /* dZ4 = dout * w4 * relu'(z4), rounded to BF16 */
+        float dZ[NT][4], dH[NT][4];
+#pragma unroll
+        for (int kt = 0; kt < KTH; ++kt) {
+            const int c = 16 * kt + 2 * t;
+            const uint32_t* h = a.H[3][kt];
+            dZ[2 * kt][0] = bf16_lo(h[0]) > 0.0f ? d0 * P.w4[c] : 0.0f;
+            dZ[2 * kt][1] = bf16_hi(h[0]) > 0.0f ? d0 * P.w4[c + 1] : 0.0f;
+            dZ[2 * kt][2] = bf16_lo(h[1]) > 0.0f ? d1 * P.w4[c] : 0.0f;
+            dZ[2 * kt][3] = bf16_hi(h[1]) > 0.0f ? d1 * P.w4[c + 1] : 0.0f;
+            dZ[2 * kt + 1][0] = bf16_lo(h[2]) > 0.0f ? d0 * P.w4[c + 8] : 0.0f;
+            dZ[2 * kt + 1][1] = bf16_hi(h[2]) > 0.0f ? d0 * P.w4[c + 9] : 0.0f;
+            dZ[2 * kt + 1][2] = bf16_lo(h[3]) > 0.0f ? d1 * P.w4[c + 8] : 0.0f;
+            dZ[2 * kt + 1][3] = bf16_hi(h[3]) > 0.0f ? d1 * P.w4[c + 9] : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < NT; ++j)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dZ[j][i] = __bfloat162float(__float2bfloat16_rn(dZ[j][i]));
+        /* layer 3 */
+        stage_A<KTH>(AT, a.H[2], col0);
+        stage_Z(ZT, dZ, col0, my + 3 * WIDTH);
+        backprop_layer(dZ, P.N[3], a.H[2], dH);
+        __syncthreads();
+        block_dW<KTH>(AT, ZT, gw + (fin(D) + 2 * WIDTH) * GS);
+        __syncthreads();
+        /* layer 2 */
+        stage_A<KTH>(AT, a.H[1], col0);
+        stage_Z(ZT, dH, col0, my + 2 * WIDTH);
+        backprop_layer(dH, P.N[2], a.H[1], dZ);
+        __syncthreads();
+        block_dW<KTH>(AT, ZT, gw + (fin(D) + WIDTH) * GS);
+        __syncthreads();
+        /* layer 1 */
+        stage_A<KTH>(AT, a.H[0], col0);
+        stage_Z(ZT, dZ, col0, my + WIDTH);
+        backprop_layer(dZ, P.N[1], a.H[0], dH);
+        __syncthreads();
+        block_dW<KTH>(AT, ZT, gw + fin(D) * GS);
+        __syncthreads();
+        /* layer 0 (features) */
+        stage_A<fin(D) / 16>(AT, a.F, col0);
+        stage_Z(ZT, dH, col0, my);
+        __syncthreads();
+        block_dW<fin(D) / 16>(AT, ZT, gw);
+        __syncthreads();
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < ng; i += blockDim.x) atomicAdd(&grad[i], gsm[i]);
+    /* the block's gradient: W rows are consecutive in gw (W0 rows, then W1..W3); the per-warp sums
+     * are added in warp order */
+    float* dst = partial + (size_t)blockIdx.x * n_params(D);
+    const int nw = (fin(D) + 3 * WIDTH) * WIDTH;
+    for (int i = threadIdx.x; i < n_params(D); i += blockDim.x) {
+        float v = 0.0f;
+        if (i < nw) {
+            v = gw[(i / WIDTH) * GS + (i % WIDTH)];
+        } else {
+            const int k = i - nw; /* db[4][64], dw4[64], db4: the slot layout */
+#pragma unroll
+            for (int w = 0; w < TRAIN_WARPS; ++w) v += slots[w * SLOT + k];
+        }
+        dst[i] = v;
+    }
+}
+
+/* grad[i] = sum over blocks of partial[b][i], in block order */
+template <int D>
+__global__ void k_mlp_reduce(const float* __restrict__ partial, int nparts, float* __restrict__ grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_params(D)) return;
+    float s = 0.0f;
+    for (int b = 0; b < nparts; ++b) s += partial[(size_t)b * n_params(D) + i];
+    grad[i] = s;
 }
 
 /* gradient layout in shared memory / global: gW0..gW3 (W order), gb0..gb3, gw4, gb4 -> parameter index */
@@ -344,16 +370,18 @@ template <int D> __device__ __forceinline__ void pack_param(char* packed, int p,
 struct AdamCfg {
     float lr, b1, b2, eps;
     int n;
+    int nparts; /* per-block partial gradients to add */
 };
 
 template <int D>
 __global__ void k_mlp_adam(const AdamCfg c, float* __restrict__ theta, float* __restrict__ m, float* __restrict__ v,
-                           float* __restrict__ grad, const uint32_t* __restrict__ step_ctr, char* __restrict__ packed) {
+                           const float* __restrict__ partial, const uint32_t* __restrict__ step_ctr,
+                           char* __restrict__ packed) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const int p = grad_to_param<D>(i);
-    const float gr = grad[i];
-    grad[i] = 0.0f;
+    float gr = 0.0f;
+    for (int b = 0; b < c.nparts; ++b) gr += partial[(size_t)b * c.n + i];
     const float t = (float)(*step_ctr + 1);
     const float mi = c.b1 * m[p] + (1.0f - c.b1) * gr;
     const float vi = c.b2 * v[p] + (1.0f - c.b2) * gr * gr;
@@ -380,7 +408,8 @@ struct BinCfg {
     uint32_t res[VCU_MAX_DIMBINS];
     int32_t dimbins;
     uint64_t nbins;
-    int32_t q; /* Gauss-Legendre nodes per dimension */
+    int32_t q;     /* Gauss-Legendre nodes per cell and dimension */
+    int32_t cells; /* composite cells per dimension            */
     float gl_x[4], gl_w[4];
 };
 
@@ -406,37 +435,42 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
     load_params<D>(smem, packed, false);
     const SmemParams<D> P = smem_params<D>(smem, false);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
+    const int qc = c.q * c.cells; /* nodes per dimension */
     int nodes = 1;
-    for (int d = 0; d < D; ++d) nodes *= c.q;
+    for (int d = 0; d < D; ++d) nodes *= qc;
+    const float inv_cells = 1.0f / (float)c.cells;
     for (uint64_t bin = (uint64_t)blockIdx.x * FWD_WARPS + warp; bin < c.nbins; bin += (uint64_t)gridDim.x * FWD_WARPS) {
         float lo[D], hi[D];
         bin_box<D>(c, bin, lo, hi);
-        float acc = 0.0f;
+        double acc = 0.0;
         for (int base = 0; base < nodes; base += 16) {
             float ug[D], ug8[D], w0 = 1.0f, w1 = 1.0f;
             const int n0 = base + g, n1 = base + g + 8;
             int r0 = n0, r1 = n1;
             for (int d = 0; d < D; ++d) {
-                const int i0 = r0 % c.q, i1 = r1 % c.q;
-                r0 /= c.q;
-                r1 /= c.q;
-                const float x0 = lo[d] + (hi[d] - lo[d]) * 0.5f * (1.0f + c.gl_x[i0]);
-                const float x1 = lo[d] + (hi[d] - lo[d]) * 0.5f * (1.0f + c.gl_x[i1]);
+                const int i0 = r0 % qc, i1 = r1 % qc;
+                r0 /= qc;
+                r1 /= qc;
+                /* node j of cell k: (k + (1 + x_j) / 2) / cells of the bin's extent */
+                const float t0 = ((float)(i0 / c.q) + 0.5f * (1.0f + c.gl_x[i0 % c.q])) * inv_cells;
+                const float t1 = ((float)(i1 / c.q) + 0.5f * (1.0f + c.gl_x[i1 % c.q])) * inv_cells;
+                const float x0 = lo[d] + (hi[d] - lo[d]) * t0;
+                const float x1 = lo[d] + (hi[d] - lo[d]) * t1;
                 const float span = c.r.rmax[d] - c.r.rmin[d];
                 ug[d] = (x0 - c.r.rmin[d]) / span;
                 ug8[d] = (x1 - c.r.rmin[d]) / span;
-                w0 *= 0.5f * c.gl_w[i0];
-                w1 *= 0.5f * c.gl_w[i1];
+                w0 *= 0.5f * c.gl_w[i0 % c.q] * inv_cells;
+                w1 *= 0.5f * c.gl_w[i1 % c.q] * inv_cells;
             }
             Acts<D> a;
             features_tile<D>(ug, ug8, a.F);
             float out[2];
             forward_tile<D>(P, a, out);
-            if ((lane & 3) == 0) acc += (n0 < nodes ? w0 * out[0] : 0.0f) + (n1 < nodes ? w1 * out[1] : 0.0f);
+            if ((lane & 3) == 0) acc += (n0 < nodes ? (double)(w0 * out[0]) : 0.0) + (n1 < nodes ? (double)(w1 * out[1]) : 0.0);
         }
 #pragma unroll
         for (int o = 4; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) integral[bin] = acc; /* mean of g over the bin */
+        if (lane == 0) integral[bin] = (float)acc; /* mean of g over the bin */
     }
 }
 
@@ -571,14 +605,14 @@ inline void init_params(int d, uint64_t seed, float* theta) {
 }
 
 struct State {
-    float *theta, *m, *v, *grad;
+    float *theta, *m, *v, *grad, *partial;
     char* packed;
     uint32_t* step;
     float* integral;
     uint32_t* fallback;
 };
 
-template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, State& s) {
+template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, uint64_t nparts, State& s) {
     const size_t np = n_params(D), ng = np; /* gradient vector has one entry per parameter */
     size_t o = 0;
     auto a = [&](size_t bytes) {
@@ -587,7 +621,7 @@ template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, State& s) {
         return at;
     };
     const size_t o_theta = a(np * 4), o_m = a(np * 4), o_v = a(np * 4), o_g = a(ng * 4), o_p = a(pack_bytes(D)),
-                 o_s = a(64), o_i = a(nbins * 4), o_f = a(64);
+                 o_s = a(64), o_i = a(nbins * 4), o_f = a(64), o_pt = a(nparts * ng * 4);
     int rc = ensure(ctx, ctx->scratch, o);
     if (rc) return rc;
     char* b = static_cast<char*>(ctx->scratch.ptr);
@@ -595,6 +629,7 @@ template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, State& s) {
     s.m = reinterpret_cast<float*>(b + o_m);
     s.v = reinterpret_cast<float*>(b + o_v);
     s.grad = reinterpret_cast<float*>(b + o_g);
+    s.partial = reinterpret_cast<float*>(b + o_pt);
     s.packed = b + o_p;
     s.step = reinterpret_cast<uint32_t*>(b + o_s);
     s.integral = reinterpret_cast<float*>(b + o_i);
@@ -628,8 +663,11 @@ template <int D> int set_smem_train(vcu_ctx* ctx) {
 template <class F, int D>
 int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_learned& opt, float* d_bins,
             float* d_integral, vcu_learned_report* report, uint32_t& launches) {
+    /* training grid: at most one block per SM, each doing `rounds` rounds of ROUND points */
+    const uint64_t want = ((uint64_t)(opt.batch > 0 ? opt.batch : 1) + ROUND - 1) / ROUND;
+    const unsigned train_blocks = (unsigned)(want < (uint64_t)ctx->sm_count ? want : (uint64_t)ctx->sm_count);
     State s;
-    int rc = alloc_state<D>(ctx, g.nbins, s);
+    int rc = alloc_state<D>(ctx, g.nbins, train_blocks, s);
     if (rc) return rc;
     if ((rc = set_smem_train<D>(ctx))) return rc;
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_residual<F, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -645,10 +683,8 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     }
     tc.k0 = (uint32_t)(opt.seed * 0x9E3779B97F4A7C15ull >> 32);
     tc.k1 = (uint32_t)(opt.seed >> 32) ^ 0x51ED270Bu;
-    const unsigned train_blocks = (unsigned)ctx->sm_count;
-    const uint32_t per_block = TRAIN_WARPS * 32;
-    tc.tiles_per_warp = (opt.batch + train_blocks * per_block - 1) / (train_blocks * per_block);
-    const uint64_t batch = (uint64_t)tc.tiles_per_warp * train_blocks * per_block;
+    tc.rounds = (uint32_t)((want + train_blocks - 1) / train_blocks);
+    const uint64_t batch = (uint64_t)tc.rounds * train_blocks * ROUND;
     tc.scale = (float)(2.0 / (double)batch);
     /* the step's training points live in the context's input buffer */
     if ((rc = ensure(ctx, ctx->in, batch * (D + 1) * 4 + 1024))) return rc;
@@ -657,7 +693,7 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     tc.u_in = su;
     tc.y_in = sy;
     tc.npts = batch;
-    AdamCfg ac{opt.learning_rate, 0.9f, 0.999f, 1e-8f, n_params(D)};
+    AdamCfg ac{opt.learning_rate, 0.9f, 0.999f, 1e-8f, n_params(D), (int)train_blocks};
     cudaEvent_t e0 = ctx->ev_tune[0], e1 = ctx->ev_tune[1];
     VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
     if (opt.train_steps > 0) {
@@ -665,8 +701,9 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
         cudaGraphExec_t exec = nullptr;
         VCU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         k_mlp_samples<F, D><<<(unsigned)((batch + 255) / 256), 256, 0, ctx->stream>>>(f, tc, batch, su, sy, s.step);
-        k_mlp_train<D><<<train_blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.grad);
-        k_mlp_adam<D><<<(unsigned)((n_params(D) + 255) / 256), 256, 0, ctx->stream>>>(ac, s.theta, s.m, s.v, s.grad,
+        k_mlp_train<D><<<train_blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed,
+                                                                                                s.partial);
+        k_mlp_adam<D><<<(unsigned)((n_params(D) + 255) / 256), 256, 0, ctx->stream>>>(ac, s.theta, s.m, s.v, s.partial,
                                                                                        s.step, s.packed);
         k_mlp_step_inc<<<1, 1, 0, ctx->stream>>>(s.step);
         const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
@@ -705,6 +742,7 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     bc.dimbins = p->dimbins;
     bc.nbins = g.nbins;
     bc.q = (int)opt.quad_nodes;
+    bc.cells = opt.quad_cells > 1 ? opt.quad_cells : 1;
     for (int i = 0; i < 4; ++i) {
         bc.gl_x[i] = kGLx[bc.q - 1][i];
         bc.gl_w[i] = kGLw[bc.q - 1][i];
@@ -760,8 +798,9 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
 template <int D>
 int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, int64_t npts, float* out, float* grad,
               uint32_t& launches) {
+    const unsigned blocks = (unsigned)((npts + ROUND - 1) / ROUND);
     State s;
-    int rc = alloc_state<D>(ctx, 1, s);
+    int rc = alloc_state<D>(ctx, 1, blocks, s);
     if (rc) return rc;
     if ((rc = set_smem_train<D>(ctx))) return rc;
     if ((rc = upload_params<D>(ctx, s, theta, launches))) return rc;
@@ -774,14 +813,16 @@ int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, 
     if (y) VCU_CUDA(ctx, cudaMemcpyAsync(dy, y, (size_t)npts * 4, cudaMemcpyHostToDevice, ctx->stream));
     else VCU_CUDA(ctx, cudaMemsetAsync(dy, 0, (size_t)npts * 4, ctx->stream));
     TrainCfg tc{};
-    tc.tiles_per_warp = 1;
+    tc.rounds = 1;
     tc.u_in = du;
     tc.y_in = dy;
     tc.out = dout;
     tc.npts = (uint64_t)npts;
     tc.scale = (float)(2.0 / (double)npts);
-    const unsigned blocks = (unsigned)((npts + TRAIN_WARPS * 32 - 1) / (TRAIN_WARPS * 32));
-    k_mlp_train<D><<<blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.grad);
+    k_mlp_train<D><<<blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.partial);
+    ++launches;
+    VCU_CUDA(ctx, cudaGetLastError());
+    k_mlp_reduce<D><<<(unsigned)((n_params(D) + 255) / 256), 256, 0, ctx->stream>>>(s.partial, (int)blocks, s.grad);
     ++launches;
     VCU_CUDA(ctx, cudaGetLastError());
     VCU_CUDA(ctx, cudaMemcpyAsync(out, dout, (size_t)npts * 4, cudaMemcpyDeviceToHost, ctx->stream));

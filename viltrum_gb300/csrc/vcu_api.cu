@@ -459,6 +459,13 @@ extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, 
     if (rc) return rc;
     if (!opt || !bins) return fail(ctx, VCU_INVALID_ARG, "null options or bins");
     if (opt->quad_nodes < 1 || opt->quad_nodes > 4) return fail(ctx, VCU_INVALID_ARG, "quad_nodes must be 1..4");
+    if (opt->quad_cells < 0 || opt->quad_cells > 256) return fail(ctx, VCU_INVALID_ARG, "quad_cells must be 0..256");
+    {
+        double nodes = 1.0;
+        const int qc = (int)opt->quad_nodes * (opt->quad_cells > 1 ? opt->quad_cells : 1);
+        for (int d = 0; d < p->dim; ++d) nodes *= qc;
+        if (nodes > 2147483647.0) return fail(ctx, VCU_INVALID_ARG, "too many quadrature nodes per bin");
+    }
     if (opt->samples_per_bin == 0 || opt->samples_per_bin > 0xffffffffull)
         return fail(ctx, VCU_INVALID_ARG, "samples per bin must be 1..2^32-1");
     if (opt->train_steps > 0 && opt->batch == 0) return fail(ctx, VCU_INVALID_ARG, "batch must be positive");
@@ -479,9 +486,6 @@ extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, 
         if (network_integral)
             VCU_CUDA(ctx, cudaMemcpyAsync(network_integral, dint, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
     }
-    double nodes = 1.0;
-    for (int d = 0; d < p->dim; ++d) nodes *= opt->quad_nodes;
-    (void)nodes;
     const uint64_t evals = (uint64_t)opt->train_steps * opt->batch + g.nbins * opt->samples_per_bin;
     return scope.end(evals, 0);
 }

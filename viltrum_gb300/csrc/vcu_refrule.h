@@ -34,20 +34,15 @@ VCU_HD void two_prod(float a, float b, float& p, float& e) {
     p = vmul(a, b);
     e = vfma(a, b, -p);
 }
+/* nextafter(x, +inf) / nextafter(x, -inf) for the finite quotients ff_div produces: one integer
+ * step of the bit pattern (+/-0 go to the smallest subnormal; infinities and NaN are returned) */
 VCU_HD float next_up(float x) {
-#if defined(__CUDA_ARCH__)
-    return nextafterf(x, __int_as_float(0x7f800000));
-#else
-    return std::nextafter(x, INFINITY);
-#endif
+    const uint32_t u = float_to_bits(x);
+    if ((u & 0x7fffffffu) == 0u) return bits_to_float(1u);
+    if ((u & 0x7f800000u) == 0x7f800000u) return (u == 0xff800000u) ? bits_to_float(0xff7fffffu) : x;
+    return bits_to_float((u >> 31) ? u - 1u : u + 1u);
 }
-VCU_HD float next_down(float x) {
-#if defined(__CUDA_ARCH__)
-    return nextafterf(x, -__int_as_float(0x7f800000));
-#else
-    return std::nextafter(x, -INFINITY);
-#endif
-}
+VCU_HD float next_down(float x) { return -next_up(-x); }
 VCU_HD bool even_bits(float x) {
 #if defined(__CUDA_ARCH__)
     return (__float_as_uint(x) & 1u) == 0u;
@@ -62,11 +57,11 @@ VCU_HD bool even_bits(float x) {
  * RN(h/D)) is within one float of the result; the exact remainder R = h + l - q0*D (two_sum of the
  * exact fma residual and l) decides: R/D beyond half the gap to the neighbour moves to it, exactly half (or within the
  * 2^-30-ulp band where the reference's intermediate double lands on the midpoint) ties to even. */
-VCU_HD float ff_div(float h, float l, float D) {
+VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
     /* q0 = RN(h/D) can be two floats away when l is a full ulp of h; one approximate correction
      * step brings it within one float of the result */
     const float q00 = vdiv(h, D);
-    const float q0 = vfma(vadd(vfma(-q00, D, h), l), vdiv(1.0f, D), q00);
+    const float q0 = vfma(vadd(vfma(-q00, D, h), l), inv_D, q00);
     float s, e;
     two_sum(vfma(-q0, D, h), l, s, e);
     const float up = next_up(q0), dn = next_down(q0);
@@ -93,7 +88,7 @@ template <> struct RefRule<3> { /* (p0 + 4.0*p1 + p2)/6.0 */
         float h, e1, h2, e2;
         two_sum(p[0], vmul(4.0f, p[1]), h, e1);
         two_sum(h, p[2], h2, e2);
-        return ff_div(h2, vadd(e1, e2), 6.0f);
+        return ff_div(h2, vadd(e1, e2), 6.0f, 0.1666666716337204f /* RN(1/6) */);
     }
     static VCU_HD float rgb(const float* p) {
         return vdiv(vadd(vadd(p[0], vmul(4.0f, p[1])), p[2]), 6.0f);
@@ -113,7 +108,7 @@ template <> struct RefRule<5> { /* (7.0*p0 + 32.0*p1 + 12.0*p2 + 32.0*p3 + 7.0*p
         two_prod(7.0f, p[4], ph, pl);
         two_sum(h, ph, h, e);
         l = vadd(l, vadd(pl, e));
-        return ff_div(h, l, 90.0f);
+        return ff_div(h, l, 90.0f, 0.011111111380159855f /* RN(1/90) */);
     }
     static VCU_HD float rgb(const float* p) {
         const float s = vadd(vadd(vadd(vadd(vmul(7.0f, p[0]), vmul(32.0f, p[1])), vmul(12.0f, p[2])), vmul(32.0f, p[3])),

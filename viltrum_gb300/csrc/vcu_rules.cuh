@@ -109,22 +109,23 @@ template <> struct Rule<5> { /* boole */
 
 /* subrange() as the reference computes it for float nodes (rules.h:41-44, 96-100, 288-293): float
  * coefficients, then the Horner steps in double ("c[k]*b/5.0" is a float product divided in double)
- * and the difference of the two ends rounded once to float.  Used where bin n region can be a short
+ * and the difference of the two ends rounded once to float.  (Divisions by 2 and 4 are exact in
+ * double, so they are written as the equal multiplications.)  Used where bin n region can be a short
  * piece of a large region (control variates), so the two Horner values nearly cancel. */
 template <int S> __device__ __forceinline__ double horner_int_ref(const float* c, float t);
 template <> __device__ __forceinline__ double horner_int_ref<2>(const float* c, float t) {
-    double r = __dadd_rn(__ddiv_rn((double)vmul(c[1], t), 2.0), (double)c[0]);
+    double r = __dadd_rn(__dmul_rn((double)vmul(c[1], t), 0.5), (double)c[0]); /* /2.0 is exact */
     return __dmul_rn(r, (double)t);
 }
 template <> __device__ __forceinline__ double horner_int_ref<3>(const float* c, float t) {
-    double r = __dadd_rn(__ddiv_rn((double)vmul(c[2], t), 3.0), __ddiv_rn((double)c[1], 2.0));
+    double r = __dadd_rn(__ddiv_rn((double)vmul(c[2], t), 3.0), __dmul_rn((double)c[1], 0.5));
     r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
     return __dmul_rn(r, (double)t);
 }
 template <> __device__ __forceinline__ double horner_int_ref<5>(const float* c, float t) {
-    double r = __dadd_rn(__ddiv_rn((double)vmul(c[4], t), 5.0), __ddiv_rn((double)c[3], 4.0));
+    double r = __dadd_rn(__ddiv_rn((double)vmul(c[4], t), 5.0), __dmul_rn((double)c[3], 0.25));
     r = __dadd_rn(__dmul_rn(r, (double)t), __ddiv_rn((double)c[2], 3.0));
-    r = __dadd_rn(__dmul_rn(r, (double)t), __ddiv_rn((double)c[1], 2.0));
+    r = __dadd_rn(__dmul_rn(r, (double)t), __dmul_rn((double)c[1], 0.5));
     r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
     return __dmul_rn(r, (double)t);
 }
