@@ -239,10 +239,156 @@ def run_ours(args) -> dict | None:
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0 and ws == 1 and not args.no_configs:
+        line["configs"] = other_configs(ctx, args)
     ctx.close()
     if ws > 1:
         dist.destroy_process_group()
     return line if rank == 0 else None
+
+
+def _median_ms(fn, reps: int = 5, warmup: int = 3) -> tuple[float, object]:
+    """median device time (the library's CUDA-event stats) of fn() after warm-up calls"""
+    for _ in range(warmup):
+        fn()
+    out = [fn() for _ in range(reps)]
+    return statistics.median(o.device_ms for o in out), out[-1]
+
+
+def other_configs(ctx, args) -> dict:
+    """One measured line per remaining workload of the path (rank 0, one GPU): per-bin Monte Carlo,
+    control variates, the batch of independent integrals and the learned control variate against
+    plain Monte Carlo and the polynomial control variate at equal bin RMSE."""
+    from viltrum_gb300 import _lib, scenes
+
+    out = {}
+    # -- per-bin Monte Carlo, sin(8x)e^-y + x^2 + y^2 into 1024 bins along x, 1024 samples per bin
+    p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [1024])
+    b = np.empty(1024, np.float32)
+    ms, st = _median_ms(lambda: ctx.per_bin_monte_carlo(p, 1024, 1, b))
+    exact = scenes.exact_bins(scenes.WAVE2, None, [0, 0], [1, 1], [1024])
+    out["per_bin_monte_carlo"] = {
+        "workload": "wave2 sin(8x)e^-y+x^2+y^2 on [0,1]^2, 1024 bins along x, 1024 Philox samples per bin",
+        "ms": round(ms, 4), "gsamples_s": round(st.evaluations / (ms * 1e6), 3),
+        "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact), "timing": "median of 5 after 3 warm-up, device"}
+    # -- control variates + residual Monte Carlo, 3 channels, 512x512 bins, 2^14 regions, 64 spp
+    params = scenes.moving_scene3(SEED)
+    res = [512, 512]
+    p = ctx.problem(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res)
+    nested = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+    b = np.empty(512 * 512 * 3, np.float32)
+    ms, st = _median_ms(lambda: ctx.control_variates(p, nested, (1 << 14) - 1, _lib.CvOpts(64, 3, 0, 0, 1.0), b),
+                        reps=3, warmup=3)
+    rows = list(range(0, 512, 64))
+    err = []
+    for r in rows:
+        y0, y1 = r / 512.0, (r + 1) / 512.0
+        # one row of bins: its values are prod(res) x integral, and this call's resolution is [512, 1]
+        ex = scenes.exact_bins(scenes.MOVING_SCENE3, params, [0, y0, 0], [1, y1, 1], [512, 1]) * 512.0
+        err.append(b.reshape(512, 512, 3)[r] - ex)
+    err = np.concatenate(err)
+    out["control_variates"] = {
+        "workload": "integrator_crespo2021(2^14-1 splits, 64 residual samples): moving-disk scene, RGB, "
+                    "x,y binned 512x512, t in [0,1]",
+        "ms": round(ms, 3), "gsamples_s": round(st.evaluations / (ms * 1e6), 3), "regions": int(st.regions),
+        "rmse_vs_fp64": float(np.sqrt(np.mean(err.astype(np.float64) ** 2))),
+        "rmse_sample": f"{len(rows)} of 512 rows of bins", "timing": "median of 3 after 3 warm-up, device"}
+    # -- batch of 4096 independent integrals (dims 2-6, budgets 256..65536, MC or nested)
+    items = scenes.batch_items(4096, seed=11)
+    prep = _lib.batch_items(items)
+    st_nested = _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37)
+    r, st, rep = ctx.integrate_batch(scenes.HALFSPACE, prep, st_nested)  # first call: layout + autotune
+    item_ms = np.zeros(4096, np.float32)
+    runs = [ctx.integrate_batch_resident(r, item_ms=item_ms) for _ in range(3)]
+    ms = statistics.median(s_.device_ms for s_, _ in runs)
+    t0 = time.perf_counter()
+    for _ in range(2):
+        ctx.integrate_batch(scenes.HALFSPACE, prep, st_nested, results=r)
+    e2e_ms = (time.perf_counter() - t0) / 2 * 1e3
+    out["batch"] = {
+        "workload": "4096 independent integrals over [0,1]^d, d uniform in 2..6, prod_d exp(-a x)cos(b x) times a "
+                    "random half-space indicator, budget log-uniform 256..65536 (MC samples or nested(simpson,"
+                    "trapezoidal) regions), seed 11",
+        "ms": round(ms, 2), "gsamples_s": round(runs[-1][0].evaluations / (ms * 1e6), 3),
+        "evaluations": int(runs[-1][0].evaluations), "nested_regions": int(rep.nested_regions),
+        "item_ms_p50": round(float(np.percentile(item_ms, 50)), 4),
+        "item_ms_p99": round(float(np.percentile(item_ms, 99)), 2), "item_ms_max": round(float(item_ms.max()), 2),
+        "threads": runs[-1][1].threads, "blocks": runs[-1][1].blocks,
+        "e2e_ms": round(e2e_ms, 2),
+        "timing": "resident: median of 3 graph launches (device); e2e: host items -> results through "
+                  "vcu_integrate_batch, wall clock"}
+    out["learned_vs_plain"] = time_to_rmse(ctx)
+    return out
+
+
+def time_to_rmse(ctx, target: float = 1e-3) -> dict:
+    """Wall time (device, one call) each estimator needs to reach bin RMSE <= target against the
+    truth: plain Monte Carlo, the polynomial control variate (crespo2021, 2^14 regions) and the learned
+    control variate (1000 training steps), each with the sample count doubled until it gets there (or
+    a cap).  Two integrands: the 5-D occluded scene (2 bin dims + 3 primary dims; truth = 16 x 65536
+    Monte Carlo samples per bin, whose own squared standard error is subtracted) at 64x64 bins, and
+    sin(8x)e^-y + x^2 + y^2 at 8x8 bins (closed-form truth)."""
+    from viltrum_gb300 import _lib, scenes
+
+    res = {}
+    cases = [("occluded_scene5_64x64", scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), 5, [64, 64]),
+             ("wave2_8x8", scenes.WAVE2, None, 2, [8, 8])]
+    for name, kind, params, dim, bres in cases:
+        nb = bres[0] * bres[1]
+        p = ctx.problem(kind, params, [0] * dim, [1] * dim, bres)
+        if kind == scenes.WAVE2:
+            truth = scenes.exact_bins(kind, None, [0, 0], [1, 1], bres)[:, 0]
+            se2 = 0.0
+        else:
+            acc = np.zeros(nb)
+            acc2 = np.zeros(nb)
+            for k in range(16):
+                b = np.empty(nb, np.float32)
+                ctx.per_bin_monte_carlo(p, 1 << 16, 1000 + k, b)
+                acc += b
+                acc2 += b.astype(np.float64) ** 2
+            truth = acc / 16
+            se2 = float(np.mean(np.maximum(acc2 / 16 - truth ** 2, 0.0) / 15))
+
+        def rmse(b):
+            return float(np.sqrt(max(np.mean((b.astype(np.float64) - truth) ** 2) - se2, 0.0)))
+
+        def sweep(run, start, cap):
+            spp, best = start, None
+            while spp <= cap:
+                b, ms = run(spp)
+                e = rmse(b)
+                best = (spp, e, ms)
+                if e <= target:
+                    return {"reached": True, "spp": spp, "rmse": e, "ms": round(ms, 3)}
+                spp *= 2
+            return {"reached": False, "spp": best[0], "rmse": best[1], "ms": round(best[2], 3)}
+
+        def mc(spp):
+            b = np.empty(nb, np.float32)
+            st = ctx.per_bin_monte_carlo(p, spp, 5, b)
+            return b, st.device_ms
+
+        def cv(spp):
+            b = np.empty(nb, np.float32)
+            st = ctx.control_variates(p, _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37), (1 << 14) - 1,
+                                      _lib.CvOpts(spp, 5, 0, 0, 1.0), b)
+            return b, st.device_ms
+
+        def lcv(spp):
+            b = np.empty(nb, np.float32)
+            q, cells = (3, 2) if dim == 5 else (4, 4)
+            st, rep = ctx.learned_control_variates(p, _lib.LearnedOpts(spp, 5, 1000, 32768, 3e-3, q, 1, cells), b)
+            return b, st.device_ms
+
+        cap = 1 << 17
+        res[name] = {"plain_mc": sweep(mc, 64, cap), "polynomial_cv": sweep(cv, 64, 1 << 12),
+                     "learned_cv": sweep(lcv, 64, 1 << 14)}
+        m, l = res[name]["plain_mc"], res[name]["learned_cv"]
+        res[name]["learned_over_plain_ms"] = round(l["ms"] / m["ms"], 3) if (m["reached"] and l["reached"]) else None
+    res["target_rmse"] = target
+    res["timing"] = "device time of the one call that reached the target (training and region construction included)"
+    return res
 
 
 def _traffic_from_profile(nbins: int):
@@ -324,6 +470,7 @@ def main(argv=None) -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", type=int, default=512, help="bins per side (512 is the benchmark workload)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' lines")
     args = ap.parse_args(argv)
     global RES
     RES = [args.res, args.res]

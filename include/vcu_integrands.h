@@ -119,9 +119,7 @@ constexpr float kInvFact10 = 2.755731998149713e-07f;
 /* e^x: x = k ln2 + r, |r| <= ln2/2, e^r by its degree-7 Taylor polynomial (truncation error
  * < 6e-9 relative), times 2^k assembled in the exponent field.  Results below 2^-126 are
  * returned as 0 (no denormals), results above FLT_MAX as +inf.                              */
-VCU_HD float vexp(float x) {
-    if (!(x > -87.0f)) return (x != x) ? x : 0.0f;
-    if (x > 88.5f) return bits_to_float(0x7f800000u);
+VCU_HD float vexp_core(float x) {
     /* k = rint(x log2e) by the 1.5*2^23 shift (exact round-to-nearest-even for |t| < 2^22);
      * the integer k is the difference of the two bit patterns, no float->int conversion */
     const float t = vadd(vmul(x, kLog2e), 12582912.0f);
@@ -143,6 +141,13 @@ VCU_HD float vexp(float x) {
     const float s1 = bits_to_float((uint32_t)(k1 + 127) << 23);
     const float s2 = bits_to_float((uint32_t)(k2 + 127) << 23);
     return vmul(vmul(p, s1), s2);
+}
+/* branch-free: the core runs on the clamped argument and the special results are selected, so
+ * that loops of exponentials (and two interleaved evaluations) compile without divergent branches */
+VCU_HD float vexp(float x) {
+    const float xc = (x > 88.5f) ? 88.5f : ((x > -87.0f) ? x : -87.0f);
+    const float core = vexp_core(xc);
+    return (x > -87.0f) ? ((x > 88.5f) ? bits_to_float(0x7f800000u) : core) : ((x != x) ? x : 0.0f);
 }
 
 /* sin and cos of the reduced argument |r| <= pi/4 (Taylor to degree 9 and 10). */
@@ -285,6 +290,30 @@ struct Scene2 {
         return acc;
     }
     VCU_HD void operator()(const float* x, float* out) const { out[0] = eval(x[0], x[1]); }
+    /* two points at once, each with exactly the arithmetic of eval(): independent chains */
+    VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
+        float a0 = 0.0f, a1 = 0.0f;
+        for (int i = 0; i < ng; ++i) {
+            const float gx = g[i][0], gy = g[i][1], gs = g[i][2], ga = g[i][3];
+            const float dx0 = vsub(x0[0], gx), dy0 = vsub(x0[1], gy);
+            const float dx1 = vsub(x1[0], gx), dy1 = vsub(x1[1], gy);
+            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
+            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
+            a0 = vfma(ga, vexp(vmul(r0, gs)), a0);
+            a1 = vfma(ga, vexp(vmul(r1, gs)), a1);
+        }
+        for (int i = 0; i < nd; ++i) {
+            const float cx = d[i][0], cy = d[i][1], rr = d[i][2], dv = d[i][3];
+            const float dx0 = vsub(x0[0], cx), dy0 = vsub(x0[1], cy);
+            const float dx1 = vsub(x1[0], cx), dy1 = vsub(x1[1], cy);
+            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
+            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
+            a0 = vadd(a0, (r0 <= rr) ? dv : 0.0f);
+            a1 = vadd(a1, (r1 <= rr) ? dv : 0.0f);
+        }
+        o0[0] = a0;
+        o1[0] = a1;
+    }
 };
 
 /* Moving scene, 3 channels, on (x, y, t):
@@ -347,6 +376,44 @@ struct MovingScene3 {
         out[0] = c0;
         out[1] = c1;
         out[2] = c2;
+    }
+    /* two points at once, each with exactly the arithmetic of operator() */
+    VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
+        float g0 = 0.0f, g1 = 0.0f;
+        for (int i = 0; i < ng; ++i) {
+            const float gx = g[i][0], gy = g[i][1], gs = g[i][2], ga = g[i][3];
+            const float dx0 = vsub(x0[0], gx), dy0 = vsub(x0[1], gy);
+            const float dx1 = vsub(x1[0], gx), dy1 = vsub(x1[1], gy);
+            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
+            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
+            g0 = vfma(ga, vexp(vmul(r0, gs)), g0);
+            g1 = vfma(ga, vexp(vmul(r1, gs)), g1);
+        }
+        float a0 = g0, a1 = g0, a2 = g0, b0 = g1, b1 = g1, b2 = g1;
+        for (int i = 0; i < nd; ++i) {
+            const float cx0 = vfma(x0[2], d[i][2], d[i][0]), cy0 = vfma(x0[2], d[i][3], d[i][1]);
+            const float cx1 = vfma(x1[2], d[i][2], d[i][0]), cy1 = vfma(x1[2], d[i][3], d[i][1]);
+            const float dx0 = vsub(x0[0], cx0), dy0 = vsub(x0[1], cy0);
+            const float dx1 = vsub(x1[0], cx1), dy1 = vsub(x1[1], cy1);
+            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
+            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
+            if (r0 <= d[i][4]) {
+                a0 = vadd(a0, d[i][5]);
+                a1 = vadd(a1, d[i][6]);
+                a2 = vadd(a2, d[i][7]);
+            }
+            if (r1 <= d[i][4]) {
+                b0 = vadd(b0, d[i][5]);
+                b1 = vadd(b1, d[i][6]);
+                b2 = vadd(b2, d[i][7]);
+            }
+        }
+        o0[0] = a0;
+        o0[1] = a1;
+        o0[2] = a2;
+        o1[0] = b0;
+        o1[1] = b1;
+        o1[2] = b2;
     }
 };
 
@@ -437,6 +504,44 @@ struct OccludedScene5 {
     VCU_HD void operator()(const float* x, float* out) const {
         const float s = scene.eval(x[0], x[1]);
         out[0] = (s == 0.0f) ? 0.0f : vmul(s, visibility(x));
+    }
+    /* two points at once: the scene by Scene2::pair, then both segments against the boxes in one
+     * loop that ends when both are blocked (each point's result is that of operator()) */
+    VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
+        float s[2];
+        {
+            const float a0[2] = {x0[0], x0[1]}, a1[2] = {x1[0], x1[1]};
+            scene.pair(a0, a1, &s[0], &s[1]);
+        }
+        const float* xs[2] = {x0, x1};
+        float o[2][3], inv[2][3];
+        for (int p = 0; p < 2; ++p) {
+            const float e[3] = {xs[p][2], xs[p][3], vfma(0.75f, xs[p][4], 0.25f)};
+            o[p][0] = xs[p][0];
+            o[p][1] = xs[p][1];
+            o[p][2] = 0.0f;
+            for (int k = 0; k < 3; ++k) inv[p][k] = vdiv(1.0f, vsub(e[k], o[p][k]));
+        }
+        bool blocked0 = false, blocked1 = false;
+        for (int i = 0; i < nb && !(blocked0 && blocked1); ++i) {
+            float t00 = 0.0f, t01 = 1.0f, t10 = 0.0f, t11 = 1.0f;
+            for (int k = 0; k < 3; ++k) {
+                float ta = vmul(vsub(lo[i][k], o[0][k]), inv[0][k]);
+                float tb = vmul(vsub(hi[i][k], o[0][k]), inv[0][k]);
+                if (ta > tb) { const float w = ta; ta = tb; tb = w; }
+                t00 = (ta > t00) ? ta : t00;
+                t01 = (tb < t01) ? tb : t01;
+                float ua = vmul(vsub(lo[i][k], o[1][k]), inv[1][k]);
+                float ub = vmul(vsub(hi[i][k], o[1][k]), inv[1][k]);
+                if (ua > ub) { const float w = ua; ua = ub; ub = w; }
+                t10 = (ua > t10) ? ua : t10;
+                t11 = (ub < t11) ? ub : t11;
+            }
+            blocked0 = blocked0 || (t00 <= t01);
+            blocked1 = blocked1 || (t10 <= t11);
+        }
+        o0[0] = (s[0] == 0.0f) ? 0.0f : vmul(s[0], blocked0 ? 0.0f : 1.0f);
+        o1[0] = (s[1] == 0.0f) ? 0.0f : vmul(s[1], blocked1 ? 0.0f : 1.0f);
     }
 };
 

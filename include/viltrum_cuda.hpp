@@ -261,5 +261,132 @@ public:
     }
 };
 
+/* ---------------------------------------------------------------- control variates */
+/* drop-in for integrator_region_based(regions_generator_adaptive_heap(nested(H,L), heuristic,
+ * iterations), regions_integrator_parallel_variance_reduction(rr_uniform_region(), weight,
+ * region_sampling_uniform(), std::mt19937(seed), samples)) -- integrator_crespo2021(iterations,
+ * samples, seed) with crespo2021() (src/control-variates/integrator-crespo2021.h:7-22); assigns.
+ * weight: cv_optimize_weight() (VCU_CV_OPTIMIZE) or cv_fixed_weight(alpha) (VCU_CV_FIXED). */
+class control_variates {
+    nested_rule rule_;
+    unsigned long iterations_, samples_;
+    std::uint64_t seed_;
+    int weight_;
+    double alpha_;
+
+public:
+    control_variates(nested_rule r, unsigned long iterations, unsigned long samples, std::uint64_t seed,
+                     int weight = VCU_CV_OPTIMIZE, double alpha = 1.0)
+        : rule_(r), iterations_(iterations), samples_(samples), seed_(seed), weight_(weight), alpha_(alpha) {}
+
+    template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
+    void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
+                   Logger& logger) const {
+        const builtin_integrand& fi = detail::as_builtin(f);
+        context& ctx = thread_context();
+        logger.log_progress(std::size_t(0), std::size_t(1));
+        vcu_problem p = detail::make_problem(fi, res, range);
+        const int ch = fi.channels();
+        std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
+        vcu_cv cv{};
+        cv.samples_per_bin = samples_;
+        cv.seed = seed_;
+        cv.weight = weight_;
+        cv.alpha = alpha_;
+        vcu_stats st{};
+        ctx.check(vcu_control_variates(ctx.get(), &p, &rule_.n, iterations_, &cv, nullptr, out.data(), nullptr,
+                                       nullptr, &st));
+        detail::write_back(bins, res, out, ch, false);
+        logger.log_progress(std::size_t(1), std::size_t(1));
+    }
+};
+
+/* nested(simpson, trapezoidal) with error_heuristic_size(error_metric_relative()), as
+ * integrator_crespo2021 builds it */
+inline nested_rule crespo2021_rule() { return simpson_trapezoidal(VCU_HEUR_SIZE, VCU_METRIC_RELATIVE); }
+inline control_variates crespo2021(unsigned long iterations, unsigned long samples, std::uint64_t seed = 0) {
+    return control_variates(crespo2021_rule(), iterations, samples, seed);
+}
+
+/* ---------------------------------------------------------------- learned control variate */
+/* No reference counterpart: per bin, a frequency-encoded 4x64 MLP g trained online on the
+ * integrand's own samples, its integral by composite Gauss-Legendre quadrature, and only f - g
+ * sampled (vcu_learned_control_variates); assigns. */
+class learned_control_variates {
+    vcu_learned opt_;
+
+public:
+    explicit learned_control_variates(unsigned long samples, std::uint64_t seed = 0, unsigned train_steps = 1000,
+                                      unsigned batch = 32768, float learning_rate = 3e-3f, unsigned quad_nodes = 3,
+                                      int quad_cells = 1, bool fallback = true)
+        : opt_{} {
+        opt_.samples_per_bin = samples;
+        opt_.seed = seed;
+        opt_.train_steps = train_steps;
+        opt_.batch = batch;
+        opt_.learning_rate = learning_rate;
+        opt_.quad_nodes = quad_nodes;
+        opt_.fallback = fallback ? 1 : 0;
+        opt_.quad_cells = quad_cells;
+    }
+
+    template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
+    void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
+                   Logger& logger) const {
+        const builtin_integrand& fi = detail::as_builtin(f);
+        context& ctx = thread_context();
+        logger.log_progress(std::size_t(0), std::size_t(1));
+        vcu_problem p = detail::make_problem(fi, res, range);
+        std::vector<float> out(detail::bin_count(res));
+        vcu_stats st{};
+        ctx.check(vcu_learned_control_variates(ctx.get(), &p, &opt_, out.data(), nullptr, nullptr, &st));
+        detail::write_back(bins, res, out, 1, false);
+        logger.log_progress(std::size_t(1), std::size_t(1));
+    }
+};
+
+/* ---------------------------------------------------------------- independent integrals */
+/* Many single-value viltrum::integrate(I, f, range) calls at once (vcu_integrate_batch): item i
+ * uses monte_carlo(budget, seed) (method VCU_BATCH_MONTE_CARLO) or
+ * integrator_adaptive_iterations(nested, budget - 1) (VCU_BATCH_NESTED) over its own range with its
+ * own parameters of one integrand family.  Returns the values in item order. */
+struct batch_item {
+    int dim = 0;
+    int method = VCU_BATCH_NESTED;
+    std::uint64_t budget = 1, seed = 0;
+    std::array<float, VCU_MAX_DIM> range_min{}, range_max{};
+    std::vector<float> params;
+};
+
+inline std::vector<float> integrate_batch(int32_t kind, const std::vector<batch_item>& items,
+                                          nested_rule rule = simpson_trapezoidal(),
+                                          std::vector<float>* item_ms = nullptr) {
+    context& ctx = thread_context();
+    std::vector<vcu_batch_item> c(items.size());
+    for (std::size_t i = 0; i < items.size(); ++i) {
+        vcu_batch_item& b = c[i];
+        b = vcu_batch_item{};
+        b.dim = items[i].dim;
+        b.method = items[i].method;
+        b.budget = items[i].budget;
+        b.seed = items[i].seed;
+        for (int d = 0; d < VCU_MAX_DIM; ++d) {
+            b.range_min[d] = items[i].range_min[d];
+            b.range_max[d] = items[i].range_max[d];
+        }
+        b.n_params = (int32_t)items[i].params.size();
+        b.params = items[i].params.empty() ? nullptr : items[i].params.data();
+    }
+    std::vector<float> out(items.size());
+    vcu_batch_report rep{};
+    if (item_ms) {
+        item_ms->assign(items.size(), 0.0f);
+        rep.item_ms = item_ms->data();
+    }
+    ctx.check(vcu_integrate_batch(ctx.get(), kind, &rule.n, c.data(), c.size(), out.data(), VCU_MEM_HOST, &rep,
+                                  nullptr));
+    return out;
+}
+
 }  // namespace cuda
 }  // namespace viltrum

@@ -46,3 +46,31 @@ def test_host_logic_without_device(lib_path):
     assert lib.vcu_integrate_batch(None, 7, None, None, 0, None, 0, None, None) == 1
     assert lib.vcu_integrate_batch_resident(None, None, 0, None, None) == 1
     assert lib.vcu_destroy(None) == 0
+
+
+def _compile_dropin(extra, out=None):
+    cmd = ["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), *extra,
+           os.path.join(ROOT, "tests", "cpp", "dropin.cc")]
+    if out:
+        cmd += ["-L", os.path.join(ROOT, "viltrum_gb300"), "-lviltrum_cuda", "-o", out]
+    else:
+        cmd += ["-fsyntax-only"]
+    return subprocess.run(cmd, capture_output=True, text=True)
+
+
+REFERENCE = "/root/reference"
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REFERENCE, "viltrum.h")), reason="reference sources absent")
+def test_cpp_dropin_compiles_against_reference():
+    """The CUDA integrators of include/viltrum_cuda.hpp go through the reference's own
+    viltrum::integrate(integrator, bins, f, range) (src/integrate.h:72-97) wherever a CPU per-bin
+    integrator would: the example compiles against the unmodified reference headers."""
+    r = _compile_dropin(["-DWITH_VILTRUM", "-I", REFERENCE])
+    assert r.returncode == 0, r.stderr
+
+
+def test_cpp_dropin_links(lib_path, tmp_path):
+    """The standalone form of the example links against libviltrum_cuda.so with the host compiler only."""
+    r = _compile_dropin(["-O1"], out=str(tmp_path / "dropin"))
+    assert r.returncode == 0, r.stderr

@@ -104,16 +104,6 @@ __device__ float region_integral_ref(const float* __restrict__ V, const float* A
     return buf[0];
 }
 
-/* fn(integral_constant<int, 0>), ..., fn(integral_constant<int, N-1>): loops whose index must be a
- * compile-time constant (strides, divisors) */
-template <class Fn, int... I>
-__device__ __forceinline__ void static_for_impl(Fn& fn, std::integer_sequence<int, I...>) {
-    (fn(std::integral_constant<int, I>{}), ...);
-}
-template <int N, class Fn> __device__ __forceinline__ void static_for(Fn fn) {
-    static_for_impl(fn, std::make_integer_sequence<int, N>{});
-}
-
 __device__ __forceinline__ uint64_t globaltimer() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

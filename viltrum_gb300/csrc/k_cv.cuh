@@ -81,51 +81,64 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
     constexpr int NNEW = (S - 1) * NL;
     extern __shared__ float smem[];
     __shared__ float CO[DIM * S], CN[S - 1];
-    __shared__ float LN[2 * DIM * NL];
+    __shared__ float LN[2 * DIM * NL], LF[(2 * DIM * NL + S - 1) / S];
     __shared__ float EC[2 * DIM];
+    __shared__ float VC0[SD * CH], VC1[SD * CH]; /* the two children of the current split, on chip */
     const int nheap = cfg.iters + 1;
     float* HE = cfg.heap_in_smem ? smem : heap_key;
     int* HS = cfg.heap_in_smem ? reinterpret_cast<int*>(smem + nheap) : heap_pay;
     const int tid = threadIdx.x;
 
-    auto errors = [&](int nreg, int r0, int r1) {
-        for (int t = tid; t < nreg * DIM * NL; t += GEN_THREADS) {
-            const int r = t / (DIM * NL), rr = t % (DIM * NL);
-            const int d = rr / NL, J = rr % NL;
-            const float* RV = vals + (size_t)(r ? r1 : r0) * SD * CH;
-            float m = 0.0f;
+    /* error estimates of the regions whose node values are R0 (and R1) into EC[r*DIM + d]
+     * (region.h:379-418): line metrics with compile-time strides, then the folds level by level */
+    auto errors = [&](int nreg, const float* R0, const float* R1, int r0, int r1) {
+        static_for<DIM>([&](auto dc) {
+            constexpr int d = decltype(dc)::value;
+            constexpr int PD = ipow(S, d);
+            for (int t = tid; t < nreg * NL; t += GEN_THREADS) {
+                const int r = t >= NL ? 1 : 0;
+                const int J = t - r * NL;
+                const float* RV = (r ? R1 : R0) + (J % PD + (J / PD) * (PD * S)) * CH;
+                float m = 0.0f;
 #pragma unroll
-            for (int c = 0; c < CH; ++c) {
-                float line[S], low[SL];
+                for (int c = 0; c < CH; ++c) {
+                    float line[S], low[SL];
 #pragma unroll
-                for (int i = 0; i < S; ++i) line[i] = RV[node_index<DIM, S>(d, J, i) * CH + c];
+                    for (int i = 0; i < S; ++i) line[i] = RV[i * PD * CH + c];
 #pragma unroll
-                for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
-                float H, L;
-                if constexpr (CH == 1) {
-                    H = RefRule<S>::scalar(line);
-                    L = RefRule<SL>::scalar(low);
-                } else {
-                    H = RefRule<S>::rgb(line);
-                    L = RefRule<SL>::rgb(low);
+                    for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+                    float H, L;
+                    if constexpr (CH == 1) {
+                        H = RefRule<S>::scalar(line);
+                        L = RefRule<SL>::scalar(low);
+                    } else {
+                        H = RefRule<S>::rgb(line);
+                        L = RefRule<SL>::rgb(low);
+                    }
+                    const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
+                    m = (c == 0) ? mv : vadd(m, mv);
                 }
-                const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
-                m = (c == 0) ? mv : vadd(m, mv);
+                LN[(r * DIM + d) * NL + J] = m;
             }
-            LN[t] = m;
-        }
+        });
         __syncthreads();
-        for (int t = tid; t < nreg * DIM; t += GEN_THREADS) {
-            const int r = t / DIM;
-            float buf[NL];
-            for (int i = 0; i < NL; ++i) buf[i] = LN[t * NL + i];
-            int n = NL;
-            for (int level = 0; level < DIM - 1; ++level) {
-                n /= S;
-                for (int i = 0; i < n; ++i) buf[i] = RefRule<S>::scalar(buf + i * S);
+        float* src = LN;
+        float* dst = LF;
+        static_for<DIM - 1>([&](auto lc) {
+            constexpr int n = NL / ipow(S, decltype(lc)::value), m = n / S;
+            for (int t = tid; t < nreg * DIM * m; t += GEN_THREADS) {
+                const int rd = t / m, i = t - rd * m;
+                float tmp[S];
+#pragma unroll
+                for (int j = 0; j < S; ++j) tmp[j] = src[rd * n + i * S + j];
+                dst[rd * m + i] = RefRule<S>::scalar(tmp);
             }
-            EC[t] = vmul(vol[r ? r1 : r0], buf[0]);
-        }
+            __syncthreads();
+            float* sw = src;
+            src = dst;
+            dst = sw;
+        });
+        if (tid < nreg * DIM) EC[tid] = vmul(vol[(tid / DIM) ? r1 : r0], src[tid]);
         __syncthreads();
     };
     auto heuristic = [&](int r, int id, float& err_out, int& dim_out) {
@@ -185,10 +198,13 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
         }
         float v[CH];
         f(x, v);
-        for (int c = 0; c < CH; ++c) vals[t * CH + c] = v[c];
+        for (int c = 0; c < CH; ++c) {
+            vals[t * CH + c] = v[c];
+            VC0[t * CH + c] = v[c];
+        }
     }
     __syncthreads();
-    errors(1, 0, 0);
+    errors(1, VC0, VC0, 0, 0);
     if (tid == 0) {
         float e;
         int dm;
@@ -216,44 +232,58 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
         const float* VP = vals + (size_t)P * SD * CH;
         float* V0 = vals + (size_t)C0 * SD * CH;
         float* V1 = vals + (size_t)C1 * SD * CH;
-        for (int t = tid; t < NNEW + S * NL; t += GEN_THREADS) {
-            if (t < NNEW) {
-                const int k = t / NL, J = t % NL;
-                float x[F::DIM];
-                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
-                int rem = J;
-                for (int e = 0; e < DIM; ++e) {
-                    if (e == dd) continue;
-                    x[e] = CO[e * S + rem % S];
-                    rem /= S;
-                }
-                x[dd] = CN[k];
+        /* new nodes at the odd positions, parent nodes at the even (region.h:345-359, split.h:13-49),
+         * built on chip and copied to the pool; one instance per split dimension */
+        auto build_children = [&](auto ddc) {
+            constexpr int DD = decltype(ddc)::value;
+            constexpr int PD = ipow(S, DD);
+            for (int t = tid; t < NNEW + S * NL; t += GEN_THREADS) {
+                const bool fresh = t < NNEW;
+                const int u = fresh ? t : t - NNEW;
+                const int q = u / NL, J = u - q * NL;
+                const int base = J % PD + (J / PD) * (PD * S);
                 float v[CH];
-                f(x, v);
-                const int i = 2 * k + 1;
+                int i;
+                if (fresh) {
+                    float x[F::DIM];
+#pragma unroll
+                    for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+                    static_for<DIM>([&](auto ec) {
+                        constexpr int e = decltype(ec)::value;
+                        if constexpr (e != DD) {
+                            constexpr int pe = e < DD ? ipow(S, e) : ipow(S, e - 1);
+                            x[e] = CO[e * S + (J / pe) % S];
+                        }
+                    });
+                    x[DD] = CN[q];
+                    f(x, v);
+                    i = 2 * q + 1;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) v[c] = VP[(base + q * PD) * CH + c];
+                    i = 2 * q;
+                }
                 if (i <= S - 1) {
-                    const int n0 = node_index<DIM, S>(dd, J, i);
-                    for (int c = 0; c < CH; ++c) V0[n0 * CH + c] = v[c];
+                    const int n0 = (base + i * PD) * CH;
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        VC0[n0 + c] = v[c];
+                        V0[n0 + c] = v[c];
+                    }
                 }
                 if (i >= S - 1) {
-                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
-                    for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = v[c];
-                }
-            } else {
-                const int u = t - NNEW;
-                const int m = u / NL, J = u % NL;
-                const int i = 2 * m;
-                const int src = node_index<DIM, S>(dd, J, m);
-                if (i <= S - 1) {
-                    const int n0 = node_index<DIM, S>(dd, J, i);
-                    for (int c = 0; c < CH; ++c) V0[n0 * CH + c] = VP[src * CH + c];
-                }
-                if (i >= S - 1) {
-                    const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
-                    for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = VP[src * CH + c];
+                    const int n1 = (base + (i - (S - 1)) * PD) * CH;
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        VC1[n1 + c] = v[c];
+                        V1[n1 + c] = v[c];
+                    }
                 }
             }
-        }
+        };
+        static_for<DIM>([&](auto dc) {
+            if (dd == decltype(dc)::value) build_children(dc);
+        });
         if (tid == 0) {
             const float pmn = pmin[dd], pmx = pmax[dd];
             const float half = vdiv(vsub(pmx, pmn), 2.0f);
@@ -274,7 +304,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
             vol[C1] = v1;
         }
         __syncthreads();
-        errors(2, C0, C1);
+        errors(2, VC0, VC1, C0, C1);
         if (tid == 0) {
             float e0, e1;
             int d0, d1;

@@ -9,7 +9,8 @@
  * coordinates from Philox4x32-10 (key = seed, counter = (j, b_lo, b_hi, block)) -- or, in replay
  * mode, from a caller-supplied point array -- maps them into the bin as u*(max-min)+min (the
  * reference's uniform_real_distribution arithmetic), evaluates the integrand and accumulates it
- * with a Kahan-compensated FP32 sum.  The 32 lane sums are combined by warp shuffles in FP64,
+ * with a Kahan-compensated FP32 sum (integrands that evaluate two points at once take samples j and
+ * j+32 together, as two independent dependency chains, and add them in sample order).  The 32 lane sums are combined by warp shuffles in FP64,
  * scaled by prod(res)*volume(bin)/samples, staged in shared memory and written with coalesced
  * stores (float4 when a block's run of bins is 16-byte aligned).
  */
@@ -51,8 +52,7 @@ __global__ void __launch_bounds__(MC_WARPS * 32)
             vol = vmul(vol, w[d]);
         }
         const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
-        for (uint64_t s = lane; s < spp; s += 32) {
-            float x[F::DIM];
+        auto point = [&](uint64_t s, float* x) {
 #pragma unroll
             for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
             if constexpr (REPLAY) {
@@ -71,14 +71,33 @@ __global__ void __launch_bounds__(MC_WARPS * 32)
                     }
                 }
             }
-            float v[CH];
-            f(x, v);
+        };
+        auto kahan = [&](const float* v) {
 #pragma unroll
             for (int c = 0; c < CH; ++c) {
                 const float y = vsub(v[c], comp[c]);
                 const float t = vadd(sum[c], y);
                 comp[c] = vsub(vsub(t, sum[c]), y);
                 sum[c] = t;
+            }
+        };
+        if constexpr (has_pair<F>::value) {
+            /* samples s and s+32 of this lane as two independent chains, added in sample order */
+            for (uint64_t s = lane; s < spp; s += 64) {
+                const bool two = s + 32 < spp;
+                float x0[F::DIM], x1[F::DIM], v0[CH], v1[CH];
+                point(s, x0);
+                point(two ? s + 32 : s, x1);
+                f.pair(x0, x1, v0, v1);
+                kahan(v0);
+                if (two) kahan(v1);
+            }
+        } else {
+            for (uint64_t s = lane; s < spp; s += 32) {
+                float x[F::DIM], v[CH];
+                point(s, x);
+                f(x, v);
+                kahan(v);
             }
         }
     }

@@ -15,8 +15,8 @@
  * persistent grid sized by occupancy).  All node values of the bin's live regions, their ranges,
  * the heap and the scratch of the error folds live in the group's slice of shared memory; the
  * group evaluates the integrand at a region's new nodes in parallel (Boole 2-D: 20 new nodes per
- * split, 5 rounds of 4 lanes), folds the per-line error metrics in parallel, and one lane keeps
- * the heap.  Nothing touches global memory but the integrand parameters (kernel parameter space)
+ * split; with 8 lanes and integrands that evaluate two points as independent chains, two rounds of
+ * 16 + 4 nodes), folds the per-line error metrics in parallel, and one lane keeps the heap.  Nothing touches global memory but the integrand parameters (kernel parameter space)
  * and the bin writes.
  */
 #pragma once
@@ -194,8 +194,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
             CO[t] = node_coord((double)j / (double)(S - 1), vsub(bmax[d], bmin[d]), bmin[d]);
         }
         __syncwarp(gmask);
-        for (int t = gl; t < SD; t += G) {
-            float x[F::DIM];
+        auto root_x = [&](int t, float* x) {
 #pragma unroll
             for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
             int rem = t;
@@ -204,10 +203,29 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                 x[d] = CO[d * S + rem % S];
                 rem /= S;
             }
-            float v[CH];
-            f(x, v);
+        };
+        if constexpr (has_pair<F>::value) {
+            for (int t = gl; t < SD; t += 2 * G) {
+                const int t2 = t + G < SD ? t + G : t;
+                float x0[F::DIM], x1[F::DIM], v0[CH], v1[CH];
+                root_x(t, x0);
+                root_x(t2, x1);
+                f.pair(x0, x1, v0, v1);
 #pragma unroll
-            for (int c = 0; c < CH; ++c) V[t * CH + c] = v[c];
+                for (int c = 0; c < CH; ++c) V[t * CH + c] = v0[c];
+                if (t2 != t) {
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) V[t2 * CH + c] = v1[c];
+                }
+            }
+        } else {
+            for (int t = gl; t < SD; t += G) {
+                float x[F::DIM], v[CH];
+                root_x(t, x);
+                f(x, v);
+#pragma unroll
+                for (int c = 0; c < CH; ++c) V[t * CH + c] = v[c];
+            }
         }
         __syncwarp(gmask);
 
@@ -315,10 +333,10 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
             float* VP = V + (size_t)P * SD * CH;
             float* V0 = V + (size_t)C0 * SD * CH;
             float* V1 = V + (size_t)C1 * SD * CH;
-            /* new nodes: odd positions of the 2(S-1)+1 grid along dd */
-            for (int t = gl; t < NNEW; t += G) {
+            /* new nodes: odd positions of the 2(S-1)+1 grid along dd; two per lane and round when the
+             * integrand can evaluate two points as independent chains */
+            auto node_x = [&](int t, float* x) {
                 const int k = t / NL, J = t % NL;
-                float x[F::DIM];
 #pragma unroll
                 for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
                 int rem = J;
@@ -329,8 +347,9 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                     rem /= S;
                 }
                 x[dd] = CN[k];
-                float v[CH];
-                f(x, v);
+            };
+            auto store_new = [&](int t, const float* v) {
+                const int k = t / NL, J = t % NL;
                 const int i = 2 * k + 1;
                 if (i <= S - 1) {
                     const int n0 = node_index<DIM, S>(dd, J, i);
@@ -341,6 +360,24 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                     const int n1 = node_index<DIM, S>(dd, J, i - (S - 1));
 #pragma unroll
                     for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = v[c];
+                }
+            };
+            if constexpr (has_pair<F>::value) {
+                for (int t = gl; t < NNEW; t += 2 * G) {
+                    const int t2 = t + G < NNEW ? t + G : t;
+                    float x0[F::DIM], x1[F::DIM], v0[CH], v1[CH];
+                    node_x(t, x0);
+                    node_x(t2, x1);
+                    f.pair(x0, x1, v0, v1);
+                    store_new(t, v0);
+                    if (t2 != t) store_new(t2, v1);
+                }
+            } else {
+                for (int t = gl; t < NNEW; t += G) {
+                    float x[F::DIM], v[CH];
+                    node_x(t, x);
+                    f(x, v);
+                    store_new(t, v);
                 }
             }
             /* parent nodes re-used at the even positions */

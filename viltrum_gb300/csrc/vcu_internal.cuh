@@ -11,6 +11,8 @@
 #include <cstring>
 #include <cmath>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/vcu_integrands.h"
@@ -143,6 +145,23 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
 }
 /* top 24 bits -> float in [0,1), exact */
 __device__ __forceinline__ float u01(uint32_t r) { return (float)(r >> 8) * 5.9604644775390625e-08f; }
+
+/* fn(integral_constant<int, 0>), ..., fn(integral_constant<int, N-1>): loops whose index must be a
+ * compile-time constant (strides, divisors) */
+template <class Fn, int... I>
+__device__ __forceinline__ void static_for_impl(Fn& fn, std::integer_sequence<int, I...>) {
+    (fn(std::integral_constant<int, I>{}), ...);
+}
+template <int N, class Fn> __device__ __forceinline__ void static_for(Fn fn) {
+    static_for_impl(fn, std::make_integer_sequence<int, N>{});
+}
+
+/* integrands that evaluate two points at once (two independent dependency chains per lane) */
+template <class F, class = void> struct has_pair : std::false_type {};
+template <class F>
+struct has_pair<F, std::void_t<decltype(std::declval<const F&>().pair((const float*)nullptr, (const float*)nullptr,
+                                                                        (float*)nullptr, (float*)nullptr))>>
+    : std::true_type {};
 
 /* Calls v(functor, channels) with the built-in functor selected by kind.  The functor object is
  * built on the host (vcu_integrands.h build()); its size decides the kernel parameter size. */
