@@ -118,6 +118,16 @@ def stripe(rank: int, world: int):
     return [0.0, rank / world], [1.0, (rank + 1) / world]
 
 
+def max_over_ranks(value: float, device: str = "cuda") -> float:
+    """the largest of every rank's value (the job's time is its slowest rank's)"""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args) -> dict | None:
     import torch
 
@@ -166,9 +176,7 @@ def run_ours(args) -> dict | None:
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
     total_ms = float(sum(step_ms))
     if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms)
     value = evals * ws / (total_ms * 1e-3) / 1e9
 
     # accuracy of this step's result against the FP64 closed-form bin integrals
@@ -460,6 +468,48 @@ def run_reference(args) -> dict | None:
     }
 
 
+def profile_workload(args) -> dict:
+    """One small run of a single workload, for profiler captures (--workload): warm-up calls, then
+    one call; prints its stats.  Not a benchmark line."""
+    import torch
+
+    import viltrum_gb300 as v
+    from viltrum_gb300 import _lib, scenes
+
+    torch.cuda.set_device(0)
+    ctx = v.Context(0)
+    r = args.res
+    w = args.workload
+    if w == "mc":
+        p = ctx.problem(scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), [0] * 5, [1] * 5, [r, r])
+        b = np.empty(r * r, np.float32)
+        call = lambda: ctx.per_bin_monte_carlo(p, 256, 5, b)
+    elif w == "cv":
+        p = ctx.problem(scenes.MOVING_SCENE3, scenes.moving_scene3(SEED), [0, 0, 0], [1, 1, 1], [r, r])
+        b = np.empty(r * r * 3, np.float32)
+        nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+        call = lambda: ctx.control_variates(p, nst, (1 << 12) - 1, _lib.CvOpts(16, 3, 0, 0, 1.0), b)
+    elif w == "batch":
+        items = _lib.batch_items(scenes.batch_items(256, seed=11, budget_hi=4096))
+        nst = _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37)
+        os.environ.setdefault("VCU_BATCH_THREADS", "512")
+        call = lambda: ctx.integrate_batch(scenes.HALFSPACE, items, nst)[1]
+    elif w == "learned":
+        p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [r, r])
+        b = np.empty(r * r, np.float32)
+        call = lambda: ctx.learned_control_variates(p, _lib.LearnedOpts(32, 5, 20, 32768, 3e-3, 3, 1, 1), b)[0]
+    else:  # nested
+        p = ctx.problem(scenes.SCENE2, scenes.scene2(SEED), [0, 0], [1, 1], [r, r])
+        b = np.empty(r * r, np.float32)
+        call = lambda: ctx.per_bin_adaptive_nested(p, _lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37), ITERS, b)
+    for _ in range(args.warmup):
+        call()
+    st = call()
+    ctx.close()
+    return {"workload": w, "res": r, "device_ms": st.device_ms, "evaluations": int(st.evaluations),
+            "kernel_launches": int(st.kernel_launches)}
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,11 +521,18 @@ def main(argv=None) -> int:
     ap.add_argument("--res", type=int, default=512, help="bins per side (512 is the benchmark workload)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' lines")
+    ap.add_argument("--workload", choices=["nested", "mc", "cv", "batch", "learned"], default=None,
+                    help="profiling aid: one small run of one workload (prints its stats, not a benchmark line)")
     args = ap.parse_args(argv)
     global RES
     RES = [args.res, args.res]
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
+    if args.workload is not None:
+        from viltrum_gb300 import build
+        build.build()
+        print(json.dumps(profile_workload(args)))
+        return 0
     if args.impl == "reference":
         line = run_reference(args)
     else:
