@@ -135,12 +135,12 @@ VCU_HD float vexp_core(float x) {
     p = vfma(p, r, kInvFact2);
     p = vfma(p, r, 1.0f);
     p = vfma(p, r, 1.0f);
-    /* k in [-126, 128]: 2^k as two factors so k = 128 never appears as an exponent */
+    /* k in [-126, 128] for the clamped argument: p * 2^k with 2^min(k,127) built in the exponent
+     * field (p in [0.7, 1.42], so p * 2^127 is exact) and one more doubling for k = 128 */
     const int ki = (int)(float_to_bits(t) - 0x4B400000u);
-    const int k1 = ki / 2, k2 = ki - k1;
-    const float s1 = bits_to_float((uint32_t)(k1 + 127) << 23);
-    const float s2 = bits_to_float((uint32_t)(k2 + 127) << 23);
-    return vmul(vmul(p, s1), s2);
+    const float s = bits_to_float((uint32_t)((ki < 127 ? ki : 127) + 127) << 23);
+    const float ps = vmul(p, s);
+    return (ki > 127) ? vmul(ps, 2.0f) : ps;
 }
 /* branch-free: the core runs on the clamped argument and the special results are selected, so
  * that loops of exponentials (and two interleaved evaluations) compile without divergent branches */

@@ -176,7 +176,8 @@ int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* n
  * accumulation -- trained online (Adam, mean squared error) on `batch` fresh Philox samples of the
  * integrand per step for `train_steps` steps by the library's own forward/backward kernels.  Per
  * bin, the integral of g is taken by composite Gauss-Legendre quadrature (`quad_cells` equal cells
- * per dimension, `quad_nodes` (1..4) nodes per cell and dimension) and only f - g is Monte Carlo
+ * per binned dimension, `quad_cells_unbinned` per unbinned dimension -- those span the whole range
+ * rather than one bin -- and `quad_nodes` (1..4) nodes per cell) and only f - g is Monte Carlo
  * sampled (`samples_per_bin` Philox points): the estimate is unbiased up to that quadrature's
  * error on the network; with
  * `fallback` set, a bin keeps the plain Monte Carlo mean of the same samples when its sample
@@ -189,9 +190,11 @@ typedef struct vcu_learned {
     float learning_rate;
     uint32_t quad_nodes;      /* Gauss-Legendre nodes per dimension for the integral of g, 1..4 */
     int32_t fallback;         /* 1: per-bin fallback to plain Monte Carlo                       */
-    int32_t quad_cells;       /* composite cells per dimension for the integral of g (0 = 1)    */
+    int32_t quad_cells;       /* composite cells per binned dimension for the integral of g (0 = 1) */
     float* theta_out;         /* nullable host buffer: receives the trained fp32 parameters
                                  (vcu_mlp_eval layout), e.g. to checkpoint the network        */
+    int32_t quad_cells_unbinned; /* cells per unbinned dimension (0 = quad_cells)             */
+    int32_t reserved2;
 } vcu_learned;
 
 typedef struct vcu_learned_report {

@@ -318,7 +318,7 @@ class learned_control_variates {
 public:
     explicit learned_control_variates(unsigned long samples, std::uint64_t seed = 0, unsigned train_steps = 1000,
                                       unsigned batch = 32768, float learning_rate = 3e-3f, unsigned quad_nodes = 3,
-                                      int quad_cells = 1, bool fallback = true)
+                                      int quad_cells = 1, bool fallback = true, int quad_cells_unbinned = 0)
         : opt_{} {
         opt_.samples_per_bin = samples;
         opt_.seed = seed;
@@ -328,6 +328,7 @@ public:
         opt_.quad_nodes = quad_nodes;
         opt_.fallback = fallback ? 1 : 0;
         opt_.quad_cells = quad_cells;
+        opt_.quad_cells_unbinned = quad_cells_unbinned;
     }
 
     template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>

@@ -67,7 +67,8 @@ class CvOpts(ctypes.Structure):
 class LearnedOpts(ctypes.Structure):
     _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("train_steps", ctypes.c_uint32),
                 ("batch", ctypes.c_uint32), ("learning_rate", ctypes.c_float), ("quad_nodes", ctypes.c_uint32),
-                ("fallback", ctypes.c_int32), ("quad_cells", ctypes.c_int32), ("theta_out", ctypes.c_void_p)]
+                ("fallback", ctypes.c_int32), ("quad_cells", ctypes.c_int32), ("theta_out", ctypes.c_void_p),
+                ("quad_cells_unbinned", ctypes.c_int32), ("reserved2", ctypes.c_int32)]
 
 
 class LearnedReport(ctypes.Structure):

@@ -568,11 +568,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         approx_d[c] = (double)approx[c];
     }
     /* residual samples */
-    double sf[CH], sa[CH];
-    for (int c = 0; c < CH; ++c) sf[c] = sa[c] = 0.0;
-    /* covariance moments of the sample norms (weight-strategy.h:187-208): Welford per lane,
-     * merged across lanes with Chan's pairwise formulas -- stable, like the reference's shifted sums */
-    double wn = 0.0, mf = 0.0, ma = 0.0, m2a = 0.0, cfa = 0.0;
+    /* per lane, in FP32: Kahan sums of the weighted samples, and the covariance moments of the
+     * sample norms (weight-strategy.h:187-208) by Welford's update; the lanes are merged in FP64
+     * (Chan's pairwise formulas), where the recombination also happens */
+    float sf32[CH], cf32[CH], sa32[CH], ca32[CH];
+    for (int c = 0; c < CH; ++c) sf32[c] = cf32[c] = sa32[c] = ca32[c] = 0.0f;
+    float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f;
     const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
     for (uint64_t j = lane; j < cfg.spp && n > 0; j += 32) {
         uint32_t chosen;
@@ -626,19 +627,32 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
                 fs[c] = vmul(vmul(__double2float_rn((double)fv[c] * cfg.factor), (float)n), v);
                 as[c] = vmul(vmul(__double2float_rn((double)gv[c] * cfg.factor), (float)n), v);
             }
-            sf[c] += (double)fs[c];
-            sa[c] += (double)as[c];
+            float y = vsub(fs[c], cf32[c]);
+            float t = vadd(sf32[c], y);
+            cf32[c] = vsub(vsub(t, sf32[c]), y);
+            sf32[c] = t;
+            y = vsub(as[c], ca32[c]);
+            t = vadd(sa32[c], y);
+            ca32[c] = vsub(vsub(t, sa32[c]), y);
+            sa32[c] = t;
         }
-        const double nf = (double)norm1(fs, CH), na = (double)norm1(as, CH);
-        wn += 1.0;
-        const double df = nf - mf;
-        mf += df / wn;
-        const double da = na - ma;
-        ma += da / wn;
-        const double da2 = na - ma;
-        m2a += da * da2;
-        cfa += df * da2;
+        const float nf = norm1(fs, CH), na = norm1(as, CH);
+        wn32 = vadd(wn32, 1.0f);
+        const float inv = vdiv(1.0f, wn32);
+        const float df = vsub(nf, mf32);
+        mf32 = vfma(df, inv, mf32);
+        const float da = vsub(na, ma32);
+        ma32 = vfma(da, inv, ma32);
+        const float da2 = vsub(na, ma32);
+        m2a32 = vfma(da, da2, m2a32);
+        cfa32 = vfma(df, da2, cfa32);
     }
+    double sf[CH], sa[CH];
+    for (int c = 0; c < CH; ++c) {
+        sf[c] = (double)sf32[c] - (double)cf32[c];
+        sa[c] = (double)sa32[c] - (double)ca32[c];
+    }
+    double wn = wn32, mf = mf32, ma = ma32, m2a = m2a32, cfa = cfa32;
     for (int off2 = 16; off2 > 0; off2 >>= 1) {
         for (int c = 0; c < CH; ++c) {
             sf[c] += __shfl_down_sync(0xffffffffu, sf[c], off2);

@@ -409,7 +409,8 @@ struct BinCfg {
     int32_t dimbins;
     uint64_t nbins;
     int32_t q;     /* Gauss-Legendre nodes per cell and dimension */
-    int32_t cells; /* composite cells per dimension            */
+    int32_t cells;          /* composite cells per binned dimension   */
+    int32_t cells_unbinned; /* composite cells per unbinned dimension */
     float gl_x[4], gl_w[4];
 };
 
@@ -435,10 +436,15 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
     load_params<D>(smem, packed, false);
     const SmemParams<D> P = smem_params<D>(smem, false);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
-    const int qc = c.q * c.cells; /* nodes per dimension */
+    /* per dimension `cells` equal cells of q Gauss-Legendre nodes; the unbinned dimensions, which
+     * span the whole range rather than one bin, have their own cell count */
+    int qd[D], cd[D];
     int nodes = 1;
-    for (int d = 0; d < D; ++d) nodes *= qc;
-    const float inv_cells = 1.0f / (float)c.cells;
+    for (int d = 0; d < D; ++d) {
+        cd[d] = d < c.dimbins ? c.cells : c.cells_unbinned;
+        qd[d] = c.q * cd[d];
+        nodes *= qd[d];
+    }
     for (uint64_t bin = (uint64_t)blockIdx.x * FWD_WARPS + warp; bin < c.nbins; bin += (uint64_t)gridDim.x * FWD_WARPS) {
         float lo[D], hi[D];
         bin_box<D>(c, bin, lo, hi);
@@ -448,10 +454,11 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
             const int n0 = base + g, n1 = base + g + 8;
             int r0 = n0, r1 = n1;
             for (int d = 0; d < D; ++d) {
-                const int i0 = r0 % qc, i1 = r1 % qc;
-                r0 /= qc;
-                r1 /= qc;
-                /* node j of cell k: (k + (1 + x_j) / 2) / cells of the bin's extent */
+                const int i0 = r0 % qd[d], i1 = r1 % qd[d];
+                r0 /= qd[d];
+                r1 /= qd[d];
+                const float inv_cells = 1.0f / (float)cd[d];
+                /* node j of cell k: (k + (1 + x_j) / 2) / cells of the extent */
                 const float t0 = ((float)(i0 / c.q) + 0.5f * (1.0f + c.gl_x[i0 % c.q])) * inv_cells;
                 const float t1 = ((float)(i1 / c.q) + 0.5f * (1.0f + c.gl_x[i1 % c.q])) * inv_cells;
                 const float x0 = lo[d] + (hi[d] - lo[d]) * t0;
@@ -498,7 +505,9 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
         bin_box<D>(c.b, bin, lo, hi);
         float vol = 1.0f;
         for (int d = 0; d < D; ++d) vol = vmul(vol, vsub(hi[d], lo[d]));
-        double sf = 0.0, sf2 = 0.0, sr = 0.0, sr2 = 0.0;
+        /* per lane, in FP32: Welford means and squared deviations of f and of f - g; merged across
+         * the lanes in FP64 (Chan's pairwise formulas) */
+        float wn = 0.0f, mf = 0.0f, m2f = 0.0f, mr = 0.0f, m2r = 0.0f;
         for (uint64_t base = 0; base < c.spp; base += 32) {
             const uint64_t s = base + lane;
             const bool valid = s < c.spp;
@@ -538,26 +547,40 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
                 if (r >= 0 && r < 16) gme = (r < 8) ? o0 : o1;
             }
             if (valid) {
-                const double fd = fv[0], rd = (double)fv[0] - (double)gme;
-                sf += fd;
-                sf2 += fd * fd;
-                sr += rd;
-                sr2 += rd * rd;
+                const float rv = vsub(fv[0], gme);
+                wn = vadd(wn, 1.0f);
+                const float inv = vdiv(1.0f, wn);
+                const float df = vsub(fv[0], mf);
+                mf = vfma(df, inv, mf);
+                m2f = vfma(df, vsub(fv[0], mf), m2f);
+                const float dr = vsub(rv, mr);
+                mr = vfma(dr, inv, mr);
+                m2r = vfma(dr, vsub(rv, mr), m2r);
             }
         }
+        double n_a = wn, mf_a = mf, m2f_a = m2f, mr_a = mr, m2r_a = m2r;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            sf += __shfl_xor_sync(0xffffffffu, sf, o);
-            sf2 += __shfl_xor_sync(0xffffffffu, sf2, o);
-            sr += __shfl_xor_sync(0xffffffffu, sr, o);
-            sr2 += __shfl_xor_sync(0xffffffffu, sr2, o);
+            const double n_b = __shfl_xor_sync(0xffffffffu, n_a, o);
+            const double mf_b = __shfl_xor_sync(0xffffffffu, mf_a, o);
+            const double m2f_b = __shfl_xor_sync(0xffffffffu, m2f_a, o);
+            const double mr_b = __shfl_xor_sync(0xffffffffu, mr_a, o);
+            const double m2r_b = __shfl_xor_sync(0xffffffffu, m2r_a, o);
+            const double nt = n_a + n_b;
+            if (nt > 0.0) {
+                const double w = n_a * n_b / nt, df = mf_b - mf_a, dr = mr_b - mr_a;
+                mf_a += df * n_b / nt;
+                mr_a += dr * n_b / nt;
+                m2f_a += m2f_b + df * df * w;
+                m2r_a += m2r_b + dr * dr * w;
+                n_a = nt;
+            }
         }
         if (lane == 0) {
-            const double n = (double)c.spp;
             const double scale = (double)c.factor * (double)vol;
-            const double est_cv = scale * ((double)integral[bin] + sr / n);
-            const double est_mc = scale * sf / n;
-            const double var_r = sr2 / n - (sr / n) * (sr / n), var_f = sf2 / n - (sf / n) * (sf / n);
+            const double est_cv = scale * ((double)integral[bin] + mr_a);
+            const double est_mc = scale * mf_a;
+            const double var_r = n_a > 0.0 ? m2r_a / n_a : 0.0, var_f = n_a > 0.0 ? m2f_a / n_a : 0.0;
             const bool use_mc = c.fallback && var_f < var_r;
             const float o = (float)(use_mc ? est_mc : est_cv);
             bins[bin] = o;
@@ -743,6 +766,7 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     bc.nbins = g.nbins;
     bc.q = (int)opt.quad_nodes;
     bc.cells = opt.quad_cells > 1 ? opt.quad_cells : 1;
+    bc.cells_unbinned = opt.quad_cells_unbinned > 0 ? opt.quad_cells_unbinned : bc.cells;
     for (int i = 0; i < 4; ++i) {
         bc.gl_x[i] = kGLx[bc.q - 1][i];
         bc.gl_w[i] = kGLw[bc.q - 1][i];

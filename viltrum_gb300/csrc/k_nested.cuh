@@ -49,14 +49,15 @@ template <int DIM, int S, int CH> struct Layout {
     static constexpr int SD = ipow(S, DIM);
     static constexpr int NL = ipow(S, DIM - 1);
     /* words of one group's slice for a given slot/heap count */
+    /* scratch of a split (line metrics, per-dimension errors, node coordinates); the final
+     * contributions of the regions reuse it (and extend it if they need more room) */
+    static constexpr int SCRATCH = 2 * DIM * NL + 2 * DIM + DIM * S + (S - 1);
     static __host__ __device__ int words(int nslot, int nheap) {
-        return nslot * SD * CH          /* node values            */
-               + nslot * (2 * DIM + 1)  /* ranges + volume        */
-               + 2 * nheap              /* heap keys + payloads   */
-               + 2 * DIM * NL           /* line metrics           */
-               + 2 * DIM                /* per-dimension errors   */
-               + DIM * S + (S - 1)      /* node coordinates       */
-               + nheap * CH;            /* region contributions   */
+        const int ct = nheap * CH;
+        return nslot * SD * CH              /* node values            */
+               + nslot * (2 * DIM + 1)      /* ranges + volume        */
+               + 2 * nheap                  /* heap keys + payloads   */
+               + (ct > SCRATCH ? ct : SCRATCH);
     }
 };
 
@@ -155,7 +156,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
     float* EC = LN + 2 * DIM * NL;
     float* CO = EC + 2 * DIM;
     float* CN = CO + DIM * S;
-    float* CT = CN + (S - 1);
+    float* CT = LN; /* the final contributions reuse the split scratch */
 
     const uint64_t ngroups = (uint64_t)gridDim.x * gpb;
     const int iters = cfg.iters;

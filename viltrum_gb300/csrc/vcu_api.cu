@@ -459,11 +459,13 @@ extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, 
     if (rc) return rc;
     if (!opt || !bins) return fail(ctx, VCU_INVALID_ARG, "null options or bins");
     if (opt->quad_nodes < 1 || opt->quad_nodes > 4) return fail(ctx, VCU_INVALID_ARG, "quad_nodes must be 1..4");
-    if (opt->quad_cells < 0 || opt->quad_cells > 256) return fail(ctx, VCU_INVALID_ARG, "quad_cells must be 0..256");
+    if (opt->quad_cells < 0 || opt->quad_cells > 256 || opt->quad_cells_unbinned < 0 || opt->quad_cells_unbinned > 256)
+        return fail(ctx, VCU_INVALID_ARG, "quad_cells must be 0..256");
     {
         double nodes = 1.0;
         const int qc = (int)opt->quad_nodes * (opt->quad_cells > 1 ? opt->quad_cells : 1);
-        for (int d = 0; d < p->dim; ++d) nodes *= qc;
+        const int qu = opt->quad_cells_unbinned > 0 ? (int)opt->quad_nodes * opt->quad_cells_unbinned : qc;
+        for (int d = 0; d < p->dim; ++d) nodes *= d < p->dimbins ? qc : qu;
         if (nodes > 2147483647.0) return fail(ctx, VCU_INVALID_ARG, "too many quadrature nodes per bin");
     }
     if (opt->samples_per_bin == 0 || opt->samples_per_bin > 0xffffffffull)
