@@ -199,9 +199,9 @@ constexpr int kMaxDisk = 32;
 constexpr int kMaxBox = 128;
 constexpr int kMaxHalfspaceDim = 6;
 #if defined(__CUDA_ARCH__)
-#define VCU_UNROLL_HS _Pragma("unroll")
+#define VCU_UNROLL _Pragma("unroll")
 #else
-#define VCU_UNROLL_HS
+#define VCU_UNROLL
 #endif
 
 /* ---------------------------------------------------------------- functors
@@ -290,29 +290,38 @@ struct Scene2 {
         return acc;
     }
     VCU_HD void operator()(const float* x, float* out) const { out[0] = eval(x[0], x[1]); }
-    /* two points at once, each with exactly the arithmetic of eval(): independent chains */
-    VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
-        float a0 = 0.0f, a1 = 0.0f;
+    /* N points at once, each with exactly the arithmetic of eval(): N independent chains */
+    template <int N> VCU_HD void multi(const float (*x)[DIM], float (*o)[CH]) const {
+        float a[N];
+        VCU_UNROLL
+        for (int p = 0; p < N; ++p) a[p] = 0.0f;
         for (int i = 0; i < ng; ++i) {
             const float gx = g[i][0], gy = g[i][1], gs = g[i][2], ga = g[i][3];
-            const float dx0 = vsub(x0[0], gx), dy0 = vsub(x0[1], gy);
-            const float dx1 = vsub(x1[0], gx), dy1 = vsub(x1[1], gy);
-            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
-            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
-            a0 = vfma(ga, vexp(vmul(r0, gs)), a0);
-            a1 = vfma(ga, vexp(vmul(r1, gs)), a1);
+            VCU_UNROLL
+            for (int p = 0; p < N; ++p) {
+                const float dx = vsub(x[p][0], gx), dy = vsub(x[p][1], gy);
+                const float r2 = vfma(dx, dx, vmul(dy, dy));
+                a[p] = vfma(ga, vexp(vmul(r2, gs)), a[p]);
+            }
         }
         for (int i = 0; i < nd; ++i) {
             const float cx = d[i][0], cy = d[i][1], rr = d[i][2], dv = d[i][3];
-            const float dx0 = vsub(x0[0], cx), dy0 = vsub(x0[1], cy);
-            const float dx1 = vsub(x1[0], cx), dy1 = vsub(x1[1], cy);
-            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
-            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
-            a0 = vadd(a0, (r0 <= rr) ? dv : 0.0f);
-            a1 = vadd(a1, (r1 <= rr) ? dv : 0.0f);
+            VCU_UNROLL
+            for (int p = 0; p < N; ++p) {
+                const float dx = vsub(x[p][0], cx), dy = vsub(x[p][1], cy);
+                const float r2 = vfma(dx, dx, vmul(dy, dy));
+                a[p] = vadd(a[p], (r2 <= rr) ? dv : 0.0f);
+            }
         }
-        o0[0] = a0;
-        o1[0] = a1;
+        VCU_UNROLL
+        for (int p = 0; p < N; ++p) o[p][0] = a[p];
+    }
+    VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
+        const float x[2][2] = {{x0[0], x0[1]}, {x1[0], x1[1]}};
+        float o[2][1];
+        multi<2>(x, o);
+        o0[0] = o[0][0];
+        o1[0] = o[1][0];
     }
 };
 
@@ -441,7 +450,7 @@ struct Halfspace {
     VCU_HD void operator()(const float* x, float* out) const {
         /* loops unrolled to the maximum arity and predicated, so that x[] stays in registers */
         float dot = 0.0f;
-        VCU_UNROLL_HS
+        VCU_UNROLL
         for (int i = 0; i < kMaxHalfspaceDim; ++i)
             if (i < dim) dot = vfma(nrm[i], x[i], dot);
         if (!(dot < c)) {
@@ -449,7 +458,7 @@ struct Halfspace {
             return;
         }
         float v = 1.0f;
-        VCU_UNROLL_HS
+        VCU_UNROLL
         for (int i = 0; i < kMaxHalfspaceDim; ++i)
             if (i < dim) v = vmul(v, vmul(vexp(-vmul(a[i], x[i])), vcos(vmul(b[i], x[i]))));
         out[0] = v;

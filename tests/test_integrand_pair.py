@@ -1,5 +1,5 @@
-"""Integrands that evaluate two points at once (pair(), used by the kernels to run two independent
-dependency chains per lane) return exactly what operator() returns for each point.  Checked on the
+"""Integrands that evaluate several points at once (pair(), multi<N>(), used by the kernels to run
+independent dependency chains per lane) return exactly what operator() returns for each point.  Checked on the
 host, where the same source compiles with the same explicitly rounded operations."""
 import os
 import subprocess
@@ -40,6 +40,17 @@ int main(int argc, char** argv) {
     static vcu::Scene2 s2; static vcu::MovingScene3 s3; static vcu::OccludedScene5 s5;
     if (s2.build(p2.data(), n2) || s3.build(p3.data(), n3) || s5.build(p5.data(), n5)) return 3;
     int bad = check(s2, 2, 20000, 1) + check(s3, 3, 20000, 2) + check(s5, 5, 20000, 3);
+    /* N-point evaluation of the scene: every point as operator() */
+    std::mt19937 rng(4);
+    std::uniform_real_distribution<float> u(-0.1f, 1.1f);
+    for (int i = 0; i < 5000 && !bad; ++i) {
+        float x[4][2], o3[3][1], o4[4][1], ref[4];
+        for (int p = 0; p < 4; ++p) { x[p][0] = u(rng); x[p][1] = u(rng); s2(x[p], &ref[p]); }
+        s2.multi<3>(x, o3);
+        s2.multi<4>(x, o4);
+        for (int p = 0; p < 4; ++p)
+            if (std::memcmp(&o4[p][0], &ref[p], 4) || (p < 3 && std::memcmp(&o3[p][0], &ref[p], 4))) { bad = 1; std::printf("multi %d\n", i); }
+    }
     std::printf(bad ? "bad\n" : "ok\n");
     return bad;
 }

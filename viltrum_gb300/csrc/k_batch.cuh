@@ -271,7 +271,7 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
     }
     for (int t = tid; t < DIM * S; t += nth) {
         const int d = t / S, j = t % S;
-        CO[t] = node_coord((double)j / (double)(S - 1), vsub(it.rmax[d], it.rmin[d]), it.rmin[d]);
+        CO[t] = node_coord(node_pos<S>(j), vsub(it.rmax[d], it.rmin[d]), it.rmin[d]);
     }
     __syncthreads();
     for (int t = tid; t < SD; t += nth) {
@@ -312,10 +312,10 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
         for (int t = tid; t < DIM * S + (S - 1); t += nth) {
             if (t < DIM * S) {
                 const int d = t / S, j = t % S;
-                CO[t] = node_coord((double)j / (double)(S - 1), vsub(pr[VCU_MAX_DIM + d], pr[d]), pr[d]);
+                CO[t] = node_coord(node_pos<S>(j), vsub(pr[VCU_MAX_DIM + d], pr[d]), pr[d]);
             } else {
                 const int q = t - DIM * S;
-                CN[q] = node_coord((double)(2 * q + 1) / (double)(2 * (S - 1)), vsub(pr[VCU_MAX_DIM + dd], pr[dd]), pr[dd]);
+                CN[q] = node_coord(mid_pos<S>(q), vsub(pr[VCU_MAX_DIM + dd], pr[dd]), pr[dd]);
             }
         }
         __syncthreads();

@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
     }
     for (int t = tid; t < DIM * S; t += GEN_THREADS) {
         const int d = t / S, j = t % S;
-        CO[t] = node_coord((double)j / (double)(S - 1), vsub(cfg.rmax[d], cfg.rmin[d]), cfg.rmin[d]);
+        CO[t] = node_coord(node_pos<S>(j), vsub(cfg.rmax[d], cfg.rmin[d]), cfg.rmin[d]);
     }
     __syncthreads();
     for (int t = tid; t < SD; t += GEN_THREADS) {
@@ -222,10 +222,10 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
         for (int t = tid; t < DIM * S + (S - 1); t += GEN_THREADS) {
             if (t < DIM * S) {
                 const int d = t / S, j = t % S;
-                CO[t] = node_coord((double)j / (double)(S - 1), vsub(pmax[d], pmin[d]), pmin[d]);
+                CO[t] = node_coord(node_pos<S>(j), vsub(pmax[d], pmin[d]), pmin[d]);
             } else {
                 const int k = t - DIM * S;
-                CN[k] = node_coord((double)(2 * k + 1) / (double)(2 * (S - 1)), vsub(pmax[dd], pmin[dd]), pmin[dd]);
+                CN[k] = node_coord(mid_pos<S>(k), vsub(pmax[dd], pmin[dd]), pmin[dd]);
             }
         }
         __syncthreads();

@@ -15,8 +15,9 @@
  * persistent grid sized by occupancy).  All node values of the bin's live regions, their ranges,
  * the heap and the scratch of the error folds live in the group's slice of shared memory; the
  * group evaluates the integrand at a region's new nodes in parallel (Boole 2-D: 20 new nodes per
- * split; with 8 lanes and integrands that evaluate two points as independent chains, two rounds of
- * 16 + 4 nodes), folds the per-line error metrics in parallel, and one lane keeps the heap.  Nothing touches global memory but the integrand parameters (kernel parameter space)
+ * split; with 8 lanes and integrands that evaluate several points as independent chains, one round
+ * of up to 3 points per lane), folds the per-line error metrics in parallel, and one lane keeps the
+ * heap.  Nothing touches global memory but the integrand parameters (kernel parameter space)
  * and the bin writes.
  */
 #pragma once
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
         }
         for (int t = gl; t < DIM * S; t += G) {
             const int d = t / S, j = t % S;
-            CO[t] = node_coord((double)j / (double)(S - 1), vsub(bmax[d], bmin[d]), bmin[d]);
+            CO[t] = node_coord(node_pos<S>(j), vsub(bmax[d], bmin[d]), bmin[d]);
         }
         __syncwarp(gmask);
         auto root_x = [&](int t, float* x) {
@@ -205,7 +206,21 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                 rem /= S;
             }
         };
-        if constexpr (has_pair<F>::value) {
+        if constexpr (has_multi<F>::value) {
+            constexpr int NR = (SD + G - 1) / G > 4 ? 4 : (SD + G - 1) / G;
+            for (int t = gl; t < SD; t += NR * G) {
+                float xs[NR][F::DIM], vs[NR][CH];
+#pragma unroll
+                for (int q = 0; q < NR; ++q) root_x(t + q * G < SD ? t + q * G : t, xs[q]);
+                f.template multi<NR>(xs, vs);
+#pragma unroll
+                for (int q = 0; q < NR; ++q)
+                    if (q == 0 || t + q * G < SD) {
+#pragma unroll
+                        for (int c = 0; c < CH; ++c) V[(t + q * G) * CH + c] = vs[q][c];
+                    }
+            }
+        } else if constexpr (has_pair<F>::value) {
             for (int t = gl; t < SD; t += 2 * G) {
                 const int t2 = t + G < SD ? t + G : t;
                 float x0[F::DIM], x1[F::DIM], v0[CH], v1[CH];
@@ -323,11 +338,11 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                 if (t < DIM * S) {
                     const int d = t / S, j = t % S;
                     const float mn = RMIN[P * DIM + d];
-                    CO[t] = node_coord((double)j / (double)(S - 1), vsub(RMAX[P * DIM + d], mn), mn);
+                    CO[t] = node_coord(node_pos<S>(j), vsub(RMAX[P * DIM + d], mn), mn);
                 } else {
                     const int k = t - DIM * S;
                     const float mn = RMIN[P * DIM + dd];
-                    CN[k] = node_coord((double)(2 * k + 1) / (double)(2 * (S - 1)), vsub(RMAX[P * DIM + dd], mn), mn);
+                    CN[k] = node_coord(mid_pos<S>(k), vsub(RMAX[P * DIM + dd], mn), mn);
                 }
             }
             __syncwarp(gmask);
@@ -363,7 +378,20 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                     for (int c = 0; c < CH; ++c) V1[n1 * CH + c] = v[c];
                 }
             };
-            if constexpr (has_pair<F>::value) {
+            if constexpr (has_multi<F>::value) {
+                /* NP points per lane in one pass: all of a split's new nodes in one round when
+                 * NNEW <= 4 G */
+                constexpr int NP = (NNEW + G - 1) / G > 4 ? 4 : (NNEW + G - 1) / G;
+                for (int t = gl; t < NNEW; t += NP * G) {
+                    float xs[NP][F::DIM], vs[NP][CH];
+#pragma unroll
+                    for (int q = 0; q < NP; ++q) node_x(t + q * G < NNEW ? t + q * G : t, xs[q]);
+                    f.template multi<NP>(xs, vs);
+#pragma unroll
+                    for (int q = 0; q < NP; ++q)
+                        if (q == 0 || t + q * G < NNEW) store_new(t + q * G, vs[q]);
+                }
+            } else if constexpr (has_pair<F>::value) {
                 for (int t = gl; t < NNEW; t += 2 * G) {
                     const int t2 = t + G < NNEW ? t + G : t;
                     float x0[F::DIM], x1[F::DIM], v0[CH], v1[CH];

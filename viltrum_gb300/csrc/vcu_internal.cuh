@@ -163,6 +163,12 @@ struct has_pair<F, std::void_t<decltype(std::declval<const F&>().pair((const flo
                                                                         (float*)nullptr, (float*)nullptr))>>
     : std::true_type {};
 
+/* integrands that evaluate N points at once (multi<N>: N independent dependency chains per lane) */
+template <class F, class = void> struct has_multi : std::false_type {};
+template <class F>
+struct has_multi<F, std::void_t<decltype(std::declval<const F&>().template multi<2>(
+                        (const float(*)[F::DIM]) nullptr, (float(*)[F::CH]) nullptr))>> : std::true_type {};
+
 /* Calls v(functor, channels) with the built-in functor selected by kind.  The functor object is
  * built on the host (vcu_integrands.h build()); its size decides the kernel parameter size. */
 template <class V> int with_integrand(vcu_ctx* ctx, const vcu_integrand& f, int dim, V&& v) {

@@ -147,6 +147,17 @@ __device__ __forceinline__ float metric_value(int relative, float min_val, float
 
 /* exact node coordinate float(p*w + m) with p a dyadic fraction, computed as the reference does
  * it in double (src/newton-cotes/region.h:39-47) */
+/* node positions in [0,1]: j/(S-1) and (2k+1)/(2(S-1)), as the reference computes them in double
+ * (region.h:62-78, split.h:13-49); S-1 is a power of two for every rule, so the quotients are
+ * exact products by a constant */
+template <int S> __device__ __forceinline__ double node_pos(int j) {
+    static_assert(S == 2 || S == 3 || S == 5, "S-1 must be a power of two");
+    return (double)j * (1.0 / (double)(S - 1));
+}
+template <int S> __device__ __forceinline__ double mid_pos(int k) {
+    static_assert(S == 2 || S == 3 || S == 5, "S-1 must be a power of two");
+    return (double)(2 * k + 1) * (0.5 / (double)(S - 1));
+}
 __device__ __forceinline__ float node_coord(double p, float w, float m) {
     return __double2float_rn(__dadd_rn(__dmul_rn(p, (double)w), (double)m));
 }
