@@ -80,10 +80,13 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
     constexpr int NL = ipow(S, DIM - 1);
     constexpr int NNEW = (S - 1) * NL;
     extern __shared__ float smem[];
-    __shared__ float CO[DIM * S], CN[S - 1];
-    __shared__ float LN[2 * DIM * NL], LF[(2 * DIM * NL + S - 1) / S];
-    __shared__ float EC[2 * DIM];
-    __shared__ float VC0[SD * CH], VC1[SD * CH]; /* the two children of the current split, on chip */
+    /* up to two splits per round: the top region's and, speculatively, the region the sequential
+     * algorithm pops next if the first split's children do not overtake it */
+    __shared__ float CO[2][DIM * S], CN[2][S - 1];
+    __shared__ float LN[4 * DIM * NL], LF[(4 * DIM * NL + S - 1) / S];
+    __shared__ float EC[4 * DIM];
+    __shared__ float VC[4][SD * CH]; /* the children of the round's splits, on chip */
+    __shared__ int s_top[2], s_nspec, s_adv;
     const int nheap = cfg.iters + 1;
     float* HE = cfg.heap_in_smem ? smem : heap_key;
     int* HS = cfg.heap_in_smem ? reinterpret_cast<int*>(smem + nheap) : heap_pay;
@@ -91,14 +94,14 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
 
     /* error estimates of the regions whose node values are R0 (and R1) into EC[r*DIM + d]
      * (region.h:379-418): line metrics with compile-time strides, then the folds level by level */
-    auto errors = [&](int nreg, const float* R0, const float* R1, int r0, int r1) {
+    auto errors = [&](int nreg, const int* rid) {
         static_for<DIM>([&](auto dc) {
             constexpr int d = decltype(dc)::value;
             constexpr int PD = ipow(S, d);
             for (int t = tid; t < nreg * NL; t += GEN_THREADS) {
-                const int r = t >= NL ? 1 : 0;
+                const int r = t / NL;
                 const int J = t - r * NL;
-                const float* RV = (r ? R1 : R0) + (J % PD + (J / PD) * (PD * S)) * CH;
+                const float* RV = VC[r] + (J % PD + (J / PD) * (PD * S)) * CH;
                 float m = 0.0f;
 #pragma unroll
                 for (int c = 0; c < CH; ++c) {
@@ -138,7 +141,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
             src = dst;
             dst = sw;
         });
-        if (tid < nreg * DIM) EC[tid] = vmul(vol[(tid / DIM) ? r1 : r0], src[tid]);
+        if (tid < nreg * DIM) EC[tid] = vmul(vol[rid[tid / DIM]], src[tid]);
         __syncthreads();
     };
     auto heuristic = [&](int r, int id, float& err_out, int& dim_out) {
@@ -185,7 +188,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
     }
     for (int t = tid; t < DIM * S; t += GEN_THREADS) {
         const int d = t / S, j = t % S;
-        CO[t] = node_coord(node_pos<S>(j), vsub(cfg.rmax[d], cfg.rmin[d]), cfg.rmin[d]);
+        CO[0][t] = node_coord(node_pos<S>(j), vsub(cfg.rmax[d], cfg.rmin[d]), cfg.rmin[d]);
     }
     __syncthreads();
     for (int t = tid; t < SD; t += GEN_THREADS) {
@@ -193,18 +196,21 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
         for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
         int rem = t;
         for (int d = 0; d < DIM; ++d) {
-            x[d] = CO[d * S + rem % S];
+            x[d] = CO[0][d * S + rem % S];
             rem /= S;
         }
         float v[CH];
         f(x, v);
         for (int c = 0; c < CH; ++c) {
             vals[t * CH + c] = v[c];
-            VC0[t * CH + c] = v[c];
+            VC[0][t * CH + c] = v[c];
         }
     }
     __syncthreads();
-    errors(1, VC0, VC0, 0, 0);
+    {
+        const int rid0[1] = {0};
+        errors(1, rid0);
+    }
     if (tid == 0) {
         float e;
         int dm;
@@ -212,113 +218,152 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
         HE[0] = e;
         HS[0] = 0 | (dm << 24);
     }
-    for (int it = 0; it < cfg.iters; ++it) {
+    constexpr int TB = NNEW + S * NL; /* tasks of one split's children */
+    int it = 0;
+    while (it < cfg.iters) {
         __syncthreads();
-        const int top = HS[0];
-        const int P = top & 0xffffff, dd = top >> 24;
-        const int C0 = 2 * it + 1, C1 = 2 * it + 2;
-        const float* pmin = rmin + (size_t)P * DIM;
-        const float* pmax = rmax + (size_t)P * DIM;
-        for (int t = tid; t < DIM * S + (S - 1); t += GEN_THREADS) {
-            if (t < DIM * S) {
-                const int d = t / S, j = t % S;
-                CO[t] = node_coord(node_pos<S>(j), vsub(pmax[d], pmin[d]), pmin[d]);
+        if (tid == 0) {
+            const int n = it + 1; /* heap size */
+            s_top[0] = HS[0];
+            int nspec = 1;
+            if (it + 1 < cfg.iters && n >= 2) {
+                /* the element libstdc++'s pop moves to the root: the right child unless it is less */
+                const int c = (n >= 3 && !(HE[2] < HE[1])) ? 2 : 1;
+                s_top[1] = HS[c];
+                nspec = 2;
+            }
+            s_nspec = nspec;
+        }
+        __syncthreads();
+        const int nspec = s_nspec;
+        for (int t = tid; t < nspec * (DIM * S + (S - 1)); t += GEN_THREADS) {
+            const int q = t / (DIM * S + (S - 1)), u = t - q * (DIM * S + (S - 1));
+            const int P = s_top[q] & 0xffffff, dd = s_top[q] >> 24;
+            const float* pmin = rmin + (size_t)P * DIM;
+            const float* pmax = rmax + (size_t)P * DIM;
+            if (u < DIM * S) {
+                const int d = u / S, j = u % S;
+                CO[q][u] = node_coord(node_pos<S>(j), vsub(pmax[d], pmin[d]), pmin[d]);
             } else {
-                const int k = t - DIM * S;
-                CN[k] = node_coord(mid_pos<S>(k), vsub(pmax[dd], pmin[dd]), pmin[dd]);
+                const int k = u - DIM * S;
+                CN[q][k] = node_coord(mid_pos<S>(k), vsub(pmax[dd], pmin[dd]), pmin[dd]);
             }
         }
         __syncthreads();
-        const float* VP = vals + (size_t)P * SD * CH;
-        float* V0 = vals + (size_t)C0 * SD * CH;
-        float* V1 = vals + (size_t)C1 * SD * CH;
         /* new nodes at the odd positions, parent nodes at the even (region.h:345-359, split.h:13-49),
-         * built on chip and copied to the pool; one instance per split dimension */
-        auto build_children = [&](auto ddc) {
+         * built on chip and copied to the pool (split q writes pool ids 2(it+q)+1, 2(it+q)+2); one
+         * instance per split dimension */
+        auto build_children = [&](auto ddc, int q, int u) {
             constexpr int DD = decltype(ddc)::value;
             constexpr int PD = ipow(S, DD);
-            for (int t = tid; t < NNEW + S * NL; t += GEN_THREADS) {
-                const bool fresh = t < NNEW;
-                const int u = fresh ? t : t - NNEW;
-                const int q = u / NL, J = u - q * NL;
-                const int base = J % PD + (J / PD) * (PD * S);
-                float v[CH];
-                int i;
-                if (fresh) {
-                    float x[F::DIM];
+            const int P = s_top[q] & 0xffffff;
+            const float* VP = vals + (size_t)P * SD * CH;
+            float* V0 = vals + (size_t)(2 * (it + q) + 1) * SD * CH;
+            float* V1 = vals + (size_t)(2 * (it + q) + 2) * SD * CH;
+            const bool fresh = u < NNEW;
+            const int w = fresh ? u : u - NNEW;
+            const int k = w / NL, J = w - k * NL;
+            const int base = J % PD + (J / PD) * (PD * S);
+            float v[CH];
+            int i;
+            if (fresh) {
+                float x[F::DIM];
 #pragma unroll
-                    for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
-                    static_for<DIM>([&](auto ec) {
-                        constexpr int e = decltype(ec)::value;
-                        if constexpr (e != DD) {
-                            constexpr int pe = e < DD ? ipow(S, e) : ipow(S, e - 1);
-                            x[e] = CO[e * S + (J / pe) % S];
-                        }
-                    });
-                    x[DD] = CN[q];
-                    f(x, v);
-                    i = 2 * q + 1;
-                } else {
-#pragma unroll
-                    for (int c = 0; c < CH; ++c) v[c] = VP[(base + q * PD) * CH + c];
-                    i = 2 * q;
-                }
-                if (i <= S - 1) {
-                    const int n0 = (base + i * PD) * CH;
-#pragma unroll
-                    for (int c = 0; c < CH; ++c) {
-                        VC0[n0 + c] = v[c];
-                        V0[n0 + c] = v[c];
+                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+                static_for<DIM>([&](auto ec) {
+                    constexpr int e = decltype(ec)::value;
+                    if constexpr (e != DD) {
+                        constexpr int pe = e < DD ? ipow(S, e) : ipow(S, e - 1);
+                        x[e] = CO[q][e * S + (J / pe) % S];
                     }
-                }
-                if (i >= S - 1) {
-                    const int n1 = (base + (i - (S - 1)) * PD) * CH;
+                });
+                x[DD] = CN[q][k];
+                f(x, v);
+                i = 2 * k + 1;
+            } else {
 #pragma unroll
-                    for (int c = 0; c < CH; ++c) {
-                        VC1[n1 + c] = v[c];
-                        V1[n1 + c] = v[c];
-                    }
+                for (int c = 0; c < CH; ++c) v[c] = VP[(base + k * PD) * CH + c];
+                i = 2 * k;
+            }
+            if (i <= S - 1) {
+                const int n0 = (base + i * PD) * CH;
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    VC[2 * q][n0 + c] = v[c];
+                    V0[n0 + c] = v[c];
+                }
+            }
+            if (i >= S - 1) {
+                const int n1 = (base + (i - (S - 1)) * PD) * CH;
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    VC[2 * q + 1][n1 + c] = v[c];
+                    V1[n1 + c] = v[c];
                 }
             }
         };
-        static_for<DIM>([&](auto dc) {
-            if (dd == decltype(dc)::value) build_children(dc);
-        });
+        for (int t = tid; t < nspec * TB; t += GEN_THREADS) {
+            const int q = t / TB, u = t - q * TB;
+            const int dd = s_top[q] >> 24;
+            static_for<DIM>([&](auto dc) {
+                if (dd == decltype(dc)::value) build_children(dc, q, u);
+            });
+        }
         if (tid == 0) {
-            const float pmn = pmin[dd], pmx = pmax[dd];
-            const float half = vdiv(vsub(pmx, pmn), 2.0f);
-            const float mid = vadd(pmn, vmul(half, 1.0f));
-            float v0 = 1.0f, v1 = 1.0f;
-            for (int d = 0; d < DIM; ++d) {
-                const float mn = pmin[d], mx = pmax[d];
-                const float mx0 = (d == dd) ? mid : mx;
-                const float mn1 = (d == dd) ? mid : mn;
-                rmin[(size_t)C0 * DIM + d] = mn;
-                rmax[(size_t)C0 * DIM + d] = mx0;
-                rmin[(size_t)C1 * DIM + d] = mn1;
-                rmax[(size_t)C1 * DIM + d] = mx;
-                v0 = vmul(v0, vsub(mx0, mn));
-                v1 = vmul(v1, vsub(mx, mn1));
+            for (int q = 0; q < nspec; ++q) {
+                const int P = s_top[q] & 0xffffff, dd = s_top[q] >> 24;
+                const int C0 = 2 * (it + q) + 1, C1 = 2 * (it + q) + 2;
+                const float* pmin = rmin + (size_t)P * DIM;
+                const float* pmax = rmax + (size_t)P * DIM;
+                const float pmn = pmin[dd], pmx = pmax[dd];
+                const float half = vdiv(vsub(pmx, pmn), 2.0f);
+                const float mid = vadd(pmn, vmul(half, 1.0f));
+                float v0 = 1.0f, v1 = 1.0f;
+                for (int d = 0; d < DIM; ++d) {
+                    const float mn = pmin[d], mx = pmax[d];
+                    const float mx0 = (d == dd) ? mid : mx;
+                    const float mn1 = (d == dd) ? mid : mn;
+                    rmin[(size_t)C0 * DIM + d] = mn;
+                    rmax[(size_t)C0 * DIM + d] = mx0;
+                    rmin[(size_t)C1 * DIM + d] = mn1;
+                    rmax[(size_t)C1 * DIM + d] = mx;
+                    v0 = vmul(v0, vsub(mx0, mn));
+                    v1 = vmul(v1, vsub(mx, mn1));
+                }
+                vol[C0] = v0;
+                vol[C1] = v1;
             }
-            vol[C0] = v0;
-            vol[C1] = v1;
         }
         __syncthreads();
-        errors(2, VC0, VC1, C0, C1);
-        if (tid == 0) {
-            float e0, e1;
-            int d0, d1;
-            heuristic(0, C0, e0, d0);
-            heuristic(1, C1, e1, d1);
-            const int n = it + 1;
-            heap_pop(HE, HS, n);
-            HE[n - 1] = e0;
-            HS[n - 1] = C0 | (d0 << 24);
-            heap_push(HE, HS, n);
-            HE[n] = e1;
-            HS[n] = C1 | (d1 << 24);
-            heap_push(HE, HS, n + 1);
+        {
+            const int rid[4] = {2 * it + 1, 2 * it + 2, 2 * it + 3, 2 * it + 4};
+            errors(2 * nspec, rid);
         }
+        if (tid == 0) {
+            /* commit the first split; commit the second only if the heap now really has it on top
+             * (same entry), which is exactly what the sequential algorithm would pop next */
+            int adv = 0;
+            for (int q = 0; q < nspec; ++q) {
+                if (q == 1 && HS[0] != s_top[1]) break;
+                const int C0 = 2 * (it + q) + 1, C1 = 2 * (it + q) + 2;
+                float e0, e1;
+                int d0, d1;
+                heuristic(2 * q, C0, e0, d0);
+                heuristic(2 * q + 1, C1, e1, d1);
+                const int n = it + q + 1;
+                heap_pop(HE, HS, n);
+                HE[n - 1] = e0;
+                HS[n - 1] = C0 | (d0 << 24);
+                heap_push(HE, HS, n);
+                HE[n] = e1;
+                HS[n] = C1 | (d1 << 24);
+                heap_push(HE, HS, n + 1);
+                ++adv;
+            }
+            s_adv = adv;
+        }
+        __syncthreads();
+        it += s_adv;
     }
     __syncthreads();
     if (cfg.heap_in_smem)

@@ -58,9 +58,11 @@ VCU_HD bool even_bits(float x) {
  * exact fma residual and l) decides: R/D beyond half the gap to the neighbour moves to it, exactly half (or within the
  * 2^-30-ulp band where the reference's intermediate double lands on the midpoint) ties to even. */
 VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
-    /* q0 = RN(h/D) can be two floats away when l is a full ulp of h; one approximate correction
-     * step brings it within one float of the result */
-    const float q00 = vdiv(h, D);
+    /* q00 ~ h/D, then one approximate correction step brings q0 within one float of the result
+     * (the exact decision below does the rest).  For |h| in [2^-90, 2^90] the product by RN(1/D)
+     * is close enough; outside that range (subnormal quotients, near overflow) a true division. */
+    const float ah = vabs(h);
+    const float q00 = (ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f) ? vmul(h, inv_D) : vdiv(h, D);
     const float q0 = vfma(vadd(vfma(-q00, D, h), l), inv_D, q00);
     float s, e;
     two_sum(vfma(-q0, D, h), l, s, e);
