@@ -150,13 +150,6 @@ VCU_HD float vexp(float x) {
     return (x > -87.0f) ? ((x > 88.5f) ? bits_to_float(0x7f800000u) : core) : ((x != x) ? x : 0.0f);
 }
 
-/* vexp for arguments that cannot exceed 0 (a Gaussian exponent -r^2/(2 s^2)): the same value as
- * vexp, without the overflow branch */
-VCU_HD float vexp_nonpos(float x) {
-    const float core = vexp_core(x > -87.0f ? x : -87.0f);
-    return (x > -87.0f) ? core : ((x != x) ? x : 0.0f);
-}
-
 /* sin and cos of the reduced argument |r| <= pi/4 (Taylor to degree 9 and 10). */
 VCU_HD float sin_kernel(float r) {
     const float r2 = vmul(r, r);
@@ -286,7 +279,7 @@ struct Scene2 {
             const float dx = vsub(x, g[i][0]);
             const float dy = vsub(y, g[i][1]);
             const float r2 = vfma(dx, dx, vmul(dy, dy));
-            acc = vfma(g[i][3], vexp_nonpos(vmul(r2, g[i][2])), acc);
+            acc = vfma(g[i][3], vexp(vmul(r2, g[i][2])), acc);
         }
         for (int i = 0; i < nd; ++i) {
             const float dx = vsub(x, d[i][0]);
@@ -308,7 +301,7 @@ struct Scene2 {
             for (int p = 0; p < N; ++p) {
                 const float dx = vsub(x[p][0], gx), dy = vsub(x[p][1], gy);
                 const float r2 = vfma(dx, dx, vmul(dy, dy));
-                a[p] = vfma(ga, vexp_nonpos(vmul(r2, gs)), a[p]);
+                a[p] = vfma(ga, vexp(vmul(r2, gs)), a[p]);
             }
         }
         for (int i = 0; i < nd; ++i) {
@@ -374,7 +367,7 @@ struct MovingScene3 {
             const float dx = vsub(x[0], g[i][0]);
             const float dy = vsub(x[1], g[i][1]);
             const float r2 = vfma(dx, dx, vmul(dy, dy));
-            grey = vfma(g[i][3], vexp_nonpos(vmul(r2, g[i][2])), grey);
+            grey = vfma(g[i][3], vexp(vmul(r2, g[i][2])), grey);
         }
         float c0 = grey, c1 = grey, c2 = grey;
         for (int i = 0; i < nd; ++i) {
@@ -402,8 +395,8 @@ struct MovingScene3 {
             const float dx1 = vsub(x1[0], gx), dy1 = vsub(x1[1], gy);
             const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
             const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
-            g0 = vfma(ga, vexp_nonpos(vmul(r0, gs)), g0);
-            g1 = vfma(ga, vexp_nonpos(vmul(r1, gs)), g1);
+            g0 = vfma(ga, vexp(vmul(r0, gs)), g0);
+            g1 = vfma(ga, vexp(vmul(r1, gs)), g1);
         }
         float a0 = g0, a1 = g0, a2 = g0, b0 = g1, b1 = g1, b2 = g1;
         for (int i = 0; i < nd; ++i) {

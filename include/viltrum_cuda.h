@@ -214,6 +214,18 @@ int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_l
 int vcu_mlp_eval(vcu_ctx* ctx, int32_t dim, const float* theta, const float* u, const float* y, int64_t npts,
                  float* out, float* grad);
 
+/* ------------------------------------------------------------------ global adaptive nested NC
+ * Replaces integrate(integrator_adaptive_iterations(nested(H,L), heuristic, iterations), bins, f,
+ * range) with the integrator used directly rather than per bin
+ * (src/nested/integrator-adaptive-iterations.h:12-15): one max-error heap over the whole range is
+ * split `iterations` times (src/nested/regions-generator-adaptive-heap.h:18-45), then every region,
+ * in heap order, is added into each bin it overlaps (src/newton-cotes/regions-integrator-sequential.h:
+ * 37-58): bins ACCUMULATE (bins[b] += prod(res) * integral over bin n region).  Also the result of
+ * integrator_adaptive_iterations_parallel (regions-integrator-parallel-regions.h) on one host thread.
+ * Regions up to S^dim = 243 nodes, iterations < 2^23. */
+int vcu_adaptive_iterations_global(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
+                                   uint64_t iterations, float* bins, vcu_stats* stats);
+
 /* ------------------------------------------------------------------ batched independent integrals
  * Many calls of the reference's single-value form, viltrum::integrate(I, f, range)
  * (src/integrate.h:105-113), each with its own dimension, range, integrand parameters, method and

@@ -176,6 +176,27 @@ void write_back(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const s
     }
 }
 
+/* the caller's bins(pos) values in viltrum's linear order (the start of an accumulating call) */
+template <class T> void load(const T& src, float* v, int ch) {
+    if constexpr (std::is_arithmetic_v<T>) {
+        v[0] = (float)src;
+    } else {
+        for (int c = 0; c < ch; ++c) v[c] = (float)src[c];
+    }
+}
+template <class Bins, std::size_t DIMBINS>
+void read_in(Bins& bins, const std::array<std::size_t, DIMBINS>& res, std::vector<float>& out, int ch) {
+    std::array<std::size_t, DIMBINS> pos{};
+    const std::size_t n = out.size() / ch;
+    for (std::size_t lin = 0; lin < n; ++lin) {
+        load(bins(pos), &out[lin * ch], ch);
+        for (std::size_t d = 0; d < DIMBINS; ++d) {
+            if (++pos[d] < res[d]) break;
+            pos[d] = 0;
+        }
+    }
+}
+
 template <class F> const builtin_integrand& as_builtin(const F& f) {
     static_assert(std::is_same_v<std::decay_t<F>, builtin_integrand>,
                   "CUDA integrators take a viltrum::cuda::builtin_integrand (integrand code cannot cross the C ABI)");
@@ -256,6 +277,34 @@ public:
         std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
         vcu_stats st{};
         ctx.check(vcu_per_bin_adaptive_nested(ctx.get(), &p, &rule_.n, iterations_, out.data(), nullptr, &st));
+        detail::write_back(bins, res, out, ch, false);
+        logger.log_progress(std::size_t(1), std::size_t(1));
+    }
+};
+
+/* drop-in for integrator_adaptive_iterations(nested(H,L), heuristic, iterations) used directly, and
+ * integrator_adaptive_iterations_parallel: one heap over the whole range, every region added into
+ * the bins it overlaps -- ACCUMULATES, like regions_integrator_sequential
+ * (src/newton-cotes/regions-integrator-sequential.h:37-58) */
+class adaptive_iterations {
+    nested_rule rule_;
+    unsigned long iterations_;
+
+public:
+    adaptive_iterations(nested_rule r, unsigned long iterations) : rule_(r), iterations_(iterations) {}
+
+    template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
+    void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
+                   Logger& logger) const {
+        const builtin_integrand& fi = detail::as_builtin(f);
+        context& ctx = thread_context();
+        logger.log_progress(std::size_t(0), std::size_t(1));
+        vcu_problem p = detail::make_problem(fi, res, range);
+        const int ch = fi.channels();
+        std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
+        detail::read_in(bins, res, out, ch);
+        vcu_stats st{};
+        ctx.check(vcu_adaptive_iterations_global(ctx.get(), &p, &rule_.n, iterations_, out.data(), &st));
         detail::write_back(bins, res, out, ch, false);
         logger.log_progress(std::size_t(1), std::size_t(1));
     }

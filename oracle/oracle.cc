@@ -533,6 +533,54 @@ void per_bin_nested_range(const Fun& fun, const Problem& p, const orc_nested& nc
     }
 }
 
+/* ------------------------------------------------------------------ global adaptive into bins */
+template <class H, class L, int DIM, class T, class Fun, class M>
+void adaptive_global(const Fun& fun, const Problem& p, const orc_nested& nc, const M& metric, uint64_t iters,
+                     float* out) {
+    using R = Region<H, L, DIM, T>;
+    const auto range = make_range<DIM>(p);
+    Fn<Fun, DIM, T> f{&fun};
+    const std::vector<R> regions = generate<H, L, DIM, T>(f, range, iters, nc, metric, nullptr);
+    uint64_t factor = 1;
+    for (int i = 0; i < p.dimbins; ++i) factor *= p.res[i];
+    std::array<float, DIM> drange;
+    for (int i = 0; i < p.dimbins; ++i) drange[i] = (range.max(i) - range.min(i)) / float(p.res[i]);
+    for (const auto& r : regions) {
+        /* pixels_in_region (region.h:454-463) */
+        std::array<uint64_t, 8> st, en;
+        for (int i = 0; i < p.dimbins; ++i) {
+            st[i] = std::max(std::size_t(0),
+                             std::size_t(float(p.res[i]) * (r.range.min(i) - range.min(i)) / (range.max(i) - range.min(i))));
+            en[i] = std::max(std::size_t(st[i] + 1),
+                             std::min(std::size_t(p.res[i]),
+                                      std::size_t(0.99f + (float(p.res[i]) * (r.range.max(i) - range.min(i)) /
+                                                           (range.max(i) - range.min(i))))));
+        }
+        std::array<uint64_t, 8> q = st;
+        for (;;) {
+            Range<DIM> binrange = range;
+            uint64_t lin = 0, mul = 1;
+            for (int i = 0; i < p.dimbins; ++i) {
+                binrange = binrange.subrange_dimension(i, range.min(i) + q[i] * drange[i], range.min(i) + (q[i] + 1) * drange[i]);
+                lin += q[i] * mul;
+                mul *= p.res[i];
+            }
+            const Range<DIM> rb = binrange.intersection(r.range);
+            if (!rb.empty()) {
+                T v = VT<T>::from(out + lin * VT<T>::CH);
+                v += double(factor) * r.integral_subrange(rb);
+                VT<T>::to(v, out + lin * VT<T>::CH);
+            }
+            int i = 0;
+            for (; i < p.dimbins; ++i) {
+                if (++q[i] < en[i]) break;
+                q[i] = st[i];
+            }
+            if (i == p.dimbins) break;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ single-value integrals */
 /* monte_carlo(budget, seed) through integrate(I, f, range): one bin of resolution {1}, the
  * integrator's own std::mt19937(seed) (moved in, not reseeded), bins(pos) += f(x) * factor */
@@ -917,6 +965,22 @@ extern "C" int orc_integrate_single(int32_t kind, const float* params, int32_t n
         return with_rules(*nested, [&](auto h, auto l) -> int {
             return with_metric(*nested, [&](auto m) -> int {
                 *out = single_nested<decltype(h), decltype(l), DIM>(f, range, *nested, m, budget - 1);
+                return 0;
+            });
+        });
+    });
+}
+
+extern "C" int orc_adaptive_global(int32_t kind, const float* params, int32_t n_params, int32_t dim, const float* rmin,
+                                   const float* rmax, int32_t dimbins, const uint64_t* res, const orc_nested* nested,
+                                   uint64_t iterations, float* out) {
+    if (!valid_problem(dim, dimbins, res) || !nested || !out) return 1;
+    Problem p{dim, dimbins, rmin, rmax, res};
+    return with_integrand(kind, params, n_params, dim, [&](const auto& f, auto D, auto t) -> int {
+        return with_rules(*nested, [&](auto h, auto l) -> int {
+            return with_metric(*nested, [&](auto m) -> int {
+                adaptive_global<decltype(h), decltype(l), decltype(D)::value, decltype(t)>(f, p, *nested, m, iterations,
+                                                                                              out);
                 return 0;
             });
         });

@@ -86,6 +86,15 @@ int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* params, int32
                                         uint64_t bin_begin, uint64_t bin_end, int32_t nthreads,
                                         float* out);
 
+/* integrate(integrator_adaptive_iterations(nested(H,L), heuristic, iters), bins, f, range) with the
+ * integrator used directly (not per bin): one max-error heap over the whole range, then every region,
+ * in heap order, added into the bins it overlaps (src/newton-cotes/regions-integrator-sequential.h:
+ * 37-58: bins(pos) += double(factor) * integral_subrange).  out holds the initial bins (it is
+ * accumulated into, as the reference does).                                                 */
+int orc_adaptive_global(int32_t kind, const float* params, int32_t n_params, int32_t dim, const float* rmin,
+                        const float* rmax, int32_t dimbins, const uint64_t* res, const orc_nested* nested,
+                        uint64_t iterations, float* out);
+
 /* One single-value viltrum::integrate(I, f, range) (src/integrate.h:105-113):
  *   method 0: I = monte_carlo(budget, seed)  (std::mt19937(seed), float accumulation,
  *             src/monte-carlo/monte-carlo.h:39-63, 89-95)

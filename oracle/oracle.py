@@ -88,6 +88,10 @@ class Oracle:
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
                       ctypes.POINTER(Nested), ctypes.c_uint64, _f32p, _i32p]
+        f = getattr(L, prefix + "adaptive_global")
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                      ctypes.POINTER(Nested), ctypes.c_uint64, _f32p]
         f = getattr(L, prefix + "integrate_single")
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32,
@@ -160,6 +164,19 @@ class Oracle:
             ctypes.byref(nested), iterations, bin_begin, bin_end, nthreads, _ptr(out))
         self._check(rc, "per_bin_adaptive_nested_threads")
         return out.reshape(nb, ch)[bin_begin:bin_end]
+
+    def adaptive_global(self, kind, params, rmin, rmax, res, nested: Nested, iterations, initial=None):
+        """integrator_adaptive_iterations used directly: one heap over the range, regions added into
+        the bins (which start from `initial`, zeros by default)."""
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        out = np.zeros(nb * ch, dtype=np.float32) if initial is None else np.array(initial, np.float32).ravel().copy()
+        rc = getattr(self.lib, self.prefix + "adaptive_global")(
+            kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
+            ctypes.byref(nested), iterations, _ptr(out))
+        self._check(rc, "adaptive_global")
+        return out.reshape(nb, ch)
 
     def integrate_single(self, kind, params, rmin, rmax, method, budget, seed=0, nested: Nested | None = None):
         """One single-value integrate(I, f, range): method 0 = monte_carlo(budget, seed), 1 = adaptive

@@ -38,13 +38,14 @@ int main() {
     const auto scene = vc::builtin_integrand::scene2(scene_params());
     const auto wave = vc::builtin_integrand::wave2();
     std::vector<std::vector<float>> image(16, std::vector<float>(16, 0.0f));
-    std::vector<float> row(64, 0.0f), cv_bins(64, 0.0f), learned(16, 0.0f);
+    std::vector<float> row(64, 0.0f), cv_bins(64, 0.0f), learned(16, 0.0f), global(32, 0.5f);
 #ifdef WITH_VILTRUM
     viltrum::integrate(vc::per_bin_adaptive_nested(vc::boole_simpson(), 15), image, scene, viltrum::range_primary<2>());
     viltrum::integrate(vc::per_bin_monte_carlo(256, 7), row, wave, viltrum::range_primary<2>());
     viltrum::integrate(vc::per_bin_monte_carlo_accumulate(256, 9), row, wave, viltrum::range_primary<2>());
     viltrum::integrate(vc::crespo2021(255, 16, 3), cv_bins, scene, viltrum::range_primary<2>());
     viltrum::integrate(vc::learned_control_variates(16, 5, 50), learned, wave, viltrum::range_primary<2>());
+    viltrum::integrate(vc::adaptive_iterations(vc::simpson_trapezoidal(), 127), global, scene, viltrum::range_primary<2>());
 #else
     quiet log;
     const box<2> unit{{0.0f, 0.0f}, {1.0f, 1.0f}};
@@ -57,6 +58,8 @@ int main() {
     vc::per_bin_monte_carlo_accumulate(256, 9).integrate(r1, std::array<std::size_t, 1>{64}, wave, unit, log);
     vc::crespo2021(255, 16, 3).integrate(c1, std::array<std::size_t, 1>{64}, scene, unit, log);
     vc::learned_control_variates(16, 5, 50).integrate(l1, std::array<std::size_t, 1>{16}, wave, unit, log);
+    auto g1 = [&](const std::array<std::size_t, 1>& p) -> float& { return global[p[0]]; };
+    vc::adaptive_iterations(vc::simpson_trapezoidal(), 127).integrate(g1, std::array<std::size_t, 1>{32}, scene, unit, log);
 #endif
     /* independent integrals: two half-space items, one nested and one Monte Carlo */
     std::vector<vc::batch_item> items(2);
@@ -74,6 +77,7 @@ int main() {
     for (float v : row) std::printf("%.9g\n", v);
     for (float v : cv_bins) std::printf("%.9g\n", v);
     for (float v : learned) std::printf("%.9g\n", v);
+    for (float v : global) std::printf("%.9g\n", v);
     for (float v : batch) std::printf("%.9g\n", v);
     return 0;
 }

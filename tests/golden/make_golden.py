@@ -85,6 +85,35 @@ CASES = [
 
 CRESPO = ("simpson", "trapezoidal", "size", "relative")
 
+# integrator_adaptive_iterations used directly (one heap over the range, regions added into bins
+# that start from a non-zero image)
+GLOBAL_CASES = [
+    ("global_scene2_bins16x16_st_abs_it255", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1],
+                                                  res=[16, 16], nested=("simpson", "trapezoidal", "default", "absolute"),
+                                                  iterations=255)),
+    ("global_moving3_rgb_bins8x8_bs_abs_it127", dict(kind=scenes.MOVING_SCENE3, params=MOVING_SMALL, rmin=[0, 0, 0],
+                                                     rmax=[1, 1, 1], res=[8, 8],
+                                                     nested=("boole", "simpson", "default", "absolute"), iterations=127)),
+    ("global_halfspace3_bins4_st_size_rel_it63", dict(kind=scenes.HALFSPACE, params=HALF3, rmin=[0, 0, 0],
+                                                      rmax=[1, 1, 1], res=[4],
+                                                      nested=("simpson", "trapezoidal", "size", "relative"),
+                                                      iterations=63)),
+]
+
+
+def global_initial(kw) -> np.ndarray:
+    nb = int(np.prod(kw["res"]))
+    ch = 3 if kw["kind"] == scenes.MOVING_SCENE3 else 1
+    return (0.125 + 0.001 * np.arange(nb * ch)).astype(np.float32)
+
+
+def run_global(lib: orc.Oracle, kw: dict) -> dict:
+    hi, lo, heur, met = kw["nested"]
+    return {"bins": lib.adaptive_global(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"],
+                                        orc.Nested.make(hi, lo, heur, met), kw["iterations"],
+                                        initial=global_initial(kw))}
+
+
 # independent single-value integrals (the batched-integrals workload at small budgets)
 BATCH_CASES = [
     ("batch_halfspace_n64_seed5", dict(n=64, seed=5, budget_lo=1, budget_hi=400)),
@@ -182,6 +211,18 @@ def main() -> int:
             meta["nested"] = np.array(kw["nested"])
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method=method, **meta, **{"out_" + k: v for k, v in r.items()})
         print(f"ok {name}")
+    for name, kw in GLOBAL_CASES:
+        r, p = run_global(ref, kw), run_global(port, kw)
+        if not np.array_equal(r["bins"].view(np.uint32), p["bins"].view(np.uint32)):
+            bad += 1
+            d = np.abs(r["bins"].astype(np.float64) - p["bins"])
+            print(f"MISMATCH {name}: max |diff| {d.max():.3e} ({int((d > 0).sum())} differ)")
+            continue
+        meta = {k: np.asarray(v) for k, v in kw.items() if k not in ("params", "nested")}
+        meta["params"] = np.asarray(kw["params"], dtype=np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), method="global", nested=np.array(kw["nested"]),
+                            initial=global_initial(kw), **meta, out_bins=r["bins"])
+        print(f"ok {name}")
     for name, kw in BATCH_CASES:
         r, p = run_batch(ref, kw), run_batch(port, kw)
         if not np.array_equal(r["values"].view(np.uint32), p["values"].view(np.uint32)):
@@ -191,7 +232,7 @@ def main() -> int:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="batch", **{k: np.asarray(v) for k, v in kw.items()},
                             out_values=r["values"])
         print(f"ok {name}")
-    total = len(CASES) + len(BATCH_CASES)
+    total = len(CASES) + len(BATCH_CASES) + len(GLOBAL_CASES)
     print(f"{total - bad} of {total} cases bit-identical")
     return 1 if bad else 0
 

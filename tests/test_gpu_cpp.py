@@ -23,8 +23,8 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
                     "-lviltrum_cuda", "-Wl,-rpath," + os.path.join(ROOT, "viltrum_gb300"), "-o", exe], check=True)
     out = np.array([float(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()],
                    np.float32)
-    assert out.size == 256 + 64 + 64 + 16 + 2
-    img, row, cvb, lrn, bat = np.split(out, [256, 320, 384, 400])
+    assert out.size == 256 + 64 + 64 + 16 + 32 + 2
+    img, row, cvb, lrn, glb, bat = np.split(out, [256, 320, 384, 400, 432])
     scene = np.array([2, 1, 0.3, 0.4, 0.05, 0.8, 0.7, 0.6, 0.1, 0.5, 0.5, 0.5, 0.2, 0.25], np.float32)
     # per-bin adaptive nested, 16x16 (image[y][x] flattened = dim-0-fastest bins)
     ref = np.empty(256, np.float32)
@@ -48,6 +48,11 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
     ctx.learned_control_variates(ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [16]),
                                  _lib.LearnedOpts(16, 5, 50, 32768, 3e-3, 3, 1, 1), l)
     assert np.array_equal(lrn.view(np.uint32), l.view(np.uint32))
+    # adaptive_iterations used directly, accumulating into bins that start at 0.5
+    gb = np.full(32, 0.5, np.float32)
+    ctx.adaptive_iterations_global(ctx.problem(scenes.SCENE2, scene, [0, 0], [1, 1], [32]),
+                                   _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37), 127, gb)
+    assert np.array_equal(glb.view(np.uint32), gb.view(np.uint32))
     # two independent integrals
     hp = np.array([2, 1.5, 0.5, 0, 0, 0, 0, 3.0, 7.0, 0, 0, 0, 0, 0.6, 0.8, 0, 0, 0, 0, 0.9], np.float32)
     items = [dict(dim=2, method=1, budget=100, seed=11, params=hp, rmin=[0, 0], rmax=[1, 1]),

@@ -37,6 +37,10 @@ def test_oracle_matches_reference_golden(port, name):
         assert np.array_equal(r["bins"].view(np.uint32), g["out_bins"].view(np.uint32))
         assert np.array_equal(r["regions"].view(np.uint32), g["out_regions"].view(np.uint32))
         assert np.array_equal(r["replay"][:, :, 1:].view(np.uint32), g["out_points"].view(np.uint32))
+    elif method == "global":
+        out = port.adaptive_global(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"], _nested(g), int(g["iterations"]),
+                                   initial=g["initial"])
+        assert np.array_equal(out.view(np.uint32), g["out_bins"].view(np.uint32))
     elif method == "batch":
         from viltrum_gb300 import scenes
         items = scenes.batch_items(int(g["n"]), int(g["seed"]), int(g["budget_lo"]), int(g["budget_hi"]))

@@ -30,7 +30,8 @@ __all__ = [
     "Context", "VcuError", "Integrand", "Range", "integrate", "range_", "range_all", "range_primary",
     "trapezoidal", "simpson", "boole", "nested", "error_metric_absolute", "error_metric_relative",
     "error_heuristic_default", "error_heuristic_size", "monte_carlo", "monte_carlo_per_bin_parallel",
-    "integrator_per_bin_parallel", "integrator_adaptive_iterations", "scenes", "load",
+    "integrator_per_bin_parallel", "integrator_adaptive_iterations", "integrator_adaptive_iterations_parallel",
+    "scenes", "load",
     "rr_uniform_region", "region_sampling_uniform", "cv_optimize_weight", "cv_fixed_weight",
     "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction", "integrator_region_based",
     "integrator_crespo2021",
@@ -197,10 +198,15 @@ class MonteCarloPerBinParallel:
 
 @dataclass
 class AdaptiveIterations:
-    """integrator_adaptive_iterations(nested, heuristic, iterations)."""
+    """integrator_adaptive_iterations(nested, heuristic, iterations).  Wrapped in
+    integrator_per_bin_parallel it runs per bin; used directly it is viltrum's global form: one heap
+    over the whole range, regions added into the bins (accumulates)."""
     rule: NestedRule
     heuristic: object
     iterations: int
+
+    def integrate(self, bins, res, f, rng, logger=None, ctx=None, device_bins=False):
+        return _run_global(self, bins, res, f, rng, logger, ctx, device_bins)
 
 
 @dataclass
@@ -224,6 +230,12 @@ def integrator_adaptive_iterations(rule: NestedRule, heuristic_or_iterations, it
     if iterations is None:
         return AdaptiveIterations(rule, error_heuristic_default(error_metric_absolute()), int(heuristic_or_iterations))
     return AdaptiveIterations(rule, heuristic_or_iterations, int(iterations))
+
+
+def integrator_adaptive_iterations_parallel(rule: NestedRule, heuristic_or_iterations, iterations: int | None = None):
+    """integrator_adaptive_iterations_parallel: the same regions and, on one host thread, the same
+    bins as integrator_adaptive_iterations (regions-integrator-parallel-regions.h)."""
+    return integrator_adaptive_iterations(rule, heuristic_or_iterations, iterations)
 
 
 def integrator_per_bin_parallel(inner) -> PerBinParallel:
@@ -353,6 +365,36 @@ def _run(integrator, bins, res, f, rng, logger, ctx, device_bins, accumulate):
             target += vals.astype(target.dtype).reshape(target.shape)
         else:
             target[...] = vals.reshape(target.shape)
+    if logger is not None:
+        logger.log_progress(1, 1)
+    return stats
+
+
+def _run_global(ai: AdaptiveIterations, bins, res, f, rng, logger, ctx, device_bins):
+    f = _as_integrand(f)
+    ctx = ctx or default_context()
+    res = [int(r) for r in res]
+    ch = f.channels
+    nb = int(np.prod(res))
+    if logger is not None:
+        logger.log_progress(0, 1)
+    mem = MEM_DEVICE if device_bins else MEM_HOST
+    p = Context.problem(f.kind, f.params, rng.min, rng.max, res, mem)
+    flat = (not device_bins and isinstance(bins, np.ndarray) and bins.ndim == 1 and bins.dtype == np.float32
+            and bins.size == nb * ch and bins.flags.c_contiguous)
+    if device_bins or flat:
+        out = bins
+    else:
+        # the caller's bins in viltrum's linear order (dim 0 fastest, channels last)
+        arr = np.asarray(bins, dtype=np.float32).reshape(tuple(res) + ((ch,) if ch > 1 else ()))
+        axes = tuple(range(len(res) - 1, -1, -1)) + ((len(res),) if ch > 1 else ())
+        out = np.ascontiguousarray(arr.transpose(axes)).ravel()
+    stats = ctx.adaptive_iterations_global(p, _nested_struct(ai.rule, ai.heuristic), ai.iterations, out)
+    if not device_bins and not flat:
+        vals = out.reshape(tuple(reversed(res)) + (ch,)).transpose(tuple(range(len(res) - 1, -1, -1)) + (len(res),))
+        if ch == 1:
+            vals = vals[..., 0]
+        bins[...] = vals.reshape(bins.shape)
     if logger is not None:
         logger.log_progress(1, 1)
     return stats

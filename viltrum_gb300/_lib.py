@@ -24,7 +24,7 @@ FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
 EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
            "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested",
            "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
-           "vcu_integrate_batch_resident"]
+           "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global"]
 BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
 
 
@@ -128,6 +128,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         L.vcu_learned_control_variates.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(LearnedOpts), vp, vp,
                                                    ctypes.POINTER(LearnedReport), ctypes.POINTER(Stats)]
         L.vcu_mlp_eval.argtypes = [vp, ctypes.c_int32, vp, vp, vp, ctypes.c_int64, vp, vp]
+        L.vcu_adaptive_iterations_global.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested),
+                                                     ctypes.c_uint64, vp, ctypes.POINTER(Stats)]
         L.vcu_integrate_batch.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Nested), ctypes.POINTER(BatchItem),
                                           ctypes.c_uint64, vp, ctypes.c_int32, ctypes.POINTER(BatchReport),
                                           ctypes.POINTER(Stats)]
@@ -251,6 +253,17 @@ def _cv_method(self, p: Problem, nested: Nested, iterations: int, cv: CvOpts, bi
 
 
 Context.control_variates = _cv_method
+
+
+def _global_method(self, p: Problem, nested: Nested, iterations: int, bins) -> Stats:
+    """integrator_adaptive_iterations used directly: accumulates into bins"""
+    st = Stats()
+    self.check(self.lib.vcu_adaptive_iterations_global(self.handle, ctypes.byref(p), ctypes.byref(nested), iterations,
+                                                       _ptr(bins), ctypes.byref(st)))
+    return st
+
+
+Context.adaptive_iterations_global = _global_method
 
 
 def _learned_method(self, p: Problem, opts: LearnedOpts, bins, network_integral=None):

@@ -478,6 +478,7 @@ struct ResCfg {
     uint32_t k0, k1;
     int32_t weight; /* VCU_CV_OPTIMIZE / VCU_CV_FIXED */
     double alpha;
+    const float* approx_init; /* nullable: the approximation starts from these bin values */
 };
 
 template <int DIM, int S, int CH>
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
     /* control-variate integral, summed in list order as the reference does */
     float approx[CH];
     double approx_d[CH];
-    for (int c = 0; c < CH; ++c) approx[c] = 0.0f;
+    for (int c = 0; c < CH; ++c) approx[c] = cfg.approx_init ? cfg.approx_init[bin * CH + c] : 0.0f;
     for (uint32_t base = 0; base < n; base += RES_CHUNK) {
         const uint32_t m = (n - base < RES_CHUNK) ? n - base : RES_CHUNK;
         for (uint32_t i = lane; i < m; i += 32) {
@@ -887,6 +888,8 @@ int cv_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, 
     rcfg.k1 = (uint32_t)(cv.seed >> 32);
     rcfg.weight = cv.weight;
     rcfg.alpha = cv.alpha;
+    /* reserved == 1 (set only by vcu_adaptive_iterations_global): accumulate into the bins' values */
+    rcfg.approx_init = cv.reserved == 1 ? d_bins : nullptr;
     const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
     k_cv_residual<F, DIM, S><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(f, rcfg, off, lists, hp, vals, rmin, rmax,
                                                                           vol, d_replay, d_bins, d_approx,

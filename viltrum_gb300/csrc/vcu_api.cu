@@ -404,6 +404,7 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     if (iterations >= (1ull << 23)) return fail(ctx, VCU_UNSUPPORTED, "control variates take at most 2^23-1 splits");
     if (cv->samples_per_bin > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "samples per bin must be < 2^32");
     if (cv->weight != VCU_CV_OPTIMIZE && cv->weight != VCU_CV_FIXED) return fail(ctx, VCU_INVALID_ARG, "unknown weight");
+    if (cv->reserved != 0) return fail(ctx, VCU_INVALID_ARG, "vcu_cv::reserved must be 0");
     if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
         return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
     if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
@@ -449,6 +450,55 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
     const uint64_t evals = (uint64_t)(sd + (double)iterations * (S - 1) * sd1) + g.nbins * cv->samples_per_bin;
     return scope.end(evals, iterations + 1);
+}
+
+extern "C" int vcu_adaptive_iterations_global(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
+                                              uint64_t iterations, float* bins, vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    BinGrid g;
+    int rc = make_grid(ctx, p, g);
+    if (rc) return rc;
+    if (!nested || !bins) return fail(ctx, VCU_INVALID_ARG, "null nested rule or bins");
+    if (iterations >= (1ull << 23)) return fail(ctx, VCU_UNSUPPORTED, "at most 2^23-1 splits");
+    if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
+    if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    const int ch = vcu_channels(p->f.kind);
+    if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
+    CallScope scope{ctx, stats};
+    if ((rc = scope.begin())) return rc;
+    const size_t bbytes = g.nbins * ch * 4;
+    float* dbins = bins;
+    if (p->mem == VCU_MEM_HOST) {
+        if ((rc = ensure(ctx, ctx->out, bbytes + 256))) return rc;
+        dbins = static_cast<float*>(ctx->out.ptr);
+        VCU_CUDA(ctx, cudaMemcpyAsync(dbins, bins, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    /* the control-variate pipeline without residual samples: its approximation, started from the
+     * bins' current values, is exactly the sequential regions integrator's accumulation */
+    vcu_cv cv{};
+    cv.samples_per_bin = 0;
+    cv.weight = VCU_CV_FIXED;
+    cv.reserved = 1;
+    cv.alpha = 1.0;
+    const int it = (int)iterations;
+    if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_cv_st(ctx, p, g, *nested, it, cv, nullptr, dbins, nullptr, nullptr, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_SIMPSON)
+        rc = run_cv_bs(ctx, p, g, *nested, it, cv, nullptr, dbins, nullptr, nullptr, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_cv_bt(ctx, p, g, *nested, it, cv, nullptr, dbins, nullptr, nullptr, scope.launches);
+    else
+        rc = fail(ctx, VCU_INVALID_ARG, "unsupported nested rule pair");
+    if (rc) return rc;
+    if (p->mem == VCU_MEM_HOST)
+        VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
+    const int S = nested->rule_hi;
+    double sd = 1.0, sd1 = 1.0;
+    for (int d = 0; d < p->dim; ++d) sd *= S;
+    for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
+    return scope.end((uint64_t)(sd + (double)iterations * (S - 1) * sd1), iterations + 1);
 }
 
 extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_learned* opt, float* bins,
