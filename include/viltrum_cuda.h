@@ -226,6 +226,17 @@ int vcu_mlp_eval(vcu_ctx* ctx, int32_t dim, const float* theta, const float* u, 
 int vcu_adaptive_iterations_global(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
                                    uint64_t iterations, float* bins, vcu_stats* stats);
 
+/* ------------------------------------------------------------------ tolerance-driven adaptive NC
+ * Replaces integrate(integrator_adaptive_tolerance(nested(H,L), heuristic, tolerance), bins, f, range)
+ * (src/nested/integrator-adaptive-tolerance.h:9-56): a region whose heuristic error is below
+ * `tolerance` is added into the bins it overlaps, any other is split and both halves visited, depth
+ * first; bins ACCUMULATE, in the reference's depth-first order.  The tree is built breadth first on
+ * the device; `max_regions` bounds the regions built (0: as many as 4 GiB of region storage holds,
+ * at most 2^24-2) and VCU_QUEUE_OVERFLOW reports a tolerance that needs more.  leaves (nullable)
+ * receives the number of leaf regions.  Regions up to S^dim = 243 nodes. */
+int vcu_adaptive_tolerance(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested, float tolerance,
+                           uint64_t max_regions, float* bins, uint64_t* leaves, vcu_stats* stats);
+
 /* ------------------------------------------------------------------ batched independent integrals
  * Many calls of the reference's single-value form, viltrum::integrate(I, f, range)
  * (src/integrate.h:105-113), each with its own dimension, range, integrand parameters, method and

@@ -310,6 +310,34 @@ public:
     }
 };
 
+/* drop-in for integrator_adaptive_tolerance(nested(H,L), heuristic, tolerance)
+ * (src/nested/integrator-adaptive-tolerance.h:9-56): ACCUMULATES, leaves in depth-first order */
+class adaptive_tolerance {
+    nested_rule rule_;
+    float tolerance_;
+    std::uint64_t max_regions_;
+
+public:
+    adaptive_tolerance(nested_rule r, float tolerance = 1e-3f, std::uint64_t max_regions = 0)
+        : rule_(r), tolerance_(tolerance), max_regions_(max_regions) {}
+
+    template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
+    void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
+                   Logger& logger) const {
+        const builtin_integrand& fi = detail::as_builtin(f);
+        context& ctx = thread_context();
+        logger.log_progress(std::size_t(0), std::size_t(1));
+        vcu_problem p = detail::make_problem(fi, res, range);
+        const int ch = fi.channels();
+        std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
+        detail::read_in(bins, res, out, ch);
+        vcu_stats st{};
+        ctx.check(vcu_adaptive_tolerance(ctx.get(), &p, &rule_.n, tolerance_, max_regions_, out.data(), nullptr, &st));
+        detail::write_back(bins, res, out, ch, false);
+        logger.log_progress(std::size_t(1), std::size_t(1));
+    }
+};
+
 /* ---------------------------------------------------------------- control variates */
 /* drop-in for integrator_region_based(regions_generator_adaptive_heap(nested(H,L), heuristic,
  * iterations), regions_integrator_parallel_variance_reduction(rr_uniform_region(), weight,

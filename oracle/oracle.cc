@@ -581,6 +581,83 @@ void adaptive_global(const Fun& fun, const Problem& p, const orc_nested& nc, con
     }
 }
 
+/* ------------------------------------------------------------------ tolerance-driven adaptive */
+/* integrator_adaptive_tolerance (src/nested/integrator-adaptive-tolerance.h:9-56): depth first, a
+ * region whose heuristic error is below the tolerance is integrated into the bins it overlaps, any
+ * other is split along the heuristic's dimension and its two halves visited in order.  Returns the
+ * number of leaves, or -1 when max_regions regions were built before the recursion closed. */
+template <class H, class L, int DIM, class T, class Fun, class M>
+int64_t adaptive_tolerance(const Fun& fun, const Problem& p, const orc_nested& nc, const M& metric, float tol,
+                           uint64_t max_regions, float* out) {
+    using R = Region<H, L, DIM, T>;
+    const auto range = make_range<DIM>(p);
+    Fn<Fun, DIM, T> f{&fun};
+    uint64_t factor = 1;
+    for (int i = 0; i < p.dimbins; ++i) factor *= p.res[i];
+    std::array<float, DIM> drange;
+    for (int i = 0; i < p.dimbins; ++i) drange[i] = (range.max(i) - range.min(i)) / float(p.res[i]);
+    auto add_region = [&](const R& r) {
+        std::array<uint64_t, 8> st, en;
+        for (int i = 0; i < p.dimbins; ++i) {
+            st[i] = std::max(std::size_t(0),
+                             std::size_t(float(p.res[i]) * (r.range.min(i) - range.min(i)) / (range.max(i) - range.min(i))));
+            en[i] = std::max(std::size_t(st[i] + 1),
+                             std::min(std::size_t(p.res[i]),
+                                      std::size_t(0.99f + (float(p.res[i]) * (r.range.max(i) - range.min(i)) /
+                                                           (range.max(i) - range.min(i))))));
+        }
+        std::array<uint64_t, 8> q = st;
+        for (;;) {
+            Range<DIM> binrange = range;
+            uint64_t lin = 0, mul = 1;
+            for (int i = 0; i < p.dimbins; ++i) {
+                binrange = binrange.subrange_dimension(i, range.min(i) + q[i] * drange[i], range.min(i) + (q[i] + 1) * drange[i]);
+                lin += q[i] * mul;
+                mul *= p.res[i];
+            }
+            const Range<DIM> rb = binrange.intersection(r.range);
+            if (!rb.empty()) {
+                T v = VT<T>::from(out + lin * VT<T>::CH);
+                v += double(factor) * r.integral_subrange(rb);
+                VT<T>::to(v, out + lin * VT<T>::CH);
+            }
+            int i = 0;
+            for (; i < p.dimbins; ++i) {
+                if (++q[i] < en[i]) break;
+                q[i] = st[i];
+            }
+            if (i == p.dimbins) break;
+        }
+    };
+    uint64_t built = 1;
+    int64_t leaves = 0;
+    R root;
+    root.range = range;
+    root.fill(f);
+    /* explicit stack in visit order (the reference recurses) */
+    std::vector<R> stack;
+    stack.push_back(std::move(root));
+    while (!stack.empty()) {
+        R r = std::move(stack.back());
+        stack.pop_back();
+        float err;
+        int dim;
+        std::tie(err, dim) = heuristic(r, nc, metric);
+        if (err < tol) {
+            add_region(r);
+            ++leaves;
+        } else {
+            if (built + 2 > max_regions) return -1;
+            R c[2];
+            r.split(f, dim, c[0], c[1]);
+            built += 2;
+            stack.push_back(std::move(c[1]));
+            stack.push_back(std::move(c[0]));
+        }
+    }
+    return leaves;
+}
+
 /* ------------------------------------------------------------------ single-value integrals */
 /* monte_carlo(budget, seed) through integrate(I, f, range): one bin of resolution {1}, the
  * integrator's own std::mt19937(seed) (moved in, not reseeded), bins(pos) += f(x) * factor */
@@ -985,4 +1062,23 @@ extern "C" int orc_adaptive_global(int32_t kind, const float* params, int32_t n_
             });
         });
     });
+}
+
+extern "C" int64_t orc_adaptive_tolerance(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                                          const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                                          const orc_nested* nested, float tolerance, uint64_t max_regions,
+                                          float* out) {
+    if (!valid_problem(dim, dimbins, res) || !nested || !out) return -2;
+    Problem p{dim, dimbins, rmin, rmax, res};
+    int64_t leaves = -2;
+    const int rc = with_integrand(kind, params, n_params, dim, [&](const auto& f, auto D, auto t) -> int {
+        return with_rules(*nested, [&](auto h, auto l) -> int {
+            return with_metric(*nested, [&](auto m) -> int {
+                leaves = adaptive_tolerance<decltype(h), decltype(l), decltype(D)::value, decltype(t)>(
+                    f, p, *nested, m, tolerance, max_regions, out);
+                return 0;
+            });
+        });
+    });
+    return rc ? -2 : leaves;
 }

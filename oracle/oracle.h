@@ -95,6 +95,14 @@ int orc_adaptive_global(int32_t kind, const float* params, int32_t n_params, int
                         const float* rmax, int32_t dimbins, const uint64_t* res, const orc_nested* nested,
                         uint64_t iterations, float* out);
 
+/* integrate(integrator_adaptive_tolerance(nested(H,L), heuristic, tolerance), bins, f, range)
+ * (src/nested/integrator-adaptive-tolerance.h:9-56): depth-first, regions whose error is below the
+ * tolerance are added into the bins (accumulating into out), others split.  Returns the number of
+ * leaf regions, -1 if more than max_regions regions would be built, -2 on a bad argument.      */
+int64_t orc_adaptive_tolerance(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                               const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                               const orc_nested* nested, float tolerance, uint64_t max_regions, float* out);
+
 /* One single-value viltrum::integrate(I, f, range) (src/integrate.h:105-113):
  *   method 0: I = monte_carlo(budget, seed)  (std::mt19937(seed), float accumulation,
  *             src/monte-carlo/monte-carlo.h:39-63, 89-95)

@@ -92,6 +92,10 @@ class Oracle:
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
                       ctypes.POINTER(Nested), ctypes.c_uint64, _f32p]
+        f = getattr(L, prefix + "adaptive_tolerance")
+        f.restype = ctypes.c_int64
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                      ctypes.POINTER(Nested), ctypes.c_float, ctypes.c_uint64, _f32p]
         f = getattr(L, prefix + "integrate_single")
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32,
@@ -177,6 +181,20 @@ class Oracle:
             ctypes.byref(nested), iterations, _ptr(out))
         self._check(rc, "adaptive_global")
         return out.reshape(nb, ch)
+
+    def adaptive_tolerance(self, kind, params, rmin, rmax, res, nested: Nested, tolerance, initial=None,
+                           max_regions=1 << 24):
+        """integrator_adaptive_tolerance: returns (bins, number of leaf regions)."""
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        out = np.zeros(nb * ch, dtype=np.float32) if initial is None else np.array(initial, np.float32).ravel().copy()
+        n = getattr(self.lib, self.prefix + "adaptive_tolerance")(
+            kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
+            ctypes.byref(nested), tolerance, max_regions, _ptr(out))
+        if n < -1:
+            raise RuntimeError(f"{self.prefix}adaptive_tolerance failed ({n})")
+        return out.reshape(nb, ch), int(n)
 
     def integrate_single(self, kind, params, rmin, rmax, method, budget, seed=0, nested: Nested | None = None):
         """One single-value integrate(I, f, range): method 0 = monte_carlo(budget, seed), 1 = adaptive

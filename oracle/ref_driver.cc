@@ -157,6 +157,22 @@ int run_global(const Fun& fun, const float* rmin, const float* rmax, const uint6
     return 0;
 }
 
+template <class Fun, std::size_t DIM, std::size_t DB, class T, class Rule, class Heur>
+int run_tolerance(const Fun& fun, const float* rmin, const float* rmax, const uint64_t* res, const Rule& rule,
+                  const Heur& heur, float tol, float* out) {
+    RefF<Fun, DIM, T> f{&fun, nullptr};
+    auto range = mk_range<DIM>(rmin, rmax);
+    BinStore<DB, T> bs{mk_res<DB>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.resize(nb);
+    for (std::size_t i = 0; i < nb; ++i) bs.v[i] = VT<T>::from(out + i * VT<T>::CH);
+    auto bins = [&bs](const std::array<std::size_t, DB>& p) -> T& { return bs.v[bs.lin(p)]; };
+    viltrum::integrate(viltrum::integrator_adaptive_tolerance(rule, heur, tol), bins, bs.res, f, range);
+    for (std::size_t i = 0; i < nb; ++i) VT<T>::to(bs.v[i], out + i * VT<T>::CH);
+    return 0;
+}
+
 template <class Fun, std::size_t DIM, std::size_t DB, class T, class Rule, class Heur, class CV>
 int run_cv(const Fun& fun, const float* rmin, const float* rmax, const uint64_t* res, const Rule& rule,
            const Heur& heur, uint64_t iters, uint64_t spp, uint64_t seed, CV cv, float* out, float* regions_out,
@@ -393,4 +409,35 @@ extern "C" int ref_adaptive_global(int32_t kind, const float* params, int32_t n_
                                                        out);
     }
     return 9;
+}
+
+extern "C" int64_t ref_adaptive_tolerance(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                                          const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                                          const orc_nested* nc, float tolerance, uint64_t max_regions, float* out) {
+    (void)max_regions;
+    using namespace viltrum;
+    const bool st_da = nc->rule_hi == ORC_RULE_SIMPSON && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
+                       nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_ABSOLUTE;
+    const bool bs_da = nc->rule_hi == ORC_RULE_BOOLE && nc->rule_lo == ORC_RULE_SIMPSON &&
+                       nc->heuristic == ORC_HEUR_DEFAULT && nc->metric == ORC_METRIC_ABSOLUTE;
+    auto hda = error_heuristic_default(error_metric_absolute());
+    if (kind == vcu::VCU_F_SCENE2 && dim == 2 && dimbins == 2 && bs_da) {
+        auto* f = new vcu::Scene2;
+        const int r = f->build(params, n_params)
+                          ? 3
+                          : run_tolerance<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(boole, simpson), hda,
+                                                                    tolerance, out);
+        delete f;
+        return r ? -2 : 0;
+    }
+    if (kind == vcu::VCU_F_MOVING_SCENE3 && dim == 3 && dimbins == 2 && st_da) {
+        auto* f = new vcu::MovingScene3;
+        const int r = f->build(params, n_params)
+                          ? 3
+                          : run_tolerance<vcu::MovingScene3, 3, 2, vrgb>(*f, rmin, rmax, res, nested(simpson, trapezoidal),
+                                                                         hda, tolerance, out);
+        delete f;
+        return r ? -2 : 0;
+    }
+    return -9;
 }

@@ -46,6 +46,7 @@ int main() {
     viltrum::integrate(vc::crespo2021(255, 16, 3), cv_bins, scene, viltrum::range_primary<2>());
     viltrum::integrate(vc::learned_control_variates(16, 5, 50), learned, wave, viltrum::range_primary<2>());
     viltrum::integrate(vc::adaptive_iterations(vc::simpson_trapezoidal(), 127), global, scene, viltrum::range_primary<2>());
+    viltrum::integrate(vc::adaptive_tolerance(vc::boole_simpson(), 1e-6f), global, scene, viltrum::range_primary<2>());
 #else
     quiet log;
     const box<2> unit{{0.0f, 0.0f}, {1.0f, 1.0f}};
@@ -60,6 +61,7 @@ int main() {
     vc::learned_control_variates(16, 5, 50).integrate(l1, std::array<std::size_t, 1>{16}, wave, unit, log);
     auto g1 = [&](const std::array<std::size_t, 1>& p) -> float& { return global[p[0]]; };
     vc::adaptive_iterations(vc::simpson_trapezoidal(), 127).integrate(g1, std::array<std::size_t, 1>{32}, scene, unit, log);
+    vc::adaptive_tolerance(vc::boole_simpson(), 1e-6f).integrate(g1, std::array<std::size_t, 1>{32}, scene, unit, log);
 #endif
     /* independent integrals: two half-space items, one nested and one Monte Carlo */
     std::vector<vc::batch_item> items(2);

@@ -114,6 +114,25 @@ def run_global(lib: orc.Oracle, kw: dict) -> dict:
                                         initial=global_initial(kw))}
 
 
+# integrator_adaptive_tolerance: depth first, leaves added into bins that start from a non-zero image
+TOL_CASES = [
+    ("tolerance_scene2_bins16x16_bs_abs_1e-6", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1],
+                                                    res=[16, 16], nested=("boole", "simpson", "default", "absolute"),
+                                                    tolerance=1e-6)),
+    ("tolerance_moving3_rgb_bins8x8_st_abs_1e-4", dict(kind=scenes.MOVING_SCENE3, params=MOVING_SMALL, rmin=[0, 0, 0],
+                                                       rmax=[1, 1, 1], res=[8, 8],
+                                                       nested=("simpson", "trapezoidal", "default", "absolute"),
+                                                       tolerance=1e-4)),
+]
+
+
+def run_tolerance(lib: orc.Oracle, kw: dict) -> dict:
+    hi, lo, heur, met = kw["nested"]
+    bins, n = lib.adaptive_tolerance(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"],
+                                     orc.Nested.make(hi, lo, heur, met), kw["tolerance"], initial=global_initial(kw))
+    return {"bins": bins}
+
+
 # independent single-value integrals (the batched-integrals workload at small budgets)
 BATCH_CASES = [
     ("batch_halfspace_n64_seed5", dict(n=64, seed=5, budget_lo=1, budget_hi=400)),
@@ -223,6 +242,17 @@ def main() -> int:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="global", nested=np.array(kw["nested"]),
                             initial=global_initial(kw), **meta, out_bins=r["bins"])
         print(f"ok {name}")
+    for name, kw in TOL_CASES:
+        r, p = run_tolerance(ref, kw), run_tolerance(port, kw)
+        if not np.array_equal(r["bins"].view(np.uint32), p["bins"].view(np.uint32)):
+            bad += 1
+            print(f"MISMATCH {name}")
+            continue
+        meta = {k: np.asarray(v) for k, v in kw.items() if k not in ("params", "nested")}
+        meta["params"] = np.asarray(kw["params"], dtype=np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), method="tolerance", nested=np.array(kw["nested"]),
+                            initial=global_initial(kw), **meta, out_bins=r["bins"])
+        print(f"ok {name}")
     for name, kw in BATCH_CASES:
         r, p = run_batch(ref, kw), run_batch(port, kw)
         if not np.array_equal(r["values"].view(np.uint32), p["values"].view(np.uint32)):
@@ -232,7 +262,7 @@ def main() -> int:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="batch", **{k: np.asarray(v) for k, v in kw.items()},
                             out_values=r["values"])
         print(f"ok {name}")
-    total = len(CASES) + len(BATCH_CASES) + len(GLOBAL_CASES)
+    total = len(CASES) + len(BATCH_CASES) + len(GLOBAL_CASES) + len(TOL_CASES)
     print(f"{total - bad} of {total} cases bit-identical")
     return 1 if bad else 0
 

@@ -48,10 +48,12 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
     ctx.learned_control_variates(ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [16]),
                                  _lib.LearnedOpts(16, 5, 50, 32768, 3e-3, 3, 1, 1), l)
     assert np.array_equal(lrn.view(np.uint32), l.view(np.uint32))
-    # adaptive_iterations used directly, accumulating into bins that start at 0.5
+    # adaptive_iterations used directly, then adaptive_tolerance, accumulating into bins that start at 0.5
     gb = np.full(32, 0.5, np.float32)
     ctx.adaptive_iterations_global(ctx.problem(scenes.SCENE2, scene, [0, 0], [1, 1], [32]),
                                    _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37), 127, gb)
+    ctx.adaptive_tolerance(ctx.problem(scenes.SCENE2, scene, [0, 0], [1, 1], [32]),
+                           _lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37), 1e-6, gb)
     assert np.array_equal(glb.view(np.uint32), gb.view(np.uint32))
     # two independent integrals
     hp = np.array([2, 1.5, 0.5, 0, 0, 0, 0, 3.0, 7.0, 0, 0, 0, 0, 0.6, 0.8, 0, 0, 0, 0, 0.9], np.float32)

@@ -41,6 +41,10 @@ def test_oracle_matches_reference_golden(port, name):
         out = port.adaptive_global(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"], _nested(g), int(g["iterations"]),
                                    initial=g["initial"])
         assert np.array_equal(out.view(np.uint32), g["out_bins"].view(np.uint32))
+    elif method == "tolerance":
+        out, _ = port.adaptive_tolerance(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"], _nested(g),
+                                         float(g["tolerance"]), initial=g["initial"])
+        assert np.array_equal(out.view(np.uint32), g["out_bins"].view(np.uint32))
     elif method == "batch":
         from viltrum_gb300 import scenes
         items = scenes.batch_items(int(g["n"]), int(g["seed"]), int(g["budget_lo"]), int(g["budget_hi"]))

@@ -31,6 +31,7 @@ __all__ = [
     "trapezoidal", "simpson", "boole", "nested", "error_metric_absolute", "error_metric_relative",
     "error_heuristic_default", "error_heuristic_size", "monte_carlo", "monte_carlo_per_bin_parallel",
     "integrator_per_bin_parallel", "integrator_adaptive_iterations", "integrator_adaptive_iterations_parallel",
+    "integrator_adaptive_tolerance",
     "scenes", "load",
     "rr_uniform_region", "region_sampling_uniform", "cv_optimize_weight", "cv_fixed_weight",
     "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction", "integrator_region_based",
@@ -232,6 +233,27 @@ def integrator_adaptive_iterations(rule: NestedRule, heuristic_or_iterations, it
     return AdaptiveIterations(rule, heuristic_or_iterations, int(iterations))
 
 
+@dataclass
+class AdaptiveTolerance:
+    """integrator_adaptive_tolerance(nested, heuristic, tolerance) (src/nested/integrator-adaptive-
+    tolerance.h:9-56): accumulates into the bins, depth first."""
+    rule: NestedRule
+    heuristic: object
+    tolerance: float
+    max_regions: int = 0
+
+    def integrate(self, bins, res, f, rng, logger=None, ctx=None, device_bins=False):
+        return _run_global(self, bins, res, f, rng, logger, ctx, device_bins)
+
+
+def integrator_adaptive_tolerance(rule: NestedRule, heuristic_or_tolerance=1e-3, tolerance: float | None = None,
+                                  max_regions: int = 0):
+    if tolerance is None and not hasattr(heuristic_or_tolerance, "metric"):
+        return AdaptiveTolerance(rule, error_heuristic_default(error_metric_absolute()), float(heuristic_or_tolerance),
+                                 max_regions)
+    return AdaptiveTolerance(rule, heuristic_or_tolerance, float(1e-3 if tolerance is None else tolerance), max_regions)
+
+
 def integrator_adaptive_iterations_parallel(rule: NestedRule, heuristic_or_iterations, iterations: int | None = None):
     """integrator_adaptive_iterations_parallel: the same regions and, on one host thread, the same
     bins as integrator_adaptive_iterations (regions-integrator-parallel-regions.h)."""
@@ -370,7 +392,7 @@ def _run(integrator, bins, res, f, rng, logger, ctx, device_bins, accumulate):
     return stats
 
 
-def _run_global(ai: AdaptiveIterations, bins, res, f, rng, logger, ctx, device_bins):
+def _run_global(ai, bins, res, f, rng, logger, ctx, device_bins):
     f = _as_integrand(f)
     ctx = ctx or default_context()
     res = [int(r) for r in res]
@@ -389,7 +411,10 @@ def _run_global(ai: AdaptiveIterations, bins, res, f, rng, logger, ctx, device_b
         arr = np.asarray(bins, dtype=np.float32).reshape(tuple(res) + ((ch,) if ch > 1 else ()))
         axes = tuple(range(len(res) - 1, -1, -1)) + ((len(res),) if ch > 1 else ())
         out = np.ascontiguousarray(arr.transpose(axes)).ravel()
-    stats = ctx.adaptive_iterations_global(p, _nested_struct(ai.rule, ai.heuristic), ai.iterations, out)
+    if isinstance(ai, AdaptiveTolerance):
+        stats, _ = ctx.adaptive_tolerance(p, _nested_struct(ai.rule, ai.heuristic), ai.tolerance, out, ai.max_regions)
+    else:
+        stats = ctx.adaptive_iterations_global(p, _nested_struct(ai.rule, ai.heuristic), ai.iterations, out)
     if not device_bins and not flat:
         vals = out.reshape(tuple(reversed(res)) + (ch,)).transpose(tuple(range(len(res) - 1, -1, -1)) + (len(res),))
         if ch == 1:

@@ -24,7 +24,7 @@ FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
 EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
            "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested",
            "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
-           "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global"]
+           "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global", "vcu_adaptive_tolerance"]
 BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
 
 
@@ -130,6 +130,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         L.vcu_mlp_eval.argtypes = [vp, ctypes.c_int32, vp, vp, vp, ctypes.c_int64, vp, vp]
         L.vcu_adaptive_iterations_global.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested),
                                                      ctypes.c_uint64, vp, ctypes.POINTER(Stats)]
+        L.vcu_adaptive_tolerance.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested), ctypes.c_float,
+                                             ctypes.c_uint64, vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(Stats)]
         L.vcu_integrate_batch.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Nested), ctypes.POINTER(BatchItem),
                                           ctypes.c_uint64, vp, ctypes.c_int32, ctypes.POINTER(BatchReport),
                                           ctypes.POINTER(Stats)]
@@ -264,6 +266,18 @@ def _global_method(self, p: Problem, nested: Nested, iterations: int, bins) -> S
 
 
 Context.adaptive_iterations_global = _global_method
+
+
+def _tolerance_method(self, p: Problem, nested: Nested, tolerance: float, bins, max_regions: int = 0):
+    """integrator_adaptive_tolerance: accumulates into bins; returns (stats, number of leaf regions)"""
+    st = Stats()
+    leaves = ctypes.c_uint64(0)
+    self.check(self.lib.vcu_adaptive_tolerance(self.handle, ctypes.byref(p), ctypes.byref(nested), tolerance,
+                                               max_regions, _ptr(bins), ctypes.byref(leaves), ctypes.byref(st)))
+    return st, int(leaves.value)
+
+
+Context.adaptive_tolerance = _tolerance_method
 
 
 def _learned_method(self, p: Problem, opts: LearnedOpts, bins, network_integral=None):

@@ -776,6 +776,78 @@ static __global__ void k_cv_regions_out(const int* __restrict__ heap_pay, const 
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+/* stages 2 and 3 over a finished set of regions: hp[0..nheap) are pool ids (low 24 bits) in the
+ * order the reference integrates them (heap order, or depth-first order for the tolerance-driven
+ * form); cnt/off/cur are per-bin scratch of nbins, nbins+1, nbins words */
+template <class F, int DIM, int SH>
+int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_cv& cv,
+                      const float* vals, const float* rmin, const float* rmax, const float* vol, const int* hp,
+                      size_t nheap, uint32_t* cnt, uint32_t* off, uint32_t* cur, const float* d_replay, float* d_bins,
+                      float* d_approx, float* d_regions, uint32_t& launches) {
+    constexpr int S = SH;
+    int rc = VCU_OK;
+    /* stage 2 */
+    ListCfg lc{};
+    for (int d = 0; d < p->dimbins; ++d) {
+        lc.rmin[d] = p->range_min[d];
+        lc.rmax[d] = p->range_max[d];
+        lc.res[d] = g.res[d];
+    }
+    lc.dim = DIM;
+    lc.dimbins = p->dimbins;
+    lc.nheap = (int)nheap;
+    VCU_CUDA(ctx, cudaMemsetAsync(cnt, 0, g.nbins * 4, ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(cur, 0, g.nbins * 4, ctx->stream));
+    const unsigned lblocks = (unsigned)((nheap * 32 + 255) / 256);
+    k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, cnt, nullptr, nullptr, nullptr, 0);
+    k_cv_scan<<<1, 1024, 0, ctx->stream>>>(cnt, off, g.nbins, ctx->d_status);
+    launches += 2;
+    VCU_CUDA(ctx, cudaGetLastError());
+    uint32_t total = 0;
+    VCU_CUDA(ctx, cudaMemcpyAsync(&total, off + g.nbins, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if ((rc = ensure(ctx, ctx->aux, (size_t)total * 8 + 512))) return rc;
+    uint32_t* lists_u = static_cast<uint32_t*>(ctx->aux.ptr);
+    uint32_t* lists = lists_u + total + 64;
+    k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, nullptr, off, cur, lists_u, 1);
+    k_cv_sort<<<(unsigned)((g.nbins * 32 + 255) / 256), 256, 0, ctx->stream>>>(off, lists_u, lists, g.nbins);
+    launches += 2;
+    VCU_CUDA(ctx, cudaGetLastError());
+
+    /* stage 3 */
+    ResCfg rcfg{};
+    for (int d = 0; d < DIM; ++d) {
+        rcfg.rmin[d] = p->range_min[d];
+        rcfg.rmax[d] = p->range_max[d];
+    }
+    for (int d = 0; d < p->dimbins; ++d) {
+        rcfg.res[d] = g.res[d];
+        rcfg.drange[d] = g.drange[d];
+    }
+    rcfg.dimbins = p->dimbins;
+    rcfg.nbins = g.nbins;
+    rcfg.factor = (double)g.factor;
+    rcfg.spp = cv.samples_per_bin;
+    rcfg.k0 = (uint32_t)cv.seed;
+    rcfg.k1 = (uint32_t)(cv.seed >> 32);
+    rcfg.weight = cv.weight;
+    rcfg.alpha = cv.alpha;
+    /* reserved == 1 (set only by vcu_adaptive_iterations_global): accumulate into the bins' values */
+    rcfg.approx_init = cv.reserved == 1 ? d_bins : nullptr;
+    const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
+    k_cv_residual<F, DIM, S><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(f, rcfg, off, lists, hp, vals, rmin, rmax,
+                                                                          vol, d_replay, d_bins, d_approx,
+                                                                          ctx->d_status);
+    ++launches;
+    if (d_regions) {
+        k_cv_regions_out<<<(unsigned)((nheap + 255) / 256), 256, 0, ctx->stream>>>(hp, rmin, rmax, DIM, (int)nheap,
+                                                                                  d_regions);
+        ++launches;
+    }
+    VCU_CUDA(ctx, cudaGetLastError());
+    return VCU_OK;
+}
+
 template <int DIM, int SH, int SL, class F>
 int cv_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iters,
               const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
@@ -842,66 +914,363 @@ int cv_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, 
     ++launches;
     VCU_CUDA(ctx, cudaGetLastError());
 
-    /* stage 2 */
-    ListCfg lc{};
-    for (int d = 0; d < p->dimbins; ++d) {
-        lc.rmin[d] = p->range_min[d];
-        lc.rmax[d] = p->range_max[d];
-        lc.res[d] = g.res[d];
-    }
-    lc.dim = DIM;
-    lc.dimbins = p->dimbins;
-    lc.nheap = (int)nheap;
-    VCU_CUDA(ctx, cudaMemsetAsync(cnt, 0, g.nbins * 4, ctx->stream));
-    VCU_CUDA(ctx, cudaMemsetAsync(cur, 0, g.nbins * 4, ctx->stream));
-    const unsigned lblocks = (unsigned)((nheap * 32 + 255) / 256);
-    k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, cnt, nullptr, nullptr, nullptr, 0);
-    k_cv_scan<<<1, 1024, 0, ctx->stream>>>(cnt, off, g.nbins, ctx->d_status);
-    launches += 2;
-    VCU_CUDA(ctx, cudaGetLastError());
-    uint32_t total = 0;
-    VCU_CUDA(ctx, cudaMemcpyAsync(&total, off + g.nbins, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if ((rc = ensure(ctx, ctx->aux, (size_t)total * 8 + 512))) return rc;
-    uint32_t* lists_u = static_cast<uint32_t*>(ctx->aux.ptr);
-    uint32_t* lists = lists_u + total + 64;
-    k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, nullptr, off, cur, lists_u, 1);
-    k_cv_sort<<<(unsigned)((g.nbins * 32 + 255) / 256), 256, 0, ctx->stream>>>(off, lists_u, lists, g.nbins);
-    launches += 2;
-    VCU_CUDA(ctx, cudaGetLastError());
+    return regions_into_bins<F, DIM, SH>(ctx, f, p, g, cv, vals, rmin, rmax, vol, hp, nheap, cnt, off, cur, d_replay,
+                                         d_bins, d_approx, d_regions, launches);
+}
 
-    /* stage 3 */
-    ResCfg rcfg{};
+
+/* ---------------------------------------------------------------- tolerance-driven adaptive
+ * integrator_adaptive_tolerance (src/nested/integrator-adaptive-tolerance.h:9-56): the reference
+ * recurses depth first -- a region whose heuristic error is below the tolerance is integrated into
+ * the bins, any other is split and its halves visited in order.  Nothing is sequential but the order
+ * the leaves are added into a bin, so the tree is built breadth first, one kernel per level, one
+ * warp per region (errors, decision, and the split's new nodes), with every level's regions in
+ * parallel.  Afterwards the leaves are ranked in depth-first order (leaf counts bottom up, offsets
+ * top down) and stages 2-3 add them into the bins in that order. */
+struct TolCfg {
+    float rmin[VCU_MAX_DIM], rmax[VCU_MAX_DIM];
+    int32_t heuristic, relative;
+    float min_val_f;
+    float tol;
+    double size_weight, min_size;
+    uint32_t capacity;
+};
+
+constexpr int TOL_WARPS = 4;
+
+template <class F, int DIM, int SH>
+__global__ void k_tol_root(const __grid_constant__ F f, const TolCfg cfg, float* __restrict__ vals,
+                           float* __restrict__ rmin, float* __restrict__ rmax, float* __restrict__ vol) {
+    constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM);
+    __shared__ float CO[DIM * S];
+    for (int t = threadIdx.x; t < DIM * S; t += blockDim.x) {
+        const int d = t / S, j = t % S;
+        CO[t] = node_coord(node_pos<S>(j), vsub(cfg.rmax[d], cfg.rmin[d]), cfg.rmin[d]);
+    }
+    if (threadIdx.x == 0) {
+        float v = 1.0f;
+        for (int d = 0; d < DIM; ++d) {
+            rmin[d] = cfg.rmin[d];
+            rmax[d] = cfg.rmax[d];
+            v = vmul(v, vsub(cfg.rmax[d], cfg.rmin[d]));
+        }
+        vol[0] = v;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < SD; t += blockDim.x) {
+        float x[F::DIM];
+        for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+        int rem = t;
+        for (int d = 0; d < DIM; ++d) {
+            x[d] = CO[d * S + rem % S];
+            rem /= S;
+        }
+        float v[CH];
+        f(x, v);
+        for (int c = 0; c < CH; ++c) vals[t * CH + c] = v[c];
+    }
+}
+
+/* one level: counters[0] = pool slots used, counters[1] = regions of the next level */
+template <class F, int DIM, int SH, int SL>
+__global__ void __launch_bounds__(TOL_WARPS * 32)
+    k_tol_level(const __grid_constant__ F f, const TolCfg cfg, const int* __restrict__ cur, int ncur,
+                int* __restrict__ next, uint32_t* __restrict__ counters, float* __restrict__ vals,
+                float* __restrict__ rmin, float* __restrict__ rmax, float* __restrict__ vol, int* __restrict__ child,
+                uint32_t* __restrict__ status) {
+    constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM), NL = ipow(S, DIM - 1), NNEW = (S - 1) * NL;
+    __shared__ float LN[TOL_WARPS][DIM * NL];
+    __shared__ float EC[TOL_WARPS][DIM];
+    __shared__ float CO[TOL_WARPS][DIM * S], CN[TOL_WARPS][S - 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * TOL_WARPS + warp;
+    if (w >= ncur) return;
+    const int id = cur[w];
+    const float* V = vals + (size_t)id * SD * CH;
+    /* per-dimension errors (region.h:379-418) with the reference's rounding */
+    for (int t = lane; t < DIM * NL; t += 32) {
+        const int d = t / NL, J = t % NL;
+        float m = 0.0f;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            float line[S], low[SL];
+#pragma unroll
+            for (int i = 0; i < S; ++i) line[i] = V[node_index<DIM, S>(d, J, i) * CH + c];
+#pragma unroll
+            for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+            float H, L;
+            if constexpr (CH == 1) {
+                H = RefRule<S>::scalar(line);
+                L = RefRule<SL>::scalar(low);
+            } else {
+                H = RefRule<S>::rgb(line);
+                L = RefRule<SL>::rgb(low);
+            }
+            const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
+            m = (c == 0) ? mv : vadd(m, mv);
+        }
+        LN[warp][t] = m;
+    }
+    __syncwarp();
+    if (lane < DIM) {
+        float buf[NL];
+        for (int i = 0; i < NL; ++i) buf[i] = LN[warp][lane * NL + i];
+        int n = NL;
+        for (int level = 0; level < DIM - 1; ++level) {
+            n /= S;
+            for (int i = 0; i < n; ++i) buf[i] = RefRule<S>::scalar(buf + i * S);
+        }
+        EC[warp][lane] = vmul(vol[id], buf[0]);
+    }
+    __syncwarp();
+    int split_dim = 0, c0 = -1;
+    if (lane == 0) {
+        const float* e = EC[warp];
+        float max_err;
+        int max_dim = 0;
+        if (cfg.heuristic == VCU_HEUR_DEFAULT) {
+            max_err = 0.0f;
+            for (int d = 0; d < DIM; ++d)
+                if (e[d] > max_err) {
+                    max_err = e[d];
+                    max_dim = d;
+                }
+        } else {
+            float wd = vsub(rmax[(size_t)id * DIM], rmin[(size_t)id * DIM]);
+            if ((double)wd < cfg.min_size || isnan(wd)) max_err = 0.0f;
+            else max_err = __double2float_rn(__dadd_rn((double)e[0], __dmul_rn(cfg.size_weight, (double)fabsf(wd))));
+            for (int d = 1; d < DIM; ++d) {
+                wd = vsub(rmax[(size_t)id * DIM + d], rmin[(size_t)id * DIM + d]);
+                float err = __double2float_rn(__dadd_rn((double)e[d], __dmul_rn(cfg.size_weight, (double)fabsf(wd))));
+                if ((double)wd < cfg.min_size) err = 0.0f;
+                if (err >= max_err) {
+                    max_err = err;
+                    max_dim = d;
+                }
+            }
+        }
+        if (max_err < cfg.tol) {
+            child[id] = -1; /* leaf */
+        } else {
+            const uint32_t c = atomicAdd(&counters[0], 2u);
+            if (c + 2 > cfg.capacity) {
+                atomicOr(status, VCU_FLAG_OVERFLOW);
+                child[id] = -1;
+            } else {
+                child[id] = (int)c;
+                const uint32_t k = atomicAdd(&counters[1], 2u);
+                next[k] = (int)c;
+                next[k + 1] = (int)c + 1;
+                c0 = (int)c;
+                split_dim = max_dim;
+            }
+        }
+    }
+    c0 = __shfl_sync(0xffffffffu, c0, 0);
+    split_dim = __shfl_sync(0xffffffffu, split_dim, 0);
+    if (c0 < 0) return;
+    const int dd = split_dim, C0 = c0, C1 = c0 + 1;
+    const float* pmin = rmin + (size_t)id * DIM;
+    const float* pmax = rmax + (size_t)id * DIM;
+    for (int t = lane; t < DIM * S + (S - 1); t += 32) {
+        if (t < DIM * S) {
+            const int d = t / S, j = t % S;
+            CO[warp][t] = node_coord(node_pos<S>(j), vsub(pmax[d], pmin[d]), pmin[d]);
+        } else {
+            const int k = t - DIM * S;
+            CN[warp][k] = node_coord(mid_pos<S>(k), vsub(pmax[dd], pmin[dd]), pmin[dd]);
+        }
+    }
+    __syncwarp();
+    float* V0 = vals + (size_t)C0 * SD * CH;
+    float* V1 = vals + (size_t)C1 * SD * CH;
+    for (int t = lane; t < NNEW + S * NL; t += 32) {
+        const bool fresh = t < NNEW;
+        const int u = fresh ? t : t - NNEW;
+        const int k = u / NL, J = u % NL;
+        float v[CH];
+        int i;
+        if (fresh) {
+            float x[F::DIM];
+            for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+            int rem = J;
+            for (int e = 0; e < DIM; ++e) {
+                if (e == dd) continue;
+                x[e] = CO[warp][e * S + rem % S];
+                rem /= S;
+            }
+            x[dd] = CN[warp][k];
+            f(x, v);
+            i = 2 * k + 1;
+        } else {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) v[c] = V[node_index<DIM, S>(dd, J, k) * CH + c];
+            i = 2 * k;
+        }
+        if (i <= S - 1) {
+            const int n0 = node_index<DIM, S>(dd, J, i) * CH;
+#pragma unroll
+            for (int c = 0; c < CH; ++c) V0[n0 + c] = v[c];
+        }
+        if (i >= S - 1) {
+            const int n1 = node_index<DIM, S>(dd, J, i - (S - 1)) * CH;
+#pragma unroll
+            for (int c = 0; c < CH; ++c) V1[n1 + c] = v[c];
+        }
+    }
+    if (lane == 0) {
+        const float pmn = pmin[dd], pmx = pmax[dd];
+        const float half = vdiv(vsub(pmx, pmn), 2.0f);
+        const float mid = vadd(pmn, vmul(half, 1.0f));
+        float v0 = 1.0f, v1 = 1.0f;
+        for (int d = 0; d < DIM; ++d) {
+            const float mn = pmin[d], mx = pmax[d];
+            const float mx0 = (d == dd) ? mid : mx;
+            const float mn1 = (d == dd) ? mid : mn;
+            rmin[(size_t)C0 * DIM + d] = mn;
+            rmax[(size_t)C0 * DIM + d] = mx0;
+            rmin[(size_t)C1 * DIM + d] = mn1;
+            rmax[(size_t)C1 * DIM + d] = mx;
+            v0 = vmul(v0, vsub(mx0, mn));
+            v1 = vmul(v1, vsub(mx, mn1));
+        }
+        vol[C0] = v0;
+        vol[C1] = v1;
+    }
+}
+
+/* leaf counts of the subtrees of one level's regions (deepest level first) */
+static __global__ void k_tol_count(const int* __restrict__ lvl, int n, const int* __restrict__ child,
+                                   uint32_t* __restrict__ leaves) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int id = lvl[i], c = child[id];
+    leaves[id] = c < 0 ? 1u : leaves[c] + leaves[c + 1];
+}
+
+/* depth-first offsets (root level first): children inherit the parent's offset, the second after the
+ * first's leaves; a leaf's offset is its depth-first rank */
+static __global__ void k_tol_rank(const int* __restrict__ lvl, int n, const int* __restrict__ child,
+                                  const uint32_t* __restrict__ leaves, uint32_t* __restrict__ first,
+                                  int* __restrict__ order) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int id = lvl[i], c = child[id];
+    const uint32_t o = first[id];
+    if (c < 0) {
+        order[o] = id;
+    } else {
+        first[c] = o;
+        first[c + 1] = o + leaves[c];
+    }
+}
+
+template <int DIM, int SH, int SL, class F>
+int tol_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, float tol,
+               uint64_t max_regions, float* d_bins, uint64_t& nregions, uint64_t& nleaves, uint32_t& launches) {
+    constexpr int S = SH;
+    constexpr int CH = F::CH;
+    constexpr int SD = ipow(S, DIM);
+    /* pool capacity: the caller's, else what 4 GiB of region storage holds */
+    const size_t per_region = (size_t)SD * CH * 4 + 2 * DIM * 4 + 4 + 4 + 4 + 4 + 4 + 4;
+    size_t cap = max_regions ? (size_t)max_regions : ((size_t)4 << 30) / per_region;
+    if (cap > (1u << 24) - 2) cap = (1u << 24) - 2;
+    if (cap < 1) cap = 1;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = align256(o + bytes);
+        return at;
+    };
+    const size_t o_vals = take(cap * SD * CH * 4), o_rmin = take(cap * DIM * 4), o_rmax = take(cap * DIM * 4),
+                 o_vol = take(cap * 4), o_child = take(cap * 4), o_lvl = take(cap * 4), o_leaves = take(cap * 4),
+                 o_first = take(cap * 4), o_order = take(cap * 4), o_ctr = take(64), o_cnt = take(g.nbins * 4),
+                 o_off = take((g.nbins + 1) * 4), o_cur = take(g.nbins * 4);
+    int rc = ensure(ctx, ctx->scratch, o);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->scratch.ptr);
+    float* vals = reinterpret_cast<float*>(base + o_vals);
+    float* rmin = reinterpret_cast<float*>(base + o_rmin);
+    float* rmax = reinterpret_cast<float*>(base + o_rmax);
+    float* vol = reinterpret_cast<float*>(base + o_vol);
+    int* child = reinterpret_cast<int*>(base + o_child);
+    int* lvl = reinterpret_cast<int*>(base + o_lvl);
+    uint32_t* leaves = reinterpret_cast<uint32_t*>(base + o_leaves);
+    uint32_t* first = reinterpret_cast<uint32_t*>(base + o_first);
+    int* order = reinterpret_cast<int*>(base + o_order);
+    uint32_t* ctr = reinterpret_cast<uint32_t*>(base + o_ctr);
+
+    TolCfg tc{};
     for (int d = 0; d < DIM; ++d) {
-        rcfg.rmin[d] = p->range_min[d];
-        rcfg.rmax[d] = p->range_max[d];
+        tc.rmin[d] = p->range_min[d];
+        tc.rmax[d] = p->range_max[d];
     }
-    for (int d = 0; d < p->dimbins; ++d) {
-        rcfg.res[d] = g.res[d];
-        rcfg.drange[d] = g.drange[d];
-    }
-    rcfg.dimbins = p->dimbins;
-    rcfg.nbins = g.nbins;
-    rcfg.factor = (double)g.factor;
-    rcfg.spp = cv.samples_per_bin;
-    rcfg.k0 = (uint32_t)cv.seed;
-    rcfg.k1 = (uint32_t)(cv.seed >> 32);
-    rcfg.weight = cv.weight;
-    rcfg.alpha = cv.alpha;
-    /* reserved == 1 (set only by vcu_adaptive_iterations_global): accumulate into the bins' values */
-    rcfg.approx_init = cv.reserved == 1 ? d_bins : nullptr;
-    const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
-    k_cv_residual<F, DIM, S><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(f, rcfg, off, lists, hp, vals, rmin, rmax,
-                                                                          vol, d_replay, d_bins, d_approx,
-                                                                          ctx->d_status);
+    tc.heuristic = nst.heuristic;
+    tc.relative = nst.metric == VCU_METRIC_RELATIVE;
+    float mv = (float)nst.min_val;
+    if ((double)mv < nst.min_val) mv = nextafterf(mv, INFINITY);
+    tc.min_val_f = mv;
+    tc.tol = tol;
+    tc.size_weight = nst.size_weight;
+    tc.min_size = nst.min_size;
+    tc.capacity = (uint32_t)cap;
+    k_tol_root<F, DIM, SH><<<1, 256, 0, ctx->stream>>>(f, tc, vals, rmin, rmax, vol);
+    const uint32_t init[2] = {1u, 0u};
+    const int zero = 0;
+    VCU_CUDA(ctx, cudaMemcpyAsync(ctr, init, 8, cudaMemcpyHostToDevice, ctx->stream));
+    VCU_CUDA(ctx, cudaMemcpyAsync(lvl, &zero, 4, cudaMemcpyHostToDevice, ctx->stream));
     ++launches;
-    if (d_regions) {
-        k_cv_regions_out<<<(unsigned)((nheap + 255) / 256), 256, 0, ctx->stream>>>(hp, rmin, rmax, DIM, (int)nheap,
-                                                                                  d_regions);
+    /* breadth first: level L's regions are lvl[starts[L] .. starts[L+1]) */
+    std::vector<size_t> starts{0, 1};
+    constexpr int MAX_LEVELS = 256;
+    for (int L = 0;; ++L) {
+        const size_t a = starts[L], n = starts[L + 1] - starts[L];
+        if (L >= MAX_LEVELS) return fail(ctx, VCU_QUEUE_OVERFLOW, "tolerance not reached within 256 levels of subdivision");
+        VCU_CUDA(ctx, cudaMemsetAsync(ctr + 1, 0, 4, ctx->stream));
+        k_tol_level<F, DIM, SH, SL><<<(unsigned)((n + TOL_WARPS - 1) / TOL_WARPS), TOL_WARPS * 32, 0, ctx->stream>>>(
+            f, tc, lvl + a, (int)n, lvl + a + n, ctr, vals, rmin, rmax, vol, child, ctx->d_status);
+        ++launches;
+        VCU_CUDA(ctx, cudaGetLastError());
+        uint32_t host[2];
+        VCU_CUDA(ctx, cudaMemcpyAsync(host, ctr, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        uint32_t flags = 0;
+        VCU_CUDA(ctx, cudaMemcpy(&flags, ctx->d_status, 4, cudaMemcpyDeviceToHost));
+        if (flags & VCU_FLAG_OVERFLOW)
+            return fail(ctx, VCU_QUEUE_OVERFLOW, "tolerance needs more than " + std::to_string(cap) + " regions");
+        if (host[1] == 0) break;
+        starts.push_back(starts.back() + host[1]);
+    }
+    const int levels = (int)starts.size() - 1;
+    nregions = starts.back();
+    /* depth-first ranks of the leaves */
+    for (int L = levels - 1; L >= 0; --L) {
+        const size_t n = starts[L + 1] - starts[L];
+        k_tol_count<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(lvl + starts[L], (int)n, child, leaves);
+        ++launches;
+    }
+    VCU_CUDA(ctx, cudaMemsetAsync(first, 0, 4, ctx->stream));
+    for (int L = 0; L < levels; ++L) {
+        const size_t n = starts[L + 1] - starts[L];
+        k_tol_rank<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(lvl + starts[L], (int)n, child, leaves, first,
+                                                                         order);
         ++launches;
     }
     VCU_CUDA(ctx, cudaGetLastError());
-    return VCU_OK;
+    uint32_t nl = 0;
+    VCU_CUDA(ctx, cudaMemcpyAsync(&nl, leaves, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    nleaves = nl;
+    /* stages 2-3: the leaves into the bins in depth-first order, accumulating */
+    vcu_cv cv{};
+    cv.samples_per_bin = 0;
+    cv.weight = VCU_CV_FIXED;
+    cv.reserved = 1;
+    cv.alpha = 1.0;
+    return regions_into_bins<F, DIM, SH>(ctx, f, p, g, cv, vals, rmin, rmax, vol, order, nl,
+                                         reinterpret_cast<uint32_t*>(base + o_cnt), reinterpret_cast<uint32_t*>(base + o_off),
+                                         reinterpret_cast<uint32_t*>(base + o_cur), nullptr, d_bins, nullptr, nullptr,
+                                         launches);
 }
 
 }  // namespace cv_detail
@@ -928,6 +1297,35 @@ int run_cv_pair(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_
             case 4: return by_dim(std::integral_constant<int, 4>{});
             case 5: return by_dim(std::integral_constant<int, 5>{});
             default: return fail(ctx, VCU_UNSUPPORTED, "half-space control variates are built for 2-5 dimensions");
+            }
+        } else {
+            return by_dim(std::integral_constant<int, F::DIM>{});
+        }
+    });
+}
+
+/* the tolerance-driven form for one rule pair (same dimension limits as the control variates) */
+template <int SH, int SL>
+int run_tol_pair(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, float tol,
+                 uint64_t max_regions, float* d_bins, uint64_t& nregions, uint64_t& nleaves, uint32_t& launches) {
+    using cv_detail::ipow;
+    return with_integrand(ctx, p->f, p->dim, [&](const auto& f) -> int {
+        using F = std::decay_t<decltype(f)>;
+        auto by_dim = [&](auto dimc) -> int {
+            constexpr int DIM = decltype(dimc)::value;
+            if constexpr (ipow(SH, DIM) <= 243)
+                return cv_detail::tol_launch<DIM, SH, SL>(ctx, f, p, g, nst, tol, max_regions, d_bins, nregions, nleaves,
+                                                          launches);
+            else
+                return fail(ctx, VCU_UNSUPPORTED, "tolerance-driven regions are limited to 243 nodes (S^dim)");
+        };
+        if constexpr (F::DIM == 6) {
+            switch (p->dim) {
+            case 2: return by_dim(std::integral_constant<int, 2>{});
+            case 3: return by_dim(std::integral_constant<int, 3>{});
+            case 4: return by_dim(std::integral_constant<int, 4>{});
+            case 5: return by_dim(std::integral_constant<int, 5>{});
+            default: return fail(ctx, VCU_UNSUPPORTED, "half-space regions are built for 2-5 dimensions");
             }
         } else {
             return by_dim(std::integral_constant<int, F::DIM>{});

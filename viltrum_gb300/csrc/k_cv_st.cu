@@ -7,4 +7,8 @@ int run_cv_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_ne
               uint32_t& launches) {
     return run_cv_pair<3, 2>(ctx, p, g, n, iterations, cv, d_replay, d_bins, d_approx, d_regions, launches);
 }
+int run_tol_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, float tol,
+               uint64_t max_regions, float* d_bins, uint64_t& nregions, uint64_t& nleaves, uint32_t& launches) {
+    return run_tol_pair<3, 2>(ctx, p, g, n, tol, max_regions, d_bins, nregions, nleaves, launches);
+}
 }  // namespace vcu

@@ -501,6 +501,50 @@ extern "C" int vcu_adaptive_iterations_global(vcu_ctx* ctx, const vcu_problem* p
     return scope.end((uint64_t)(sd + (double)iterations * (S - 1) * sd1), iterations + 1);
 }
 
+extern "C" int vcu_adaptive_tolerance(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested, float tolerance,
+                                      uint64_t max_regions, float* bins, uint64_t* leaves, vcu_stats* stats) {
+    if (!ctx) return VCU_INVALID_ARG;
+    BinGrid g;
+    int rc = make_grid(ctx, p, g);
+    if (rc) return rc;
+    if (!nested || !bins) return fail(ctx, VCU_INVALID_ARG, "null nested rule or bins");
+    if (!(tolerance > 0.0f)) return fail(ctx, VCU_INVALID_ARG, "tolerance must be positive");
+    if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
+    if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    const int ch = vcu_channels(p->f.kind);
+    if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
+    CallScope scope{ctx, stats};
+    if ((rc = scope.begin())) return rc;
+    const size_t bbytes = g.nbins * ch * 4;
+    float* dbins = bins;
+    if (p->mem == VCU_MEM_HOST) {
+        if ((rc = ensure(ctx, ctx->out, bbytes + 256))) return rc;
+        dbins = static_cast<float*>(ctx->out.ptr);
+        VCU_CUDA(ctx, cudaMemcpyAsync(dbins, bins, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    uint64_t nregions = 0, nleaves = 0;
+    if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_tol_st(ctx, p, g, *nested, tolerance, max_regions, dbins, nregions, nleaves, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_SIMPSON)
+        rc = run_tol_bs(ctx, p, g, *nested, tolerance, max_regions, dbins, nregions, nleaves, scope.launches);
+    else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
+        rc = run_tol_bt(ctx, p, g, *nested, tolerance, max_regions, dbins, nregions, nleaves, scope.launches);
+    else
+        rc = fail(ctx, VCU_INVALID_ARG, "unsupported nested rule pair");
+    if (rc) return rc;
+    if (p->mem == VCU_MEM_HOST)
+        VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (leaves) *leaves = nleaves;
+    const int S = nested->rule_hi;
+    double sd = 1.0, sd1 = 1.0;
+    for (int d = 0; d < p->dim; ++d) sd *= S;
+    for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
+    const uint64_t splits = nregions > 0 ? (nregions - 1) / 2 : 0;
+    return scope.end((uint64_t)(sd + (double)splits * (S - 1) * sd1), nregions);
+}
+
 extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_learned* opt, float* bins,
                                             float* network_integral, vcu_learned_report* report, vcu_stats* stats) {
     if (!ctx) return VCU_INVALID_ARG;

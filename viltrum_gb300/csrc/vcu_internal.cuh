@@ -261,6 +261,12 @@ int run_batch_bt(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_it
 /* (re)capture the batch's queue reset + launch as a graph and launch it; launch it again */
 int batch_capture(vcu_ctx* ctx, uint32_t& launches);
 int batch_launch(vcu_ctx* ctx, uint32_t& launches);
+int run_tol_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, float tol,
+               uint64_t max_regions, float* d_bins, uint64_t& nregions, uint64_t& nleaves, uint32_t& launches);
+int run_tol_bs(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, float tol,
+               uint64_t max_regions, float* d_bins, uint64_t& nregions, uint64_t& nleaves, uint32_t& launches);
+int run_tol_bt(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, float tol,
+               uint64_t max_regions, float* d_bins, uint64_t& nregions, uint64_t& nleaves, uint32_t& launches);
 int run_cv_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
               const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
               uint32_t& launches);
