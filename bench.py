@@ -275,10 +275,17 @@ def other_configs(ctx, args) -> dict:
     b = np.empty(1024, np.float32)
     ms, st = _median_ms(lambda: ctx.per_bin_monte_carlo(p, 1024, 1, b))
     exact = scenes.exact_bins(scenes.WAVE2, None, [0, 0], [1, 1], [1024])
+    from oracle import oracle as orc
+    port = orc.port()
+    t0 = time.perf_counter()
+    port.per_bin_monte_carlo(scenes.WAVE2, None, [0, 0], [1, 1], [1024], 1024, 1)
+    cpu_s = time.perf_counter() - t0
     out["per_bin_monte_carlo"] = {
         "workload": "wave2 sin(8x)e^-y+x^2+y^2 on [0,1]^2, 1024 bins along x, 1024 Philox samples per bin",
         "ms": round(ms, 4), "gsamples_s": round(st.evaluations / (ms * 1e6), 3),
-        "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact), "timing": "median of 5 after 3 warm-up, device"}
+        "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact), "timing": "median of 5 after 3 warm-up, device",
+        "cpu_baseline": {"ms": round(cpu_s * 1e3, 2), "gsamples_s": round(1024 * 1024 / cpu_s / 1e9, 4), "cores": 1,
+                         "kind": "port", "sample": "the whole workload (the reference's per-bin mt19937 path)"}}
     # -- control variates + residual Monte Carlo, 3 channels, 512x512 bins, 2^14 regions, 64 spp
     params = scenes.moving_scene3(SEED)
     res = [512, 512]
@@ -295,12 +302,19 @@ def other_configs(ctx, args) -> dict:
         ex = scenes.exact_bins(scenes.MOVING_SCENE3, params, [0, y0, 0], [1, y1, 1], [512, 1]) * 512.0
         err.append(b.reshape(512, 512, 3)[r] - ex)
     err = np.concatenate(err)
+    t0 = time.perf_counter()
+    port.control_variates(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], [128, 128],
+                          orc.Nested.make("simpson", "trapezoidal", "size", "relative"), (1 << 14) - 1, 64, 3)
+    cv_cpu_s = time.perf_counter() - t0
     out["control_variates"] = {
         "workload": "integrator_crespo2021(2^14-1 splits, 64 residual samples): moving-disk scene, RGB, "
                     "x,y binned 512x512, t in [0,1]",
         "ms": round(ms, 3), "gsamples_s": round(st.evaluations / (ms * 1e6), 3), "regions": int(st.regions),
         "rmse_vs_fp64": float(np.sqrt(np.mean(err.astype(np.float64) ** 2))),
-        "rmse_sample": f"{len(rows)} of 512 rows of bins", "timing": "median of 3 after 3 warm-up, device"}
+        "rmse_sample": f"{len(rows)} of 512 rows of bins", "timing": "median of 3 after 3 warm-up, device",
+        "cpu_baseline": {"ms_128x128": round(cv_cpu_s * 1e3, 1), "cores": 1, "kind": "port",
+                         "sample": "the same regions (2^14-1 splits) and 64 samples/bin over 128x128 bins (1/16 of "
+                                   "the bins; the residual part scales with the bins)"}}
     # -- batch of 4096 independent integrals (dims 2-6, budgets 256..65536, MC or nested)
     items = scenes.batch_items(4096, seed=11)
     prep = _lib.batch_items(items)
@@ -313,6 +327,29 @@ def other_configs(ctx, args) -> dict:
     for _ in range(2):
         ctx.integrate_batch(scenes.HALFSPACE, prep, st_nested, results=r)
     e2e_ms = (time.perf_counter() - t0) / 2 * 1e3
+    # the reference's per-item CPU path on all host threads over 64 random items of the batch (items of
+    # at most 3 M evaluations, so that the sample stays within seconds)
+    import concurrent.futures as cf
+    import random
+
+    def evals_of(it):
+        return it["budget"] if it["method"] == 0 else 3 ** it["dim"] + (it["budget"] - 1) * 2 * 3 ** (it["dim"] - 1)
+
+    small = [i for i, it in enumerate(items) if evals_of(it) <= 3_000_000]
+    pick = random.Random(1).sample(small, 64)
+    nst_o = orc.Nested.make("simpson", "trapezoidal")
+
+    def one(i):
+        it = items[i]
+        port.integrate_single(scenes.HALFSPACE, it["params"], it["rmin"], it["rmax"], it["method"], it["budget"],
+                              it["seed"], nst_o)
+        return evals_of(it)
+
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        cpu_evals = sum(ex.map(one, pick))
+    batch_cpu_s = time.perf_counter() - t0
     out["batch"] = {
         "workload": "4096 independent integrals over [0,1]^d, d uniform in 2..6, prod_d exp(-a x)cos(b x) times a "
                     "random half-space indicator, budget log-uniform 256..65536 (MC samples or nested(simpson,"
@@ -324,7 +361,10 @@ def other_configs(ctx, args) -> dict:
         "threads": runs[-1][1].threads, "blocks": runs[-1][1].blocks,
         "e2e_ms": round(e2e_ms, 2),
         "timing": "resident: median of 3 graph launches (device); e2e: host items -> results through "
-                  "vcu_integrate_batch, wall clock"}
+                  "vcu_integrate_batch, wall clock",
+        "cpu_baseline": {"gsamples_s": round(cpu_evals / batch_cpu_s / 1e9, 4), "cores": threads, "kind": "port",
+                         "sample": f"64 random items of at most 3 M evaluations ({cpu_evals} evaluations) in "
+                                   f"{batch_cpu_s:.1f} s"}}
     out["learned_vs_plain"] = time_to_rmse(ctx)
     return out
 
