@@ -59,6 +59,9 @@ enum { VCU_HEUR_DEFAULT = 0, VCU_HEUR_SIZE = 1 };
 enum { VCU_METRIC_ABSOLUTE = 0, VCU_METRIC_RELATIVE = 1 };
 /* control-variate weights (src/control-variates/weight-strategy.h) */
 enum { VCU_CV_OPTIMIZE = 0, VCU_CV_FIXED = 1 };
+/* residual region choice (src/control-variates/region-russian-roulette.h): rr_uniform_region,
+ * rr_integral_region, rr_error_region (NormDefault) */
+enum { VCU_RR_UNIFORM = 0, VCU_RR_INTEGRAL = 1, VCU_RR_ERROR = 2 };
 
 typedef struct vcu_ctx vcu_ctx;
 
@@ -144,14 +147,17 @@ int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_ne
 
 /* ------------------------------------------------------------------ control variates
  * Replaces integrator_region_based(regions_generator_adaptive_heap(nested(H,L), heuristic, iterations),
- * regions_integrator_parallel_variance_reduction(rr_uniform_region(), cv_optimize_weight() or
- * cv_fixed_weight(alpha), region_sampling_uniform(), std::mt19937(seed), samples))
+ * regions_integrator_parallel_variance_reduction(rr, cv_optimize_weight() or cv_fixed_weight(alpha),
+ * region_sampling_uniform(), std::mt19937(seed), samples)) with rr one of rr_uniform_region(),
+ * rr_integral_region(), rr_error_region() (region-russian-roulette.h:9-108)
  * (src/control-variates/regions-integrator-parallel-variance-reduction.h:32-109,
  * src/control-variates/integrator-crespo2021.h:7-22 for nested(simpson,trapezoidal) with
  * error_heuristic_size(error_metric_relative(), 1e-5)): one max-error heap of regions over the whole
  * range (iterations splits), per-bin lists of the regions overlapping each bin, the polynomial
  * integral over bin n region as control variate, and `samples` residual samples per bin
- * (region chosen uniformly, point uniform in bin n region).  The result is ASSIGNED to the bins.
+ * (region chosen uniformly, or with probability proportional to |integral over bin n region| or to
+ * |region error| x its share of volume in the bin, floored at 1% of the mean weight; point uniform
+ * in bin n region).  The result is ASSIGNED to the bins.
  * Residual sample j of bin b draws from Philox4x32-10 unless `replay` is given: nbins x samples x
  * (1 + dim) floats (index of the chosen region in the bin's list, then the point), e.g. the
  * reference's own draws.  approximation (nullable) receives the control-variate integral per bin,
@@ -161,8 +167,10 @@ typedef struct vcu_cv {
     uint64_t samples_per_bin; /* residual samples per bin (spp)                         */
     uint64_t seed;            /* Philox key                                             */
     int32_t weight;           /* VCU_CV_OPTIMIZE or VCU_CV_FIXED                        */
-    int32_t reserved;
+    int32_t reserved;         /* 0                                                      */
     double alpha;             /* cv_fixed_weight's alpha                                */
+    int32_t rr;               /* VCU_RR_UNIFORM, VCU_RR_INTEGRAL or VCU_RR_ERROR        */
+    int32_t reserved2;        /* 0                                                      */
 } vcu_cv;
 
 int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,

@@ -350,11 +350,15 @@ class control_variates {
     std::uint64_t seed_;
     int weight_;
     double alpha_;
+    int rr_;
 
 public:
+    /* rr: VCU_RR_UNIFORM (rr_uniform_region), VCU_RR_INTEGRAL (rr_integral_region) or VCU_RR_ERROR
+     * (rr_error_region), src/control-variates/region-russian-roulette.h:9-110 */
     control_variates(nested_rule r, unsigned long iterations, unsigned long samples, std::uint64_t seed,
-                     int weight = VCU_CV_OPTIMIZE, double alpha = 1.0)
-        : rule_(r), iterations_(iterations), samples_(samples), seed_(seed), weight_(weight), alpha_(alpha) {}
+                     int weight = VCU_CV_OPTIMIZE, double alpha = 1.0, int rr = VCU_RR_UNIFORM)
+        : rule_(r), iterations_(iterations), samples_(samples), seed_(seed), weight_(weight), alpha_(alpha),
+          rr_(rr) {}
 
     template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
     void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
@@ -370,6 +374,7 @@ public:
         cv.seed = seed_;
         cv.weight = weight_;
         cv.alpha = alpha_;
+        cv.rr = rr_;
         vcu_stats st{};
         ctx.check(vcu_control_variates(ctx.get(), &p, &rule_.n, iterations_, &cv, nullptr, out.data(), nullptr,
                                        nullptr, &st));

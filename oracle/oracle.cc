@@ -22,9 +22,10 @@
  *     src/monte-carlo/monte-carlo-per-bin-parallel.h:40-71,
  *     src/newton-cotes/regions-integrator-sequential.h:37-58, pixels_in_region region.h:454-463;
  *   - control variates: src/control-variates/regions-integrator-parallel-variance-reduction.h:32-109,
- *     weight-strategy.h:7-110, region-russian-roulette.h:9-28, region-sampling.h:9-20.
+ *     weight-strategy.h:7-110, region-russian-roulette.h:9-108, region-sampling.h:9-20.
  * Random numbers come from libstdc++ (std::mt19937, uniform_real_distribution<float>,
- * uniform_int_distribution<size_t>) exactly as the reference draws them.
+ * uniform_int_distribution<size_t>, discrete_distribution<size_t>) exactly as the reference
+ * draws them.
  */
 #include "oracle.h"
 
@@ -300,6 +301,19 @@ template <class H, class L, int DIM, class T> struct Region {
         std::vector<float> e = fold<S, float>(data, DIM, dim, line_err);
         const float folded = fold_all<S>(e, DIM - 1, [&](const float* v) -> float { return h.rule(v); });
         return range.volume() * folded;
+    }
+    /* the whole region's error estimate, volume * (fold_all(H) - fold_all(low)) (region.h:422-426,
+     * nested.h:17-24) */
+    T error_total() const {
+        H h;
+        L l;
+        const T hi = fold_all<S>(data, DIM, [&](const T* v) -> T { return h.rule(v); });
+        const T lo = fold_all<S>(data, DIM, [&](const T* v) -> T {
+            T plow[L::S];
+            for (int i = 0; i < L::S; ++i) plow[i] = v[i * (H::S - 1) / (L::S - 1)];
+            return l.rule(plow);
+        });
+        return range.volume() * (hi - lo);
     }
     /* integral over [a,b] (absolute coordinates), region.h:141-169 */
     T integral_subrange(const Range<DIM>& r) const {
@@ -746,8 +760,8 @@ template <class T> struct CvFixed {
 
 template <class H, class L, int DIM, class T, class Fun, class M>
 void control_variates(const Fun& fun, const Problem& p, const orc_nested& nc, const M& metric, uint64_t iters,
-                      uint64_t spp, uint64_t seed, int weight, double alpha, float* out, float* approx_out,
-                      float* regions_out, float* replay_out) {
+                      uint64_t spp, uint64_t seed, int weight, double alpha, int rr_mode, float* out,
+                      float* approx_out, float* regions_out, float* replay_out) {
     using R = Region<H, L, DIM, T>;
     const auto range = make_range<DIM>(p);
     Fn<Fun, DIM, T> f{&fun};
@@ -812,11 +826,39 @@ void control_variates(const Fun& fun, const Problem& p, const orc_nested& nc, co
         }
         if (approx_out) VT<T>::to(approximation, approx_out + b * VT<T>::CH);
         float* rep = replay_out ? replay_out + b * spp * (1 + DIM) : nullptr;
+        /* region choice: uniform (region-russian-roulette.h:9-28), or proportional to the norm of
+         * the control variate's integral over bin n region (:30-68) or of the region's error scaled
+         * by the share of its volume in the bin (:70-108), with a floor of 1% of the mean weight */
+        std::uniform_int_distribution<std::size_t> uniform(0, list.size() - 1);
+        std::discrete_distribution<std::size_t> weighted;
+        if (rr_mode != ORC_RR_UNIFORM) {
+            std::vector<double> w(list.size());
+            for (std::size_t i = 0; i < list.size(); ++i) {
+                if (rr_mode == ORC_RR_INTEGRAL) w[i] = norm_default(list[i]->integral_subrange(rr[i]));
+                else w[i] = norm_default(list[i]->error_total()) * rr[i].volume() / list[i]->range.volume();
+            }
+            double sum = 0.0;
+            for (double v : w) sum += v;
+            if (sum <= 0.0)
+                for (double& v : w) v = 1.0;
+            else
+                for (double& v : w) v = std::max(v, 0.01 * sum / double(w.size()));
+            weighted = std::discrete_distribution<std::size_t>(w.begin(), w.end());
+        }
+        auto choose = [&](std::size_t& chosen, double& rrfactor) {
+            if (rr_mode == ORC_RR_UNIFORM) {
+                chosen = uniform(rng);
+                rrfactor = double(uniform.max() + 1);
+            } else {
+                chosen = weighted(rng);
+                rrfactor = 1.0 / weighted.probabilities()[chosen];
+            }
+        };
         auto body = [&](auto& acc) {
-            std::uniform_int_distribution<std::size_t> roulette(0, list.size() - 1);
             for (uint64_t s = 0; s < spp; ++s) {
-                const std::size_t chosen = roulette(rng);
-                const std::size_t rrfactor = roulette.max() + 1;
+                std::size_t chosen;
+                double rrfactor;
+                choose(chosen, rrfactor);
                 const R* r = list[chosen];
                 const Range<DIM>& rbr = rr[chosen];
                 std::array<float, DIM> x;
@@ -1009,15 +1051,17 @@ extern "C" int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* pa
 extern "C" int orc_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
                                     const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
                                     const orc_nested* nested, uint64_t iterations, uint64_t spp, uint64_t seed,
-                                    int32_t weight, double alpha, float* out, float* approx_out, float* regions_out,
-                                    float* replay_out) {
+                                    int32_t weight, double alpha, int32_t rr, float* out, float* approx_out,
+                                    float* regions_out, float* replay_out) {
     if (!valid_problem(dim, dimbins, res) || !nested) return 1;
+    if (rr != ORC_RR_UNIFORM && rr != ORC_RR_INTEGRAL && rr != ORC_RR_ERROR) return 1;
     Problem p{dim, dimbins, rmin, rmax, res};
     return with_integrand(kind, params, n_params, dim, [&](const auto& f, auto D, auto t) -> int {
         return with_rules(*nested, [&](auto h, auto l) -> int {
             return with_metric(*nested, [&](auto m) -> int {
                 control_variates<decltype(h), decltype(l), decltype(D)::value, decltype(t)>(
-                    f, p, *nested, m, iterations, spp, seed, weight, alpha, out, approx_out, regions_out, replay_out);
+                    f, p, *nested, m, iterations, spp, seed, weight, alpha, rr, out, approx_out, regions_out,
+                    replay_out);
                 return 0;
             });
         });

@@ -31,6 +31,9 @@ enum { ORC_HEUR_DEFAULT = 0, ORC_HEUR_SIZE = 1 };
 enum { ORC_METRIC_ABSOLUTE = 0, ORC_METRIC_RELATIVE = 1 };
 /* control-variate weight strategies (src/control-variates/weight-strategy.h) */
 enum { ORC_CV_OPTIMIZE = 0, ORC_CV_FIXED = 1 };
+/* residual region choice (src/control-variates/region-russian-roulette.h): rr_uniform_region,
+ * rr_integral_region, rr_error_region */
+enum { ORC_RR_UNIFORM = 0, ORC_RR_INTEGRAL = 1, ORC_RR_ERROR = 2 };
 /* Monte Carlo flavours */
 enum {
     ORC_MC_PER_BIN_PARALLEL = 0, /* integrator_per_bin_parallel(monte_carlo(spp, seed))    */
@@ -65,16 +68,18 @@ int orc_per_bin_adaptive_nested(int32_t kind, const float* params, int32_t n_par
                                 uint64_t iterations, float* out, int32_t* trace);
 
 /* integrator_region_based(regions_generator_adaptive_heap(nested, heuristic, iters),
- *   regions_integrator_parallel_variance_reduction(rr_uniform_region(), cv, region_sampling_uniform(),
- *   std::mt19937(seed), spp))  -- crespo2021 when nested = (simpson, trapezoidal, size, relative).
+ *   regions_integrator_parallel_variance_reduction(rr, cv, region_sampling_uniform(),
+ *   std::mt19937(seed), spp))  -- crespo2021 when nested = (simpson, trapezoidal, size, relative) and
+ *   rr = ORC_RR_UNIFORM (rr_uniform_region(); ORC_RR_INTEGRAL / ORC_RR_ERROR: rr_integral_region() /
+ *   rr_error_region() with NormDefault).
  * approx_out (nullable): per-bin control-variate integral (the "approximation").
  * regions_out (nullable): (iters+1) x (2*dim) float ranges in heap order.
  * replay_out (nullable): per bin, spp x (chosen list index, dim coordinates) as floats.      */
 int orc_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
                          const float* rmin, const float* rmax, int32_t dimbins,
                          const uint64_t* res, const orc_nested* nested, uint64_t iterations,
-                         uint64_t spp, uint64_t seed, int32_t weight, double alpha, float* out,
-                         float* approx_out, float* regions_out, float* replay_out);
+                         uint64_t spp, uint64_t seed, int32_t weight, double alpha, int32_t rr,
+                         float* out, float* approx_out, float* regions_out, float* replay_out);
 
 /* Same per-bin Monte Carlo arithmetic over a contiguous slice of bins [bin_begin, bin_end),
  * on nthreads host threads (bins are independent once their seeds are drawn in bin order, as

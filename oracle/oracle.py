@@ -23,6 +23,7 @@ RULE = {"trapezoidal": 2, "simpson": 3, "boole": 5}
 HEUR = {"default": 0, "size": 1}
 METRIC = {"absolute": 0, "relative": 1}
 CV_OPTIMIZE, CV_FIXED = 0, 1
+RR_UNIFORM, RR_INTEGRAL, RR_ERROR = 0, 1, 2  # rr_uniform_region, rr_integral_region, rr_error_region
 MC_PER_BIN_PARALLEL, MC_PER_BIN_PARALLEL_SINGLE = 0, 1
 
 _f32p = ctypes.POINTER(ctypes.c_float)
@@ -104,7 +105,7 @@ class Oracle:
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
                       ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32,
-                      ctypes.c_double, _f32p, _f32p, _f32p, _f32p]
+                      ctypes.c_double, ctypes.c_int32, _f32p, _f32p, _f32p, _f32p]
 
     # ------------------------------------------------------------------ helpers
     @staticmethod
@@ -208,7 +209,7 @@ class Oracle:
         return float(out[0])
 
     def control_variates(self, kind, params, rmin, rmax, res, nested: Nested, iterations, spp, seed,
-                         weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False):
+                         weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False, rr=RR_UNIFORM):
         params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
         nb = int(np.prod(res))
         ch = self.channels(kind)
@@ -220,7 +221,7 @@ class Oracle:
         rp = np.zeros(nb * spp * width, dtype=np.float32) if replay else None
         rc = getattr(self.lib, self.prefix + "control_variates")(
             kind, _ptr(params), params.size, dim, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
-            ctypes.byref(nested), iterations, spp, seed, weight, alpha, _ptr(out), _ptr(ap), _ptr(rg), _ptr(rp))
+            ctypes.byref(nested), iterations, spp, seed, weight, alpha, rr, _ptr(out), _ptr(ap), _ptr(rg), _ptr(rp))
         self._check(rc, "control_variates")
         return {
             "bins": out.reshape(nb, ch),

@@ -38,7 +38,9 @@ int main() {
     const auto scene = vc::builtin_integrand::scene2(scene_params());
     const auto wave = vc::builtin_integrand::wave2();
     std::vector<std::vector<float>> image(16, std::vector<float>(16, 0.0f));
-    std::vector<float> row(64, 0.0f), cv_bins(64, 0.0f), learned(16, 0.0f), global(32, 0.5f);
+    std::vector<float> row(64, 0.0f), cv_bins(64, 0.0f), learned(16, 0.0f), global(32, 0.5f), cv_err(64, 0.0f);
+    /* rr_error_region with cv_fixed_weight(0.5) */
+    const auto cv_error = vc::control_variates(vc::crespo2021_rule(), 255, 16, 4, VCU_CV_FIXED, 0.5, VCU_RR_ERROR);
 #ifdef WITH_VILTRUM
     viltrum::integrate(vc::per_bin_adaptive_nested(vc::boole_simpson(), 15), image, scene, viltrum::range_primary<2>());
     viltrum::integrate(vc::per_bin_monte_carlo(256, 7), row, wave, viltrum::range_primary<2>());
@@ -47,6 +49,7 @@ int main() {
     viltrum::integrate(vc::learned_control_variates(16, 5, 50), learned, wave, viltrum::range_primary<2>());
     viltrum::integrate(vc::adaptive_iterations(vc::simpson_trapezoidal(), 127), global, scene, viltrum::range_primary<2>());
     viltrum::integrate(vc::adaptive_tolerance(vc::boole_simpson(), 1e-6f), global, scene, viltrum::range_primary<2>());
+    viltrum::integrate(cv_error, cv_err, scene, viltrum::range_primary<2>());
 #else
     quiet log;
     const box<2> unit{{0.0f, 0.0f}, {1.0f, 1.0f}};
@@ -62,6 +65,8 @@ int main() {
     auto g1 = [&](const std::array<std::size_t, 1>& p) -> float& { return global[p[0]]; };
     vc::adaptive_iterations(vc::simpson_trapezoidal(), 127).integrate(g1, std::array<std::size_t, 1>{32}, scene, unit, log);
     vc::adaptive_tolerance(vc::boole_simpson(), 1e-6f).integrate(g1, std::array<std::size_t, 1>{32}, scene, unit, log);
+    auto e1 = [&](const std::array<std::size_t, 1>& p) -> float& { return cv_err[p[0]]; };
+    cv_error.integrate(e1, std::array<std::size_t, 1>{64}, scene, unit, log);
 #endif
     /* independent integrals: two half-space items, one nested and one Monte Carlo */
     std::vector<vc::batch_item> items(2);
@@ -81,5 +86,6 @@ int main() {
     for (float v : learned) std::printf("%.9g\n", v);
     for (float v : global) std::printf("%.9g\n", v);
     for (float v : batch) std::printf("%.9g\n", v);
+    for (float v : cv_err) std::printf("%.9g\n", v);
     return 0;
 }

@@ -81,6 +81,27 @@ CASES = [
     ("cv_poly2_crespo_bins1_it16_spp64_seed0", "cv", dict(kind=scenes.POLY2, params=None, rmin=[0, 0], rmax=[1, 1],
                                                          res=[1], iterations=16, spp=64, seed=0, weight=0,
                                                          alpha=1.0)),
+    # residual region choice by importance: rr_integral_region / rr_error_region (rr = 1 / 2)
+    ("cv_scene2_rrintegral_bins16x16_it127_spp8_seed9", "cv", dict(kind=scenes.SCENE2, params=SCENE_SMALL,
+                                                                  rmin=[0, 0], rmax=[1, 1], res=[16, 16],
+                                                                  iterations=127, spp=8, seed=9, weight=0, alpha=1.0,
+                                                                  rr=1)),
+    ("cv_scene2_rrintegral_fixed0_bins8x8_it63_spp8_seed10", "cv", dict(kind=scenes.SCENE2, params=SCENE_SMALL,
+                                                                       rmin=[0, 0], rmax=[1, 1], res=[8, 8],
+                                                                       iterations=63, spp=8, seed=10, weight=1,
+                                                                       alpha=0.0, rr=1)),
+    ("cv_scene2_rrerror_bins16x16_it127_spp8_seed11", "cv", dict(kind=scenes.SCENE2, params=SCENE_SMALL,
+                                                                rmin=[0, 0], rmax=[1, 1], res=[16, 16],
+                                                                iterations=127, spp=8, seed=11, weight=0, alpha=1.0,
+                                                                rr=2)),
+    ("cv_moving3_rgb_rrerror_bins16x16_it255_spp16_seed12", "cv", dict(kind=scenes.MOVING_SCENE3,
+                                                                      params=MOVING_SMALL, rmin=[0, 0, 0],
+                                                                      rmax=[1, 1, 1], res=[16, 16], iterations=255,
+                                                                      spp=16, seed=12, weight=0, alpha=1.0, rr=2)),
+    ("cv_moving3_rgb_rrintegral_bins8x8_it127_spp16_seed13", "cv", dict(kind=scenes.MOVING_SCENE3,
+                                                                       params=MOVING_SMALL, rmin=[0, 0, 0],
+                                                                       rmax=[1, 1, 1], res=[8, 8], iterations=127,
+                                                                       spp=16, seed=13, weight=0, alpha=1.0, rr=1)),
 ]
 
 CRESPO = ("simpson", "trapezoidal", "size", "relative")
@@ -192,7 +213,7 @@ def run(lib: orc.Oracle, method: str, kw: dict) -> dict:
         nested = orc.Nested.make(*CRESPO)
         r = lib.control_variates(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"], nested,
                                  kw["iterations"], kw["spp"], kw["seed"], kw["weight"], kw["alpha"], regions=True,
-                                 replay=True)
+                                 replay=True, rr=kw.get("rr", 0))
         pts = r["replay"]
         if lib.kind == "port":
             pts = pts[:, :, 1:]

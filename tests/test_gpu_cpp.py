@@ -23,8 +23,8 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
                     "-lviltrum_cuda", "-Wl,-rpath," + os.path.join(ROOT, "viltrum_gb300"), "-o", exe], check=True)
     out = np.array([float(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()],
                    np.float32)
-    assert out.size == 256 + 64 + 64 + 16 + 32 + 2
-    img, row, cvb, lrn, glb, bat = np.split(out, [256, 320, 384, 400, 432])
+    assert out.size == 256 + 64 + 64 + 16 + 32 + 2 + 64
+    img, row, cvb, lrn, glb, bat, cve = np.split(out, [256, 320, 384, 400, 432, 434])
     scene = np.array([2, 1, 0.3, 0.4, 0.05, 0.8, 0.7, 0.6, 0.1, 0.5, 0.5, 0.5, 0.2, 0.25], np.float32)
     # per-bin adaptive nested, 16x16 (image[y][x] flattened = dim-0-fastest bins)
     ref = np.empty(256, np.float32)
@@ -43,6 +43,10 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
     ctx.control_variates(ctx.problem(scenes.SCENE2, scene, [0, 0], [1, 1], [64]),
                          _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37), 255, _lib.CvOpts(16, 3, 0, 0, 1.0), c)
     assert np.array_equal(cvb.view(np.uint32), c.view(np.uint32))
+    # rr_error_region with cv_fixed_weight(0.5), seed 4
+    ctx.control_variates(ctx.problem(scenes.SCENE2, scene, [0, 0], [1, 1], [64]),
+                         _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37), 255, _lib.CvOpts(16, 4, 1, 0, 0.5, 2), c)
+    assert np.array_equal(cve.view(np.uint32), c.view(np.uint32))
     # learned control variate (16 samples, seed 5, 50 steps, defaults of the header)
     l = np.empty(16, np.float32)
     ctx.learned_control_variates(ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [16]),

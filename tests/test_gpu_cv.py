@@ -9,6 +9,9 @@ reference.
   bins within 1e-5 of the scale of the combined terms (the reference sums its samples in float).
 * With Philox draws the estimator's error against the FP64 bin integrals matches the reference
   estimator's at equal samples (mean squared error ratio in [0.7, 1.4] over seeds).
+* The importance choices of the residual's region (rr_integral_region, rr_error_region) pass the
+  same three checks; their choice probabilities are summed warp-parallel in FP64 rather than in the
+  reference's sequential order, far below the 1e-5 tolerance.
 """
 import numpy as np
 import pytest
@@ -22,7 +25,8 @@ pytestmark = pytest.mark.gpu
 CRESPO = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
 
 
-def _gpu_cv(ctx, kind, params, rmin, rmax, res, iters, spp, seed, weight=0, alpha=1.0, replay=None, nested=CRESPO):
+def _gpu_cv(ctx, kind, params, rmin, rmax, res, iters, spp, seed, weight=0, alpha=1.0, replay=None, nested=CRESPO,
+            rr=0):
     p = ctx.problem(kind, params, rmin, rmax, res)
     nb = int(np.prod(res))
     ch = 3 if kind == scenes.MOVING_SCENE3 else 1
@@ -31,7 +35,7 @@ def _gpu_cv(ctx, kind, params, rmin, rmax, res, iters, spp, seed, weight=0, alph
     app = np.empty(nb * ch, np.float32)
     reg = np.empty((iters + 1) * 2 * dim, np.float32)
     rp = None if replay is None else np.ascontiguousarray(replay, np.float32)
-    st = ctx.control_variates(p, nested, iters, _lib.CvOpts(spp, seed, weight, 0, alpha), out, app, reg, rp)
+    st = ctx.control_variates(p, nested, iters, _lib.CvOpts(spp, seed, weight, 0, alpha, rr), out, app, reg, rp)
     return out.reshape(nb, ch), app.reshape(nb, ch), reg.reshape(iters + 1, 2, dim), st
 
 
@@ -40,13 +44,14 @@ def test_cv_matches_reference_golden(ctx, port, name):
     g = load_golden(name)
     kind, res, iters, spp, seed = int(g["kind"]), [int(r) for r in g["res"]], int(g["iterations"]), int(g["spp"]), \
         int(g["seed"])
-    weight, alpha = int(g["weight"]), float(g["alpha"])
+    weight, alpha, rr = int(g["weight"]), float(g["alpha"]), int(g.get("rr", 0))
     params = g.get("params")
     ref = port.control_variates(kind, params, g["rmin"], g["rmax"], res,
                                 orc.Nested.make("simpson", "trapezoidal", "size", "relative"), iters, spp, seed,
-                                weight, alpha, replay=True, approx=True)
+                                weight, alpha, replay=True, approx=True, rr=rr)
+    assert np.array_equal(ref["bins"].reshape(-1).view(np.uint32), g["out_bins"].reshape(-1).view(np.uint32))
     out, app, reg, st = _gpu_cv(ctx, kind, params, g["rmin"], g["rmax"], res, iters, spp, seed, weight, alpha,
-                                replay=ref["replay"])
+                                replay=ref["replay"], rr=rr)
     # 1. the same regions, in the same heap order
     assert np.array_equal(reg.view(np.uint32), g["out_regions"].view(np.uint32))
     # 2. the control-variate integral
@@ -104,3 +109,62 @@ def test_python_crespo2021_api(ctx):
                 ctx=ctx)
     out, _, _, _ = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], [16, 16], 255, 16, 3)
     assert np.array_equal(bins.transpose(1, 0, 2).reshape(-1, 3), out)
+
+
+@pytest.mark.parametrize("rr", [orc.RR_INTEGRAL, orc.RR_ERROR])
+def test_cv_importance_many_regions_per_bin(ctx, port, rr):
+    """Bins holding hundreds of regions (the choice tables span many warp-wide chunks), replaying
+    the oracle's draws: the same bins within 1e-5 of the scale of the combined terms."""
+    params = scenes.scene2(7, n_gauss=16, n_disk=8)
+    res, iters, spp = [2, 2], 2047, 96
+    nst = orc.Nested.make("simpson", "trapezoidal", "size", "relative")
+    ref = port.control_variates(scenes.SCENE2, params, [0, 0], [1, 1], res, nst, iters, spp, 5, replay=True,
+                                approx=True, rr=rr)
+    assert ref["replay"][:, :, 0].max() > 300  # region indices deep into the lists
+    out, app, _, st = _gpu_cv(ctx, scenes.SCENE2, params, [0, 0], [1, 1], res, iters, spp, 5, replay=ref["replay"],
+                              rr=rr)
+    ra = ref["approximation"].astype(np.float64)
+    rb = ref["bins"].astype(np.float64)
+    scale = np.abs(rb) + np.abs(ra) + 1e-3 * np.max(np.abs(ra))
+    assert np.all(np.abs(out - rb) <= 1e-5 * scale), np.max(np.abs(out - rb) / scale)
+    assert st.flags == 0
+
+
+@pytest.mark.parametrize("rr", [orc.RR_INTEGRAL, orc.RR_ERROR])
+def test_cv_importance_statistics_against_fp64(ctx, port, rr):
+    """Philox importance choice: mean squared error against the FP64 bin integrals comparable to the
+    reference estimator's (std::mt19937 draws) over four seeds, for the optimised weight and for
+    alpha = 0 (plain Monte Carlo whose points are importance-sampled among the regions)."""
+    params = scenes.moving_scene3(7, n_gauss=16, n_disk=16)
+    res, iters, spp = [32, 32], 511, 16
+    exact = scenes.exact_bins(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, t_nodes=96)
+    nst = orc.Nested.make("simpson", "trapezoidal", "size", "relative")
+    for weight, alpha in ((0, 1.0), (1, 0.0)):
+        gpu_sq, ref_sq = [], []
+        for seed in (1, 2, 3, 4):
+            out, _, _, st = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, iters, spp, seed,
+                                    weight, alpha, rr=rr)
+            assert st.flags == 0
+            gpu_sq.append(np.mean((out - exact) ** 2))
+            ref = port.control_variates(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, nst, iters, spp,
+                                        seed, weight, alpha, rr=rr)
+            ref_sq.append(np.mean((ref["bins"] - exact) ** 2))
+        ratio = np.mean(gpu_sq) / np.mean(ref_sq)
+        assert 0.7 <= ratio <= 1.4, (weight, gpu_sq, ref_sq)
+
+
+def test_cv_importance_python_api_and_bad_choice(ctx):
+    params = scenes.scene2(7, n_gauss=8, n_disk=4)
+    bins = np.zeros((8, 8), np.float32)
+    integ = v.integrator_adaptive_variance_reduction_parallel(
+        v.nested(v.simpson, v.trapezoidal), v.error_heuristic_size(v.error_metric_relative(), 1e-5), 127,
+        v.rr_error_region(), v.cv_optimize_weight(), 16, 9)
+    v.integrate(integ, bins, v.Integrand.scene2(params), v.range_primary(2), ctx=ctx)
+    out, _, _, _ = _gpu_cv(ctx, scenes.SCENE2, params, [0, 0], [1, 1], [8, 8], 127, 16, 9, rr=orc.RR_ERROR)
+    assert np.array_equal(bins.T.reshape(-1), out[:, 0])
+    p = ctx.problem(scenes.SCENE2, params, [0, 0], [1, 1], [8, 8])
+    o = np.empty(64, np.float32)
+    for bad in (_lib.CvOpts(4, 1, 0, 0, 1.0, 3), _lib.CvOpts(4, 1, 0, 0, 1.0, 1, 1)):
+        with pytest.raises(_lib.VcuError) as e:
+            ctx.control_variates(p, CRESPO, 15, bad, o)
+        assert e.value.code == 1

@@ -33,7 +33,7 @@ def test_oracle_matches_reference_golden(port, name):
         r = port.control_variates(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"],
                                   orc.Nested.make("simpson", "trapezoidal", "size", "relative"), int(g["iterations"]),
                                   int(g["spp"]), int(g["seed"]), int(g["weight"]), float(g["alpha"]), regions=True,
-                                  replay=True)
+                                  replay=True, rr=int(g.get("rr", 0)))
         assert np.array_equal(r["bins"].view(np.uint32), g["out_bins"].view(np.uint32))
         assert np.array_equal(r["regions"].view(np.uint32), g["out_regions"].view(np.uint32))
         assert np.array_equal(r["replay"][:, :, 1:].view(np.uint32), g["out_points"].view(np.uint32))

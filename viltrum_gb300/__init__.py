@@ -24,7 +24,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import scenes
-from ._lib import MEM_DEVICE, MEM_HOST, Context, Nested, VcuError, default_context, load
+from ._lib import (MEM_DEVICE, MEM_HOST, RR_ERROR, RR_INTEGRAL, RR_UNIFORM, Context, Nested, VcuError,
+                   default_context, load)
 
 __all__ = [
     "Context", "VcuError", "Integrand", "Range", "integrate", "range_", "range_all", "range_primary",
@@ -33,9 +34,9 @@ __all__ = [
     "integrator_per_bin_parallel", "integrator_adaptive_iterations", "integrator_adaptive_iterations_parallel",
     "integrator_adaptive_tolerance",
     "scenes", "load",
-    "rr_uniform_region", "region_sampling_uniform", "cv_optimize_weight", "cv_fixed_weight",
-    "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction", "integrator_region_based",
-    "integrator_crespo2021",
+    "rr_uniform_region", "rr_integral_region", "rr_error_region", "region_sampling_uniform", "cv_optimize_weight",
+    "cv_fixed_weight", "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction",
+    "integrator_region_based", "integrator_adaptive_variance_reduction_parallel", "integrator_crespo2021",
 ]
 
 
@@ -268,6 +269,23 @@ def integrator_per_bin_parallel(inner) -> PerBinParallel:
 @dataclass(frozen=True)
 class rr_uniform_region:  # noqa: N801  (reference name)
     """Uniform choice of the residual's region, weight = number of regions (region-russian-roulette.h:9-28)."""
+    code = RR_UNIFORM
+
+
+@dataclass(frozen=True)
+class rr_integral_region:  # noqa: N801
+    """The residual's region chosen with probability proportional to the norm (sum of |channel|) of the
+    control variate's integral over bin n region, floored at 1% of the mean weight; sample weight
+    1/probability (region-russian-roulette.h:30-68)."""
+    code = RR_INTEGRAL
+
+
+@dataclass(frozen=True)
+class rr_error_region:  # noqa: N801
+    """The residual's region chosen with probability proportional to norm(region error estimate) x
+    volume(bin n region) / volume(region), floored at 1% of the mean weight; sample weight
+    1/probability (region-russian-roulette.h:70-110)."""
+    code = RR_ERROR
 
 
 @dataclass(frozen=True)
@@ -330,13 +348,40 @@ def regions_integrator_parallel_variance_reduction(rr, cv, *args) -> VarianceRed
         sampling, (samples, seed) = region_sampling_uniform(), args
     else:
         raise TypeError("regions_integrator_parallel_variance_reduction(rr, cv, [sampling,] ...)")
-    if not isinstance(rr, rr_uniform_region) or not isinstance(sampling, region_sampling_uniform):
-        raise NotImplementedError("the CUDA control variates implement rr_uniform_region and region_sampling_uniform")
+    if not isinstance(rr, (rr_uniform_region, rr_integral_region, rr_error_region)):
+        raise NotImplementedError("the CUDA control variates implement rr_uniform_region, rr_integral_region and "
+                                  "rr_error_region")
+    if not isinstance(sampling, region_sampling_uniform):
+        raise NotImplementedError("the CUDA control variates implement region_sampling_uniform")
     return VarianceReduction(rr, cv, sampling, int(seed), int(samples))
 
 
 def integrator_region_based(generator: AdaptiveHeapGenerator, integrator: VarianceReduction) -> RegionBased:
     return RegionBased(generator, integrator)
+
+
+def integrator_adaptive_variance_reduction_parallel(rule: NestedRule, *args) -> RegionBased:
+    """integrator_adaptive_variance_reduction_parallel(rule, [error_heuristic,] iterations, rr, cv,
+    [region_sampler,] samples, [seed]) (integrator-adaptive-variance-reduction.h:12-41): the adaptive
+    heap generator (default heuristic with the absolute metric when none is given) followed by
+    regions_integrator_parallel_variance_reduction."""
+    args = list(args)
+    heur = error_heuristic_default(error_metric_absolute())
+    if args and not isinstance(args[0], (int, np.integer)):
+        heur = args.pop(0)
+    if len(args) < 4:
+        raise TypeError("integrator_adaptive_variance_reduction_parallel(rule, [heuristic,] iterations, rr, cv, "
+                        "[sampler,] samples, [seed])")
+    iterations, rr, cv = args[0], args[1], args[2]
+    rest = args[3:]
+    sampling = region_sampling_uniform()
+    if rest and not isinstance(rest[0], (int, np.integer)):
+        sampling = rest.pop(0)
+    if not rest or len(rest) > 2:
+        raise TypeError("samples (and optionally seed) expected after the cv strategy")
+    samples, seed = int(rest[0]), int(rest[1]) if len(rest) > 1 else 0
+    return integrator_region_based(regions_generator_adaptive_heap(rule, heur, iterations),
+                                   regions_integrator_parallel_variance_reduction(rr, cv, sampling, seed, samples))
 
 
 def integrator_crespo2021(iterations: int, spp: int, seed: int = 0) -> RegionBased:
@@ -440,7 +485,7 @@ def _run_cv(rb: RegionBased, bins, res, f, rng, logger, ctx, device_bins, replay
     flat = (not device_bins and isinstance(bins, np.ndarray) and bins.ndim == 1 and bins.dtype == np.float32
             and bins.size == nb * ch and bins.flags.c_contiguous)
     out = bins if (device_bins or flat) else np.empty(nb * ch, dtype=np.float32)
-    opts = CvOpts(vr.samples, vr.seed, 1 if vr.cv.fixed else 0, 0, float(vr.cv.alpha))
+    opts = CvOpts(vr.samples, vr.seed, 1 if vr.cv.fixed else 0, 0, float(vr.cv.alpha), vr.rr.code)
     stats = ctx.control_variates(p, _nested_struct(g.rule, g.heuristic), g.iterations, opts, out, approximation,
                                  regions, replay)
     if not device_bins and not flat:

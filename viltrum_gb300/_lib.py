@@ -26,6 +26,8 @@ EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vc
            "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
            "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global", "vcu_adaptive_tolerance"]
 BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
+CV_OPTIMIZE, CV_FIXED = 0, 1
+RR_UNIFORM, RR_INTEGRAL, RR_ERROR = 0, 1, 2  # residual region choice
 
 
 class VcuError(RuntimeError):
@@ -61,7 +63,8 @@ class Stats(ctypes.Structure):
 
 class CvOpts(ctypes.Structure):
     _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("weight", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double)]
+                ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double), ("rr", ctypes.c_int32),
+                ("reserved2", ctypes.c_int32)]
 
 
 class LearnedOpts(ctypes.Structure):

@@ -479,7 +479,51 @@ struct ResCfg {
     int32_t weight; /* VCU_CV_OPTIMIZE / VCU_CV_FIXED */
     double alpha;
     const float* approx_init; /* nullable: the approximation starts from these bin values */
+    int32_t rr;               /* VCU_RR_UNIFORM / VCU_RR_INTEGRAL / VCU_RR_ERROR */
+    const float* rerr;        /* VCU_RR_ERROR: norm of each heap region's error estimate */
+    double* cdf;              /* importance choice, per list entry: cumulative probability */
+    double* rrf;              /* importance choice, per list entry: 1 / probability */
 };
+
+/* rr_error_region weighs a region by norm(error()), error() = volume * (fold_all(H) - fold_all(low))
+ * (region.h:422-426, nested.h:17-24, norm.h:11-24), folded from dimension 0 with the reference's
+ * rounding; one thread per heap region */
+template <int DIM, int SH, int SL, int CH>
+__global__ void k_cv_region_error(const int* __restrict__ heap_pay, const float* __restrict__ vals,
+                                  const float* __restrict__ rvol, int nheap, float* __restrict__ rerr) {
+    constexpr int SD = ipow(SH, DIM);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nheap) return;
+    const int id = heap_pay[k] & 0xffffff;
+    const float* V = vals + (size_t)id * SD * CH;
+    float nrm = 0.0f;
+    for (int c = 0; c < CH; ++c) {
+        float hb[SD / SH], lb[SD / SH];
+        for (int i = 0; i < SD / SH; ++i) {
+            float line[SH], low[SL];
+#pragma unroll
+            for (int j = 0; j < SH; ++j) line[j] = V[(i * SH + j) * CH + c];
+#pragma unroll
+            for (int j = 0; j < SL; ++j) low[j] = line[j * (SH - 1) / (SL - 1)];
+            hb[i] = (CH == 1) ? RefRule<SH>::scalar(line) : RefRule<SH>::rgb(line);
+            lb[i] = (CH == 1) ? RefRule<SL>::scalar(low) : RefRule<SL>::rgb(low);
+        }
+        for (int n = SD / SH; n > 1; n /= SH) {
+            for (int i = 0; i < n / SH; ++i) {
+                float line[SH], low[SL];
+#pragma unroll
+                for (int j = 0; j < SH; ++j) line[j] = hb[i * SH + j];
+#pragma unroll
+                for (int j = 0; j < SL; ++j) low[j] = lb[i * SH + j * (SH - 1) / (SL - 1)];
+                hb[i] = (CH == 1) ? RefRule<SH>::scalar(line) : RefRule<SH>::rgb(line);
+                lb[i] = (CH == 1) ? RefRule<SL>::scalar(low) : RefRule<SL>::rgb(low);
+            }
+        }
+        const float e = vabs(vmul(rvol[id], vsub(hb[0], lb[0])));
+        nrm = (c == 0) ? e : vadd(nrm, e);
+    }
+    rerr[k] = nrm;
+}
 
 template <int DIM, int S, int CH>
 __device__ float poly_subrange(const float* V, int c, const float* A, const float* B) {
@@ -595,6 +639,10 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             for (int c = 0; c < CH; ++c)
                 stage[warp][i][c] = empty ? __int_as_float(0x7fc00001)
                                           : vmul(rvol[id], poly_subrange<DIM, S, CH>(vals + (size_t)id * SD * CH, c, A, B));
+            if (cfg.rr == VCU_RR_INTEGRAL) /* norm(integral over bin n region); an empty one integrates to 0 */
+                cfg.cdf[off + base + i] = empty ? 0.0 : (double)norm1(stage[warp][i], CH);
+            else if (cfg.rr == VCU_RR_ERROR) /* norm(error) * volume(bin n region) / volume(region) */
+                cfg.cdf[off + base + i] = (double)vdiv(vmul(cfg.rerr[lists[off + base + i]], v), rvol[id]);
         }
         __syncwarp();
         if (lane == 0)
@@ -612,6 +660,42 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
     for (int c = 0; c < CH; ++c) {
         approx[c] = __shfl_sync(0xffffffffu, approx[c], 0);
         approx_d[c] = (double)approx[c];
+    }
+    /* importance choice among the bin's regions (region-russian-roulette.h:30-108): weights floored at
+     * 1% of their mean (all 1 when they sum to <= 0), then std::discrete_distribution's normalised
+     * probabilities and their running sum, the last set to 1.  The sums are warp-parallel in FP64, so
+     * they can differ from the sequential ones in the last bits. */
+    if (cfg.rr != VCU_RR_UNIFORM && n > 0) {
+        double* W = cfg.cdf + off;
+        auto warp_sum = [&](double x) {
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            return __shfl_sync(0xffffffffu, x, 0);
+        };
+        double s1 = 0.0;
+        for (uint32_t i = lane; i < n; i += 32) s1 += W[i];
+        s1 = warp_sum(s1);
+        const double floor_w = 0.01 * s1 / (double)n;
+        auto clamped = [&](double w) { return (s1 <= 0.0) ? 1.0 : (w < floor_w ? floor_w : w); };
+        double s2 = 0.0;
+        for (uint32_t i = lane; i < n; i += 32) s2 += clamped(W[i]);
+        s2 = warp_sum(s2);
+        double carry = 0.0;
+        for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+            const uint32_t i = b0 + lane;
+            const double pi = (i < n) ? clamped(W[i]) / s2 : 0.0;
+            double x = pi;
+            for (int o = 1; o < 32; o <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            __syncwarp();
+            if (i < n) {
+                W[i] = (i == n - 1) ? 1.0 : carry + x;
+                cfg.rrf[off + i] = (n == 1) ? 1.0 : 1.0 / pi;
+            }
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
     }
     /* residual samples */
     /* per lane, in FP32: Kahan sums of the weighted samples, and the covariance moments of the
@@ -639,7 +723,20 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             for (int d = 0; d < DIM; ++d) x[d] = rec[1 + d];
         } else {
             const U4 r0 = philox4x32_10(U4{(uint32_t)j, blo, bhi, 0xC0DE0000u}, cfg.k0, cfg.k1);
-            chosen = (uint32_t)(((uint64_t)r0.x * n) >> 32); /* uniform index in [0, n) */
+            if (cfg.rr == VCU_RR_UNIFORM) {
+                chosen = (uint32_t)(((uint64_t)r0.x * n) >> 32); /* uniform index in [0, n) */
+            } else {
+                /* the first running probability >= u, u uniform in [0, 1) with 53 random bits */
+                const U4 r2 = philox4x32_10(U4{(uint32_t)j, blo, bhi, 0xC0DE1000u}, cfg.k0, cfg.k1);
+                const double u = (double)(((uint64_t)(r2.x >> 11) << 32) | r2.y) * 0x1p-53;
+                uint32_t lo = 0, hi = n - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (cfg.cdf[off + mid] < u) lo = mid + 1;
+                    else hi = mid;
+                }
+                chosen = lo;
+            }
             const int id = heap_pay[lists[off + chosen]] & 0xffffff;
             isect(id, a, b, A, B, v, empty);
             const uint32_t rr[3] = {r0.y, r0.z, r0.w};
@@ -663,15 +760,16 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             p[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));
         }
         for (int c = 0; c < CH; ++c) gv[c] = poly_at<DIM, S, CH>(vals + (size_t)id * SD * CH, c, p);
-        /* sample weights: prod(res) * n (russian roulette) * volume(bin n region) */
+        /* sample weights: prod(res) * 1/P(region) (n for the uniform choice) * volume(bin n region) */
+        const double rrf = (cfg.rr == VCU_RR_UNIFORM) ? (double)n : cfg.rrf[off + chosen];
         float fs[CH], as[CH];
         for (int c = 0; c < CH; ++c) {
             if (CH == 1) {
-                fs[c] = __double2float_rn((double)fv[c] * cfg.factor * (double)n * (double)v);
-                as[c] = __double2float_rn((double)gv[c] * cfg.factor * (double)n * (double)v);
-            } else {
-                fs[c] = vmul(vmul(__double2float_rn((double)fv[c] * cfg.factor), (float)n), v);
-                as[c] = vmul(vmul(__double2float_rn((double)gv[c] * cfg.factor), (float)n), v);
+                fs[c] = __double2float_rn((double)fv[c] * cfg.factor * rrf * (double)v);
+                as[c] = __double2float_rn((double)gv[c] * cfg.factor * rrf * (double)v);
+            } else { /* per channel: scales by double rounded to float, then the float volume */
+                fs[c] = vmul(__double2float_rn((double)__double2float_rn((double)fv[c] * cfg.factor) * rrf), v);
+                as[c] = vmul(__double2float_rn((double)__double2float_rn((double)gv[c] * cfg.factor) * rrf), v);
             }
             float y = vsub(fs[c], cf32[c]);
             float t = vadd(sf32[c], y);
@@ -779,7 +877,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 /* stages 2 and 3 over a finished set of regions: hp[0..nheap) are pool ids (low 24 bits) in the
  * order the reference integrates them (heap order, or depth-first order for the tolerance-driven
  * form); cnt/off/cur are per-bin scratch of nbins, nbins+1, nbins words */
-template <class F, int DIM, int SH>
+template <class F, int DIM, int SH, int SL>
 int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_cv& cv,
                       const float* vals, const float* rmin, const float* rmax, const float* vol, const int* hp,
                       size_t nheap, uint32_t* cnt, uint32_t* off, uint32_t* cur, const float* d_replay, float* d_bins,
@@ -806,9 +904,17 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     uint32_t total = 0;
     VCU_CUDA(ctx, cudaMemcpyAsync(&total, off + g.nbins, 4, cudaMemcpyDeviceToHost, ctx->stream));
     VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if ((rc = ensure(ctx, ctx->aux, (size_t)total * 8 + 512))) return rc;
+    /* aux: unsorted and sorted lists; for an importance choice also the per-entry running
+     * probabilities and inverse probabilities (FP64) and, for rr_error, each heap region's error norm */
+    const bool importance = cv.rr != VCU_RR_UNIFORM;
+    const size_t o_cdf = align256((size_t)total * 8 + 512);
+    const size_t o_rrf = align256(o_cdf + (size_t)total * 8);
+    const size_t o_rerr = align256(o_rrf + (size_t)total * 8);
+    const size_t aux_bytes = importance ? o_rerr + nheap * 4 : (size_t)total * 8 + 512;
+    if ((rc = ensure(ctx, ctx->aux, aux_bytes))) return rc;
     uint32_t* lists_u = static_cast<uint32_t*>(ctx->aux.ptr);
     uint32_t* lists = lists_u + total + 64;
+    char* aux = static_cast<char*>(ctx->aux.ptr);
     k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, nullptr, off, cur, lists_u, 1);
     k_cv_sort<<<(unsigned)((g.nbins * 32 + 255) / 256), 256, 0, ctx->stream>>>(off, lists_u, lists, g.nbins);
     launches += 2;
@@ -834,6 +940,18 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     rcfg.alpha = cv.alpha;
     /* reserved == 1 (set only by vcu_adaptive_iterations_global): accumulate into the bins' values */
     rcfg.approx_init = cv.reserved == 1 ? d_bins : nullptr;
+    rcfg.rr = cv.rr;
+    if (importance) {
+        rcfg.cdf = reinterpret_cast<double*>(aux + o_cdf);
+        rcfg.rrf = reinterpret_cast<double*>(aux + o_rrf);
+        if (cv.rr == VCU_RR_ERROR) {
+            float* rerr = reinterpret_cast<float*>(aux + o_rerr);
+            k_cv_region_error<DIM, SH, SL, F::CH>
+                <<<(unsigned)((nheap + 127) / 128), 128, 0, ctx->stream>>>(hp, vals, vol, (int)nheap, rerr);
+            ++launches;
+            rcfg.rerr = rerr;
+        }
+    }
     const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
     k_cv_residual<F, DIM, S><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(f, rcfg, off, lists, hp, vals, rmin, rmax,
                                                                           vol, d_replay, d_bins, d_approx,
@@ -914,7 +1032,7 @@ int cv_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, 
     ++launches;
     VCU_CUDA(ctx, cudaGetLastError());
 
-    return regions_into_bins<F, DIM, SH>(ctx, f, p, g, cv, vals, rmin, rmax, vol, hp, nheap, cnt, off, cur, d_replay,
+    return regions_into_bins<F, DIM, SH, SL>(ctx, f, p, g, cv, vals, rmin, rmax, vol, hp, nheap, cnt, off, cur, d_replay,
                                          d_bins, d_approx, d_regions, launches);
 }
 
@@ -1267,7 +1385,7 @@ int tol_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g,
     cv.weight = VCU_CV_FIXED;
     cv.reserved = 1;
     cv.alpha = 1.0;
-    return regions_into_bins<F, DIM, SH>(ctx, f, p, g, cv, vals, rmin, rmax, vol, order, nl,
+    return regions_into_bins<F, DIM, SH, SL>(ctx, f, p, g, cv, vals, rmin, rmax, vol, order, nl,
                                          reinterpret_cast<uint32_t*>(base + o_cnt), reinterpret_cast<uint32_t*>(base + o_off),
                                          reinterpret_cast<uint32_t*>(base + o_cur), nullptr, d_bins, nullptr, nullptr,
                                          launches);

@@ -404,7 +404,9 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     if (iterations >= (1ull << 23)) return fail(ctx, VCU_UNSUPPORTED, "control variates take at most 2^23-1 splits");
     if (cv->samples_per_bin > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "samples per bin must be < 2^32");
     if (cv->weight != VCU_CV_OPTIMIZE && cv->weight != VCU_CV_FIXED) return fail(ctx, VCU_INVALID_ARG, "unknown weight");
-    if (cv->reserved != 0) return fail(ctx, VCU_INVALID_ARG, "vcu_cv::reserved must be 0");
+    if (cv->reserved != 0 || cv->reserved2 != 0) return fail(ctx, VCU_INVALID_ARG, "vcu_cv::reserved must be 0");
+    if (cv->rr != VCU_RR_UNIFORM && cv->rr != VCU_RR_INTEGRAL && cv->rr != VCU_RR_ERROR)
+        return fail(ctx, VCU_INVALID_ARG, "unknown residual region choice");
     if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
         return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
     if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
