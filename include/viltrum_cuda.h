@@ -61,7 +61,11 @@ enum { VCU_METRIC_ABSOLUTE = 0, VCU_METRIC_RELATIVE = 1 };
 enum { VCU_CV_OPTIMIZE = 0, VCU_CV_FIXED = 1 };
 /* residual region choice (src/control-variates/region-russian-roulette.h): rr_uniform_region,
  * rr_integral_region, rr_error_region (NormDefault) */
-enum { VCU_RR_UNIFORM = 0, VCU_RR_INTEGRAL = 1, VCU_RR_ERROR = 2 };
+enum { VCU_RR_UNIFORM = 0, VCU_RR_INTEGRAL = 1, VCU_RR_ERROR = 2, VCU_RR_PDF = 3 };
+/* residual point sampling in bin n region (src/control-variates/region-sampling.h):
+ * region_sampling_uniform, region_sampling_importance, region_sampling_russian_roulette,
+ * region_sampling_mis (NormDefault) */
+enum { VCU_RS_UNIFORM = 0, VCU_RS_IMPORTANCE = 1, VCU_RS_RUSSIAN_ROULETTE = 2, VCU_RS_MIS = 3 };
 
 typedef struct vcu_ctx vcu_ctx;
 
@@ -155,13 +159,16 @@ int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_ne
  * error_heuristic_size(error_metric_relative(), 1e-5)): one max-error heap of regions over the whole
  * range (iterations splits), per-bin lists of the regions overlapping each bin, the polynomial
  * integral over bin n region as control variate, and `samples` residual samples per bin
- * (region chosen uniformly, or with probability proportional to |integral over bin n region| or to
- * |region error| x its share of volume in the bin, floored at 1% of the mean weight; point uniform
- * in bin n region).  The result is ASSIGNED to the bins.
+ * (region chosen uniformly, or with probability proportional to |integral over bin n region|, to
+ * |region error| x its share of volume in the bin, or to the integral of the region's pdf over bin
+ * n region, floored at 1% (rr_factor) of the mean weight; point uniform in bin n region or drawn
+ * from the pdf of the region's polynomial -- Simpson high rule only).  The result is ASSIGNED to the
+ * bins.
  * Residual sample j of bin b draws from Philox4x32-10 unless `replay` is given: nbins x samples x
- * (1 + dim) floats (index of the chosen region in the bin's list, then the point), e.g. the
- * reference's own draws.  approximation (nullable) receives the control-variate integral per bin,
- * regions (nullable) the (iterations+1) x (min[dim], max[dim]) region ranges in heap order.  All
+ * vcu_cv_replay_width(dim, sampling) floats (index of the chosen region in the bin's list, then the
+ * point, ...), e.g. the reference's own draws.  approximation (nullable) receives the
+ * control-variate integral per bin, regions (nullable) the (iterations+1) x (min[dim], max[dim])
+ * region ranges in heap order.  All
  * pointers follow p->mem. */
 typedef struct vcu_cv {
     uint64_t samples_per_bin; /* residual samples per bin (spp)                         */
@@ -169,9 +176,18 @@ typedef struct vcu_cv {
     int32_t weight;           /* VCU_CV_OPTIMIZE or VCU_CV_FIXED                        */
     int32_t reserved;         /* 0                                                      */
     double alpha;             /* cv_fixed_weight's alpha                                */
-    int32_t rr;               /* VCU_RR_UNIFORM, VCU_RR_INTEGRAL or VCU_RR_ERROR        */
+    int32_t rr;               /* VCU_RR_UNIFORM, _INTEGRAL, _ERROR or _PDF              */
+    int32_t sampling;         /* VCU_RS_UNIFORM, _IMPORTANCE, _RUSSIAN_ROULETTE or _MIS */
+    float rr_factor;          /* VCU_RR_PDF: rr_pdf_region's factor_prob (0.01f there) */
     int32_t reserved2;        /* 0                                                      */
+    double mis_power;         /* VCU_RS_MIS: region_sampling_mis(power, cutoff)        */
+    double mis_cutoff;
 } vcu_cv;
+
+/* floats per residual sample in vcu_control_variates' replay records: the chosen list index and
+ * the point; then, for VCU_RS_RUSSIAN_ROULETTE and VCU_RS_MIS, 1 when the point came from the
+ * region's pdf (0 when uniform); then, for VCU_RS_MIS, the pdf point its weight was computed at */
+int vcu_cv_replay_width(int32_t dim, int32_t sampling);
 
 int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
                          uint64_t iterations, const vcu_cv* cv, const float* replay, float* bins,

@@ -350,15 +350,21 @@ class control_variates {
     std::uint64_t seed_;
     int weight_;
     double alpha_;
-    int rr_;
+    int rr_, sampling_;
+    float rr_factor_;
+    double mis_power_, mis_cutoff_;
 
 public:
-    /* rr: VCU_RR_UNIFORM (rr_uniform_region), VCU_RR_INTEGRAL (rr_integral_region) or VCU_RR_ERROR
-     * (rr_error_region), src/control-variates/region-russian-roulette.h:9-110 */
+    /* rr: VCU_RR_UNIFORM (rr_uniform_region), VCU_RR_INTEGRAL (rr_integral_region), VCU_RR_ERROR
+     * (rr_error_region) or VCU_RR_PDF (rr_pdf_region(rr_factor)), region-russian-roulette.h:9-149;
+     * sampling: VCU_RS_UNIFORM (region_sampling_uniform), VCU_RS_IMPORTANCE, VCU_RS_RUSSIAN_ROULETTE or
+     * VCU_RS_MIS (region_sampling_mis(mis_power, mis_cutoff)), region-sampling.h:9-135 */
     control_variates(nested_rule r, unsigned long iterations, unsigned long samples, std::uint64_t seed,
-                     int weight = VCU_CV_OPTIMIZE, double alpha = 1.0, int rr = VCU_RR_UNIFORM)
+                     int weight = VCU_CV_OPTIMIZE, double alpha = 1.0, int rr = VCU_RR_UNIFORM,
+                     int sampling = VCU_RS_UNIFORM, float rr_factor = 0.01f, double mis_power = 1.0,
+                     double mis_cutoff = 0.0)
         : rule_(r), iterations_(iterations), samples_(samples), seed_(seed), weight_(weight), alpha_(alpha),
-          rr_(rr) {}
+          rr_(rr), sampling_(sampling), rr_factor_(rr_factor), mis_power_(mis_power), mis_cutoff_(mis_cutoff) {}
 
     template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
     void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
@@ -375,6 +381,10 @@ public:
         cv.weight = weight_;
         cv.alpha = alpha_;
         cv.rr = rr_;
+        cv.sampling = sampling_;
+        cv.rr_factor = rr_factor_;
+        cv.mis_power = mis_power_;
+        cv.mis_cutoff = mis_cutoff_;
         vcu_stats st{};
         ctx.check(vcu_control_variates(ctx.get(), &p, &rule_.n, iterations_, &cv, nullptr, out.data(), nullptr,
                                        nullptr, &st));

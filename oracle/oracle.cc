@@ -194,6 +194,87 @@ inline float norm_default(const vrgb& v) {
     return s;
 }
 
+/* ------------------------------------------------------------------ Simpson's pdf (rules.h:102-248)
+ * The polynomial importance sampling of the control variate: the parabola through the norms of the
+ * three node values, lifted so its minimum on [0,1] is 0 (pdf_points), its integral, value, cdf and
+ * an inverse cdf by the closed-form roots of the cubic (Cardano / Viete), in the reference's mix of
+ * float and double arithmetic. */
+struct SimpsonPdf {
+    template <class T> static std::array<float, 3> points(const T* p) {
+        std::array<float, 3> q;
+        for (int i = 0; i < 3; ++i) q[i] = norm_default(p[i]);
+        float cs[3];
+        Simpson().coefficients(q.data(), cs);
+        float ymin = 0;
+        if (cs[2] > 0) {
+            const float tmin = -cs[1] / (2.0 * cs[2]);
+            if ((tmin > 0) && (tmin < 1)) {
+                const float ytmin = (cs[2] * tmin + cs[1]) * tmin + cs[0];
+                if (ytmin < ymin) ymin = ytmin;
+            }
+        }
+        for (int i = 0; i < 3; ++i) q[i] -= ymin;
+        return q;
+    }
+    static float integral(float t0, float t1, const std::array<float, 3>& ps) { return Simpson().subrange(t0, t1, ps.data()); }
+    static float at(float t, const std::array<float, 3>& ps) { return Simpson().at(t, ps.data()); }
+    static float cdf(float t, const std::array<float, 3>& ps) {
+        float c[3];
+        Simpson().coefficients(ps.data(), c);
+        return ((c[2] * t / 3.0 + c[1] / 2.0) * t + c[0]) * t;
+    }
+    static double cuberoot(double x) { return (x < 0) ? (-1 * std::pow(-x, 1. / 3.)) : std::pow(x, 1. / 3.); }
+    static std::vector<float> inv_cdf(float x, const std::array<float, 3>& pts) {
+        std::vector<float> sol;
+        float co[3];
+        Simpson().coefficients(pts.data(), co);
+        double a = co[2] / 3.;
+        double b = co[1] / 2.;
+        float c = co[0];
+        float d = -x;
+        const double sum = a + b + c + d;
+        a /= sum;
+        b /= sum;
+        c /= sum;
+        d /= sum;
+        if (std::abs(a) < 1.e-3) {
+            if (std::abs(b) < 1.e-3) {
+                if (std::abs(c) >= 1.e-3) sol.push_back(-d / c);
+            } else {
+                const double disc = c * c - 4 * b * d;
+                if (disc >= 0) {
+                    sol.push_back((-c + std::sqrt(disc)) / (2 * b));
+                    sol.push_back((-c - std::sqrt(disc)) / (2 * b));
+                }
+            }
+        } else {
+            const double p = c / a - std::pow(b, 2.) / (3. * std::pow(a, 2.));
+            const double q = 2 * std::pow(b, 3.) / (27. * std::pow(a, 3.)) - b * c / (3. * std::pow(a, 2.)) + d / a;
+            const double sqr = std::pow(q / 2., 2.) + std::pow(p / 3., 3.);
+            if (sqr >= 0.) {
+                sol.push_back(cuberoot(-q / 2. - std::sqrt(sqr)) + cuberoot(-q / 2. + std::sqrt(sqr)) - b / (3 * a));
+            } else {
+                for (int i = 0; i < 3; i++)
+                    sol.push_back(2. * std::sqrt(-p / 3.) *
+                                      std::cos(1. / 3. * std::acos(3. * q / (2. * p) * std::sqrt(-3. / p)) - 2. * M_PI * i / 3.) -
+                                  b / (3. * a));
+            }
+        }
+        return sol;
+    }
+    /* a point of [t0,t1] with density proportional to the lifted parabola; uniform when no root fits */
+    template <class T> static float sample(float s, float t0, float t1, const T* p) {
+        const auto ps = points(p);
+        const float x = s * cdf(t1, ps) + (float(1) - s) * cdf(t0, ps);
+        for (float r : inv_cdf(x, ps)) {
+            if ((r < t0) && (std::abs(t0 - r) < 1.e-5)) r = t0;
+            if ((r > t1) && (std::abs(r - t1) < 1.e-5)) r = t1;
+            if ((r >= t0) && (r <= t1) && (!std::isnan(r))) return r;
+        }
+        return s * (t1 - t0) + t0;
+    }
+};
+
 /* ------------------------------------------------------------------ nd folds */
 template <int S, class U, class T, class Fn>
 std::vector<U> fold(const std::vector<T>& in, int k, int d, const Fn& fn) {
@@ -338,6 +419,63 @@ template <class H, class L, int DIM, class T> struct Region {
         for (int k = DIM, d = 0; k >= 1; --k, ++d)
             v = fold<S, T>(v, k, 0, [&](const T* line) -> T { return h.at(p[d], line); });
         return v[0] * 1.0f;
+    }
+    /* Simpson regions only: the pdf integral over [a,b] folding from the last dimension
+     * (region.h:267-290), the unnormalised pdf at a point (:296-311), the normalised pdf (:326-331) */
+    template <class Line> float pdf_fold(const float* a, const float* b, const Line& line_fn) const {
+        std::vector<float> v = fold<S, float>(data, DIM, DIM - 1, [&](const T* l) { return line_fn(DIM - 1, l); });
+        for (int k = DIM - 1; k >= 1; --k)
+            v = fold<S, float>(v, k, k - 1, [&](const float* l) { return line_fn(k - 1, l); });
+        (void)a;
+        (void)b;
+        return v[0];
+    }
+    float pdf_integral_subrange(const Range<DIM>& r) const {
+        const auto a = range.pos_in_range(r.a);
+        const auto b = range.pos_in_range(r.b);
+        return range.volume() * pdf_fold(a.data(), b.data(), [&](int d, const auto* l) {
+                   return SimpsonPdf::integral(a[d], b[d], SimpsonPdf::points(l));
+               });
+    }
+    float pdf_subrange(const std::array<float, DIM>& pos, const Range<DIM>& r) const {
+        const auto p = range.pos_in_range(pos);
+        const auto a = range.pos_in_range(r.a);
+        const auto b = range.pos_in_range(r.b);
+        const float at = pdf_fold(a.data(), b.data(), [&](int d, const auto* l) {
+            return SimpsonPdf::at(p[d], SimpsonPdf::points(l));
+        });
+        return at / pdf_integral_subrange(r);
+    }
+    /* a point of bin n region drawn from the pdf: the marginal of the first remaining dimension (the
+     * others integrated over [a,b], last first), sampled; then the pdf conditioned on it and the
+     * next dimension (region.h:220-257) */
+    template <class U>
+    void sample_rec(const std::vector<U>& ma, int k, int off, const float* s, const float* a, const float* b,
+                    float* sol) const {
+        if (k == 1) {
+            sol[off] = SimpsonPdf::sample(s[off], a[off], b[off], ma.data());
+            return;
+        }
+        std::vector<float> m = fold<S, float>(ma, k, k - 1, [&](const U* l) {
+            return SimpsonPdf::integral(a[off + k - 1], b[off + k - 1], SimpsonPdf::points(l));
+        });
+        for (int j = k - 1; j >= 2; --j)
+            m = fold<S, float>(m, j, j - 1, [&](const float* l) {
+                return SimpsonPdf::integral(a[off + j - 1], b[off + j - 1], SimpsonPdf::points(l));
+            });
+        sol[off] = SimpsonPdf::sample(s[off], a[off], b[off], m.data());
+        const float t = sol[off];
+        std::vector<float> c = fold<S, float>(ma, k, 0, [&](const U* l) { return SimpsonPdf::at(t, SimpsonPdf::points(l)); });
+        sample_rec<float>(c, k - 1, off + 1, s, a, b, sol);
+    }
+    std::array<float, DIM> sample_subrange(const std::array<float, DIM>& s, const Range<DIM>& r) const {
+        const auto a = range.pos_in_range(r.a);
+        const auto b = range.pos_in_range(r.b);
+        std::array<float, DIM> sol;
+        sample_rec<T>(data, DIM, 0, s.data(), a.data(), b.data(), sol.data());
+        std::array<float, DIM> x;
+        for (int i = 0; i < DIM; ++i) x[i] = sol[i] * (range.max(i) - range.min(i)) + range.min(i);
+        return x;
     }
 };
 
@@ -760,8 +898,11 @@ template <class T> struct CvFixed {
 
 template <class H, class L, int DIM, class T, class Fun, class M>
 void control_variates(const Fun& fun, const Problem& p, const orc_nested& nc, const M& metric, uint64_t iters,
-                      uint64_t spp, uint64_t seed, int weight, double alpha, int rr_mode, float* out,
-                      float* approx_out, float* regions_out, float* replay_out) {
+                      uint64_t spp, uint64_t seed, const orc_cv& cv, float* out, float* approx_out,
+                      float* regions_out, float* replay_out) {
+    const int weight = cv.weight, rr_mode = cv.rr, sampling = cv.sampling;
+    const double alpha = cv.alpha;
+    const int width = orc_replay_width(DIM, sampling);
     using R = Region<H, L, DIM, T>;
     const auto range = make_range<DIM>(p);
     Fn<Fun, DIM, T> f{&fun};
@@ -825,7 +966,7 @@ void control_variates(const Fun& fun, const Problem& p, const orc_nested& nc, co
             if (!rr[i].empty()) approximation += double(factor) * list[i]->integral_subrange(rr[i]);
         }
         if (approx_out) VT<T>::to(approximation, approx_out + b * VT<T>::CH);
-        float* rep = replay_out ? replay_out + b * spp * (1 + DIM) : nullptr;
+        float* rep = replay_out ? replay_out + b * spp * width : nullptr;
         /* region choice: uniform (region-russian-roulette.h:9-28), or proportional to the norm of
          * the control variate's integral over bin n region (:30-68) or of the region's error scaled
          * by the share of its volume in the bin (:70-108), with a floor of 1% of the mean weight */
@@ -835,12 +976,16 @@ void control_variates(const Fun& fun, const Problem& p, const orc_nested& nc, co
             std::vector<double> w(list.size());
             for (std::size_t i = 0; i < list.size(); ++i) {
                 if (rr_mode == ORC_RR_INTEGRAL) w[i] = norm_default(list[i]->integral_subrange(rr[i]));
-                else w[i] = norm_default(list[i]->error_total()) * rr[i].volume() / list[i]->range.volume();
+                else if (rr_mode == ORC_RR_ERROR)
+                    w[i] = norm_default(list[i]->error_total()) * rr[i].volume() / list[i]->range.volume();
+                else if constexpr (R::S == 3) w[i] = list[i]->pdf_integral_subrange(rr[i]); /* rr_pdf_region (:112-149) */
             }
             double sum = 0.0;
             for (double v : w) sum += v;
             if (sum <= 0.0)
                 for (double& v : w) v = 1.0;
+            else if (rr_mode == ORC_RR_PDF)
+                for (double& v : w) v = std::max(v, cv.rr_factor * sum / double(w.size()));
             else
                 for (double& v : w) v = std::max(v, 0.01 * sum / double(w.size()));
             weighted = std::discrete_distribution<std::size_t>(w.begin(), w.end());
@@ -861,15 +1006,83 @@ void control_variates(const Fun& fun, const Problem& p, const orc_nested& nc, co
                 choose(chosen, rrfactor);
                 const R* r = list[chosen];
                 const Range<DIM>& rbr = rr[chosen];
-                std::array<float, DIM> x;
-                for (int i = 0; i < DIM; ++i) {
-                    std::uniform_real_distribution<float> dis(rbr.min(i), rbr.max(i));
-                    x[i] = dis(rng);
+                std::array<float, DIM> x, ximp{};
+                float sfactor;
+                int branch = 0;
+                auto uniform_point = [&]() {
+                    for (int i = 0; i < DIM; ++i) {
+                        std::uniform_real_distribution<float> dis(rbr.min(i), rbr.max(i));
+                        x[i] = dis(rng);
+                    }
+                    sfactor = rbr.volume();
+                };
+                if constexpr (R::S == 3) {
+                    std::uniform_real_distribution<float> dis(0, 1);
+                    std::array<float, DIM> u;
+                    if (sampling == ORC_RS_IMPORTANCE) { /* region-sampling.h:22-43 */
+                        if (rbr.volume() < 1.e-5) uniform_point();
+                        else {
+                            for (int i = 0; i < DIM; ++i) u[i] = dis(rng);
+                            x = r->sample_subrange(u, rbr);
+                            const float pdf = r->pdf_subrange(x, rbr);
+                            sfactor = (pdf < 1.e-5) ? 0.0 : (1.0 / pdf);
+                        }
+                    } else if (sampling == ORC_RS_RUSSIAN_ROULETTE) { /* :47-81 */
+                        for (int i = 0; i < DIM; ++i) u[i] = dis(rng);
+                        const float pdf_importance = r->pdf_integral_subrange(rbr);
+                        const float pdf_uniform = rbr.volume();
+                        const float rr_sample = dis(rng);
+                        float pdf = 0;
+                        if (rr_sample < (pdf_importance / (pdf_importance + pdf_uniform))) {
+                            x = r->sample_subrange(u, rbr);
+                            pdf = r->pdf_subrange(x, rbr);
+                            branch = 1;
+                        } else {
+                            for (int i = 0; i < DIM; ++i) x[i] = rbr.min(i) + u[i] * (rbr.max(i) - rbr.min(i));
+                            pdf = float(1) / rbr.volume();
+                        }
+                        sfactor = (pdf < 1.e-10) ? 0.0 : (1.0 / pdf);
+                    } else if (sampling == ORC_RS_MIS) { /* :84-135 */
+                        for (int i = 0; i < DIM; ++i) u[i] = dis(rng);
+                        x = r->sample_subrange(u, rbr);
+                        ximp = x;
+                        const float pdf_importance = r->pdf_subrange(x, rbr);
+                        const float pdf_uniform = float(1) / rbr.volume();
+                        float mis_importance = std::pow(pdf_importance, cv.mis_power);
+                        float mis_uniform = std::pow(pdf_uniform, cv.mis_power);
+                        float mis_sum = mis_importance + mis_uniform;
+                        if (mis_importance < (cv.mis_cutoff * mis_sum)) {
+                            mis_importance = 0;
+                            mis_sum = mis_uniform;
+                        }
+                        if (mis_uniform < (cv.mis_cutoff * mis_sum)) {
+                            mis_uniform = 0;
+                            mis_sum = mis_importance;
+                        }
+                        const float p_rr_importance =
+                            (pdf_importance > 1.e-10) ? (mis_importance / pdf_importance) : float(0);
+                        const float p_rr_uniform = mis_uniform * rbr.volume();
+                        const float p_rr_sum = p_rr_importance + p_rr_uniform;
+                        sfactor = p_rr_sum / mis_sum;
+                        const float rr_sample = dis(rng);
+                        branch = 1;
+                        if (rr_sample < (p_rr_uniform / p_rr_sum)) {
+                            for (int i = 0; i < DIM; ++i) x[i] = rbr.min(i) + u[i] * (rbr.max(i) - rbr.min(i));
+                            branch = 0;
+                        }
+                    } else {
+                        uniform_point();
+                    }
+                } else {
+                    uniform_point();
                 }
-                const float sfactor = rbr.volume();
                 if (rep) {
-                    rep[s * (1 + DIM)] = float(chosen);
-                    for (int i = 0; i < DIM; ++i) rep[s * (1 + DIM) + 1 + i] = x[i];
+                    float* rc = rep + s * width;
+                    rc[0] = float(chosen);
+                    for (int i = 0; i < DIM; ++i) rc[1 + i] = x[i];
+                    if (sampling == ORC_RS_RUSSIAN_ROULETTE || sampling == ORC_RS_MIS) rc[1 + DIM] = float(branch);
+                    if (sampling == ORC_RS_MIS)
+                        for (int i = 0; i < DIM; ++i) rc[2 + DIM + i] = ximp[i];
                 }
                 const T fs = f(x) * double(factor) * rrfactor * sfactor;
                 const T as = r->approximation_at(x) * double(factor) * rrfactor * sfactor;
@@ -1051,17 +1264,19 @@ extern "C" int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* pa
 extern "C" int orc_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
                                     const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
                                     const orc_nested* nested, uint64_t iterations, uint64_t spp, uint64_t seed,
-                                    int32_t weight, double alpha, int32_t rr, float* out, float* approx_out,
-                                    float* regions_out, float* replay_out) {
-    if (!valid_problem(dim, dimbins, res) || !nested) return 1;
-    if (rr != ORC_RR_UNIFORM && rr != ORC_RR_INTEGRAL && rr != ORC_RR_ERROR) return 1;
+                                    const orc_cv* cv, float* out, float* approx_out, float* regions_out,
+                                    float* replay_out) {
+    if (!valid_problem(dim, dimbins, res) || !nested || !cv) return 1;
+    if (cv->rr < ORC_RR_UNIFORM || cv->rr > ORC_RR_PDF) return 1;
+    if (cv->sampling < ORC_RS_UNIFORM || cv->sampling > ORC_RS_MIS) return 1;
+    /* the pdf machinery exists for Simpson only (src/newton-cotes/rules.h:102-248) */
+    if ((cv->rr == ORC_RR_PDF || cv->sampling != ORC_RS_UNIFORM) && nested->rule_hi != ORC_RULE_SIMPSON) return 2;
     Problem p{dim, dimbins, rmin, rmax, res};
     return with_integrand(kind, params, n_params, dim, [&](const auto& f, auto D, auto t) -> int {
         return with_rules(*nested, [&](auto h, auto l) -> int {
             return with_metric(*nested, [&](auto m) -> int {
                 control_variates<decltype(h), decltype(l), decltype(D)::value, decltype(t)>(
-                    f, p, *nested, m, iterations, spp, seed, weight, alpha, rr, out, approx_out, regions_out,
-                    replay_out);
+                    f, p, *nested, m, iterations, spp, seed, *cv, out, approx_out, regions_out, replay_out);
                 return 0;
             });
         });

@@ -33,7 +33,29 @@ enum { ORC_METRIC_ABSOLUTE = 0, ORC_METRIC_RELATIVE = 1 };
 enum { ORC_CV_OPTIMIZE = 0, ORC_CV_FIXED = 1 };
 /* residual region choice (src/control-variates/region-russian-roulette.h): rr_uniform_region,
  * rr_integral_region, rr_error_region */
-enum { ORC_RR_UNIFORM = 0, ORC_RR_INTEGRAL = 1, ORC_RR_ERROR = 2 };
+enum { ORC_RR_UNIFORM = 0, ORC_RR_INTEGRAL = 1, ORC_RR_ERROR = 2, ORC_RR_PDF = 3 };
+/* residual point sampling in bin n region (src/control-variates/region-sampling.h):
+ * region_sampling_uniform, region_sampling_importance, region_sampling_russian_roulette,
+ * region_sampling_mis; all but uniform need a Simpson high rule */
+enum { ORC_RS_UNIFORM = 0, ORC_RS_IMPORTANCE = 1, ORC_RS_RUSSIAN_ROULETTE = 2, ORC_RS_MIS = 3 };
+
+/* residual strategy of the control-variate integrator */
+typedef struct orc_cv {
+    int32_t weight;     /* ORC_CV_OPTIMIZE / ORC_CV_FIXED                                */
+    int32_t rr;         /* ORC_RR_*                                                      */
+    double alpha;       /* cv_fixed_weight(alpha)                                        */
+    float rr_factor;    /* rr_pdf_region(factor_prob): floor of the weights (0.01f)      */
+    int32_t sampling;   /* ORC_RS_*                                                      */
+    double mis_power;   /* region_sampling_mis(power, cutoff)                            */
+    double mis_cutoff;
+} orc_cv;
+
+/* floats per residual sample in replay_out: the chosen list index and the point, then for
+ * ORC_RS_RUSSIAN_ROULETTE / ORC_RS_MIS a 1/0 flag (importance branch taken) and for ORC_RS_MIS
+ * the importance point its weight was computed at */
+static inline int orc_replay_width(int dim, int sampling) {
+    return 1 + dim + (sampling == ORC_RS_RUSSIAN_ROULETTE ? 1 : sampling == ORC_RS_MIS ? 1 + dim : 0);
+}
 /* Monte Carlo flavours */
 enum {
     ORC_MC_PER_BIN_PARALLEL = 0, /* integrator_per_bin_parallel(monte_carlo(spp, seed))    */
@@ -68,18 +90,19 @@ int orc_per_bin_adaptive_nested(int32_t kind, const float* params, int32_t n_par
                                 uint64_t iterations, float* out, int32_t* trace);
 
 /* integrator_region_based(regions_generator_adaptive_heap(nested, heuristic, iters),
- *   regions_integrator_parallel_variance_reduction(rr, cv, region_sampling_uniform(),
- *   std::mt19937(seed), spp))  -- crespo2021 when nested = (simpson, trapezoidal, size, relative) and
- *   rr = ORC_RR_UNIFORM (rr_uniform_region(); ORC_RR_INTEGRAL / ORC_RR_ERROR: rr_integral_region() /
- *   rr_error_region() with NormDefault).
+ *   regions_integrator_parallel_variance_reduction(rr, weight, sampling, std::mt19937(seed), spp))
+ *   -- crespo2021 when nested = (simpson, trapezoidal, size, relative), rr = ORC_RR_UNIFORM and
+ *   sampling = ORC_RS_UNIFORM.  rr: rr_uniform_region(), rr_integral_region(), rr_error_region(),
+ *   rr_pdf_region(rr_factor); sampling: region_sampling_uniform(), region_sampling_importance(),
+ *   region_sampling_russian_roulette(), region_sampling_mis(power, cutoff); NormDefault throughout.
  * approx_out (nullable): per-bin control-variate integral (the "approximation").
  * regions_out (nullable): (iters+1) x (2*dim) float ranges in heap order.
- * replay_out (nullable): per bin, spp x (chosen list index, dim coordinates) as floats.      */
+ * replay_out (nullable): per bin, spp x orc_replay_width(dim, sampling) floats.               */
 int orc_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
                          const float* rmin, const float* rmax, int32_t dimbins,
                          const uint64_t* res, const orc_nested* nested, uint64_t iterations,
-                         uint64_t spp, uint64_t seed, int32_t weight, double alpha, int32_t rr,
-                         float* out, float* approx_out, float* regions_out, float* replay_out);
+                         uint64_t spp, uint64_t seed, const orc_cv* cv, float* out, float* approx_out,
+                         float* regions_out, float* replay_out);
 
 /* Same per-bin Monte Carlo arithmetic over a contiguous slice of bins [bin_begin, bin_end),
  * on nthreads host threads (bins are independent once their seeds are drawn in bin order, as

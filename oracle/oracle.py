@@ -23,12 +23,26 @@ RULE = {"trapezoidal": 2, "simpson": 3, "boole": 5}
 HEUR = {"default": 0, "size": 1}
 METRIC = {"absolute": 0, "relative": 1}
 CV_OPTIMIZE, CV_FIXED = 0, 1
-RR_UNIFORM, RR_INTEGRAL, RR_ERROR = 0, 1, 2  # rr_uniform_region, rr_integral_region, rr_error_region
+RR_UNIFORM, RR_INTEGRAL, RR_ERROR, RR_PDF = 0, 1, 2, 3  # rr_{uniform,integral,error,pdf}_region
+# region_sampling_{uniform,importance,russian_roulette,mis}
+RS_UNIFORM, RS_IMPORTANCE, RS_RUSSIAN_ROULETTE, RS_MIS = 0, 1, 2, 3
+
+
+def replay_width(dim, sampling=RS_UNIFORM):
+    """Floats per residual sample of the oracle's replay records (orc_replay_width)."""
+    return 1 + dim + (1 if sampling == RS_RUSSIAN_ROULETTE else 1 + dim if sampling == RS_MIS else 0)
 MC_PER_BIN_PARALLEL, MC_PER_BIN_PARALLEL_SINGLE = 0, 1
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+class CvStrategy(ctypes.Structure):
+    """orc_cv: the control-variate integrator's residual strategy."""
+    _fields_ = [("weight", ctypes.c_int32), ("rr", ctypes.c_int32), ("alpha", ctypes.c_double),
+                ("rr_factor", ctypes.c_float), ("sampling", ctypes.c_int32), ("mis_power", ctypes.c_double),
+                ("mis_cutoff", ctypes.c_double)]
 
 
 class Nested(ctypes.Structure):
@@ -104,8 +118,8 @@ class Oracle:
         f = getattr(L, prefix + "control_variates")
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
-                      ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32,
-                      ctypes.c_double, ctypes.c_int32, _f32p, _f32p, _f32p, _f32p]
+                      ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                      ctypes.POINTER(CvStrategy), _f32p, _f32p, _f32p, _f32p]
 
     # ------------------------------------------------------------------ helpers
     @staticmethod
@@ -209,7 +223,8 @@ class Oracle:
         return float(out[0])
 
     def control_variates(self, kind, params, rmin, rmax, res, nested: Nested, iterations, spp, seed,
-                         weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False, rr=RR_UNIFORM):
+                         weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False, rr=RR_UNIFORM,
+                         sampling=RS_UNIFORM, rr_factor=0.01, mis_power=1.0, mis_cutoff=0.0):
         params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
         nb = int(np.prod(res))
         ch = self.channels(kind)
@@ -217,11 +232,13 @@ class Oracle:
         out = np.zeros(nb * ch, dtype=np.float32)
         ap = np.zeros(nb * ch, dtype=np.float32) if approx else None
         rg = np.zeros((iterations + 1) * 2 * dim, dtype=np.float32) if regions else None
-        width = (1 + dim) if self.prefix == "orc_" else dim
+        width = replay_width(dim, sampling) if self.prefix == "orc_" else dim
+        strategy = CvStrategy(weight, rr, alpha, rr_factor, sampling, mis_power, mis_cutoff)
         rp = np.zeros(nb * spp * width, dtype=np.float32) if replay else None
         rc = getattr(self.lib, self.prefix + "control_variates")(
             kind, _ptr(params), params.size, dim, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
-            ctypes.byref(nested), iterations, spp, seed, weight, alpha, rr, _ptr(out), _ptr(ap), _ptr(rg), _ptr(rp))
+            ctypes.byref(nested), iterations, spp, seed, ctypes.byref(strategy), _ptr(out), _ptr(ap), _ptr(rg),
+            _ptr(rp))
         self._check(rc, "control_variates")
         return {
             "bins": out.reshape(nb, ch),

@@ -173,9 +173,9 @@ int run_tolerance(const Fun& fun, const float* rmin, const float* rmax, const ui
     return 0;
 }
 
-template <class Fun, std::size_t DIM, std::size_t DB, class T, class Rule, class Heur, class RR, class CV>
+template <class Fun, std::size_t DIM, std::size_t DB, class T, class Rule, class Heur, class RR, class CV, class RS>
 int run_cv(const Fun& fun, const float* rmin, const float* rmax, const uint64_t* res, const Rule& rule,
-           const Heur& heur, uint64_t iters, uint64_t spp, uint64_t seed, RR rr, CV cv, float* out,
+           const Heur& heur, uint64_t iters, uint64_t spp, uint64_t seed, RR rr, CV cv, RS rs, float* out,
            float* regions_out, float* points) {
     Recorder rec{nullptr};
     RefF<Fun, DIM, T> f{&fun, &rec};
@@ -187,8 +187,8 @@ int run_cv(const Fun& fun, const float* rmin, const float* rmax, const uint64_t*
     auto bins = [&bs](const std::array<std::size_t, DB>& p) -> T& { return bs.v[bs.lin(p)]; };
     auto integrator = viltrum::integrator_region_based(
         viltrum::regions_generator_adaptive_heap(rule, heur, iters),
-        viltrum::regions_integrator_parallel_variance_reduction(std::move(rr), std::move(cv),
-                                                                viltrum::region_sampling_uniform(), std::mt19937(seed),
+        viltrum::regions_integrator_parallel_variance_reduction(std::move(rr), std::move(cv), std::move(rs),
+                                                                std::mt19937(seed),
                                                                 spp));
     RegionLogger logger;
     logger.regions_out = regions_out;
@@ -291,12 +291,34 @@ extern "C" int ref_per_bin_adaptive_nested(int32_t kind, const float* params, in
     return 9;
 }
 
-/* the residual's region choice, one of the reference's strategies */
-template <class Fn> int with_rr(int32_t rr, Fn&& fn) {
-    switch (rr) {
-    case ORC_RR_UNIFORM: return fn(viltrum::rr_uniform_region());
-    case ORC_RR_INTEGRAL: return fn(viltrum::rr_integral_region());
-    case ORC_RR_ERROR: return fn(viltrum::rr_error_region());
+/* the residual strategy, as the reference's own objects: the region choice (rr_uniform_region,
+ * rr_integral_region, rr_error_region, rr_pdf_region) and the point sampler (region_sampling_uniform,
+ * region_sampling_importance, region_sampling_russian_roulette, region_sampling_mis).  The point
+ * samplers other than uniform are built with the uniform or the pdf region choice only. */
+template <class Fn> int with_rr(const orc_cv& cv, Fn&& fn) {
+    using namespace viltrum;
+    const float fp = cv.rr_factor;
+    switch (cv.sampling) {
+    case ORC_RS_UNIFORM:
+        switch (cv.rr) {
+        case ORC_RR_UNIFORM: return fn(rr_uniform_region(), region_sampling_uniform());
+        case ORC_RR_INTEGRAL: return fn(rr_integral_region(), region_sampling_uniform());
+        case ORC_RR_ERROR: return fn(rr_error_region(), region_sampling_uniform());
+        case ORC_RR_PDF: return fn(rr_pdf_region(fp), region_sampling_uniform());
+        default: return 1;
+        }
+    case ORC_RS_IMPORTANCE:
+        if (cv.rr == ORC_RR_UNIFORM) return fn(rr_uniform_region(), region_sampling_importance());
+        if (cv.rr == ORC_RR_PDF) return fn(rr_pdf_region(fp), region_sampling_importance());
+        return 9;
+    case ORC_RS_RUSSIAN_ROULETTE:
+        if (cv.rr == ORC_RR_UNIFORM) return fn(rr_uniform_region(), region_sampling_russian_roulette());
+        if (cv.rr == ORC_RR_PDF) return fn(rr_pdf_region(fp), region_sampling_russian_roulette());
+        return 9;
+    case ORC_RS_MIS:
+        if (cv.rr == ORC_RR_UNIFORM) return fn(rr_uniform_region(), region_sampling_mis(cv.mis_power, cv.mis_cutoff));
+        if (cv.rr == ORC_RR_PDF) return fn(rr_pdf_region(fp), region_sampling_mis(cv.mis_power, cv.mis_cutoff));
+        return 9;
     default: return 1;
     }
 }
@@ -304,8 +326,8 @@ template <class Fn> int with_rr(int32_t rr, Fn&& fn) {
 extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n_params, int32_t dim,
                                     const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
                                     const orc_nested* nc, uint64_t iterations, uint64_t spp, uint64_t seed,
-                                    int32_t weight, double alpha, int32_t rr, float* out, float* approx_out,
-                                    float* regions_out, float* replay_out) {
+                                    const orc_cv* cv, float* out, float* approx_out, float* regions_out,
+                                    float* replay_out) {
     (void)approx_out;
     using namespace viltrum;
     const bool st_sr = nc->rule_hi == ORC_RULE_SIMPSON && nc->rule_lo == ORC_RULE_TRAPEZOIDAL &&
@@ -314,14 +336,14 @@ extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n
     auto hsr = error_heuristic_size(error_metric_relative(nc->min_val), nc->size_weight, nc->min_size);
     /* replay_out receives the recorded sample points only (spp x dim per bin); the chosen
      * region indices are internal to the reference */
-    return with_rr(rr, [&](auto rrs) -> int {
-        if (kind == vcu::VCU_F_MOVING_SCENE3 && dim == 3 && dimbins == 2 && weight == ORC_CV_OPTIMIZE) {
+    return with_rr(*cv, [&](auto rrs, auto rs) -> int {
+        if (kind == vcu::VCU_F_MOVING_SCENE3 && dim == 3 && dimbins == 2 && cv->weight == ORC_CV_OPTIMIZE) {
             auto* f = new vcu::MovingScene3;
             int r = f->build(params, n_params)
                         ? 3
                         : run_cv<vcu::MovingScene3, 3, 2, vrgb>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr,
-                                                                 iterations, spp, seed, rrs, cv_optimize_weight(), out,
-                                                                 regions_out, replay_out);
+                                                                 iterations, spp, seed, rrs, cv_optimize_weight(), rs,
+                                                                 out, regions_out, replay_out);
             delete f;
             return r;
         }
@@ -329,22 +351,22 @@ extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n
             auto* f = new vcu::Scene2;
             int r = 3;
             if (!f->build(params, n_params)) {
-                if (weight == ORC_CV_OPTIMIZE)
+                if (cv->weight == ORC_CV_OPTIMIZE)
                     r = run_cv<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr,
-                                                          iterations, spp, seed, rrs, cv_optimize_weight(), out,
+                                                          iterations, spp, seed, rrs, cv_optimize_weight(), rs, out,
                                                           regions_out, replay_out);
                 else
                     r = run_cv<vcu::Scene2, 2, 2, float>(*f, rmin, rmax, res, nested(simpson, trapezoidal), hsr,
-                                                          iterations, spp, seed, rrs, cv_fixed_weight(alpha), out,
-                                                          regions_out, replay_out);
+                                                          iterations, spp, seed, rrs, cv_fixed_weight(cv->alpha), rs,
+                                                          out, regions_out, replay_out);
             }
             delete f;
             return r;
         }
-        if (kind == vcu::VCU_F_POLY2 && dim == 2 && dimbins == 1 && weight == ORC_CV_OPTIMIZE) {
+        if (kind == vcu::VCU_F_POLY2 && dim == 2 && dimbins == 1 && cv->weight == ORC_CV_OPTIMIZE) {
             vcu::Poly2 f{};
             return run_cv<vcu::Poly2, 2, 1, float>(f, rmin, rmax, res, nested(simpson, trapezoidal), hsr, iterations,
-                                                    spp, seed, rrs, cv_optimize_weight(), out, regions_out,
+                                                    spp, seed, rrs, cv_optimize_weight(), rs, out, regions_out,
                                                     replay_out);
         }
         return 9;

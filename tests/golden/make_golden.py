@@ -102,7 +102,32 @@ CASES = [
                                                                        params=MOVING_SMALL, rmin=[0, 0, 0],
                                                                        rmax=[1, 1, 1], res=[8, 8], iterations=127,
                                                                        spp=16, seed=13, weight=0, alpha=1.0, rr=1)),
+    # the Simpson pdf of the control variate: rr_pdf_region (rr = 3) and the point samplers
+    # region_sampling_importance / _russian_roulette / _mis (sampling = 1 / 2 / 3)
+    ("cv_scene2_rrpdf_bins16x16_it127_spp8_seed14", "cv", dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0],
+                                                              rmax=[1, 1], res=[16, 16], iterations=127, spp=8,
+                                                              seed=14, weight=0, alpha=1.0, rr=3)),
+    ("cv_scene2_importance_rrpdf_fixed0_bins8x8_it63_spp8_seed15", "cv",
+     dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1], res=[8, 8], iterations=63, spp=8,
+          seed=15, weight=1, alpha=0.0, rr=3, sampling=1)),
+    ("cv_scene2_importance_bins16x16_it127_spp8_seed16", "cv",
+     dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1], res=[16, 16], iterations=127, spp=8,
+          seed=16, weight=0, alpha=1.0, sampling=1)),
+    ("cv_scene2_rrsampling_rrpdf_bins16x16_it127_spp8_seed17", "cv",
+     dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1], res=[16, 16], iterations=127, spp=8,
+          seed=17, weight=0, alpha=1.0, rr=3, sampling=2)),
+    ("cv_scene2_mis_p2_c005_bins16x16_it127_spp8_seed18", "cv",
+     dict(kind=scenes.SCENE2, params=SCENE_SMALL, rmin=[0, 0], rmax=[1, 1], res=[16, 16], iterations=127, spp=8,
+          seed=18, weight=0, alpha=1.0, sampling=3, mis_power=2.0, mis_cutoff=0.05)),
+    ("cv_moving3_rgb_importance_rrpdf_bins16x16_it255_spp16_seed19", "cv",
+     dict(kind=scenes.MOVING_SCENE3, params=MOVING_SMALL, rmin=[0, 0, 0], rmax=[1, 1, 1], res=[16, 16],
+          iterations=255, spp=16, seed=19, weight=0, alpha=1.0, rr=3, sampling=1)),
+    ("cv_poly2_mis_bins1_it16_spp64_seed20", "cv", dict(kind=scenes.POLY2, params=None, rmin=[0, 0], rmax=[1, 1],
+                                                        res=[1], iterations=16, spp=64, seed=20, weight=0, alpha=1.0,
+                                                        sampling=3)),
 ]
+
+CV_STRATEGY_KEYS = ("rr", "sampling", "mis_power", "mis_cutoff")
 
 CRESPO = ("simpson", "trapezoidal", "size", "relative")
 
@@ -213,10 +238,10 @@ def run(lib: orc.Oracle, method: str, kw: dict) -> dict:
         nested = orc.Nested.make(*CRESPO)
         r = lib.control_variates(kw["kind"], kw["params"], kw["rmin"], kw["rmax"], kw["res"], nested,
                                  kw["iterations"], kw["spp"], kw["seed"], kw["weight"], kw["alpha"], regions=True,
-                                 replay=True, rr=kw.get("rr", 0))
+                                 replay=True, **{k: kw[k] for k in CV_STRATEGY_KEYS if k in kw})
         pts = r["replay"]
         if lib.kind == "port":
-            pts = pts[:, :, 1:]
+            pts = pts[:, :, 1:1 + len(kw["rmin"])]
         else:
             fixed = np.empty_like(pts)
             fixed[visit_to_linear(kw["res"], int(kw["res"][0]) >= 4)] = pts

@@ -9,6 +9,13 @@ from conftest import golden_names, load_golden
 from oracle import oracle as orc
 
 
+def cv_strategy(g):
+    """The residual strategy a control-variate fixture was made with (uniform when absent)."""
+    out = {k: int(g[k]) for k in ("rr", "sampling") if k in g}
+    out.update({k: float(g[k]) for k in ("mis_power", "mis_cutoff") if k in g})
+    return out
+
+
 def _nested(g):
     hi, lo, heur, met = [str(x) for x in g["nested"]]
     return orc.Nested.make(hi, lo, heur, met)
@@ -33,10 +40,11 @@ def test_oracle_matches_reference_golden(port, name):
         r = port.control_variates(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"],
                                   orc.Nested.make("simpson", "trapezoidal", "size", "relative"), int(g["iterations"]),
                                   int(g["spp"]), int(g["seed"]), int(g["weight"]), float(g["alpha"]), regions=True,
-                                  replay=True, rr=int(g.get("rr", 0)))
+                                  replay=True, **cv_strategy(g))
         assert np.array_equal(r["bins"].view(np.uint32), g["out_bins"].view(np.uint32))
         assert np.array_equal(r["regions"].view(np.uint32), g["out_regions"].view(np.uint32))
-        assert np.array_equal(r["replay"][:, :, 1:].view(np.uint32), g["out_points"].view(np.uint32))
+        dim = len(g["rmin"])
+        assert np.array_equal(r["replay"][:, :, 1:1 + dim].view(np.uint32), g["out_points"].view(np.uint32))
     elif method == "global":
         out = port.adaptive_global(int(g["kind"]), params, g["rmin"], g["rmax"], g["res"], _nested(g), int(g["iterations"]),
                                    initial=g["initial"])

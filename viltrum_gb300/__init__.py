@@ -24,8 +24,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import scenes
-from ._lib import (MEM_DEVICE, MEM_HOST, RR_ERROR, RR_INTEGRAL, RR_UNIFORM, Context, Nested, VcuError,
-                   default_context, load)
+from ._lib import (MEM_DEVICE, MEM_HOST, RR_ERROR, RR_INTEGRAL, RR_PDF, RR_UNIFORM, RS_IMPORTANCE, RS_MIS,
+                   RS_RUSSIAN_ROULETTE, RS_UNIFORM, Context, Nested, VcuError, default_context, load)
 
 __all__ = [
     "Context", "VcuError", "Integrand", "Range", "integrate", "range_", "range_all", "range_primary",
@@ -34,7 +34,8 @@ __all__ = [
     "integrator_per_bin_parallel", "integrator_adaptive_iterations", "integrator_adaptive_iterations_parallel",
     "integrator_adaptive_tolerance",
     "scenes", "load",
-    "rr_uniform_region", "rr_integral_region", "rr_error_region", "region_sampling_uniform", "cv_optimize_weight",
+    "rr_uniform_region", "rr_integral_region", "rr_error_region", "rr_pdf_region", "region_sampling_uniform",
+    "region_sampling_importance", "region_sampling_russian_roulette", "region_sampling_mis", "cv_optimize_weight",
     "cv_fixed_weight", "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction",
     "integrator_region_based", "integrator_adaptive_variance_reduction_parallel", "integrator_crespo2021",
 ]
@@ -289,8 +290,41 @@ class rr_error_region:  # noqa: N801
 
 
 @dataclass(frozen=True)
+class rr_pdf_region:  # noqa: N801
+    """The residual's region chosen with probability proportional to the integral of its polynomial's
+    pdf over bin n region, floored at factor_prob of the mean weight; sample weight 1/probability
+    (region-russian-roulette.h:112-149).  Simpson high rule only."""
+    factor_prob: float = 0.01
+    code = RR_PDF
+
+
+@dataclass(frozen=True)
 class region_sampling_uniform:  # noqa: N801
     """Uniform point in bin n region, weight = its volume (region-sampling.h:9-20)."""
+    code = RS_UNIFORM
+
+
+@dataclass(frozen=True)
+class region_sampling_importance:  # noqa: N801
+    """Point drawn from the region polynomial's pdf over bin n region (uniform when that range's volume
+    is below 1e-5), weight 1/pdf (region-sampling.h:22-43).  Simpson high rule only."""
+    code = RS_IMPORTANCE
+
+
+@dataclass(frozen=True)
+class region_sampling_russian_roulette:  # noqa: N801
+    """Pdf point or uniform point, chosen by the pdf's integral against the volume; weight 1/pdf of the
+    strategy taken (region-sampling.h:47-81).  Simpson high rule only."""
+    code = RS_RUSSIAN_ROULETTE
+
+
+@dataclass(frozen=True)
+class region_sampling_mis:  # noqa: N801
+    """Pdf point kept or replaced by a uniform one with the power heuristic's probabilities
+    (region-sampling.h:84-135).  Simpson high rule only."""
+    power: float = 1.0
+    cutoff: float = 0.0
+    code = RS_MIS
 
 
 @dataclass(frozen=True)
@@ -348,11 +382,13 @@ def regions_integrator_parallel_variance_reduction(rr, cv, *args) -> VarianceRed
         sampling, (samples, seed) = region_sampling_uniform(), args
     else:
         raise TypeError("regions_integrator_parallel_variance_reduction(rr, cv, [sampling,] ...)")
-    if not isinstance(rr, (rr_uniform_region, rr_integral_region, rr_error_region)):
-        raise NotImplementedError("the CUDA control variates implement rr_uniform_region, rr_integral_region and "
-                                  "rr_error_region")
-    if not isinstance(sampling, region_sampling_uniform):
-        raise NotImplementedError("the CUDA control variates implement region_sampling_uniform")
+    if not isinstance(rr, (rr_uniform_region, rr_integral_region, rr_error_region, rr_pdf_region)):
+        raise NotImplementedError("the CUDA control variates implement rr_uniform_region, rr_integral_region, "
+                                  "rr_error_region and rr_pdf_region")
+    if not isinstance(sampling, (region_sampling_uniform, region_sampling_importance,
+                                 region_sampling_russian_roulette, region_sampling_mis)):
+        raise NotImplementedError("the CUDA control variates implement region_sampling_uniform, _importance, "
+                                  "_russian_roulette and _mis")
     return VarianceReduction(rr, cv, sampling, int(seed), int(samples))
 
 
@@ -485,7 +521,9 @@ def _run_cv(rb: RegionBased, bins, res, f, rng, logger, ctx, device_bins, replay
     flat = (not device_bins and isinstance(bins, np.ndarray) and bins.ndim == 1 and bins.dtype == np.float32
             and bins.size == nb * ch and bins.flags.c_contiguous)
     out = bins if (device_bins or flat) else np.empty(nb * ch, dtype=np.float32)
-    opts = CvOpts(vr.samples, vr.seed, 1 if vr.cv.fixed else 0, 0, float(vr.cv.alpha), vr.rr.code)
+    opts = CvOpts(vr.samples, vr.seed, 1 if vr.cv.fixed else 0, 0, float(vr.cv.alpha), vr.rr.code, vr.sampling.code,
+                  float(getattr(vr.rr, "factor_prob", 0.01)), 0, float(getattr(vr.sampling, "power", 1.0)),
+                  float(getattr(vr.sampling, "cutoff", 0.0)))
     stats = ctx.control_variates(p, _nested_struct(g.rule, g.heuristic), g.iterations, opts, out, approximation,
                                  regions, replay)
     if not device_bins and not flat:

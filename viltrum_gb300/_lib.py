@@ -24,10 +24,17 @@ FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
 EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
            "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested",
            "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
-           "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global", "vcu_adaptive_tolerance"]
+           "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global", "vcu_adaptive_tolerance",
+           "vcu_cv_replay_width"]
 BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
 CV_OPTIMIZE, CV_FIXED = 0, 1
-RR_UNIFORM, RR_INTEGRAL, RR_ERROR = 0, 1, 2  # residual region choice
+RR_UNIFORM, RR_INTEGRAL, RR_ERROR, RR_PDF = 0, 1, 2, 3  # residual region choice
+RS_UNIFORM, RS_IMPORTANCE, RS_RUSSIAN_ROULETTE, RS_MIS = 0, 1, 2, 3  # residual point sampling
+
+
+def cv_replay_width(dim: int, sampling: int = RS_UNIFORM) -> int:
+    """Floats per residual sample of vcu_control_variates' replay records."""
+    return 1 + dim + (1 if sampling == RS_RUSSIAN_ROULETTE else 1 + dim if sampling == RS_MIS else 0)
 
 
 class VcuError(RuntimeError):
@@ -64,7 +71,8 @@ class Stats(ctypes.Structure):
 class CvOpts(ctypes.Structure):
     _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("weight", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double), ("rr", ctypes.c_int32),
-                ("reserved2", ctypes.c_int32)]
+                ("sampling", ctypes.c_int32), ("rr_factor", ctypes.c_float), ("reserved2", ctypes.c_int32),
+                ("mis_power", ctypes.c_double), ("mis_cutoff", ctypes.c_double)]
 
 
 class LearnedOpts(ctypes.Structure):

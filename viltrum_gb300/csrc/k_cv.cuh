@@ -33,6 +33,7 @@
 
 #include "vcu_heap.h"
 #include "vcu_internal.cuh"
+#include "vcu_pdf.cuh"
 #include "vcu_rules.cuh"
 
 namespace vcu {
@@ -479,7 +480,11 @@ struct ResCfg {
     int32_t weight; /* VCU_CV_OPTIMIZE / VCU_CV_FIXED */
     double alpha;
     const float* approx_init; /* nullable: the approximation starts from these bin values */
-    int32_t rr;               /* VCU_RR_UNIFORM / VCU_RR_INTEGRAL / VCU_RR_ERROR */
+    int32_t rr;               /* VCU_RR_UNIFORM / VCU_RR_INTEGRAL / VCU_RR_ERROR / VCU_RR_PDF */
+    int32_t sampling;         /* VCU_RS_UNIFORM / VCU_RS_IMPORTANCE / VCU_RS_RUSSIAN_ROULETTE / VCU_RS_MIS */
+    float rr_factor;          /* VCU_RR_PDF: floor of the weights, a fraction of their mean */
+    uint32_t rec_w;           /* floats per replayed sample */
+    double mis_power, mis_cutoff;
     const float* rerr;        /* VCU_RR_ERROR: norm of each heap region's error estimate */
     double* cdf;              /* importance choice, per list entry: cumulative probability */
     double* rrf;              /* importance choice, per list entry: 1 / probability */
@@ -581,7 +586,7 @@ __device__ __forceinline__ float norm1(const float* v, int ch) {
     return s;
 }
 
-template <class F, int DIM, int S>
+template <class F, int DIM, int S, bool PDF>
 __global__ void __launch_bounds__(RES_WARPS * 32)
     k_cv_residual(const __grid_constant__ F f, const ResCfg cfg, const uint32_t* __restrict__ offsets,
                   const uint32_t* __restrict__ lists, const int* __restrict__ heap_pay, const float* __restrict__ vals,
@@ -590,7 +595,39 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
                   uint32_t* __restrict__ status) {
     constexpr int CH = F::CH;
     constexpr int SD = ipow(S, DIM);
+    static_assert(!PDF || S == 3, "the pdf of a region exists for Simpson's rule only");
     __shared__ float stage[RES_WARPS][RES_CHUNK][CH];
+    /* the pdf of region id over bin n region [A,B] (region.h:267-290), and at an absolute point x
+     * (pdf_subrange, region.h:326-331); NV holds 3^DIM node norms, overwritten */
+    float NV[PDF ? SD : 1], MV[PDF ? SD / 3 + 1 : 1];
+    auto load_norms = [&](int id) {
+        if constexpr (PDF) {
+#pragma unroll 1
+            for (int i = 0; i < SD; ++i) NV[i] = norm1(vals + ((size_t)id * SD + i) * CH, CH);
+        }
+    };
+    auto pdf_integral = [&](int id, const float* A, const float* B) -> float {
+        if constexpr (PDF) {
+            load_norms(id);
+            return vmul(rvol[id], pdf3::Region<DIM>::integral(NV, A, B));
+        } else {
+            return 0.0f;
+        }
+    };
+    auto pdf_at = [&](int id, const float* A, const float* B, const float* x) -> float {
+        if constexpr (PDF) {
+            float P[DIM];
+            for (int d = 0; d < DIM; ++d) {
+                const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
+                P[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));
+            }
+            load_norms(id);
+            const float at = pdf3::Region<DIM>::at(NV, P);
+            return vdiv(at, pdf_integral(id, A, B));
+        } else {
+            return 0.0f;
+        }
+    };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint64_t bin = (uint64_t)blockIdx.x * RES_WARPS + warp;
     if (bin >= cfg.nbins) return;
@@ -643,6 +680,8 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
                 cfg.cdf[off + base + i] = empty ? 0.0 : (double)norm1(stage[warp][i], CH);
             else if (cfg.rr == VCU_RR_ERROR) /* norm(error) * volume(bin n region) / volume(region) */
                 cfg.cdf[off + base + i] = (double)vdiv(vmul(cfg.rerr[lists[off + base + i]], v), rvol[id]);
+            else if (cfg.rr == VCU_RR_PDF) /* the pdf's integral over bin n region */
+                cfg.cdf[off + base + i] = empty ? 0.0 : (double)pdf_integral(id, A, B);
         }
         __syncwarp();
         if (lane == 0)
@@ -661,8 +700,9 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         approx[c] = __shfl_sync(0xffffffffu, approx[c], 0);
         approx_d[c] = (double)approx[c];
     }
-    /* importance choice among the bin's regions (region-russian-roulette.h:30-108): weights floored at
-     * 1% of their mean (all 1 when they sum to <= 0), then std::discrete_distribution's normalised
+    /* importance choice among the bin's regions (region-russian-roulette.h:30-149): weights floored at
+     * 1% (rr_pdf_region: its factor) of their mean (all 1 when they sum to <= 0), then
+     * std::discrete_distribution's normalised
      * probabilities and their running sum, the last set to 1.  The sums are warp-parallel in FP64, so
      * they can differ from the sequential ones in the last bits. */
     if (cfg.rr != VCU_RR_UNIFORM && n > 0) {
@@ -674,7 +714,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         double s1 = 0.0;
         for (uint32_t i = lane; i < n; i += 32) s1 += W[i];
         s1 = warp_sum(s1);
-        const double floor_w = 0.01 * s1 / (double)n;
+        const double floor_w = (cfg.rr == VCU_RR_PDF ? (double)cfg.rr_factor : 0.01) * s1 / (double)n;
         auto clamped = [&](double w) { return (s1 <= 0.0) ? 1.0 : (w < floor_w ? floor_w : w); };
         double s2 = 0.0;
         for (uint32_t i = lane; i < n; i += 32) s2 += clamped(W[i]);
@@ -711,8 +751,33 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
         float a[DIM], b[DIM], A[DIM], B[DIM], v;
         bool empty;
+        float sfac; /* the point's weight: volume(bin n region) for a uniform point, else 1/pdf */
+        /* region_sampling_mis's weight from the importance point's pdf (region-sampling.h:93-135);
+         * also whether the uniform point is taken for a draw rr_u */
+        auto mis_weight = [&](float pdf_imp, float vol, float rr_u, bool& uniform) -> float {
+            const float pdf_uni = vdiv(1.0f, vol);
+            float mis_imp = __double2float_rn(pow((double)pdf_imp, cfg.mis_power));
+            float mis_uni = __double2float_rn(pow((double)pdf_uni, cfg.mis_power));
+            float mis_sum = vadd(mis_imp, mis_uni);
+            if ((double)mis_imp < cfg.mis_cutoff * (double)mis_sum) {
+                mis_imp = 0.0f;
+                mis_sum = mis_uni;
+            }
+            if ((double)mis_uni < cfg.mis_cutoff * (double)mis_sum) {
+                mis_uni = 0.0f;
+                mis_sum = mis_imp;
+            }
+            const float p_imp = ((double)pdf_imp > 1.e-10) ? vdiv(mis_imp, pdf_imp) : 0.0f;
+            const float p_uni = vmul(mis_uni, vol);
+            const float p_sum = vadd(p_imp, p_uni);
+            uniform = rr_u < vdiv(p_uni, p_sum);
+            return vdiv(p_sum, mis_sum);
+        };
+        auto inv_pdf = [&](float pdf, double eps) -> float {
+            return ((double)pdf < eps) ? 0.0f : __double2float_rn(__ddiv_rn(1.0, (double)pdf));
+        };
         if (replay) {
-            const float* rec = replay + (bin * cfg.spp + j) * (1 + DIM);
+            const float* rec = replay + (bin * cfg.spp + j) * cfg.rec_w;
             chosen = (uint32_t)rec[0];
             if (chosen >= n) {
                 atomicOr(status, VCU_FLAG_OVERFLOW);
@@ -721,6 +786,17 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             const int id = heap_pay[lists[off + chosen]] & 0xffffff;
             isect(id, a, b, A, B, v, empty);
             for (int d = 0; d < DIM; ++d) x[d] = rec[1 + d];
+            sfac = v;
+            if constexpr (PDF) {
+                if (cfg.sampling == VCU_RS_IMPORTANCE) {
+                    if (!((double)v < 1.e-5)) sfac = inv_pdf(pdf_at(id, A, B, x), 1.e-5);
+                } else if (cfg.sampling == VCU_RS_RUSSIAN_ROULETTE) {
+                    sfac = inv_pdf(rec[1 + DIM] != 0.0f ? pdf_at(id, A, B, x) : vdiv(1.0f, v), 1.e-10);
+                } else if (cfg.sampling == VCU_RS_MIS) {
+                    bool uni;
+                    sfac = mis_weight(pdf_at(id, A, B, rec + 2 + DIM), v, 0.0f, uni);
+                }
+            }
         } else {
             const U4 r0 = philox4x32_10(U4{(uint32_t)j, blo, bhi, 0xC0DE0000u}, cfg.k0, cfg.k1);
             if (cfg.rr == VCU_RR_UNIFORM) {
@@ -740,6 +816,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             const int id = heap_pay[lists[off + chosen]] & 0xffffff;
             isect(id, a, b, A, B, v, empty);
             const uint32_t rr[3] = {r0.y, r0.z, r0.w};
+            float u[DIM];
             for (int d = 0; d < DIM; ++d) {
                 uint32_t bits;
                 if (d < 3) bits = rr[d];
@@ -749,7 +826,51 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
                     const uint32_t q[4] = {r1.x, r1.y, r1.z, r1.w};
                     bits = q[(d - 3) % 4];
                 }
-                x[d] = vadd(vmul(u01(bits), vsub(b[d], a[d])), a[d]);
+                u[d] = u01(bits);
+                x[d] = vadd(vmul(u[d], vsub(b[d], a[d])), a[d]);
+            }
+            sfac = v;
+            if constexpr (PDF) {
+                if (cfg.sampling != VCU_RS_UNIFORM) {
+                    const int id = heap_pay[lists[off + chosen]] & 0xffffff;
+                    const float rr_u =
+                        u01(philox4x32_10(U4{(uint32_t)j, blo, bhi, 0xC0DE1000u}, cfg.k0, cfg.k1).z);
+                    /* a point drawn from the region's pdf over bin n region (region.h:241-257) */
+                    auto importance_point = [&](float* xx) {
+                        float sol[DIM];
+                        load_norms(id);
+                        pdf3::Region<DIM>::sample(NV, MV, u, A, B, sol);
+                        for (int d = 0; d < DIM; ++d) {
+                            const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
+                            xx[d] = vadd(vmul(sol[d], vsub(rmx, rmn)), rmn);
+                        }
+                    };
+                    auto uniform_point = [&]() {
+                        for (int d = 0; d < DIM; ++d) x[d] = vadd(a[d], vmul(u[d], vsub(b[d], a[d])));
+                    };
+                    if (cfg.sampling == VCU_RS_IMPORTANCE) { /* region-sampling.h:22-43 */
+                        if (!((double)v < 1.e-5)) {
+                            importance_point(x);
+                            sfac = inv_pdf(pdf_at(id, A, B, x), 1.e-5);
+                        }
+                    } else if (cfg.sampling == VCU_RS_RUSSIAN_ROULETTE) { /* :47-81 */
+                        const float pdf_imp = pdf_integral(id, A, B);
+                        float pdf;
+                        if (rr_u < vdiv(pdf_imp, vadd(pdf_imp, v))) {
+                            importance_point(x);
+                            pdf = pdf_at(id, A, B, x);
+                        } else {
+                            uniform_point();
+                            pdf = vdiv(1.0f, v);
+                        }
+                        sfac = inv_pdf(pdf, 1.e-10);
+                    } else { /* region_sampling_mis, :84-135 */
+                        importance_point(x);
+                        bool uni;
+                        sfac = mis_weight(pdf_at(id, A, B, x), v, rr_u, uni);
+                        if (uni) uniform_point();
+                    }
+                }
             }
         }
         const int id = heap_pay[lists[off + chosen]] & 0xffffff;
@@ -760,16 +881,16 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             p[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));
         }
         for (int c = 0; c < CH; ++c) gv[c] = poly_at<DIM, S, CH>(vals + (size_t)id * SD * CH, c, p);
-        /* sample weights: prod(res) * 1/P(region) (n for the uniform choice) * volume(bin n region) */
+        /* sample weights: prod(res) * 1/P(region) (n for the uniform choice) * the point's weight */
         const double rrf = (cfg.rr == VCU_RR_UNIFORM) ? (double)n : cfg.rrf[off + chosen];
         float fs[CH], as[CH];
         for (int c = 0; c < CH; ++c) {
             if (CH == 1) {
-                fs[c] = __double2float_rn((double)fv[c] * cfg.factor * rrf * (double)v);
-                as[c] = __double2float_rn((double)gv[c] * cfg.factor * rrf * (double)v);
-            } else { /* per channel: scales by double rounded to float, then the float volume */
-                fs[c] = vmul(__double2float_rn((double)__double2float_rn((double)fv[c] * cfg.factor) * rrf), v);
-                as[c] = vmul(__double2float_rn((double)__double2float_rn((double)gv[c] * cfg.factor) * rrf), v);
+                fs[c] = __double2float_rn((double)fv[c] * cfg.factor * rrf * (double)sfac);
+                as[c] = __double2float_rn((double)gv[c] * cfg.factor * rrf * (double)sfac);
+            } else { /* per channel: scales by double rounded to float, then the float point weight */
+                fs[c] = vmul(__double2float_rn((double)__double2float_rn((double)fv[c] * cfg.factor) * rrf), sfac);
+                as[c] = vmul(__double2float_rn((double)__double2float_rn((double)gv[c] * cfg.factor) * rrf), sfac);
             }
             float y = vsub(fs[c], cf32[c]);
             float t = vadd(sf32[c], y);
@@ -952,10 +1073,25 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
             rcfg.rerr = rerr;
         }
     }
+    rcfg.sampling = cv.sampling;
+    rcfg.rr_factor = cv.rr_factor;
+    rcfg.mis_power = cv.mis_power;
+    rcfg.mis_cutoff = cv.mis_cutoff;
+    rcfg.rec_w = (uint32_t)vcu_cv_replay_width(DIM, cv.sampling);
     const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
-    k_cv_residual<F, DIM, S><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(f, rcfg, off, lists, hp, vals, rmin, rmax,
-                                                                          vol, d_replay, d_bins, d_approx,
-                                                                          ctx->d_status);
+    const bool pdf = cv.rr == VCU_RR_PDF || cv.sampling != VCU_RS_UNIFORM;
+    if constexpr (S == 3) {
+        if (pdf)
+            k_cv_residual<F, DIM, S, true><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(
+                f, rcfg, off, lists, hp, vals, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
+        else
+            k_cv_residual<F, DIM, S, false><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(
+                f, rcfg, off, lists, hp, vals, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
+    } else {
+        if (pdf) return fail(ctx, VCU_UNSUPPORTED, "the pdf strategies need a Simpson high rule");
+        k_cv_residual<F, DIM, S, false><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(
+            f, rcfg, off, lists, hp, vals, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
+    }
     ++launches;
     if (d_regions) {
         k_cv_regions_out<<<(unsigned)((nheap + 255) / 256), 256, 0, ctx->stream>>>(hp, rmin, rmax, DIM, (int)nheap,

@@ -393,6 +393,10 @@ extern "C" int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, c
     return scope.end(evals, g.nbins * (iterations + 1));
 }
 
+extern "C" int vcu_cv_replay_width(int32_t dim, int32_t sampling) {
+    return 1 + dim + (sampling == VCU_RS_RUSSIAN_ROULETTE ? 1 : sampling == VCU_RS_MIS ? 1 + dim : 0);
+}
+
 extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested, uint64_t iterations,
                                     const vcu_cv* cv, const float* replay, float* bins, float* approximation,
                                     float* regions, vcu_stats* stats) {
@@ -405,8 +409,11 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     if (cv->samples_per_bin > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "samples per bin must be < 2^32");
     if (cv->weight != VCU_CV_OPTIMIZE && cv->weight != VCU_CV_FIXED) return fail(ctx, VCU_INVALID_ARG, "unknown weight");
     if (cv->reserved != 0 || cv->reserved2 != 0) return fail(ctx, VCU_INVALID_ARG, "vcu_cv::reserved must be 0");
-    if (cv->rr != VCU_RR_UNIFORM && cv->rr != VCU_RR_INTEGRAL && cv->rr != VCU_RR_ERROR)
-        return fail(ctx, VCU_INVALID_ARG, "unknown residual region choice");
+    if (cv->rr < VCU_RR_UNIFORM || cv->rr > VCU_RR_PDF) return fail(ctx, VCU_INVALID_ARG, "unknown residual region choice");
+    if (cv->sampling < VCU_RS_UNIFORM || cv->sampling > VCU_RS_MIS)
+        return fail(ctx, VCU_INVALID_ARG, "unknown residual point sampling");
+    if ((cv->rr == VCU_RR_PDF || cv->sampling != VCU_RS_UNIFORM) && nested->rule_hi != VCU_RULE_SIMPSON)
+        return fail(ctx, VCU_UNSUPPORTED, "the pdf strategies need a Simpson high rule (rules.h:102-248)");
     if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
         return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
     if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
@@ -425,7 +432,7 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
         dapprox = approximation ? reinterpret_cast<float*>(o + ((bbytes + 255) & ~size_t(255))) : nullptr;
         dregions = regions ? reinterpret_cast<float*>(o + 2 * ((bbytes + 255) & ~size_t(255))) : nullptr;
         if (replay) {
-            const size_t pbytes = g.nbins * cv->samples_per_bin * (1 + p->dim) * 4;
+            const size_t pbytes = g.nbins * cv->samples_per_bin * (size_t)vcu_cv_replay_width(p->dim, cv->sampling) * 4;
             if ((rc = ensure(ctx, ctx->in, pbytes))) return rc;
             VCU_CUDA(ctx, cudaMemcpyAsync(ctx->in.ptr, replay, pbytes, cudaMemcpyHostToDevice, ctx->stream));
             dreplay = static_cast<const float*>(ctx->in.ptr);
