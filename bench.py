@@ -365,7 +365,80 @@ def other_configs(ctx, args) -> dict:
         "cpu_baseline": {"gsamples_s": round(cpu_evals / batch_cpu_s / 1e9, 4), "cores": threads, "kind": "port",
                          "sample": f"64 random items of at most 3 M evaluations ({cpu_evals} evaluations) in "
                                    f"{batch_cpu_s:.1f} s"}}
+    out.update(adaptive_forms(ctx, port))
     out["learned_vs_plain"] = time_to_rmse(ctx)
+    return out
+
+
+def adaptive_forms(ctx, port) -> dict:
+    """The other forms of the path, one line each: integrator_adaptive_iterations used directly (one
+    heap over the range), the tolerance-driven form, and the control variates' importance strategies
+    (rr_pdf_region + region_sampling_importance against the uniform choices, equal samples)."""
+    from oracle import oracle as orc
+    from viltrum_gb300 import _lib, scenes
+
+    out = {}
+    params = scenes.scene2(SEED)
+    res = [512, 512]
+    exact = scenes.exact_bins(scenes.SCENE2, params, [0, 0], [1, 1], res)
+    p = ctx.problem(scenes.SCENE2, params, [0, 0], [1, 1], res)
+    b = np.zeros(512 * 512, np.float32)
+    # -- one heap of 2^18 regions over the whole range, accumulated into 512x512 bins
+    st_abs = _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37)
+    splits = (1 << 18) - 1
+
+    def glob():
+        b[:] = 0.0
+        return ctx.adaptive_iterations_global(p, st_abs, splits, b)
+
+    ms, st = _median_ms(glob, reps=3, warmup=3)
+    t0 = time.perf_counter()
+    port.adaptive_global(scenes.SCENE2, params, [0, 0], [1, 1], res, orc.Nested.make("simpson", "trapezoidal"), splits)
+    cpu_s = time.perf_counter() - t0
+    out["adaptive_global"] = {
+        "workload": "integrator_adaptive_iterations(nested(simpson,trapezoidal), 2^18-1) used directly: one heap over "
+                    "the 2-D scene, regions added into 512x512 bins",
+        "ms": round(ms, 2), "regions": int(st.regions), "evaluations": int(st.evaluations),
+        "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact), "timing": "median of 3 after 3 warm-up, device",
+        "cpu_baseline": {"ms": round(cpu_s * 1e3, 1), "cores": 1, "kind": "port",
+                         "sample": "the whole workload"}}
+    # -- tolerance-driven: every region split until its error is below 1e-9
+    bs_abs = _lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37)
+    leaves = [0]
+
+    def tol():
+        b[:] = 0.0
+        st_, n = ctx.adaptive_tolerance(p, bs_abs, 1e-9, b)
+        leaves[0] = n
+        return st_
+
+    ms, st = _median_ms(tol, reps=3, warmup=3)
+    t0 = time.perf_counter()
+    _, cpu_leaves = port.adaptive_tolerance(scenes.SCENE2, params, [0, 0], [1, 1], res,
+                                            orc.Nested.make("boole", "simpson"), 1e-9)
+    cpu_s = time.perf_counter() - t0
+    out["adaptive_tolerance"] = {
+        "workload": "integrator_adaptive_tolerance(nested(boole,simpson), 1e-9) over the 2-D scene into 512x512 bins",
+        "ms": round(ms, 2), "leaf_regions": int(leaves[0]), "evaluations": int(st.evaluations),
+        "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact), "timing": "median of 3 after 3 warm-up, device",
+        "cpu_baseline": {"ms": round(cpu_s * 1e3, 1), "cores": 1, "kind": "port", "leaf_regions": int(cpu_leaves),
+                         "sample": "the whole workload"}}
+    # -- the residual's region and point from the control variate's pdf, against the uniform ones
+    res = [128, 128]
+    exact = scenes.exact_bins(scenes.WAVE2, None, [0, 0], [1, 1], res)
+    p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], res)
+    crespo = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+    b = np.empty(128 * 128, np.float32)
+    lines = {}
+    for name, rr, rs in (("uniform", 0, 0), ("rr_pdf_importance", 3, 1)):
+        opts = _lib.CvOpts(16, 3, 1, 0, 0.0, rr, rs, 0.01, 0, 1.0, 0.0)
+        ms, st = _median_ms(lambda: ctx.control_variates(p, crespo, (1 << 12) - 1, opts, b), reps=3, warmup=3)
+        lines[name] = {"ms": round(ms, 3), "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact)}
+    out["cv_importance"] = {
+        "workload": "regions_integrator_parallel_variance_reduction(rr, cv_fixed_weight(0), sampler, 16 spp) over "
+                    "2^12 regions of wave2, 128x128 bins: rr_uniform_region + region_sampling_uniform against "
+                    "rr_pdf_region + region_sampling_importance",
+        **lines, "timing": "median of 3 after 3 warm-up, device"}
     return out
 
 

@@ -163,7 +163,12 @@ int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_ne
  * |region error| x its share of volume in the bin, or to the integral of the region's pdf over bin
  * n region, floored at 1% (rr_factor) of the mean weight; point uniform in bin n region or drawn
  * from the pdf of the region's polynomial -- Simpson high rule only).  The result is ASSIGNED to the
- * bins.
+ * bins.  With fubini_dims = 2 (nested(simpson, trapezoidal), integrands of 3+ dimensions, at most 2
+ * binned): integrator_crespo2021_infinite<2> / integrator_adaptive_fubini_variance_reduction_parallel<2>
+ * (integrator-crespo2021.h:24-44, integrator-adaptive-fubini-variance-reduction.h:28-41): the regions
+ * span dimensions 0-1 and every evaluation integrates the others by Monte Carlo (tail_samples Philox
+ * points for the region nodes, one for a residual sample); replay records and region ranges then
+ * have 2 coordinates.
  * Residual sample j of bin b draws from Philox4x32-10 unless `replay` is given: nbins x samples x
  * vcu_cv_replay_width(dim, sampling) floats (index of the chosen region in the bin's list, then the
  * point, ...), e.g. the reference's own draws.  approximation (nullable) receives the
@@ -182,6 +187,8 @@ typedef struct vcu_cv {
     int32_t reserved2;        /* 0                                                      */
     double mis_power;         /* VCU_RS_MIS: region_sampling_mis(power, cutoff)        */
     double mis_cutoff;
+    int32_t fubini_dims;      /* 0, or 2: regions over the first 2 dimensions only     */
+    uint32_t tail_samples;    /* fubini_dims 2: Monte Carlo samples per evaluation     */
 } vcu_cv;
 
 /* floats per residual sample in vcu_control_variates' replay records: the chosen list index and

@@ -353,6 +353,8 @@ class control_variates {
     int rr_, sampling_;
     float rr_factor_;
     double mis_power_, mis_cutoff_;
+    int fubini_dims_ = 0;
+    unsigned tail_samples_ = 0;
 
 public:
     /* rr: VCU_RR_UNIFORM (rr_uniform_region), VCU_RR_INTEGRAL (rr_integral_region), VCU_RR_ERROR
@@ -365,6 +367,15 @@ public:
                      double mis_cutoff = 0.0)
         : rule_(r), iterations_(iterations), samples_(samples), seed_(seed), weight_(weight), alpha_(alpha),
           rr_(rr), sampling_(sampling), rr_factor_(rr_factor), mis_power_(mis_power), mis_cutoff_(mis_cutoff) {}
+
+    /* regions over the first `dims` (2) dimensions only, the others integrated by `tail_samples` Monte
+     * Carlo samples in every evaluation: regions_generator_fubini<2>(..., monte_carlo(tail_samples, ...))
+     * (src/combination/regions-generator-fubini.h:7-28) */
+    control_variates& fubini(int dims, unsigned tail_samples) {
+        fubini_dims_ = dims;
+        tail_samples_ = tail_samples;
+        return *this;
+    }
 
     template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>
     void integrate(Bins& bins, const std::array<std::size_t, DIMBINS>& res, const F& f, const R& range,
@@ -385,6 +396,8 @@ public:
         cv.rr_factor = rr_factor_;
         cv.mis_power = mis_power_;
         cv.mis_cutoff = mis_cutoff_;
+        cv.fubini_dims = fubini_dims_;
+        cv.tail_samples = tail_samples_;
         vcu_stats st{};
         ctx.check(vcu_control_variates(ctx.get(), &p, &rule_.n, iterations_, &cv, nullptr, out.data(), nullptr,
                                        nullptr, &st));
@@ -398,6 +411,12 @@ public:
 inline nested_rule crespo2021_rule() { return simpson_trapezoidal(VCU_HEUR_SIZE, VCU_METRIC_RELATIVE); }
 inline control_variates crespo2021(unsigned long iterations, unsigned long samples, std::uint64_t seed = 0) {
     return control_variates(crespo2021_rule(), iterations, samples, seed);
+}
+/* integrator_crespo2021_infinite<2>(iterations, mc_samples, spp, seed) over a finite range
+ * (src/control-variates/integrator-crespo2021.h:24-44) */
+inline control_variates crespo2021_infinite(unsigned long iterations, unsigned mc_samples, unsigned long samples,
+                                            std::uint64_t seed = 0) {
+    return control_variates(crespo2021_rule(), iterations, samples, seed).fubini(2, mc_samples);
 }
 
 /* ---------------------------------------------------------------- learned control variate */

@@ -38,6 +38,7 @@ __all__ = [
     "region_sampling_importance", "region_sampling_russian_roulette", "region_sampling_mis", "cv_optimize_weight",
     "cv_fixed_weight", "regions_generator_adaptive_heap", "regions_integrator_parallel_variance_reduction",
     "integrator_region_based", "integrator_adaptive_variance_reduction_parallel", "integrator_crespo2021",
+    "regions_generator_fubini", "integrator_crespo2021_infinite", "integrator_adaptive_fubini_variance_reduction_parallel",
 ]
 
 
@@ -374,6 +375,23 @@ def regions_generator_adaptive_heap(rule: NestedRule, heuristic, iterations: int
     return AdaptiveHeapGenerator(rule, heuristic, int(iterations))
 
 
+@dataclass
+class FubiniGenerator:
+    """regions_generator_fubini<N>(generator, monte_carlo(samples, seed)) (regions-generator-fubini.h:7-28):
+    regions over the first N dimensions, the others integrated by Monte Carlo in every evaluation."""
+    dims: int
+    generator: AdaptiveHeapGenerator
+    rest: MonteCarlo
+
+
+def regions_generator_fubini(dims: int, generator: AdaptiveHeapGenerator, rest) -> FubiniGenerator:
+    if not isinstance(rest, MonteCarlo):
+        raise NotImplementedError("the CUDA Fubini tail integrates the remaining dimensions by monte_carlo(n, seed)")
+    if int(dims) != 2:
+        raise NotImplementedError("the CUDA Fubini tail takes regions over the first 2 dimensions")
+    return FubiniGenerator(int(dims), generator, rest)
+
+
 def regions_integrator_parallel_variance_reduction(rr, cv, *args) -> VarianceReduction:
     """(rr, cv, sampling, seed, samples) or (rr, cv, samples, seed) as the reference's overloads."""
     if len(args) == 3:
@@ -392,8 +410,31 @@ def regions_integrator_parallel_variance_reduction(rr, cv, *args) -> VarianceRed
     return VarianceReduction(rr, cv, sampling, int(seed), int(samples))
 
 
-def integrator_region_based(generator: AdaptiveHeapGenerator, integrator: VarianceReduction) -> RegionBased:
+def integrator_region_based(generator, integrator: VarianceReduction) -> RegionBased:
     return RegionBased(generator, integrator)
+
+
+def integrator_crespo2021_infinite(dims: int, iterations: int, mc_samples: int, spp: int, seed: int = 0) -> RegionBased:
+    """integrator_crespo2021_infinite<dims>(iterations, mc_samples, spp, seed) (integrator-crespo2021.h:24-44)
+    over a finite range: crespo2021's regions over the first `dims` dimensions, the others integrated by
+    monte_carlo(mc_samples, 2*seed+1) inside every evaluation."""
+    return integrator_region_based(
+        regions_generator_fubini(dims, regions_generator_adaptive_heap(
+            nested(simpson, trapezoidal), error_heuristic_size(error_metric_relative(), 1e-5), iterations),
+            monte_carlo(mc_samples, 2 * seed + 1)),
+        regions_integrator_parallel_variance_reduction(rr_uniform_region(), cv_optimize_weight(),
+                                                       region_sampling_uniform(), seed, spp))
+
+
+def integrator_adaptive_fubini_variance_reduction_parallel(dims: int, rule: NestedRule, heuristic, iterations: int,
+                                                           mc_samples: int, rr, cv, sampler, spp: int,
+                                                           seed: int = 0) -> RegionBased:
+    """integrator_adaptive_fubini_variance_reduction_parallel<dims>(rule, heuristic, iterations, mc_samples, rr,
+    cv, sampler, spp, seed) (integrator-adaptive-fubini-variance-reduction.h:28-41)."""
+    return integrator_region_based(
+        regions_generator_fubini(dims, regions_generator_adaptive_heap(rule, heuristic, iterations),
+                                 monte_carlo(mc_samples, 2 * seed + 1)),
+        regions_integrator_parallel_variance_reduction(rr, cv, sampler, seed, spp))
 
 
 def integrator_adaptive_variance_reduction_parallel(rule: NestedRule, *args) -> RegionBased:
@@ -516,6 +557,9 @@ def _run_cv(rb: RegionBased, bins, res, f, rng, logger, ctx, device_bins, replay
     if logger is not None:
         logger.log_progress(0, 1)
     g, vr = rb.generator, rb.integrator
+    fubini_dims, tail = 0, 0
+    if isinstance(g, FubiniGenerator):
+        fubini_dims, tail, g = g.dims, int(g.rest.samples), g.generator
     mem = MEM_DEVICE if device_bins else MEM_HOST
     p = Context.problem(f.kind, f.params, rng.min, rng.max, res, mem)
     flat = (not device_bins and isinstance(bins, np.ndarray) and bins.ndim == 1 and bins.dtype == np.float32
@@ -523,7 +567,7 @@ def _run_cv(rb: RegionBased, bins, res, f, rng, logger, ctx, device_bins, replay
     out = bins if (device_bins or flat) else np.empty(nb * ch, dtype=np.float32)
     opts = CvOpts(vr.samples, vr.seed, 1 if vr.cv.fixed else 0, 0, float(vr.cv.alpha), vr.rr.code, vr.sampling.code,
                   float(getattr(vr.rr, "factor_prob", 0.01)), 0, float(getattr(vr.sampling, "power", 1.0)),
-                  float(getattr(vr.sampling, "cutoff", 0.0)))
+                  float(getattr(vr.sampling, "cutoff", 0.0)), fubini_dims, tail)
     stats = ctx.control_variates(p, _nested_struct(g.rule, g.heuristic), g.iterations, opts, out, approximation,
                                  regions, replay)
     if not device_bins and not flat:

@@ -72,7 +72,8 @@ class CvOpts(ctypes.Structure):
     _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("weight", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double), ("rr", ctypes.c_int32),
                 ("sampling", ctypes.c_int32), ("rr_factor", ctypes.c_float), ("reserved2", ctypes.c_int32),
-                ("mis_power", ctypes.c_double), ("mis_cutoff", ctypes.c_double)]
+                ("mis_power", ctypes.c_double), ("mis_cutoff", ctypes.c_double), ("fubini_dims", ctypes.c_int32),
+                ("tail_samples", ctypes.c_uint32)]
 
 
 class LearnedOpts(ctypes.Structure):

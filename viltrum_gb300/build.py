@@ -64,7 +64,8 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(todo), os.cpu_count() or 4)) as ex:
             for obj, log in ex.map(lambda s: _compile(s, verbose_ptxas), todo):
                 logs.append(log)
-    if todo or not os.path.exists(LIB):
+    # relink also when an object is newer than the library (a link that failed earlier)
+    if todo or not os.path.exists(LIB) or max(os.path.getmtime(o) for o in objs) > os.path.getmtime(LIB):
         tmp = LIB + ".tmp"
         cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)

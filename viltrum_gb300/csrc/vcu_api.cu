@@ -414,6 +414,16 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
         return fail(ctx, VCU_INVALID_ARG, "unknown residual point sampling");
     if ((cv->rr == VCU_RR_PDF || cv->sampling != VCU_RS_UNIFORM) && nested->rule_hi != VCU_RULE_SIMPSON)
         return fail(ctx, VCU_UNSUPPORTED, "the pdf strategies need a Simpson high rule (rules.h:102-248)");
+    const bool fubini = cv->fubini_dims != 0;
+    if (fubini) {
+        if (cv->fubini_dims != 2 || p->dim < 3 || p->dimbins > 2)
+            return fail(ctx, VCU_UNSUPPORTED, "a Fubini tail takes regions over 2 dimensions of a 3+ dimensional "
+                                              "integrand, at most 2 of them binned");
+        if (cv->tail_samples == 0) return fail(ctx, VCU_INVALID_ARG, "tail_samples must be >= 1");
+        if (nested->rule_hi != VCU_RULE_SIMPSON || nested->rule_lo != VCU_RULE_TRAPEZOIDAL)
+            return fail(ctx, VCU_UNSUPPORTED, "a Fubini tail is built for nested(simpson, trapezoidal)");
+    }
+    const int rdim = fubini ? cv->fubini_dims : p->dim; /* dimensions of the regions */
     if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
         return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
     if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
@@ -422,7 +432,7 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
     CallScope scope{ctx, stats};
     if ((rc = scope.begin())) return rc;
-    const size_t bbytes = g.nbins * ch * 4, rbytes = (iterations + 1) * 2 * p->dim * 4;
+    const size_t bbytes = g.nbins * ch * 4, rbytes = (iterations + 1) * 2 * rdim * 4;
     float *dbins = bins, *dapprox = approximation, *dregions = regions;
     const float* dreplay = replay;
     if (p->mem == VCU_MEM_HOST) {
@@ -432,7 +442,7 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
         dapprox = approximation ? reinterpret_cast<float*>(o + ((bbytes + 255) & ~size_t(255))) : nullptr;
         dregions = regions ? reinterpret_cast<float*>(o + 2 * ((bbytes + 255) & ~size_t(255))) : nullptr;
         if (replay) {
-            const size_t pbytes = g.nbins * cv->samples_per_bin * (size_t)vcu_cv_replay_width(p->dim, cv->sampling) * 4;
+            const size_t pbytes = g.nbins * cv->samples_per_bin * (size_t)vcu_cv_replay_width(rdim, cv->sampling) * 4;
             if ((rc = ensure(ctx, ctx->in, pbytes))) return rc;
             VCU_CUDA(ctx, cudaMemcpyAsync(ctx->in.ptr, replay, pbytes, cudaMemcpyHostToDevice, ctx->stream));
             dreplay = static_cast<const float*>(ctx->in.ptr);
@@ -440,7 +450,8 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     }
     const int it = (int)iterations;
     if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
-        rc = run_cv_st(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+        rc = fubini ? run_cv_fubini(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches)
+                    : run_cv_st(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
     else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_SIMPSON)
         rc = run_cv_bs(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
     else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
@@ -455,9 +466,11 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     }
     const int S = nested->rule_hi;
     double sd = 1.0, sd1 = 1.0;
-    for (int d = 0; d < p->dim; ++d) sd *= S;
-    for (int d = 0; d < p->dim - 1; ++d) sd1 *= S;
-    const uint64_t evals = (uint64_t)(sd + (double)iterations * (S - 1) * sd1) + g.nbins * cv->samples_per_bin;
+    for (int d = 0; d < rdim; ++d) sd *= S;
+    for (int d = 0; d < rdim - 1; ++d) sd1 *= S;
+    const double per_node = fubini ? (double)cv->tail_samples : 1.0; /* integrand calls per node value */
+    const uint64_t evals =
+        (uint64_t)((sd + (double)iterations * (S - 1) * sd1) * per_node) + g.nbins * cv->samples_per_bin;
     return scope.end(evals, iterations + 1);
 }
 

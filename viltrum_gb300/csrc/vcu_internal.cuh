@@ -270,6 +270,9 @@ int run_tol_bt(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_n
 int run_cv_st(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
               const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
               uint32_t& launches);
+int run_cv_fubini(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
+                  const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+                  uint32_t& launches);
 int run_cv_bs(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
               const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
               uint32_t& launches);

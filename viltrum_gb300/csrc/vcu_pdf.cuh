@@ -67,7 +67,7 @@ __device__ __forceinline__ float cdf(float t, const float* c) {
 __device__ __forceinline__ double cuberoot(double x) { return (x < 0) ? -pow(-x, 1.0 / 3.0) : pow(x, 1.0 / 3.0); }
 
 /* the roots of cdf(t) = x in the reference's order (rules.h:182-225); returns how many */
-__device__ __noinline__ int inv_cdf(float x, const float* q, float* sol) {
+static __device__ __noinline__ int inv_cdf(float x, const float* q, float* sol) {
     float co[3];
     Rule<3>::coefficients(q, co);
     double a = __ddiv_rn((double)co[2], 3.0);
@@ -116,7 +116,7 @@ __device__ __noinline__ int inv_cdf(float x, const float* q, float* sol) {
 
 /* a coordinate of [t0,t1] with density proportional to the lifted parabola of the line; uniform when
  * no root lies in the interval (rules.h:227-246) */
-__device__ __noinline__ float line_sample(float s, float t0, float t1, const float* in) {
+static __device__ __noinline__ float line_sample(float s, float t0, float t1, const float* in) {
     float q[3], c[3];
     points(in, q);
     Rule<3>::coefficients(q, c);
