@@ -434,6 +434,22 @@ def adaptive_forms(ctx, port) -> dict:
         opts = _lib.CvOpts(16, 3, 1, 0, 0.0, rr, rs, 0.01, 0, 1.0, 0.0)
         ms, st = _median_ms(lambda: ctx.control_variates(p, crespo, (1 << 12) - 1, opts, b), reps=3, warmup=3)
         lines[name] = {"ms": round(ms, 3), "rmse_vs_fp64": scenes.bin_rmse(b.reshape(-1, 1), exact)}
+    # -- crespo2021 with regions over (x, y) only, time integrated by Monte Carlo in every evaluation
+    params = scenes.moving_scene3(SEED)
+    res = [512, 512]
+    p3 = ctx.problem(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res)
+    b3 = np.empty(512 * 512 * 3, np.float32)
+    fopts = _lib.CvOpts(64, 3, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 16)
+    ms, st = _median_ms(lambda: ctx.control_variates(p3, crespo, (1 << 14) - 1, fopts, b3), reps=3, warmup=3)
+    rows = list(range(0, 512, 64))
+    err = np.concatenate([b3.reshape(512, 512, 3)[r] - scenes.exact_bins(
+        scenes.MOVING_SCENE3, params, [0, r / 512.0, 0], [1, (r + 1) / 512.0, 1], [512, 1]) * 512.0 for r in rows])
+    out["cv_fubini"] = {
+        "workload": "integrator_crespo2021_infinite<2>(2^14-1 splits, 16 tail samples, 64 residual samples): regions "
+                    "over x,y of the moving-disk scene (RGB, 512x512 bins), time by Monte Carlo in every evaluation",
+        "ms": round(ms, 3), "gsamples_s": round(st.evaluations / (ms * 1e6), 3),
+        "rmse_vs_fp64": float(np.sqrt(np.mean(err.astype(np.float64) ** 2))),
+        "rmse_sample": f"{len(rows)} of 512 rows of bins", "timing": "median of 3 after 3 warm-up, device"}
     out["cv_importance"] = {
         "workload": "regions_integrator_parallel_variance_reduction(rr, cv_fixed_weight(0), sampler, 16 spp) over "
                     "2^12 regions of wave2, 128x128 bins: rr_uniform_region + region_sampling_uniform against "

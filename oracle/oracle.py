@@ -222,6 +222,21 @@ class Oracle:
         self._check(rc, "integrate_single")
         return float(out[0])
 
+    def crespo2021_infinite(self, kind, params, rmin, rmax, res, iterations, mc_samples, spp, seed):
+        """integrator_crespo2021_infinite<2> over a finite range (the unmodified reference only)."""
+        params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
+        nb = int(np.prod(res))
+        ch = self.channels(kind)
+        out = np.zeros(nb * ch, dtype=np.float32)
+        f = getattr(self.lib, self.prefix + "crespo2021_infinite")
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
+                      ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _f32p]
+        rc = f(kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
+               iterations, mc_samples, spp, seed, _ptr(out))
+        self._check(rc, "crespo2021_infinite")
+        return out.reshape(nb, ch)
+
     def control_variates(self, kind, params, rmin, rmax, res, nested: Nested, iterations, spp, seed,
                          weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False, rr=RR_UNIFORM,
                          sampling=RS_UNIFORM, rr_factor=0.01, mis_power=1.0, mis_cutoff=0.0):

@@ -373,6 +373,33 @@ extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n
     });
 }
 
+/* integrator_crespo2021_infinite<2>(iterations, mc_samples, spp, seed) over the finite range of the
+ * moving-disk scene: regions over (x, y), time integrated by Monte Carlo in every evaluation
+ * (src/control-variates/integrator-crespo2021.h:24-44) */
+extern "C" int ref_crespo2021_infinite(int32_t kind, const float* params, int32_t n_params, int32_t dim,
+                                       const float* rmin, const float* rmax, int32_t dimbins, const uint64_t* res,
+                                       uint64_t iterations, uint64_t mc_samples, uint64_t spp, uint64_t seed,
+                                       float* out) {
+    if (kind != vcu::VCU_F_MOVING_SCENE3 || dim != 3 || dimbins != 2) return 9;
+    auto* fn = new vcu::MovingScene3;
+    if (fn->build(params, n_params)) {
+        delete fn;
+        return 3;
+    }
+    RefF<vcu::MovingScene3, 3, vrgb> f{fn, nullptr};
+    auto range = mk_range<3>(rmin, rmax);
+    BinStore<2, vrgb> bs{mk_res<2>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.assign(nb, vrgb(0.0));
+    auto bins = [&bs](const std::array<std::size_t, 2>& q) -> vrgb& { return bs.v[bs.lin(q)]; };
+    viltrum::integrate(viltrum::integrator_crespo2021_infinite<2>(iterations, mc_samples, spp, seed), bins, bs.res, f,
+                       range);
+    for (std::size_t i = 0; i < nb; ++i) VT<vrgb>::to(bs.v[i], out + i * 3);
+    delete fn;
+    return 0;
+}
+
 /* single-value integrate(I, f, range) of the half-space family: the items of a batch of
  * independent integrals (monte_carlo(budget, seed), or adaptive nested(simpson, trapezoidal) with
  * budget regions and the default heuristic / absolute metric) */

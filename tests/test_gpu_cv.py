@@ -236,3 +236,53 @@ def test_cv_pdf_strategies_statistics_against_fp64(ctx, port, rr, sampling, powe
         ref_sq.append(np.mean((ref["bins"] - exact) ** 2))
     ratio = np.mean(gpu_sq) / np.mean(ref_sq)
     assert 0.7 <= ratio <= 1.4, (gpu_sq, ref_sq)
+
+
+def test_cv_fubini_tail_against_reference_statistics(ctx):
+    """integrator_crespo2021_infinite<2> over the moving-disk scene (regions over x, y; time by Monte
+    Carlo in every evaluation): the reference draws its tail samples from one sequential stream, so
+    its outputs for eight seeds (fixture) are compared statistically -- the device's mean squared
+    error against the FP64 truth over the same seeds within [0.7, 1.4] of the reference's."""
+    g = load_golden("fubini_moving3_rgb_bins32x32_it511_mc8_spp16")
+    params, res = g["params"], [int(r) for r in g["res"]]
+    exact = scenes.exact_bins(scenes.MOVING_SCENE3, params, g["rmin"], g["rmax"], res, t_nodes=96)
+    ref_sq = [np.mean((b - exact) ** 2) for b in g["out_bins"]]
+    p = ctx.problem(scenes.MOVING_SCENE3, params, g["rmin"], g["rmax"], res)
+    gpu_sq = []
+    reg = np.empty((int(g["iterations"]) + 1) * 2 * 2, np.float32)
+    for seed in g["seeds"]:
+        out = np.empty(int(np.prod(res)) * 3, np.float32)
+        opts = _lib.CvOpts(int(g["spp"]), int(seed), 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, int(g["mc_samples"]))
+        st = ctx.control_variates(p, CRESPO, int(g["iterations"]), opts, out, None, reg)
+        assert st.flags == 0 and np.isfinite(out).all()
+        gpu_sq.append(np.mean((out.reshape(-1, 3) - exact) ** 2))
+        # the regions tile the (x, y) square
+        r = reg.reshape(-1, 2, 2).astype(np.float64)
+        assert abs(np.prod(r[:, 1] - r[:, 0], axis=1).sum() - 1.0) < 1e-6
+    ratio = np.mean(gpu_sq) / np.mean(ref_sq)
+    assert 0.7 <= ratio <= 1.4, (gpu_sq, ref_sq)
+
+
+def test_cv_fubini_python_api_and_limits(ctx):
+    params = scenes.moving_scene3(7, n_gauss=8, n_disk=8)
+    bins = np.zeros((16, 16, 3), np.float32)
+    v.integrate(v.integrator_crespo2021_infinite(2, 255, 4, 16, 3), bins, v.Integrand.moving_scene3(params),
+                v.range_primary(3), ctx=ctx)
+    p = ctx.problem(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], [16, 16])
+    out = np.empty(16 * 16 * 3, np.float32)
+    ctx.control_variates(p, CRESPO, 255, _lib.CvOpts(16, 3, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 4), out)
+    assert np.array_equal(bins.transpose(1, 0, 2).reshape(-1), out)
+    # a deterministic function of its inputs: the same call gives the same bits
+    again = np.empty_like(out)
+    ctx.control_variates(p, CRESPO, 255, _lib.CvOpts(16, 3, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 4), again)
+    assert np.array_equal(out.view(np.uint32), again.view(np.uint32))
+    # regions over 2 of >= 3 dimensions, nested(simpson, trapezoidal), at least one tail sample
+    q = ctx.problem(scenes.SCENE2, scenes.scene2(7), [0, 0], [1, 1], [8, 8])
+    bad = [(q, CRESPO, _lib.CvOpts(4, 1, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 4), 8),
+           (p, CRESPO, _lib.CvOpts(4, 1, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 1, 4), 8),
+           (p, CRESPO, _lib.CvOpts(4, 1, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 0), 1),
+           (p, _lib.Nested(5, 3, 1, 1, 1e-5, 1e-37, 1e-37), _lib.CvOpts(4, 1, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 4), 8)]
+    for prob, nst, opts, code in bad:
+        with pytest.raises(_lib.VcuError) as e:
+            ctx.control_variates(prob, nst, 15, opts, np.empty(16 * 16 * 3, np.float32))
+        assert e.value.code == code
