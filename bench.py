@@ -618,6 +618,17 @@ def profile_workload(args) -> dict:
         b = np.empty(r * r * 3, np.float32)
         nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
         call = lambda: ctx.control_variates(p, nst, (1 << 12) - 1, _lib.CvOpts(16, 3, 0, 0, 1.0), b)
+    elif w in ("cv_importance", "cv_fubini"):
+        nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+        if w == "cv_importance":  # rr_pdf_region + region_sampling_importance, alpha 0
+            p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [r, r])
+            b = np.empty(r * r, np.float32)
+            opts = _lib.CvOpts(16, 3, 1, 0, 0.0, 3, 1, 0.01, 0, 1.0, 0.0)
+        else:  # regions over (x, y), 16 tail samples of t per node value
+            p = ctx.problem(scenes.MOVING_SCENE3, scenes.moving_scene3(SEED), [0, 0, 0], [1, 1, 1], [r, r])
+            b = np.empty(r * r * 3, np.float32)
+            opts = _lib.CvOpts(16, 3, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, 16)
+        call = lambda: ctx.control_variates(p, nst, (1 << 12) - 1, opts, b)
     elif w == "batch":
         items = _lib.batch_items(scenes.batch_items(256, seed=11, budget_hi=4096))
         nst = _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37)
@@ -650,7 +661,7 @@ def main(argv=None) -> int:
     ap.add_argument("--res", type=int, default=512, help="bins per side (512 is the benchmark workload)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' lines")
-    ap.add_argument("--workload", choices=["nested", "mc", "cv", "batch", "learned"], default=None,
+    ap.add_argument("--workload", choices=["nested", "mc", "cv", "cv_importance", "cv_fubini", "batch", "learned"], default=None,
                     help="profiling aid: one small run of one workload (prints its stats, not a benchmark line)")
     args = ap.parse_args(argv)
     global RES

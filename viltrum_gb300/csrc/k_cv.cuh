@@ -7,13 +7,16 @@
  * error_heuristic_size(error_metric_relative(), 1e-5) (src/control-variates/integrator-crespo2021.h:7-22).
  *
  * Three stages:
- *  1. k_cv_generate: ONE cooperative thread block builds the global region heap over the whole
- *     range exactly as src/nested/regions-generator-adaptive-heap.h:18-45 does (same split choices:
- *     error estimates with the reference's rounding, libstdc++ heap order).  The heap lives in shared
- *     memory (up to ~28k regions) or global memory; node values, ranges and volumes of all
- *     2*iters+1 regions ever built live in a global pool (region k of the pool is never moved, the
- *     heap holds pool ids).  Splits are inherently sequential; the block evaluates each split's new
- *     nodes and both children's error folds in parallel.
+ *  1. The global region heap over the whole range, exactly as
+ *     src/nested/regions-generator-adaptive-heap.h:18-45 builds it (same split choices: error
+ *     estimates with the reference's rounding, libstdc++ heap order).  From 512 splits on, in waves
+ *     (wave_launch, below): the regions of largest bottleneck error are split together, one warp per
+ *     region, and the host replays the heap sequence on their errors.  Below that, or when the waves
+ *     give up (NaN errors, a pool overflow from masses of equal errors), k_cv_generate: ONE
+ *     cooperative thread block splitting in order, the heap in shared memory (up to ~28k regions) or
+ *     global memory, each split's new nodes and both children's error folds evaluated by the block
+ *     in parallel.  Node values, ranges and volumes of every region built live in a global pool (a
+ *     region's slot never moves; the heap holds pool ids).
  *  2. k_cv_count / k_cv_fill / k_cv_sort: per-bin region lists.  Every region, in heap order, is
  *     appended to the bins pixels_in_region gives (src/newton-cotes/region.h:454-463, the 0.99 rule),
  *     as the reference's stratification does (regions-integrator-parallel-variance-reduction.h:49-57):
@@ -29,7 +32,9 @@
  *     (chosen list index, point) records.
  */
 #pragma once
+#include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "vcu_heap.h"
 #include "vcu_internal.cuh"
@@ -1152,9 +1157,28 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
 }
 
 template <int DIM, int SH, int SL, class F>
+int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iters,
+                const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+                uint32_t& launches);
+
+/* which generator builds the heap: the waves from 512 splits on (VCU_CV_GENERATOR=wave|sequential
+ * overrides), the single-block sequential one below that or when the waves give up */
+inline bool use_waves(int iters) {
+    const char* e = std::getenv("VCU_CV_GENERATOR");
+    if (e && std::strcmp(e, "sequential") == 0) return false;
+    if (e && std::strcmp(e, "wave") == 0) return iters > 0;
+    return iters >= 512;
+}
+
+template <int DIM, int SH, int SL, class F>
 int cv_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iters,
               const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
               uint32_t& launches) {
+    if (use_waves(iters)) {
+        const int rc = wave_launch<DIM, SH, SL>(ctx, f, p, g, nst, iters, cv, d_replay, d_bins, d_approx, d_regions,
+                                                launches);
+        if (rc != -1) return rc; /* -1: the waves gave up, build the heap sequentially */
+    }
     constexpr int S = SH;
     constexpr int CH = F::CH;
     constexpr int SD = ipow(S, DIM);
@@ -1241,6 +1265,82 @@ struct TolCfg {
 
 constexpr int TOL_WARPS = 4;
 
+/* The heuristic error and split dimension of the region whose node values are V, computed by one
+ * warp (lane 0 holds the result): per-dimension errors (region.h:379-418) with the reference's
+ * rounding, then error_heuristic_default / error_heuristic_size (error-heuristic.h:10-47).  LN holds
+ * DIM * S^(DIM-1) floats, EC DIM floats, both private to the warp. */
+template <int DIM, int S, int SL, int CH>
+__device__ __forceinline__ void warp_heuristic(const TolCfg& cfg, const float* V, float vol, const float* rmn,
+                                               const float* rmx, float* LN, float* EC, int lane, float& err,
+                                               int& dim) {
+    constexpr int NL = ipow(S, DIM - 1);
+    for (int t = lane; t < DIM * NL; t += 32) {
+        const int d = t / NL, J = t % NL;
+        float m = 0.0f;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            float line[S], low[SL];
+#pragma unroll
+            for (int i = 0; i < S; ++i) line[i] = V[node_index<DIM, S>(d, J, i) * CH + c];
+#pragma unroll
+            for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+            float H, L;
+            if constexpr (CH == 1) {
+                H = RefRule<S>::scalar(line);
+                L = RefRule<SL>::scalar(low);
+            } else {
+                H = RefRule<S>::rgb(line);
+                L = RefRule<SL>::rgb(low);
+            }
+            const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
+            m = (c == 0) ? mv : vadd(m, mv);
+        }
+        LN[t] = m;
+    }
+    __syncwarp();
+    if (lane < DIM) {
+        float buf[NL];
+        for (int i = 0; i < NL; ++i) buf[i] = LN[lane * NL + i];
+        int n = NL;
+        for (int level = 0; level < DIM - 1; ++level) {
+            n /= S;
+            for (int i = 0; i < n; ++i) buf[i] = RefRule<S>::scalar(buf + i * S);
+        }
+        EC[lane] = vmul(vol, buf[0]);
+    }
+    __syncwarp();
+    err = 0.0f;
+    dim = 0;
+    if (lane == 0) {
+        const float* e = EC;
+        float max_err;
+        int max_dim = 0;
+        if (cfg.heuristic == VCU_HEUR_DEFAULT) {
+            max_err = 0.0f;
+            for (int d = 0; d < DIM; ++d)
+                if (e[d] > max_err) {
+                    max_err = e[d];
+                    max_dim = d;
+                }
+        } else {
+            float wd = vsub(rmx[0], rmn[0]);
+            if ((double)wd < cfg.min_size || isnan(wd)) max_err = 0.0f;
+            else max_err = __double2float_rn(__dadd_rn((double)e[0], __dmul_rn(cfg.size_weight, (double)fabsf(wd))));
+            for (int d = 1; d < DIM; ++d) {
+                wd = vsub(rmx[d], rmn[d]);
+                float er = __double2float_rn(__dadd_rn((double)e[d], __dmul_rn(cfg.size_weight, (double)fabsf(wd))));
+                if ((double)wd < cfg.min_size) er = 0.0f;
+                if (er >= max_err) {
+                    max_err = er;
+                    max_dim = d;
+                }
+            }
+        }
+        err = max_err;
+        dim = max_dim;
+    }
+}
+
 template <class F, int DIM, int SH>
 __global__ void k_tol_root(const __grid_constant__ F f, const TolCfg cfg, float* __restrict__ vals,
                            float* __restrict__ rmin, float* __restrict__ rmax, float* __restrict__ vol) {
@@ -1274,114 +1374,24 @@ __global__ void k_tol_root(const __grid_constant__ F f, const TolCfg cfg, float*
     }
 }
 
-/* one level: counters[0] = pool slots used, counters[1] = regions of the next level */
-template <class F, int DIM, int SH, int SL>
-__global__ void __launch_bounds__(TOL_WARPS * 32)
-    k_tol_level(const __grid_constant__ F f, const TolCfg cfg, const int* __restrict__ cur, int ncur,
-                int* __restrict__ next, uint32_t* __restrict__ counters, float* __restrict__ vals,
-                float* __restrict__ rmin, float* __restrict__ rmax, float* __restrict__ vol, int* __restrict__ child,
-                uint32_t* __restrict__ status) {
-    constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM), NL = ipow(S, DIM - 1), NNEW = (S - 1) * NL;
-    __shared__ float LN[TOL_WARPS][DIM * NL];
-    __shared__ float EC[TOL_WARPS][DIM];
-    __shared__ float CO[TOL_WARPS][DIM * S], CN[TOL_WARPS][S - 1];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = blockIdx.x * TOL_WARPS + warp;
-    if (w >= ncur) return;
-    const int id = cur[w];
-    const float* V = vals + (size_t)id * SD * CH;
-    /* per-dimension errors (region.h:379-418) with the reference's rounding */
-    for (int t = lane; t < DIM * NL; t += 32) {
-        const int d = t / NL, J = t % NL;
-        float m = 0.0f;
-#pragma unroll
-        for (int c = 0; c < CH; ++c) {
-            float line[S], low[SL];
-#pragma unroll
-            for (int i = 0; i < S; ++i) line[i] = V[node_index<DIM, S>(d, J, i) * CH + c];
-#pragma unroll
-            for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
-            float H, L;
-            if constexpr (CH == 1) {
-                H = RefRule<S>::scalar(line);
-                L = RefRule<SL>::scalar(low);
-            } else {
-                H = RefRule<S>::rgb(line);
-                L = RefRule<SL>::rgb(low);
-            }
-            const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
-            m = (c == 0) ? mv : vadd(m, mv);
-        }
-        LN[warp][t] = m;
-    }
-    __syncwarp();
-    if (lane < DIM) {
-        float buf[NL];
-        for (int i = 0; i < NL; ++i) buf[i] = LN[warp][lane * NL + i];
-        int n = NL;
-        for (int level = 0; level < DIM - 1; ++level) {
-            n /= S;
-            for (int i = 0; i < n; ++i) buf[i] = RefRule<S>::scalar(buf + i * S);
-        }
-        EC[warp][lane] = vmul(vol[id], buf[0]);
-    }
-    __syncwarp();
-    int split_dim = 0, c0 = -1;
-    if (lane == 0) {
-        const float* e = EC[warp];
-        float max_err;
-        int max_dim = 0;
-        if (cfg.heuristic == VCU_HEUR_DEFAULT) {
-            max_err = 0.0f;
-            for (int d = 0; d < DIM; ++d)
-                if (e[d] > max_err) {
-                    max_err = e[d];
-                    max_dim = d;
-                }
-        } else {
-            float wd = vsub(rmax[(size_t)id * DIM], rmin[(size_t)id * DIM]);
-            if ((double)wd < cfg.min_size || isnan(wd)) max_err = 0.0f;
-            else max_err = __double2float_rn(__dadd_rn((double)e[0], __dmul_rn(cfg.size_weight, (double)fabsf(wd))));
-            for (int d = 1; d < DIM; ++d) {
-                wd = vsub(rmax[(size_t)id * DIM + d], rmin[(size_t)id * DIM + d]);
-                float err = __double2float_rn(__dadd_rn((double)e[d], __dmul_rn(cfg.size_weight, (double)fabsf(wd))));
-                if ((double)wd < cfg.min_size) err = 0.0f;
-                if (err >= max_err) {
-                    max_err = err;
-                    max_dim = d;
-                }
-            }
-        }
-        if (max_err < cfg.tol) {
-            child[id] = -1; /* leaf */
-        } else {
-            const uint32_t c = atomicAdd(&counters[0], 2u);
-            if (c + 2 > cfg.capacity) {
-                atomicOr(status, VCU_FLAG_OVERFLOW);
-                child[id] = -1;
-            } else {
-                child[id] = (int)c;
-                const uint32_t k = atomicAdd(&counters[1], 2u);
-                next[k] = (int)c;
-                next[k + 1] = (int)c + 1;
-                c0 = (int)c;
-                split_dim = max_dim;
-            }
-        }
-    }
-    c0 = __shfl_sync(0xffffffffu, c0, 0);
-    split_dim = __shfl_sync(0xffffffffu, split_dim, 0);
-    if (c0 < 0) return;
-    const int dd = split_dim, C0 = c0, C1 = c0 + 1;
+/* Split region id along dd into pool slots C0 (lower half) and C0+1 (upper half), one warp: the new
+ * nodes at the odd positions are evaluated, the parent's nodes fill the even ones (region.h:345-359,
+ * split.h:13-49), and the children's ranges and volumes are written.  CO (DIM*S floats) and CN (S-1)
+ * are the warp's scratch. */
+template <class F, int DIM, int S>
+__device__ __forceinline__ void warp_split(const F& f, const float* V, int id, int dd, int C0, float* vals, float* rmin,
+                                           float* rmax, float* vol, float* CO, float* CN, int lane) {
+    constexpr int CH = F::CH, SD = ipow(S, DIM), NL = ipow(S, DIM - 1), NNEW = (S - 1) * NL;
+    const int C1 = C0 + 1;
     const float* pmin = rmin + (size_t)id * DIM;
     const float* pmax = rmax + (size_t)id * DIM;
     for (int t = lane; t < DIM * S + (S - 1); t += 32) {
         if (t < DIM * S) {
             const int d = t / S, j = t % S;
-            CO[warp][t] = node_coord(node_pos<S>(j), vsub(pmax[d], pmin[d]), pmin[d]);
+            CO[t] = node_coord(node_pos<S>(j), vsub(pmax[d], pmin[d]), pmin[d]);
         } else {
             const int k = t - DIM * S;
-            CN[warp][k] = node_coord(mid_pos<S>(k), vsub(pmax[dd], pmin[dd]), pmin[dd]);
+            CN[k] = node_coord(mid_pos<S>(k), vsub(pmax[dd], pmin[dd]), pmin[dd]);
         }
     }
     __syncwarp();
@@ -1399,10 +1409,10 @@ __global__ void __launch_bounds__(TOL_WARPS * 32)
             int rem = J;
             for (int e = 0; e < DIM; ++e) {
                 if (e == dd) continue;
-                x[e] = CO[warp][e * S + rem % S];
+                x[e] = CO[e * S + rem % S];
                 rem /= S;
             }
-            x[dd] = CN[warp][k];
+            x[dd] = CN[k];
             f(x, v);
             i = 2 * k + 1;
         } else {
@@ -1440,6 +1450,51 @@ __global__ void __launch_bounds__(TOL_WARPS * 32)
         vol[C0] = v0;
         vol[C1] = v1;
     }
+}
+
+/* one level: counters[0] = pool slots used, counters[1] = regions of the next level */
+template <class F, int DIM, int SH, int SL>
+__global__ void __launch_bounds__(TOL_WARPS * 32)
+    k_tol_level(const __grid_constant__ F f, const TolCfg cfg, const int* __restrict__ cur, int ncur,
+                int* __restrict__ next, uint32_t* __restrict__ counters, float* __restrict__ vals,
+                float* __restrict__ rmin, float* __restrict__ rmax, float* __restrict__ vol, int* __restrict__ child,
+                uint32_t* __restrict__ status) {
+    constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM), NL = ipow(S, DIM - 1);
+    __shared__ float LN[TOL_WARPS][DIM * NL];
+    __shared__ float EC[TOL_WARPS][DIM];
+    __shared__ float CO[TOL_WARPS][DIM * S], CN[TOL_WARPS][S - 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * TOL_WARPS + warp;
+    if (w >= ncur) return;
+    const int id = cur[w];
+    const float* V = vals + (size_t)id * SD * CH;
+    float max_err;
+    int max_dim;
+    warp_heuristic<DIM, S, SL, CH>(cfg, V, vol[id], rmin + (size_t)id * DIM, rmax + (size_t)id * DIM, LN[warp], EC[warp],
+                                   lane, max_err, max_dim);
+    int split_dim = 0, c0 = -1;
+    if (lane == 0) {
+        if (max_err < cfg.tol) {
+            child[id] = -1; /* leaf */
+        } else {
+            const uint32_t c = atomicAdd(&counters[0], 2u);
+            if (c + 2 > cfg.capacity) {
+                atomicOr(status, VCU_FLAG_OVERFLOW);
+                child[id] = -1;
+            } else {
+                child[id] = (int)c;
+                const uint32_t k = atomicAdd(&counters[1], 2u);
+                next[k] = (int)c;
+                next[k + 1] = (int)c + 1;
+                c0 = (int)c;
+                split_dim = max_dim;
+            }
+        }
+    }
+    c0 = __shfl_sync(0xffffffffu, c0, 0);
+    split_dim = __shfl_sync(0xffffffffu, split_dim, 0);
+    if (c0 < 0) return;
+    warp_split<F, DIM, S>(f, V, id, split_dim, c0, vals, rmin, rmax, vol, CO[warp], CN[warp], lane);
 }
 
 /* leaf counts of the subtrees of one level's regions (deepest level first) */
@@ -1574,6 +1629,337 @@ int tol_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g,
                                          reinterpret_cast<uint32_t*>(base + o_cnt), reinterpret_cast<uint32_t*>(base + o_off),
                                          reinterpret_cast<uint32_t*>(base + o_cur), nullptr, d_bins, nullptr, nullptr,
                                          launches);
+}
+
+/* ---------------------------------------------------------------- the heap's regions in waves
+ * regions_generator_adaptive_heap (regions-generator-adaptive-heap.h:18-45) pops the region of
+ * largest error and pushes its two halves, `iterations` times.  Which regions it splits can be found
+ * without following it step by step: a region is split before any region whose path from the root
+ * holds a smaller error, so the split set is (ties aside) the `iterations` regions of largest
+ * bottleneck b(v) = min of the errors from the root to v.  Waves expand the unsplit regions of
+ * largest b together (one warp per region: its new nodes, then its halves' errors), until the
+ * regions already split with b >= the largest b left unsplit number `iterations`.  The host then
+ * replays the reference's exact heap sequence (libstdc++ push/pop, vcu_heap.h) on the computed
+ * errors, which fixes the final heap order (the order regions are integrated in) and resolves ties
+ * exactly; a region that sequence pops but no wave split sends the waves further.  The result is the
+ * sequential generator's, region for region and position for position. */
+constexpr int WAVE_WARPS = 4;
+constexpr int WAVE_SHIFT = 19;                      /* bucket = bits(b) >> 19: 4096 buckets */
+constexpr int WAVE_BUCKETS = 1 << (31 - WAVE_SHIFT);
+/* counters: */
+enum { WC_POOL = 0, WC_NEW = 1, WC_EXPAND = 2, WC_FRONT2 = 3, WC_SPLIT = 4, WC_MAXB = 5, WC_GE = 6, WC_NAN = 7,
+       WC_FRONT = 8, WC_OVF = 9, WC_N = 16 };
+
+__device__ __forceinline__ uint32_t wave_bits(float b) {
+    const uint32_t u = __float_as_uint(b);
+    return (u & 0x80000000u) ? 0u : u; /* errors are >= 0; -0 counts as 0 */
+}
+
+/* errors of the listed regions; b = min(b(parent), error) */
+template <class F, int DIM, int SH, int SL>
+__global__ void __launch_bounds__(WAVE_WARPS * 32)
+    k_wave_eval(const TolCfg cfg, const int* __restrict__ list, const uint32_t* __restrict__ nlist,
+                const float* __restrict__ vals, const float* __restrict__ rmin, const float* __restrict__ rmax,
+                const float* __restrict__ vol, const int* __restrict__ parent, float* __restrict__ key,
+                int* __restrict__ kdim, float* __restrict__ bneck, uint32_t* __restrict__ ctr) {
+    constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM), NL = ipow(S, DIM - 1);
+    __shared__ float LN[WAVE_WARPS][DIM * NL];
+    __shared__ float EC[WAVE_WARPS][DIM];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t w = blockIdx.x * WAVE_WARPS + warp;
+    if (w >= *nlist) return;
+    const int id = list[w];
+    float e;
+    int dm;
+    warp_heuristic<DIM, S, SL, CH>(cfg, vals + (size_t)id * SD * CH, vol[id], rmin + (size_t)id * DIM,
+                                   rmax + (size_t)id * DIM, LN[warp], EC[warp], lane, e, dm);
+    if (lane == 0) {
+        key[id] = e;
+        kdim[id] = dm;
+        const int par = parent[id];
+        const float bp = par < 0 ? e : bneck[par];
+        bneck[id] = (e < bp) ? e : bp;
+        if (isnan(e)) atomicOr(&ctr[WC_NAN], 1u);
+    }
+}
+
+/* the largest b of the unsplit regions, and their histogram of b; the count of split regions with
+ * b >= that largest b comes next (k_wave_count) */
+static __global__ void k_wave_stats(const int* __restrict__ front, const uint32_t* __restrict__ nfront,
+                                    const float* __restrict__ bneck, uint32_t* __restrict__ ctr,
+                                    uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[WAVE_BUCKETS];
+    for (int i = threadIdx.x; i < WAVE_BUCKETS; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint32_t n = *nfront;
+    uint32_t mx = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t u = wave_bits(bneck[front[i]]);
+        mx = u > mx ? u : mx;
+        atomicAdd(&h[u >> WAVE_SHIFT], 1u);
+    }
+    atomicMax(&ctr[WC_MAXB], mx);
+    __syncthreads();
+    for (int i = threadIdx.x; i < WAVE_BUCKETS; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+static __global__ void k_wave_count(const int* __restrict__ split, const uint32_t* __restrict__ nsplit,
+                                    const float* __restrict__ bneck, uint32_t* __restrict__ ctr) {
+    const uint32_t n = *nsplit, m = ctr[WC_MAXB];
+    uint32_t c = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        c += wave_bits(bneck[split[i]]) >= m;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&ctr[WC_GE], c);
+}
+
+/* the unsplit regions whose b lies in bucket >= thr are split this wave (and recorded as split);
+ * the others stay unsplit */
+static __global__ void k_wave_select(const int* __restrict__ front, const uint32_t* __restrict__ nfront,
+                                     const float* __restrict__ bneck, uint32_t thr, int* __restrict__ expand,
+                                     int* __restrict__ front2, int* __restrict__ split, uint32_t* __restrict__ ctr) {
+    const uint32_t n = *nfront;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int id = front[i];
+        if ((wave_bits(bneck[id]) >> WAVE_SHIFT) >= thr) {
+            expand[atomicAdd(&ctr[WC_EXPAND], 1u)] = id;
+            split[atomicAdd(&ctr[WC_SPLIT], 1u)] = id;
+        } else {
+            front2[atomicAdd(&ctr[WC_FRONT2], 1u)] = id;
+        }
+    }
+}
+
+/* split the selected regions along their heuristic dimension; the halves join the unsplit list
+ * and the list whose errors are computed next */
+template <class F, int DIM, int SH>
+__global__ void __launch_bounds__(WAVE_WARPS * 32)
+    k_wave_split(const __grid_constant__ F f, const int* __restrict__ expand, const uint32_t* __restrict__ nexpand,
+                 const int* __restrict__ kdim, uint32_t capacity, float* __restrict__ vals, float* __restrict__ rmin,
+                 float* __restrict__ rmax, float* __restrict__ vol, int* __restrict__ child, int* __restrict__ parent,
+                 int* __restrict__ fresh, int* __restrict__ front2, uint32_t* __restrict__ ctr) {
+    constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM);
+    __shared__ float CO[WAVE_WARPS][DIM * S], CN[WAVE_WARPS][S - 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t w = blockIdx.x * WAVE_WARPS + warp;
+    if (w >= *nexpand) return;
+    const int id = expand[w];
+    int c0 = -1;
+    if (lane == 0) {
+        const uint32_t c = atomicAdd(&ctr[WC_POOL], 2u);
+        if (c + 2 > capacity) {
+            atomicOr(&ctr[WC_OVF], 1u);
+        } else {
+            c0 = (int)c;
+            child[id] = c0;
+            parent[c0] = id;
+            parent[c0 + 1] = id;
+            child[c0] = -1;
+            child[c0 + 1] = -1;
+            const uint32_t k = atomicAdd(&ctr[WC_NEW], 2u);
+            fresh[k] = c0;
+            fresh[k + 1] = c0 + 1;
+            const uint32_t q = atomicAdd(&ctr[WC_FRONT2], 2u);
+            front2[q] = c0;
+            front2[q + 1] = c0 + 1;
+        }
+    }
+    c0 = __shfl_sync(0xffffffffu, c0, 0);
+    if (c0 < 0) return;
+    warp_split<F, DIM, S>(f, vals + (size_t)id * SD * CH, id, kdim[id], c0, vals, rmin, rmax, vol, CO[warp], CN[warp],
+                          lane);
+}
+
+template <int DIM, int SH, int SL, class F>
+int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_nested& nst, int iters,
+                const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
+                uint32_t& launches) {
+    constexpr int S = SH;
+    constexpr int CH = F::CH;
+    constexpr int SD = ipow(S, DIM);
+    const size_t N = (size_t)iters;
+    /* pool: the split set plus room for the waves' overshoot */
+    size_t cap = 6 * N + 4096;
+    const size_t per_node = (size_t)SD * CH * 4 + 2 * DIM * 4 + 4 * 4 + 6 * 4;
+    if (cap > ((size_t)6 << 30) / per_node) cap = ((size_t)6 << 30) / per_node;
+    if (cap > (1u << 24) - 2) cap = (1u << 24) - 2;
+    if (cap < 2 * N + 1) return -1; /* too large: the sequential generator */
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = align256(o + bytes);
+        return at;
+    };
+    const size_t o_vals = take(cap * SD * CH * 4), o_rmin = take(cap * DIM * 4), o_rmax = take(cap * DIM * 4),
+                 o_vol = take(cap * 4), o_key = take(cap * 4), o_kdim = take(cap * 4), o_b = take(cap * 4),
+                 o_par = take(cap * 4), o_child = take(cap * 4), o_fa = take(cap * 4), o_fb = take(cap * 4),
+                 o_exp = take(cap * 4), o_split = take(cap * 4), o_fresh = take(cap * 4), o_hp = take((N + 1) * 4),
+                 o_ctr = take(WC_N * 4), o_hist = take(WAVE_BUCKETS * 4), o_cnt = take(g.nbins * 4),
+                 o_off = take((g.nbins + 1) * 4), o_cur = take(g.nbins * 4);
+    int rc = ensure(ctx, ctx->scratch, o);
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->scratch.ptr);
+    float* vals = reinterpret_cast<float*>(base + o_vals);
+    float* rmin = reinterpret_cast<float*>(base + o_rmin);
+    float* rmax = reinterpret_cast<float*>(base + o_rmax);
+    float* vol = reinterpret_cast<float*>(base + o_vol);
+    float* key = reinterpret_cast<float*>(base + o_key);
+    int* kdim = reinterpret_cast<int*>(base + o_kdim);
+    float* bneck = reinterpret_cast<float*>(base + o_b);
+    int* parent = reinterpret_cast<int*>(base + o_par);
+    int* child = reinterpret_cast<int*>(base + o_child);
+    int* fa = reinterpret_cast<int*>(base + o_fa);
+    int* fb = reinterpret_cast<int*>(base + o_fb);
+    int* expand = reinterpret_cast<int*>(base + o_exp);
+    int* split = reinterpret_cast<int*>(base + o_split);
+    int* fresh = reinterpret_cast<int*>(base + o_fresh);
+    int* hp = reinterpret_cast<int*>(base + o_hp);
+    uint32_t* ctr = reinterpret_cast<uint32_t*>(base + o_ctr);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base + o_hist);
+
+    TolCfg tc{};
+    for (int d = 0; d < DIM; ++d) {
+        tc.rmin[d] = p->range_min[d];
+        tc.rmax[d] = p->range_max[d];
+    }
+    tc.heuristic = nst.heuristic;
+    tc.relative = nst.metric == VCU_METRIC_RELATIVE;
+    float mv = (float)nst.min_val;
+    if ((double)mv < nst.min_val) mv = nextafterf(mv, INFINITY);
+    tc.min_val_f = mv;
+    tc.size_weight = nst.size_weight;
+    tc.min_size = nst.min_size;
+    tc.capacity = (uint32_t)cap;
+
+    /* the root, its error; it is the one unsplit region */
+    k_tol_root<F, DIM, SH><<<1, 256, 0, ctx->stream>>>(f, tc, vals, rmin, rmax, vol);
+    {
+        uint32_t init[WC_N] = {};
+        init[WC_POOL] = 1;
+        init[WC_NEW] = 1;
+        init[WC_FRONT] = 1;
+        const int root[3] = {0, -1, -1}; /* fresh/front list, parent, child of the root */
+        VCU_CUDA(ctx, cudaMemcpyAsync(ctr, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(fresh, root, 4, cudaMemcpyHostToDevice, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(fa, root, 4, cudaMemcpyHostToDevice, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(parent, root + 1, 4, cudaMemcpyHostToDevice, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(child, root + 2, 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    k_wave_eval<F, DIM, SH, SL><<<1, WAVE_WARPS * 32, 0, ctx->stream>>>(tc, fresh, ctr + WC_NEW, vals, rmin, rmax, vol,
+                                                                      parent, key, kdim, bneck, ctr);
+    launches += 2;
+    int* front = fa;
+    int* front2 = fb;
+    uint32_t nfront = 1;
+    std::vector<uint32_t> h(WAVE_BUCKETS);
+    std::vector<float> hkey, hb;
+    std::vector<int> hdim, hchild;
+    std::vector<float> HE(N + 1);
+    std::vector<int> HS(N + 1);
+    uint32_t force = 0xffffffffu; /* after an incomplete replay: split every unsplit b bucket >= force */
+    for (int round = 0; round < 8; ++round) {
+        /* waves */
+        for (int wave = 0;; ++wave) {
+            if (wave > 100000) return -1;
+            VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_MAXB, 0, 8, ctx->stream));
+            VCU_CUDA(ctx, cudaMemsetAsync(hist, 0, WAVE_BUCKETS * 4, ctx->stream));
+            const unsigned sb = (unsigned)std::min<size_t>((nfront + 255) / 256, (size_t)ctx->sm_count * 4);
+            k_wave_stats<<<sb ? sb : 1, 256, 0, ctx->stream>>>(front, ctr + WC_FRONT, bneck, ctr, hist);
+            k_wave_count<<<(unsigned)ctx->sm_count * 4, 256, 0, ctx->stream>>>(split, ctr + WC_SPLIT, bneck, ctr);
+            launches += 2;
+            uint32_t hc[WC_N];
+            VCU_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(h.data(), hist, WAVE_BUCKETS * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (hc[WC_OVF] || hc[WC_NAN]) return -1; /* pool too small, or NaN errors: the sequential generator */
+            nfront = hc[WC_FRONT];
+            const uint32_t ge = hc[WC_GE];
+            const uint32_t maxb = hc[WC_MAXB] >> WAVE_SHIFT;
+            if (nfront == 0) break;
+            const bool forced = force != 0xffffffffu && maxb >= force;
+            if (ge >= N && !forced) break;
+            /* split the unsplit regions of the top buckets, as many as still needed */
+            const uint32_t need = ge >= N ? 1u : (uint32_t)(N - ge);
+            uint32_t thr = 0, acc = 0;
+            for (int bkt = WAVE_BUCKETS - 1; bkt >= 0; --bkt) {
+                acc += h[bkt];
+                if (acc >= need) {
+                    thr = (uint32_t)bkt;
+                    break;
+                }
+            }
+            /* and only those within a factor 4 of the largest b (two octaves of buckets): a wave splits
+             * nothing far below what the sequence is splitting now, so the tree does not grow
+             * breadth-first into regions the sequence never reaches */
+            const uint32_t floor_bkt = maxb > 2u * (1u << (23 - WAVE_SHIFT)) ? maxb - 2u * (1u << (23 - WAVE_SHIFT)) : 0u;
+            if (thr < floor_bkt) thr = floor_bkt;
+            if (forced && force < thr) thr = force;
+            acc = 0;
+            for (uint32_t bkt = thr; bkt < (uint32_t)WAVE_BUCKETS; ++bkt) acc += h[bkt];
+            if (hc[WC_POOL] + 2ull * acc > cap) return -1;
+            VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_NEW, 0, 12, ctx->stream)); /* NEW, EXPAND, FRONT2 */
+            const unsigned gb = (unsigned)((nfront + 255) / 256);
+            k_wave_select<<<gb, 256, 0, ctx->stream>>>(front, ctr + WC_FRONT, bneck, thr, expand, front2, split, ctr);
+            const unsigned wb = (unsigned)((nfront + WAVE_WARPS - 1) / WAVE_WARPS);
+            k_wave_split<F, DIM, SH><<<wb, WAVE_WARPS * 32, 0, ctx->stream>>>(
+                f, expand, ctr + WC_EXPAND, kdim, (uint32_t)cap, vals, rmin, rmax, vol, child, parent, fresh, front2, ctr);
+            const unsigned eb = (unsigned)((2 * (size_t)nfront + WAVE_WARPS - 1) / WAVE_WARPS);
+            k_wave_eval<F, DIM, SH, SL><<<eb, WAVE_WARPS * 32, 0, ctx->stream>>>(tc, fresh, ctr + WC_NEW, vals, rmin, rmax,
+                                                                               vol, parent, key, kdim, bneck, ctr);
+            VCU_CUDA(ctx, cudaMemcpyAsync(ctr + WC_FRONT, ctr + WC_FRONT2, 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            launches += 3;
+            VCU_CUDA(ctx, cudaGetLastError());
+            std::swap(front, front2);
+            nfront = nfront * 3; /* upper bound until the next read */
+        }
+        /* replay the reference's heap sequence on the computed errors */
+        uint32_t pool = 0;
+        VCU_CUDA(ctx, cudaMemcpyAsync(&pool, ctr + WC_POOL, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        hkey.resize(pool);
+        hdim.resize(pool);
+        hchild.resize(pool);
+        hb.resize(pool);
+        VCU_CUDA(ctx, cudaMemcpyAsync(hkey.data(), key, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(hdim.data(), kdim, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(hchild.data(), child, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaMemcpyAsync(hb.data(), bneck, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        HE[0] = hkey[0];
+        HS[0] = 0 | (hdim[0] << 24);
+        int missing = -1;
+        for (size_t it = 0; it < N; ++it) {
+            const int top = HS[0] & 0xffffff;
+            const int c = hchild[top];
+            if (c < 0) {
+                missing = top;
+                break;
+            }
+            const int n = (int)it + 1;
+            heap_pop(HE.data(), HS.data(), n);
+            HE[n - 1] = hkey[c];
+            HS[n - 1] = c | (hdim[c] << 24);
+            heap_push(HE.data(), HS.data(), n);
+            HE[n] = hkey[c + 1];
+            HS[n] = (c + 1) | (hdim[c + 1] << 24);
+            heap_push(HE.data(), HS.data(), n + 1);
+        }
+        if (missing < 0) {
+            VCU_CUDA(ctx, cudaMemcpyAsync(hp, HS.data(), (N + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
+            return regions_into_bins<F, DIM, SH, SL>(ctx, residual_functor(f), p, g, cv, vals, rmin, rmax, vol, hp, N + 1,
+                                                     reinterpret_cast<uint32_t*>(base + o_cnt),
+                                                     reinterpret_cast<uint32_t*>(base + o_off),
+                                                     reinterpret_cast<uint32_t*>(base + o_cur), d_replay, d_bins,
+                                                     d_approx, d_regions, launches);
+        }
+        /* the sequence needs a region no wave split: split every unsplit region down to its b */
+        uint32_t u;
+        std::memcpy(&u, &hb[missing], 4);
+        if (u & 0x80000000u) u = 0;
+        force = u >> WAVE_SHIFT;
+    }
+    return -1;
 }
 
 }  // namespace cv_detail
