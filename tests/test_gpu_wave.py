@@ -1,7 +1,7 @@
 """The adaptive heap's regions built in parallel waves equal the sequential generator's.
 
 Both generators serve vcu_control_variates and vcu_adaptive_iterations_global
-(VCU_CV_GENERATOR=wave|sequential selects one; by default the waves run from 512 splits on).  The
+(VCU_CV_GENERATOR=wave|sequential selects one; by default the waves run from 128 splits on).  The
 waves split, together, the regions of largest bottleneck error, and the host replays the
 reference's heap sequence on their errors; the result must be the sequential generator's region for
 region and position for position -- bit-equal region ranges in heap order and bit-equal bins (the

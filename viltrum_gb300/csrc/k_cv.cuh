@@ -9,7 +9,7 @@
  * Three stages:
  *  1. The global region heap over the whole range, exactly as
  *     src/nested/regions-generator-adaptive-heap.h:18-45 builds it (same split choices: error
- *     estimates with the reference's rounding, libstdc++ heap order).  From 512 splits on, in waves
+ *     estimates with the reference's rounding, libstdc++ heap order).  From 128 splits on, in waves
  *     (wave_launch, below): the regions of largest bottleneck error are split together, one warp per
  *     region, and the host replays the heap sequence on their errors.  Below that, or when the waves
  *     give up (NaN errors, a pool overflow from masses of equal errors), k_cv_generate: ONE
@@ -26,8 +26,9 @@
  *     sum_i prod(res) * integral over (bin n region_i) (:77-88), then the residual: sample j picks a
  *     region uniformly (rr_uniform_region, weight n) and a uniform point in bin n region (weight
  *     volume), pushes f*w and g*w (g = the region polynomial, region.h:103-112) into the
- *     cv_optimize_weight / cv_fixed_weight estimator (weight-strategy.h:7-110); moments and the final
- *     recombination (sum_f - a*sum_g)/n + a*approximation are in FP64.  Sample j of bin b draws from
+ *     cv_optimize_weight / cv_fixed_weight estimator (weight-strategy.h:7-110); sums in FP32 (Kahan
+ *     per lane, float-float across lanes), moments FP32 per lane and FP64 across lanes, the final
+ *     recombination (sum_f - a*sum_g)/n + a*approximation in FP64.  Sample j of bin b draws from
  *     Philox4x32-10 (key = seed, counter = (j, b_lo, b_hi, 0xC0DE0000 | block)), or replays given
  *     (chosen list index, point) records.
  */
@@ -534,6 +535,7 @@ struct ResCfg {
     int32_t weight; /* VCU_CV_OPTIMIZE / VCU_CV_FIXED */
     double alpha;
     const float* approx_init; /* nullable: the approximation starts from these bin values */
+    int32_t factor_f32;       /* prod(res) < 2^24: it converts to float exactly */
     int32_t rr;               /* VCU_RR_UNIFORM / VCU_RR_INTEGRAL / VCU_RR_ERROR / VCU_RR_PDF */
     int32_t sampling;         /* VCU_RS_UNIFORM / VCU_RS_IMPORTANCE / VCU_RS_RUSSIAN_ROULETTE / VCU_RS_MIS */
     float rr_factor;          /* VCU_RR_PDF: floor of the weights, a fraction of their mean */
@@ -744,8 +746,11 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
                 for (int c = 0; c < CH; ++c) {
                     if (CH == 1) /* float += double(factor) * float */
                         approx[c] = __double2float_rn((double)approx[c] + cfg.factor * (double)stage[warp][i][c]);
-                    else /* 3-channel value type: double scale rounded per channel, then float add */
-                        approx[c] = vadd(approx[c], __double2float_rn(cfg.factor * (double)stage[warp][i][c]));
+                    else /* 3-channel value type: double scale rounded per channel (a float product when
+                          * prod(res) is an exact float), then float add */
+                        approx[c] = vadd(approx[c], cfg.factor_f32
+                                                        ? vmul(stage[warp][i][c], (float)cfg.factor)
+                                                        : __double2float_rn(cfg.factor * (double)stage[warp][i][c]));
                 }
             }
         __syncwarp();
@@ -793,8 +798,9 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
     }
     /* residual samples */
     /* per lane, in FP32: Kahan sums of the weighted samples, and the covariance moments of the
-     * sample norms (weight-strategy.h:187-208) by Welford's update; the lanes are merged in FP64
-     * (Chan's pairwise formulas), where the recombination also happens */
+     * sample norms (weight-strategy.h:187-208) by Welford's update.  Across lanes the sums merge as
+     * float-float pairs (two-sum, FP32) and the moments by Chan's formulas in FP64 with one division
+     * per step; the recombination is FP64 -- FP64 runs at a small fraction of the FP32 rate here */
     float sf32[CH], cf32[CH], sa32[CH], ca32[CH];
     for (int c = 0; c < CH; ++c) sf32[c] = cf32[c] = sa32[c] = ca32[c] = 0.0f;
     float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f;
@@ -942,6 +948,11 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             if (CH == 1) {
                 fs[c] = __double2float_rn((double)fv[c] * cfg.factor * rrf * (double)sfac);
                 as[c] = __double2float_rn((double)gv[c] * cfg.factor * rrf * (double)sfac);
+            } else if (cfg.rr == VCU_RR_UNIFORM && cfg.factor_f32) {
+                /* per channel each scale rounds to float once; with prod(res) and n integers below 2^24
+                 * the double product of a float and either is exact, so the float products equal them */
+                fs[c] = vmul(vmul(vmul(fv[c], (float)cfg.factor), (float)n), sfac);
+                as[c] = vmul(vmul(vmul(gv[c], (float)cfg.factor), (float)n), sfac);
             } else { /* per channel: scales by double rounded to float, then the float point weight */
                 fs[c] = vmul(__double2float_rn((double)__double2float_rn((double)fv[c] * cfg.factor) * rrf), sfac);
                 as[c] = vmul(__double2float_rn((double)__double2float_rn((double)gv[c] * cfg.factor) * rrf), sfac);
@@ -966,16 +977,30 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         m2a32 = vfma(da, da2, m2a32);
         cfa32 = vfma(df, da2, cfa32);
     }
-    double sf[CH], sa[CH];
+    /* lanes merged in FP32: each Kahan sum as the float-float pair (sum, -compensation) added with
+     * two-sum, the moments by Chan's pairwise formulas (one division per step) */
+    float sfh[CH], sfl[CH], sah[CH], sal[CH];
     for (int c = 0; c < CH; ++c) {
-        sf[c] = (double)sf32[c] - (double)cf32[c];
-        sa[c] = (double)sa32[c] - (double)ca32[c];
+        sfh[c] = sf32[c];
+        sfl[c] = -cf32[c];
+        sah[c] = sa32[c];
+        sal[c] = -ca32[c];
     }
+    auto ff_add = [](float& h, float& l, float bh, float bl) {
+        float s_, e_;
+        two_sum(h, bh, s_, e_);
+        e_ = vadd(e_, vadd(l, bl));
+        two_sum(s_, e_, h, l);
+    };
+    /* the moments stay FP64 across lanes: alpha = cov/var can sit where a last-bit change of the
+     * moments moves the estimate (large sample weights whose f and g terms cancel) */
     double wn = wn32, mf = mf32, ma = ma32, m2a = m2a32, cfa = cfa32;
     for (int off2 = 16; off2 > 0; off2 >>= 1) {
         for (int c = 0; c < CH; ++c) {
-            sf[c] += __shfl_down_sync(0xffffffffu, sf[c], off2);
-            sa[c] += __shfl_down_sync(0xffffffffu, sa[c], off2);
+            const float bh = __shfl_down_sync(0xffffffffu, sfh[c], off2), bl = __shfl_down_sync(0xffffffffu, sfl[c], off2);
+            const float ch_ = __shfl_down_sync(0xffffffffu, sah[c], off2), cl = __shfl_down_sync(0xffffffffu, sal[c], off2);
+            ff_add(sfh[c], sfl[c], bh, bl);
+            ff_add(sah[c], sal[c], ch_, cl);
         }
         const double nb = __shfl_down_sync(0xffffffffu, wn, off2);
         const double mfb = __shfl_down_sync(0xffffffffu, mf, off2);
@@ -984,14 +1009,20 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         const double cb = __shfl_down_sync(0xffffffffu, cfa, off2);
         const double nt = wn + nb;
         if (nb > 0.0 && nt > 0.0) {
+            const double r = nb / nt; /* the one division of the step */
             const double dfm = mfb - mf, dam = mab - ma;
-            const double w = wn * nb / nt;
-            mf += dfm * nb / nt;
-            ma += dam * nb / nt;
+            const double w = wn * r;
+            mf += dfm * r;
+            ma += dam * r;
             m2a += m2b + dam * dam * w;
             cfa += cb + dfm * dam * w;
             wn = nt;
         }
+    }
+    double sf[CH], sa[CH];
+    for (int c = 0; c < CH; ++c) {
+        sf[c] = (double)sfh[c] + (double)sfl[c];
+        sa[c] = (double)sah[c] + (double)sal[c];
     }
     if (lane != 0) return;
     const double N = (n > 0) ? (double)cfg.spp : 0.0;
@@ -1108,6 +1139,7 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     rcfg.dimbins = p->dimbins;
     rcfg.nbins = g.nbins;
     rcfg.factor = (double)g.factor;
+    rcfg.factor_f32 = g.factor < (1ull << 24);
     rcfg.spp = cv.samples_per_bin;
     rcfg.k0 = (uint32_t)cv.seed;
     rcfg.k1 = (uint32_t)(cv.seed >> 32);
@@ -1161,13 +1193,13 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
                 const vcu_cv& cv, const float* d_replay, float* d_bins, float* d_approx, float* d_regions,
                 uint32_t& launches);
 
-/* which generator builds the heap: the waves from 512 splits on (VCU_CV_GENERATOR=wave|sequential
+/* which generator builds the heap: the waves from 128 splits on (VCU_CV_GENERATOR=wave|sequential
  * overrides), the single-block sequential one below that or when the waves give up */
 inline bool use_waves(int iters) {
     const char* e = std::getenv("VCU_CV_GENERATOR");
     if (e && std::strcmp(e, "sequential") == 0) return false;
     if (e && std::strcmp(e, "wave") == 0) return iters > 0;
-    return iters >= 512;
+    return iters >= 128;
 }
 
 template <int DIM, int SH, int SL, class F>

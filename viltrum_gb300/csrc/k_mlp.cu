@@ -506,7 +506,8 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
         float vol = 1.0f;
         for (int d = 0; d < D; ++d) vol = vmul(vol, vsub(hi[d], lo[d]));
         /* per lane, in FP32: Welford means and squared deviations of f and of f - g; merged across
-         * the lanes in FP64 (Chan's pairwise formulas) */
+         * the lanes in FP32 too (Chan's pairwise formulas, one division per step): FP64 runs at a
+         * small fraction of the FP32 rate, and the means are only summed into the estimate in FP64 */
         float wn = 0.0f, mf = 0.0f, m2f = 0.0f, mr = 0.0f, m2r = 0.0f;
         for (uint64_t base = 0; base < c.spp; base += 32) {
             const uint64_t s = base + lane;
@@ -558,29 +559,30 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
                 m2r = vfma(dr, vsub(rv, mr), m2r);
             }
         }
-        double n_a = wn, mf_a = mf, m2f_a = m2f, mr_a = mr, m2r_a = m2r;
+        float n_a = wn, mf_a = mf, m2f_a = m2f, mr_a = mr, m2r_a = m2r;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double n_b = __shfl_xor_sync(0xffffffffu, n_a, o);
-            const double mf_b = __shfl_xor_sync(0xffffffffu, mf_a, o);
-            const double m2f_b = __shfl_xor_sync(0xffffffffu, m2f_a, o);
-            const double mr_b = __shfl_xor_sync(0xffffffffu, mr_a, o);
-            const double m2r_b = __shfl_xor_sync(0xffffffffu, m2r_a, o);
-            const double nt = n_a + n_b;
-            if (nt > 0.0) {
-                const double w = n_a * n_b / nt, df = mf_b - mf_a, dr = mr_b - mr_a;
-                mf_a += df * n_b / nt;
-                mr_a += dr * n_b / nt;
-                m2f_a += m2f_b + df * df * w;
-                m2r_a += m2r_b + dr * dr * w;
+            const float n_b = __shfl_xor_sync(0xffffffffu, n_a, o);
+            const float mf_b = __shfl_xor_sync(0xffffffffu, mf_a, o);
+            const float m2f_b = __shfl_xor_sync(0xffffffffu, m2f_a, o);
+            const float mr_b = __shfl_xor_sync(0xffffffffu, mr_a, o);
+            const float m2r_b = __shfl_xor_sync(0xffffffffu, m2r_a, o);
+            const float nt = vadd(n_a, n_b);
+            if (nt > 0.0f) {
+                const float r = vdiv(n_b, nt);
+                const float w = vmul(n_a, r), df = vsub(mf_b, mf_a), dr = vsub(mr_b, mr_a);
+                mf_a = vfma(df, r, mf_a);
+                mr_a = vfma(dr, r, mr_a);
+                m2f_a = vadd(m2f_a, vfma(vmul(df, df), w, m2f_b));
+                m2r_a = vadd(m2r_a, vfma(vmul(dr, dr), w, m2r_b));
                 n_a = nt;
             }
         }
         if (lane == 0) {
             const double scale = (double)c.factor * (double)vol;
-            const double est_cv = scale * ((double)integral[bin] + mr_a);
-            const double est_mc = scale * mf_a;
-            const double var_r = n_a > 0.0 ? m2r_a / n_a : 0.0, var_f = n_a > 0.0 ? m2f_a / n_a : 0.0;
+            const double est_cv = scale * ((double)integral[bin] + (double)mr_a);
+            const double est_mc = scale * (double)mf_a;
+            const double var_r = n_a > 0.0f ? (double)m2r_a / n_a : 0.0, var_f = n_a > 0.0f ? (double)m2f_a / n_a : 0.0;
             const bool use_mc = c.fallback && var_f < var_r;
             const float o = (float)(use_mc ? est_mc : est_cv);
             bins[bin] = o;
