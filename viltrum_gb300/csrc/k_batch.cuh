@@ -52,8 +52,21 @@ struct Item {
     int32_t dim, method, index, pad;
 };
 
-/* words of shared scratch the nested items of rule S need (line metrics, fold ping-pong,
- * node coordinates, per-dimension errors) */
+/* splits a round of a nested item attempts together: the heap's top and the regions that by their
+ * keys pop after it, as many as keep a round near two passes of 512 threads (2..8) */
+template <int DIM, int S> __host__ __device__ constexpr int spec_width() {
+    const int tasks = ipow(S, DIM) + (S - 1) * ipow(S, DIM - 1); /* one split's children */
+    const int k = 1024 / tasks;
+    return k < 2 ? 2 : (k > 8 ? 8 : k);
+}
+/* words of shared scratch one round of a DIM-dimensional item of rule S needs: line metrics and the
+ * first fold level of 2K children, node coordinates of K parents, per-dimension errors, the
+ * children's node values, ranges and volumes */
+template <int DIM, int S> __host__ __device__ constexpr int round_words() {
+    const int K = spec_width<DIM, S>(), NL = ipow(S, DIM - 1), SD = ipow(S, DIM);
+    return 2 * K * DIM * NL + 2 * K * DIM * NL / S + K * DIM * S + K * (S - 1) + 2 * K * DIM + 2 * K * SD +
+           2 * K * 2 * VCU_MAX_DIM + 2 * K;
+}
 template <int S> __host__ __device__ constexpr int max_nl() {
     int best = 1;
     for (int d = 1; d <= VCU_MAX_DIM; ++d)
@@ -61,11 +74,16 @@ template <int S> __host__ __device__ constexpr int max_nl() {
     return best;
 }
 template <int S> __host__ __device__ constexpr int scratch_words() {
-    return 2 * VCU_MAX_DIM * max_nl<S>()         /* line metrics of two regions */
-           + 2 * VCU_MAX_DIM * max_nl<S>() / S   /* first fold level           */
-           + VCU_MAX_DIM * S + S                 /* node coordinates           */
-           + 2 * VCU_MAX_DIM                     /* per-dimension errors       */
-           + 2 * max_nl<S>() * S;                /* node values of the two children of a split */
+    int best = 0;
+    for (int d = 1; d <= VCU_MAX_DIM; ++d) {
+        if (ipow(S, d) > 729) break;
+        const int K = 1024 / (ipow(S, d) + (S - 1) * ipow(S, d - 1));
+        const int Kc = K < 2 ? 2 : (K > 8 ? 8 : K), NL = ipow(S, d - 1), SD = ipow(S, d);
+        const int w = 2 * Kc * d * NL + 2 * Kc * d * NL / S + Kc * d * S + Kc * (S - 1) + 2 * Kc * d + 2 * Kc * SD +
+                      2 * Kc * 2 * VCU_MAX_DIM + 2 * Kc;
+        if (w > best) best = w;
+    }
+    return best;
 }
 
 /* the integral of a region's polynomial over [A,B] (normalised) as the reference rounds it: folds
@@ -166,13 +184,17 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
     constexpr int NL = ipow(S, DIM - 1);
     constexpr int NNEW = (S - 1) * NL;
     const int tid = threadIdx.x, nth = blockDim.x;
-    float* LN = sm;                                 /* 2*DIM*NL line metrics      */
-    float* LF = LN + 2 * VCU_MAX_DIM * max_nl<S>(); /* first fold level           */
-    float* CO = LF + 2 * VCU_MAX_DIM * max_nl<S>() / S;
-    float* CN = CO + VCU_MAX_DIM * S;
-    float* EC = CN + S;
-    float* VC0 = EC + 2 * VCU_MAX_DIM; /* the two children of the current split, on chip */
-    float* VC1 = VC0 + max_nl<S>() * S;
+    constexpr int K = spec_width<DIM, S>();
+    constexpr int TASKS = NNEW + S * NL; /* one split's children: new nodes, then the parent's */
+    static_assert(round_words<DIM, S>() <= scratch_words<S>(), "scratch too small for a round");
+    float* LN = sm;                          /* 2K*DIM*NL line metrics          */
+    float* LF = LN + 2 * K * DIM * NL;       /* first fold level                */
+    float* CO = LF + 2 * K * DIM * NL / S;   /* K x DIM*S node coordinates      */
+    float* CN = CO + K * DIM * S;            /* K x (S-1) new coordinates       */
+    float* EC = CN + K * (S - 1);            /* 2K x DIM errors                 */
+    float* VC = EC + 2 * K * DIM;            /* 2K x SD children node values    */
+    float* CR = VC + 2 * K * SD;             /* 2K x SLOT_FLOATS children ranges */
+    float* CV = CR + 2 * K * SLOT_FLOATS;    /* 2K children volumes             */
     float* V = vals + it.val_off;
     float* R = ranges + it.slot_off * SLOT_FLOATS;
     float* VOL = vols + it.slot_off;
@@ -180,18 +202,18 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
     const HeapSplit h{hs, heap + it.heap_off, cfg.hcap};
     const int iters = (int)it.budget - 1;
 
-    /* error estimates of the regions whose node values are in R0 (and R1) into EC[r*DIM + d]
-     * (region.h:379-418); volumes of slots s0, s1 */
-    auto region_errors = [&](int nreg, const float* R0, const float* R1, int s0, int s1) {
+    /* error estimates of the nreg regions whose node values are VC[r*SD ..] and volumes CV[r] into
+     * EC[r*DIM + d] (region.h:379-418) */
+    auto region_errors = [&](int nreg) {
         /* line metrics LN[(r*DIM + d)*NL + J]: the line of region r along dimension d whose other
          * coordinates are J's digits; its nodes are base + i*S^d */
         static_for<DIM>([&](auto dc) {
             constexpr int d = decltype(dc)::value;
             constexpr int PD = ipow(S, d);
             for (int t = tid; t < nreg * NL; t += nth) {
-                const int r = t >= NL ? 1 : 0;
+                const int r = t / NL;
                 const int J = t - r * NL;
-                const float* RV = (r ? R1 : R0) + (J % PD + (J / PD) * (PD * S));
+                const float* RV = VC + r * SD + (J % PD + (J / PD) * (PD * S));
                 float line[S], low[SL];
 #pragma unroll
                 for (int i = 0; i < S; ++i) line[i] = RV[i * PD];
@@ -219,13 +241,13 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
             src = dst;
             dst = sw;
         });
-        if (tid < nreg * DIM) EC[tid] = vmul(VOL[(tid / DIM) ? s1 : s0], src[tid]);
+        if (tid < nreg * DIM) EC[tid] = vmul(CV[tid / DIM], src[tid]);
         __syncthreads();
     };
-    /* error_heuristic_default / error_heuristic_size (error-heuristic.h:10-47) */
-    auto heuristic = [&](int r, int s, float& err_out, int& dim_out) {
+    /* error_heuristic_default / error_heuristic_size (error-heuristic.h:10-47) of region r with ranges
+     * rs (rmin at 0, rmax at VCU_MAX_DIM) */
+    auto heuristic = [&](int r, const float* rs, float& err_out, int& dim_out) {
         const float* e = EC + r * DIM;
-        const float* rs = R + (size_t)s * SLOT_FLOATS;
         if (cfg.heuristic == VCU_HEUR_DEFAULT) {
             float max_err = 0.0f;
             int max_dim = 0;
@@ -268,6 +290,7 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
             vol = vmul(vol, vsub(it.rmax[d], it.rmin[d]));
         }
         VOL[0] = vol;
+        CV[0] = vol;
     }
     for (int t = tid; t < DIM * S; t += nth) {
         const int d = t / S, j = t % S;
@@ -286,94 +309,135 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
         }
         float v[1];
         f(x, v);
-        VC0[t] = v[0];
+        VC[t] = v[0];
         V[t] = v[0];
     }
     __syncthreads();
-    region_errors(1, VC0, VC0, 0, 0);
-    __shared__ int s_top, s_scratch;
+    region_errors(1);
+    __shared__ int s_cand[8], s_slot[16], s_nc, s_adv, s_scratch;
     if (tid == 0) {
         float e;
         int dm;
-        heuristic(0, 0, e, dm);
+        heuristic(0, R, e, dm);
         h.set(0, HeapEntry{e, 0 | (dm << 24)});
         s_scratch = 1;
     }
 
+    /* Rounds: split the heap's top and the K-1 regions that by their keys pop after it, all children
+     * on chip; then commit in order -- split q only if, after splits 0..q-1 went into the heap, q's
+     * region is exactly the top the sequential algorithm pops (same entry) -- and copy the committed
+     * children to the pool.  Slots follow the sequential scheme (first child in the slot the previous
+     * split freed, second in slot k+2), so the result is the sequential one, bit for bit. */
+    int k = 0;
 #pragma unroll 1
-    for (int k = 0; k < iters; ++k) {
+    while (k < iters) {
         __syncthreads();
-        if (tid == 0) s_top = h.get(0).pay;
+        if (tid == 0) {
+            const int n = k + 1; /* heap size */
+            int nc = (K < iters - k) ? K : iters - k;
+            /* the next pops by key: a small queue of heap positions whose parents were taken */
+            int qpos[2 * 8 + 2];
+            float qkey[2 * 8 + 2];
+            int qn = 0;
+            s_cand[0] = h.get(0).pay;
+            for (int c = 1; c <= 2; ++c)
+                if (c < n) {
+                    qpos[qn] = c;
+                    qkey[qn] = h.get(c).key;
+                    ++qn;
+                }
+            for (int c = 1; c < nc; ++c) {
+                if (qn == 0) {
+                    nc = c;
+                    break;
+                }
+                int b = 0;
+                for (int i = 1; i < qn; ++i)
+                    if (qkey[b] < qkey[i]) b = i;
+                const int pos = qpos[b];
+                s_cand[c] = h.get(pos).pay;
+                qpos[b] = qpos[qn - 1];
+                qkey[b] = qkey[qn - 1];
+                --qn;
+                for (int ch = 2 * pos + 1; ch <= 2 * pos + 2; ++ch)
+                    if (ch < n) {
+                        qpos[qn] = ch;
+                        qkey[qn] = h.get(ch).key;
+                        ++qn;
+                    }
+            }
+            s_nc = nc;
+        }
         __syncthreads();
-        const int top = s_top;
-        const int P = top & 0xffffff, dd = top >> 24;
-        const int C0 = s_scratch, C1 = k + 2;
-        const float* pr = R + (size_t)P * SLOT_FLOATS;
-        for (int t = tid; t < DIM * S + (S - 1); t += nth) {
-            if (t < DIM * S) {
-                const int d = t / S, j = t % S;
-                CO[t] = node_coord(node_pos<S>(j), vsub(pr[VCU_MAX_DIM + d], pr[d]), pr[d]);
+        const int nc = s_nc;
+        /* node coordinates of each candidate, and of its new nodes along its split dimension */
+        for (int t = tid; t < nc * (DIM * S + (S - 1)); t += nth) {
+            const int q = t / (DIM * S + (S - 1)), u = t - q * (DIM * S + (S - 1));
+            const int P = s_cand[q] & 0xffffff, dd = s_cand[q] >> 24;
+            const float* pr = R + (size_t)P * SLOT_FLOATS;
+            if (u < DIM * S) {
+                const int d = u / S, j = u % S;
+                CO[q * DIM * S + u] = node_coord(node_pos<S>(j), vsub(pr[VCU_MAX_DIM + d], pr[d]), pr[d]);
             } else {
-                const int q = t - DIM * S;
-                CN[q] = node_coord(mid_pos<S>(q), vsub(pr[VCU_MAX_DIM + dd], pr[dd]), pr[dd]);
+                const int c = u - DIM * S;
+                CN[q * (S - 1) + c] = node_coord(mid_pos<S>(c), vsub(pr[VCU_MAX_DIM + dd], pr[dd]), pr[dd]);
             }
         }
         __syncthreads();
-        const float* VP = V + (size_t)P * SD;
-        float* V0 = V + (size_t)C0 * SD;
-        float* V1 = V + (size_t)C1 * SD;
-        /* region.h:345-359 / split.h:13-49: new nodes at the odd positions, parent nodes at the even;
-         * the children are built on chip and copied to the pool for later splits and the final sum.
-         * One instance per split dimension, so every stride and divisor is a constant. */
-        auto build_children = [&](auto ddc) {
+        /* region.h:345-359 / split.h:13-49: new nodes at the odd positions, parent nodes at the even,
+         * built on chip.  One instance per split dimension, so every stride and divisor is a constant. */
+        auto build_children = [&](auto ddc, int q, int u) {
             constexpr int DD = decltype(ddc)::value;
             constexpr int PD = ipow(S, DD);
-            for (int t = tid; t < NNEW + S * NL; t += nth) {
-                const bool fresh = t < NNEW;
-                const int u = fresh ? t : t - NNEW;
-                const int q = u / NL, J = u - q * NL;
-                const int base = J % PD + (J / PD) * (PD * S);
-                float v;
-                int i;
-                if (fresh) {
-                    float x[F::DIM];
+            const int P = s_cand[q] & 0xffffff;
+            const float* VP = V + (size_t)P * SD;
+            float* W0 = VC + (2 * q) * SD;
+            float* W1 = W0 + SD;
+            const bool fresh = u < NNEW;
+            const int w = fresh ? u : u - NNEW;
+            const int c = w / NL, J = w - c * NL;
+            const int base = J % PD + (J / PD) * (PD * S);
+            float v;
+            int i;
+            if (fresh) {
+                float x[F::DIM];
 #pragma unroll
-                    for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
-                    static_for<DIM>([&](auto ec) {
-                        constexpr int e = decltype(ec)::value;
-                        if constexpr (e != DD) {
-                            constexpr int pe = e < DD ? ipow(S, e) : ipow(S, e - 1);
-                            x[e] = CO[e * S + (J / pe) % S];
-                        }
-                    });
-                    x[DD] = CN[q];
-                    float fv[1];
-                    f(x, fv);
-                    v = fv[0];
-                    i = 2 * q + 1;
-                } else {
-                    v = VP[base + q * PD];
-                    i = 2 * q;
-                }
-                if (i <= S - 1) {
-                    VC0[base + i * PD] = v;
-                    V0[base + i * PD] = v;
-                }
-                if (i >= S - 1) {
-                    VC1[base + (i - (S - 1)) * PD] = v;
-                    V1[base + (i - (S - 1)) * PD] = v;
-                }
+                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+                static_for<DIM>([&](auto ec) {
+                    constexpr int e = decltype(ec)::value;
+                    if constexpr (e != DD) {
+                        constexpr int pe = e < DD ? ipow(S, e) : ipow(S, e - 1);
+                        x[e] = CO[q * DIM * S + e * S + (J / pe) % S];
+                    }
+                });
+                x[DD] = CN[q * (S - 1) + c];
+                float fv[1];
+                f(x, fv);
+                v = fv[0];
+                i = 2 * c + 1;
+            } else {
+                v = VP[base + c * PD];
+                i = 2 * c;
             }
+            if (i <= S - 1) W0[base + i * PD] = v;
+            if (i >= S - 1) W1[base + (i - (S - 1)) * PD] = v;
         };
-        static_for<DIM>([&](auto dc) {
-            if (dd == decltype(dc)::value) build_children(dc);
-        });
-        if (tid == 0) {
+        for (int t = tid; t < nc * TASKS; t += nth) {
+            const int q = t / TASKS, u = t - q * TASKS;
+            const int dd = s_cand[q] >> 24;
+            static_for<DIM>([&](auto dc) {
+                if (dd == decltype(dc)::value) build_children(dc, q, u);
+            });
+        }
+        /* the children's ranges and volumes */
+        for (int q = tid; q < nc; q += nth) {
+            const int P = s_cand[q] & 0xffffff, dd = s_cand[q] >> 24;
+            const float* pr = R + (size_t)P * SLOT_FLOATS;
             const float pmn = pr[dd], pmx = pr[VCU_MAX_DIM + dd];
             const float half = vdiv(vsub(pmx, pmn), 2.0f);
             const float mid = vadd(pmn, vmul(half, 1.0f));
-            float* r0 = R + (size_t)C0 * SLOT_FLOATS;
-            float* r1 = R + (size_t)C1 * SLOT_FLOATS;
+            float* r0 = CR + (2 * q) * SLOT_FLOATS;
+            float* r1 = r0 + SLOT_FLOATS;
             float vol0 = 1.0f, vol1 = 1.0f;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
@@ -387,24 +451,54 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
                 vol0 = vmul(vol0, vsub(mx0, mn));
                 vol1 = vmul(vol1, vsub(mx, mn1));
             }
-            VOL[C0] = vol0;
-            VOL[C1] = vol1;
+            CV[2 * q] = vol0;
+            CV[2 * q + 1] = vol1;
         }
         __syncthreads();
-        region_errors(2, VC0, VC1, C0, C1);
+        region_errors(2 * nc);
         if (tid == 0) {
-            float e0, e1;
-            int d0, d1;
-            heuristic(0, C0, e0, d0);
-            heuristic(1, C1, e1, d1);
-            const int n = k + 1; /* heap size before this split */
-            heap_pop_entries(h, n);
-            h.set(n - 1, HeapEntry{e0, C0 | (d0 << 24)});
-            heap_push_entries(h, n);
-            h.set(n, HeapEntry{e1, C1 | (d1 << 24)});
-            heap_push_entries(h, n + 1);
-            s_scratch = P; /* the split region's slot holds the next split's first child */
+            int adv = 0, scratch = s_scratch;
+            for (int q = 0; q < nc; ++q) {
+                if (q > 0 && h.get(0).pay != s_cand[q]) break;
+                const int C0 = scratch, C1 = k + q + 2;
+                const float* r0 = CR + (2 * q) * SLOT_FLOATS;
+                const float* r1 = r0 + SLOT_FLOATS;
+                float* d0r = R + (size_t)C0 * SLOT_FLOATS;
+                float* d1r = R + (size_t)C1 * SLOT_FLOATS;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    d0r[d] = r0[d];
+                    d0r[VCU_MAX_DIM + d] = r0[VCU_MAX_DIM + d];
+                    d1r[d] = r1[d];
+                    d1r[VCU_MAX_DIM + d] = r1[VCU_MAX_DIM + d];
+                }
+                VOL[C0] = CV[2 * q];
+                VOL[C1] = CV[2 * q + 1];
+                float e0, e1;
+                int dm0, dm1;
+                heuristic(2 * q, r0, e0, dm0);
+                heuristic(2 * q + 1, r1, e1, dm1);
+                const int n = k + q + 1; /* heap size before this split */
+                heap_pop_entries(h, n);
+                h.set(n - 1, HeapEntry{e0, C0 | (dm0 << 24)});
+                heap_push_entries(h, n);
+                h.set(n, HeapEntry{e1, C1 | (dm1 << 24)});
+                heap_push_entries(h, n + 1);
+                s_slot[2 * q] = C0;
+                s_slot[2 * q + 1] = C1;
+                scratch = s_cand[q] & 0xffffff; /* the split region's slot holds the next first child */
+                ++adv;
+            }
+            s_scratch = scratch;
+            s_adv = adv;
         }
+        __syncthreads();
+        const int adv = s_adv;
+        for (int t = tid; t < adv * 2 * SD; t += nth) {
+            const int r = t / SD, i = t - r * SD;
+            V[(size_t)s_slot[r] * SD + i] = VC[r * SD + i];
+        }
+        k += adv;
     }
     __syncthreads();
     /* ---- every region's integral over (range n region), in heap order; the single bin's range has
@@ -632,9 +726,12 @@ int run_batch_pair(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_
             auto kern = k_batch<F, SH, SL>;
             const size_t fixed = ((sizeof(F) + 15) & ~size_t(15)) + 8 + (size_t)scratch_words<SH>() * 4;
             auto smem_for = [&](int hcap) { return fixed + (size_t)(hcap + 1) * sizeof(HeapEntry); };
-            if (smem_for(1) > ctx->smem_optin) return fail(ctx, VCU_UNSUPPORTED, "integrand too large for the batch kernel");
-            VCU_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)(ctx->smem_optin - (MC_LANES * sizeof(double) + 64))));
+            /* dynamic shared memory: what the opt-in limit leaves beside the kernel's static arrays */
+            cudaFuncAttributes fa;
+            VCU_CUDA(ctx, cudaFuncGetAttributes(&fa, kern));
+            const size_t room = ctx->smem_optin - fa.sharedSizeBytes;
+            if (smem_for(1) > room) return fail(ctx, VCU_UNSUPPORTED, "integrand too large for the batch kernel");
+            VCU_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room));
             const size_t smem = smem_for(1);
             vcu_batch_state& P = ctx->batch;
             P.valid = false;
@@ -665,7 +762,6 @@ int run_batch_pair(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_
             auto launch_with = [&](int si) -> int {
                 int hcap = shapes[si].hcap;
                 /* the kernel's static shared memory (Monte Carlo lanes, a few words) comes on top */
-                const size_t room = ctx->smem_optin - (MC_LANES * sizeof(double) + 64);
                 while (hcap > 1 && smem_for(hcap) > room) hcap = (hcap - 1) / 2;
                 const size_t sm = smem_for(hcap);
                 int per_sm = 0;
