@@ -74,3 +74,30 @@ def test_cpp_dropin_links(lib_path, tmp_path):
     """The standalone form of the example links against libviltrum_cuda.so with the host compiler only."""
     r = _compile_dropin(["-O1"], out=str(tmp_path / "dropin"))
     assert r.returncode == 0, r.stderr
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror in viltrum_gb300/_lib.py has the C struct's size and field offsets (the
+    host compiler prints them from include/viltrum_cuda.h)."""
+    from viltrum_gb300 import _lib
+    pairs = {"vcu_integrand": _lib.Integrand, "vcu_problem": _lib.Problem, "vcu_nested": _lib.Nested, "vcu_stats": _lib.Stats, "vcu_cv": _lib.CvOpts,
+             "vcu_learned": _lib.LearnedOpts, "vcu_learned_report": _lib.LearnedReport, "vcu_opts": _lib.Opts,
+             "vcu_batch_item": _lib.BatchItem, "vcu_batch_report": _lib.BatchReport}
+    lines = ['#include <cstdio>', '#include <cstddef>', '#include "viltrum_cuda.h"', "int main() {"]
+    for cname, cls in pairs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.cc"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        c, f, v = ln.split()
+        got[(c, f)] = int(v)
+    for cname, cls in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
