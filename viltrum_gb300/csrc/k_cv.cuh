@@ -27,8 +27,8 @@
  *     region uniformly (rr_uniform_region, weight n) and a uniform point in bin n region (weight
  *     volume), pushes f*w and g*w (g = the region polynomial, region.h:103-112) into the
  *     cv_optimize_weight / cv_fixed_weight estimator (weight-strategy.h:7-110); sums in FP32 (Kahan
- *     per lane, float-float across lanes), moments FP32 per lane and FP64 across lanes, the final
- *     recombination (sum_f - a*sum_g)/n + a*approximation in FP64.  Sample j of bin b draws from
+ *     per lane, float-float across lanes), moments FP32 per lane and float-float across lanes, the
+ *     final recombination (sum_f - a*sum_g)/n + a*approximation in FP64.  Sample j of bin b draws from
  *     Philox4x32-10 (key = seed, counter = (j, b_lo, b_hi, 0xC0DE0000 | block)), or replays given
  *     (chosen list index, point) records.
  */
@@ -642,6 +642,39 @@ __device__ __forceinline__ float norm1(const float* v, int ch) {
     return s;
 }
 
+/* float-float numbers: value = h + l with |l| <= ulp(h)/2, about 48 significant bits from FP32
+ * operations (two-sum / two-product with an exact FMA; division by one Newton-style correction) */
+namespace ffn {
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ FF make(float a) { return FF{a, 0.0f}; }
+__device__ __forceinline__ FF norm(float s, float e) { /* |s| >= |e| */
+    const float h = vadd(s, e);
+    return FF{h, vsub(e, vsub(h, s))};
+}
+__device__ __forceinline__ FF add(FF a, FF b) {
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    return norm(s, vadd(e, vadd(a.l, b.l)));
+}
+__device__ __forceinline__ FF sub(FF a, FF b) { return add(a, FF{-b.h, -b.l}); }
+__device__ __forceinline__ FF mul(FF a, FF b) {
+    float p, e;
+    two_prod(a.h, b.h, p, e);
+    return norm(p, vfma(a.h, b.l, vfma(a.l, b.h, e)));
+}
+__device__ __forceinline__ FF div(FF a, FF b) {
+    const float q1 = vdiv(a.h, b.h);
+    const FF r = sub(a, mul(b, make(q1)));
+    return norm(q1, vdiv(r.h, b.h));
+}
+__device__ __forceinline__ FF shfl_down(FF a, int off) {
+    return FF{__shfl_down_sync(0xffffffffu, a.h, off), __shfl_down_sync(0xffffffffu, a.l, off)};
+}
+__device__ __forceinline__ double to_double(FF a) { return (double)a.h + (double)a.l; }
+}  // namespace ffn
+
 template <class F, int DIM, int S, bool PDF>
 __global__ void __launch_bounds__(RES_WARPS * 32)
     k_cv_residual(const __grid_constant__ F f, const ResCfg cfg, const uint32_t* __restrict__ offsets,
@@ -720,7 +753,6 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
     };
     /* control-variate integral, summed in list order as the reference does */
     float approx[CH];
-    double approx_d[CH];
     for (int c = 0; c < CH; ++c) approx[c] = cfg.approx_init ? cfg.approx_init[bin * CH + c] : 0.0f;
     for (uint32_t base = 0; base < n; base += RES_CHUNK) {
         const uint32_t m = (n - base < RES_CHUNK) ? n - base : RES_CHUNK;
@@ -757,7 +789,6 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
     }
     for (int c = 0; c < CH; ++c) {
         approx[c] = __shfl_sync(0xffffffffu, approx[c], 0);
-        approx_d[c] = (double)approx[c];
     }
     /* importance choice among the bin's regions (region-russian-roulette.h:30-149): weights floored at
      * 1% (rr_pdf_region: its factor) of their mean (all 1 when they sum to <= 0), then
@@ -799,8 +830,8 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
     /* residual samples */
     /* per lane, in FP32: Kahan sums of the weighted samples, and the covariance moments of the
      * sample norms (weight-strategy.h:187-208) by Welford's update.  Across lanes the sums merge as
-     * float-float pairs (two-sum, FP32) and the moments by Chan's formulas in FP64 with one division
-     * per step; the recombination is FP64 -- FP64 runs at a small fraction of the FP32 rate here */
+     * float-float pairs (two-sum, FP32) and the moments by Chan's formulas in float-float; only the
+     * recombination is FP64 -- FP64 runs at a small fraction of the FP32 rate here */
     float sf32[CH], cf32[CH], sa32[CH], ca32[CH];
     for (int c = 0; c < CH; ++c) sf32[c] = cf32[c] = sa32[c] = ca32[c] = 0.0f;
     float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f;
@@ -992,9 +1023,11 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         e_ = vadd(e_, vadd(l, bl));
         two_sum(s_, e_, h, l);
     };
-    /* the moments stay FP64 across lanes: alpha = cov/var can sit where a last-bit change of the
-     * moments moves the estimate (large sample weights whose f and g terms cancel) */
-    double wn = wn32, mf = mf32, ma = ma32, m2a = m2a32, cfa = cfa32;
+    /* the moments merge in float-float (~48 bits): alpha = cov/var can sit where a last-bit change
+     * of FP32 moments moves the estimate (large sample weights whose f and g terms cancel), and FP64
+     * runs at a small fraction of the FP32 rate here */
+    ffn::FF mf = ffn::make(mf32), ma = ffn::make(ma32), m2a = ffn::make(m2a32), cfa = ffn::make(cfa32);
+    float wn = wn32;
     for (int off2 = 16; off2 > 0; off2 >>= 1) {
         for (int c = 0; c < CH; ++c) {
             const float bh = __shfl_down_sync(0xffffffffu, sfh[c], off2), bl = __shfl_down_sync(0xffffffffu, sfl[c], off2);
@@ -1002,51 +1035,61 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
             ff_add(sfh[c], sfl[c], bh, bl);
             ff_add(sah[c], sal[c], ch_, cl);
         }
-        const double nb = __shfl_down_sync(0xffffffffu, wn, off2);
-        const double mfb = __shfl_down_sync(0xffffffffu, mf, off2);
-        const double mab = __shfl_down_sync(0xffffffffu, ma, off2);
-        const double m2b = __shfl_down_sync(0xffffffffu, m2a, off2);
-        const double cb = __shfl_down_sync(0xffffffffu, cfa, off2);
-        const double nt = wn + nb;
-        if (nb > 0.0 && nt > 0.0) {
-            const double r = nb / nt; /* the one division of the step */
-            const double dfm = mfb - mf, dam = mab - ma;
-            const double w = wn * r;
-            mf += dfm * r;
-            ma += dam * r;
-            m2a += m2b + dam * dam * w;
-            cfa += cb + dfm * dam * w;
+        const float nb = __shfl_down_sync(0xffffffffu, wn, off2);
+        const ffn::FF mfb = ffn::shfl_down(mf, off2), mab = ffn::shfl_down(ma, off2);
+        const ffn::FF m2b = ffn::shfl_down(m2a, off2), cb = ffn::shfl_down(cfa, off2);
+        const float nt = vadd(wn, nb); /* counts: exact */
+        if (nb > 0.0f && nt > 0.0f) {
+            const ffn::FF r = ffn::div(ffn::make(nb), ffn::make(nt));
+            const ffn::FF dfm = ffn::sub(mfb, mf), dam = ffn::sub(mab, ma);
+            const ffn::FF w = ffn::mul(ffn::make(wn), r);
+            mf = ffn::add(mf, ffn::mul(dfm, r));
+            ma = ffn::add(ma, ffn::mul(dam, r));
+            m2a = ffn::add(m2a, ffn::add(m2b, ffn::mul(ffn::mul(dam, dam), w)));
+            cfa = ffn::add(cfa, ffn::add(cb, ffn::mul(ffn::mul(dfm, dam), w)));
             wn = nt;
         }
     }
-    double sf[CH], sa[CH];
-    for (int c = 0; c < CH; ++c) {
-        sf[c] = (double)sfh[c] + (double)sfl[c];
-        sa[c] = (double)sah[c] + (double)sal[c];
-    }
     if (lane != 0) return;
-    const double N = (n > 0) ? (double)cfg.spp : 0.0;
-    double out[CH];
+    /* the recombination (sum_f - a sum_g)/n + a approximation (weight-strategy.h:94-101) in
+     * float-float too: each FP64 instruction costs the whole warp's issue slots many times over on
+     * this part, and ~48 bits leave the float result unchanged but for rare last-bit ties */
+    using ffn::FF;
+    auto exact_ff = [](double v) { /* v's nearest float-float */
+        const float h = __double2float_rn(v);
+        return FF{h, __double2float_rn(v - (double)h)};
+    };
+    const FF N = (n > 0) ? exact_ff((double)cfg.spp) : ffn::make(0.0f);
+    FF alpha = ffn::make(1.0f);
+    bool use_approx = (n == 0 || cfg.spp == 0); /* no residual samples: the approximation alone */
     if (cfg.weight == VCU_CV_FIXED) {
-        for (int c = 0; c < CH; ++c)
-            out[c] = (N == 0.0) ? approx_d[c] : (sf[c] - cfg.alpha * sa[c]) / N + cfg.alpha * approx_d[c];
+        alpha = exact_ff(cfg.alpha);
     } else {
-        double alpha = 1.0;
-        if (N >= 2.0) {
-            const double cov = cfa / (N - 1.0);
-            const double var = m2a / (N - 1.0);
-            const double vv = var > 0.0 ? var : 0.0;
-            if (vv > 0.0) {
-                const double cc = cov > 0.0 ? cov : 0.0;
-                alpha = (cc < vv ? cc : vv) / vv;
+        use_approx = use_approx || N.h < 2.0f;
+        if (!use_approx) {
+            const FF nm1 = ffn::sub(N, ffn::make(1.0f));
+            const FF cov = ffn::div(cfa, nm1), var = ffn::div(m2a, nm1);
+            const FF vv = var.h > 0.0f ? var : ffn::make(0.0f);
+            if (vv.h > 0.0f) {
+                const FF cc = cov.h > 0.0f ? cov : ffn::make(0.0f);
+                const bool lt = cc.h < vv.h || (cc.h == vv.h && cc.l < vv.l);
+                alpha = ffn::div(lt ? cc : vv, vv);
             }
         }
-        for (int c = 0; c < CH; ++c)
-            out[c] = (N < 2.0) ? approx_d[c] : (sf[c] - alpha * sa[c]) / N + alpha * approx_d[c];
+    }
+    FF out[CH];
+    for (int c = 0; c < CH; ++c) {
+        const FF ap = ffn::make(approx[c]);
+        if (use_approx) {
+            out[c] = ap;
+        } else {
+            const FF sf = FF{sfh[c], sfl[c]}, sa = FF{sah[c], sal[c]};
+            out[c] = ffn::add(ffn::div(ffn::sub(sf, ffn::mul(alpha, sa)), N), ffn::mul(alpha, ap));
+        }
     }
     bool nan = false;
     for (int c = 0; c < CH; ++c) {
-        const float o = (float)out[c];
+        const float o = vadd(out[c].h, out[c].l);
         nan = nan || isnan(o);
         bins[bin * CH + c] = o;
         if (approx_out) approx_out[bin * CH + c] = approx[c];
