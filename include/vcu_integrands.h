@@ -191,7 +191,8 @@ enum IntegrandKind : int32_t {
     VCU_F_SCENE2 = 5,         /* Gaussian bumps + hard-edged disks on 2-D                          */
     VCU_F_MOVING_SCENE3 = 6,  /* bumps + disks moving over t, RGB, on 3-D (x, y, t)                */
     VCU_F_HALFSPACE = 7,      /* prod_d e^{-a_d x_d} cos(b_d x_d) [n.x < c], 2..6-D                */
-    VCU_F_OCCLUDED_SCENE5 = 8 /* SCENE2(x,y) times box visibility of a segment, 5-D                */
+    VCU_F_OCCLUDED_SCENE5 = 8, /* SCENE2(x,y) times box visibility of a segment, 5-D               */
+    VCU_F_WALK2 = 9           /* random walk over SCENE2 from (x,y): unbounded dimensions          */
 };
 
 constexpr int kMaxGauss = 64;
@@ -568,6 +569,98 @@ struct OccludedScene5 {
         o0[0] = (s[0] == 0.0f) ? 0.0f : vmul(s[0], blocked0 ? 0.0f : 1.0f);
         o1[0] = (s[1] == 0.0f) ? 0.0f : vmul(s[1], blocked1 ? 0.0f : 1.0f);
     }
+};
+
+/* ---------------------------------------------------------------- unbounded dimensions
+ * Philox4x32-10 (Salmon et al., SC'11) on host and device alike: the stream of uniforms an
+ * integrand of unbounded dimension draws after its first coordinates. */
+VCU_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
+#endif
+}
+VCU_HD void philox_round(uint32_t* c, uint32_t k0, uint32_t k1) {
+    const uint32_t h0 = mulhi32(0xD2511F53u, c[0]), l0 = 0xD2511F53u * c[0];
+    const uint32_t h1 = mulhi32(0xCD9E8D57u, c[2]), l1 = 0xCD9E8D57u * c[2];
+    const uint32_t n0 = h1 ^ c[1] ^ k0, n2 = h0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = l1;
+    c[2] = n2;
+    c[3] = l0;
+}
+VCU_HD void philox10(uint32_t* c, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        philox_round(c, k0, k1);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+/* A random walk over the 2-D scene, an integrand of unbounded dimension (viltrum's
+ * range_infinite / random_sequence integrands, src/range-infinite.h, src/monte-carlo/random-
+ * sequence-*.h): coordinates 0-1 start the walk at (x, y) with the scene's value there; then each
+ * bounce draws three more -- it continues with probability `keep` (weight *= albedo / keep), turns
+ * by 2 pi u and moves u * step on the torus [0,1)^2, adding the weighted scene value -- for at most
+ * `max_bounces` bounces.  walk() takes the coordinates from any source (a reference random
+ * sequence, a device stream); operator() draws them from a Philox stream keyed by the point, so the
+ * library's 2-D integrators see a function of (x, y). */
+struct Walk2 {
+    static constexpr int DIM = 2, CH = 1;
+    static constexpr bool kUnbounded = true;
+    Scene2 scene;
+    float albedo, keep, step;
+    int32_t max_bounces;
+    uint32_t k0, k1; /* key of the coordinates after the first two */
+
+    /* params: albedo, keep, step, max_bounces, key, then the scene's parameters */
+    int build(const float* p, int n) {
+        if (n < 5) return 1;
+        albedo = p[0];
+        keep = p[1];
+        step = p[2];
+        max_bounces = (int32_t)p[3];
+        if (!(keep > 0.0f && keep <= 1.0f) || max_bounces < 0 || max_bounces > 4096) return 1;
+        k0 = (uint32_t)p[4];
+        k1 = 0x5EED0000u;
+        return scene.build(p + 5, n - 5);
+    }
+    template <class Next> VCU_HD float walk(float x, float y, Next&& next) const {
+        float v = scene.eval(x, y);
+        float w = 1.0f;
+        const float gain = vdiv(albedo, keep);
+        for (int k = 0; k < max_bounces; ++k) {
+            if (!(next() < keep)) break;
+            w = vmul(w, gain);
+            const float ang = vmul(next(), 6.2831854820251465f);
+            const float len = vmul(next(), step);
+            x = vfma(len, vcos(ang), x);
+            y = vfma(len, vsin(ang), y);
+            x = vsub(x, floorf(x));
+            y = vsub(y, floorf(y));
+            v = vfma(w, scene.eval(x, y), v);
+        }
+        return v;
+    }
+    /* the walk from (x, y) whose further coordinates are stream `idx` of the point */
+    VCU_HD float sample(float x, float y, uint32_t idx) const {
+        uint32_t c[4], blk = 0;
+        int used = 4;
+        auto next = [&]() {
+            if (used == 4) {
+                c[0] = float_to_bits(x);
+                c[1] = float_to_bits(y);
+                c[2] = idx;
+                c[3] = blk++;
+                philox10(c, k0, k1);
+                used = 0;
+            }
+            return (float)(c[used++] >> 8) * 5.9604644775390625e-08f;
+        };
+        return walk(x, y, next);
+    }
+    VCU_HD void operator()(const float* x, float* out) const { out[0] = sample(x[0], x[1], 0u); }
 };
 
 }  // namespace vcu

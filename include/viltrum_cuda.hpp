@@ -93,6 +93,9 @@ public:
     static builtin_integrand scene2(std::vector<float> p) { return {vcu::VCU_F_SCENE2, std::move(p)}; }
     static builtin_integrand moving_scene3(std::vector<float> p) { return {vcu::VCU_F_MOVING_SCENE3, std::move(p)}; }
     static builtin_integrand halfspace(std::vector<float> p) { return {vcu::VCU_F_HALFSPACE, std::move(p)}; }
+    /* the random walk over scene2: unbounded dimension (integrate it over the first two coordinates,
+     * e.g. viltrum::range_infinite(0, 0, 1, 1); it draws the rest itself) */
+    static builtin_integrand walk2(std::vector<float> p) { return {vcu::VCU_F_WALK2, std::move(p)}; }
     static builtin_integrand occluded_scene5(std::vector<float> p) {
         return {vcu::VCU_F_OCCLUDED_SCENE5, std::move(p)};
     }

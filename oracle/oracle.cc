@@ -1152,6 +1152,14 @@ template <class Visitor> int with_integrand(int32_t kind, const float* params, i
         default: return 2;
         }
     }
+    case vcu::VCU_F_WALK2: {
+        if (dim != 2) return 2;
+        auto* f = new vcu::Walk2;
+        if (f->build(params, n)) { delete f; return 3; }
+        const int r = v(*f, std::integral_constant<int, 2>{}, float{});
+        delete f;
+        return r;
+    }
     case vcu::VCU_F_OCCLUDED_SCENE5: {
         if (dim != 5) return 2;
         auto* f = new vcu::OccludedScene5;

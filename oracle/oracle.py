@@ -222,6 +222,24 @@ class Oracle:
         self._check(rc, "integrate_single")
         return float(out[0])
 
+    def walk(self, params, rmin, rmax, res, method, spp, seed, iterations=0, mc_samples=0):
+        """The random walk over the scene (an integrand of unbounded dimension) over
+        range_infinite(rmin, rmax): per-bin Monte Carlo (method 0) or crespo2021_infinite<2> (method
+        1), the unmodified reference only."""
+        params = np.ascontiguousarray(params, np.float32)
+        rmin = np.ascontiguousarray(rmin, np.float32)
+        rmax = np.ascontiguousarray(rmax, np.float32)
+        res = np.ascontiguousarray(res, np.uint64)
+        out = np.zeros(int(np.prod(res)), dtype=np.float32)
+        f = getattr(self.lib, self.prefix + "walk")
+        f.restype = ctypes.c_int
+        f.argtypes = [_f32p, ctypes.c_int32, _f32p, _f32p, _u64p, ctypes.c_int32, ctypes.c_uint64, ctypes.c_uint64,
+                      ctypes.c_uint64, ctypes.c_uint64, _f32p]
+        rc = f(_ptr(params), params.size, _ptr(rmin), _ptr(rmax), _ptr(res, _u64p), method, spp, seed, iterations,
+               mc_samples, _ptr(out))
+        self._check(rc, "walk")
+        return out
+
     def crespo2021_infinite(self, kind, params, rmin, rmax, res, iterations, mc_samples, spp, seed):
         """integrator_crespo2021_infinite<2> over a finite range (the unmodified reference only)."""
         params, rmin, rmax, res = self._problem(params, rmin, rmax, res)

@@ -373,6 +373,53 @@ extern "C" int ref_control_variates(int32_t kind, const float* params, int32_t n
     });
 }
 
+/* the walk over the scene as the reference takes an integrand of unbounded dimension: a callable
+ * on its random sequence (src/monte-carlo/random-sequence-*.h), read in order */
+struct RefWalk {
+    const vcu::Walk2* w;
+    template <class Seq> float operator()(const Seq& seq) const {
+        auto it = seq.begin();
+        const float x = *it;
+        ++it;
+        const float y = *it;
+        ++it;
+        return w->walk(x, y, [&]() {
+            const float v = *it;
+            ++it;
+            return v;
+        });
+    }
+};
+
+/* over range_infinite(rmin, rmax) (two listed dimensions, the rest [0,1]): per-bin Monte Carlo
+ * (method 0: integrator_per_bin_parallel(monte_carlo(spp, seed))) or crespo2021_infinite<2>
+ * (method 1, iterations, mc_samples) into res[0] x res[1] bins */
+extern "C" int ref_walk(const float* params, int32_t n_params, const float* rmin, const float* rmax,
+                        const uint64_t* res, int32_t method, uint64_t spp, uint64_t seed, uint64_t iterations,
+                        uint64_t mc_samples, float* out) {
+    auto* fn = new vcu::Walk2;
+    if (fn->build(params, n_params)) {
+        delete fn;
+        return 3;
+    }
+    RefWalk f{fn};
+    const auto range = viltrum::range_infinite(rmin[0], rmin[1], rmax[0], rmax[1]);
+    BinStore<2, float> bs{mk_res<2>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.assign(nb, 0.0f);
+    auto bins = [&bs](const std::array<std::size_t, 2>& q) -> float& { return bs.v[bs.lin(q)]; };
+    if (method == 0)
+        viltrum::integrate(viltrum::integrator_per_bin_parallel(viltrum::monte_carlo(spp, seed)), bins, bs.res, f,
+                           range);
+    else
+        viltrum::integrate(viltrum::integrator_crespo2021_infinite<2>(iterations, mc_samples, spp, seed), bins, bs.res,
+                           f, range);
+    for (std::size_t i = 0; i < nb; ++i) out[i] = bs.v[i];
+    delete fn;
+    return 0;
+}
+
 /* integrator_crespo2021_infinite<2>(iterations, mc_samples, spp, seed) over the finite range of the
  * moving-disk scene: regions over (x, y), time integrated by Monte Carlo in every evaluation
  * (src/control-variates/integrator-crespo2021.h:24-44) */

@@ -192,6 +192,22 @@ FUBINI_CASES = [
 ]
 
 
+# the random walk over the scene (an integrand of unbounded dimension) over range_infinite: the
+# reference's per-bin Monte Carlo and crespo2021_infinite<2>, several seeds each (statistical)
+WALK_CASES = [
+    ("walk_mc_bins16x16_spp256", dict(params=scenes.walk2(), rmin=[0, 0], rmax=[1, 1], res=[16, 16], walk_method=0,
+                                     spp=256, iterations=0, mc_samples=0, seeds=list(range(1, 9)))),
+    ("walk_crespo_infinite_bins16x16_it255_mc8_spp16", dict(params=scenes.walk2(), rmin=[0, 0], rmax=[1, 1],
+                                                            res=[16, 16], walk_method=1, spp=16, iterations=255,
+                                                            mc_samples=8, seeds=list(range(1, 9)))),
+]
+
+
+def run_walk(ref: orc.Oracle, kw: dict) -> np.ndarray:
+    return np.stack([ref.walk(kw["params"], kw["rmin"], kw["rmax"], kw["res"], kw["walk_method"], kw["spp"], seed,
+                              kw["iterations"], kw["mc_samples"]) for seed in kw["seeds"]])
+
+
 def run_fubini(ref: orc.Oracle, kw: dict) -> np.ndarray:
     return np.stack([ref.crespo2021_infinite(scenes.MOVING_SCENE3, kw["params"], kw["rmin"], kw["rmax"], kw["res"],
                                              kw["iterations"], kw["mc_samples"], kw["spp"], seed)
@@ -330,6 +346,12 @@ def main() -> int:
         out = run_fubini(ref, kw)
         meta = {k: np.asarray(v) for k, v in kw.items() if k != "params"}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="fubini", kind=scenes.MOVING_SCENE3,
+                            params=np.asarray(kw["params"], np.float32), **meta, out_bins=out)
+        print(f"ok {name} (reference outputs, compared statistically)")
+    for name, kw in WALK_CASES:
+        out = run_walk(ref, kw)
+        meta = {k: np.asarray(v) for k, v in kw.items() if k != "params"}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), method="walk", kind=scenes.WALK2,
                             params=np.asarray(kw["params"], np.float32), **meta, out_bins=out)
         print(f"ok {name} (reference outputs, compared statistically)")
     total = len(CASES) + len(BATCH_CASES) + len(GLOBAL_CASES) + len(TOL_CASES)

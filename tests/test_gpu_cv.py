@@ -286,3 +286,45 @@ def test_cv_fubini_python_api_and_limits(ctx):
         with pytest.raises(_lib.VcuError) as e:
             ctx.control_variates(prob, nst, 15, opts, np.empty(16 * 16 * 3, np.float32))
         assert e.value.code == code
+
+
+def test_walk_unbounded_dimension_against_reference_statistics(ctx):
+    """The random walk over the scene, an integrand of unbounded dimension over range_infinite:
+    fixtures hold the unmodified reference's per-bin Monte Carlo and crespo2021_infinite<2> bins for
+    eight seeds each.  Truth: the device's per-bin Monte Carlo with 2^16 walks per bin.  The
+    reference's seed mean lies within 4 standard errors of it in all but a few bins (the device's walk
+    has the reference's expectation), and over the same seeds the device's mean squared error for both
+    integrators is within [0.7, 1.4] of the reference's."""
+    gm = load_golden("walk_mc_bins16x16_spp256")
+    gc = load_golden("walk_crespo_infinite_bins16x16_it255_mc8_spp16")
+    params, res = gm["params"], [16, 16]
+    p = ctx.problem(scenes.WALK2, params, [0, 0], [1, 1], res)
+    truth = np.empty(256, np.float32)
+    ctx.per_bin_monte_carlo(p, 1 << 16, 99, truth)
+    truth = truth.astype(np.float64)
+    ref = gm["out_bins"].astype(np.float64)
+    se = ref.std(axis=0, ddof=1) / np.sqrt(ref.shape[0])
+    assert int((np.abs(ref.mean(axis=0) - truth) > 4 * se + 1e-6).sum()) <= 3
+    for g, run in ((gm, lambda s, o: ctx.per_bin_monte_carlo(p, int(gm["spp"]), s, o)),
+                   (gc, lambda s, o: ctx.control_variates(
+                       p, CRESPO, int(gc["iterations"]),
+                       _lib.CvOpts(int(gc["spp"]), s, 0, 0, 1.0, 0, 0, 0.01, 0, 1.0, 0.0, 2, int(gc["mc_samples"])), o))):
+        gpu_sq, ref_sq = [], []
+        for i, seed in enumerate(g["seeds"]):
+            out = np.empty(256, np.float32)
+            run(int(seed), out)
+            gpu_sq.append(np.mean((out - truth) ** 2))
+            ref_sq.append(np.mean((g["out_bins"][i] - truth) ** 2))
+        ratio = np.mean(gpu_sq) / np.mean(ref_sq)
+        assert 0.7 <= ratio <= 1.4, (str(g["method"]), gpu_sq, ref_sq)
+
+
+def test_walk_python_api(ctx):
+    bins = np.zeros((8, 8), np.float32)
+    v.integrate(v.integrator_per_bin_parallel(v.monte_carlo(64, 3)), bins, v.Integrand.walk2(),
+                v.range_infinite([0, 0], [1, 1]), ctx=ctx)
+    assert np.isfinite(bins).all() and bins.mean() > 0
+    c = np.zeros((8, 8), np.float32)
+    v.integrate(v.integrator_crespo2021_infinite(2, 127, 4, 8, 3), c, v.Integrand.walk2(),
+                v.range_infinite([0, 0], [1, 1]), ctx=ctx)
+    assert np.isfinite(c).all() and abs(c.mean() - bins.mean()) < 0.2 * bins.mean()

@@ -28,7 +28,7 @@ from ._lib import (MEM_DEVICE, MEM_HOST, RR_ERROR, RR_INTEGRAL, RR_PDF, RR_UNIFO
                    RS_RUSSIAN_ROULETTE, RS_UNIFORM, Context, Nested, VcuError, default_context, load)
 
 __all__ = [
-    "Context", "VcuError", "Integrand", "Range", "integrate", "range_", "range_all", "range_primary",
+    "Context", "VcuError", "Integrand", "Range", "integrate", "range_", "range_all", "range_primary", "range_infinite",
     "trapezoidal", "simpson", "boole", "nested", "error_metric_absolute", "error_metric_relative",
     "error_heuristic_default", "error_heuristic_size", "monte_carlo", "monte_carlo_per_bin_parallel",
     "integrator_per_bin_parallel", "integrator_adaptive_iterations", "integrator_adaptive_iterations_parallel",
@@ -71,6 +71,13 @@ def range_all(n: int, a: float, b: float) -> Range:
 def range_primary(n: int) -> Range:
     """range_primary<N>(): [0,1]^N (src/range.h:196-199)."""
     return range_all(n, 0.0, 1.0)
+
+
+def range_infinite(a, b) -> Range:
+    """range_infinite(a, b) (src/range-infinite.h:91-120): the listed leading dimensions; every
+    further one is [0,1].  For integrands of unbounded dimension (Integrand.walk2), which draw the
+    further coordinates themselves."""
+    return range_(a, b)
 
 
 # ------------------------------------------------------------------------------------ integrands
@@ -119,6 +126,13 @@ class Integrand:
     def occluded_scene5(cls, params=None, seed: int = 7):
         p = scenes.occluded_scene5(seed) if params is None else np.asarray(params, np.float32)
         return cls(scenes.OCCLUDED_SCENE5, p, 5)
+
+    @classmethod
+    def walk2(cls, params=None, seed: int = 7):
+        """The random walk over the 2-D scene: an integrand of unbounded dimension; integrate it over
+        range_infinite(a, b) (its first two coordinates; the rest are [0,1) and drawn per sample)."""
+        p = scenes.walk2(seed) if params is None else np.asarray(params, np.float32)
+        return cls(scenes.WALK2, p, 2)
 
 
 # ------------------------------------------------------------------------------------ rules

@@ -97,6 +97,16 @@ template <class F, int N> struct TailMC {
     __device__ void operator()(const float* x, float* out) const {
         float acc[CH];
         for (int c = 0; c < CH; ++c) acc[c] = 0.0f;
+        if constexpr (is_unbounded<F>::value) {
+            /* an integrand of unbounded dimension: the rest is its own stream, one per sample
+             * (the range beyond the first coordinates is [0,1) per dimension, volume 1) */
+            for (uint32_t s = 0; s < k; ++s) {
+                const float v = f.sample(x[0], x[1], tag ^ s);
+                acc[0] = __double2float_rn(__dadd_rn((double)acc[0], __dmul_rn((double)v, factor)));
+            }
+            out[0] = acc[0];
+            return;
+        }
         float full[F::DIM];
         for (int d = 0; d < F::DIM; ++d) full[d] = 0.0f;
         for (int d = 0; d < N; ++d) full[d] = x[d];

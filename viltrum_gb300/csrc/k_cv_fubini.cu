@@ -8,7 +8,7 @@ int run_cv_fubini(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vc
                   uint32_t& launches) {
     return with_integrand(ctx, p->f, p->dim, [&](const auto& f) -> int {
         using F = std::decay_t<decltype(f)>;
-        if constexpr (F::DIM < 3) {
+        if constexpr (F::DIM < 3 && !is_unbounded<F>::value) {
             return fail(ctx, VCU_UNSUPPORTED, "a Fubini tail needs an integrand of 3 or more dimensions");
         } else {
             cv_detail::TailMC<F, 2> t{};
@@ -20,6 +20,7 @@ int run_cv_fubini(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vc
             t.k0 = (uint32_t)key;
             t.k1 = (uint32_t)(key >> 32);
             t.tag = 0xF0B10000u;
+            if constexpr (is_unbounded<F>::value) t.f.k1 ^= (uint32_t)key; /* its own stream, keyed by the call too */
             float vol = 1.0f; /* Range<Float, DIM-N>::volume(), a float product (range.h) */
             for (int d = 2; d < p->dim; ++d) {
                 t.tmin[d] = p->range_min[d];

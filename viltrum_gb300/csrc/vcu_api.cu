@@ -276,7 +276,7 @@ extern "C" int vcu_last_error(const vcu_ctx* ctx, char* buf, size_t len) {
 extern "C" int vcu_channels(int32_t kind) {
     switch (kind) {
     case VCU_F_POLY2: case VCU_F_SIN1: case VCU_F_SPHERE3: case VCU_F_WAVE2: case VCU_F_SCENE2:
-    case VCU_F_HALFSPACE: case VCU_F_OCCLUDED_SCENE5:
+    case VCU_F_HALFSPACE: case VCU_F_OCCLUDED_SCENE5: case VCU_F_WALK2:
         return 1;
     case VCU_F_MOVING_SCENE3:
         return 3;
@@ -416,7 +416,8 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
         return fail(ctx, VCU_UNSUPPORTED, "the pdf strategies need a Simpson high rule (rules.h:102-248)");
     const bool fubini = cv->fubini_dims != 0;
     if (fubini) {
-        if (cv->fubini_dims != 2 || p->dim < 3 || p->dimbins > 2)
+        const bool unbounded = p->f.kind == VCU_F_WALK2; /* its tail has no finite dimension */
+        if (cv->fubini_dims != 2 || (p->dim < 3 && !unbounded) || p->dimbins > 2)
             return fail(ctx, VCU_UNSUPPORTED, "a Fubini tail takes regions over 2 dimensions of a 3+ dimensional "
                                               "integrand, at most 2 of them binned");
         if (cv->tail_samples == 0) return fail(ctx, VCU_INVALID_ARG, "tail_samples must be >= 1");

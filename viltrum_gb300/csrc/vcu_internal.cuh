@@ -163,6 +163,11 @@ struct has_pair<F, std::void_t<decltype(std::declval<const F&>().pair((const flo
                                                                         (float*)nullptr, (float*)nullptr))>>
     : std::true_type {};
 
+/* integrands of unbounded dimension (a kUnbounded member): their first DIM coordinates come from
+ * the integrator, the rest from a stream the functor draws itself */
+template <class F, class = void> struct is_unbounded : std::false_type {};
+template <class F> struct is_unbounded<F, std::void_t<decltype(F::kUnbounded)>> : std::bool_constant<F::kUnbounded> {};
+
 /* integrands that evaluate N points at once (multi<N>: N independent dependency chains per lane) */
 template <class F, class = void> struct has_multi : std::false_type {};
 template <class F>
@@ -209,6 +214,12 @@ template <class V> int with_integrand(vcu_ctx* ctx, const vcu_integrand& f, int 
         Halfspace fn{};
         if (fn.build(f.params, f.n_params)) return fail(ctx, VCU_INVALID_ARG, "bad half-space parameters");
         if (fn.dim != dim) break;
+        return v(fn);
+    }
+    case VCU_F_WALK2: {
+        if (dim != 2) break;
+        static thread_local Walk2 fn;
+        if (fn.build(f.params, f.n_params)) return fail(ctx, VCU_INVALID_ARG, "bad walk parameters");
         return v(fn);
     }
     case VCU_F_OCCLUDED_SCENE5: {

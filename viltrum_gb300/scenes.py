@@ -13,7 +13,7 @@ import numpy as np
 from scipy.special import erf
 
 # integrand tags (vcu_integrands.h)
-POLY2, SIN1, SPHERE3, WAVE2, SCENE2, MOVING_SCENE3, HALFSPACE, OCCLUDED_SCENE5 = 1, 2, 3, 4, 5, 6, 7, 8
+POLY2, SIN1, SPHERE3, WAVE2, SCENE2, MOVING_SCENE3, HALFSPACE, OCCLUDED_SCENE5, WALK2 = 1, 2, 3, 4, 5, 6, 7, 8, 9
 DIMS = {POLY2: 2, SIN1: 1, SPHERE3: 3, WAVE2: 2, SCENE2: 2, MOVING_SCENE3: 3, OCCLUDED_SCENE5: 5}
 CHANNELS = {MOVING_SCENE3: 3}
 
@@ -97,6 +97,14 @@ def batch_items(n: int, seed: int = 11, budget_lo: int = 256, budget_hi: int = 6
         items.append(dict(dim=dim, method=method, budget=budget, seed=item_seed,
                           params=halfspace(seed * 1000003 + i, dim), rmin=[0.0] * dim, rmax=[1.0] * dim))
     return items
+
+
+def walk2(seed: int = 7, n_gauss: int = 16, n_disk: int = 8, albedo: float = 0.6, keep: float = 0.7,
+          step: float = 0.15, max_bounces: int = 32, key: int = 11) -> np.ndarray:
+    """The random walk over scene2(seed): an integrand of unbounded dimension (vcu_integrands.h
+    Walk2): [albedo, keep, step, max_bounces, key] then the scene's parameters."""
+    return np.concatenate([np.array([albedo, keep, step, max_bounces, key], np.float32),
+                           scene2(seed, n_gauss, n_disk)]).astype(np.float32)
 
 
 def occluded_scene5(seed: int = 7, n_gauss: int = 64, n_disk: int = 32, n_box: int = 128) -> np.ndarray:
