@@ -79,6 +79,14 @@ VCU_HD float vabs(float a) {
     return std::fabs(a);
 #endif
 }
+/* index of the lowest set bit of a non-zero mask */
+VCU_HD int ctz64(uint64_t m) {
+#if defined(__CUDA_ARCH__)
+    return __ffsll((long long)m) - 1;
+#else
+    return __builtin_ctzll(m);
+#endif
+}
 VCU_HD uint32_t float_to_bits(float f) {
 #if defined(__CUDA_ARCH__)
     return __float_as_uint(f);
@@ -291,6 +299,80 @@ struct Scene2 {
         return acc;
     }
     VCU_HD void operator()(const float* x, float* out) const { out[0] = eval(x[0], x[1]); }
+    /* The terms that can be non-zero somewhere in the box [lo, hi]: a bump whose exponent rounds to
+     * -87 or below at every point of the box contributes exactly 0 (vexp returns 0 there and
+     * fma(a, 0, acc) == acc, acc never being -0), as does a disk that misses the box.  The test is
+     * conservative: the box grown by 1e-6 plus 1e-6 of each bound's magnitude (the evaluated points
+     * may stray a few ulps outside the box of a bin) and a 1e-4 relative margin on the squared
+     * distance, far above the rounding of the evaluation's own dx, dy, r^2 and product.  multi_cull() then sums
+     * only the kept terms, in the same order, so its results equal multi()'s bit for bit. */
+    struct Cull {
+        uint64_t g;
+        uint32_t d;
+    };
+    VCU_HD Cull cull(const float* lo, const float* hi) const {
+        auto grow = [](float v) { return vadd(1e-6f, vmul(v < 0.0f ? -v : v, 1e-6f)); };
+        const float x0 = vsub(lo[0], grow(lo[0])), y0 = vsub(lo[1], grow(lo[1]));
+        const float x1 = vadd(hi[0], grow(hi[0])), y1 = vadd(hi[1], grow(hi[1]));
+        auto dist2 = [&](float cx, float cy) {
+            const float ex = vsub(x0, cx), fx = vsub(cx, x1), ey = vsub(y0, cy), fy = vsub(cy, y1);
+            const float dx = ex > 0.0f ? ex : (fx > 0.0f ? fx : 0.0f);
+            const float dy = ey > 0.0f ? ey : (fy > 0.0f ? fy : 0.0f);
+            return vfma(dx, dx, vmul(dy, dy));
+        };
+        Cull c{0ull, 0u};
+        for (int i = 0; i < ng; ++i)
+            if (!(vmul(vmul(dist2(g[i][0], g[i][1]), -g[i][2]), 0.9999f) > 87.0f)) c.g |= 1ull << i;
+        for (int i = 0; i < nd; ++i)
+            if (!(vmul(dist2(d[i][0], d[i][1]), 0.9999f) > d[i][2])) c.d |= 1u << i;
+        return c;
+    }
+    template <int N> VCU_HD void multi_cull(const Cull& c, const float (*x)[DIM], float (*o)[CH]) const {
+        float a[N];
+        VCU_UNROLL
+        for (int p = 0; p < N; ++p) a[p] = 0.0f;
+        uint64_t m = c.g;
+        while (m) {
+            const int i = ctz64(m);
+            m &= m - 1;
+            const float gx0 = g[i][0], gy0 = g[i][1], gs0 = g[i][2], ga0 = g[i][3];
+            if (m) { /* two kept bumps per step, independent exponentials, the sum in order */
+                const int j = ctz64(m);
+                m &= m - 1;
+                const float gx1 = g[j][0], gy1 = g[j][1], gs1 = g[j][2], ga1 = g[j][3];
+                float e0[N], e1[N];
+                VCU_UNROLL
+                for (int p = 0; p < N; ++p) {
+                    const float dx0 = vsub(x[p][0], gx0), dy0 = vsub(x[p][1], gy0);
+                    const float dx1 = vsub(x[p][0], gx1), dy1 = vsub(x[p][1], gy1);
+                    e0[p] = vexp(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
+                    e1[p] = vexp(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
+                }
+                VCU_UNROLL
+                for (int p = 0; p < N; ++p) a[p] = vfma(ga1, e1[p], vfma(ga0, e0[p], a[p]));
+            } else {
+                VCU_UNROLL
+                for (int p = 0; p < N; ++p) {
+                    const float dx = vsub(x[p][0], gx0), dy = vsub(x[p][1], gy0);
+                    a[p] = vfma(ga0, vexp(vmul(vfma(dx, dx, vmul(dy, dy)), gs0)), a[p]);
+                }
+            }
+        }
+        uint32_t dm = c.d;
+        while (dm) {
+            const int i = ctz64(dm);
+            dm &= dm - 1;
+            const float cx = d[i][0], cy = d[i][1], rr = d[i][2], dv = d[i][3];
+            VCU_UNROLL
+            for (int p = 0; p < N; ++p) {
+                const float dx = vsub(x[p][0], cx), dy = vsub(x[p][1], cy);
+                const float r2 = vfma(dx, dx, vmul(dy, dy));
+                a[p] = vadd(a[p], (r2 <= rr) ? dv : 0.0f);
+            }
+        }
+        VCU_UNROLL
+        for (int p = 0; p < N; ++p) o[p][0] = a[p];
+    }
     /* N points at once, each with exactly the arithmetic of eval(): N independent chains */
     template <int N> VCU_HD void multi(const float (*x)[DIM], float (*o)[CH]) const {
         float a[N];

@@ -1,0 +1,100 @@
+"""The culled evaluation of the scene (multi_cull: only the terms that can be non-zero in a box)
+returns exactly what operator() returns at every point of the box -- checked on the host, where the
+same source compiles with the same explicitly rounded operations: boxes from 1/2048 of the square
+(finer than the benchmark's bins) to the whole square, at the origin and far from it, points drawn inside, on the edges and at the
+corners, and the node coordinates a nested rule places there."""
+import os
+import subprocess
+
+import numpy as np
+
+from conftest import ROOT
+from viltrum_gb300 import scenes
+
+PROG = r'''
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <vector>
+#include "vcu_integrands.h"
+int main(int argc, char** argv) {
+    std::vector<float> p;
+    FILE* fp = std::fopen(argv[1], "rb");
+    int n;
+    if (std::fread(&n, 4, 1, fp) != 1) return 2;
+    p.resize(n);
+    if (std::fread(p.data(), 4, n, fp) != (size_t)n) return 2;
+    std::fclose(fp);
+    const float off = (float)std::atof(argv[2]);
+    static vcu::Scene2 s;
+    if (s.build(p.data(), n)) return 3;
+    std::mt19937 rng(5);
+    std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+    long kept = 0, terms = 0, checked = 0;
+    const float widths[] = {1.0f / 2048, 1.0f / 512, 1.0f / 64, 1.0f / 8, 1.0f};
+    for (float w : widths) {
+        for (int b = 0; b < 2000; ++b) {
+            float lo[2], hi[2];
+            for (int k = 0; k < 2; ++k) {
+                const int cells = (int)(1.0f / w);
+                const int pos = (int)(u01(rng) * cells) % (cells > 0 ? cells : 1);
+                lo[k] = vcu::vadd(off, vcu::vmul((float)pos, w));
+                hi[k] = vcu::vadd(off, vcu::vmul((float)(pos + 1), w));
+            }
+            const auto c = s.cull(lo, hi);
+            kept += __builtin_popcountll(c.g) + __builtin_popcount(c.d);
+            terms += s.ng + s.nd;
+            for (int q = 0; q < 24; ++q) {
+                float x[4][2];
+                for (int t = 0; t < 4; ++t)
+                    for (int k = 0; k < 2; ++k) {
+                        const int mode = (q + t + k) % 6;
+                        /* inside, edges, corners, Boole's node positions */
+                        const float v = mode == 0 ? lo[k] : mode == 1 ? hi[k]
+                                      : mode == 2 ? vcu::vadd(lo[k], vcu::vmul(0.25f, vcu::vsub(hi[k], lo[k])))
+                                      : mode == 3 ? vcu::vadd(lo[k], vcu::vmul(0.75f, vcu::vsub(hi[k], lo[k])))
+                                      : vcu::vadd(lo[k], vcu::vmul(u01(rng), vcu::vsub(hi[k], lo[k])));
+                        x[t][k] = v;
+                    }
+                float o[4][1];
+                s.multi_cull<4>(c, x, o);
+                for (int t = 0; t < 4; ++t) {
+                    float r[1];
+                    s(x[t], r);
+                    ++checked;
+                    if (std::memcmp(r, o[t], 4)) {
+                        std::printf("mismatch w=%g box [%a,%a]x[%a,%a] at (%a,%a): %a vs %a\n", w, lo[0], hi[0],
+                                    lo[1], hi[1], x[t][0], x[t][1], r[0], o[t][0]);
+                        return 1;
+                    }
+                }
+            }
+        }
+    }
+    std::printf("%ld %ld %ld\n", checked, kept, terms);
+    return 0;
+}
+'''
+
+
+def test_culled_scene_equals_full_evaluation(tmp_path):
+    src = tmp_path / "cull.cc"
+    src.write_text(PROG)
+    exe = tmp_path / "cull"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe)], check=True)
+    # the scene over [0,1]^2, and moved to [100,101]^2 where a coordinate's ulp is 8e-6
+    for seed, off in ((7, 0.0), (3, 0.0), (7, 100.0)):
+        p = np.asarray(scenes.scene2(seed), np.float32)
+        ng, nd = int(p[0]), int(p[1])
+        for base in [2 + 4 * i for i in range(ng + nd)]:
+            p[base:base + 2] += np.float32(off)
+        f = tmp_path / f"p{seed}_{int(off)}.bin"
+        with open(f, "wb") as fh:
+            fh.write(np.int32(p.size).tobytes())
+            fh.write(p.tobytes())
+        r = subprocess.run([str(exe), str(f), str(off)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        checked, kept, terms = (int(x) for x in r.stdout.split())
+        assert checked == 5 * 2000 * 24 * 4 and kept < terms  # something is culled

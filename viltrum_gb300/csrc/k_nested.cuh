@@ -129,6 +129,18 @@ __device__ float region_subrange(const float* V, int c, const float* A, const fl
     return buf[0];
 }
 
+/* culled evaluation when the integrand supports it over the kernel's full dimension */
+template <class F, int DIM> constexpr bool use_cull = has_cull<F>::value && DIM == F::DIM;
+template <class F, bool = has_cull<F>::value> struct cull_of { using type = int; };
+template <class F> struct cull_of<F, true> { using type = typename F::Cull; };
+
+template <int N, int DIM, class F>
+__device__ __forceinline__ void eval_points(const F& f, const typename cull_of<F>::type& cl, const float (*xs)[F::DIM],
+                                            float (*vs)[F::CH]) {
+    if constexpr (use_cull<F, DIM>) f.template multi_cull<N>(cl, xs, vs);
+    else f.template multi<N>(xs, vs);
+}
+
 template <class F, int DIM, int SH, int SL, int G>
 __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_constant__ F f, const BinGrid g,
                                                                const NcCfg cfg, float* __restrict__ bins,
@@ -164,21 +176,47 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
 
     for (uint64_t bin = (uint64_t)blockIdx.x * gpb + gib; bin < g.nbins; bin += ngroups) {
         /* ---- bin sub-range (integrator-per-bin-parallel.h:30-32) */
-        float bmin[DIM], bmax[DIM];
-        {
-            uint64_t rem = bin;
+        auto bin_box = [&](uint64_t b, float* lo, float* hi) {
+            uint64_t rem = b;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
                 if (d < g.dimbins) {
                     const uint32_t pos = (uint32_t)(rem % g.res[d]);
                     rem /= g.res[d];
-                    bmin[d] = vadd(g.rmin[d], vmul((float)pos, g.drange[d]));
-                    bmax[d] = vadd(g.rmin[d], vmul((float)(pos + 1), g.drange[d]));
+                    lo[d] = vadd(g.rmin[d], vmul((float)pos, g.drange[d]));
+                    hi[d] = vadd(g.rmin[d], vmul((float)(pos + 1), g.drange[d]));
                 } else {
-                    bmin[d] = g.rmin[d];
-                    bmax[d] = g.rmax[d];
+                    lo[d] = g.rmin[d];
+                    hi[d] = g.rmax[d];
                 }
             }
+        };
+        float bmin[DIM], bmax[DIM];
+        bin_box(bin, bmin, bmax);
+        /* terms of the integrand that can be non-zero in the box of the bins of this warp's groups
+         * (consecutive bins): one list for the whole warp, so the term loop stays uniform */
+        [[maybe_unused]] typename cull_of<F>::type cl{};
+        if constexpr (use_cull<F, DIM>) {
+            constexpr int GPW = 32 / G;
+            const uint64_t w0 = bin - (uint64_t)(gib % GPW);
+            float lo[DIM], hi[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                lo[d] = bmin[d];
+                hi[d] = bmax[d];
+            }
+#pragma unroll 1
+            for (int k = 0; k < GPW; ++k) {
+                if (w0 + k >= g.nbins) break;
+                float l2[DIM], h2[DIM];
+                bin_box(w0 + k, l2, h2);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    lo[d] = fminf(lo[d], l2[d]);
+                    hi[d] = fmaxf(hi[d], h2[d]);
+                }
+            }
+            cl = f.cull(lo, hi);
         }
         /* ---- root region in slot 0 */
         if (gl == 0) {
@@ -212,7 +250,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                 float xs[NR][F::DIM], vs[NR][CH];
 #pragma unroll
                 for (int q = 0; q < NR; ++q) root_x(t + q * G < SD ? t + q * G : t, xs[q]);
-                f.template multi<NR>(xs, vs);
+                eval_points<NR, DIM>(f, cl, xs, vs);
 #pragma unroll
                 for (int q = 0; q < NR; ++q)
                     if (q == 0 || t + q * G < SD) {
@@ -386,7 +424,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                     float xs[NP][F::DIM], vs[NP][CH];
 #pragma unroll
                     for (int q = 0; q < NP; ++q) node_x(t + q * G < NNEW ? t + q * G : t, xs[q]);
-                    f.template multi<NP>(xs, vs);
+                    eval_points<NP, DIM>(f, cl, xs, vs);
 #pragma unroll
                     for (int q = 0; q < NP; ++q)
                         if (q == 0 || t + q * G < NNEW) store_new(t + q * G, vs[q]);

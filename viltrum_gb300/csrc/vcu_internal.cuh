@@ -174,6 +174,14 @@ template <class F>
 struct has_multi<F, std::void_t<decltype(std::declval<const F&>().template multi<2>(
                         (const float(*)[F::DIM]) nullptr, (float(*)[F::CH]) nullptr))>> : std::true_type {};
 
+/* integrands that can list the terms that may be non-zero in a box (cull) and evaluate only those
+ * (multi_cull<N>), bit for bit what multi<N> returns at any point of the box */
+template <class F, class = void> struct has_cull : std::false_type {};
+template <class F>
+struct has_cull<F, std::void_t<typename F::Cull,
+                               decltype(std::declval<const F&>().cull((const float*)nullptr, (const float*)nullptr))>>
+    : std::true_type {};
+
 /* Calls v(functor, channels) with the built-in functor selected by kind.  The functor object is
  * built on the host (vcu_integrands.h build()); its size decides the kernel parameter size. */
 template <class V> int with_integrand(vcu_ctx* ctx, const vcu_integrand& f, int dim, V&& v) {
