@@ -79,6 +79,26 @@ VCU_HD float vabs(float a) {
     return std::fabs(a);
 #endif
 }
+/* RN_d(x / D) of a float x (D = 3 or 5, the divisors of the reference's double-promoted Horner
+ * steps) without the double division routine: q0 = RN_d(x * RN_d(1/D)), then one correction by the
+ * exact remainder, q = RN_d(q0 + (x - q0*D) * RN_d(1/D)) (the correction step of Markstein's
+ * division; Brisebarre, Muller and Raina, IEEE Trans. Computers 53(8), 2004).  q equals the
+ * correctly rounded quotient for every finite non-zero float x (checked over all 2^32 floats;
+ * tests/test_ddivf.py re-checks every significand at several exponents); zeros, infinities and NaN
+ * return q0, which is exact for them. */
+template <int D> VCU_HD double ddiv_f(float xf) {
+    static_assert(D == 3 || D == 5, "ddiv_f: divisor not checked");
+    const double x = (double)xf;
+    constexpr double inv = 1.0 / (double)D;
+#if defined(__CUDA_ARCH__)
+    const double q0 = __dmul_rn(x, inv);
+    const double q = __fma_rn(__fma_rn(-q0, (double)D, x), inv, q0);
+#else
+    const double q0 = x * inv;
+    const double q = std::fma(std::fma(-q0, (double)D, x), inv, q0);
+#endif
+    return (xf != 0.0f && vabs(xf) <= 3.4028234663852886e38f) ? q : q0;
+}
 /* index of the lowest set bit of a non-zero mask */
 VCU_HD int ctz64(uint64_t m) {
 #if defined(__CUDA_ARCH__)

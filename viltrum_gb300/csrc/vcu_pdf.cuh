@@ -59,7 +59,7 @@ __device__ __forceinline__ float line_at(float t, const float* in) {
 
 /* cdf(t) of the lifted parabola (rules.h:176-180): float product, Horner steps in double */
 __device__ __forceinline__ float cdf(float t, const float* c) {
-    double r = __dadd_rn(__ddiv_rn((double)vmul(c[2], t), 3.0), __dmul_rn((double)c[1], 0.5));
+    double r = __dadd_rn(ddiv_f<3>(vmul(c[2], t)), __dmul_rn((double)c[1], 0.5));
     r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
     return __double2float_rn(__dmul_rn(r, (double)t));
 }
@@ -70,7 +70,7 @@ __device__ __forceinline__ double cuberoot(double x) { return (x < 0) ? -pow(-x,
 static __device__ __noinline__ int inv_cdf(float x, const float* q, float* sol) {
     float co[3];
     Rule<3>::coefficients(q, co);
-    double a = __ddiv_rn((double)co[2], 3.0);
+    double a = ddiv_f<3>(co[2]);
     double b = __dmul_rn((double)co[1], 0.5);
     float c = co[0];
     float d = -x;

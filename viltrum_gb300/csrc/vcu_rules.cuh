@@ -118,13 +118,13 @@ template <> __device__ __forceinline__ double horner_int_ref<2>(const float* c, 
     return __dmul_rn(r, (double)t);
 }
 template <> __device__ __forceinline__ double horner_int_ref<3>(const float* c, float t) {
-    double r = __dadd_rn(__ddiv_rn((double)vmul(c[2], t), 3.0), __dmul_rn((double)c[1], 0.5));
+    double r = __dadd_rn(ddiv_f<3>(vmul(c[2], t)), __dmul_rn((double)c[1], 0.5));
     r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
     return __dmul_rn(r, (double)t);
 }
 template <> __device__ __forceinline__ double horner_int_ref<5>(const float* c, float t) {
-    double r = __dadd_rn(__ddiv_rn((double)vmul(c[4], t), 5.0), __dmul_rn((double)c[3], 0.25));
-    r = __dadd_rn(__dmul_rn(r, (double)t), __ddiv_rn((double)c[2], 3.0));
+    double r = __dadd_rn(ddiv_f<5>(vmul(c[4], t)), __dmul_rn((double)c[3], 0.25));
+    r = __dadd_rn(__dmul_rn(r, (double)t), ddiv_f<3>(c[2]));
     r = __dadd_rn(__dmul_rn(r, (double)t), __dmul_rn((double)c[1], 0.5));
     r = __dadd_rn(__dmul_rn(r, (double)t), (double)c[0]);
     return __dmul_rn(r, (double)t);
