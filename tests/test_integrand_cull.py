@@ -98,3 +98,53 @@ def test_culled_scene_equals_full_evaluation(tmp_path):
         assert r.returncode == 0, r.stdout + r.stderr
         checked, kept, terms = (int(x) for x in r.stdout.split())
         assert checked == 5 * 2000 * 24 * 4 and kept < terms  # something is culled
+
+
+COUNT = r'''
+#include <cstdio>
+#include <vector>
+#include "vcu_integrands.h"
+int main(int argc, char** argv) {
+    std::vector<float> p;
+    FILE* fp = std::fopen(argv[1], "rb");
+    int n;
+    if (std::fread(&n, 4, 1, fp) != 1) return 2;
+    p.resize(n);
+    if (std::fread(p.data(), 4, n, fp) != (size_t)n) return 2;
+    std::fclose(fp);
+    static vcu::Scene2 s;
+    if (s.build(p.data(), n)) return 3;
+    const int res = 128;
+    double flops = 0.0;
+    for (int j = 0; j < res; ++j)
+        for (int i = 0; i < res; ++i) {
+            const float lo[2] = {vcu::vmul((float)i, 1.0f / res), vcu::vmul((float)j, 1.0f / res)};
+            const float hi[2] = {vcu::vmul((float)(i + 1), 1.0f / res), vcu::vmul((float)(j + 1), 1.0f / res)};
+            const auto c = s.cull(lo, hi);
+            flops += 31.0 * __builtin_popcountll(c.g) + 6.0 * __builtin_popcount(c.d);
+        }
+    std::printf("%.6f\n", flops / (res * res));
+    return 0;
+}
+'''
+
+
+def test_benchmark_flop_count_matches_the_cull(tmp_path):
+    """The benchmark's roofline counts the flops of the terms a bin keeps (bench.culled_flops_per_eval,
+    exact geometry); the device's conservative cull keeps at least those and only slightly more."""
+    import bench
+
+    src = tmp_path / "count.cc"
+    src.write_text(COUNT)
+    exe = tmp_path / "count"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe)], check=True)
+    p = np.asarray(scenes.scene2(7), np.float32)
+    f = tmp_path / "p.bin"
+    with open(f, "wb") as fh:
+        fh.write(np.int32(p.size).tobytes())
+        fh.write(p.tobytes())
+    r = subprocess.run([str(exe), str(f)], capture_output=True, text=True, check=True)
+    device = float(r.stdout)
+    model = bench.culled_flops_per_eval(p, [0, 0], [1, 1], [128, 128])
+    assert model <= device <= model * 1.01, (model, device)
