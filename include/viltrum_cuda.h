@@ -315,8 +315,8 @@ int vcu_integrate_batch_resident(vcu_ctx* ctx, float* results, int32_t results_m
 
 /* ------------------------------------------------------------------ allocation-free variant
  * No counterpart in the reference.  For host programs that must not allocate device memory -- a
- * plugin inside a process whose GPU memory belongs to another allocator, code running while the
- * caller builds a CUDA graph, or a service with a fixed memory budget -- this runs the same per-bin
+ * plugin inside a process whose GPU memory belongs to another allocator, a real-time frame loop
+ * that cannot take the device-wide synchronisation of cudaMalloc/cudaFree, or a service with a fixed memory budget -- this runs the same per-bin
  * adaptive nested quadrature as vcu_per_bin_adaptive_nested without a context and without any
  * cudaMalloc/cudaFree or allocating library call.  Its device scratch is a fixed array compiled
  * into the library (the status word plus a staging area of VCU_STATIC_MAX_BIN_VALUES floats for

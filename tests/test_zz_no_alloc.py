@@ -2,7 +2,8 @@
 entry point (vcu_per_bin_adaptive_nested) returns, on two calls in a row, through the C ABI.
 
 It exists for callers that may not allocate device memory (plugins inside another allocator's
-process, code running during graph capture, fixed-budget services): it uses only a scratch array
+process, real-time frame loops that cannot take cudaMalloc/cudaFree's device-wide
+synchronisation, fixed-budget services): it uses only a scratch array
 compiled into the library.  This file is collected last so a failure here does not hide the others;
 it passes alone in a fresh process and after the rest of the suite."""
 import ctypes

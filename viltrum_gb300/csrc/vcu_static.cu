@@ -3,9 +3,9 @@
  * memory.
  *
  * Some host programs must not call cudaMalloc at all: plugins loaded into a process whose CUDA
- * memory is owned by another allocator (a renderer or a framework with its own pool), code that runs
- * while a CUDA graph is being built around it, or hosts with a fixed memory budget checked at
- * start-up.  vcu_per_bin_adaptive_nested_static() serves them.  It creates no context and allocates
+ * memory is owned by another allocator (a renderer or a framework with its own pool), real-time
+ * frame loops that cannot take the device-wide synchronisation cudaMalloc/cudaFree may imply, or
+ * hosts with a fixed memory budget checked at start-up.  vcu_per_bin_adaptive_nested_static() serves them.  It creates no context and allocates
  * nothing: its only device scratch -- the status word and, for host-memory bins, the staging copy of
  * the bin values -- is the file-scope array below, which every GPU that loads the library holds until
  * the process exits.
