@@ -1349,3 +1349,31 @@ extern "C" int64_t orc_adaptive_tolerance(int32_t kind, const float* params, int
     });
     return rc ? -2 : leaves;
 }
+
+/* ------------------------------------------------------------------ accumulator and 1-D pdf probes */
+extern "C" int orc_cv_optimize_moments(const float* f, const float* g, uint64_t n, float approximation,
+                                       double* out) {
+    if ((n && (!f || !g)) || !out) return 1;
+    CvOptimize<float> acc(0.0f);
+    for (uint64_t i = 0; i < n; ++i) acc.push(f[i], g[i]);
+    out[0] = acc.variance();
+    out[1] = acc.covariance();
+    out[2] = acc.alpha();
+    out[3] = acc.integral(approximation);
+    return 0;
+}
+
+/* a 1-D region over [0,1] has volume 1 and maps positions unchanged, so its pdf and sampler are
+ * the Simpson line's own */
+extern "C" int orc_simpson_pdf_1d(const float* nodes, float t, float t0, float t1, float* out) {
+    if (!nodes || !out) return 1;
+    const auto ps = SimpsonPdf::points(nodes);
+    *out = SimpsonPdf::at(t, ps) / SimpsonPdf::integral(t0, t1, ps);
+    return 0;
+}
+
+extern "C" int orc_simpson_sample_1d(const float* nodes, float s, float t0, float t1, float* out) {
+    if (!nodes || !out) return 1;
+    *out = SimpsonPdf::sample(s, t0, t1, nodes);
+    return 0;
+}

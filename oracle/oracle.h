@@ -140,6 +140,20 @@ int orc_integrate_single(int32_t kind, const float* params, int32_t n_params, in
                          const float* rmin, const float* rmax, int32_t method, uint64_t budget,
                          uint64_t seed, const orc_nested* nested, float* out);
 
+
+/* Control-variate weight accumulator (cv_optimize_weight, src/control-variates/weight-strategy.h:40-110)
+ * fed the n pairs (f[i], g[i]) in order, f the function sample and g the approximation's ->
+ * out[0] = variance of g, out[1] = covariance of (f, g) (both online, shifted by the first pair,
+ * divided by n-1), out[2] = alpha, out[3] = integral(approximation). */
+int orc_cv_optimize_moments(const float* f, const float* g, uint64_t n, float approximation, double* out);
+
+/* A one-dimensional Simpson region over [0,1] whose three nodes hold nodes[3]
+ * (src/newton-cotes/region.h, rules.h:102-248):
+ *   pdf_1d    -> *out = pdf_subrange(t, [t0,t1])  (region.h:324-342)
+ *   sample_1d -> *out = sample_subrange(s, [t0,t1]) for a uniform s in [0,1)  (region.h:243-268) */
+int orc_simpson_pdf_1d(const float* nodes, float t, float t0, float t1, float* out);
+int orc_simpson_sample_1d(const float* nodes, float s, float t0, float t1, float* out);
+
 #ifdef __cplusplus
 }
 #endif

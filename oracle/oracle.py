@@ -115,6 +115,13 @@ class Oracle:
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32,
                       ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(Nested), _f32p]
+        f = getattr(L, prefix + "cv_optimize_moments")
+        f.restype = ctypes.c_int
+        f.argtypes = [_f32p, _f32p, ctypes.c_uint64, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]
+        for name in ("simpson_pdf_1d", "simpson_sample_1d"):
+            f = getattr(L, prefix + name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_f32p, ctypes.c_float, ctypes.c_float, ctypes.c_float, _f32p]
         f = getattr(L, prefix + "control_variates")
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
@@ -279,9 +286,41 @@ class Oracle:
             "regions": None if rg is None else rg.reshape(iterations + 1, 2, dim),
             "replay": None if rp is None else rp.reshape(nb, spp, width),
         }
+    # ------------------------------------------------------------------ probes of single pieces
+    def cv_optimize_moments(self, f, g, approximation=0.0):
+        """cv_optimize_weight's accumulator fed (f[i], g[i]) in order ->
+        (variance of g, covariance of f and g, alpha, integral(approximation))."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        g = np.ascontiguousarray(g, dtype=np.float32)
+        assert f.shape == g.shape
+        out = np.zeros(4, dtype=np.float64)
+        rc = getattr(self.lib, self.prefix + "cv_optimize_moments")(
+            _ptr(f), _ptr(g), f.size, approximation, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        self._check(rc, "cv_optimize_moments")
+        return tuple(float(v) for v in out)
+
+    def _simpson_1d(self, name, nodes, u, t0, t1):
+        nodes = np.ascontiguousarray(nodes, dtype=np.float32)
+        assert nodes.size == 3
+        out = np.zeros(1, dtype=np.float32)
+        fn = getattr(self.lib, self.prefix + name)
+        res = np.empty(len(u), dtype=np.float32)
+        for i, v in enumerate(u):
+            self._check(fn(_ptr(nodes), float(v), t0, t1, _ptr(out)), name)
+            res[i] = out[0]
+        return res
+
+    def simpson_pdf_1d(self, nodes, t, t0, t1):
+        """pdf_subrange at each t over [t0,t1] of a 1-D Simpson region over [0,1] with these nodes."""
+        return self._simpson_1d("simpson_pdf_1d", nodes, t, t0, t1)
+
+    def simpson_sample_1d(self, nodes, s, t0, t1):
+        """sample_subrange over [t0,t1] for each uniform s, same region."""
+        return self._simpson_1d("simpson_sample_1d", nodes, s, t0, t1)
 
 
 _port = None
+
 
 
 def port() -> Oracle:

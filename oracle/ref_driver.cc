@@ -552,3 +552,37 @@ extern "C" int64_t ref_adaptive_tolerance(int32_t kind, const float* params, int
     }
     return -9;
 }
+
+/* the weight accumulator and the 1-D Simpson pdf / sampler of the reference itself */
+extern "C" int ref_cv_optimize_moments(const float* f, const float* g, uint64_t n, float approximation,
+                                       double* out) {
+    if ((n && (!f || !g)) || !out) return 1;
+    auto acc = viltrum::cv_optimize_weight().accumulator<float>();
+    for (uint64_t i = 0; i < n; ++i) acc.push(f[i], g[i]);
+    out[0] = acc.variance();
+    out[1] = acc.covariance();
+    out[2] = acc.alpha();
+    out[3] = acc.integral(approximation);
+    return 0;
+}
+
+namespace {
+/* a region over [0,1] whose nodes 0, 0.5, 1 read the given values */
+auto node_region(const float* nodes) {
+    const float n0 = nodes[0], n1 = nodes[1], n2 = nodes[2];
+    auto f = [n0, n1, n2](const std::array<float, 1>& x) { return (x[0] == 0.0f) ? n0 : ((x[0] == 1.0f) ? n2 : n1); };
+    return viltrum::region(f, viltrum::simpson, viltrum::range(0.0f, 1.0f));
+}
+}  // namespace
+
+extern "C" int ref_simpson_pdf_1d(const float* nodes, float t, float t0, float t1, float* out) {
+    if (!nodes || !out) return 1;
+    *out = node_region(nodes).pdf_subrange(std::array<float, 1>{t}, viltrum::range(t0, t1));
+    return 0;
+}
+
+extern "C" int ref_simpson_sample_1d(const float* nodes, float s, float t0, float t1, float* out) {
+    if (!nodes || !out) return 1;
+    *out = node_region(nodes).sample_subrange(std::array<float, 1>{s}, viltrum::range(t0, t1))[0];
+    return 0;
+}

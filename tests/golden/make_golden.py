@@ -284,7 +284,55 @@ def run(lib: orc.Oracle, method: str, kw: dict) -> dict:
     raise ValueError(method)
 
 
+def pieces_inputs() -> dict:
+    """Inputs of the single-piece probes: the control-variate weight accumulator on paired samples
+    (the shape of main/compilation-tests/covariance.cc, plus constant, anti-correlated and one-sample
+    series) and the 1-D Simpson pdf / sampler (the node values of main/compilation-tests/region-sample.cc
+    and inverse.cc, plus lifted, constant and edge-peaked parabolas) over three sub-ranges."""
+    rng = np.random.default_rng(21)
+    x = rng.uniform(0, 2 * np.pi, 1000).astype(np.float32)
+    v0 = np.sin(x).astype(np.float32)
+    series = []
+    for n, noise in ((20, 0.1), (1000, 0.5)):
+        g = v0[:n]
+        f = (g + rng.uniform(-noise, noise, n)).astype(np.float32)
+        series.append((f, g))
+    series.append((v0[:50].copy(), np.full(50, 0.25, np.float32)))          # variance 0: alpha 1
+    series.append(((1.5 - np.abs(v0[:50])).astype(np.float32), v0[:50].copy()))  # |f|, |g| anti-correlated: alpha 0
+    series.append((v0[:1].copy(), v0[1:2].copy()))                          # one sample: the approximation
+    cv_len = np.array([len(f) for f, _ in series], np.int64)
+    nodes = np.array([[1, 0.2, 1], [0.43, 0.9, 0.42], [0, 0, 1], [1, -0.5, 1], [2, 2, 2], [0, 1, 0],
+                      [0.1, 3.0, 0.05]], np.float32)
+    ranges = np.array([[0, 1], [0, 0.125], [0.3, 0.7]], np.float32)
+    t = np.linspace(0.0, 1.0, 9).astype(np.float32)
+    s = np.concatenate([np.arange(10) * np.float32(0.1), rng.uniform(0, 1, 6)]).astype(np.float32)
+    return {"cv_f": np.concatenate([f for f, _ in series]), "cv_g": np.concatenate([g for _, g in series]),
+            "cv_len": cv_len, "cv_approx": np.float32(0.7), "nodes": nodes, "ranges": ranges, "t": t, "s": s}
+
+
+def run_pieces(lib: orc.Oracle, kw: dict) -> dict:
+    moments, off = [], 0
+    for n in kw["cv_len"]:
+        moments.append(lib.cv_optimize_moments(kw["cv_f"][off:off + n], kw["cv_g"][off:off + n], float(kw["cv_approx"])))
+        off += int(n)
+    pdf = np.zeros((len(kw["nodes"]), len(kw["ranges"]), len(kw["t"])), np.float32)
+    smp = np.zeros((len(kw["nodes"]), len(kw["ranges"]), len(kw["s"])), np.float32)
+    for i, nd in enumerate(kw["nodes"]):
+        for j, (t0, t1) in enumerate(kw["ranges"]):
+            # the pdf is read inside the sub-range: t mapped onto [t0, t1]
+            tt = (np.float32(t0) + kw["t"] * np.float32(t1 - t0)).astype(np.float32)
+            pdf[i, j] = lib.simpson_pdf_1d(nd, tt, float(t0), float(t1))
+            smp[i, j] = lib.simpson_sample_1d(nd, kw["s"], float(t0), float(t1))
+    return {"moments": np.array(moments, np.float64), "pdf": pdf, "samples": smp}
+
+
 def main() -> int:
+    """Regenerates every fixture, or only those whose names start with one of the arguments."""
+    only = sys.argv[1:]
+
+    def wanted(name: str) -> bool:
+        return not only or any(name.startswith(o) for o in only)
+
     ref = orc.reference()
     if ref is None:
         print("oracle/_ref/libvref.so is missing: run `make -C oracle ref` where the reference exists")
@@ -292,6 +340,8 @@ def main() -> int:
     port = orc.port()
     bad = 0
     for name, method, kw in CASES:
+        if not wanted(name):
+            continue
         r = run(ref, method, kw)
         p = run(port, method, kw)
         same = all(np.array_equal(r[k].view(np.uint32), p[k].view(np.uint32)) for k in r)
@@ -311,6 +361,8 @@ def main() -> int:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method=method, **meta, **{"out_" + k: v for k, v in r.items()})
         print(f"ok {name}")
     for name, kw in GLOBAL_CASES:
+        if not wanted(name):
+            continue
         r, p = run_global(ref, kw), run_global(port, kw)
         if not np.array_equal(r["bins"].view(np.uint32), p["bins"].view(np.uint32)):
             bad += 1
@@ -323,6 +375,8 @@ def main() -> int:
                             initial=global_initial(kw), **meta, out_bins=r["bins"])
         print(f"ok {name}")
     for name, kw in TOL_CASES:
+        if not wanted(name):
+            continue
         r, p = run_tolerance(ref, kw), run_tolerance(port, kw)
         if not np.array_equal(r["bins"].view(np.uint32), p["bins"].view(np.uint32)):
             bad += 1
@@ -334,6 +388,8 @@ def main() -> int:
                             initial=global_initial(kw), **meta, out_bins=r["bins"])
         print(f"ok {name}")
     for name, kw in BATCH_CASES:
+        if not wanted(name):
+            continue
         r, p = run_batch(ref, kw), run_batch(port, kw)
         if not np.array_equal(r["values"].view(np.uint32), p["values"].view(np.uint32)):
             bad += 1
@@ -343,18 +399,34 @@ def main() -> int:
                             out_values=r["values"])
         print(f"ok {name}")
     for name, kw in FUBINI_CASES:
+        if not wanted(name):
+            continue
         out = run_fubini(ref, kw)
         meta = {k: np.asarray(v) for k, v in kw.items() if k != "params"}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="fubini", kind=scenes.MOVING_SCENE3,
                             params=np.asarray(kw["params"], np.float32), **meta, out_bins=out)
         print(f"ok {name} (reference outputs, compared statistically)")
     for name, kw in WALK_CASES:
+        if not wanted(name):
+            continue
         out = run_walk(ref, kw)
         meta = {k: np.asarray(v) for k, v in kw.items() if k != "params"}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="walk", kind=scenes.WALK2,
                             params=np.asarray(kw["params"], np.float32), **meta, out_bins=out)
         print(f"ok {name} (reference outputs, compared statistically)")
-    total = len(CASES) + len(BATCH_CASES) + len(GLOBAL_CASES) + len(TOL_CASES)
+    if wanted("pieces_cv_moments_simpson_pdf"):
+        kw = pieces_inputs()
+        r, p = run_pieces(ref, kw), run_pieces(port, kw)
+        if all(np.array_equal(r[k].view(np.uint8), p[k].view(np.uint8)) for k in r):
+            np.savez_compressed(os.path.join(HERE, "pieces_cv_moments_simpson_pdf.npz"), method="pieces", **kw,
+                                **{"out_" + k: v for k, v in r.items()})
+            print("ok pieces_cv_moments_simpson_pdf")
+        else:
+            bad += 1
+            print("MISMATCH pieces_cv_moments_simpson_pdf: " +
+                  ", ".join(k for k in r if not np.array_equal(r[k].view(np.uint8), p[k].view(np.uint8))))
+    total = sum(wanted(n) for n in [c[0] for c in CASES] + [c[0] for c in BATCH_CASES + GLOBAL_CASES + TOL_CASES]
+                + ["pieces_cv_moments_simpson_pdf"])
     print(f"{total - bad} of {total} cases bit-identical")
     return 1 if bad else 0
 

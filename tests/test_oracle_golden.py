@@ -74,6 +74,11 @@ def test_oracle_matches_reference_golden(port, name):
         out = np.array([port.integrate_single(scenes.HALFSPACE, it["params"], it["rmin"], it["rmax"], it["method"],
                                               it["budget"], it["seed"], nested) for it in items], dtype=np.float32)
         assert np.array_equal(out.view(np.uint32), g["out_values"].view(np.uint32))
+    elif method == "pieces":
+        from golden.make_golden import run_pieces  # the fixture's own probe loop
+        out = run_pieces(port, g)
+        for k in ("moments", "pdf", "samples"):
+            assert np.array_equal(out[k].view(np.uint8), g["out_" + k].view(np.uint8)), k
     else:
         pytest.fail(method)
 
