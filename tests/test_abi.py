@@ -101,3 +101,25 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for fname, _ in cls._fields_:
             assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """Without the built CUDA library the Python package raises; nothing falls back to the CPU."""
+    from viltrum_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.load(str(tmp_path / "libviltrum_cuda.so"))
+
+
+def test_context_without_device_raises(lib_path):
+    """Creating a context where no CUDA device is visible is an error, not a silent CPU run; the
+    allocation-free entry point validates its arguments before touching a device."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is visible")
+    import viltrum_gb300 as v
+    from viltrum_gb300 import _lib
+    with pytest.raises(_lib.VcuError):
+        v.Context(0)
+    lib = ctypes.CDLL(lib_path)
+    assert lib.vcu_per_bin_adaptive_nested_static(None, None, ctypes.c_uint64(15), None, None) == 1
