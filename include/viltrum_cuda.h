@@ -113,6 +113,13 @@ int vcu_abi_version(void);
 int vcu_create(vcu_ctx** ctx, const vcu_opts* opts);
 int vcu_destroy(vcu_ctx* ctx);
 int vcu_last_error(const vcu_ctx* ctx, char* buf, size_t len);
+/* No reference counterpart (viltrum allocates with std::vector and has no budget).  A context grows
+ * its device buffers on demand and keeps them; with a limit set, a call whose buffers would take
+ * the context past `bytes` in total returns VCU_OOM (before freeing or allocating anything) and
+ * the context stays usable.  0 removes the limit.  vcu_device_memory_held() returns the bytes the
+ * context's buffers hold now. */
+int vcu_set_device_memory_limit(vcu_ctx* ctx, uint64_t bytes);
+uint64_t vcu_device_memory_held(const vcu_ctx* ctx);
 /* value channels of a built-in integrand (1 or 3), or a negative vcu_status */
 int vcu_channels(int32_t kind);
 
@@ -136,6 +143,15 @@ int vcu_per_bin_monte_carlo(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples
  * nbins x samples x dim floats), e.g. the points the reference drew for the same call. */
 int vcu_per_bin_monte_carlo_replay(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
                                    const float* points, float* bins, vcu_stats* stats);
+
+/* Replaces monte_carlo_per_bin_parallel(samples, seed)
+ * (src/monte-carlo/monte-carlo-per-bin-parallel.h:40-71) with its own arithmetic: bins ACCUMULATE,
+ * bins[b] += volume(range)/samples x sum f over the bin's samples (the factor of :45, the += of
+ * :69; the reference rounds to float after every sample, this adds the compensated sum once).
+ * bins is read and written (follows mem).  points (nullable, same layout as the replay call's)
+ * replaces the Philox draws, e.g. by the points the reference drew. */
+int vcu_per_bin_monte_carlo_accumulate(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
+                                       uint64_t seed, const float* points, float* bins, vcu_stats* stats);
 
 /* ------------------------------------------------------------------ per-bin adaptive nested NC
  * Replaces integrator_per_bin_parallel(integrator_adaptive_iterations(nested(H,L), heuristic,
@@ -326,8 +342,10 @@ int vcu_integrate_batch_resident(vcu_ctx* ctx, float* results, int32_t results_m
  *     p->mem == VCU_MEM_DEVICE: bins is the caller's device buffer (no size limit).
  *   - Runs on the current device and on `stream` (a cudaStream_t, NULL = legacy default stream),
  *     and returns after the results are written.  Returns VCU_NAN_DETECTED if a bin is NaN.
- *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress); make
- *     that first call before any stream capture.
+ *   - The array's device address is looked up (cudaGetSymbolAddress) with the device current;
+ *     the first call on a device does this set-up, so make it before any stream capture.  Calls
+ *     on a stream that is not capturing look the address up again, so a cudaDeviceReset in the
+ *     host process (which can move the array) is picked up by the next such call.
  *   - All calls share the array: calls that overlap on the GPU race and must be serialised.
  *   - No trace, no stats, no message: only the status code. */
 #define VCU_STATIC_MAX_BIN_VALUES (1u << 20)

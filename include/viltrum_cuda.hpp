@@ -236,8 +236,14 @@ public:
         const int ch = fi.channels();
         std::vector<float> out(detail::bin_count(res) * (std::size_t)ch);
         vcu_stats st{};
-        ctx.check(vcu_per_bin_monte_carlo(ctx.get(), &p, samples_, seed_, out.data(), &st));
-        detail::write_back(bins, res, out, ch, accumulate_);
+        if (accumulate_) {
+            /* monte_carlo_per_bin_parallel's own factor, added on the device to the current values */
+            detail::read_in(bins, res, out, ch);
+            ctx.check(vcu_per_bin_monte_carlo_accumulate(ctx.get(), &p, samples_, seed_, nullptr, out.data(), &st));
+        } else {
+            ctx.check(vcu_per_bin_monte_carlo(ctx.get(), &p, samples_, seed_, out.data(), &st));
+        }
+        detail::write_back(bins, res, out, ch, false);
         logger.log_progress(std::size_t(1), std::size_t(1));
     }
 };

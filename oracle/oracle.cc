@@ -1246,7 +1246,8 @@ extern "C" int orc_per_bin_adaptive_nested(int32_t kind, const float* params, in
 extern "C" int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* params, int32_t n_params, int32_t dim,
                                                    const float* rmin, const float* rmax, int32_t dimbins,
                                                    const uint64_t* res, const orc_nested* nested, uint64_t iterations,
-                                                   uint64_t bin_begin, uint64_t bin_end, int32_t nthreads, float* out) {
+                                                   uint64_t bin_begin, uint64_t bin_end, int32_t nthreads, float* out,
+                                                   int32_t* trace) {
     if (!valid_problem(dim, dimbins, res) || !nested || bin_end < bin_begin || nthreads < 1) return 1;
     Problem p{dim, dimbins, rmin, rmax, res};
     if (bin_end > p.nbins()) return 1;
@@ -1259,7 +1260,7 @@ extern "C" int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* pa
                     const uint64_t a = bin_begin + n * k / nthreads, b = bin_begin + n * (k + 1) / nthreads;
                     pool.emplace_back([&, a, b] {
                         per_bin_nested_range<decltype(h), decltype(l), decltype(D)::value, decltype(t)>(
-                            f, p, *nested, m, iterations, a, b, out, nullptr);
+                            f, p, *nested, m, iterations, a, b, out, trace);
                     });
                 }
                 for (auto& th : pool) th.join();

@@ -104,15 +104,16 @@ int orc_control_variates(int32_t kind, const float* params, int32_t n_params, in
                          uint64_t spp, uint64_t seed, const orc_cv* cv, float* out, float* approx_out,
                          float* regions_out, float* replay_out);
 
-/* Same per-bin Monte Carlo arithmetic over a contiguous slice of bins [bin_begin, bin_end),
- * on nthreads host threads (bins are independent once their seeds are drawn in bin order, as
- * integrator-per-bin-parallel.h:24 draws them).  Used to time the CPU path on all host cores. */
+/* Same per-bin adaptive nested arithmetic over a contiguous slice of bins [bin_begin, bin_end),
+ * on nthreads host threads (bins are independent: integrator-per-bin-parallel.h:28-34).  Used to
+ * time the CPU path on all host cores and to check full-size images; trace (optional, indexed by
+ * the absolute bin like orc_per_bin_adaptive_nested's) receives the split traces of the slice. */
 int orc_per_bin_adaptive_nested_threads(int32_t kind, const float* params, int32_t n_params,
                                         int32_t dim, const float* rmin, const float* rmax,
                                         int32_t dimbins, const uint64_t* res,
                                         const orc_nested* nested, uint64_t iterations,
                                         uint64_t bin_begin, uint64_t bin_end, int32_t nthreads,
-                                        float* out);
+                                        float* out, int32_t* trace);
 
 /* integrate(integrator_adaptive_iterations(nested(H,L), heuristic, iters), bins, f, range) with the
  * integrator used directly (not per bin): one max-error heap over the whole range, then every region,

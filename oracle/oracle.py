@@ -64,6 +64,25 @@ class Nested(ctypes.Structure):
         return cls(RULE[hi], RULE[lo], HEUR[heuristic], METRIC[metric], size_weight, min_size, min_val)
 
 
+def reference_sources() -> str | None:
+    """Directory of the viltrum sources (viltrum.h and src/) that the reference driver and the
+    header-compatibility test compile against: $VILTRUM_REFERENCE, else the checkout this oracle
+    was pinned against; None where neither holds the sources (e.g. the GPU hosts)."""
+    for cand in (os.environ.get("VILTRUM_REFERENCE"), "/root/reference"):
+        if cand and os.path.exists(os.path.join(cand, "viltrum.h")):
+            return cand
+    return None
+
+
+def build_reference() -> str | None:
+    """Build oracle/_ref/libvref.so (oracle/Makefile `ref`) where the reference sources exist."""
+    src = reference_sources()
+    if src is None:
+        return None
+    subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFERENCE={src}"])
+    return REF_SO
+
+
 def build(force: bool = False) -> str:
     """Compile liboracle.so from oracle.cc with the flags of oracle/Makefile."""
     src = os.path.join(HERE, "oracle.cc")
@@ -94,7 +113,7 @@ class Oracle:
             L.orc_per_bin_adaptive_nested_threads.restype = ctypes.c_int
             L.orc_per_bin_adaptive_nested_threads.argtypes = [
                 ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
-                ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, _f32p]
+                ctypes.POINTER(Nested), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, _f32p, _i32p]
         f = getattr(L, prefix + "per_bin_monte_carlo")
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int32, _f32p, ctypes.c_int32, ctypes.c_int32, _f32p, _f32p, ctypes.c_int32, _u64p,
@@ -180,16 +199,22 @@ class Oracle:
         return out.reshape(nb, ch), (tr.reshape(nb, iterations, 2) if trace else None)
 
     def per_bin_adaptive_nested_threads(self, kind, params, rmin, rmax, res, nested, iterations, bin_begin,
-                                        bin_end, nthreads):
+                                        bin_end, nthreads, trace=False):
+        """bins [bin_begin, bin_end) on `nthreads` host threads; with trace=True also the split trace
+        (dimension, popped error bits) of those bins, as per_bin_adaptive_nested returns it."""
         params, rmin, rmax, res = self._problem(params, rmin, rmax, res)
         nb = int(np.prod(res))
         ch = self.channels(kind)
         out = np.zeros(nb * ch, dtype=np.float32)
+        tr = np.zeros(nb * iterations * 2, dtype=np.int32) if trace else None
         rc = self.lib.orc_per_bin_adaptive_nested_threads(
             kind, _ptr(params), params.size, rmin.size, _ptr(rmin), _ptr(rmax), res.size, _ptr(res, _u64p),
-            ctypes.byref(nested), iterations, bin_begin, bin_end, nthreads, _ptr(out))
+            ctypes.byref(nested), iterations, bin_begin, bin_end, nthreads, _ptr(out), _ptr(tr, _i32p))
         self._check(rc, "per_bin_adaptive_nested_threads")
-        return out.reshape(nb, ch)[bin_begin:bin_end]
+        bins = out.reshape(nb, ch)[bin_begin:bin_end]
+        if not trace:
+            return bins
+        return bins, tr.reshape(nb, iterations, 2)[bin_begin:bin_end]
 
     def adaptive_global(self, kind, params, rmin, rmax, res, nested: Nested, iterations, initial=None):
         """integrator_adaptive_iterations used directly: one heap over the range, regions added into

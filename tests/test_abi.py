@@ -8,6 +8,7 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle import oracle as orc
 
 
 def _declared_symbols() -> set[str]:
@@ -45,6 +46,8 @@ def test_host_logic_without_device(lib_path):
     assert lib.vcu_per_bin_monte_carlo(None, None, 1, 1, None, None) == 1  # null context -> INVALID_ARG
     assert lib.vcu_integrate_batch(None, 7, None, None, 0, None, 0, None, None) == 1
     assert lib.vcu_integrate_batch_resident(None, None, 0, None, None) == 1
+    assert lib.vcu_per_bin_monte_carlo_accumulate(None, None, 1, 1, None, None, None) == 1
+    assert lib.vcu_set_device_memory_limit(None, ctypes.c_uint64(1)) == 1
     assert lib.vcu_destroy(None) == 0
 
 
@@ -58,15 +61,12 @@ def _compile_dropin(extra, out=None):
     return subprocess.run(cmd, capture_output=True, text=True)
 
 
-REFERENCE = "/root/reference"
-
-
-@pytest.mark.skipif(not os.path.exists(os.path.join(REFERENCE, "viltrum.h")), reason="reference sources absent")
+@pytest.mark.skipif(orc.reference_sources() is None, reason="reference sources absent")
 def test_cpp_dropin_compiles_against_reference():
     """The CUDA integrators of include/viltrum_cuda.hpp go through the reference's own
     viltrum::integrate(integrator, bins, f, range) (src/integrate.h:72-97) wherever a CPU per-bin
     integrator would: the example compiles against the unmodified reference headers."""
-    r = _compile_dropin(["-DWITH_VILTRUM", "-I", REFERENCE])
+    r = _compile_dropin(["-DWITH_VILTRUM", "-I", orc.reference_sources()])
     assert r.returncode == 0, r.stderr
 
 

@@ -2,8 +2,7 @@
 
 tests/cpp/dropin.cc is built with the host compiler against libviltrum_cuda.so and run; each of its
 outputs is recomputed here through the same library calls (Python binding) and must match bit for
-bit: the header adds only the bins(pos) write-back (assign, or accumulate for
-per_bin_monte_carlo_accumulate) in viltrum's dim-0-fastest order."""
+bit: the header adds only the bins(pos) read-in and write-back in viltrum's dim-0-fastest order."""
 import os
 import subprocess
 
@@ -36,8 +35,8 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
     b = np.empty(64, np.float32)
     p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [64])
     ctx.per_bin_monte_carlo(p, 256, 7, a)
-    ctx.per_bin_monte_carlo(p, 256, 9, b)
-    assert np.array_equal(row.view(np.uint32), (a + b).view(np.uint32))
+    ctx.per_bin_monte_carlo_accumulate(p, 256, 9, a)
+    assert np.array_equal(row.view(np.uint32), a.view(np.uint32))
     # crespo2021(255 splits, 16 samples, seed 3)
     c = np.empty(64, np.float32)
     ctx.control_variates(ctx.problem(scenes.SCENE2, scene, [0, 0], [1, 1], [64]),

@@ -94,9 +94,35 @@ def test_cv_statistics_against_fp64(ctx, port):
     assert 0.7 <= ratio <= 1.4, (gpu_sq, ref_sq)
 
 
+def test_cv_fullsize_matches_oracle(ctx, port):
+    """The control-variate workload at its full size -- integrator_crespo2021(2^14 - 1 splits, 64
+    residual samples) on the RGB moving-disk scene into 512x512 bins -- against the oracle: the same
+    2^14 regions in the same heap order (bit-equal ranges), the control-variate integral within 1e-5
+    relative in every bin and channel, and, replaying the oracle's own residual draws for every bin,
+    the oracle's bins within 1e-5 of the scale of the combined terms."""
+    params = scenes.moving_scene3(7)
+    res, iters, spp, seed = [512, 512], (1 << 14) - 1, 64, 3
+    ref = port.control_variates(scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res,
+                                orc.Nested.make("simpson", "trapezoidal", "size", "relative"), iters, spp, seed,
+                                regions=True, replay=True, approx=True)
+    out, app, reg, st = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, iters, spp, seed,
+                                replay=ref["replay"])
+    assert st.flags == 0
+    assert np.array_equal(reg.view(np.uint32), ref["regions"].view(np.uint32))
+    ra = ref["approximation"].astype(np.float64)
+    floor = 1e-3 * np.max(np.abs(ra))
+    aerr = np.abs(app - ra)
+    assert np.all(aerr <= 1e-5 * np.maximum(np.abs(ra), floor)), \
+        f"max rel approximation err {np.max(aerr / np.maximum(np.abs(ra), floor)):.3e}"
+    rb = ref["bins"].astype(np.float64)
+    scale = np.abs(rb) + np.abs(ra) + floor
+    err = np.abs(out - rb)
+    assert np.all(err <= 1e-5 * scale), f"max scaled err {np.max(err / scale):.3e}"
+
+
 def test_cv_fullsize_crespo(ctx):
-    """512x512 bins, 2^14 regions, 64 residual samples on the moving RGB scene: deterministic,
-    finite, and far more accurate than plain Monte Carlo at the same samples."""
+    """The same workload with the device's Philox draws: deterministic, finite, regions tiling the
+    domain, and far more accurate than plain Monte Carlo at the same samples."""
     params = scenes.moving_scene3(7)
     res = [512, 512]
     a, app, reg, st = _gpu_cv(ctx, scenes.MOVING_SCENE3, params, [0, 0, 0], [1, 1, 1], res, (1 << 14) - 1, 64, 3)

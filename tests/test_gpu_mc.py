@@ -39,21 +39,30 @@ def _bins_geometry(rmin, rmax, res, dim):
 @pytest.mark.parametrize("name", golden_names("mc_"))
 def test_replay_matches_reference(ctx, port, name):
     g = load_golden(name)
-    if "out_points" not in g or int(g["flavour"]) != 0:
-        pytest.skip("fixture without recorded points or accumulating flavour")
+    if "out_points" not in g:
+        pytest.skip("fixture without recorded points")
     kind, res, spp = int(g["kind"]), [int(r) for r in g["res"]], int(g["spp"])
     pts = np.ascontiguousarray(g["out_points"], np.float32)
     dim = pts.shape[2]
     p = ctx.problem(kind, g.get("params"), g["rmin"], g["rmax"], res)
     nb = int(np.prod(res))
     ch = 3 if kind == scenes.MOVING_SCENE3 else 1
-    out = np.empty(nb * ch, np.float32)
-    ctx.per_bin_monte_carlo_replay(p, spp, pts, out)
-    out = out.reshape(nb, ch).astype(np.float64)
     fvals = port.eval(kind, g.get("params"), pts.reshape(-1, dim)).reshape(nb, spp, ch).astype(np.float64)
-    lo, w = _bins_geometry(g["rmin"], g["rmax"], res, dim)
-    vol = np.prod(w.astype(np.float32), axis=1, dtype=np.float32).astype(np.float64)
-    factor = float(np.prod(res)) * vol / spp
+    if int(g["flavour"]) == 0:
+        # integrator_per_bin_parallel(monte_carlo): prod(res) * volume(bin) / spp * sum f, assigned
+        out = np.empty(nb * ch, np.float32)
+        ctx.per_bin_monte_carlo_replay(p, spp, pts, out)
+        lo, w = _bins_geometry(g["rmin"], g["rmax"], res, dim)
+        vol = np.prod(w.astype(np.float32), axis=1, dtype=np.float32).astype(np.float64)
+        factor = float(np.prod(res)) * vol / spp
+    else:
+        # monte_carlo_per_bin_parallel (monte-carlo-per-bin-parallel.h:45,69): bins (zero here, as
+        # in the fixture) += volume(range) / spp * f per sample
+        out = np.zeros(nb * ch, np.float32)
+        ctx.per_bin_monte_carlo_accumulate(p, spp, 0, out, points=pts)
+        width = np.asarray(g["rmax"], np.float32) - np.asarray(g["rmin"], np.float32)
+        factor = np.full(nb, float(np.prod(width, dtype=np.float32)) / spp)
+    out = out.reshape(nb, ch).astype(np.float64)
     exact = fvals.sum(axis=1) * factor[:, None]
     assert np.all(np.abs(out - exact) <= 1e-6 * np.abs(exact) + 1e-12)
     ref = g["out_bins"].astype(np.float64)
@@ -111,6 +120,25 @@ def test_philox_statistics_against_fp64(ctx, port):
         ref_sq.append(np.mean((ref[:, 0] - exact) ** 2))
     ratio = np.mean(gpu_sq) / np.mean(ref_sq)
     assert 0.8 <= ratio <= 1.25
+
+
+def test_accumulating_flavour_adds_to_current_values(ctx, port):
+    """monte_carlo_per_bin_parallel adds volume(range)/spp * sum f to whatever the bins hold: the
+    oracle's own points replayed onto a non-zero start equal start + the oracle's zero-start bins
+    (within the reference's float-accumulation bound)."""
+    res, spp = [6, 5], 32
+    start = np.linspace(-2.0, 3.0, 30, dtype=np.float32)
+    ref0, pts = port.per_bin_monte_carlo(scenes.WAVE2, None, [0, -1], [2, 1], res, spp, 4, flavour=1, record=True)
+    ref, _ = port.per_bin_monte_carlo(scenes.WAVE2, None, [0, -1], [2, 1], res, spp, 4, flavour=1,
+                                      initial=start)
+    p = ctx.problem(scenes.WAVE2, None, [0, -1], [2, 1], res)
+    out = start.copy()
+    ctx.per_bin_monte_carlo_accumulate(p, spp, 0, out, points=np.ascontiguousarray(pts))
+    fv = port.eval(scenes.WAVE2, None, pts.reshape(-1, 2))[:, 0].reshape(30, spp).astype(np.float64)
+    exact = start.astype(np.float64) + fv.sum(axis=1) * 4.0 / spp
+    assert np.all(np.abs(out - exact) <= 2 * U * np.abs(exact) + 1e-12)
+    bound = (spp + 1) * U * (np.abs(fv).sum(axis=1) * 4.0 / spp + np.abs(start))
+    assert np.all(np.abs(out - ref[:, 0]) <= bound)
 
 
 def test_accumulating_flavour_and_rgb(ctx, port):

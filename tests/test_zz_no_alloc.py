@@ -62,3 +62,60 @@ def test_static_entry_point_device_buffers_and_limit(ctx):
     big = np.empty(1025 * 1024, np.float32)
     assert fn(ctypes.byref(p_big), ctypes.byref(_lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37)), 15,
               big.ctypes.data, None) == 8
+
+
+def test_static_entry_point_status_codes_and_streams(ctx):
+    """Status codes of the allocation-free path: a NaN-producing integrand returns
+    VCU_NAN_DETECTED and the next clean call returns VCU_OK (the shared status word is cleared per
+    call); an unsupported rule pair, heuristic or metric returns VCU_INVALID_ARG, as the regular
+    entry point does; a caller's side stream gives the regular entry point's bits."""
+    torch = pytest.importorskip("torch")
+    fn = _static_fn()
+    st = _lib.Nested(3, 2, 0, 0, 1e-5, 1e-37, 1e-37)
+    params = scenes.halfspace(3, 2).copy()
+    params[1] = np.nan  # a_0 = NaN -> exp(NaN) inside the half-space
+    params[19] = 10.0   # the whole domain inside the half-space
+    p_nan = ctx.problem(scenes.HALFSPACE, params, [0, 0], [1, 1], [4, 4])
+    out = np.empty(16, np.float32)
+    assert fn(ctypes.byref(p_nan), ctypes.byref(st), 3, out.ctypes.data, None) == 5
+    p_ok = ctx.problem(scenes.SCENE2, scenes.scene2(4), [0, 0], [1, 1], [32, 8])
+    regular = np.empty(256, np.float32)
+    ctx.per_bin_adaptive_nested(p_ok, _lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37), 15, regular)
+    out = np.empty(256, np.float32)
+    assert fn(ctypes.byref(p_ok), ctypes.byref(_lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37)), 15,
+              out.ctypes.data, None) == 0
+    assert np.array_equal(out.view(np.uint32), regular.view(np.uint32))
+    for bad in (_lib.Nested(3, 5, 0, 0, 1e-5, 1e-37, 1e-37),   # low rule above the high rule
+                _lib.Nested(5, 3, 7, 0, 1e-5, 1e-37, 1e-37),   # unknown heuristic
+                _lib.Nested(5, 3, 0, 9, 1e-5, 1e-37, 1e-37)):  # unknown metric
+        assert fn(ctypes.byref(p_ok), ctypes.byref(bad), 15, out.ctypes.data, None) == 1
+        with pytest.raises(Exception):
+            ctx.per_bin_adaptive_nested(p_ok, bad, 15, np.empty(256, np.float32))
+    side = torch.cuda.Stream()
+    p_dev = ctx.problem(scenes.SCENE2, scenes.scene2(4), [0, 0], [1, 1], [32, 8], mem=_lib.MEM_DEVICE)
+    dev = torch.full((256,), float("nan"), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    assert fn(ctypes.byref(p_dev), ctypes.byref(_lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37)), 15, dev.data_ptr(),
+              ctypes.c_void_p(side.cuda_stream)) == 0
+    assert np.array_equal(dev.cpu().numpy().view(np.uint32), regular.view(np.uint32))
+
+
+def test_static_entry_point_allocates_nothing(ctx):
+    """After one warm-up call, calls of different sizes (host and device bins) leave the device's
+    free memory unchanged: the path makes no device allocation."""
+    torch = pytest.importorskip("torch")
+    fn = _static_fn()
+    nested = _lib.Nested(5, 3, 0, 0, 1e-5, 1e-37, 1e-37)
+    dev = torch.empty(128 * 128, dtype=torch.float32, device="cuda")
+    host = np.empty(200 * 100, np.float32)
+    p_small = ctx.problem(scenes.SCENE2, scenes.scene2(2), [0, 0], [1, 1], [16, 16])
+    assert fn(ctypes.byref(p_small), ctypes.byref(nested), 15, host.ctypes.data, None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for res, mem, buf in (([200, 100], _lib.MEM_HOST, host.ctypes.data), ([128, 128], _lib.MEM_DEVICE, dev.data_ptr()),
+                          ([7, 3], _lib.MEM_HOST, host.ctypes.data)):
+        p = ctx.problem(scenes.SCENE2, scenes.scene2(2), [0, 0], [1, 1], res, mem=mem)
+        assert fn(ctypes.byref(p), ctypes.byref(nested), 15, buf, None) == 0
+        torch.cuda.synchronize()
+        free, _ = torch.cuda.mem_get_info()
+        assert free == free0

@@ -508,7 +508,15 @@ def _run(integrator, bins, res, f, rng, logger, ctx, device_bins, accumulate):
             and bins.dtype == np.float32 and bins.size == nb * ch and bins.flags.c_contiguous)
     out = bins if (device_bins or flat) else np.empty(nb * ch, dtype=np.float32)
     inner = integrator.inner if isinstance(integrator, PerBinParallel) else integrator
-    if isinstance(inner, (MonteCarlo, MonteCarloPerBinParallel)):
+    if isinstance(inner, MonteCarloPerBinParallel):
+        # monte_carlo_per_bin_parallel's own factor, added on the device to the current values
+        if not device_bins:
+            arr = np.asarray(bins, dtype=np.float32).reshape(tuple(res) + ((ch,) if ch > 1 else ()))
+            axes = tuple(range(len(res) - 1, -1, -1)) + ((len(res),) if ch > 1 else ())
+            out[...] = np.ascontiguousarray(arr.transpose(axes)).ravel()
+        stats = ctx.per_bin_monte_carlo_accumulate(p, inner.samples, inner.seed, out)
+        accumulate = False
+    elif isinstance(inner, MonteCarlo):
         stats = ctx.per_bin_monte_carlo(p, inner.samples, inner.seed, out)
     elif isinstance(inner, AdaptiveIterations):
         stats = ctx.per_bin_adaptive_nested(p, _nested_struct(inner.rule, inner.heuristic), inner.iterations, out)

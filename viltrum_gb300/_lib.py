@@ -22,10 +22,11 @@ STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "QUEUE_OVERFLOW", 4: "DEVICE_T
 FLAG_NAN, FLAG_TIMEOUT, FLAG_OVERFLOW = 1, 2, 4
 
 EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vcu_channels", "vcu_eval",
-           "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_adaptive_nested",
+           "vcu_per_bin_monte_carlo", "vcu_per_bin_monte_carlo_replay", "vcu_per_bin_monte_carlo_accumulate",
+           "vcu_per_bin_adaptive_nested",
            "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
            "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global", "vcu_adaptive_tolerance",
-           "vcu_cv_replay_width"]
+           "vcu_cv_replay_width", "vcu_set_device_memory_limit", "vcu_device_memory_held"]
 BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
 CV_OPTIMIZE, CV_FIXED = 0, 1
 RR_UNIFORM, RR_INTEGRAL, RR_ERROR, RR_PDF = 0, 1, 2, 3  # residual region choice
@@ -128,11 +129,16 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         L.vcu_destroy.argtypes = [vp]
         L.vcu_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
         L.vcu_channels.argtypes = [ctypes.c_int32]
+        L.vcu_set_device_memory_limit.argtypes = [vp, ctypes.c_uint64]
+        L.vcu_device_memory_held.argtypes = [vp]
+        L.vcu_device_memory_held.restype = ctypes.c_uint64
         L.vcu_eval.argtypes = [vp, ctypes.POINTER(Integrand), ctypes.c_int32, vp, ctypes.c_int64, vp, ctypes.c_int32]
         L.vcu_per_bin_monte_carlo.argtypes = [vp, ctypes.POINTER(Problem), ctypes.c_uint64, ctypes.c_uint64, vp,
                                               ctypes.POINTER(Stats)]
         L.vcu_per_bin_monte_carlo_replay.argtypes = [vp, ctypes.POINTER(Problem), ctypes.c_uint64, vp, vp,
                                                      ctypes.POINTER(Stats)]
+        L.vcu_per_bin_monte_carlo_accumulate.argtypes = [vp, ctypes.POINTER(Problem), ctypes.c_uint64,
+                                                         ctypes.c_uint64, vp, vp, ctypes.POINTER(Stats)]
         L.vcu_per_bin_adaptive_nested.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested),
                                                   ctypes.c_uint64, vp, vp, ctypes.POINTER(Stats)]
         L.vcu_control_variates.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(Nested), ctypes.c_uint64,
@@ -238,6 +244,13 @@ class Context:
         self.check(self.lib.vcu_eval(self.handle, ctypes.byref(f), dim, _ptr(x), npts, _ptr(out), mem))
         return out
 
+    def set_device_memory_limit(self, nbytes: int) -> None:
+        """cap the bytes the context's device buffers may hold (0: no cap)"""
+        self.check(self.lib.vcu_set_device_memory_limit(self.handle, int(nbytes)))
+
+    def device_memory_held(self) -> int:
+        return int(self.lib.vcu_device_memory_held(self.handle))
+
     def per_bin_monte_carlo(self, p: Problem, spp: int, seed: int, bins) -> Stats:
         st = Stats()
         self.check(self.lib.vcu_per_bin_monte_carlo(self.handle, ctypes.byref(p), spp, seed, _ptr(bins),
@@ -248,6 +261,13 @@ class Context:
         st = Stats()
         self.check(self.lib.vcu_per_bin_monte_carlo_replay(self.handle, ctypes.byref(p), spp, _ptr(points),
                                                            _ptr(bins), ctypes.byref(st)))
+        return st
+
+    def per_bin_monte_carlo_accumulate(self, p: Problem, spp: int, seed: int, bins, points=None) -> Stats:
+        """monte_carlo_per_bin_parallel: bins (read and written) += volume(range)/spp * sum f."""
+        st = Stats()
+        self.check(self.lib.vcu_per_bin_monte_carlo_accumulate(self.handle, ctypes.byref(p), spp, seed, _ptr(points),
+                                                               _ptr(bins), ctypes.byref(st)))
         return st
 
     def per_bin_adaptive_nested(self, p: Problem, nested: Nested, iterations: int, bins, trace=None) -> Stats:

@@ -13,6 +13,11 @@
  * j+32 together, as two independent dependency chains, and add them in sample order).  The 32 lane sums are combined by warp shuffles in FP64,
  * scaled by prod(res)*volume(bin)/samples, staged in shared memory and written with coalesced
  * stores (float4 when a block's run of bins is 16-byte aligned).
+ *
+ * The accumulating flavour (ACCUM) is monte_carlo_per_bin_parallel's arithmetic
+ * (monte-carlo-per-bin-parallel.h:45,69): the sum is scaled by volume(range)/samples -- the whole
+ * range's float volume, not prod(res)*volume(bin) -- and ADDED to the bin's current value in FP64
+ * before the one rounding to float (the reference rounds after every sample).
  */
 #include "vcu_internal.cuh"
 
@@ -22,10 +27,11 @@ namespace {
 
 constexpr int MC_WARPS = 8;
 
-template <class F, int DIM, bool REPLAY>
+template <class F, int DIM, bool REPLAY, bool ACCUM>
 __global__ void __launch_bounds__(MC_WARPS * 32)
     k_per_bin_mc(const __grid_constant__ F f, const BinGrid g, uint64_t spp, uint32_t k0, uint32_t k1,
-                 const float* __restrict__ points, float* __restrict__ bins, uint32_t* __restrict__ status) {
+                 const float* __restrict__ points, float* __restrict__ bins, uint32_t* __restrict__ status,
+                 float range_volume) {
     constexpr int CH = F::CH;
     __shared__ float stage[MC_WARPS * CH];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -107,7 +113,11 @@ __global__ void __launch_bounds__(MC_WARPS * 32)
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
         if (lane == 0) {
-            const double est = (double)g.factor * (double)vol / (double)spp * t;
+            double est;
+            if constexpr (ACCUM)
+                est = (bin < g.nbins ? (double)bins[bin * CH + c] : 0.0) + (double)range_volume / (double)spp * t;
+            else
+                est = (double)g.factor * (double)vol / (double)spp * t;
             const float e = (float)est;
             if (bin < g.nbins && isnan(e)) atomicOr(status, VCU_FLAG_NAN);
             stage[warp * CH + c] = e;
@@ -159,18 +169,28 @@ template <class F, class Body> int by_arity(vcu_ctx* ctx, int dim, Body&& body) 
 }  // namespace
 
 int run_mc(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, uint64_t spp, uint64_t seed, const float* points,
-           float* d_bins, uint32_t& launches) {
+           float* d_bins, bool accumulate, uint32_t& launches) {
+    /* Range::volume() (range.h:24-25): the float product of the widths */
+    float range_volume = 1.0f;
+    for (int d = 0; d < p->dim; ++d) range_volume *= (p->range_max[d] - p->range_min[d]);
     return with_integrand(ctx, p->f, p->dim, [&](const auto& f) -> int {
         using F = std::decay_t<decltype(f)>;
         return by_arity<F>(ctx, p->dim, [&](auto dimc) -> int {
             constexpr int DIM = decltype(dimc)::value;
             const unsigned blocks = (unsigned)((g.nbins + MC_WARPS - 1) / MC_WARPS);
-            if (points)
-                k_per_bin_mc<F, DIM, true><<<blocks, MC_WARPS * 32, 0, ctx->stream>>>(
-                    f, g, spp, (uint32_t)seed, (uint32_t)(seed >> 32), points, d_bins, ctx->d_status);
+            const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+            if (points && accumulate)
+                k_per_bin_mc<F, DIM, true, true><<<blocks, MC_WARPS * 32, 0, ctx->stream>>>(
+                    f, g, spp, k0, k1, points, d_bins, ctx->d_status, range_volume);
+            else if (points)
+                k_per_bin_mc<F, DIM, true, false><<<blocks, MC_WARPS * 32, 0, ctx->stream>>>(
+                    f, g, spp, k0, k1, points, d_bins, ctx->d_status, range_volume);
+            else if (accumulate)
+                k_per_bin_mc<F, DIM, false, true><<<blocks, MC_WARPS * 32, 0, ctx->stream>>>(
+                    f, g, spp, k0, k1, nullptr, d_bins, ctx->d_status, range_volume);
             else
-                k_per_bin_mc<F, DIM, false><<<blocks, MC_WARPS * 32, 0, ctx->stream>>>(
-                    f, g, spp, (uint32_t)seed, (uint32_t)(seed >> 32), nullptr, d_bins, ctx->d_status);
+                k_per_bin_mc<F, DIM, false, false><<<blocks, MC_WARPS * 32, 0, ctx->stream>>>(
+                    f, g, spp, k0, k1, nullptr, d_bins, ctx->d_status, range_volume);
             ++launches;
             VCU_CUDA(ctx, cudaGetLastError());
             return VCU_OK;

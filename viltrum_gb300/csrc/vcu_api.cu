@@ -43,6 +43,20 @@ int make_grid(vcu_ctx* ctx, const vcu_problem* p, BinGrid& g) {
     return VCU_OK;
 }
 
+int check_per_bin_nested(vcu_ctx* ctx, const vcu_nested& n) {
+    if (n.heuristic != VCU_HEUR_DEFAULT && n.heuristic != VCU_HEUR_SIZE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
+    if (n.metric != VCU_METRIC_ABSOLUTE && n.metric != VCU_METRIC_RELATIVE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    const bool pair = (n.rule_hi == VCU_RULE_BOOLE && n.rule_lo == VCU_RULE_SIMPSON) ||
+                      (n.rule_hi == VCU_RULE_BOOLE && n.rule_lo == VCU_RULE_TRAPEZOIDAL) ||
+                      (n.rule_hi == VCU_RULE_SIMPSON && n.rule_lo == VCU_RULE_TRAPEZOIDAL);
+    if (!pair)
+        return fail(ctx, VCU_INVALID_ARG,
+                    "unsupported nested rule pair (boole/simpson, boole/trapezoidal, simpson/trapezoidal)");
+    return VCU_OK;
+}
+
 int CallScope::begin() {
     if (stats) std::memset(stats, 0, sizeof(*stats));
     VCU_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -267,6 +281,14 @@ extern "C" int vcu_destroy(vcu_ctx* ctx) {
     return VCU_OK;
 }
 
+extern "C" int vcu_set_device_memory_limit(vcu_ctx* ctx, uint64_t bytes) {
+    if (!ctx) return VCU_INVALID_ARG;
+    ctx->mem_limit = bytes;
+    return VCU_OK;
+}
+
+extern "C" uint64_t vcu_device_memory_held(const vcu_ctx* ctx) { return ctx ? (uint64_t)ctx->held : 0; }
+
 extern "C" int vcu_last_error(const vcu_ctx* ctx, char* buf, size_t len) {
     if (!ctx || !buf || len == 0) return VCU_INVALID_ARG;
     std::snprintf(buf, len, "%s", ctx->last_error.c_str());
@@ -310,7 +332,7 @@ extern "C" int vcu_eval(vcu_ctx* ctx, const vcu_integrand* f, int32_t dim, const
 }
 
 static int per_bin_mc(vcu_ctx* ctx, const vcu_problem* p, uint64_t spp, uint64_t seed, const float* points, float* bins,
-                      vcu_stats* stats) {
+                      bool accumulate, vcu_stats* stats) {
     if (!ctx) return VCU_INVALID_ARG;
     BinGrid g;
     int rc = make_grid(ctx, p, g);
@@ -323,6 +345,8 @@ static int per_bin_mc(vcu_ctx* ctx, const vcu_problem* p, uint64_t spp, uint64_t
     if ((rc = scope.begin())) return rc;
     float* dbins = nullptr;
     if ((rc = out_buffer(ctx, p, bins, g.nbins * ch * 4, &dbins))) return rc;
+    if (accumulate && p->mem == VCU_MEM_HOST)
+        VCU_CUDA(ctx, cudaMemcpyAsync(dbins, bins, g.nbins * ch * 4, cudaMemcpyHostToDevice, ctx->stream));
     const float* dpts = points;
     if (points && p->mem == VCU_MEM_HOST) {
         const size_t bytes = g.nbins * spp * p->dim * 4;
@@ -330,7 +354,7 @@ static int per_bin_mc(vcu_ctx* ctx, const vcu_problem* p, uint64_t spp, uint64_t
         VCU_CUDA(ctx, cudaMemcpyAsync(ctx->in.ptr, points, bytes, cudaMemcpyHostToDevice, ctx->stream));
         dpts = static_cast<const float*>(ctx->in.ptr);
     }
-    if ((rc = run_mc(ctx, p, g, spp, seed, dpts, dbins, scope.launches))) return rc;
+    if ((rc = run_mc(ctx, p, g, spp, seed, dpts, dbins, accumulate, scope.launches))) return rc;
     if (p->mem == VCU_MEM_HOST)
         VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, g.nbins * ch * 4, cudaMemcpyDeviceToHost, ctx->stream));
     return scope.end(g.nbins * spp, 0);
@@ -338,13 +362,18 @@ static int per_bin_mc(vcu_ctx* ctx, const vcu_problem* p, uint64_t spp, uint64_t
 
 extern "C" int vcu_per_bin_monte_carlo(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin, uint64_t seed,
                                        float* bins, vcu_stats* stats) {
-    return per_bin_mc(ctx, p, samples_per_bin, seed, nullptr, bins, stats);
+    return per_bin_mc(ctx, p, samples_per_bin, seed, nullptr, bins, false, stats);
 }
 
 extern "C" int vcu_per_bin_monte_carlo_replay(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
                                               const float* points, float* bins, vcu_stats* stats) {
     if (ctx && !points) return fail(ctx, VCU_INVALID_ARG, "null points");
-    return per_bin_mc(ctx, p, samples_per_bin, 0, points, bins, stats);
+    return per_bin_mc(ctx, p, samples_per_bin, 0, points, bins, false, stats);
+}
+
+extern "C" int vcu_per_bin_monte_carlo_accumulate(vcu_ctx* ctx, const vcu_problem* p, uint64_t samples_per_bin,
+                                                  uint64_t seed, const float* points, float* bins, vcu_stats* stats) {
+    return per_bin_mc(ctx, p, samples_per_bin, seed, points, bins, true, stats);
 }
 
 extern "C" int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* nested,
@@ -355,10 +384,7 @@ extern "C" int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, c
     if (rc) return rc;
     if (!nested || !bins) return fail(ctx, VCU_INVALID_ARG, "null nested rule or bins");
     if (iterations > 62) return fail(ctx, VCU_UNSUPPORTED, "per-bin region budget is limited to 62 splits (63 regions)");
-    if (nested->heuristic != VCU_HEUR_DEFAULT && nested->heuristic != VCU_HEUR_SIZE)
-        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
-    if (nested->metric != VCU_METRIC_ABSOLUTE && nested->metric != VCU_METRIC_RELATIVE)
-        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    if ((rc = check_per_bin_nested(ctx, *nested))) return rc;
     const int ch = vcu_channels(p->f.kind);
     if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
     CallScope scope{ctx, stats};
@@ -377,8 +403,6 @@ extern "C" int vcu_per_bin_adaptive_nested(vcu_ctx* ctx, const vcu_problem* p, c
         rc = run_nested_bt(ctx, p, g, *nested, (int)iterations, dbins, dtrace, scope.launches);
     else if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
         rc = run_nested_st(ctx, p, g, *nested, (int)iterations, dbins, dtrace, scope.launches);
-    else
-        rc = fail(ctx, VCU_INVALID_ARG, "unsupported nested rule pair (boole/simpson, boole/trapezoidal, simpson/trapezoidal)");
     if (rc) return rc;
     if (p->mem == VCU_MEM_HOST) {
         VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, g.nbins * ch * 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -82,6 +82,8 @@ struct vcu_ctx {
     vcu_buffer out, aux, in, scratch;
     vcu_buffer batch_in, batch_pool; /* owned by the batched-integral path only */
     vcu_batch_state batch;
+    size_t held = 0;              /* bytes held by the grow-only buffers                 */
+    uint64_t mem_limit = 0;       /* vcu_set_device_memory_limit (0: none)               */
     std::string last_error;
 };
 
@@ -100,18 +102,26 @@ inline int cuda_fail(vcu_ctx* ctx, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return vcu::cuda_fail(ctx, e_, #call); \
     } while (0)
 
-/* grow-only device buffer owned by the context */
+/* grow-only device buffer owned by the context; a growth that would take the context's buffers
+ * past its memory limit fails with VCU_OOM before anything is freed or allocated */
 inline int ensure(vcu_ctx* ctx, vcu_buffer& b, size_t bytes) {
     if (b.bytes >= bytes) return VCU_OK;
+    if (ctx && ctx->mem_limit && ctx->held - b.bytes + bytes > ctx->mem_limit)
+        return fail(ctx, VCU_OOM, std::string("device allocation of ") + std::to_string(bytes) +
+                                      " bytes would exceed the context's memory limit of " +
+                                      std::to_string(ctx->mem_limit) + " bytes");
     if (b.ptr) cudaFree(b.ptr);
+    if (ctx) ctx->held -= b.bytes;
     b.ptr = nullptr;
     b.bytes = 0;
     cudaError_t e = cudaMalloc(&b.ptr, bytes < 256 ? 256 : bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
+        b.ptr = nullptr;
         return fail(ctx, VCU_OOM, std::string("device allocation of ") + std::to_string(bytes) + " bytes failed");
     }
     b.bytes = bytes;
+    if (ctx) ctx->held += bytes;
     return VCU_OK;
 }
 
@@ -126,6 +136,9 @@ struct BinGrid {
 };
 
 int make_grid(vcu_ctx* ctx, const vcu_problem* p, BinGrid& g);
+/* VCU_INVALID_ARG unless heuristic, metric and rule pair are ones the per-bin nested kernels
+ * instantiate (boole/simpson, boole/trapezoidal, simpson/trapezoidal) */
+int check_per_bin_nested(vcu_ctx* ctx, const vcu_nested& n);
 
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the multiply-xor bijection
  * with the published multipliers and Weyl key increments. */
@@ -258,7 +271,7 @@ struct CallScope {
 /* entry points implemented by the method translation units */
 namespace vcu {
 int run_mc(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, uint64_t spp, uint64_t seed, const float* points,
-           float* d_bins, uint32_t& launches);
+           float* d_bins, bool accumulate, uint32_t& launches);
 int run_nested_bs(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,
                   float* d_bins, int32_t* d_trace, uint32_t& launches);
 int run_nested_bt(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_nested& n, int iterations,

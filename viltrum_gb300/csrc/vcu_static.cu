@@ -11,11 +11,17 @@
  * the process exits.
  *
  * The array's name is only a host-side stand-in in host code; the kernel receives its device
- * address, taken with cudaGetSymbolAddress once per device the first time the entry point runs with
- * that device current (so make that first call before any stream capture).  All calls share the
- * array and it keeps the last call's contents: the status word is cleared at the start of every
- * call, and calls that overlap on the GPU (on different streams, or from different host threads)
- * race on it -- serialise them.
+ * address, taken with cudaGetSymbolAddress with the caller's device current.  The first call on a
+ * device does this set-up, so it should come before any stream capture.  Every call on a stream
+ * that is not capturing looks the address up again (a cudaDeviceReset in the host process reloads
+ * the module and can move the array); the per-device cache serves only calls on a capturing
+ * stream.  All calls share the array and it keeps the last call's contents: the status word is
+ * cleared at the start of every call, and calls that overlap on the GPU (on different streams, or
+ * from different host threads) race on it -- serialise them.
+ *
+ * Nothing is allocated on the device, on any path.  On success nothing is allocated on the host
+ * either; a call that fails inside the launch code shared with the regular entry point formats its
+ * message into a host string that is then discarded (this entry point returns only the code).
  */
 #include <mutex>
 
@@ -31,17 +37,26 @@ static __device__ __align__(256) float g_static_scratch[64 + VCU_STATIC_MAX_BIN_
 std::mutex g_static_mutex;
 float* g_static_ptr[VCU_STATIC_MAX_DEVICES] = {};
 
-/* device address of g_static_scratch on the current device (taken once per device) */
-int static_scratch(int device, float** out) {
+/* device address of g_static_scratch on the current device: looked up on every uncaptured call
+ * (the module, and the array with it, moves after a cudaDeviceReset), the cached value during a
+ * stream capture */
+int static_scratch(int device, cudaStream_t stream, float** out) {
     if (device < 0 || device >= VCU_STATIC_MAX_DEVICES) return VCU_UNSUPPORTED;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return VCU_CUDA_ERROR;
+    }
     std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_ptr[device]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) {
             cudaGetLastError();
             return VCU_CUDA_ERROR;
         }
         g_static_ptr[device] = static_cast<float*>(p);
+    } else if (!g_static_ptr[device]) {
+        return VCU_UNSUPPORTED; /* first call on this device inside a capture */
     }
     *out = g_static_ptr[device];
     return VCU_OK;
@@ -56,6 +71,7 @@ extern "C" int vcu_per_bin_adaptive_nested_static(const vcu_problem* p, const vc
     const int ch = vcu_channels(p->f.kind);
     if (ch < 0) return VCU_INVALID_ARG;
     if (iterations > 62) return VCU_UNSUPPORTED;
+    if (check_per_bin_nested(nullptr, *nested)) return VCU_INVALID_ARG;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) {
         cudaGetLastError();
@@ -78,7 +94,7 @@ extern "C" int vcu_per_bin_adaptive_nested_static(const vcu_problem* p, const vc
     if (rc) return rc;
     if (g.nbins * (uint64_t)ch > VCU_STATIC_MAX_BIN_VALUES) return VCU_UNSUPPORTED;
     float* scratch = nullptr;
-    if ((rc = static_scratch(device, &scratch))) return rc;
+    if ((rc = static_scratch(device, ctx.stream, &scratch))) return rc;
     ctx.d_status = reinterpret_cast<uint32_t*>(scratch);
     if (cudaMemsetAsync(ctx.d_status, 0, sizeof(uint32_t), ctx.stream) != cudaSuccess) return VCU_CUDA_ERROR;
     float* dbins = (p->mem == VCU_MEM_DEVICE) ? bins : scratch + 64;
@@ -87,10 +103,8 @@ extern "C" int vcu_per_bin_adaptive_nested_static(const vcu_problem* p, const vc
         rc = run_nested_bs(&ctx, p, g, *nested, (int)iterations, dbins, nullptr, launches);
     else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
         rc = run_nested_bt(&ctx, p, g, *nested, (int)iterations, dbins, nullptr, launches);
-    else if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
-        rc = run_nested_st(&ctx, p, g, *nested, (int)iterations, dbins, nullptr, launches);
     else
-        rc = VCU_INVALID_ARG;
+        rc = run_nested_st(&ctx, p, g, *nested, (int)iterations, dbins, nullptr, launches);
     if (rc) return rc;
     if (p->mem == VCU_MEM_HOST &&
         cudaMemcpyAsync(bins, dbins, g.nbins * ch * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess)
