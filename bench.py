@@ -488,74 +488,146 @@ def adaptive_forms(ctx, port) -> dict:
     return out
 
 
-def time_to_rmse(ctx, target: float = 1e-3) -> dict:
-    """Wall time (device, one call) each estimator needs to reach bin RMSE <= target against the
-    truth: plain Monte Carlo, the polynomial control variate (crespo2021, 2^14 regions) and the learned
-    control variate (1000 training steps), each with the sample count doubled until it gets there (or
-    a cap).  Two integrands: the 5-D occluded scene (2 bin dims + 3 primary dims; truth = 16 x 65536
-    Monte Carlo samples per bin, whose own squared standard error is subtracted) at 64x64 bins, and
-    sin(8x)e^-y + x^2 + y^2 at 8x8 bins (closed-form truth)."""
+def time_to_rmse(ctx, target: float = 1e-3, res_side: int = 1024, seeds=(1, 2, 3)) -> dict:
+    """Time each estimator needs to reach bin RMSE <= target against the truth on the 5-D occluded
+    scene (2 bin dims + 3 primary dims) at res_side^2 bins: plain Monte Carlo, the polynomial control
+    variate (crespo2021, 2^14 regions) and the learned control variate (early-stopped training, the
+    network's interpolant on 6 Simpson cells per primary dimension, per-bin pilot choice against
+    plain Monte Carlo).  Per estimator and seed the samples per bin double until the target is met,
+    starting from the power of two below the count a 256-sample run predicts; the time is the device
+    time of the one call that met it (training and region construction included) and `spp_below`
+    the largest count tried that did not.  The RMSE is taken over four 32x32 windows of the image
+    (4096 bins), whose truth is plain Monte Carlo with 2^21 samples per bin (its squared standard
+    error is subtracted).  A smaller closed-form case (sin(8x)e^-y + x^2 + y^2 at 8x8 bins) follows."""
     from viltrum_gb300 import _lib, scenes
 
-    res = {}
-    cases = [("occluded_scene5_64x64", scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), 5, [64, 64]),
-             ("wave2_8x8", scenes.WAVE2, None, 2, [8, 8])]
-    for name, kind, params, dim, bres in cases:
-        nb = bres[0] * bres[1]
-        p = ctx.problem(kind, params, [0] * dim, [1] * dim, bres)
-        if kind == scenes.WAVE2:
-            truth = scenes.exact_bins(kind, None, [0, 0], [1, 1], bres)[:, 0]
-            se2 = 0.0
-        else:
-            acc = np.zeros(nb)
-            acc2 = np.zeros(nb)
-            for k in range(16):
-                b = np.empty(nb, np.float32)
-                ctx.per_bin_monte_carlo(p, 1 << 16, 1000 + k, b)
-                acc += b
-                acc2 += b.astype(np.float64) ** 2
-            truth = acc / 16
-            se2 = float(np.mean(np.maximum(acc2 / 16 - truth ** 2, 0.0) / 15))
+    out = {}
+    params = scenes.occluded_scene5(SEED)
+    R = res_side
+    p = ctx.problem(scenes.OCCLUDED_SCENE5, params, [0] * 5, [1] * 5, [R, R])
+    nb = R * R
+    W = 32
+    corners = [(R // 8, R // 8), (R // 2, R // 4), (R // 4, 5 * R // 8), (3 * R // 4, 3 * R // 4)]
+    idx, truth, se2 = [], [], []
+    t0 = time.perf_counter()
+    for cx, cy in corners:
+        sub = ctx.problem(scenes.OCCLUDED_SCENE5, params, [cx / R, cy / R, 0, 0, 0],
+                          [(cx + W) / R, (cy + W) / R, 1, 1, 1], [W, W])
+        reps = []
+        for k in range(2):
+            b = np.empty(W * W, np.float32)
+            ctx.per_bin_monte_carlo(sub, 1 << 20, 9000 + k, b)
+            reps.append(b.astype(np.float64))
+        reps = np.array(reps)
+        truth.append(reps.mean(axis=0))
+        se2.append(reps.var(axis=0, ddof=1) / 2)
+        jj, ii = np.meshgrid(np.arange(W), np.arange(W), indexing="ij")
+        idx.append(((cy + jj) * R + (cx + ii)).ravel())
+    idx = np.concatenate(idx)
+    truth = np.concatenate(truth)
+    se2 = float(np.mean(np.concatenate(se2)))
+    truth_s = time.perf_counter() - t0
 
-        def rmse(b):
-            return float(np.sqrt(max(np.mean((b.astype(np.float64) - truth) ** 2) - se2, 0.0)))
+    def rmse(b):
+        return float(np.sqrt(max(np.mean((b[idx].astype(np.float64) - truth) ** 2) - se2, 0.0)))
 
-        def sweep(run, start, cap):
-            spp, best = start, None
-            while spp <= cap:
-                b, ms = run(spp)
-                e = rmse(b)
-                best = (spp, e, ms)
-                if e <= target:
-                    return {"reached": True, "spp": spp, "rmse": e, "ms": round(ms, 3)}
+    buf = np.empty(nb, np.float32)
+
+    def mc(spp, seed):
+        st = ctx.per_bin_monte_carlo(p, spp, seed, buf)
+        return st.device_ms, {}
+
+    nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+
+    def cv(spp, seed):
+        st = ctx.control_variates(p, nst, (1 << 14) - 1, _lib.CvOpts(spp, seed, 0, 0, 1.0), buf)
+        return st.device_ms, {}
+
+    def lcv(spp, seed):
+        st, rep = ctx.learned_control_variates(
+            p, _lib.LearnedOpts(spp, seed, 4000, 32768, 3e-3, 100, 1, 0, None, 6), buf)
+        return st.device_ms, {"train_steps": rep.train_steps_run, "train_ms": round(rep.train_ms, 2),
+                              "grid_ms": round(rep.integral_ms, 2), "residual_ms": round(rep.residual_ms, 2),
+                              "plain_mc_bins": rep.fallback_bins, "nodes_per_bin": rep.nodes_per_bin}
+
+    def sweep(run, seed, cap):
+        """smallest power-of-two samples per bin that reaches the target: start at the power of two
+        below the count a 256-sample run predicts, halve while that still reaches, else double"""
+        run(256, seed)
+        need = 256 * (rmse(buf) / target) ** 2
+        spp = 256
+        while spp * 2 <= min(need, cap):
+            spp *= 2
+        tried = {}
+        while 256 <= spp <= cap:
+            ms, extra = run(spp, seed)
+            e = rmse(buf)
+            tried[spp] = (e <= target, e, ms, extra)
+            if e <= target:
+                if spp // 2 in tried or spp == 256:
+                    break
+                spp //= 2
+            else:
+                if spp * 2 in tried:
+                    spp *= 2
+                    break
                 spp *= 2
-            return {"reached": False, "spp": best[0], "rmse": best[1], "ms": round(best[2], 3)}
+        ok = [k for k, v in tried.items() if v[0]]
+        if not ok:
+            k = max(tried)
+            return {"reached": False, "spp": k, "rmse": tried[k][1], "ms": round(tried[k][2], 2)}
+        k = min(ok)
+        below = [q for q, v in tried.items() if not v[0] and q < k]
+        return {"reached": True, "spp": k, "spp_below": max(below) if below else None, "rmse": tried[k][1],
+                "ms": round(tried[k][2], 2), **tried[k][3]}
 
-        def mc(spp):
-            b = np.empty(nb, np.float32)
-            st = ctx.per_bin_monte_carlo(p, spp, 5, b)
-            return b, st.device_ms
+    case = {"bins": [R, R], "rmse_bins": int(idx.size), "truth_spp": 2 << 20, "truth_s": round(truth_s, 1)}
+    for name, run, cap in (("plain_mc", mc, 1 << 18), ("polynomial_cv", cv, 1 << 16), ("learned_cv", lcv, 1 << 17)):
+        per = [sweep(run, seed, cap) for seed in seeds]
+        reached = all(r["reached"] for r in per)
+        case[name] = {"reached": reached, "mean_ms": round(float(np.mean([r["ms"] for r in per])), 2)
+                      if reached else None, "seeds": per}
+    m, l, c = case["plain_mc"], case["learned_cv"], case["polynomial_cv"]
+    case["learned_over_plain_ms"] = round(l["mean_ms"] / m["mean_ms"], 3) if (m["reached"] and l["reached"]) else None
+    case["learned_over_polynomial_ms"] = round(l["mean_ms"] / c["mean_ms"], 3) if (c["reached"] and l["reached"]) \
+        else None
+    out[f"occluded_scene5_{R}x{R}"] = case
 
-        def cv(spp):
-            b = np.empty(nb, np.float32)
-            st = ctx.control_variates(p, _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37), (1 << 14) - 1,
-                                      _lib.CvOpts(spp, 5, 0, 0, 1.0), b)
-            return b, st.device_ms
+    # the smooth 2-D case, closed-form truth, 8x8 bins
+    p2 = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [8, 8])
+    exact = scenes.exact_bins(scenes.WAVE2, None, [0, 0], [1, 1], [8, 8])[:, 0]
+    b2 = np.empty(64, np.float32)
 
-        def lcv(spp):
-            b = np.empty(nb, np.float32)
-            q, cells = (3, 2) if dim == 5 else (4, 4)
-            st, rep = ctx.learned_control_variates(p, _lib.LearnedOpts(spp, 5, 1000, 32768, 3e-3, q, 1, cells), b)
-            return b, st.device_ms
+    def run2(kind, spp, seed):
+        if kind == "plain_mc":
+            return ctx.per_bin_monte_carlo(p2, spp, seed, b2).device_ms
+        if kind == "polynomial_cv":
+            return ctx.control_variates(p2, nst, (1 << 14) - 1, _lib.CvOpts(spp, seed, 0, 0, 1.0), b2).device_ms
+        return ctx.learned_control_variates(p2, _lib.LearnedOpts(spp, seed, 4000, 32768, 3e-3, 100, 1, 4, None, 1),
+                                            b2)[0].device_ms
 
-        cap = 1 << 17
-        res[name] = {"plain_mc": sweep(mc, 64, cap), "polynomial_cv": sweep(cv, 64, 1 << 12),
-                     "learned_cv": sweep(lcv, 64, 1 << 14)}
-        m, l = res[name]["plain_mc"], res[name]["learned_cv"]
-        res[name]["learned_over_plain_ms"] = round(l["ms"] / m["ms"], 3) if (m["reached"] and l["reached"]) else None
-    res["target_rmse"] = target
-    res["timing"] = "device time of the one call that reached the target (training and region construction included)"
-    return res
+    small = {}
+    for kind in ("plain_mc", "polynomial_cv", "learned_cv"):
+        per = []
+        for seed in seeds:
+            spp, res_ = 16, None
+            while spp <= 1 << 20:
+                ms = run2(kind, spp, seed)
+                e = float(np.sqrt(np.mean((b2.astype(np.float64) - exact) ** 2)))
+                if e <= target:
+                    res_ = {"reached": True, "spp": spp, "rmse": e, "ms": round(ms, 3)}
+                    break
+                spp *= 2
+            per.append(res_ or {"reached": False})
+        ok = all(r["reached"] for r in per)
+        small[kind] = {"reached": ok, "mean_ms": round(float(np.mean([r["ms"] for r in per])), 3) if ok else None,
+                       "seeds": per}
+    out["wave2_8x8"] = small
+    out["target_rmse"] = target
+    out["seeds"] = list(seeds)
+    out["timing"] = "device time of the one call that reached the target (training and region construction " \
+                    "included), mean over the seeds"
+    return out
 
 
 def _traffic_from_profile(nbins: int):
@@ -667,7 +739,12 @@ def profile_workload(args) -> dict:
     elif w == "learned":
         p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [r, r])
         b = np.empty(r * r, np.float32)
-        call = lambda: ctx.learned_control_variates(p, _lib.LearnedOpts(32, 5, 20, 32768, 3e-3, 3, 1, 1), b)[0]
+        if args.res > 256:  # the 5-D occluded scene: the configuration the time-to-RMSE sweep runs
+            p = ctx.problem(scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), [0] * 5, [1] * 5, [r, r])
+            opts = _lib.LearnedOpts(64, 5, 200, 32768, 3e-3, 0, 1, 0, None, 6)
+        else:
+            opts = _lib.LearnedOpts(32, 5, 20, 32768, 3e-3, 0, 1, 2, None, 1)
+        call = lambda: ctx.learned_control_variates(p, opts, b)[0]
     else:  # nested
         p = ctx.problem(scenes.SCENE2, scenes.scene2(SEED), [0, 0], [1, 1], [r, r])
         b = np.empty(r * r, np.float32)

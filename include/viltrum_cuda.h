@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define VCU_ABI_VERSION 1
+#define VCU_ABI_VERSION 2
 #define VCU_MAX_DIM 6     /* viltrum's VILTRUM_MAX_DIMENSIONS_REGION (src/newton-cotes/region.h:16-18) */
 #define VCU_MAX_DIMBINS 4
 
@@ -205,6 +205,9 @@ typedef struct vcu_cv {
     double mis_cutoff;
     int32_t fubini_dims;      /* 0, or 2: regions over the first 2 dimensions only     */
     uint32_t tail_samples;    /* fubini_dims 2: Monte Carlo samples per evaluation     */
+    float* variance;          /* nullable (follows mem): per bin, the estimated variance of the
+                                 bin's estimate, Var(norm f - alpha norm g) / samples from the
+                                 residual's sample moments (infinite below 2 samples)  */
 } vcu_cv;
 
 /* floats per residual sample in vcu_control_variates' replay records: the chosen list index and
@@ -218,39 +221,50 @@ int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* n
 
 /* ------------------------------------------------------------------ learned control variate
  * No reference counterpart: per-bin integration (the integrator_per_bin_parallel contract,
- * src/integrator-per-bin-parallel.h:17-35, values ASSIGNED) with a small MLP control variate g --
+ * src/integrator-per-bin-parallel.h:17-35, values ASSIGNED) with a small MLP control variate --
  * frequency encoding (6 bands), 4 hidden layers of 64, BF16 weights on the tensor cores, FP32
  * accumulation -- trained online (Adam, mean squared error) on `batch` fresh Philox samples of the
- * integrand per step for `train_steps` steps by the library's own forward/backward kernels.  Per
- * bin, the integral of g is taken by composite Gauss-Legendre quadrature (`quad_cells` equal cells
- * per binned dimension, `quad_cells_unbinned` per unbinned dimension -- those span the whole range
- * rather than one bin -- and `quad_nodes` (1..4) nodes per cell) and only f - g is Monte Carlo
- * sampled (`samples_per_bin` Philox points): the estimate is unbiased up to that quadrature's
- * error on the network; with
- * `fallback` set, a bin keeps the plain Monte Carlo mean of the same samples when its sample
- * variance is lower than the residual's.  Scalar integrands of dimension 2, 3 or 5.            */
+ * integrand per step, for at most `train_steps` steps, by the library's own forward/backward
+ * kernels; with `check_every` > 0 the mean squared error on a fixed held-out set is measured every
+ * `check_every` steps and training stops once it no longer improves by 0.5 %.
+ * The control variate of a bin is h, the piecewise-quadratic interpolant of the trained network g
+ * on a grid of Simpson nodes -- `cells` cells per binned dimension inside the bin (0: h is constant
+ * there, g's value at the bin centre) and `cells_unbinned` cells per unbinned dimension over the
+ * range -- i.e. nested quadrature's own polynomial: the integral of h over the bin is exactly the
+ * composite Simpson sum of the node values, so the estimate  integral(h) + mean(f - h)  over
+ * `samples_per_bin` Philox points is unbiased.  With `fallback` set, `pilot` separate samples per
+ * bin (0: samples/8 clamped to 8..256; not reused in the estimate) decide per bin between the
+ * learned estimate and plain Monte Carlo of the same samples (the lower pilot variance), and, when
+ * poly_bins/poly_variance are given (vcu_control_variates' bins and vcu_cv::variance for the same
+ * problem), the polynomial control variate's estimate replaces the bin's when its variance is the
+ * lower one.  At most 4913 grid nodes per bin.  Scalar integrands of dimension 2, 3 or 5. */
 typedef struct vcu_learned {
     uint64_t samples_per_bin;
     uint64_t seed;
-    uint32_t train_steps;
+    uint32_t train_steps;     /* at most this many Adam steps                                  */
     uint32_t batch;           /* training samples per step (rounded up to whole blocks)        */
     float learning_rate;
-    uint32_t quad_nodes;      /* Gauss-Legendre nodes per dimension for the integral of g, 1..4 */
-    int32_t fallback;         /* 1: per-bin fallback to plain Monte Carlo                       */
-    int32_t quad_cells;       /* composite cells per binned dimension for the integral of g (0 = 1) */
+    uint32_t check_every;     /* held-out check period for early stopping (0: all steps)       */
+    int32_t fallback;         /* 1: per-bin choice of the lowest-variance estimator            */
+    int32_t cells;            /* Simpson cells per binned dimension in a bin (0: constant)     */
     float* theta_out;         /* nullable host buffer: receives the trained fp32 parameters
                                  (vcu_mlp_eval layout), e.g. to checkpoint the network        */
-    int32_t quad_cells_unbinned; /* cells per unbinned dimension (0 = quad_cells)             */
-    int32_t reserved2;
+    int32_t cells_unbinned;   /* Simpson cells per unbinned dimension over the range (>= 1)    */
+    uint32_t pilot;           /* pilot samples per bin for the fallback choice (0: automatic)  */
+    const float* poly_bins;   /* nullable (follows mem): the polynomial CV's bins              */
+    const float* poly_variance; /* nullable (follows mem): their variances; both or neither    */
 } vcu_learned;
 
 typedef struct vcu_learned_report {
     double train_ms, integral_ms, residual_ms;
-    uint32_t fallback_bins;   /* bins that kept the plain Monte Carlo estimate */
-    uint32_t reserved;
+    double heldout_mse;       /* held-out mean squared error of the network at the end         */
+    uint32_t fallback_bins;   /* bins that took the plain Monte Carlo estimate                 */
+    uint32_t polynomial_bins; /* bins that took the polynomial control variate's estimate      */
+    uint32_t train_steps_run; /* Adam steps taken (early stopping)                             */
+    uint32_t nodes_per_bin;   /* grid nodes of the interpolant per bin                         */
 } vcu_learned_report;
 
-/* network_integral (nullable, follows p->mem): per bin, the mean of g over the bin */
+/* network_integral (nullable, follows p->mem): per bin, the mean of h over the bin */
 int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_learned* opt, float* bins,
                                  float* network_integral, vcu_learned_report* report, vcu_stats* stats);
 

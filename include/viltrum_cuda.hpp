@@ -430,25 +430,28 @@ inline control_variates crespo2021_infinite(unsigned long iterations, unsigned m
 
 /* ---------------------------------------------------------------- learned control variate */
 /* No reference counterpart: per bin, a frequency-encoded 4x64 MLP g trained online on the
- * integrand's own samples, its integral by composite Gauss-Legendre quadrature, and only f - g
- * sampled (vcu_learned_control_variates); assigns. */
+ * integrand's own samples (early stopping on a held-out set every check_every steps), the
+ * piecewise-quadratic interpolant h of g on each bin's grid of Simpson nodes as the control variate
+ * (its integral is exact: the estimate is unbiased), and only f - h sampled; with fallback, a pilot
+ * per bin picks the lower-variance of this and plain Monte Carlo (vcu_learned_control_variates);
+ * assigns. */
 class learned_control_variates {
     vcu_learned opt_;
 
 public:
     explicit learned_control_variates(unsigned long samples, std::uint64_t seed = 0, unsigned train_steps = 1000,
-                                      unsigned batch = 32768, float learning_rate = 3e-3f, unsigned quad_nodes = 3,
-                                      int quad_cells = 1, bool fallback = true, int quad_cells_unbinned = 0)
+                                      unsigned batch = 32768, float learning_rate = 3e-3f, int cells = 2,
+                                      int cells_unbinned = 4, bool fallback = true, unsigned check_every = 0)
         : opt_{} {
         opt_.samples_per_bin = samples;
         opt_.seed = seed;
         opt_.train_steps = train_steps;
         opt_.batch = batch;
         opt_.learning_rate = learning_rate;
-        opt_.quad_nodes = quad_nodes;
+        opt_.check_every = check_every;
         opt_.fallback = fallback ? 1 : 0;
-        opt_.quad_cells = quad_cells;
-        opt_.quad_cells_unbinned = quad_cells_unbinned;
+        opt_.cells = cells;
+        opt_.cells_unbinned = cells_unbinned;
     }
 
     template <class Bins, std::size_t DIMBINS, class F, class R, class Logger>

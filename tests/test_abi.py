@@ -41,7 +41,7 @@ def test_library_exports_every_declared_symbol(lib_path):
 def test_host_logic_without_device(lib_path):
     """ABI version, channel table, and argument validation that happens before any device use."""
     lib = ctypes.CDLL(lib_path)
-    assert lib.vcu_abi_version() == 1
+    assert lib.vcu_abi_version() == 2
     assert lib.vcu_channels(5) == 1 and lib.vcu_channels(6) == 3 and lib.vcu_channels(99) < 0
     assert lib.vcu_per_bin_monte_carlo(None, None, 1, 1, None, None) == 1  # null context -> INVALID_ARG
     assert lib.vcu_integrate_batch(None, 7, None, None, 0, None, 0, None, None) == 1

@@ -49,7 +49,7 @@ def test_cpp_dropin_matches_c_abi(ctx, tmp_path):
     # learned control variate (16 samples, seed 5, 50 steps, defaults of the header)
     l = np.empty(16, np.float32)
     ctx.learned_control_variates(ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [16]),
-                                 _lib.LearnedOpts(16, 5, 50, 32768, 3e-3, 3, 1, 1), l)
+                                 _lib.LearnedOpts(16, 5, 50, 32768, 3e-3, 0, 1, 2, None, 4), l)
     assert np.array_equal(lrn.view(np.uint32), l.view(np.uint32))
     # adaptive_iterations used directly, then adaptive_tolerance, accumulating into bins that start at 0.5
     gb = np.full(32, 0.5, np.float32)

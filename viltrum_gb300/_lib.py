@@ -74,22 +74,27 @@ class CvOpts(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("alpha", ctypes.c_double), ("rr", ctypes.c_int32),
                 ("sampling", ctypes.c_int32), ("rr_factor", ctypes.c_float), ("reserved2", ctypes.c_int32),
                 ("mis_power", ctypes.c_double), ("mis_cutoff", ctypes.c_double), ("fubini_dims", ctypes.c_int32),
-                ("tail_samples", ctypes.c_uint32)]
+                ("tail_samples", ctypes.c_uint32), ("variance", ctypes.c_void_p)]
 
 
 class LearnedOpts(ctypes.Structure):
+    """vcu_learned.  Positional: samples_per_bin, seed, train_steps, batch, learning_rate,
+    check_every, fallback, cells, theta_out, cells_unbinned, pilot, poly_bins, poly_variance."""
     _fields_ = [("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("train_steps", ctypes.c_uint32),
-                ("batch", ctypes.c_uint32), ("learning_rate", ctypes.c_float), ("quad_nodes", ctypes.c_uint32),
-                ("fallback", ctypes.c_int32), ("quad_cells", ctypes.c_int32), ("theta_out", ctypes.c_void_p),
-                ("quad_cells_unbinned", ctypes.c_int32), ("reserved2", ctypes.c_int32)]
+                ("batch", ctypes.c_uint32), ("learning_rate", ctypes.c_float), ("check_every", ctypes.c_uint32),
+                ("fallback", ctypes.c_int32), ("cells", ctypes.c_int32), ("theta_out", ctypes.c_void_p),
+                ("cells_unbinned", ctypes.c_int32), ("pilot", ctypes.c_uint32), ("poly_bins", ctypes.c_void_p),
+                ("poly_variance", ctypes.c_void_p)]
 
 
 class LearnedReport(ctypes.Structure):
     _fields_ = [("train_ms", ctypes.c_double), ("integral_ms", ctypes.c_double), ("residual_ms", ctypes.c_double),
-                ("fallback_bins", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("heldout_mse", ctypes.c_double), ("fallback_bins", ctypes.c_uint32),
+                ("polynomial_bins", ctypes.c_uint32), ("train_steps_run", ctypes.c_uint32),
+                ("nodes_per_bin", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class BatchItem(ctypes.Structure):

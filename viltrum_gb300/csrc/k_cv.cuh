@@ -554,6 +554,7 @@ struct ResCfg {
     const float* rerr;        /* VCU_RR_ERROR: norm of each heap region's error estimate */
     double* cdf;              /* importance choice, per list entry: cumulative probability */
     double* rrf;              /* importance choice, per list entry: 1 / probability */
+    float* var_out;           /* nullable: per bin, the estimated variance of the estimate */
 };
 
 /* rr_error_region weighs a region by norm(error()), error() = volume * (fold_all(H) - fold_all(low))
@@ -844,7 +845,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
      * recombination is FP64 -- FP64 runs at a small fraction of the FP32 rate here */
     float sf32[CH], cf32[CH], sa32[CH], ca32[CH];
     for (int c = 0; c < CH; ++c) sf32[c] = cf32[c] = sa32[c] = ca32[c] = 0.0f;
-    float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f;
+    float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f, m2f32 = 0.0f;
     const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
     for (uint64_t j = lane; j < cfg.spp && n > 0; j += 32) {
         uint32_t chosen;
@@ -1017,6 +1018,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         const float da2 = vsub(na, ma32);
         m2a32 = vfma(da, da2, m2a32);
         cfa32 = vfma(df, da2, cfa32);
+        if (cfg.var_out) m2f32 = vfma(df, vsub(nf, mf32), m2f32);
     }
     /* lanes merged in FP32: each Kahan sum as the float-float pair (sum, -compensation) added with
      * two-sum, the moments by Chan's pairwise formulas (one division per step) */
@@ -1037,6 +1039,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
      * of FP32 moments moves the estimate (large sample weights whose f and g terms cancel), and FP64
      * runs at a small fraction of the FP32 rate here */
     ffn::FF mf = ffn::make(mf32), ma = ffn::make(ma32), m2a = ffn::make(m2a32), cfa = ffn::make(cfa32);
+    float m2f = m2f32; /* only for the variance report: FP32 is enough */
     float wn = wn32;
     for (int off2 = 16; off2 > 0; off2 >>= 1) {
         for (int c = 0; c < CH; ++c) {
@@ -1048,11 +1051,13 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         const float nb = __shfl_down_sync(0xffffffffu, wn, off2);
         const ffn::FF mfb = ffn::shfl_down(mf, off2), mab = ffn::shfl_down(ma, off2);
         const ffn::FF m2b = ffn::shfl_down(m2a, off2), cb = ffn::shfl_down(cfa, off2);
+        const float m2fb = __shfl_down_sync(0xffffffffu, m2f, off2);
         const float nt = vadd(wn, nb); /* counts: exact */
         if (nb > 0.0f && nt > 0.0f) {
             const ffn::FF r = ffn::div(ffn::make(nb), ffn::make(nt));
             const ffn::FF dfm = ffn::sub(mfb, mf), dam = ffn::sub(mab, ma);
             const ffn::FF w = ffn::mul(ffn::make(wn), r);
+            m2f = m2f + m2fb + dfm.h * dfm.h * w.h;
             mf = ffn::add(mf, ffn::mul(dfm, r));
             ma = ffn::add(ma, ffn::mul(dam, r));
             m2a = ffn::add(m2a, ffn::add(m2b, ffn::mul(ffn::mul(dam, dam), w)));
@@ -1103,6 +1108,17 @@ __global__ void __launch_bounds__(RES_WARPS * 32)
         nan = nan || isnan(o);
         bins[bin * CH + c] = o;
         if (approx_out) approx_out[bin * CH + c] = approx[c];
+    }
+    if (cfg.var_out) {
+        /* variance of the estimate, Var(norm f - alpha norm g) / n from the sample moments of the
+         * weighted norms (exact for a non-negative scalar integrand); infinite without 2 samples */
+        float var = __int_as_float(0x7f800000);
+        if (!use_approx && cfg.spp >= 2) {
+            const float nn = (float)cfg.spp, a = vadd(alpha.h, alpha.l);
+            const float m2 = vfma(vmul(a, a), m2a.h, vfma(vmul(-2.0f, a), cfa.h, m2f));
+            var = m2 > 0.0f ? vdiv(m2, vmul(nn, vsub(nn, 1.0f))) : 0.0f;
+        }
+        cfg.var_out[bin] = var;
     }
     if (nan) atomicOr(status, VCU_FLAG_NAN);
 }
@@ -1217,6 +1233,7 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     rcfg.mis_power = cv.mis_power;
     rcfg.mis_cutoff = cv.mis_cutoff;
     rcfg.rec_w = (uint32_t)vcu_cv_replay_width(DIM, cv.sampling);
+    rcfg.var_out = cv.variance;
     const unsigned rblocks = (unsigned)((g.nbins + RES_WARPS - 1) / RES_WARPS);
     const bool pdf = cv.rr == VCU_RR_PDF || cv.sampling != VCU_RS_UNIFORM;
     if constexpr (S == 3) {

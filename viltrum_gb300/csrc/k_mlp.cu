@@ -1,20 +1,27 @@
 /*
- * k_mlp.cu -- learned control variate: online training, per-bin integral of the network, residual.
+ * k_mlp.cu -- learned control variate: online training, the network's interpolant per bin, residual.
  *
  * No reference counterpart (the task's learned part; the per-bin wrapper it plugs into is
  * src/integrator-per-bin-parallel.h:17-35).  Pipeline of vcu_learned_control_variates:
- *  1. train: `train_steps` Adam steps on fresh samples of the integrand (Philox points over the
- *     range, the integrand evaluated by the device) minimising mean (g - f)^2; each step is one
- *     sampling kernel, one fused forward+backward kernel (k_mlp_train: every block writes its own
- *     partial gradient, no atomics), one Adam kernel that sums the partials in a fixed order and
- *     rewrites the BF16 image of the weights, and one counter kernel -- captured once in a CUDA
- *     graph and replayed for all steps;
- *  2. k_mlp_integral: per bin, Gauss-Legendre quadrature (q nodes per dimension) of g over the bin;
- *  3. k_mlp_residual: per bin, `samples` Philox points, estimate = integral of g + mean(f - g)
- *     (control variate with weight 1: unbiased up to the quadrature error of the network's
- *     integral); optionally the plain Monte Carlo mean of the same samples is kept instead when
- *     its sample variance is lower (per-bin fallback).
+ *  1. train: Adam steps on fresh samples of the integrand (Philox points over the range, the
+ *     integrand evaluated by the device) minimising mean (g - f)^2; each step is one sampling
+ *     kernel, one fused forward+backward kernel (k_mlp_train: every block writes its own partial
+ *     gradient, no atomics), one Adam kernel that sums the partials in a fixed order and rewrites
+ *     the BF16 image of the weights, and one counter kernel -- captured once in a CUDA graph and
+ *     replayed; every `check_every` steps the mean squared error on a fixed held-out set is summed
+ *     per block (k_mlp_heldout) and added in block order on the host, and training stops once it
+ *     no longer improves;
+ *  2. k_mlp_nodes: the network at the Simpson nodes of every bin's grid (tensor cores, 16-point
+ *     tiles), a chunk of bins at a time;
+ *  3. k_mlp_cv: per bin, the interpolant h of those node values (piecewise quadratic, Lagrange on
+ *     the three nodes of a cell per dimension; constant in a dimension with one node) is the
+ *     control variate: its mean over the bin is the composite Simpson sum of the nodes -- exact, so
+ *     integral(h) + mean(f - h) over the residual samples is unbiased.  Optional per-bin choice,
+ *     from separate pilot samples, of the lowest-variance of this estimate, plain Monte Carlo and a
+ *     given polynomial control variate.
  */
+#include <algorithm>
+
 #include "k_mlp.cuh"
 
 namespace vcu {
@@ -401,21 +408,64 @@ template <int D> __global__ void k_mlp_pack(const float* __restrict__ theta, cha
     if (p < n_params(D)) pack_param<D>(packed, p, theta[p]);
 }
 
-/* ---------------------------------------------------------------- per-bin integral of g */
-struct BinCfg {
+/* ---------------------------------------------------------------- held-out loss */
+/* per block: the sum of (g - y)^2 over its points of the held-out set, FP64 in a fixed order */
+template <int D>
+__global__ void __launch_bounds__(FWD_WARPS * 32)
+    k_mlp_heldout(const char* __restrict__ packed, const float* __restrict__ u, const float* __restrict__ y,
+                  uint64_t npts, double* __restrict__ partial) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ double wsum[FWD_WARPS];
+    load_params<D>(smem, packed, false);
+    const SmemParams<D> P = smem_params<D>(smem, false);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
+    double acc = 0.0;
+    const uint64_t tiles = (npts + 15) / 16;
+    for (uint64_t tile = (uint64_t)blockIdx.x * FWD_WARPS + warp; tile < tiles; tile += (uint64_t)gridDim.x * FWD_WARPS) {
+        const uint64_t s0 = tile * 16 + g, s1 = s0 + 8;
+        float ug[D], ug8[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            ug[d] = s0 < npts ? u[s0 * D + d] : 0.5f;
+            ug8[d] = s1 < npts ? u[s1 * D + d] : 0.5f;
+        }
+        Acts<D> a;
+        features_tile<D>(ug, ug8, a.F);
+        float out[2];
+        forward_tile<D>(P, a, out);
+        if ((lane & 3) == 0) {
+            if (s0 < npts) acc += (double)(out[0] - y[s0]) * (double)(out[0] - y[s0]);
+            if (s1 < npts) acc += (double)(out[1] - y[s1]) * (double)(out[1] - y[s1]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) wsum[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < FWD_WARPS; ++w) t += wsum[w];
+        partial[blockIdx.x] = t;
+    }
+}
+
+/* ---------------------------------------------------------------- the interpolation grid */
+/* Per dimension the grid has n[d] = 2 cells + 1 Simpson nodes (or one node, at the bin centre, for
+ * a binned dimension with no cells); the nodes of a bin are numbered dimension 0 fastest. */
+struct GridCfg {
     RangeCfg r;
     float drange[VCU_MAX_DIMBINS];
     uint32_t res[VCU_MAX_DIMBINS];
     int32_t dimbins;
     uint64_t nbins;
-    int32_t q;     /* Gauss-Legendre nodes per cell and dimension */
-    int32_t cells;          /* composite cells per binned dimension   */
-    int32_t cells_unbinned; /* composite cells per unbinned dimension */
-    float gl_x[4], gl_w[4];
+    int32_t n[VCU_MAX_DIM]; /* nodes per dimension */
+    int32_t npb;            /* nodes per bin        */
 };
 
+/* lower/upper corner of the box the grid spans in each dimension: the bin in binned dimensions,
+ * the range in the others */
 template <int D>
-__device__ __forceinline__ void bin_box(const BinCfg& c, uint64_t bin, float* lo, float* hi) {
+__device__ __forceinline__ void grid_box(const GridCfg& c, uint64_t bin, float* lo, float* hi) {
     uint64_t rem = bin;
     for (int d = 0; d < D; ++d) {
         lo[d] = c.r.rmin[d];
@@ -429,164 +479,232 @@ __device__ __forceinline__ void bin_box(const BinCfg& c, uint64_t bin, float* lo
     }
 }
 
+/* the network at every grid node of bins [bin0, bin0 + count): out[(bin - bin0) * npb + node] */
 template <int D>
 __global__ void __launch_bounds__(FWD_WARPS * 32)
-    k_mlp_integral(const BinCfg c, const char* __restrict__ packed, float* __restrict__ integral) {
+    k_mlp_nodes(const GridCfg c, const char* __restrict__ packed, uint64_t bin0, uint64_t count,
+                float* __restrict__ out) {
     extern __shared__ __align__(16) char smem[];
     load_params<D>(smem, packed, false);
     const SmemParams<D> P = smem_params<D>(smem, false);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
-    /* per dimension `cells` equal cells of q Gauss-Legendre nodes; the unbinned dimensions, which
-     * span the whole range rather than one bin, have their own cell count */
-    int qd[D], cd[D];
-    int nodes = 1;
-    for (int d = 0; d < D; ++d) {
-        cd[d] = d < c.dimbins ? c.cells : c.cells_unbinned;
-        qd[d] = c.q * cd[d];
-        nodes *= qd[d];
-    }
-    for (uint64_t bin = (uint64_t)blockIdx.x * FWD_WARPS + warp; bin < c.nbins; bin += (uint64_t)gridDim.x * FWD_WARPS) {
+    const uint64_t tiles_per_bin = (uint64_t)(c.npb + 15) / 16, tiles = count * tiles_per_bin;
+    for (uint64_t tile = (uint64_t)blockIdx.x * FWD_WARPS + warp; tile < tiles; tile += (uint64_t)gridDim.x * FWD_WARPS) {
+        const uint64_t lb = tile / tiles_per_bin;
+        const int n0 = (int)(tile % tiles_per_bin) * 16 + g, n1 = n0 + 8;
         float lo[D], hi[D];
-        bin_box<D>(c, bin, lo, hi);
-        double acc = 0.0;
-        for (int base = 0; base < nodes; base += 16) {
-            float ug[D], ug8[D], w0 = 1.0f, w1 = 1.0f;
-            const int n0 = base + g, n1 = base + g + 8;
-            int r0 = n0, r1 = n1;
-            for (int d = 0; d < D; ++d) {
-                const int i0 = r0 % qd[d], i1 = r1 % qd[d];
-                r0 /= qd[d];
-                r1 /= qd[d];
-                const float inv_cells = 1.0f / (float)cd[d];
-                /* node j of cell k: (k + (1 + x_j) / 2) / cells of the extent */
-                const float t0 = ((float)(i0 / c.q) + 0.5f * (1.0f + c.gl_x[i0 % c.q])) * inv_cells;
-                const float t1 = ((float)(i1 / c.q) + 0.5f * (1.0f + c.gl_x[i1 % c.q])) * inv_cells;
-                const float x0 = lo[d] + (hi[d] - lo[d]) * t0;
-                const float x1 = lo[d] + (hi[d] - lo[d]) * t1;
-                const float span = c.r.rmax[d] - c.r.rmin[d];
-                ug[d] = (x0 - c.r.rmin[d]) / span;
-                ug8[d] = (x1 - c.r.rmin[d]) / span;
-                w0 *= 0.5f * c.gl_w[i0 % c.q] * inv_cells;
-                w1 *= 0.5f * c.gl_w[i1 % c.q] * inv_cells;
-            }
-            Acts<D> a;
-            features_tile<D>(ug, ug8, a.F);
-            float out[2];
-            forward_tile<D>(P, a, out);
-            if ((lane & 3) == 0) acc += (n0 < nodes ? (double)(w0 * out[0]) : 0.0) + (n1 < nodes ? (double)(w1 * out[1]) : 0.0);
-        }
+        grid_box<D>(c, bin0 + lb, lo, hi);
+        float ug[D], ug8[D];
+        int r0 = n0 < c.npb ? n0 : 0, r1 = n1 < c.npb ? n1 : 0;
 #pragma unroll
-        for (int o = 4; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) integral[bin] = (float)acc; /* mean of g over the bin */
+        for (int d = 0; d < D; ++d) {
+            const int i0 = r0 % c.n[d], i1 = r1 % c.n[d];
+            r0 /= c.n[d];
+            r1 /= c.n[d];
+            /* node i of n: lo + (hi - lo) * i / (n - 1); the centre when n == 1 */
+            const float t0 = c.n[d] == 1 ? 0.5f : (float)i0 / (float)(c.n[d] - 1);
+            const float t1 = c.n[d] == 1 ? 0.5f : (float)i1 / (float)(c.n[d] - 1);
+            const float span = c.r.rmax[d] - c.r.rmin[d];
+            ug[d] = (lo[d] + (hi[d] - lo[d]) * t0 - c.r.rmin[d]) / span;
+            ug8[d] = (lo[d] + (hi[d] - lo[d]) * t1 - c.r.rmin[d]) / span;
+        }
+        Acts<D> a;
+        features_tile<D>(ug, ug8, a.F);
+        float o[2];
+        forward_tile<D>(P, a, o);
+        if ((lane & 3) == 0) {
+            float* dst = out + lb * (uint64_t)c.npb;
+            if (n0 < c.npb) dst[n0] = o[0];
+            if (n1 < c.npb) dst[n1] = o[1];
+        }
     }
 }
 
 /* ---------------------------------------------------------------- residual */
-struct ResidualCfg {
-    BinCfg b;
-    uint64_t spp;
+struct CvCfg {
+    GridCfg gr;
+    uint64_t spp, pilot;
     uint32_t k0, k1;
     int32_t fallback;
     float factor; /* prod(res) */
+    const float* poly_bins;
+    const float* poly_var;
 };
 
+/* weight of node j (of n) in the composite Simpson mean over [0,1] with (n-1)/2 cells */
+__device__ __forceinline__ float simpson_weight(int j, int n) {
+    if (n == 1) return 1.0f;
+    const float cells = 0.5f * (float)(n - 1);
+    const float w = (j == 0 || j == n - 1) ? 1.0f : ((j & 1) ? 4.0f : 2.0f);
+    return w / (6.0f * cells);
+}
+
+/* sum over the nodes of the point's cell of weight x node value, one dimension per level: a
+ * dimension contributes 3 nodes (Lagrange weights w0..w2) or 1 (weight 1) */
+template <int d, int D>
+__device__ __forceinline__ float interp_level(const float* __restrict__ nodes, const int* off, const int* stride,
+                                              const int* nw, const float (*w)[3], int idx, float wacc) {
+    if constexpr (d == D) {
+        return wacc * __ldg(nodes + idx);
+    } else {
+        float h = interp_level<d + 1, D>(nodes, off, stride, nw, w, idx + off[d], wacc * w[d][0]);
+        if (nw[d] == 3) {
+            h += interp_level<d + 1, D>(nodes, off, stride, nw, w, idx + off[d] + stride[d], wacc * w[d][1]);
+            h += interp_level<d + 1, D>(nodes, off, stride, nw, w, idx + off[d] + 2 * stride[d], wacc * w[d][2]);
+        }
+        return h;
+    }
+}
+
+/* h at a point (normalised coordinates t in [0,1] per dimension of the grid box): Lagrange
+ * interpolation on the three nodes of the point's cell in each dimension with cells */
+template <int D>
+__device__ __forceinline__ float interpolant(const GridCfg& c, const float* __restrict__ nodes, const float* t) {
+    int off[D], stride[D], nw[D];
+    float w[D][3];
+    int st = 1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        stride[d] = st;
+        if (c.n[d] == 1) {
+            off[d] = 0;
+            nw[d] = 1;
+            w[d][0] = 1.0f;
+            w[d][1] = w[d][2] = 0.0f;
+        } else {
+            const int cells = (c.n[d] - 1) >> 1;
+            const float sc = t[d] * (float)cells;
+            int k = (int)sc;
+            k = k < 0 ? 0 : (k > cells - 1 ? cells - 1 : k);
+            const float s = sc - (float)k; /* in [0, 1] */
+            off[d] = 2 * k * st;
+            nw[d] = 3;
+            w[d][0] = 2.0f * (s - 0.5f) * (s - 1.0f);
+            w[d][1] = -4.0f * s * (s - 1.0f);
+            w[d][2] = 2.0f * s * (s - 0.5f);
+        }
+        st *= c.n[d];
+    }
+    return interp_level<0, D>(nodes, off, stride, nw, w, 0, 1.0f);
+}
+
+/* Welford update of a (count, mean, M2) triple, FP32 */
+__device__ __forceinline__ void welford(float& n, float& m, float& m2, float x) {
+    n += 1.0f;
+    const float dx = x - m;
+    m = fmaf(dx, 1.0f / n, m);
+    m2 = fmaf(dx, x - m, m2);
+}
+/* Chan's pairwise merge of two such triples across the lanes of a warp (xor shuffles) */
+__device__ __forceinline__ void warp_merge(float& n, float& m, float& m2) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float nb = __shfl_xor_sync(0xffffffffu, n, o);
+        const float mb = __shfl_xor_sync(0xffffffffu, m, o);
+        const float m2b = __shfl_xor_sync(0xffffffffu, m2, o);
+        const float nt = n + nb;
+        if (nt > 0.0f) {
+            const float r = nb / nt, dm = mb - m;
+            m = fmaf(dm, r, m);
+            m2 = m2 + m2b + dm * dm * n * r;
+            n = nt;
+        }
+    }
+}
+
+/* one warp per bin of the chunk: mean of h by Simpson weights, optional pilot choice, residual */
 template <class F, int D>
 __global__ void __launch_bounds__(FWD_WARPS * 32)
-    k_mlp_residual(const __grid_constant__ F f, const ResidualCfg c, const char* __restrict__ packed,
-                   const float* __restrict__ integral, float* __restrict__ bins, uint32_t* __restrict__ fallback_count,
-                   uint32_t* __restrict__ status) {
-    extern __shared__ __align__(16) char smem[];
-    load_params<D>(smem, packed, false);
-    const SmemParams<D> P = smem_params<D>(smem, false);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2;
-    for (uint64_t bin = (uint64_t)blockIdx.x * FWD_WARPS + warp; bin < c.b.nbins;
-         bin += (uint64_t)gridDim.x * FWD_WARPS) {
+    k_mlp_cv(const __grid_constant__ F f, const CvCfg c, uint64_t bin0, uint64_t count, const float* __restrict__ nodes,
+             float* __restrict__ bins, float* __restrict__ integral, uint32_t* __restrict__ counters,
+             uint32_t* __restrict__ status) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint64_t lb = (uint64_t)blockIdx.x * FWD_WARPS + warp; lb < count; lb += (uint64_t)gridDim.x * FWD_WARPS) {
+        const uint64_t bin = bin0 + lb;
+        const float* nd = nodes + lb * (uint64_t)c.gr.npb;
         float lo[D], hi[D];
-        bin_box<D>(c.b, bin, lo, hi);
+        grid_box<D>(c.gr, bin, lo, hi);
+        /* the grid box is the bin's integration box: the bin in binned dimensions, the range in the others */
         float vol = 1.0f;
         for (int d = 0; d < D; ++d) vol = vmul(vol, vsub(hi[d], lo[d]));
-        /* per lane, in FP32: Welford means and squared deviations of f and of f - g; merged across
-         * the lanes in FP32 too (Chan's pairwise formulas, one division per step): FP64 runs at a
-         * small fraction of the FP32 rate, and the means are only summed into the estimate in FP64 */
-        float wn = 0.0f, mf = 0.0f, m2f = 0.0f, mr = 0.0f, m2r = 0.0f;
-        for (uint64_t base = 0; base < c.spp; base += 32) {
-            const uint64_t s = base + lane;
-            const bool valid = s < c.spp;
-            float u[D], x[F::DIM];
-            for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+        /* mean of h over the box: composite Simpson weights of the nodes, FP64 lane sums */
+        double mh = 0.0;
+        for (int k = lane; k < c.gr.npb; k += 32) {
+            int r = k;
+            float w = 1.0f;
 #pragma unroll
-            for (int blk = 0; blk < (D + 3) / 4; ++blk) {
-                const U4 r = philox4x32_10(U4{(uint32_t)s, (uint32_t)bin, (uint32_t)(bin >> 32), 0x5E5D0000u + blk},
-                                           c.k0, c.k1);
-                const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int d = blk * 4 + k;
-                    if (d < D) x[d] = vadd(vmul(u01(rr[k]), vsub(hi[d], lo[d])), lo[d]);
-                }
+            for (int d = 0; d < D; ++d) {
+                w *= simpson_weight(r % c.gr.n[d], c.gr.n[d]);
+                r /= c.gr.n[d];
             }
-            for (int d = 0; d < D; ++d) u[d] = (x[d] - c.b.r.rmin[d]) / (c.b.r.rmax[d] - c.b.r.rmin[d]);
-            float fv[1];
-            f(x, fv);
-            /* g at the 32 points: two 16-point tiles */
-            float gme = 0.0f;
+            mh += (double)w * (double)__ldg(nd + k);
+        }
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                float ug[D], ug8[D];
-                for (int d = 0; d < D; ++d) {
-                    ug[d] = __shfl_sync(0xffffffffu, u[d], 16 * half + g);
-                    ug8[d] = __shfl_sync(0xffffffffu, u[d], 16 * half + g + 8);
+        for (int o = 16; o > 0; o >>= 1) mh += __shfl_xor_sync(0xffffffffu, mh, o);
+        const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
+        /* samples of stream `tag`: f and r = f - h, Welford per lane */
+        auto run = [&](uint64_t n, uint32_t tag, float* st) {
+            float nf = 0.0f, mf = 0.0f, m2f = 0.0f, nr = 0.0f, mr = 0.0f, m2r = 0.0f;
+            for (uint64_t s = lane; s < n; s += 32) {
+                float x[F::DIM], t[D];
+                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+#pragma unroll
+                for (int blk = 0; blk < (D + 3) / 4; ++blk) {
+                    const U4 rr4 = philox4x32_10(U4{(uint32_t)s, blo, bhi, tag + blk}, c.k0, c.k1);
+                    const uint32_t rr[4] = {rr4.x, rr4.y, rr4.z, rr4.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int d = blk * 4 + k;
+                        if (d < D) {
+                            const float u = u01(rr[k]);
+                            x[d] = vadd(vmul(u, vsub(hi[d], lo[d])), lo[d]);
+                            t[d] = u;
+                        }
+                    }
                 }
-                Acts<D> a;
-                features_tile<D>(ug, ug8, a.F);
-                float out[2];
-                forward_tile<D>(P, a, out);
-                /* point p = 16*half + r lives in lanes 4*(r%8).. as out[r/8] */
-                const int r = lane - 16 * half;
-                const float o0 = __shfl_sync(0xffffffffu, out[0], 4 * (lane & 7));
-                const float o1 = __shfl_sync(0xffffffffu, out[1], 4 * (lane & 7));
-                if (r >= 0 && r < 16) gme = (r < 8) ? o0 : o1;
+                float fv[1];
+                f(x, fv);
+                const float hv = interpolant<D>(c.gr, nd, t);
+                welford(nf, mf, m2f, fv[0]);
+                welford(nr, mr, m2r, fv[0] - hv);
             }
-            if (valid) {
-                const float rv = vsub(fv[0], gme);
-                wn = vadd(wn, 1.0f);
-                const float inv = vdiv(1.0f, wn);
-                const float df = vsub(fv[0], mf);
-                mf = vfma(df, inv, mf);
-                m2f = vfma(df, vsub(fv[0], mf), m2f);
-                const float dr = vsub(rv, mr);
-                mr = vfma(dr, inv, mr);
-                m2r = vfma(dr, vsub(rv, mr), m2r);
+            warp_merge(nf, mf, m2f);
+            warp_merge(nr, mr, m2r);
+            st[0] = nf;
+            st[1] = mf;
+            st[2] = m2f;
+            st[3] = mr;
+            st[4] = m2r;
+        };
+        /* 0: learned, 1: plain Monte Carlo, 2: polynomial control variate */
+        int choice = 0;
+        if (c.fallback) {
+            float ps[5];
+            run(c.pilot, 0x91107000u, ps);
+            const float var_r = ps[4], var_f = ps[2]; /* both over the same pilot count */
+            choice = var_f < var_r ? 1 : 0;
+            if (c.poly_bins) {
+                /* variance of this bin's estimate: the pilot variance over the residual samples,
+                 * scaled to bin values, against the polynomial estimate's own */
+                const double scale = (double)c.factor * (double)vol;
+                const double pv = ps[0] > 1.0f ? (double)(choice ? var_f : var_r) / (ps[0] - 1.0f) : INFINITY;
+                const double v_mine = pv * scale * scale / (double)c.spp;
+                const float v_poly = c.poly_var[bin];
+                if ((double)v_poly < v_mine) choice = 2;
             }
         }
-        float n_a = wn, mf_a = mf, m2f_a = m2f, mr_a = mr, m2r_a = m2r;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float n_b = __shfl_xor_sync(0xffffffffu, n_a, o);
-            const float mf_b = __shfl_xor_sync(0xffffffffu, mf_a, o);
-            const float m2f_b = __shfl_xor_sync(0xffffffffu, m2f_a, o);
-            const float mr_b = __shfl_xor_sync(0xffffffffu, mr_a, o);
-            const float m2r_b = __shfl_xor_sync(0xffffffffu, m2r_a, o);
-            const float nt = vadd(n_a, n_b);
-            if (nt > 0.0f) {
-                const float r = vdiv(n_b, nt);
-                const float w = vmul(n_a, r), df = vsub(mf_b, mf_a), dr = vsub(mr_b, mr_a);
-                mf_a = vfma(df, r, mf_a);
-                mr_a = vfma(dr, r, mr_a);
-                m2f_a = vadd(m2f_a, vfma(vmul(df, df), w, m2f_b));
-                m2r_a = vadd(m2r_a, vfma(vmul(dr, dr), w, m2r_b));
-                n_a = nt;
-            }
-        }
+        float ms[5];
+        if (choice != 2) run(c.spp, 0x5E5D0000u, ms);
         if (lane == 0) {
             const double scale = (double)c.factor * (double)vol;
-            const double est_cv = scale * ((double)integral[bin] + (double)mr_a);
-            const double est_mc = scale * (double)mf_a;
-            const double var_r = n_a > 0.0f ? (double)m2r_a / n_a : 0.0, var_f = n_a > 0.0f ? (double)m2f_a / n_a : 0.0;
-            const bool use_mc = c.fallback && var_f < var_r;
-            const float o = (float)(use_mc ? est_mc : est_cv);
+            float o;
+            if (choice == 2) o = c.poly_bins[bin];
+            else if (choice == 1) o = (float)(scale * (double)ms[1]);
+            else o = (float)(scale * (mh + (double)ms[3]));
             bins[bin] = o;
-            if (use_mc) atomicAdd(fallback_count, 1u);
+            if (integral) integral[bin] = (float)mh;
+            if (choice == 1) atomicAdd(counters, 1u);
+            if (choice == 2) atomicAdd(counters + 1, 1u);
             if (isnan(o)) atomicOr(status, VCU_FLAG_NAN);
         }
     }
@@ -598,15 +716,6 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
 /* ------------------------------------------------------------------------------------ host side */
 namespace vcu {
 namespace mlp {
-
-constexpr float kGLx[4][4] = {{0.0f, 0.0f, 0.0f, 0.0f},
-                              {-0.5773502691896258f, 0.5773502691896258f, 0.0f, 0.0f},
-                              {-0.7745966692414834f, 0.0f, 0.7745966692414834f, 0.0f},
-                              {-0.8611363115940526f, -0.3399810435848563f, 0.3399810435848563f, 0.8611363115940526f}};
-constexpr float kGLw[4][4] = {{2.0f, 0.0f, 0.0f, 0.0f},
-                              {1.0f, 1.0f, 0.0f, 0.0f},
-                              {0.5555555555555556f, 0.8888888888888888f, 0.5555555555555556f, 0.0f},
-                              {0.3478548451374538f, 0.6521451548625461f, 0.6521451548625461f, 0.3478548451374538f}};
 
 /* He-uniform initial weights from a SplitMix64 stream, zero biases */
 inline void init_params(int d, uint64_t seed, float* theta) {
@@ -632,12 +741,17 @@ inline void init_params(int d, uint64_t seed, float* theta) {
 struct State {
     float *theta, *m, *v, *grad, *partial;
     char* packed;
-    uint32_t* step;
-    float* integral;
-    uint32_t* fallback;
+    uint32_t* step;     /* [0]: Adam step counter; [1]: the held-out set's fixed counter */
+    uint32_t* counters; /* [0]: plain Monte Carlo bins, [1]: polynomial control-variate bins */
+    double* heldout;    /* per-block partial sums of the held-out squared error */
+    float* nodes;       /* a chunk of bins' grid node values */
 };
 
-template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, uint64_t nparts, State& s) {
+constexpr int HELDOUT_BLOCKS = 64;
+constexpr uint64_t HELDOUT_POINTS = 16384;
+constexpr size_t NODE_CHUNK_BYTES = size_t(1) << 30; /* grid values held at once */
+
+template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nparts, size_t node_floats, State& s) {
     const size_t np = n_params(D), ng = np; /* gradient vector has one entry per parameter */
     size_t o = 0;
     auto a = [&](size_t bytes) {
@@ -646,7 +760,8 @@ template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, uint64_t nparts, 
         return at;
     };
     const size_t o_theta = a(np * 4), o_m = a(np * 4), o_v = a(np * 4), o_g = a(ng * 4), o_p = a(pack_bytes(D)),
-                 o_s = a(64), o_i = a(nbins * 4), o_f = a(64), o_pt = a(nparts * ng * 4);
+                 o_s = a(64), o_c = a(64), o_h = a(HELDOUT_BLOCKS * 8), o_pt = a(nparts * ng * 4),
+                 o_n = a(node_floats * 4);
     int rc = ensure(ctx, ctx->scratch, o);
     if (rc) return rc;
     char* b = static_cast<char*>(ctx->scratch.ptr);
@@ -657,8 +772,9 @@ template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nbins, uint64_t nparts, 
     s.partial = reinterpret_cast<float*>(b + o_pt);
     s.packed = b + o_p;
     s.step = reinterpret_cast<uint32_t*>(b + o_s);
-    s.integral = reinterpret_cast<float*>(b + o_i);
-    s.fallback = reinterpret_cast<uint32_t*>(b + o_f);
+    s.counters = reinterpret_cast<uint32_t*>(b + o_c);
+    s.heldout = reinterpret_cast<double*>(b + o_h);
+    s.nodes = reinterpret_cast<float*>(b + o_n);
     return VCU_OK;
 }
 
@@ -680,7 +796,9 @@ template <int D> int set_smem_train(vcu_ctx* ctx) {
     const int tb = train_smem_bytes<D>();
     if ((size_t)tb > ctx->smem_optin) return fail(ctx, VCU_UNSUPPORTED, "training block does not fit in shared memory");
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_train<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb));
-    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_integral<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_nodes<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       smem_fwd_bytes<D>()));
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_heldout<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        smem_fwd_bytes<D>()));
     return VCU_OK;
 }
@@ -688,19 +806,35 @@ template <int D> int set_smem_train(vcu_ctx* ctx) {
 template <class F, int D>
 int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, const vcu_learned& opt, float* d_bins,
             float* d_integral, vcu_learned_report* report, uint32_t& launches) {
+    /* the interpolation grid */
+    GridCfg gc{};
+    for (int d = 0; d < D; ++d) {
+        gc.r.rmin[d] = p->range_min[d];
+        gc.r.rmax[d] = p->range_max[d];
+        gc.n[d] = d < p->dimbins ? 2 * opt.cells + 1 : 2 * opt.cells_unbinned + 1;
+    }
+    for (int d = 0; d < p->dimbins; ++d) {
+        gc.drange[d] = g.drange[d];
+        gc.res[d] = g.res[d];
+    }
+    gc.dimbins = p->dimbins;
+    gc.nbins = g.nbins;
+    gc.npb = 1;
+    for (int d = 0; d < D; ++d) gc.npb *= gc.n[d];
+    uint64_t chunk = NODE_CHUNK_BYTES / (4ull * (uint64_t)gc.npb);
+    if (chunk > g.nbins) chunk = g.nbins;
+    if (chunk < 1) chunk = 1;
     /* training grid: at most one block per SM, each doing `rounds` rounds of ROUND points */
     const uint64_t want = ((uint64_t)(opt.batch > 0 ? opt.batch : 1) + ROUND - 1) / ROUND;
     const unsigned train_blocks = (unsigned)(want < (uint64_t)ctx->sm_count ? want : (uint64_t)ctx->sm_count);
     State s;
-    int rc = alloc_state<D>(ctx, g.nbins, train_blocks, s);
+    int rc = alloc_state<D>(ctx, train_blocks, chunk * (uint64_t)gc.npb, s);
     if (rc) return rc;
     if ((rc = set_smem_train<D>(ctx))) return rc;
-    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_residual<F, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       smem_fwd_bytes<D>()));
     std::vector<float> theta(n_params(D));
     init_params(D, opt.seed, theta.data());
     if ((rc = upload_params<D>(ctx, s, theta.data(), launches))) return rc;
-    /* 1. training: one graph of (train, adam, step) replayed train_steps times */
+    /* 1. training: one graph of (samples, train, adam, step) replayed; held-out checks between */
     TrainCfg tc{};
     for (int d = 0; d < D; ++d) {
         tc.r.rmin[d] = p->range_min[d];
@@ -711,16 +845,45 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     tc.rounds = (uint32_t)((want + train_blocks - 1) / train_blocks);
     const uint64_t batch = (uint64_t)tc.rounds * train_blocks * ROUND;
     tc.scale = (float)(2.0 / (double)batch);
-    /* the step's training points live in the context's input buffer */
-    if ((rc = ensure(ctx, ctx->in, batch * (D + 1) * 4 + 1024))) return rc;
+    /* the step's training points and the held-out set live in the context's input buffer */
+    const bool early = opt.check_every > 0 && opt.train_steps > 0;
+    const uint64_t hn = early ? HELDOUT_POINTS : 0;
+    if ((rc = ensure(ctx, ctx->in, (batch + hn) * (D + 1) * 4 + 1024))) return rc;
     float* su = static_cast<float*>(ctx->in.ptr);
     float* sy = su + batch * D;
+    float* hu = sy + batch;
+    float* hy = hu + hn * D;
     tc.u_in = su;
     tc.y_in = sy;
     tc.npts = batch;
     AdamCfg ac{opt.learning_rate, 0.9f, 0.999f, 1e-8f, n_params(D), (int)train_blocks};
     cudaEvent_t e0 = ctx->ev_tune[0], e1 = ctx->ev_tune[1];
     VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+    uint32_t steps_run = 0;
+    double heldout_mse = NAN;
+    if (early) {
+        /* the held-out set: its own Philox key and a fixed counter word (step[1] = 0xFFFFFFFF) */
+        TrainCfg hc = tc;
+        hc.k0 ^= 0xA5A5A5A5u;
+        hc.k1 ^= 0x3C3C3C3Cu;
+        VCU_CUDA(ctx, cudaMemsetAsync(s.step + 1, 0xFF, 4, ctx->stream));
+        k_mlp_samples<F, D><<<(unsigned)((hn + 255) / 256), 256, 0, ctx->stream>>>(f, hc, hn, hu, hy, s.step + 1);
+        ++launches;
+        VCU_CUDA(ctx, cudaGetLastError());
+    }
+    auto heldout = [&](double& mse) -> int {
+        k_mlp_heldout<D><<<HELDOUT_BLOCKS, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(s.packed, hu, hy, hn,
+                                                                                               s.heldout);
+        ++launches;
+        VCU_CUDA(ctx, cudaGetLastError());
+        double part[HELDOUT_BLOCKS];
+        VCU_CUDA(ctx, cudaMemcpyAsync(part, s.heldout, sizeof(part), cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        double t = 0.0;
+        for (int b = 0; b < HELDOUT_BLOCKS; ++b) t += part[b]; /* block order: deterministic */
+        mse = t / (double)hn;
+        return VCU_OK;
+    };
     if (opt.train_steps > 0) {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
@@ -738,84 +901,103 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
             cudaGraphDestroy(graph);
             return cuda_fail(ctx, ie, "cudaGraphInstantiate");
         }
-        for (uint32_t i = 0; i < opt.train_steps; ++i) {
-            const cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
-            if (le != cudaSuccess) {
+        double best = INFINITY;
+        int stale = 0;
+        while (steps_run < opt.train_steps) {
+            const uint32_t n = early ? std::min(opt.check_every, opt.train_steps - steps_run) : opt.train_steps;
+            for (uint32_t i = 0; i < n; ++i) {
+                const cudaError_t le = cudaGraphLaunch(exec, ctx->stream);
+                if (le != cudaSuccess) {
+                    cudaGraphExecDestroy(exec);
+                    cudaGraphDestroy(graph);
+                    return cuda_fail(ctx, le, "cudaGraphLaunch");
+                }
+            }
+            steps_run += n;
+            launches += 4 * n;
+            if (!early) break;
+            double mse = 0.0;
+            if ((rc = heldout(mse))) {
                 cudaGraphExecDestroy(exec);
                 cudaGraphDestroy(graph);
-                return cuda_fail(ctx, le, "cudaGraphLaunch");
+                return rc;
+            }
+            heldout_mse = mse;
+            /* stop after two checks in a row without a 0.5 % improvement on the best */
+            if (mse < best * 0.995) {
+                best = mse;
+                stale = 0;
+            } else if (++stale >= 2) {
+                break;
             }
         }
-        launches += 4 * opt.train_steps;
         cudaGraphExecDestroy(exec);
         cudaGraphDestroy(graph);
+    } else if (early) {
+        if ((rc = heldout(heldout_mse))) return rc;
     }
     VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
     float train_ms = 0.0f;
     VCU_CUDA(ctx, cudaEventSynchronize(e1));
     VCU_CUDA(ctx, cudaEventElapsedTime(&train_ms, e0, e1));
-    /* 2. per-bin integral of g */
-    BinCfg bc{};
-    for (int d = 0; d < D; ++d) {
-        bc.r.rmin[d] = p->range_min[d];
-        bc.r.rmax[d] = p->range_max[d];
-    }
-    for (int d = 0; d < p->dimbins; ++d) {
-        bc.drange[d] = g.drange[d];
-        bc.res[d] = g.res[d];
-    }
-    bc.dimbins = p->dimbins;
-    bc.nbins = g.nbins;
-    bc.q = (int)opt.quad_nodes;
-    bc.cells = opt.quad_cells > 1 ? opt.quad_cells : 1;
-    bc.cells_unbinned = opt.quad_cells_unbinned > 0 ? opt.quad_cells_unbinned : bc.cells;
-    for (int i = 0; i < 4; ++i) {
-        bc.gl_x[i] = kGLx[bc.q - 1][i];
-        bc.gl_w[i] = kGLw[bc.q - 1][i];
-    }
+    /* 2.-3. per chunk of bins: the network at the grid nodes, then the residual */
+    CvCfg cc{};
+    cc.gr = gc;
+    cc.spp = opt.samples_per_bin;
+    cc.pilot = learned_pilot(opt.samples_per_bin, opt.pilot);
+    cc.k0 = (uint32_t)opt.seed;
+    cc.k1 = (uint32_t)(opt.seed >> 32);
+    cc.fallback = opt.fallback;
+    cc.factor = g.factor;
+    cc.poly_bins = opt.poly_bins;
+    cc.poly_var = opt.poly_variance;
     int per_sm = 0;
-    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_integral<D>, FWD_WARPS * 32,
+    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_nodes<D>, FWD_WARPS * 32,
                                                                 smem_fwd_bytes<D>()));
-    const uint64_t need = (g.nbins + FWD_WARPS - 1) / FWD_WARPS;
-    const uint64_t cap = (uint64_t)ctx->sm_count * (per_sm > 0 ? per_sm : 1) * 4;
-    const unsigned blocks = (unsigned)(need < cap ? need : cap);
-    float* integral = d_integral ? d_integral : s.integral;
-    VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
-    k_mlp_integral<D><<<blocks, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(bc, s.packed, integral);
-    ++launches;
-    VCU_CUDA(ctx, cudaGetLastError());
-    VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
-    float integral_ms = 0.0f;
-    VCU_CUDA(ctx, cudaEventSynchronize(e1));
-    VCU_CUDA(ctx, cudaEventElapsedTime(&integral_ms, e0, e1));
-    /* 3. residual */
-    ResidualCfg rcfg{};
-    rcfg.b = bc;
-    rcfg.spp = opt.samples_per_bin;
-    rcfg.k0 = (uint32_t)opt.seed;
-    rcfg.k1 = (uint32_t)(opt.seed >> 32);
-    rcfg.fallback = opt.fallback;
-    rcfg.factor = g.factor;
-    VCU_CUDA(ctx, cudaMemsetAsync(s.fallback, 0, 4, ctx->stream));
-    VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
-    k_mlp_residual<F, D><<<blocks, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(f, rcfg, s.packed, integral,
-                                                                                        d_bins, s.fallback,
-                                                                                        ctx->d_status);
-    ++launches;
-    VCU_CUDA(ctx, cudaGetLastError());
-    VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
-    float residual_ms = 0.0f;
-    VCU_CUDA(ctx, cudaEventSynchronize(e1));
-    VCU_CUDA(ctx, cudaEventElapsedTime(&residual_ms, e0, e1));
+    const unsigned node_blocks = (unsigned)ctx->sm_count * (unsigned)(per_sm > 0 ? per_sm : 1);
+    int per_sm_cv = 0;
+    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cv, k_mlp_cv<F, D>, FWD_WARPS * 32, 0));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, ctx->stream));
+    float integral_ms = 0.0f, residual_ms = 0.0f;
+    for (uint64_t b0 = 0; b0 < g.nbins; b0 += chunk) {
+        const uint64_t cnt = std::min(chunk, g.nbins - b0);
+        VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        k_mlp_nodes<D><<<node_blocks, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(gc, s.packed, b0, cnt,
+                                                                                           s.nodes);
+        ++launches;
+        VCU_CUDA(ctx, cudaGetLastError());
+        VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        VCU_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        VCU_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        integral_ms += ms;
+        const uint64_t need = (cnt + FWD_WARPS - 1) / FWD_WARPS;
+        const uint64_t cap = (uint64_t)ctx->sm_count * (per_sm_cv > 0 ? per_sm_cv : 1) * 8;
+        const unsigned blocks = (unsigned)(need < cap ? need : cap);
+        VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        k_mlp_cv<F, D><<<blocks, FWD_WARPS * 32, 0, ctx->stream>>>(f, cc, b0, cnt, s.nodes, d_bins, d_integral,
+                                                                   s.counters, ctx->d_status);
+        ++launches;
+        VCU_CUDA(ctx, cudaGetLastError());
+        VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        VCU_CUDA(ctx, cudaEventSynchronize(e1));
+        VCU_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        residual_ms += ms;
+    }
     if (opt.theta_out)
         VCU_CUDA(ctx, cudaMemcpyAsync(opt.theta_out, s.theta, n_params(D) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    uint32_t cnts[2] = {0, 0};
+    VCU_CUDA(ctx, cudaMemcpyAsync(cnts, s.counters, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (report) {
-        uint32_t fb = 0;
-        VCU_CUDA(ctx, cudaMemcpy(&fb, s.fallback, 4, cudaMemcpyDeviceToHost));
-        report->fallback_bins = fb;
+        report->fallback_bins = cnts[0];
+        report->polynomial_bins = cnts[1];
         report->train_ms = train_ms;
         report->integral_ms = integral_ms;
         report->residual_ms = residual_ms;
+        report->heldout_mse = heldout_mse;
+        report->train_steps_run = steps_run;
+        report->nodes_per_bin = (uint32_t)gc.npb;
     }
     return VCU_OK;
 }
@@ -826,7 +1008,7 @@ int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, 
               uint32_t& launches) {
     const unsigned blocks = (unsigned)((npts + ROUND - 1) / ROUND);
     State s;
-    int rc = alloc_state<D>(ctx, 1, blocks, s);
+    int rc = alloc_state<D>(ctx, blocks, 0, s);
     if (rc) return rc;
     if ((rc = set_smem_train<D>(ctx))) return rc;
     if ((rc = upload_params<D>(ctx, s, theta, launches))) return rc;

@@ -457,15 +457,18 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     if (ch < 0) return fail(ctx, VCU_INVALID_ARG, "unknown integrand kind");
     CallScope scope{ctx, stats};
     if ((rc = scope.begin())) return rc;
-    const size_t bbytes = g.nbins * ch * 4, rbytes = (iterations + 1) * 2 * rdim * 4;
+    const size_t bbytes = g.nbins * ch * 4, rbytes = (iterations + 1) * 2 * rdim * 4, vbytes = g.nbins * 4;
     float *dbins = bins, *dapprox = approximation, *dregions = regions;
     const float* dreplay = replay;
+    vcu_cv cvd = *cv; /* with the variance output moved to device memory */
     if (p->mem == VCU_MEM_HOST) {
-        if ((rc = ensure(ctx, ctx->out, 2 * bbytes + rbytes + 512))) return rc;
+        const size_t bb = (bbytes + 255) & ~size_t(255), rb = (rbytes + 255) & ~size_t(255);
+        if ((rc = ensure(ctx, ctx->out, 2 * bb + rb + vbytes + 512))) return rc;
         char* o = static_cast<char*>(ctx->out.ptr);
         dbins = reinterpret_cast<float*>(o);
-        dapprox = approximation ? reinterpret_cast<float*>(o + ((bbytes + 255) & ~size_t(255))) : nullptr;
-        dregions = regions ? reinterpret_cast<float*>(o + 2 * ((bbytes + 255) & ~size_t(255))) : nullptr;
+        dapprox = approximation ? reinterpret_cast<float*>(o + bb) : nullptr;
+        dregions = regions ? reinterpret_cast<float*>(o + 2 * bb) : nullptr;
+        cvd.variance = cv->variance ? reinterpret_cast<float*>(o + 2 * bb + rb) : nullptr;
         if (replay) {
             const size_t pbytes = g.nbins * cv->samples_per_bin * (size_t)vcu_cv_replay_width(rdim, cv->sampling) * 4;
             if ((rc = ensure(ctx, ctx->in, pbytes))) return rc;
@@ -475,12 +478,12 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
     }
     const int it = (int)iterations;
     if (nested->rule_hi == VCU_RULE_SIMPSON && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
-        rc = fubini ? run_cv_fubini(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches)
-                    : run_cv_st(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+        rc = fubini ? run_cv_fubini(ctx, p, g, *nested, it, cvd, dreplay, dbins, dapprox, dregions, scope.launches)
+                    : run_cv_st(ctx, p, g, *nested, it, cvd, dreplay, dbins, dapprox, dregions, scope.launches);
     else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_SIMPSON)
-        rc = run_cv_bs(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+        rc = run_cv_bs(ctx, p, g, *nested, it, cvd, dreplay, dbins, dapprox, dregions, scope.launches);
     else if (nested->rule_hi == VCU_RULE_BOOLE && nested->rule_lo == VCU_RULE_TRAPEZOIDAL)
-        rc = run_cv_bt(ctx, p, g, *nested, it, *cv, dreplay, dbins, dapprox, dregions, scope.launches);
+        rc = run_cv_bt(ctx, p, g, *nested, it, cvd, dreplay, dbins, dapprox, dregions, scope.launches);
     else
         rc = fail(ctx, VCU_INVALID_ARG, "unsupported nested rule pair");
     if (rc) return rc;
@@ -488,6 +491,8 @@ extern "C" int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vc
         VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
         if (approximation) VCU_CUDA(ctx, cudaMemcpyAsync(approximation, dapprox, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
         if (regions) VCU_CUDA(ctx, cudaMemcpyAsync(regions, dregions, rbytes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (cv->variance)
+            VCU_CUDA(ctx, cudaMemcpyAsync(cv->variance, cvd.variance, vbytes, cudaMemcpyDeviceToHost, ctx->stream));
     }
     const int S = nested->rule_hi;
     double sd = 1.0, sd1 = 1.0;
@@ -599,37 +604,49 @@ extern "C" int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, 
     int rc = make_grid(ctx, p, g);
     if (rc) return rc;
     if (!opt || !bins) return fail(ctx, VCU_INVALID_ARG, "null options or bins");
-    if (opt->quad_nodes < 1 || opt->quad_nodes > 4) return fail(ctx, VCU_INVALID_ARG, "quad_nodes must be 1..4");
-    if (opt->quad_cells < 0 || opt->quad_cells > 256 || opt->quad_cells_unbinned < 0 || opt->quad_cells_unbinned > 256)
-        return fail(ctx, VCU_INVALID_ARG, "quad_cells must be 0..256");
+    if (opt->cells < 0 || opt->cells > 64 || opt->cells_unbinned < 1 || opt->cells_unbinned > 64)
+        return fail(ctx, VCU_INVALID_ARG, "cells must be 0..64 and cells_unbinned 1..64");
     {
         double nodes = 1.0;
-        const int qc = (int)opt->quad_nodes * (opt->quad_cells > 1 ? opt->quad_cells : 1);
-        const int qu = opt->quad_cells_unbinned > 0 ? (int)opt->quad_nodes * opt->quad_cells_unbinned : qc;
-        for (int d = 0; d < p->dim; ++d) nodes *= d < p->dimbins ? qc : qu;
-        if (nodes > 2147483647.0) return fail(ctx, VCU_INVALID_ARG, "too many quadrature nodes per bin");
+        for (int d = 0; d < p->dim; ++d) nodes *= d < p->dimbins ? 2 * opt->cells + 1 : 2 * opt->cells_unbinned + 1;
+        if (nodes > 4913.0) return fail(ctx, VCU_UNSUPPORTED, "at most 4913 interpolation nodes per bin");
     }
     if (opt->samples_per_bin == 0 || opt->samples_per_bin > 0xffffffffull)
         return fail(ctx, VCU_INVALID_ARG, "samples per bin must be 1..2^32-1");
     if (opt->train_steps > 0 && opt->batch == 0) return fail(ctx, VCU_INVALID_ARG, "batch must be positive");
+    if ((opt->poly_bins == nullptr) != (opt->poly_variance == nullptr))
+        return fail(ctx, VCU_INVALID_ARG, "poly_bins and poly_variance go together");
     if (vcu_channels(p->f.kind) != 1) return fail(ctx, VCU_UNSUPPORTED, "learned control variates take scalar integrands");
     CallScope scope{ctx, stats};
     if ((rc = scope.begin())) return rc;
     float *dbins = bins, *dint = network_integral;
-    const size_t bbytes = g.nbins * 4;
+    vcu_learned o = *opt; /* with the polynomial estimates moved to device memory */
+    const size_t bbytes = g.nbins * 4, bb = (bbytes + 255) & ~size_t(255);
     if (p->mem == VCU_MEM_HOST) {
-        if ((rc = ensure(ctx, ctx->out, 2 * bbytes + 512))) return rc;
-        dbins = static_cast<float*>(ctx->out.ptr);
-        dint = network_integral ? reinterpret_cast<float*>(static_cast<char*>(ctx->out.ptr) + ((bbytes + 255) & ~size_t(255)))
-                                : nullptr;
+        if ((rc = ensure(ctx, ctx->out, 4 * bb + 512))) return rc;
+        char* base = static_cast<char*>(ctx->out.ptr);
+        dbins = reinterpret_cast<float*>(base);
+        dint = network_integral ? reinterpret_cast<float*>(base + bb) : nullptr;
+        if (opt->poly_bins) {
+            float* pb = reinterpret_cast<float*>(base + 2 * bb);
+            float* pv = reinterpret_cast<float*>(base + 3 * bb);
+            VCU_CUDA(ctx, cudaMemcpyAsync(pb, opt->poly_bins, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(pv, opt->poly_variance, bbytes, cudaMemcpyHostToDevice, ctx->stream));
+            o.poly_bins = pb;
+            o.poly_variance = pv;
+        }
     }
-    if ((rc = run_learned(ctx, p, g, *opt, dbins, dint, report, scope.launches))) return rc;
+    vcu_learned_report rep{};
+    if ((rc = run_learned(ctx, p, g, o, dbins, dint, &rep, scope.launches))) return rc;
+    if (report) *report = rep;
     if (p->mem == VCU_MEM_HOST) {
         VCU_CUDA(ctx, cudaMemcpyAsync(bins, dbins, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
         if (network_integral)
             VCU_CUDA(ctx, cudaMemcpyAsync(network_integral, dint, bbytes, cudaMemcpyDeviceToHost, ctx->stream));
     }
-    const uint64_t evals = (uint64_t)opt->train_steps * opt->batch + g.nbins * opt->samples_per_bin;
+    /* integrand evaluations: training and held-out samples, then pilot + residual samples per bin */
+    const uint64_t pilot = opt->fallback ? learned_pilot(opt->samples_per_bin, opt->pilot) : 0;
+    const uint64_t evals = (uint64_t)rep.train_steps_run * opt->batch + g.nbins * (opt->samples_per_bin + pilot);
     return scope.end(evals, 0);
 }
 

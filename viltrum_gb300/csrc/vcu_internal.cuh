@@ -282,6 +282,12 @@ int run_eval(vcu_ctx* ctx, const vcu_integrand& f, int dim, const float* d_x, in
              uint32_t& launches);
 int run_learned(vcu_ctx* ctx, const vcu_problem* p, const BinGrid& g, const vcu_learned& opt, float* d_bins,
                 float* d_integral, vcu_learned_report* report, uint32_t& launches);
+/* pilot samples per bin of the learned control variate's per-bin choice */
+inline uint64_t learned_pilot(uint64_t spp, uint32_t pilot) {
+    if (pilot) return pilot;
+    const uint64_t p = spp / 8;
+    return p < 8 ? 8 : (p > 256 ? 256 : p);
+}
 int run_mlp_eval(vcu_ctx* ctx, int dim, const float* theta, const float* u, const float* y, int64_t npts, float* out,
                  float* grad, uint32_t& launches);
 int run_batch_st(vcu_ctx* ctx, int kind, const vcu_nested& n, const vcu_batch_item* items, uint64_t count,
