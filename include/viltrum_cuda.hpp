@@ -45,11 +45,14 @@
 namespace viltrum {
 namespace cuda {
 
+#ifndef VILTRUM_CUDA_ERROR_DEFINED
+#define VILTRUM_CUDA_ERROR_DEFINED
 class error : public std::runtime_error {
 public:
     int code;
     error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
+#endif
 
 /* RAII owner of a vcu_ctx */
 class context {

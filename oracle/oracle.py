@@ -87,7 +87,7 @@ def build(force: bool = False) -> str:
     """Compile liboracle.so from oracle.cc with the flags of oracle/Makefile."""
     src = os.path.join(HERE, "oracle.cc")
     if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(
-            os.path.getmtime(os.path.join(HERE, f)) for f in ("oracle.cc", "oracle.h", "vrgb.h")):
+            os.path.getmtime(os.path.join(HERE, f)) for f in ("oracle.cc", "oracle_impl.h", "oracle.h", "vrgb.h")):
         cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
                "-o", PORT_SO, src, "-lpthread"]
         subprocess.check_call(cmd)

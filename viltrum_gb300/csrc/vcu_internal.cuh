@@ -135,10 +135,54 @@ struct BinGrid {
     float factor; /* prod(res) as float (exact below 2^24) */
 };
 
-int make_grid(vcu_ctx* ctx, const vcu_problem* p, BinGrid& g);
+/* the bin grid of a problem, with viltrum's float arithmetic for the bin widths */
+inline int make_grid(vcu_ctx* ctx, const vcu_problem* p, BinGrid& g) {
+    if (!p) return fail(ctx, VCU_INVALID_ARG, "null problem");
+    if (p->dim < 1 || p->dim > VCU_MAX_DIM) return fail(ctx, VCU_INVALID_ARG, "dim must be 1..6");
+    if (p->dimbins < 1 || p->dimbins > VCU_MAX_DIMBINS || p->dimbins > p->dim)
+        return fail(ctx, VCU_INVALID_ARG, "dimbins must be 1..min(dim,4)");
+    if (p->mem != VCU_MEM_HOST && p->mem != VCU_MEM_DEVICE) return fail(ctx, VCU_INVALID_ARG, "mem must be host or device");
+    std::memset(&g, 0, sizeof(g));
+    g.dim = p->dim;
+    g.dimbins = p->dimbins;
+    for (int d = 0; d < p->dim; ++d) {
+        if (!std::isfinite(p->range_min[d]) || !std::isfinite(p->range_max[d]))
+            return fail(ctx, VCU_INVALID_ARG, "range bounds must be finite");
+        g.rmin[d] = p->range_min[d];
+        g.rmax[d] = p->range_max[d];
+    }
+    uint64_t nb = 1;
+    double prod = 1.0;
+    for (int d = 0; d < p->dimbins; ++d) {
+        const uint64_t r = p->resolution[d];
+        if (r == 0 || r > 0xffffffffull) return fail(ctx, VCU_INVALID_ARG, "resolution must be 1..2^32-1");
+        if (nb > (1ull << 40) / r) return fail(ctx, VCU_INVALID_ARG, "too many bins");
+        nb *= r;
+        prod *= (double)r;
+        g.res[d] = (uint32_t)r;
+        /* (range.max(i) - range.min(i)) / Float(res[i]) in float (integrator-per-bin-parallel.h:22) */
+        volatile float w = p->range_max[d] - p->range_min[d];
+        g.drange[d] = w / (float)r;
+    }
+    g.nbins = nb;
+    g.factor = (float)prod;
+    return VCU_OK;
+}
 /* VCU_INVALID_ARG unless heuristic, metric and rule pair are ones the per-bin nested kernels
  * instantiate (boole/simpson, boole/trapezoidal, simpson/trapezoidal) */
-int check_per_bin_nested(vcu_ctx* ctx, const vcu_nested& n);
+inline int check_per_bin_nested(vcu_ctx* ctx, const vcu_nested& n) {
+    if (n.heuristic != VCU_HEUR_DEFAULT && n.heuristic != VCU_HEUR_SIZE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error heuristic");
+    if (n.metric != VCU_METRIC_ABSOLUTE && n.metric != VCU_METRIC_RELATIVE)
+        return fail(ctx, VCU_INVALID_ARG, "unknown error metric");
+    const bool pair = (n.rule_hi == VCU_RULE_BOOLE && n.rule_lo == VCU_RULE_SIMPSON) ||
+                      (n.rule_hi == VCU_RULE_BOOLE && n.rule_lo == VCU_RULE_TRAPEZOIDAL) ||
+                      (n.rule_hi == VCU_RULE_SIMPSON && n.rule_lo == VCU_RULE_TRAPEZOIDAL);
+    if (!pair)
+        return fail(ctx, VCU_INVALID_ARG,
+                    "unsupported nested rule pair (boole/simpson, boole/trapezoidal, simpson/trapezoidal)");
+    return VCU_OK;
+}
 
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the multiply-xor bijection
  * with the published multipliers and Weyl key increments. */
