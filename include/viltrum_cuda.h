@@ -219,6 +219,39 @@ int vcu_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_nested* n
                          uint64_t iterations, const vcu_cv* cv, const float* replay, float* bins,
                          float* approximation, float* regions, vcu_stats* stats);
 
+/* ------------------------------------------------------------------ Fubini over per-bin integrators
+ * Replaces integrate(integrator_fubini<2>(first, monte_carlo(tail_samples, tail_seed)), bins, f, range)
+ * and integrator_fubini({d0, d1}, first, rest) (src/combination/fubini.h:75-125) for a per-bin
+ * first integrator: first = integrator_per_bin_parallel(monte_carlo(samples_per_bin, seed))
+ * (method VCU_FUBINI_MONTE_CARLO) or integrator_per_bin_parallel(integrator_adaptive_iterations(
+ * nested, iterations)) (VCU_FUBINI_NESTED: nested(simpson, trapezoidal) or nested(boole, simpson)).
+ * The first integrator works over the first 2 dimensions (the bins take at most those), and every
+ * evaluation at x integrates the remaining ones by Monte Carlo:  sum_k f(x, u_k) volume(rest) / K
+ * accumulated in float (fubini.h:51-63, monte-carlo.h:41-63), with u_k from Philox keyed by
+ * tail_seed and the bits of x (the reference draws them from one sequential std::mt19937, so the
+ * agreement is statistical).  With n_order > 0 the problem is first reordered as integrator_reorder
+ * does (src/combination/reorder.h:15-58): the integrator sees f(reorder(x)) over reorder(range),
+ * where reorder puts coordinate `from` at place `to` for each (to, from) pair of `order` and the
+ * others, in order, into the free places -- integrator_fubini({d0, d1}, ...) is the pairs (0, d0),
+ * (1, d1).  Integrands of 3 or more dimensions (or of unbounded dimension, without reordering).
+ * Bins are ASSIGNED. */
+enum { VCU_FUBINI_MONTE_CARLO = 0, VCU_FUBINI_NESTED = 1 };
+
+typedef struct vcu_fubini {
+    int32_t dims;             /* dimensions integrated by the per-bin integrator: 2              */
+    uint32_t tail_samples;    /* Monte Carlo samples of the remaining dimensions per evaluation  */
+    uint64_t tail_seed;
+    int32_t method;           /* VCU_FUBINI_MONTE_CARLO or VCU_FUBINI_NESTED                     */
+    int32_t n_order;          /* (to, from) pairs in order[] (0: no reordering)                  */
+    int32_t order[2 * VCU_MAX_DIM];
+    uint64_t samples_per_bin; /* VCU_FUBINI_MONTE_CARLO                                          */
+    uint64_t seed;
+    vcu_nested nested;        /* VCU_FUBINI_NESTED                                               */
+    uint64_t iterations;
+} vcu_fubini;
+
+int vcu_per_bin_fubini(vcu_ctx* ctx, const vcu_problem* p, const vcu_fubini* fubini, float* bins, vcu_stats* stats);
+
 /* ------------------------------------------------------------------ learned control variate
  * No reference counterpart: per-bin integration (the integrator_per_bin_parallel contract,
  * src/integrator-per-bin-parallel.h:17-35, values ASSIGNED) with a small MLP control variate --

@@ -287,6 +287,25 @@ class Oracle:
         self._check(rc, "crespo2021_infinite")
         return out.reshape(nb, ch)
 
+    def per_bin_fubini(self, params, rmin, rmax, res, method, spp, iterations, mc_samples, seed, swap_xt=False):
+        """integrator_fubini<2>(integrator_per_bin_parallel(first), monte_carlo(mc_samples, seed + 1)) over the
+        moving-disk scene, first = monte_carlo(spp, seed) (method 0) or adaptive nested(simpson,
+        trapezoidal) with `iterations` splits (method 1); swap_xt: integrator_fubini({0, 2}, ...), bins
+        over dimensions 0 and 2 (the unmodified reference only)."""
+        params = np.ascontiguousarray(params, np.float32)
+        rmin = np.ascontiguousarray(rmin, np.float32)
+        rmax = np.ascontiguousarray(rmax, np.float32)
+        res = np.ascontiguousarray(res, np.uint64)
+        out = np.zeros(int(np.prod(res)) * 3, dtype=np.float32)
+        f = getattr(self.lib, self.prefix + "per_bin_fubini")
+        f.restype = ctypes.c_int
+        f.argtypes = [_f32p, ctypes.c_int32, _f32p, _f32p, _u64p, ctypes.c_int32, ctypes.c_uint64, ctypes.c_uint64,
+                      ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, _f32p]
+        rc = f(_ptr(params), params.size, _ptr(rmin), _ptr(rmax), _ptr(res, _u64p), method, spp, iterations,
+               mc_samples, seed, 1 if swap_xt else 0, _ptr(out))
+        self._check(rc, "per_bin_fubini")
+        return out.reshape(-1, 3)
+
     def control_variates(self, kind, params, rmin, rmax, res, nested: Nested, iterations, spp, seed,
                          weight=CV_OPTIMIZE, alpha=1.0, regions=False, replay=False, approx=False, rr=RR_UNIFORM,
                          sampling=RS_UNIFORM, rr_factor=0.01, mis_power=1.0, mis_cutoff=0.0):

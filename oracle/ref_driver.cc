@@ -447,6 +447,47 @@ extern "C" int ref_crespo2021_infinite(int32_t kind, const float* params, int32_
     return 0;
 }
 
+/* integrator_fubini<2>(integrator_per_bin_parallel(first), monte_carlo(mc_samples, seed + 1)) over the
+ * moving-disk scene (RGB), first = monte_carlo(spp, seed) (method 0) or
+ * integrator_adaptive_iterations(nested(simpson, trapezoidal), iterations) (method 1); with
+ * swap_xt the problem is reordered first, integrator_fubini({0, 2}, ...) (fubini.h:111-115): the
+ * bins span dimensions 0 and 2 and dimension 1 is the Monte Carlo tail */
+extern "C" int ref_per_bin_fubini(const float* params, int32_t n_params, const float* rmin, const float* rmax,
+                                  const uint64_t* res, int32_t method, uint64_t spp, uint64_t iterations,
+                                  uint64_t mc_samples, uint64_t seed, int32_t swap_xt, float* out) {
+    auto* fn = new vcu::MovingScene3;
+    if (fn->build(params, n_params)) {
+        delete fn;
+        return 3;
+    }
+    using namespace viltrum;
+    RefF<vcu::MovingScene3, 3, vrgb> f{fn, nullptr};
+    auto range = mk_range<3>(rmin, rmax);
+    BinStore<2, vrgb> bs{mk_res<2>(res), {}};
+    std::size_t nb = 1;
+    for (auto r : bs.res) nb *= r;
+    bs.v.assign(nb, vrgb(0.0));
+    auto bins = [&bs](const std::array<std::size_t, 2>& q) -> vrgb& { return bs.v[bs.lin(q)]; };
+    auto rest = monte_carlo((unsigned long)mc_samples, (std::size_t)(seed + 1));
+    auto go = [&](const auto& first) {
+        /* integrator_fubini's return type takes the argument types as deduced: pass rvalues */
+        auto a = first;
+        auto b = rest;
+        if (swap_xt)
+            integrate(integrator_fubini(std::tuple<std::size_t, std::size_t>{0, 2}, std::move(a), std::move(b)), bins,
+                      bs.res, f, range);
+        else
+            integrate(integrator_fubini<2>(std::move(a), std::move(b)), bins, bs.res, f, range);
+    };
+    if (method == 0)
+        go(integrator_per_bin_parallel(monte_carlo((unsigned long)spp, (std::size_t)seed)));
+    else
+        go(integrator_per_bin_parallel(integrator_adaptive_iterations(nested(simpson, trapezoidal), (std::size_t)iterations)));
+    for (std::size_t i = 0; i < nb; ++i) VT<vrgb>::to(bs.v[i], out + i * 3);
+    delete fn;
+    return 0;
+}
+
 /* single-value integrate(I, f, range) of the half-space family: the items of a batch of
  * independent integrals (monte_carlo(budget, seed), or adaptive nested(simpson, trapezoidal) with
  * budget regions and the default heuristic / absolute metric) */

@@ -214,6 +214,32 @@ def run_fubini(ref: orc.Oracle, kw: dict) -> np.ndarray:
                      for seed in kw["seeds"]])
 
 
+# integrator_fubini<2> over a per-bin integrator with a Monte Carlo tail, without and with the
+# reorder of integrator_fubini({0, 2}, ...): the reference's bins for several seeds (statistical:
+# the tail draws from one sequential std::mt19937 stream)
+PER_BIN_FUBINI_CASES = [
+    ("fubini_perbin_nested_moving3_bins16x16_it15_mc8", dict(params=scenes.moving_scene3(seed=7, n_gauss=16, n_disk=16),
+                                                             rmin=[0, 0, 0], rmax=[1, 1, 1], res=[16, 16], method=1,
+                                                             spp=0, iterations=15, mc_samples=8, swap_xt=False,
+                                                             seeds=list(range(1, 9)))),
+    ("fubini_perbin_nested_moving3_xt_bins16x16_it15_mc8", dict(params=scenes.moving_scene3(seed=7, n_gauss=16,
+                                                                                              n_disk=16),
+                                                                rmin=[0, 0, 0], rmax=[1, 1, 1], res=[16, 16], method=1,
+                                                                spp=0, iterations=15, mc_samples=8, swap_xt=True,
+                                                                seeds=list(range(1, 9)))),
+    ("fubini_perbin_mc_moving3_xt_bins16x16_spp16_mc4", dict(params=scenes.moving_scene3(seed=7, n_gauss=16, n_disk=16),
+                                                             rmin=[0, 0, 0], rmax=[1, 1, 1], res=[16, 16], method=0,
+                                                             spp=16, iterations=0, mc_samples=4, swap_xt=True,
+                                                             seeds=list(range(1, 9)))),
+]
+
+
+def run_per_bin_fubini(ref: orc.Oracle, kw: dict) -> np.ndarray:
+    return np.stack([ref.per_bin_fubini(kw["params"], kw["rmin"], kw["rmax"], kw["res"], kw["method"], kw["spp"],
+                                        kw["iterations"], kw["mc_samples"], seed, kw["swap_xt"])
+                     for seed in kw["seeds"]])
+
+
 BATCH_CASES = [
     ("batch_halfspace_n64_seed5", dict(n=64, seed=5, budget_lo=1, budget_hi=400)),
 ]
@@ -404,6 +430,14 @@ def main() -> int:
         out = run_fubini(ref, kw)
         meta = {k: np.asarray(v) for k, v in kw.items() if k != "params"}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), method="fubini", kind=scenes.MOVING_SCENE3,
+                            params=np.asarray(kw["params"], np.float32), **meta, out_bins=out)
+        print(f"ok {name} (reference outputs, compared statistically)")
+    for name, kw in PER_BIN_FUBINI_CASES:
+        if not wanted(name):
+            continue
+        out = run_per_bin_fubini(ref, kw)
+        meta = {("first" if k == "method" else k): np.asarray(v) for k, v in kw.items() if k != "params"}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), method="per_bin_fubini", kind=scenes.MOVING_SCENE3,
                             params=np.asarray(kw["params"], np.float32), **meta, out_bins=out)
         print(f"ok {name} (reference outputs, compared statistically)")
     for name, kw in WALK_CASES:

@@ -81,7 +81,7 @@ def test_ctypes_structs_match_the_header(tmp_path):
     host compiler prints them from include/viltrum_cuda.h)."""
     from viltrum_gb300 import _lib
     pairs = {"vcu_integrand": _lib.Integrand, "vcu_problem": _lib.Problem, "vcu_nested": _lib.Nested, "vcu_stats": _lib.Stats, "vcu_cv": _lib.CvOpts,
-             "vcu_learned": _lib.LearnedOpts, "vcu_learned_report": _lib.LearnedReport, "vcu_opts": _lib.Opts,
+             "vcu_learned": _lib.LearnedOpts, "vcu_fubini": _lib.FubiniOpts, "vcu_learned_report": _lib.LearnedReport, "vcu_opts": _lib.Opts,
              "vcu_batch_item": _lib.BatchItem, "vcu_batch_report": _lib.BatchReport}
     lines = ['#include <cstdio>', '#include <cstddef>', '#include "viltrum_cuda.h"', "int main() {"]
     for cname, cls in pairs.items():

@@ -26,7 +26,7 @@ EXPORTS = ["vcu_abi_version", "vcu_create", "vcu_destroy", "vcu_last_error", "vc
            "vcu_per_bin_adaptive_nested",
            "vcu_control_variates", "vcu_learned_control_variates", "vcu_mlp_eval", "vcu_integrate_batch",
            "vcu_integrate_batch_resident", "vcu_adaptive_iterations_global", "vcu_adaptive_tolerance",
-           "vcu_cv_replay_width", "vcu_set_device_memory_limit", "vcu_device_memory_held"]
+           "vcu_cv_replay_width", "vcu_set_device_memory_limit", "vcu_device_memory_held", "vcu_per_bin_fubini"]
 BATCH_MONTE_CARLO, BATCH_NESTED = 0, 1
 CV_OPTIMIZE, CV_FIXED = 0, 1
 RR_UNIFORM, RR_INTEGRAL, RR_ERROR, RR_PDF = 0, 1, 2, 3  # residual region choice
@@ -75,6 +75,36 @@ class CvOpts(ctypes.Structure):
                 ("sampling", ctypes.c_int32), ("rr_factor", ctypes.c_float), ("reserved2", ctypes.c_int32),
                 ("mis_power", ctypes.c_double), ("mis_cutoff", ctypes.c_double), ("fubini_dims", ctypes.c_int32),
                 ("tail_samples", ctypes.c_uint32), ("variance", ctypes.c_void_p)]
+
+
+FUBINI_MONTE_CARLO, FUBINI_NESTED = 0, 1
+
+
+class FubiniOpts(ctypes.Structure):
+    """vcu_fubini"""
+    _fields_ = [("dims", ctypes.c_int32), ("tail_samples", ctypes.c_uint32), ("tail_seed", ctypes.c_uint64),
+                ("method", ctypes.c_int32), ("n_order", ctypes.c_int32), ("order", ctypes.c_int32 * (2 * VCU_MAX_DIM)),
+                ("samples_per_bin", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("nested", Nested),
+                ("iterations", ctypes.c_uint64)]
+
+    @classmethod
+    def make(cls, tail_samples, tail_seed, method, samples_per_bin=0, seed=0, nested=None, iterations=0, order=()):
+        """order: (to, from) pairs of integrator_reorder; integrator_fubini({d0, d1}, ...) is ((0, d0), (1, d1))"""
+        o = cls()
+        o.dims = 2
+        o.tail_samples = tail_samples
+        o.tail_seed = tail_seed
+        o.method = method
+        o.samples_per_bin = samples_per_bin
+        o.seed = seed
+        if nested is not None:
+            o.nested = nested
+        o.iterations = iterations
+        o.n_order = len(order)
+        for k, (to, frm) in enumerate(order):
+            o.order[2 * k] = to
+            o.order[2 * k + 1] = frm
+        return o
 
 
 class LearnedOpts(ctypes.Structure):
@@ -135,6 +165,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         L.vcu_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
         L.vcu_channels.argtypes = [ctypes.c_int32]
         L.vcu_set_device_memory_limit.argtypes = [vp, ctypes.c_uint64]
+        L.vcu_per_bin_fubini.argtypes = [vp, ctypes.POINTER(Problem), ctypes.POINTER(FubiniOpts), vp,
+                                         ctypes.POINTER(Stats)]
         L.vcu_device_memory_held.argtypes = [vp]
         L.vcu_device_memory_held.restype = ctypes.c_uint64
         L.vcu_eval.argtypes = [vp, ctypes.POINTER(Integrand), ctypes.c_int32, vp, ctypes.c_int64, vp, ctypes.c_int32]
@@ -273,6 +305,13 @@ class Context:
         st = Stats()
         self.check(self.lib.vcu_per_bin_monte_carlo_accumulate(self.handle, ctypes.byref(p), spp, seed, _ptr(points),
                                                                _ptr(bins), ctypes.byref(st)))
+        return st
+
+    def per_bin_fubini(self, p: Problem, opts: "FubiniOpts", bins) -> Stats:
+        """integrator_fubini<2>(per-bin integrator, monte_carlo(K)) with an optional reorder; assigns"""
+        st = Stats()
+        self.check(self.lib.vcu_per_bin_fubini(self.handle, ctypes.byref(p), ctypes.byref(opts), _ptr(bins),
+                                               ctypes.byref(st)))
         return st
 
     def per_bin_adaptive_nested(self, p: Problem, nested: Nested, iterations: int, bins, trace=None) -> Stats:
