@@ -303,8 +303,9 @@ int vcu_learned_control_variates(vcu_ctx* ctx, const vcu_problem* p, const vcu_l
 
 /* The network alone, for checking the kernels: outputs g(u) at npts points u in [0,1]^dim (host
  * arrays, row-major) for the fp32 parameter vector theta (layout: W0[FIN][64], b0, W1[64][64], b1,
- * W2, b2, W3, b3, w4[64], b4 with FIN = 16*ceil(13*dim/16)); if y and grad are given, grad receives
- * the gradient of mean((g - y)^2) computed by the training kernel.  dim 2, 3 or 5. */
+ * W2, b2, W3, b3, w4[64], b4 with FIN = 16*ceil(13*dim/16)).  Without grad the outputs come from the
+ * tcgen05 forward kernel the learned control variate evaluates its grid with; with y and grad
+ * given, outputs and the gradient of mean((g - y)^2) come from the training kernel.  dim 2, 3 or 5. */
 int vcu_mlp_eval(vcu_ctx* ctx, int32_t dim, const float* theta, const float* u, const float* y, int64_t npts,
                  float* out, float* grad);
 

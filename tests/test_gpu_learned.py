@@ -37,6 +37,24 @@ def test_forward_backward_against_fp64_reference(ctx, dim):
         assert np.linalg.norm(gb - rb) <= 3e-2 * np.linalg.norm(rb) + 1e-7
 
 
+@pytest.mark.parametrize("dim", [2, 3, 5])
+def test_tensor_core_forward_against_fp64_reference(ctx, dim):
+    """The forward-only path (tcgen05.mma into TMEM, k_mlp_tc.cuh) -- what the learned control variate
+    evaluates its grid nodes with -- against the FP64 reference and against the training kernel's
+    own forward outputs (mma.sync), on a point count that leaves a partial 128-point tile."""
+    rng = np.random.default_rng(100 + dim)
+    theta = (mlp_ref.init(dim, seed=20 + dim) + rng.normal(0, 0.05, mlp_ref.n_params(dim))).astype(np.float32)
+    n = 3000
+    u = rng.random((n, dim)).astype(np.float32)
+    out, _ = ctx.mlp_eval(dim, theta, u)
+    ref_out, _ = mlp_ref.forward_backward(theta, u.astype(np.float64), np.zeros(n))
+    assert np.isfinite(out).all()
+    rel = np.linalg.norm(out - ref_out) / np.linalg.norm(ref_out)
+    assert rel < 2e-3, rel
+    train_out, _ = ctx.mlp_eval(dim, theta, u, np.zeros(n, np.float32), grad=True)
+    assert np.linalg.norm(out - train_out) / np.linalg.norm(train_out) < 2e-3
+
+
 def _learned(ctx, kind, params, rmin, rmax, res, spp, seed, steps, fallback=0, lr=2e-3, batch=32768, cells=0,
              cells_unbinned=2, check_every=0, poly=None, pilot=0):
     p = ctx.problem(kind, params, rmin, rmax, res)
@@ -109,7 +127,7 @@ def test_interpolant_integral_is_the_simpson_sum_of_the_network(ctx):
         ys = (np.float32(iy) * np.float32(1 / 3) + np.float32(1 / 3) * np.arange(n, dtype=np.float32) / np.float32(4))
         X, Y = np.meshgrid(xs, ys, indexing="xy")
         u = np.stack([X.ravel(), Y.ravel()], 1).astype(np.float32)
-        g = ctx.mlp_eval(2, theta, u).reshape(n, n).astype(np.float64)
+        g = ctx.mlp_eval(2, theta, u)[0].reshape(n, n).astype(np.float64)
         host = float(w @ g @ w)
         assert abs(host - integ[b]) <= 1e-5 * max(1.0, abs(host)), (b, host, integ[b])
 

@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "k_mlp.cuh"
+#include "k_mlp_tc.cuh"
 
 namespace vcu {
 namespace mlp {
@@ -520,6 +521,42 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
     }
 }
 
+/* the same on the 5th-generation tensor cores (k_mlp_tc.cuh): one warpgroup per CTA, 128 nodes per
+ * tile, persistent over the chunk's nodes */
+template <int D>
+__global__ void __launch_bounds__(tc::THREADS)
+    k_mlp_nodes_tc(const GridCfg c, const char* __restrict__ packed, uint64_t bin0, uint64_t count,
+                   float* __restrict__ out, uint32_t* __restrict__ status) {
+    auto point = [&](uint64_t i, float* u) -> bool {
+        const uint64_t lb = i / (uint64_t)c.npb;
+        int r = (int)(i % (uint64_t)c.npb);
+        float lo[D], hi[D];
+        grid_box<D>(c, bin0 + lb, lo, hi);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int j = r % c.n[d];
+            r /= c.n[d];
+            const float tt = c.n[d] == 1 ? 0.5f : (float)j / (float)(c.n[d] - 1);
+            u[d] = (lo[d] + (hi[d] - lo[d]) * tt - c.r.rmin[d]) / (c.r.rmax[d] - c.r.rmin[d]);
+        }
+        return true;
+    };
+    tc::forward_points<D>(packed, count * (uint64_t)c.npb, point, out, status);
+}
+
+/* the network at explicit points u[n][D] (vcu_mlp_eval without a gradient), tensor cores */
+template <int D>
+__global__ void __launch_bounds__(tc::THREADS)
+    k_mlp_forward_tc(const char* __restrict__ packed, const float* __restrict__ u_in, uint64_t n,
+                     float* __restrict__ out, uint32_t* __restrict__ status) {
+    auto point = [&](uint64_t i, float* u) -> bool {
+#pragma unroll
+        for (int d = 0; d < D; ++d) u[d] = u_in[i * D + d];
+        return true;
+    };
+    tc::forward_points<D>(packed, n, point, out, status);
+}
+
 /* ---------------------------------------------------------------- residual */
 struct CvCfg {
     GridCfg gr;
@@ -800,6 +837,10 @@ template <int D> int set_smem_train(vcu_ctx* ctx) {
                                        smem_fwd_bytes<D>()));
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_heldout<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        smem_fwd_bytes<D>()));
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_nodes_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tc::Smem<D>::BYTES));
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_forward_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tc::Smem<D>::BYTES));
     return VCU_OK;
 }
 
@@ -952,8 +993,8 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     cc.poly_bins = opt.poly_bins;
     cc.poly_var = opt.poly_variance;
     int per_sm = 0;
-    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_nodes<D>, FWD_WARPS * 32,
-                                                                smem_fwd_bytes<D>()));
+    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_nodes_tc<D>, tc::THREADS,
+                                                                tc::Smem<D>::BYTES));
     const unsigned node_blocks = (unsigned)ctx->sm_count * (unsigned)(per_sm > 0 ? per_sm : 1);
     int per_sm_cv = 0;
     VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cv, k_mlp_cv<F, D>, FWD_WARPS * 32, 0));
@@ -962,8 +1003,8 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     for (uint64_t b0 = 0; b0 < g.nbins; b0 += chunk) {
         const uint64_t cnt = std::min(chunk, g.nbins - b0);
         VCU_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
-        k_mlp_nodes<D><<<node_blocks, FWD_WARPS * 32, smem_fwd_bytes<D>(), ctx->stream>>>(gc, s.packed, b0, cnt,
-                                                                                           s.nodes);
+        k_mlp_nodes_tc<D><<<node_blocks, tc::THREADS, tc::Smem<D>::BYTES, ctx->stream>>>(gc, s.packed, b0, cnt,
+                                                                                          s.nodes, ctx->d_status);
         ++launches;
         VCU_CUDA(ctx, cudaGetLastError());
         VCU_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
@@ -1020,6 +1061,19 @@ int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, 
     VCU_CUDA(ctx, cudaMemcpyAsync(du, u, (size_t)npts * D * 4, cudaMemcpyHostToDevice, ctx->stream));
     if (y) VCU_CUDA(ctx, cudaMemcpyAsync(dy, y, (size_t)npts * 4, cudaMemcpyHostToDevice, ctx->stream));
     else VCU_CUDA(ctx, cudaMemsetAsync(dy, 0, (size_t)npts * 4, ctx->stream));
+    if (!grad) {
+        int per_sm = 0;
+        VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_forward_tc<D>, tc::THREADS,
+                                                                    tc::Smem<D>::BYTES));
+        const uint64_t tiles = ((uint64_t)npts + tc::TILE - 1) / tc::TILE;
+        const uint64_t cap = (uint64_t)ctx->sm_count * (uint64_t)(per_sm > 0 ? per_sm : 1);
+        k_mlp_forward_tc<D><<<(unsigned)(tiles < cap ? tiles : cap), tc::THREADS, tc::Smem<D>::BYTES, ctx->stream>>>(
+            s.packed, du, (uint64_t)npts, dout, ctx->d_status);
+        ++launches;
+        VCU_CUDA(ctx, cudaGetLastError());
+        VCU_CUDA(ctx, cudaMemcpyAsync(out, dout, (size_t)npts * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        return VCU_OK;
+    }
     TrainCfg tc{};
     tc.rounds = 1;
     tc.u_in = du;
