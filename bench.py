@@ -518,7 +518,8 @@ def time_to_rmse(ctx, target: float = 1e-3, res_side: int = 1024, seeds=(1, 2, 3
             b = np.empty(W * W, np.float32)
             ctx.per_bin_monte_carlo(sub, 1 << 20, 9000 + k, b)
             reps.append(b.astype(np.float64))
-        reps = np.array(reps)
+        # a window's bins are normalised by its own prod(res) = W^2: rescale to the image's R^2
+        reps = np.array(reps) * (R * R) / (W * W)
         truth.append(reps.mean(axis=0))
         se2.append(reps.var(axis=0, ddof=1) / 2)
         jj, ii = np.meshgrid(np.arange(W), np.arange(W), indexing="ij")
@@ -737,13 +738,10 @@ def profile_workload(args) -> dict:
         os.environ.setdefault("VCU_BATCH_THREADS", "512")
         call = lambda: ctx.integrate_batch(scenes.HALFSPACE, items, nst)[1]
     elif w == "learned":
-        p = ctx.problem(scenes.WAVE2, None, [0, 0], [1, 1], [r, r])
+        # the 5-D occluded scene with the options of the time-to-RMSE sweep (fewer training steps)
+        p = ctx.problem(scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), [0] * 5, [1] * 5, [r, r])
         b = np.empty(r * r, np.float32)
-        if args.res > 256:  # the 5-D occluded scene: the configuration the time-to-RMSE sweep runs
-            p = ctx.problem(scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), [0] * 5, [1] * 5, [r, r])
-            opts = _lib.LearnedOpts(64, 5, 200, 32768, 3e-3, 0, 1, 0, None, 6)
-        else:
-            opts = _lib.LearnedOpts(32, 5, 20, 32768, 3e-3, 0, 1, 2, None, 1)
+        opts = _lib.LearnedOpts(256, 5, 200, 32768, 3e-3, 0, 1, 0, None, 6)
         call = lambda: ctx.learned_control_variates(p, opts, b)[0]
     else:  # nested
         p = ctx.problem(scenes.SCENE2, scenes.scene2(SEED), [0, 0], [1, 1], [r, r])

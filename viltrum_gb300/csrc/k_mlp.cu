@@ -680,30 +680,46 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
         for (int o = 16; o > 0; o >>= 1) mh += __shfl_xor_sync(0xffffffffu, mh, o);
         const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
         /* samples of stream `tag`: f and r = f - h, Welford per lane */
-        auto run = [&](uint64_t n, uint32_t tag, float* st) {
-            float nf = 0.0f, mf = 0.0f, m2f = 0.0f, nr = 0.0f, mr = 0.0f, m2r = 0.0f;
-            for (uint64_t s = lane; s < n; s += 32) {
-                float x[F::DIM], t[D];
-                for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+        auto draw = [&](uint64_t s, uint32_t tag, float* x, float* t) {
+            for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
 #pragma unroll
-                for (int blk = 0; blk < (D + 3) / 4; ++blk) {
-                    const U4 rr4 = philox4x32_10(U4{(uint32_t)s, blo, bhi, tag + blk}, c.k0, c.k1);
-                    const uint32_t rr[4] = {rr4.x, rr4.y, rr4.z, rr4.w};
+            for (int blk = 0; blk < (D + 3) / 4; ++blk) {
+                const U4 rr4 = philox4x32_10(U4{(uint32_t)s, blo, bhi, tag + blk}, c.k0, c.k1);
+                const uint32_t rr[4] = {rr4.x, rr4.y, rr4.z, rr4.w};
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int d = blk * 4 + k;
-                        if (d < D) {
-                            const float u = u01(rr[k]);
-                            x[d] = vadd(vmul(u, vsub(hi[d], lo[d])), lo[d]);
-                            t[d] = u;
-                        }
+                for (int k = 0; k < 4; ++k) {
+                    const int d = blk * 4 + k;
+                    if (d < D) {
+                        const float u = u01(rr[k]);
+                        x[d] = vadd(vmul(u, vsub(hi[d], lo[d])), lo[d]);
+                        t[d] = u;
                     }
                 }
-                float fv[1];
-                f(x, fv);
-                const float hv = interpolant<D>(c.gr, nd, t);
-                welford(nf, mf, m2f, fv[0]);
-                welford(nr, mr, m2r, fv[0] - hv);
+            }
+        };
+        auto run = [&](uint64_t n, uint32_t tag, float* st) {
+            float nf = 0.0f, mf = 0.0f, m2f = 0.0f, nr = 0.0f, mr = 0.0f, m2r = 0.0f;
+            /* samples s and s + 32 of this lane as two independent chains (the integrand's pair form
+             * where it has one) */
+            for (uint64_t s = lane; s < n; s += 64) {
+                const bool two = s + 32 < n;
+                float x0[F::DIM], x1[F::DIM], t0[D], t1[D], v0[1], v1[1];
+                draw(s, tag, x0, t0);
+                draw(two ? s + 32 : s, tag, x1, t1);
+                if constexpr (has_pair<F>::value) {
+                    f.pair(x0, x1, v0, v1);
+                } else {
+                    f(x0, v0);
+                    f(x1, v1);
+                }
+                const float h0 = interpolant<D>(c.gr, nd, t0);
+                welford(nf, mf, m2f, v0[0]);
+                welford(nr, mr, m2r, v0[0] - h0);
+                if (two) {
+                    const float h1 = interpolant<D>(c.gr, nd, t1);
+                    welford(nf, mf, m2f, v1[0]);
+                    welford(nr, mr, m2r, v1[0] - h1);
+                }
             }
             warp_merge(nf, mf, m2f);
             warp_merge(nr, mr, m2r);
