@@ -259,18 +259,21 @@ int vcu_per_bin_fubini(vcu_ctx* ctx, const vcu_problem* p, const vcu_fubini* fub
  * accumulation -- trained online (Adam, mean squared error) on `batch` fresh Philox samples of the
  * integrand per step, for at most `train_steps` steps, by the library's own forward/backward
  * kernels; with `check_every` > 0 the mean squared error on a fixed held-out set is measured every
- * `check_every` steps and training stops once it no longer improves by 0.5 %.
+ * `check_every` steps: after two checks without a 0.5 % improvement the learning rate drops to 0.3
+ * of itself, and the third such plateau ends training.
  * The control variate of a bin is h, the piecewise-quadratic interpolant of the trained network g
  * on a grid of Simpson nodes -- `cells` cells per binned dimension inside the bin (0: h is constant
  * there, g's value at the bin centre) and `cells_unbinned` cells per unbinned dimension over the
  * range -- i.e. nested quadrature's own polynomial: the integral of h over the bin is exactly the
  * composite Simpson sum of the node values, so the estimate  integral(h) + mean(f - h)  over
  * `samples_per_bin` Philox points is unbiased.  With `fallback` set, `pilot` separate samples per
- * bin (0: samples/8 clamped to 8..256; not reused in the estimate) decide per bin between the
- * learned estimate and plain Monte Carlo of the same samples (the lower pilot variance), and, when
- * poly_bins/poly_variance are given (vcu_control_variates' bins and vcu_cv::variance for the same
- * problem), the polynomial control variate's estimate replaces the bin's when its variance is the
- * lower one.  At most 4913 grid nodes per bin.  Scalar integrands of dimension 2, 3 or 5. */
+ * bin (0: samples/8 clamped to 8..256; not reused in the estimate) give the bin's weight
+ * alpha = cov(f, h) / var(h), clamped to [0, 1.5], fixed before the residual samples: the estimate
+ * is then  alpha integral(h) + mean(f - alpha h)  (still unbiased; alpha 0 is plain Monte Carlo of
+ * the residual samples), and, when poly_bins/poly_variance are given (vcu_control_variates' bins
+ * and vcu_cv::variance for the same problem), the polynomial control variate's estimate replaces
+ * the bin's when its variance is the lower one.  At most 4913 grid nodes per bin.  Scalar
+ * integrands of dimension 2, 3 or 5. */
 typedef struct vcu_learned {
     uint64_t samples_per_bin;
     uint64_t seed;
@@ -278,7 +281,7 @@ typedef struct vcu_learned {
     uint32_t batch;           /* training samples per step (rounded up to whole blocks)        */
     float learning_rate;
     uint32_t check_every;     /* held-out check period for early stopping (0: all steps)       */
-    int32_t fallback;         /* 1: per-bin choice of the lowest-variance estimator            */
+    int32_t fallback;         /* 1: per-bin weight and choice of estimator from the pilot       */
     int32_t cells;            /* Simpson cells per binned dimension in a bin (0: constant)     */
     float* theta_out;         /* nullable host buffer: receives the trained fp32 parameters
                                  (vcu_mlp_eval layout), e.g. to checkpoint the network        */
@@ -291,7 +294,7 @@ typedef struct vcu_learned {
 typedef struct vcu_learned_report {
     double train_ms, integral_ms, residual_ms;
     double heldout_mse;       /* held-out mean squared error of the network at the end         */
-    uint32_t fallback_bins;   /* bins that took the plain Monte Carlo estimate                 */
+    uint32_t fallback_bins;   /* bins whose weight is 0: the plain Monte Carlo estimate        */
     uint32_t polynomial_bins; /* bins that took the polynomial control variate's estimate      */
     uint32_t train_steps_run; /* Adam steps taken (early stopping)                             */
     uint32_t nodes_per_bin;   /* grid nodes of the interpolant per bin                         */

@@ -132,17 +132,19 @@ def test_interpolant_integral_is_the_simpson_sum_of_the_network(ctx):
         assert abs(host - integ[b]) <= 1e-5 * max(1.0, abs(host)), (b, host, integ[b])
 
 
-def test_learned_estimator_is_unbiased_on_the_occluded_scene(ctx):
+@pytest.mark.parametrize("fallback", [0, 1])
+def test_learned_estimator_is_unbiased_on_the_occluded_scene(ctx, fallback):
     """The interpolant's integral is exact, so the learned estimator is unbiased even where the
-    network fits the integrand poorly (the 5-D occluded scene, whose visibility is discontinuous):
-    over 8 seeds the mean error against a Monte Carlo truth is within 4 standard errors of zero."""
+    network fits the integrand poorly (the 5-D occluded scene, whose visibility is discontinuous),
+    with weight 1 and with the per-bin weight the pilot fixes before the residual samples: over 8
+    seeds the mean error against a Monte Carlo truth is within 4 standard errors of zero."""
     params = scenes.occluded_scene5(7)
     res, spp = [8, 8], 64
     truth, se2 = _mc_truth(ctx, scenes.OCCLUDED_SCENE5, params, 5, res)
     errs = []
     for seed in range(8):
         out, _, st, _ = _learned(ctx, scenes.OCCLUDED_SCENE5, params, [0] * 5, [1] * 5, res, spp, 100 + seed,
-                                 steps=60, cells=0, cells_unbinned=2)
+                                 steps=60, cells=0, cells_unbinned=2, fallback=fallback)
         assert st.flags == 0
         errs.append(out - truth)
     errs = np.array(errs)
@@ -154,8 +156,8 @@ def test_learned_estimator_is_unbiased_on_the_occluded_scene(ctx):
 def test_learned_beats_plain_monte_carlo_on_the_occluded_scene(ctx):
     """At equal residual samples (32x32 bins of the 5-D occluded scene, 256 samples per bin, the
     interpolant on 4 Simpson cells per primary dimension) the learned estimator's bin RMSE against
-    a Monte Carlo truth is below plain Monte Carlo's -- and with the per-bin fallback it is never
-    worse than plain Monte Carlo by more than the pilot's selection noise."""
+    a Monte Carlo truth is below plain Monte Carlo's, and lower still with the per-bin weight the
+    pilot estimates (weight 0 in a bin is plain Monte Carlo)."""
     params = scenes.occluded_scene5(7)
     res, spp = [32, 32], 256
     truth, se2 = _mc_truth(ctx, scenes.OCCLUDED_SCENE5, params, 5, res, spp=1 << 16, reps=4)
@@ -177,7 +179,7 @@ def test_learned_beats_plain_monte_carlo_on_the_occluded_scene(ctx):
         lr_sq.append(rmse(lrn) ** 2)
         fb_sq.append(rmse(fb) ** 2)
     assert np.mean(lr_sq) < 0.9 * np.mean(mc_sq), (lr_sq, mc_sq)
-    assert np.mean(fb_sq) < np.mean(mc_sq), (fb_sq, mc_sq)
+    assert np.mean(fb_sq) < np.mean(lr_sq) * 1.05, (fb_sq, lr_sq)
 
 
 def test_polynomial_fallback_takes_the_better_bins(ctx):

@@ -16,9 +16,10 @@
  *  3. k_mlp_cv: per bin, the interpolant h of those node values (piecewise quadratic, Lagrange on
  *     the three nodes of a cell per dimension; constant in a dimension with one node) is the
  *     control variate: its mean over the bin is the composite Simpson sum of the nodes -- exact, so
- *     integral(h) + mean(f - h) over the residual samples is unbiased.  Optional per-bin choice,
- *     from separate pilot samples, of the lowest-variance of this estimate, plain Monte Carlo and a
- *     given polynomial control variate.
+ *     integral(h) + mean(f - h) over the residual samples is unbiased.  Optionally, separate pilot
+ *     samples per bin give the bin's weight alpha = cov(f, h) / var(h) (estimate alpha integral(h) +
+ *     mean(f - alpha h); alpha 0 is plain Monte Carlo) and choose a given polynomial control
+ *     variate's estimate where its variance is lower.
  */
 #include <algorithm>
 
@@ -390,14 +391,15 @@ __global__ void k_mlp_adam(const AdamCfg c, float* __restrict__ theta, float* __
     const int p = grad_to_param<D>(i);
     float gr = 0.0f;
     for (int b = 0; b < c.nparts; ++b) gr += partial[(size_t)b * c.n + i];
-    const float t = (float)(*step_ctr + 1);
+    const float t = (float)(step_ctr[0] + 1);
+    const float lr = c.lr * __uint_as_float(step_ctr[2]); /* step_ctr[2]: the learning-rate scale */
     const float mi = c.b1 * m[p] + (1.0f - c.b1) * gr;
     const float vi = c.b2 * v[p] + (1.0f - c.b2) * gr * gr;
     m[p] = mi;
     v[p] = vi;
     const float mh = mi / (1.0f - powf(c.b1, t));
     const float vh = vi / (1.0f - powf(c.b2, t));
-    const float w = theta[p] - c.lr * mh / (sqrtf(vh) + c.eps);
+    const float w = theta[p] - lr * mh / (sqrtf(vh) + c.eps);
     theta[p] = w;
     pack_param<D>(packed, p, w);
 }
@@ -697,10 +699,26 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
                 }
             }
         };
-        auto run = [&](uint64_t n, uint32_t tag, float* st) {
-            float nf = 0.0f, mf = 0.0f, m2f = 0.0f, nr = 0.0f, mr = 0.0f, m2r = 0.0f;
-            /* samples s and s + 32 of this lane as two independent chains (the integrand's pair form
-             * where it has one) */
+        /* samples of stream `tag`, two per lane and round (the integrand's pair form where it has
+         * one): Welford moments of f and of f - alpha h; the pilot (P) also those of h */
+        auto run = [&](auto pilot, uint64_t n, uint32_t tag, float alpha, float* st) {
+            constexpr bool P = decltype(pilot)::value;
+            float cnt = 0.0f, mf = 0.0f, m2f = 0.0f, mr = 0.0f, m2r = 0.0f, mhs = 0.0f, m2h = 0.0f;
+            auto add = [&](float fv, float hv) {
+                cnt += 1.0f;
+                const float inv = 1.0f / cnt;
+                const float rv = fv - alpha * hv;
+                const float df = fv - mf, dr = rv - mr;
+                mf = fmaf(df, inv, mf);
+                m2f = fmaf(df, fv - mf, m2f);
+                mr = fmaf(dr, inv, mr);
+                m2r = fmaf(dr, rv - mr, m2r);
+                if constexpr (P) {
+                    const float dh = hv - mhs;
+                    mhs = fmaf(dh, inv, mhs);
+                    m2h = fmaf(dh, hv - mhs, m2h);
+                }
+            };
             for (uint64_t s = lane; s < n; s += 64) {
                 const bool two = s + 32 < n;
                 float x0[F::DIM], x1[F::DIM], t0[D], t1[D], v0[1], v1[1];
@@ -712,51 +730,52 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
                     f(x0, v0);
                     f(x1, v1);
                 }
-                const float h0 = interpolant<D>(c.gr, nd, t0);
-                welford(nf, mf, m2f, v0[0]);
-                welford(nr, mr, m2r, v0[0] - h0);
-                if (two) {
-                    const float h1 = interpolant<D>(c.gr, nd, t1);
-                    welford(nf, mf, m2f, v1[0]);
-                    welford(nr, mr, m2r, v1[0] - h1);
-                }
+                add(v0[0], interpolant<D>(c.gr, nd, t0));
+                if (two) add(v1[0], interpolant<D>(c.gr, nd, t1));
             }
-            warp_merge(nf, mf, m2f);
-            warp_merge(nr, mr, m2r);
-            st[0] = nf;
+            float n1 = cnt, n2 = cnt, n3 = cnt;
+            warp_merge(n1, mf, m2f);
+            warp_merge(n2, mr, m2r);
+            if constexpr (P) warp_merge(n3, mhs, m2h);
+            st[0] = n1;
             st[1] = mf;
             st[2] = m2f;
             st[3] = mr;
             st[4] = m2r;
+            st[5] = m2h;
         };
-        /* 0: learned, 1: plain Monte Carlo, 2: polynomial control variate */
+        /* 0: control variate with weight alpha (alpha 0: plain Monte Carlo), 2: polynomial */
         int choice = 0;
+        float alpha = 1.0f;
         if (c.fallback) {
-            float ps[5];
-            run(c.pilot, 0x91107000u, ps);
-            const float var_r = ps[4], var_f = ps[2]; /* both over the same pilot count */
-            choice = var_f < var_r ? 1 : 0;
+            /* pilot (samples of their own stream, not reused): alpha = cov(f, h) / var(h), the
+             * variance-minimising weight, clamped to [0, 1.5]; fixed before the residual samples, so
+             * the estimate stays unbiased */
+            float ps[6];
+            run(std::true_type{}, c.pilot, 0x91107000u, 1.0f, ps);
+            const float m2f = ps[2], m2r1 = ps[4], m2h = ps[5]; /* sums of squares over the pilot */
+            const float cov = 0.5f * (m2f + m2h - m2r1);
+            alpha = m2h > 0.0f ? fminf(fmaxf(cov / m2h, 0.0f), 1.5f) : 0.0f;
             if (c.poly_bins) {
-                /* variance of this bin's estimate: the pilot variance over the residual samples,
-                 * scaled to bin values, against the polynomial estimate's own */
+                /* variance of this bin's estimate from the pilot, scaled to bin values and to the
+                 * residual samples, against the polynomial estimate's own */
+                const float m2a = fmaxf(m2f - 2.0f * alpha * cov + alpha * alpha * m2h, 0.0f);
                 const double scale = (double)c.factor * (double)vol;
-                const double pv = ps[0] > 1.0f ? (double)(choice ? var_f : var_r) / (ps[0] - 1.0f) : INFINITY;
+                const double pv = ps[0] > 1.0f ? (double)m2a / (ps[0] - 1.0f) : INFINITY;
                 const double v_mine = pv * scale * scale / (double)c.spp;
-                const float v_poly = c.poly_var[bin];
-                if ((double)v_poly < v_mine) choice = 2;
+                if ((double)c.poly_var[bin] < v_mine) choice = 2;
             }
         }
-        float ms[5];
-        if (choice != 2) run(c.spp, 0x5E5D0000u, ms);
+        float ms[6];
+        if (choice != 2) run(std::false_type{}, c.spp, 0x5E5D0000u, alpha, ms);
         if (lane == 0) {
             const double scale = (double)c.factor * (double)vol;
             float o;
             if (choice == 2) o = c.poly_bins[bin];
-            else if (choice == 1) o = (float)(scale * (double)ms[1]);
-            else o = (float)(scale * (mh + (double)ms[3]));
+            else o = (float)(scale * ((double)alpha * mh + (double)ms[3]));
             bins[bin] = o;
             if (integral) integral[bin] = (float)mh;
-            if (choice == 1) atomicAdd(counters, 1u);
+            if (choice == 0 && alpha == 0.0f) atomicAdd(counters, 1u);
             if (choice == 2) atomicAdd(counters + 1, 1u);
             if (isnan(o)) atomicOr(status, VCU_FLAG_NAN);
         }
@@ -794,7 +813,8 @@ inline void init_params(int d, uint64_t seed, float* theta) {
 struct State {
     float *theta, *m, *v, *grad, *partial;
     char* packed;
-    uint32_t* step;     /* [0]: Adam step counter; [1]: the held-out set's fixed counter */
+    uint32_t* step;     /* [0]: Adam step counter; [1]: the held-out set's fixed counter; [2]: the
+                         * learning-rate scale (float bits) */
     uint32_t* counters; /* [0]: plain Monte Carlo bins, [1]: polynomial control-variate bins */
     double* heldout;    /* per-block partial sums of the held-out squared error */
     float* nodes;       /* a chunk of bins' grid node values */
@@ -839,6 +859,8 @@ template <int D> int upload_params(vcu_ctx* ctx, const State& s, const float* th
     VCU_CUDA(ctx, cudaMemsetAsync(s.grad, 0, np * 4, ctx->stream));
     VCU_CUDA(ctx, cudaMemsetAsync(s.packed, 0, pack_bytes(D), ctx->stream));
     VCU_CUDA(ctx, cudaMemsetAsync(s.step, 0, 64, ctx->stream));
+    static const float one = 1.0f; /* the learning-rate scale starts at 1 */
+    VCU_CUDA(ctx, cudaMemcpyAsync(s.step + 2, &one, 4, cudaMemcpyHostToDevice, ctx->stream));
     k_mlp_pack<D><<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(s.theta, s.packed);
     ++launches;
     VCU_CUDA(ctx, cudaGetLastError());
@@ -857,6 +879,12 @@ template <int D> int set_smem_train(vcu_ctx* ctx) {
                                        tc::Smem<D>::BYTES));
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_forward_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        tc::Smem<D>::BYTES));
+    /* all of the unified L1/shared storage as shared memory: 4 CTAs of ~57 KB per SM, so one CTA's
+     * tensor-core work overlaps the others' feature and epilogue work */
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_nodes_tc<D>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
+    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_forward_tc<D>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
     return VCU_OK;
 }
 
@@ -959,7 +987,8 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
             return cuda_fail(ctx, ie, "cudaGraphInstantiate");
         }
         double best = INFINITY;
-        int stale = 0;
+        int stale = 0, drops = 0;
+        float lr_scale = 1.0f;
         while (steps_run < opt.train_steps) {
             const uint32_t n = early ? std::min(opt.check_every, opt.train_steps - steps_run) : opt.train_steps;
             for (uint32_t i = 0; i < n; ++i) {
@@ -980,12 +1009,18 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
                 return rc;
             }
             heldout_mse = mse;
-            /* stop after two checks in a row without a 0.5 % improvement on the best */
+            /* after two checks in a row without a 0.5 % improvement on the best, the learning rate
+             * drops to 0.3 of itself; the third such plateau ends training */
             if (mse < best * 0.995) {
                 best = mse;
                 stale = 0;
             } else if (++stale >= 2) {
-                break;
+                if (drops == 2) break;
+                ++drops;
+                stale = 0;
+                lr_scale *= 0.3f;
+                VCU_CUDA(ctx, cudaMemcpyAsync(s.step + 2, &lr_scale, 4, cudaMemcpyHostToDevice, ctx->stream));
+                VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); /* lr_scale is a host local */
             }
         }
         cudaGraphExecDestroy(exec);

@@ -169,12 +169,30 @@ __device__ __forceinline__ void forward_points(const char* __restrict__ packed, 
         const bool valid = i < n && point(i, u);
         if (!valid)
             for (int d = 0; d < D; ++d) u[d] = 0.5f;
-        /* features of row t: [u, sin(2^k pi u), cos(2^k pi u)], zero-padded, BF16, 16 bytes at a time */
+        /* features of row t: [u, sin(2^k pi u), cos(2^k pi u)] in feature<D>'s order, zero-padded:
+         * sinpi/cospi of the first band, the others by angle doubling (sin 2a = 2 sin a cos a,
+         * cos 2a = 1 - 2 sin^2 a; a few ulp of FP32, far below the BF16 the MMA takes) */
+        float ft[L::K0];
+#pragma unroll
+        for (int k = 0; k < L::K0; ++k) ft[k] = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            ft[d] = u[d];
+            float sn = sinpif(u[d]), cs = cospif(u[d]);
+#pragma unroll
+            for (int k = 0; k < BANDS; ++k) {
+                ft[D + 12 * d + 2 * k] = sn;
+                ft[D + 12 * d + 2 * k + 1] = cs;
+                const float s2 = 2.0f * sn * cs, c2 = fmaf(-2.0f * sn, sn, 1.0f);
+                sn = s2;
+                cs = c2;
+            }
+        }
 #pragma unroll
         for (int kg = 0; kg < L::K0 / 8; ++kg) {
             uint32_t w[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) w[q] = pack_bf16x2(feature<D>(u, 8 * kg + 2 * q), feature<D>(u, 8 * kg + 2 * q + 1));
+            for (int q = 0; q < 4; ++q) w[q] = pack_bf16x2(ft[8 * kg + 2 * q], ft[8 * kg + 2 * q + 1]);
             *reinterpret_cast<uint4*>(A + core_off(t, 8 * kg, L::K0)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
         float o = 0.0f;
