@@ -641,6 +641,23 @@ struct OccludedScene5 {
             const float a0[2] = {x0[0], x0[1]}, a1[2] = {x1[0], x1[1]};
             scene.pair(a0, a1, &s[0], &s[1]);
         }
+        visible_pair(s, x0, x1, o0, o1);
+    }
+    /* The scene terms that can be non-zero over the box [lo, hi] of the first two coordinates
+     * (Scene2::cull), and pair() evaluating only those: bit for bit pair()'s results for points
+     * whose first two coordinates lie in the box. */
+    using CullBox = Scene2::Cull;
+    VCU_HD CullBox cull_box(const float* lo, const float* hi) const { return scene.cull(lo, hi); }
+    VCU_HD void pair_culled(const CullBox& c, const float* x0, const float* x1, float* o0, float* o1) const {
+        const float a[2][2] = {{x0[0], x0[1]}, {x1[0], x1[1]}};
+        float so[2][1];
+        scene.multi_cull<2>(c, a, so);
+        const float s[2] = {so[0][0], so[1][0]};
+        visible_pair(s, x0, x1, o0, o1);
+    }
+    /* scene values s times the visibility of the two points' segments; a point whose scene value is
+     * 0 skips the boxes (its result is 0 either way, as operator() gives) */
+    VCU_HD void visible_pair(const float* s, const float* x0, const float* x1, float* o0, float* o1) const {
         const float* xs[2] = {x0, x1};
         float o[2][3], inv[2][3];
         for (int p = 0; p < 2; ++p) {
@@ -650,7 +667,7 @@ struct OccludedScene5 {
             o[p][2] = 0.0f;
             for (int k = 0; k < 3; ++k) inv[p][k] = vdiv(1.0f, vsub(e[k], o[p][k]));
         }
-        bool blocked0 = false, blocked1 = false;
+        bool blocked0 = s[0] == 0.0f, blocked1 = s[1] == 0.0f;
         for (int i = 0; i < nb && !(blocked0 && blocked1); ++i) {
             float t00 = 0.0f, t01 = 1.0f, t10 = 0.0f, t11 = 1.0f;
             for (int k = 0; k < 3; ++k) {

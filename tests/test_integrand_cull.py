@@ -148,3 +148,84 @@ def test_benchmark_flop_count_matches_the_cull(tmp_path):
     device = float(r.stdout)
     model = bench.culled_flops_per_eval(p, [0, 0], [1, 1], [128, 128])
     assert model <= device <= model * 1.01, (model, device)
+
+
+OCCLUDED = r'''
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+#include "vcu_integrands.h"
+int main(int argc, char** argv) {
+    std::vector<float> p;
+    FILE* fp = std::fopen(argv[1], "rb");
+    int n;
+    if (std::fread(&n, 4, 1, fp) != 1) return 2;
+    p.resize(n);
+    if (std::fread(p.data(), 4, n, fp) != (size_t)n) return 2;
+    std::fclose(fp);
+    static vcu::OccludedScene5 s;
+    if (s.build(p.data(), n)) return 3;
+    std::mt19937 rng(9);
+    std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+    long checked = 0, zero = 0;
+    for (int res : {1024, 64, 8}) {
+        const float w = 1.0f / (float)res;
+        for (int b = 0; b < 1500; ++b) {
+            const int ix = (int)(u01(rng) * res) % res, iy = (int)(u01(rng) * res) % res;
+            const float lo[2] = {vcu::vmul((float)ix, w), vcu::vmul((float)iy, w)};
+            const float wx = vcu::vsub(vcu::vmul((float)(ix + 1), w), lo[0]);
+            const float wy = vcu::vsub(vcu::vmul((float)(iy + 1), w), lo[1]);
+            const float hi[2] = {vcu::vadd(lo[0], wx), vcu::vadd(lo[1], wy)};
+            const auto c = s.cull_box(lo, hi);
+            for (int q = 0; q < 16; ++q) {
+                float x0[5], x1[5];
+                /* as the per-bin Monte Carlo kernel draws them: u * width + lo */
+                x0[0] = vcu::vadd(vcu::vmul(u01(rng), wx), lo[0]);
+                x0[1] = vcu::vadd(vcu::vmul(u01(rng), wy), lo[1]);
+                x1[0] = q & 1 ? lo[0] : hi[0];
+                x1[1] = q & 2 ? lo[1] : hi[1];
+                for (int k = 2; k < 5; ++k) {
+                    x0[k] = u01(rng);
+                    x1[k] = u01(rng);
+                }
+                float a0[1], a1[1], b0[1], b1[1], r0[1], r1[1];
+                s.pair_culled(c, x0, x1, a0, a1);
+                s.pair(x0, x1, b0, b1);
+                s(x0, r0);
+                s(x1, r1);
+                checked += 2;
+                zero += (r0[0] == 0.0f) + (r1[0] == 0.0f);
+                if (std::memcmp(a0, r0, 4) || std::memcmp(a1, r1, 4) || std::memcmp(b0, r0, 4) || std::memcmp(b1, r1, 4)) {
+                    std::printf("mismatch res=%d bin (%d,%d): %a %a %a | %a %a %a\n", res, ix, iy, r0[0], a0[0], b0[0],
+                                r1[0], a1[0], b1[0]);
+                    return 1;
+                }
+            }
+        }
+    }
+    std::printf("%ld %ld\n", checked, zero);
+    return 0;
+}
+'''
+
+
+def test_occluded_scene_culled_pair_equals_full_evaluation(tmp_path):
+    """The occluded 5-D scene's pair_culled (only the scene terms that can be non-zero over a bin's box
+    of the first two coordinates) and its pair (which skips the visibility of a point whose scene
+    value is 0) return what operator() returns, bit for bit, at points drawn inside the bins and at
+    their corners."""
+    src = tmp_path / "occ.cc"
+    src.write_text(OCCLUDED)
+    exe = tmp_path / "occ"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe)], check=True)
+    p = np.asarray(scenes.occluded_scene5(7), np.float32)
+    f = tmp_path / "occ.bin"
+    with open(f, "wb") as fh:
+        fh.write(np.int32(p.size).tobytes())
+        fh.write(p.tobytes())
+    r = subprocess.run([str(exe), str(f)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    checked, zero = (int(x) for x in r.stdout.split())
+    assert checked == 3 * 1500 * 16 * 2 and 0 < zero < checked

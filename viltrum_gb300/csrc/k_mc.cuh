@@ -72,13 +72,21 @@ __global__ void __launch_bounds__(MC_WARPS * 32)
             }
         };
         if constexpr (has_pair<F>::value) {
+            /* with Philox points (inside the bin) an integrand that can cull its terms to the bin's
+             * box of the first two coordinates evaluates only those -- the same bits */
+            [[maybe_unused]] typename cull_box_of<F>::type cl{};
+            if constexpr (has_pair_cull<F>::value && !REPLAY && DIM >= 2) {
+                const float clo[2] = {lo[0], lo[1]}, chi[2] = {vadd(lo[0], w[0]), vadd(lo[1], w[1])};
+                cl = f.cull_box(clo, chi);
+            }
             /* samples s and s+32 of this lane as two independent chains, added in sample order */
             for (uint64_t s = lane; s < spp; s += 64) {
                 const bool two = s + 32 < spp;
                 float x0[F::DIM], x1[F::DIM], v0[CH], v1[CH];
                 point(s, x0);
                 point(two ? s + 32 : s, x1);
-                f.pair(x0, x1, v0, v1);
+                if constexpr (has_pair_cull<F>::value && !REPLAY && DIM >= 2) f.pair_culled(cl, x0, x1, v0, v1);
+                else f.pair(x0, x1, v0, v1);
                 kahan(v0);
                 if (two) kahan(v1);
             }

@@ -701,6 +701,12 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
         };
         /* samples of stream `tag`, two per lane and round (the integrand's pair form where it has
          * one): Welford moments of f and of f - alpha h; the pilot (P) also those of h */
+        /* the scene terms that can be non-zero over the bin's box of the first two coordinates */
+        [[maybe_unused]] typename cull_box_of<F>::type cl{};
+        if constexpr (has_pair_cull<F>::value && D >= 2) {
+            const float clo[2] = {lo[0], lo[1]}, chi[2] = {hi[0], hi[1]};
+            cl = f.cull_box(clo, chi);
+        }
         auto run = [&](auto pilot, uint64_t n, uint32_t tag, float alpha, float* st) {
             constexpr bool P = decltype(pilot)::value;
             float cnt = 0.0f, mf = 0.0f, m2f = 0.0f, mr = 0.0f, m2r = 0.0f, mhs = 0.0f, m2h = 0.0f;
@@ -724,7 +730,9 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
                 float x0[F::DIM], x1[F::DIM], t0[D], t1[D], v0[1], v1[1];
                 draw(s, tag, x0, t0);
                 draw(two ? s + 32 : s, tag, x1, t1);
-                if constexpr (has_pair<F>::value) {
+                if constexpr (has_pair_cull<F>::value && D >= 2) {
+                    f.pair_culled(cl, x0, x1, v0, v1);
+                } else if constexpr (has_pair<F>::value) {
                     f.pair(x0, x1, v0, v1);
                 } else {
                     f(x0, v0);

@@ -239,6 +239,19 @@ struct has_cull<F, std::void_t<typename F::Cull,
                                decltype(std::declval<const F&>().cull((const float*)nullptr, (const float*)nullptr))>>
     : std::true_type {};
 
+/* integrands that list the terms that can be non-zero over a box of their first two coordinates
+ * (cull_box) and evaluate two points with only those (pair_culled), bit for bit pair()'s results:
+ * the per-bin Monte Carlo and learned residual kernels cull once per warp (one bin) */
+template <class F, class = void> struct has_pair_cull : std::false_type {};
+template <class F>
+struct has_pair_cull<F, std::void_t<typename F::CullBox,
+                                    decltype(std::declval<const F&>().cull_box((const float*)nullptr,
+                                                                                 (const float*)nullptr))>>
+    : std::true_type {};
+
+template <class F, bool = has_pair_cull<F>::value> struct cull_box_of { using type = int; };
+template <class F> struct cull_box_of<F, true> { using type = typename F::CullBox; };
+
 /* Calls v(functor, channels) with the built-in functor selected by kind.  The functor object is
  * built on the host (vcu_integrands.h build()); its size decides the kernel parameter size. */
 template <class V> int with_integrand(vcu_ctx* ctx, const vcu_integrand& f, int dim, V&& v) {
