@@ -1051,10 +1051,10 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
     cc.factor = g.factor;
     cc.poly_bins = opt.poly_bins;
     cc.poly_var = opt.poly_variance;
-    int per_sm = 0;
-    VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_nodes_tc<D>, tc::THREADS,
-                                                                tc::Smem<D>::BYTES));
-    const unsigned node_blocks = (unsigned)ctx->sm_count * (unsigned)(per_sm > 0 ? per_sm : 1);
+    /* persistent: CTAs_PER_SM CTAs per SM (the shared memory of 4 fits with the max-shared carveout; 4 x 64
+     * TMEM columns of the 512); the occupancy query is not used here because it ignores the carveout
+     * preference and answers 1 */
+    const unsigned node_blocks = (unsigned)ctx->sm_count * tc::CTAS_PER_SM;
     int per_sm_cv = 0;
     VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cv, k_mlp_cv<F, D>, FWD_WARPS * 32, 0));
     VCU_CUDA(ctx, cudaMemsetAsync(s.counters, 0, 8, ctx->stream));
@@ -1121,11 +1121,8 @@ int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, 
     if (y) VCU_CUDA(ctx, cudaMemcpyAsync(dy, y, (size_t)npts * 4, cudaMemcpyHostToDevice, ctx->stream));
     else VCU_CUDA(ctx, cudaMemsetAsync(dy, 0, (size_t)npts * 4, ctx->stream));
     if (!grad) {
-        int per_sm = 0;
-        VCU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_forward_tc<D>, tc::THREADS,
-                                                                    tc::Smem<D>::BYTES));
         const uint64_t tiles = ((uint64_t)npts + tc::TILE - 1) / tc::TILE;
-        const uint64_t cap = (uint64_t)ctx->sm_count * (uint64_t)(per_sm > 0 ? per_sm : 1);
+        const uint64_t cap = (uint64_t)ctx->sm_count * tc::CTAS_PER_SM;
         k_mlp_forward_tc<D><<<(unsigned)(tiles < cap ? tiles : cap), tc::THREADS, tc::Smem<D>::BYTES, ctx->stream>>>(
             s.packed, du, (uint64_t)npts, dout, ctx->d_status);
         ++launches;

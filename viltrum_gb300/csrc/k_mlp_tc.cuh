@@ -26,6 +26,7 @@ namespace tc {
 constexpr int TILE = 128;    /* points per tile = M of the MMA */
 constexpr int THREADS = 128; /* one warpgroup: thread t owns row t */
 constexpr int TMEM_COLS = 64;
+constexpr unsigned CTAS_PER_SM = 4; /* persistent grid: 4 x ~57 KB of shared memory, 4 x 64 TMEM columns */
 constexpr int MMA_N = 64;
 
 /* byte offset of element (row, k) of a row-major-by-K operand with K columns, in the canonical
