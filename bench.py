@@ -502,9 +502,9 @@ def adaptive_forms(ctx, port) -> dict:
 def time_to_rmse(ctx, target: float = 1e-3, res_side: int = 1024, seeds=(1, 2, 3)) -> dict:
     """Time each estimator needs to reach bin RMSE <= target against the truth on the 5-D occluded
     scene (2 bin dims + 3 primary dims) at res_side^2 bins: plain Monte Carlo, the polynomial control
-    variate (crespo2021, 2^14 regions) and the learned control variate (early-stopped training, the
-    network's interpolant on 6 Simpson cells per primary dimension, per-bin pilot choice against
-    plain Monte Carlo).  Per estimator and seed the samples per bin double until the target is met,
+    variate (crespo2021, 2^14 regions) and the learned control variate (at most 12 000 Adam steps of
+    32 768 samples, held-out checks every 200 with learning-rate drops on plateaus, the network's
+    interpolant on 6 Simpson cells per primary dimension, per-bin weight from a pilot).  Per estimator and seed the samples per bin double until the target is met,
     starting from the power of two below the count a 256-sample run predicts; the time is the device
     time of the one call that met it (training and region construction included) and `spp_below`
     the largest count tried that did not.  The RMSE is taken over four 32x32 windows of the image
@@ -557,7 +557,7 @@ def time_to_rmse(ctx, target: float = 1e-3, res_side: int = 1024, seeds=(1, 2, 3
 
     def lcv(spp, seed):
         st, rep = ctx.learned_control_variates(
-            p, _lib.LearnedOpts(spp, seed, 4000, 32768, 3e-3, 100, 1, 0, None, 6), buf)
+            p, _lib.LearnedOpts(spp, seed, 12000, 32768, 3e-3, 200, 1, 0, None, 6), buf)
         return st.device_ms, {"train_steps": rep.train_steps_run, "train_ms": round(rep.train_ms, 2),
                               "grid_ms": round(rep.integral_ms, 2), "residual_ms": round(rep.residual_ms, 2),
                               "plain_mc_bins": rep.fallback_bins, "nodes_per_bin": rep.nodes_per_bin}
@@ -615,7 +615,7 @@ def time_to_rmse(ctx, target: float = 1e-3, res_side: int = 1024, seeds=(1, 2, 3
             return ctx.per_bin_monte_carlo(p2, spp, seed, b2).device_ms
         if kind == "polynomial_cv":
             return ctx.control_variates(p2, nst, (1 << 14) - 1, _lib.CvOpts(spp, seed, 0, 0, 1.0), b2).device_ms
-        return ctx.learned_control_variates(p2, _lib.LearnedOpts(spp, seed, 4000, 32768, 3e-3, 100, 1, 4, None, 1),
+        return ctx.learned_control_variates(p2, _lib.LearnedOpts(spp, seed, 4000, 32768, 3e-3, 200, 1, 4, None, 1),
                                             b2)[0].device_ms
 
     small = {}
@@ -732,6 +732,11 @@ def profile_workload(args) -> dict:
         b = np.empty(r * r * 3, np.float32)
         nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
         call = lambda: ctx.control_variates(p, nst, (1 << 12) - 1, _lib.CvOpts(16, 3, 0, 0, 1.0), b)
+    elif w == "cv_crespo":  # the control-variate workload itself: crespo2021(2^14 - 1, 64), RGB moving scene
+        p = ctx.problem(scenes.MOVING_SCENE3, scenes.moving_scene3(SEED), [0, 0, 0], [1, 1, 1], [r, r])
+        b = np.empty(r * r * 3, np.float32)
+        nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+        call = lambda: ctx.control_variates(p, nst, (1 << 14) - 1, _lib.CvOpts(64, 3, 0, 0, 1.0), b)
     elif w in ("cv_importance", "cv_fubini"):
         nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
         if w == "cv_importance":  # rr_pdf_region + region_sampling_importance, alpha 0
@@ -777,7 +782,8 @@ def main(argv=None) -> int:
     ap.add_argument("--res", type=int, default=512, help="bins per side (512 is the benchmark workload)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' lines")
-    ap.add_argument("--workload", choices=["nested", "mc", "cv", "cv_importance", "cv_fubini", "batch", "learned"], default=None,
+    ap.add_argument("--workload", choices=["nested", "mc", "cv", "cv_crespo", "cv_importance", "cv_fubini", "batch",
+                             "learned"], default=None,
                     help="profiling aid: one small run of one workload (prints its stats, not a benchmark line)")
     args = ap.parse_args(argv)
     global RES
