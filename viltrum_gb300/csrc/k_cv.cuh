@@ -440,33 +440,82 @@ static __global__ void k_cv_lists(const ListCfg c, const int* __restrict__ heap_
     }
 }
 
-/* exclusive scan of the bin counts by one block (counts are small; nbins up to ~1e7) */
-static __global__ void k_cv_scan(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets, uint64_t n,
-                          uint32_t* __restrict__ status) {
-    __shared__ uint64_t part[1024];
-    const int tid = threadIdx.x;
-    const uint64_t per = (n + 1023) / 1024;
-    const uint64_t a = tid * per, b = (a + per < n) ? a + per : n;
-    uint64_t s = 0;
-    for (uint64_t i = a; i < b; ++i) s += counts[i];
-    part[tid] = s;
+/* exclusive scan of the bin counts into the list offsets, in three coalesced passes: per block of
+ * SCAN_TILE counts a block-local scan and the block's total (k_cv_scan_tiles), one block scanning the
+ * totals (k_cv_scan_totals, which also writes offsets[n] and flags a total beyond 32 bits), and the
+ * tiles' bases added (k_cv_scan_add) */
+constexpr int SCAN_THREADS = 256, SCAN_PER = 4, SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+/* inclusive scan of v over the block's threads (warp shuffles, then the warp totals) */
+__device__ __forceinline__ uint64_t block_inclusive_scan(uint64_t v, uint64_t* warp_tot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) warp_tot[warp] = v;
     __syncthreads();
-    if (tid == 0) {
-        uint64_t acc = 0;
-        for (int i = 0; i < 1024; ++i) {
-            const uint64_t v = part[i];
-            part[i] = acc;
-            acc += v;
+    if (warp == 0) {
+        uint64_t t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t u = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += u;
         }
-        if (acc > 0xffffffffull) atomicOr(status, VCU_FLAG_OVERFLOW);
-        offsets[n] = (uint32_t)acc;
+        warp_tot[lane] = t;
     }
     __syncthreads();
-    uint64_t acc = part[tid];
-    for (uint64_t i = a; i < b; ++i) {
-        offsets[i] = (uint32_t)acc;
-        acc += counts[i];
+    return v + (warp ? warp_tot[warp - 1] : 0);
+}
+
+static __global__ void __launch_bounds__(SCAN_THREADS)
+    k_cv_scan_tiles(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets, uint64_t n,
+                    uint64_t* __restrict__ tile_tot) {
+    __shared__ uint64_t wt[32];
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_PER;
+    uint32_t c[SCAN_PER];
+    uint64_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; ++k) {
+        c[k] = base + k < n ? counts[base + k] : 0u;
+        sum += c[k];
     }
+    const uint64_t incl = block_inclusive_scan(sum, wt);
+    uint64_t acc = incl - sum; /* exclusive within the tile */
+#pragma unroll
+    for (int k = 0; k < SCAN_PER; ++k) {
+        if (base + k < n) offsets[base + k] = (uint32_t)acc;
+        acc += c[k];
+    }
+    if (threadIdx.x == SCAN_THREADS - 1) tile_tot[blockIdx.x] = incl;
+}
+
+static __global__ void __launch_bounds__(SCAN_THREADS)
+    k_cv_scan_totals(uint64_t* __restrict__ tile_tot, uint64_t ntiles, uint32_t* __restrict__ offsets, uint64_t n,
+                     uint32_t* __restrict__ status) {
+    __shared__ uint64_t wt[32];
+    uint64_t carry = 0;
+    for (uint64_t b = 0; b < ntiles; b += SCAN_THREADS) {
+        const uint64_t i = b + threadIdx.x;
+        const uint64_t v = i < ntiles ? tile_tot[i] : 0;
+        const uint64_t incl = block_inclusive_scan(v, wt);
+        if (i < ntiles) tile_tot[i] = carry + incl - v; /* exclusive base of tile i */
+        __syncthreads();
+        if (threadIdx.x == SCAN_THREADS - 1) wt[0] = incl; /* this chunk's total */
+        __syncthreads();
+        carry += wt[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (carry > 0xffffffffull) atomicOr(status, VCU_FLAG_OVERFLOW);
+        offsets[n] = (uint32_t)carry;
+    }
+}
+
+static __global__ void k_cv_scan_add(uint32_t* __restrict__ offsets, uint64_t n, const uint64_t* __restrict__ tile_tot) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) offsets[i] += (uint32_t)tile_tot[i / SCAN_TILE];
 }
 
 /* sort each bin's list by heap position (rank sort by one warp per bin) */
@@ -639,7 +688,7 @@ __device__ __forceinline__ double to_double(FF a) { return (double)a.h + (double
 }  // namespace ffn
 
 template <class F, int DIM, int S, bool PDF>
-__global__ void __launch_bounds__(RES_WARPS * 32)
+__global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
     k_cv_residual(const __grid_constant__ F f, const ResCfg cfg, const uint32_t* __restrict__ offsets,
                   const uint32_t* __restrict__ lists, const int* __restrict__ heap_pay, const float* __restrict__ vals,
                   const float* __restrict__ rmin, const float* __restrict__ rmax, const float* __restrict__ rvol,
@@ -1125,8 +1174,17 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     VCU_CUDA(ctx, cudaMemsetAsync(cur, 0, g.nbins * 4, ctx->stream));
     const unsigned lblocks = (unsigned)((nheap * 32 + 255) / 256);
     k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, cnt, nullptr, nullptr, nullptr, 0);
-    k_cv_scan<<<1, 1024, 0, ctx->stream>>>(cnt, off, g.nbins, ctx->d_status);
-    launches += 2;
+    {
+        const uint64_t ntiles = (g.nbins + SCAN_TILE - 1) / SCAN_TILE;
+        /* the tile totals live in cur (256-byte aligned, nbins words, at least 256 bytes: room for
+         * ntiles = nbins / 1024 eight-byte totals), which is zeroed again before the fill uses it */
+        uint64_t* tt = reinterpret_cast<uint64_t*>(cur);
+        k_cv_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, ctx->stream>>>(cnt, off, g.nbins, tt);
+        k_cv_scan_totals<<<1, SCAN_THREADS, 0, ctx->stream>>>(tt, ntiles, off, g.nbins, ctx->d_status);
+        k_cv_scan_add<<<(unsigned)((g.nbins + 255) / 256), 256, 0, ctx->stream>>>(off, g.nbins, tt);
+        VCU_CUDA(ctx, cudaMemsetAsync(cur, 0, g.nbins * 4, ctx->stream));
+        launches += 4;
+    }
     VCU_CUDA(ctx, cudaGetLastError());
     uint32_t total = 0;
     VCU_CUDA(ctx, cudaMemcpyAsync(&total, off + g.nbins, 4, cudaMemcpyDeviceToHost, ctx->stream));
