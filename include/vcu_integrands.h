@@ -505,6 +505,74 @@ struct MovingScene3 {
         out[1] = c1;
         out[2] = c2;
     }
+    /* The terms that can be non-zero over the box [lo, hi] of (x, y, t): a bump as Scene2::cull
+     * decides (static), a disk whose centre's path over [lo[2], hi[2]] -- the segment between its
+     * centres at the two ends, the centre being monotone in t -- stays farther than its radius from the
+     * box.  Same conservative margins as Scene2::cull (box grown by 1e-6 plus 1e-6 of each bound's
+     * magnitude, 1e-4 relative on the squared distance).  eval_culled() then sums only the kept terms in
+     * the same order, so it returns operator()'s bits at every point of the box (a skipped bump adds
+     * fma(a, 0, grey) = grey, a skipped disk adds nothing). */
+    struct CullBox {
+        uint64_t g;
+        uint32_t d;
+    };
+    VCU_HD CullBox cull_box(const float* lo, const float* hi) const {
+        auto grow = [](float v) { return vadd(1e-6f, vmul(v < 0.0f ? -v : v, 1e-6f)); };
+        const float x0 = vsub(lo[0], grow(lo[0])), y0 = vsub(lo[1], grow(lo[1]));
+        const float x1 = vadd(hi[0], grow(hi[0])), y1 = vadd(hi[1], grow(hi[1]));
+        auto gap = [](float a0, float a1, float b0, float b1) { /* distance between [a0,a1] and [b0,b1] */
+            const float e = vsub(b0, a1), f = vsub(a0, b1);
+            return e > 0.0f ? e : (f > 0.0f ? f : 0.0f);
+        };
+        CullBox c{0ull, 0u};
+        for (int i = 0; i < ng; ++i) {
+            const float dx = gap(x0, x1, g[i][0], g[i][0]), dy = gap(y0, y1, g[i][1], g[i][1]);
+            if (!(vmul(vmul(vfma(dx, dx, vmul(dy, dy)), -g[i][2]), 0.9999f) > 87.0f)) c.g |= 1ull << i;
+        }
+        for (int i = 0; i < nd; ++i) {
+            const float ca = vfma(lo[2], d[i][2], d[i][0]), cb = vfma(hi[2], d[i][2], d[i][0]);
+            const float da = vfma(lo[2], d[i][3], d[i][1]), db = vfma(hi[2], d[i][3], d[i][1]);
+            float sx0 = ca < cb ? ca : cb, sx1 = ca < cb ? cb : ca, sy0 = da < db ? da : db, sy1 = da < db ? db : da;
+            sx0 = vsub(sx0, grow(sx0));
+            sx1 = vadd(sx1, grow(sx1));
+            sy0 = vsub(sy0, grow(sy0));
+            sy1 = vadd(sy1, grow(sy1));
+            const float dx = gap(x0, x1, sx0, sx1), dy = gap(y0, y1, sy0, sy1);
+            if (!(vmul(vfma(dx, dx, vmul(dy, dy)), 0.9999f) > d[i][4])) c.d |= 1u << i;
+        }
+        return c;
+    }
+    VCU_HD void eval_culled(const CullBox& c, const float* x, float* out) const {
+        float grey = 0.0f;
+        uint64_t m = c.g;
+        while (m) {
+            const int i = ctz64(m);
+            m &= m - 1;
+            const float dx = vsub(x[0], g[i][0]);
+            const float dy = vsub(x[1], g[i][1]);
+            const float r2 = vfma(dx, dx, vmul(dy, dy));
+            grey = vfma(g[i][3], vexp(vmul(r2, g[i][2])), grey);
+        }
+        float c0 = grey, c1 = grey, c2 = grey;
+        uint32_t dm = c.d;
+        while (dm) {
+            const int i = ctz64(dm);
+            dm &= dm - 1;
+            const float cx = vfma(x[2], d[i][2], d[i][0]);
+            const float cy = vfma(x[2], d[i][3], d[i][1]);
+            const float dx = vsub(x[0], cx);
+            const float dy = vsub(x[1], cy);
+            const float r2 = vfma(dx, dx, vmul(dy, dy));
+            if (r2 <= d[i][4]) {
+                c0 = vadd(c0, d[i][5]);
+                c1 = vadd(c1, d[i][6]);
+                c2 = vadd(c2, d[i][7]);
+            }
+        }
+        out[0] = c0;
+        out[1] = c1;
+        out[2] = c2;
+    }
     /* two points at once, each with exactly the arithmetic of operator() */
     VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
         float g0 = 0.0f, g1 = 0.0f;
@@ -643,9 +711,9 @@ struct OccludedScene5 {
         }
         visible_pair(s, x0, x1, o0, o1);
     }
-    /* The scene terms that can be non-zero over the box [lo, hi] of the first two coordinates
-     * (Scene2::cull), and pair() evaluating only those: bit for bit pair()'s results for points
-     * whose first two coordinates lie in the box. */
+    /* The scene terms that can be non-zero over the box [lo, hi] (its first two coordinates:
+     * Scene2::cull), and pair() evaluating only those: bit for bit pair()'s results for points whose
+     * first two coordinates lie in the box. */
     using CullBox = Scene2::Cull;
     VCU_HD CullBox cull_box(const float* lo, const float* hi) const { return scene.cull(lo, hi); }
     VCU_HD void pair_culled(const CullBox& c, const float* x0, const float* x1, float* o0, float* o1) const {

@@ -229,3 +229,80 @@ def test_occluded_scene_culled_pair_equals_full_evaluation(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     checked, zero = (int(x) for x in r.stdout.split())
     assert checked == 3 * 1500 * 16 * 2 and 0 < zero < checked
+
+
+MOVING = r'''
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+#include "vcu_integrands.h"
+int main(int argc, char** argv) {
+    std::vector<float> p;
+    FILE* fp = std::fopen(argv[1], "rb");
+    int n;
+    if (std::fread(&n, 4, 1, fp) != 1) return 2;
+    p.resize(n);
+    if (std::fread(p.data(), 4, n, fp) != (size_t)n) return 2;
+    std::fclose(fp);
+    static vcu::MovingScene3 s;
+    if (s.build(p.data(), n)) return 3;
+    std::mt19937 rng(11);
+    std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+    long checked = 0, kept = 0, terms = 0;
+    for (int res : {512, 64, 8}) {
+        for (int tcut : {1, 4}) { /* the whole of t, or a quarter of it */
+            const float w = 1.0f / (float)res;
+            for (int b = 0; b < 1500; ++b) {
+                const int ix = (int)(u01(rng) * res) % res, iy = (int)(u01(rng) * res) % res;
+                const int it = (int)(u01(rng) * tcut) % tcut;
+                const float lo[3] = {vcu::vmul((float)ix, w), vcu::vmul((float)iy, w), vcu::vmul((float)it, 1.0f / tcut)};
+                const float hi[3] = {vcu::vmul((float)(ix + 1), w), vcu::vmul((float)(iy + 1), w),
+                                     vcu::vmul((float)(it + 1), 1.0f / tcut)};
+                const auto c = s.cull_box(lo, hi);
+                kept += __builtin_popcountll(c.g) + __builtin_popcount(c.d);
+                terms += s.ng + s.nd;
+                for (int q = 0; q < 16; ++q) {
+                    float x[3];
+                    for (int k = 0; k < 3; ++k) {
+                        const int mode = (q + k) % 4; /* inside, or on either face */
+                        x[k] = mode == 0 ? lo[k] : mode == 1 ? hi[k]
+                             : vcu::vadd(lo[k], vcu::vmul(u01(rng), vcu::vsub(hi[k], lo[k])));
+                    }
+                    float a[3], r[3];
+                    s.eval_culled(c, x, a);
+                    s(x, r);
+                    ++checked;
+                    if (std::memcmp(a, r, sizeof(a))) {
+                        std::printf("mismatch res=%d at (%a,%a,%a)\n", res, x[0], x[1], x[2]);
+                        return 1;
+                    }
+                }
+            }
+        }
+    }
+    std::printf("%ld %ld %ld\n", checked, kept, terms);
+    return 0;
+}
+'''
+
+
+def test_moving_scene_culled_evaluation_equals_full_evaluation(tmp_path):
+    """The moving-disk scene's eval_culled (bumps culled as in the 2-D scene, disks by their centre's
+    path over the box's time interval) returns operator()'s three channels bit for bit at points of
+    the box, for bins of 1/512 to 1/8 and the whole or a quarter of the time range."""
+    src = tmp_path / "mov.cc"
+    src.write_text(MOVING)
+    exe = tmp_path / "mov"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe)], check=True)
+    for seed in (7, 3):
+        p = np.asarray(scenes.moving_scene3(seed), np.float32)
+        f = tmp_path / f"mov{seed}.bin"
+        with open(f, "wb") as fh:
+            fh.write(np.int32(p.size).tobytes())
+            fh.write(p.tobytes())
+        r = subprocess.run([str(exe), str(f)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        checked, kept, terms = (int(x) for x in r.stdout.split())
+        assert checked == 3 * 2 * 1500 * 16 and kept < terms

@@ -749,7 +749,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
     }
     const uint32_t off = offsets[bin];
     const uint32_t n = offsets[bin + 1] - off;
-    /* intersection bin n region (range.h:405-414) and its normalised bounds in the region */
+    /* the integrand's terms that can be non-zero in the bin (points drawn here lie in it; replayed
+     * points are the caller's, so they are evaluated in full) */
+    [[maybe_unused]] typename cull_box_of<F>::type cl{};
+    if constexpr (has_eval_cull<F>::value && F::DIM == DIM) {
+        if (!replay) cl = f.cull_box(bmin, bmax);
+    }
     auto isect = [&](int id, float* a, float* b, float* A, float* B, float& v, bool& empty) {
         empty = false;
         v = 1.0f;
@@ -978,7 +983,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
         }
         const int id = heap_pay[lists[off + chosen]] & 0xffffff;
         float fv[CH], gv[CH], p[DIM];
-        f(x, fv);
+        if constexpr (has_eval_cull<F>::value && F::DIM == DIM) {
+            if (!replay) f.eval_culled(cl, x, fv);
+            else f(x, fv);
+        } else {
+            f(x, fv);
+        }
         for (int d = 0; d < DIM; ++d) {
             const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
             p[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));

@@ -76,7 +76,13 @@ __global__ void __launch_bounds__(MC_WARPS * 32)
              * box of the first two coordinates evaluates only those -- the same bits */
             [[maybe_unused]] typename cull_box_of<F>::type cl{};
             if constexpr (has_pair_cull<F>::value && !REPLAY && DIM >= 2) {
-                const float clo[2] = {lo[0], lo[1]}, chi[2] = {vadd(lo[0], w[0]), vadd(lo[1], w[1])};
+                float clo[F::DIM], chi[F::DIM];
+                for (int d = 0; d < F::DIM; ++d) clo[d] = chi[d] = 0.0f;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    clo[d] = lo[d];
+                    chi[d] = vadd(lo[d], w[d]);
+                }
                 cl = f.cull_box(clo, chi);
             }
             /* samples s and s+32 of this lane as two independent chains, added in sample order */

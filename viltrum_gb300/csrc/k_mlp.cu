@@ -707,7 +707,12 @@ __global__ void __launch_bounds__(FWD_WARPS * 32)
         /* the scene terms that can be non-zero over the bin's box of the first two coordinates */
         [[maybe_unused]] typename cull_box_of<F>::type cl{};
         if constexpr (has_pair_cull<F>::value && D >= 2) {
-            const float clo[2] = {lo[0], lo[1]}, chi[2] = {hi[0], hi[1]};
+            float clo[F::DIM], chi[F::DIM];
+            for (int d = 0; d < F::DIM; ++d) clo[d] = chi[d] = 0.0f;
+            for (int d = 0; d < D; ++d) {
+                clo[d] = lo[d];
+                chi[d] = hi[d];
+            }
             cl = f.cull_box(clo, chi);
         }
         auto run = [&](auto pilot, uint64_t n, uint32_t tag, float alpha, float* st) {

@@ -239,17 +239,28 @@ struct has_cull<F, std::void_t<typename F::Cull,
                                decltype(std::declval<const F&>().cull((const float*)nullptr, (const float*)nullptr))>>
     : std::true_type {};
 
-/* integrands that list the terms that can be non-zero over a box of their first two coordinates
- * (cull_box) and evaluate two points with only those (pair_culled), bit for bit pair()'s results:
- * the per-bin Monte Carlo and learned residual kernels cull once per warp (one bin) */
+/* integrands that list the terms that can be non-zero over a box of their coordinates (cull_box,
+ * lo/hi of F::DIM entries) and evaluate with only those -- two points (pair_culled) or one
+ * (eval_culled) -- bit for bit what pair() / operator() return at points of the box: the per-bin
+ * Monte Carlo, learned residual and control-variate residual kernels cull once per warp (one bin) */
+template <class F, class = void> struct has_cull_box : std::false_type {};
+template <class F>
+struct has_cull_box<F, std::void_t<typename F::CullBox,
+                                   decltype(std::declval<const F&>().cull_box((const float*)nullptr,
+                                                                                (const float*)nullptr))>>
+    : std::true_type {};
 template <class F, class = void> struct has_pair_cull : std::false_type {};
 template <class F>
-struct has_pair_cull<F, std::void_t<typename F::CullBox,
-                                    decltype(std::declval<const F&>().cull_box((const float*)nullptr,
-                                                                                 (const float*)nullptr))>>
+struct has_pair_cull<F, std::void_t<decltype(std::declval<const F&>().pair_culled(
+                            std::declval<const typename F::CullBox&>(), (const float*)nullptr, (const float*)nullptr,
+                            (float*)nullptr, (float*)nullptr))>> : std::true_type {};
+template <class F, class = void> struct has_eval_cull : std::false_type {};
+template <class F>
+struct has_eval_cull<F, std::void_t<decltype(std::declval<const F&>().eval_culled(
+                            std::declval<const typename F::CullBox&>(), (const float*)nullptr, (float*)nullptr))>>
     : std::true_type {};
 
-template <class F, bool = has_pair_cull<F>::value> struct cull_box_of { using type = int; };
+template <class F, bool = has_cull_box<F>::value> struct cull_box_of { using type = int; };
 template <class F> struct cull_box_of<F, true> { using type = typename F::CullBox; };
 
 /* Calls v(functor, channels) with the built-in functor selected by kind.  The functor object is
