@@ -99,6 +99,17 @@ template <int D> VCU_HD double ddiv_f(float xf) {
 #endif
     return (xf != 0.0f && vabs(xf) <= 3.4028234663852886e38f) ? q : q0;
 }
+/* RN(x / D) of a float x for D = 3 or 5 without the division routine: q0 = RN(x RN(1/D)), then the
+ * same correction by the exact remainder as ddiv_f, in float.  q equals the IEEE quotient for every
+ * finite non-zero float x (all 2^32 checked; tests/test_ddivf.py re-checks every significand at
+ * several exponents); zeros, infinities and NaN return q0, which is the IEEE quotient for them. */
+template <int D> VCU_HD float fdiv_c(float x) {
+    static_assert(D == 3 || D == 5, "fdiv_c: divisor not checked");
+    constexpr float inv = 1.0f / (float)D;
+    const float q0 = vmul(x, inv);
+    const float q = vfma(vfma(-q0, (float)D, x), inv, q0);
+    return (x != 0.0f && vabs(x) <= 3.4028234663852886e38f) ? q : q0;
+}
 /* index of the lowest set bit of a non-zero mask */
 VCU_HD int ctz64(uint64_t m) {
 #if defined(__CUDA_ARCH__)
@@ -176,6 +187,31 @@ VCU_HD float vexp(float x) {
     const float xc = (x > 88.5f) ? 88.5f : ((x > -87.0f) ? x : -87.0f);
     const float core = vexp_core(xc);
     return (x > -87.0f) ? ((x > 88.5f) ? bits_to_float(0x7f800000u) : core) : ((x != x) ? x : 0.0f);
+}
+/* vexp(x) for the arguments of a Gaussian bump, x <= 0 or NaN: the same bits (NaN for NaN), with
+ * the selects and the exponent assembly of the positive range left out.  One predicate clamps the
+ * argument and zeroes the result; a NaN passes the clamp and propagates through the polynomial.
+ * k = rint(x log2e) lies in [-126, 0], so 2^k is (k + 127) << 23, and bits(t) = 0x4B400000 + k
+ * has the low 9 bits of k: bits(t) << 23 is (k << 23) mod 2^32, one multiply-add. */
+VCU_HD float vexp_nonpos(float x) {
+    const bool under = x <= -87.0f;
+    const float xc = under ? -87.0f : x;
+    const float t = vadd(vmul(xc, kLog2e), 12582912.0f);
+    const float k = vsub(t, 12582912.0f);
+    float r = vfma(-k, kLn2Hi, xc);
+    r = vfma(-k, kLn2Mi, r);
+    r = vfma(-k, kLn2Lo, r);
+    float p = kInvFact7;
+    p = vfma(p, r, kInvFact6);
+    p = vfma(p, r, kInvFact5);
+    p = vfma(p, r, kInvFact4);
+    p = vfma(p, r, kInvFact3);
+    p = vfma(p, r, kInvFact2);
+    p = vfma(p, r, 1.0f);
+    p = vfma(p, r, 1.0f);
+    const float s = bits_to_float(float_to_bits(t) * 8388608u + 0x3F800000u);
+    const float ps = vmul(p, s);
+    return under ? 0.0f : ps;
 }
 
 /* sin and cos of the reduced argument |r| <= pi/4 (Taylor to degree 9 and 10). */
@@ -308,7 +344,7 @@ struct Scene2 {
             const float dx = vsub(x, g[i][0]);
             const float dy = vsub(y, g[i][1]);
             const float r2 = vfma(dx, dx, vmul(dy, dy));
-            acc = vfma(g[i][3], vexp(vmul(r2, g[i][2])), acc);
+            acc = vfma(g[i][3], vexp_nonpos(vmul(r2, g[i][2])), acc);
         }
         for (int i = 0; i < nd; ++i) {
             const float dx = vsub(x, d[i][0]);
@@ -365,8 +401,8 @@ struct Scene2 {
                 for (int p = 0; p < N; ++p) {
                     const float dx0 = vsub(x[p][0], gx0), dy0 = vsub(x[p][1], gy0);
                     const float dx1 = vsub(x[p][0], gx1), dy1 = vsub(x[p][1], gy1);
-                    e0[p] = vexp(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
-                    e1[p] = vexp(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
+                    e0[p] = vexp_nonpos(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
+                    e1[p] = vexp_nonpos(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
                 }
                 VCU_UNROLL
                 for (int p = 0; p < N; ++p) a[p] = vfma(ga1, e1[p], vfma(ga0, e0[p], a[p]));
@@ -374,7 +410,7 @@ struct Scene2 {
                 VCU_UNROLL
                 for (int p = 0; p < N; ++p) {
                     const float dx = vsub(x[p][0], gx0), dy = vsub(x[p][1], gy0);
-                    a[p] = vfma(ga0, vexp(vmul(vfma(dx, dx, vmul(dy, dy)), gs0)), a[p]);
+                    a[p] = vfma(ga0, vexp_nonpos(vmul(vfma(dx, dx, vmul(dy, dy)), gs0)), a[p]);
                 }
             }
         }
@@ -408,8 +444,8 @@ struct Scene2 {
             for (int p = 0; p < N; ++p) {
                 const float dx0 = vsub(x[p][0], gx0), dy0 = vsub(x[p][1], gy0);
                 const float dx1 = vsub(x[p][0], gx1), dy1 = vsub(x[p][1], gy1);
-                e0[p] = vexp(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
-                e1[p] = vexp(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
+                e0[p] = vexp_nonpos(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
+                e1[p] = vexp_nonpos(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
             }
             VCU_UNROLL
             for (int p = 0; p < N; ++p) a[p] = vfma(ga1, e1[p], vfma(ga0, e0[p], a[p]));
@@ -420,7 +456,7 @@ struct Scene2 {
             for (int p = 0; p < N; ++p) {
                 const float dx = vsub(x[p][0], gx), dy = vsub(x[p][1], gy);
                 const float r2 = vfma(dx, dx, vmul(dy, dy));
-                a[p] = vfma(ga, vexp(vmul(r2, gs)), a[p]);
+                a[p] = vfma(ga, vexp_nonpos(vmul(r2, gs)), a[p]);
             }
         }
         for (int i = 0; i < nd; ++i) {
@@ -486,7 +522,7 @@ struct MovingScene3 {
             const float dx = vsub(x[0], g[i][0]);
             const float dy = vsub(x[1], g[i][1]);
             const float r2 = vfma(dx, dx, vmul(dy, dy));
-            grey = vfma(g[i][3], vexp(vmul(r2, g[i][2])), grey);
+            grey = vfma(g[i][3], vexp_nonpos(vmul(r2, g[i][2])), grey);
         }
         float c0 = grey, c1 = grey, c2 = grey;
         for (int i = 0; i < nd; ++i) {
@@ -551,7 +587,7 @@ struct MovingScene3 {
             const float dx = vsub(x[0], g[i][0]);
             const float dy = vsub(x[1], g[i][1]);
             const float r2 = vfma(dx, dx, vmul(dy, dy));
-            grey = vfma(g[i][3], vexp(vmul(r2, g[i][2])), grey);
+            grey = vfma(g[i][3], vexp_nonpos(vmul(r2, g[i][2])), grey);
         }
         float c0 = grey, c1 = grey, c2 = grey;
         uint32_t dm = c.d;
@@ -582,8 +618,8 @@ struct MovingScene3 {
             const float dx1 = vsub(x1[0], gx), dy1 = vsub(x1[1], gy);
             const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
             const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
-            g0 = vfma(ga, vexp(vmul(r0, gs)), g0);
-            g1 = vfma(ga, vexp(vmul(r1, gs)), g1);
+            g0 = vfma(ga, vexp_nonpos(vmul(r0, gs)), g0);
+            g1 = vfma(ga, vexp_nonpos(vmul(r1, gs)), g1);
         }
         float a0 = g0, a1 = g0, a2 = g0, b0 = g1, b1 = g1, b2 = g1;
         for (int i = 0; i < nd; ++i) {

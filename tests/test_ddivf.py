@@ -1,9 +1,9 @@
-"""ddiv_f<D> (the double quotient of a float by 3 or 5 through a product and one remainder
-correction, used in the reference-rounded Horner steps) returns the correctly rounded double
-quotient: every significand and sign at exponents across the float range, plus zeros, subnormals,
-the largest float, infinities and NaN.  The correction is one fused operation at the quotient's
-scale and a float's quotient is far from double underflow and overflow, so the exponents here stand
-for the rest; a pass over all 2^32 floats was also run once."""
+"""ddiv_f<D> and fdiv_c<D> (the double and the float quotient of a float by 3 or 5 through a
+product and one remainder correction, used in the reference-rounded Horner steps and in the rules'
+power-basis coefficients) return the correctly rounded quotient: every significand and sign at
+exponents across the float range, plus zeros, subnormals, the largest float, infinities and NaN.
+The exponents here stand for the rest (the correction is one fused operation at the quotient's
+scale); a pass over all 2^32 floats was also run once for each."""
 import os
 import subprocess
 
@@ -28,6 +28,17 @@ template <int D> static long check(float x) {
     }
     return 0;
 }
+template <int D> static long checkf(float x) {
+    const float q = vcu::fdiv_c<D>(x);
+    volatile float dd = (float)D;
+    const float r = x / dd;
+    if (std::isnan(r)) return std::isnan(q) ? 0 : 1;
+    if (std::memcmp(&q, &r, 4) != 0) {
+        std::printf("D=%d x=%a got %a want %a (float)\n", D, x, q, r);
+        return 1;
+    }
+    return 0;
+}
 template <int D> static long sweep() {
     long bad = 0;
     const int exps[] = {-126, -100, -60, -1, 0, 1, 23, 60, 100, 127};
@@ -37,15 +48,16 @@ template <int D> static long sweep() {
                 unsigned u = (s << 31) | ((unsigned)(e + 127) << 23) | m;
                 float x;
                 std::memcpy(&x, &u, 4);
-                bad += check<D>(x);
+                bad += check<D>(x) + checkf<D>(x);
             }
     for (unsigned u = 0; u < (1u << 16); ++u) {  /* zeros and subnormals */
         float x;
         unsigned v = u * 127u;
         std::memcpy(&x, &v, 4);
-        bad += check<D>(x) + check<D>(-x);
+        bad += check<D>(x) + check<D>(-x) + checkf<D>(x) + checkf<D>(-x);
     }
     bad += check<D>(INFINITY) + check<D>(-INFINITY) + check<D>(NAN) + check<D>(3.4028235e38f) + check<D>(-0.0f);
+    bad += checkf<D>(INFINITY) + checkf<D>(-INFINITY) + checkf<D>(NAN) + checkf<D>(3.4028235e38f) + checkf<D>(-0.0f);
     return bad;
 }
 int main() {

@@ -16,6 +16,8 @@ CASES = [
     (scenes.SPHERE3, None, 3, -1.0, 1.0),
     (scenes.WAVE2, None, 2, 0.0, 1.0),
     (scenes.SCENE2, scenes.scene2(7), 2, 0.0, 1.0),
+    # one unit bump at the origin: e^(-r^2/2) over r^2/2 in [0, 100], across the clamp at -87
+    (scenes.SCENE2, np.array([1, 0, 0, 0, 1, 1], np.float32), 2, 0.0, 10.0),
     (scenes.MOVING_SCENE3, scenes.moving_scene3(7), 3, 0.0, 1.0),
     (scenes.HALFSPACE, scenes.halfspace(11, 4), 4, 0.0, 1.0),
     (scenes.HALFSPACE, scenes.halfspace(12, 6), 6, 0.0, 1.0),

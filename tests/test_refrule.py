@@ -50,3 +50,70 @@ def test_refrule_matches_reference_rounding():
         assert n == 2000000
         # only the reference's own double-rounding cases may differ (probability ~2^-29 per value)
         assert bad5 <= 2 and bad3 <= 2, (bad5, bad3)
+
+
+PROG_FAST = r'''
+#include <cstdio>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include "vcu_refrule.h"
+/* ff_div without its common-case return: the candidate and remainder as ff_div forms them, then
+ * the exact decision */
+static float full(float h, float l, float D, float inv) {
+    const float ah = vcu::vabs(h);
+    const float q00 = (ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f) ? h * inv : h / D;
+    const float q0 = std::fmaf(std::fmaf(-q00, D, h) + l, inv, q00);
+    float s, e;
+    vcu::two_sum(std::fmaf(-q0, D, h), l, s, e);
+    return vcu::ff_div_decide(q0, s, e, D);
+}
+int main() {
+    std::mt19937 rng(11);
+    std::uniform_int_distribution<unsigned> mant(0, (1u << 23) - 1), sgn(0, 1);
+    std::uniform_int_distribution<int> ex(-100, 100);
+    std::uniform_real_distribution<double> off(-1.0, 1.0);
+    const float Ds[2] = {6.0f, 90.0f}, invs[2] = {0.1666666716337204f, 0.011111111380159855f};
+    long bad = 0, n = 0;
+    for (int t = 0; t < 4000000; ++t) {
+        const int k = t & 1;
+        const float D = Ds[k], inv = invs[k];
+        unsigned u = (sgn(rng) << 31) | ((unsigned)(ex(rng) + 127) << 23) | mant(rng);
+        float q;
+        std::memcpy(&q, &u, 4);
+        const double ulp = std::ldexp(1.0, std::ilogb(q) - 23);
+        /* the quotient a random offset away from q, or within 2^-18 ulp of a midpoint (the band
+         * around it included) */
+        const int mode = (t >> 1) % 4;
+        double delta = off(rng);
+        if (mode == 1) delta = 0.5 + std::ldexp(off(rng), -18);
+        if (mode == 2) delta = -0.5 + std::ldexp(off(rng), -18);
+        if (mode == 3) delta = (t & 2 ? 0.5 : -0.5) + std::ldexp(off(rng), -29);
+        const double target = ((double)q + delta * ulp) * (double)D;
+        const float h = (float)target;
+        const float l = (float)(target - (double)h);
+        const float a = vcu::ff_div(h, l, D, inv), b = full(h, l, D, inv);
+        if (std::memcmp(&a, &b, 4) != 0) {
+            if (bad < 5) std::printf("h=%a l=%a D=%g fast %a full %a\n", h, l, D, a, b);
+            ++bad;
+        }
+        ++n;
+    }
+    std::printf("%ld %ld\n", n, bad);
+    return 0;
+}
+'''
+
+
+def test_ff_div_common_case_matches_exact_decision():
+    """ff_div's early return (remainder well inside the half gap) gives the exact decision's result,
+    including quotients within 2^-18 and 2^-29 ulp of a rounding midpoint."""
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "f.cc")
+        exe = os.path.join(d, "f")
+        open(src, "w").write(PROG_FAST)
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                               "-I", os.path.join(ROOT, "viltrum_gb300", "csrc"), src, "-o", exe])
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+        n, bad = int(out[-2]), int(out[-1])
+        assert n == 4000000 and bad == 0, " ".join(out)

@@ -129,6 +129,35 @@ __device__ float region_subrange(const float* V, int c, const float* A, const fl
     return buf[0];
 }
 
+/* Newton-Cotes weights of an S-node rule on [0, 1]: the exact integral of the interpolant */
+/* region_subrange() over the whole region, [0, 1] in every dimension (Rule<S>::subrange01) */
+template <int DIM, int S, int CH>
+__device__ float region_subrange01(const float* V, int c) {
+    constexpr int SD = ipow(S, DIM);
+    constexpr int inner = SD / S;
+    float buf[inner];
+#pragma unroll
+    for (int i = 0; i < inner; ++i) {
+        float line[S];
+#pragma unroll
+        for (int j = 0; j < S; ++j) line[j] = V[(i + j * inner) * CH + c];
+        buf[i] = Rule<S>::subrange01(line);
+    }
+    int n = inner;
+#pragma unroll
+    for (int d = DIM - 2; d >= 0; --d) {
+        const int m = n / S;
+        for (int i = 0; i < m; ++i) {
+            float line[S];
+#pragma unroll
+            for (int j = 0; j < S; ++j) line[j] = buf[i + j * m];
+            buf[i] = Rule<S>::subrange01(line);
+        }
+        n = m;
+    }
+    return buf[0];
+}
+
 /* culled evaluation when the integrand supports it over the kernel's full dimension */
 template <class F, int DIM> constexpr bool use_cull = has_cull<F>::value && DIM == F::DIM;
 template <class F, bool = has_cull<F>::value> struct cull_of { using type = int; };
@@ -512,23 +541,39 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
         const int nreg = iters + 1;
         for (int k = gl; k < nreg; k += G) {
             const int s = HS[k] & 0xff;
-            float A[DIM], B[DIM];
-            bool empty = false;
+            float a[DIM], b[DIM];
+            bool empty = false, whole = true;
 #pragma unroll
             for (int d = 0; d < DIM; ++d) {
                 const float blo = bmin[d];
                 const float bhi = (d == 0) ? vadd(bmin[0], vmul(1.0f, vdiv(vsub(bmax[0], bmin[0]), 1.0f))) : bmax[d];
                 const float rmn = RMIN[s * DIM + d], rmx = RMAX[s * DIM + d];
-                const float a = smax(blo, rmn);
-                const float b = smax(a, smin(bhi, rmx));
-                empty = empty || (a >= b);
-                A[d] = (rmn >= rmx) ? rmn : vdiv(vsub(a, rmn), vsub(rmx, rmn));
-                B[d] = (rmn >= rmx) ? rmn : vdiv(vsub(b, rmn), vsub(rmx, rmn));
+                a[d] = smax(blo, rmn);
+                b[d] = smax(a[d], smin(bhi, rmx));
+                empty = empty || (a[d] >= b[d]);
+                whole = whole && a[d] == rmn && b[d] == rmx;
             }
+            if (empty) {
+                CT[k * CH] = __int_as_float(0x7fc00001); /* marker: skipped region */
+            } else if (whole) {
+                /* the region lies inside the bin (every region, unless the bin's first upper bound,
+                 * rebuilt as min + (max - min), rounds below it): the normalised intersection is
+                 * [0, 1] in every dimension, A and B need no division */
 #pragma unroll
-            for (int c = 0; c < CH; ++c)
-                CT[k * CH + c] = empty ? 0.0f : vmul(VOL[s], region_subrange<DIM, S, CH>(V + (size_t)s * SD * CH, c, A, B));
-            if (empty) CT[k * CH] = __int_as_float(0x7fc00001); /* marker: skipped region */
+                for (int c = 0; c < CH; ++c)
+                    CT[k * CH + c] = vmul(VOL[s], region_subrange01<DIM, S, CH>(V + (size_t)s * SD * CH, c));
+            } else {
+                float A[DIM], B[DIM];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const float rmn = RMIN[s * DIM + d], rmx = RMAX[s * DIM + d];
+                    A[d] = (rmn >= rmx) ? rmn : vdiv(vsub(a[d], rmn), vsub(rmx, rmn));
+                    B[d] = (rmn >= rmx) ? rmn : vdiv(vsub(b[d], rmn), vsub(rmx, rmn));
+                }
+#pragma unroll
+                for (int c = 0; c < CH; ++c)
+                    CT[k * CH + c] = vmul(VOL[s], region_subrange<DIM, S, CH>(V + (size_t)s * SD * CH, c, A, B));
+            }
         }
         __syncwarp(gmask);
         if (gl == 0) {

@@ -52,20 +52,11 @@ VCU_HD bool even_bits(float x) {
     return (u & 1u) == 0u;
 #endif
 }
-/* RN_f(RN_d((h + l) / D)) for the float-float pair (h, l) and a small positive integer D, as the
- * reference's "double sum / double constant, assigned to float" rounds it.  q0 (a corrected
- * RN(h/D)) is within one float of the result; the exact remainder R = h + l - q0*D (two_sum of the
- * exact fma residual and l) decides: R/D beyond half the gap to the neighbour moves to it, exactly half (or within the
- * 2^-30-ulp band where the reference's intermediate double lands on the midpoint) ties to even. */
-VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
-    /* q00 ~ h/D, then one approximate correction step brings q0 within one float of the result
-     * (the exact decision below does the rest).  For |h| in [2^-90, 2^90] the product by RN(1/D)
-     * is close enough; outside that range (subnormal quotients, near overflow) a true division. */
-    const float ah = vabs(h);
-    const float q00 = (ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f) ? vmul(h, inv_D) : vdiv(h, D);
-    const float q0 = vfma(vadd(vfma(-q00, D, h), l), inv_D, q00);
-    float s, e;
-    two_sum(vfma(-q0, D, h), l, s, e);
+/* The exact rounding decision of ff_div below for its candidate q0 and the exact remainder
+ * R = s + e = h + l - q0*D: R/D beyond half the gap to a neighbour moves to it, exactly half (or
+ * within the 2^-30-ulp band where the reference's intermediate double lands on the midpoint) ties
+ * to even. */
+VCU_HD float ff_div_decide(float q0, float s, float e, float D) {
     const float up = next_up(q0), dn = next_down(q0);
     const float tu = vmul(D, vmul(vsub(up, q0), 0.5f)); /* exact: D * half gap above */
     const float td = vmul(D, vmul(vsub(q0, dn), 0.5f)); /* exact: D * half gap below */
@@ -78,6 +69,31 @@ VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
     if (du > 0.0f) return up;
     if (dd > 0.0f) return dn;
     return q0;
+}
+/* RN_f(RN_d((h + l) / D)) for the float-float pair (h, l) and a small positive integer D, as the
+ * reference's "double sum / double constant, assigned to float" rounds it.  q0 (a corrected
+ * RN(h/D)) is within one float of the result; the exact remainder R = h + l - q0*D (two_sum of the
+ * exact fma residual and l) decides (ff_div_decide). */
+VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
+    /* q00 ~ h/D, then one approximate correction step brings q0 within one float of the result
+     * (the exact decision does the rest).  For |h| in [2^-90, 2^90] the product by RN(1/D)
+     * is close enough; outside that range (subnormal quotients, near overflow) a true division. */
+    const float ah = vabs(h);
+    const float q00 = (ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f) ? vmul(h, inv_D) : vdiv(h, D);
+    const float q0 = vfma(vadd(vfma(-q00, D, h), l), inv_D, q00);
+    float s, e;
+    two_sum(vfma(-q0, D, h), l, s, e);
+    /* Common case first: q0 normal, not a power of two (both neighbours one ulp away, so the
+     * half gaps tu = td = D ulp / 2) and |s| below tu (1 - 2^-20), with |e| <= 2^-24 |s|: then R/D
+     * is farther than 2^-21 ulp from either midpoint, outside the tie band, and ff_div_decide returns
+     * q0.  The threshold RN(D (1 - 2^-20) / 2) ulp is within 2^-24 of that bound. */
+    const uint32_t u = float_to_bits(q0);
+    const uint32_t ex = u & 0x7f800000u;
+    if ((u & 0x007fffffu) != 0u && ex >= (25u << 23) && ex < (254u << 23)) {
+        const float ulp = bits_to_float(ex - (23u << 23));
+        if (vabs(s) <= vmul(ulp, vmul(D, 0.49999952316284180f /* (1 - 2^-20) / 2 */))) return q0;
+    }
+    return ff_div_decide(q0, s, e, D);
 }
 
 template <int S> struct RefRule;

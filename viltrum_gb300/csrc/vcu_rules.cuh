@@ -18,6 +18,11 @@ namespace vcu {
 
 template <int S> struct Rule;
 
+/* Divisions by the rules' constants: by 2 and 4 as the equal products (exact scalings), by 3 and 5
+ * through fdiv_c (the IEEE quotient, see vcu_integrands.h).  subrange01() is subrange(0, 1, p):
+ * the antiderivative at 1 with the products by 1 left out, minus the one at 0, which is a zero for
+ * finite coefficients -- subtracting it changes at most the sign of a zero result -- so it is
+ * evaluated only when the value at 1 is not finite. */
 template <> struct Rule<2> { /* trapezoidal */
     static __device__ __forceinline__ float rule(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
     static __device__ __forceinline__ void coefficients(const float* p, float* c) {
@@ -30,12 +35,19 @@ template <> struct Rule<2> { /* trapezoidal */
         return vadd(vmul(c[1], t), c[0]);
     }
     static __device__ __forceinline__ float horner_int(const float* c, float t) {
-        return vmul(vadd(vdiv(vmul(c[1], t), 2.0f), c[0]), t);
+        return vmul(vadd(vmul(vmul(c[1], t), 0.5f), c[0]), t);
     }
+    static __device__ __forceinline__ float horner_int1(const float* c) { return vadd(vmul(c[1], 0.5f), c[0]); }
     static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
         float c[2];
         coefficients(p, c);
         return vsub(horner_int(c, b), horner_int(c, a));
+    }
+    static __device__ __forceinline__ float subrange01(const float* p) {
+        float c[2];
+        coefficients(p, c);
+        const float h1 = horner_int1(c);
+        return isfinite(h1) ? h1 : vsub(h1, horner_int(c, 0.0f));
     }
 };
 
@@ -54,14 +66,23 @@ template <> struct Rule<3> { /* simpson */
         return vadd(vmul(vadd(vmul(c[2], t), c[1]), t), c[0]);
     }
     static __device__ __forceinline__ float horner_int(const float* c, float t) {
-        float r = vadd(vdiv(vmul(c[2], t), 3.0f), vdiv(c[1], 2.0f));
+        float r = vadd(fdiv_c<3>(vmul(c[2], t)), vmul(c[1], 0.5f));
         r = vadd(vmul(r, t), c[0]);
         return vmul(r, t);
+    }
+    static __device__ __forceinline__ float horner_int1(const float* c) {
+        return vadd(vadd(fdiv_c<3>(c[2]), vmul(c[1], 0.5f)), c[0]);
     }
     static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
         float c[3];
         coefficients(p, c);
         return vsub(horner_int(c, b), horner_int(c, a));
+    }
+    static __device__ __forceinline__ float subrange01(const float* p) {
+        float c[3];
+        coefficients(p, c);
+        const float h1 = horner_int1(c);
+        return isfinite(h1) ? h1 : vsub(h1, horner_int(c, 0.0f));
     }
 };
 
@@ -72,18 +93,18 @@ template <> struct Rule<5> { /* boole */
     }
     static __device__ __forceinline__ void coefficients(const float* p, float* c) {
         c[0] = p[0];
-        c[1] = vsub(vadd(vsub(vadd(vdiv(vmul(-25.0f, p[0]), 3.0f), vmul(16.0f, p[1])), vmul(12.0f, p[2])),
-                         vdiv(vmul(16.0f, p[3]), 3.0f)),
+        c[1] = vsub(vadd(vsub(vadd(fdiv_c<3>(vmul(-25.0f, p[0])), vmul(16.0f, p[1])), vmul(12.0f, p[2])),
+                         fdiv_c<3>(vmul(16.0f, p[3]))),
                     p[4]);
-        c[2] = vadd(vsub(vadd(vsub(vdiv(vmul(70.0f, p[0]), 3.0f), vdiv(vmul(208.0f, p[1]), 3.0f)), vmul(76.0f, p[2])),
-                         vdiv(vmul(112.0f, p[3]), 3.0f)),
-                    vdiv(vmul(22.0f, p[4]), 3.0f));
-        c[3] = vsub(vadd(vsub(vadd(vdiv(vmul(-80.0f, p[0]), 3.0f), vmul(96.0f, p[1])), vmul(128.0f, p[2])),
-                         vdiv(vmul(224.0f, p[3]), 3.0f)),
+        c[2] = vadd(vsub(vadd(vsub(fdiv_c<3>(vmul(70.0f, p[0])), fdiv_c<3>(vmul(208.0f, p[1]))), vmul(76.0f, p[2])),
+                         fdiv_c<3>(vmul(112.0f, p[3]))),
+                    fdiv_c<3>(vmul(22.0f, p[4])));
+        c[3] = vsub(vadd(vsub(vadd(fdiv_c<3>(vmul(-80.0f, p[0])), vmul(96.0f, p[1])), vmul(128.0f, p[2])),
+                         fdiv_c<3>(vmul(224.0f, p[3]))),
                     vmul(16.0f, p[4]));
-        c[4] = vadd(vsub(vadd(vsub(vdiv(vmul(32.0f, p[0]), 3.0f), vdiv(vmul(128.0f, p[1]), 3.0f)), vmul(64.0f, p[2])),
-                         vdiv(vmul(128.0f, p[3]), 3.0f)),
-                    vdiv(vmul(32.0f, p[4]), 3.0f));
+        c[4] = vadd(vsub(vadd(vsub(fdiv_c<3>(vmul(32.0f, p[0])), fdiv_c<3>(vmul(128.0f, p[1]))), vmul(64.0f, p[2])),
+                         fdiv_c<3>(vmul(128.0f, p[3]))),
+                    fdiv_c<3>(vmul(32.0f, p[4])));
     }
     static __device__ __forceinline__ float at(float t, const float* p) {
         float c[5];
@@ -94,16 +115,28 @@ template <> struct Rule<5> { /* boole */
         return vadd(vmul(r, t), c[0]);
     }
     static __device__ __forceinline__ float horner_int(const float* c, float t) {
-        float r = vadd(vdiv(vmul(c[4], t), 5.0f), vdiv(c[3], 4.0f));
-        r = vadd(vmul(r, t), vdiv(c[2], 3.0f));
-        r = vadd(vmul(r, t), vdiv(c[1], 2.0f));
+        float r = vadd(fdiv_c<5>(vmul(c[4], t)), vmul(c[3], 0.25f));
+        r = vadd(vmul(r, t), fdiv_c<3>(c[2]));
+        r = vadd(vmul(r, t), vmul(c[1], 0.5f));
         r = vadd(vmul(r, t), c[0]);
         return vmul(r, t);
+    }
+    static __device__ __forceinline__ float horner_int1(const float* c) {
+        float r = vadd(fdiv_c<5>(c[4]), vmul(c[3], 0.25f));
+        r = vadd(r, fdiv_c<3>(c[2]));
+        r = vadd(r, vmul(c[1], 0.5f));
+        return vadd(r, c[0]);
     }
     static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
         float c[5];
         coefficients(p, c);
         return vsub(horner_int(c, b), horner_int(c, a));
+    }
+    static __device__ __forceinline__ float subrange01(const float* p) {
+        float c[5];
+        coefficients(p, c);
+        const float h1 = horner_int1(c);
+        return isfinite(h1) ? h1 : vsub(h1, horner_int(c, 0.0f));
     }
 };
 
@@ -159,7 +192,9 @@ template <int S> __device__ __forceinline__ double mid_pos(int k) {
     return (double)(2 * k + 1) * (0.5 / (double)(S - 1));
 }
 __device__ __forceinline__ float node_coord(double p, float w, float m) {
-    return __double2float_rn(__dadd_rn(__dmul_rn(p, (double)w), (double)m));
+    /* p has at most 3 significant bits, so p*w is exact in double and the fused form rounds
+     * p*w + m once, as the reference's product-then-sum does */
+    return __double2float_rn(__fma_rn(p, (double)w, (double)m));
 }
 
 /* std::max / std::min semantics: (a < b) ? b : a */
