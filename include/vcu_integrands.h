@@ -118,6 +118,13 @@ VCU_HD int ctz64(uint64_t m) {
     return __builtin_ctzll(m);
 #endif
 }
+VCU_HD int ctz32(uint32_t m) {
+#if defined(__CUDA_ARCH__)
+    return __ffs((int)m) - 1;
+#else
+    return __builtin_ctz(m);
+#endif
+}
 VCU_HD uint32_t float_to_bits(float f) {
 #if defined(__CUDA_ARCH__)
     return __float_as_uint(f);
@@ -189,13 +196,14 @@ VCU_HD float vexp(float x) {
     return (x > -87.0f) ? ((x > 88.5f) ? bits_to_float(0x7f800000u) : core) : ((x != x) ? x : 0.0f);
 }
 /* vexp(x) for the arguments of a Gaussian bump, x <= 0 or NaN: the same bits (NaN for NaN), with
- * the selects and the exponent assembly of the positive range left out.  One predicate clamps the
- * argument and zeroes the result; a NaN passes the clamp and propagates through the polynomial.
- * k = rint(x log2e) lies in [-126, 0], so 2^k is (k + 127) << 23, and bits(t) = 0x4B400000 + k
- * has the low 9 bits of k: bits(t) << 23 is (k << 23) mod 2^32, one multiply-add. */
+ * the clamps and the exponent assembly of the positive range left out.  The core runs on x itself:
+ * for x <= -87 (where its value is meaningless) one select returns 0; a NaN propagates through the
+ * polynomial.  For x in (-87, 0], k = rint(x log2e) lies in [-126, 0], so 2^k is (k + 127) << 23,
+ * and bits(t) = 0x4B400000 + k has the low 9 bits of k: bits(t) << 23 is (k << 23) mod 2^32, one
+ * multiply-add. */
 VCU_HD float vexp_nonpos(float x) {
     const bool under = x <= -87.0f;
-    const float xc = under ? -87.0f : x;
+    const float xc = x;
     const float t = vadd(vmul(xc, kLog2e), 12582912.0f);
     const float k = vsub(t, 12582912.0f);
     float r = vfma(-k, kLn2Hi, xc);
@@ -366,57 +374,79 @@ struct Scene2 {
         uint64_t g;
         uint32_t d;
     };
-    VCU_HD Cull cull(const float* lo, const float* hi) const {
+    /* The same decision term by term, for callers that spread the terms over lanes: the grown box
+     * (x0, y0, x1, y1), then term t of the mask's three 32-bit words (bumps 0-31, bumps 32-63,
+     * disks 0-31; false past ng / nd) */
+    static constexpr int kCullWords = 3, kCullBox = 4;
+    VCU_HD void cull_prepare(const float* lo, const float* hi, float* box) const {
         auto grow = [](float v) { return vadd(1e-6f, vmul(v < 0.0f ? -v : v, 1e-6f)); };
-        const float x0 = vsub(lo[0], grow(lo[0])), y0 = vsub(lo[1], grow(lo[1]));
-        const float x1 = vadd(hi[0], grow(hi[0])), y1 = vadd(hi[1], grow(hi[1]));
+        box[0] = vsub(lo[0], grow(lo[0]));
+        box[1] = vsub(lo[1], grow(lo[1]));
+        box[2] = vadd(hi[0], grow(hi[0]));
+        box[3] = vadd(hi[1], grow(hi[1]));
+    }
+    VCU_HD bool cull_keep(int t, const float* box) const {
         auto dist2 = [&](float cx, float cy) {
-            const float ex = vsub(x0, cx), fx = vsub(cx, x1), ey = vsub(y0, cy), fy = vsub(cy, y1);
+            const float ex = vsub(box[0], cx), fx = vsub(cx, box[2]), ey = vsub(box[1], cy), fy = vsub(cy, box[3]);
             const float dx = ex > 0.0f ? ex : (fx > 0.0f ? fx : 0.0f);
             const float dy = ey > 0.0f ? ey : (fy > 0.0f ? fy : 0.0f);
             return vfma(dx, dx, vmul(dy, dy));
         };
-        Cull c{0ull, 0u};
-        for (int i = 0; i < ng; ++i)
-            if (!(vmul(vmul(dist2(g[i][0], g[i][1]), -g[i][2]), 0.9999f) > 87.0f)) c.g |= 1ull << i;
-        for (int i = 0; i < nd; ++i)
-            if (!(vmul(dist2(d[i][0], d[i][1]), 0.9999f) > d[i][2])) c.d |= 1u << i;
-        return c;
+        if (t < 64) {
+            if (t >= ng) return false;
+            return !(vmul(vmul(dist2(g[t][0], g[t][1]), -g[t][2]), 0.9999f) > 87.0f);
+        }
+        const int i = t - 64;
+        if (i >= nd) return false;
+        return !(vmul(dist2(d[i][0], d[i][1]), 0.9999f) > d[i][2]);
+    }
+    VCU_HD static Cull cull_from_words(const uint32_t* w) { return Cull{(uint64_t)w[0] | ((uint64_t)w[1] << 32), w[2]}; }
+    VCU_HD Cull cull(const float* lo, const float* hi) const {
+        float box[4];
+        cull_prepare(lo, hi, box);
+        uint32_t w[kCullWords] = {0u, 0u, 0u};
+        for (int t = 0; t < 32 * kCullWords; ++t)
+            if (cull_keep(t, box)) w[t >> 5] |= 1u << (t & 31);
+        return cull_from_words(w);
     }
     template <int N> VCU_HD void multi_cull(const Cull& c, const float (*x)[DIM], float (*o)[CH]) const {
         float a[N];
         VCU_UNROLL
         for (int p = 0; p < N; ++p) a[p] = 0.0f;
-        uint64_t m = c.g;
-        while (m) {
-            const int i = ctz64(m);
-            m &= m - 1;
-            const float gx0 = g[i][0], gy0 = g[i][1], gs0 = g[i][2], ga0 = g[i][3];
-            if (m) { /* two kept bumps per step, independent exponentials, the sum in order */
-                const int j = ctz64(m);
+        /* the kept bumps in index order, one 32-bit half of the mask after the other */
+        for (int half = 0; half < 2; ++half) {
+            uint32_t m = half ? (uint32_t)(c.g >> 32) : (uint32_t)c.g;
+            const int base = 32 * half;
+            while (m) {
+                const int i = base + ctz32(m);
                 m &= m - 1;
-                const float gx1 = g[j][0], gy1 = g[j][1], gs1 = g[j][2], ga1 = g[j][3];
-                float e0[N], e1[N];
-                VCU_UNROLL
-                for (int p = 0; p < N; ++p) {
-                    const float dx0 = vsub(x[p][0], gx0), dy0 = vsub(x[p][1], gy0);
-                    const float dx1 = vsub(x[p][0], gx1), dy1 = vsub(x[p][1], gy1);
-                    e0[p] = vexp_nonpos(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
-                    e1[p] = vexp_nonpos(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
-                }
-                VCU_UNROLL
-                for (int p = 0; p < N; ++p) a[p] = vfma(ga1, e1[p], vfma(ga0, e0[p], a[p]));
-            } else {
-                VCU_UNROLL
-                for (int p = 0; p < N; ++p) {
-                    const float dx = vsub(x[p][0], gx0), dy = vsub(x[p][1], gy0);
-                    a[p] = vfma(ga0, vexp_nonpos(vmul(vfma(dx, dx, vmul(dy, dy)), gs0)), a[p]);
+                const float gx0 = g[i][0], gy0 = g[i][1], gs0 = g[i][2], ga0 = g[i][3];
+                if (m) { /* two kept bumps per step, independent exponentials, the sum in order */
+                    const int j = base + ctz32(m);
+                    m &= m - 1;
+                    const float gx1 = g[j][0], gy1 = g[j][1], gs1 = g[j][2], ga1 = g[j][3];
+                    float e0[N], e1[N];
+                    VCU_UNROLL
+                    for (int p = 0; p < N; ++p) {
+                        const float dx0 = vsub(x[p][0], gx0), dy0 = vsub(x[p][1], gy0);
+                        const float dx1 = vsub(x[p][0], gx1), dy1 = vsub(x[p][1], gy1);
+                        e0[p] = vexp_nonpos(vmul(vfma(dx0, dx0, vmul(dy0, dy0)), gs0));
+                        e1[p] = vexp_nonpos(vmul(vfma(dx1, dx1, vmul(dy1, dy1)), gs1));
+                    }
+                    VCU_UNROLL
+                    for (int p = 0; p < N; ++p) a[p] = vfma(ga1, e1[p], vfma(ga0, e0[p], a[p]));
+                } else {
+                    VCU_UNROLL
+                    for (int p = 0; p < N; ++p) {
+                        const float dx = vsub(x[p][0], gx0), dy = vsub(x[p][1], gy0);
+                        a[p] = vfma(ga0, vexp_nonpos(vmul(vfma(dx, dx, vmul(dy, dy)), gs0)), a[p]);
+                    }
                 }
             }
         }
         uint32_t dm = c.d;
         while (dm) {
-            const int i = ctz64(dm);
+            const int i = ctz32(dm);
             dm &= dm - 1;
             const float cx = d[i][0], cy = d[i][1], rr = d[i][2], dv = d[i][3];
             VCU_UNROLL
@@ -592,7 +622,7 @@ struct MovingScene3 {
         float c0 = grey, c1 = grey, c2 = grey;
         uint32_t dm = c.d;
         while (dm) {
-            const int i = ctz64(dm);
+            const int i = ctz32(dm);
             dm &= dm - 1;
             const float cx = vfma(x[2], d[i][2], d[i][0]);
             const float cy = vfma(x[2], d[i][3], d[i][1]);

@@ -434,7 +434,7 @@ __device__ float nested_item(const F& f, const Item& it, const Cfg& cfg, float* 
             const int P = s_cand[q] & 0xffffff, dd = s_cand[q] >> 24;
             const float* pr = R + (size_t)P * SLOT_FLOATS;
             const float pmn = pr[dd], pmx = pr[VCU_MAX_DIM + dd];
-            const float half = vdiv(vsub(pmx, pmn), 2.0f);
+            const float half = vmul(vsub(pmx, pmn), 0.5f); /* = (max - min) / 2.0, exactly */
             const float mid = vadd(pmn, vmul(half, 1.0f));
             float* r0 = CR + (2 * q) * SLOT_FLOATS;
             float* r1 = r0 + SLOT_FLOATS;

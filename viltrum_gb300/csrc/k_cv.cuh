@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(GEN_THREADS, 1)
                 const float* pmin = rmin + (size_t)P * DIM;
                 const float* pmax = rmax + (size_t)P * DIM;
                 const float pmn = pmin[dd], pmx = pmax[dd];
-                const float half = vdiv(vsub(pmx, pmn), 2.0f);
+                const float half = vmul(vsub(pmx, pmn), 0.5f); /* = (max - min) / 2.0, exactly */
                 const float mid = vadd(pmn, vmul(half, 1.0f));
                 float v0 = 1.0f, v1 = 1.0f;
                 for (int d = 0; d < DIM; ++d) {
@@ -1555,7 +1555,7 @@ __device__ __forceinline__ void warp_split(const F& f, const float* V, int id, i
     }
     if (lane == 0) {
         const float pmn = pmin[dd], pmx = pmax[dd];
-        const float half = vdiv(vsub(pmx, pmn), 2.0f);
+        const float half = vmul(vsub(pmx, pmn), 0.5f); /* = (max - min) / 2.0, exactly */
         const float mid = vadd(pmn, vmul(half, 1.0f));
         float v0 = 1.0f, v1 = 1.0f;
         for (int d = 0; d < DIM; ++d) {

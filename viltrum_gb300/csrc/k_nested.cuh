@@ -171,7 +171,7 @@ __device__ __forceinline__ void eval_points(const F& f, const typename cull_of<F
 }
 
 template <class F, int DIM, int SH, int SL, int G>
-__global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_constant__ F f, const BinGrid g,
+__global__ void __launch_bounds__(NC_THREADS, DIM == 2 ? 6 : 1) k_per_bin_nested(const __grid_constant__ F f, const BinGrid g,
                                                                const NcCfg cfg, float* __restrict__ bins,
                                                                int32_t* __restrict__ trace,
                                                                uint32_t* __restrict__ status) {
@@ -245,7 +245,27 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                     hi[d] = fmaxf(hi[d], h2[d]);
                 }
             }
-            cl = f.cull(lo, hi);
+            if constexpr (has_cull_terms<F>::value) {
+                /* the group's lanes share the per-term tests; one vote per G terms */
+                float box[F::kCullBox];
+                f.cull_prepare(lo, hi, box);
+                uint32_t words[F::kCullWords];
+                const int gbase = lane & ~(G - 1);
+                constexpr uint32_t gbits = (G == 32) ? 0xffffffffu : ((1u << (G & 31)) - 1u);
+#pragma unroll
+                for (int k = 0; k < F::kCullWords; ++k) {
+                    uint32_t word = 0u;
+#pragma unroll
+                    for (int q = 0; q < 32 / G; ++q) {
+                        const uint32_t b = __ballot_sync(gmask, f.cull_keep(32 * k + G * q + gl, box));
+                        word |= ((b >> gbase) & gbits) << (G * q);
+                    }
+                    words[k] = word;
+                }
+                cl = F::cull_from_words(words);
+            } else {
+                cl = f.cull(lo, hi);
+            }
         }
         /* ---- root region in slot 0 */
         if (gl == 0) {
@@ -312,34 +332,40 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
         }
         __syncwarp(gmask);
 
-        /* ---- error estimates of `nreg` regions (slots sl[0..nreg)) into EC[r*DIM + d] */
-        auto region_errors = [&](int nreg, int s0, int s1) {
-            for (int t = gl; t < nreg * DIM * NL; t += G) {
+        /* ---- error estimates of `nreg` regions (slots s0, s1) into EC[r*DIM + d] */
+        auto region_errors = [&](auto nreg_c, int s0, int s1) {
+            constexpr int NT = decltype(nreg_c)::value * DIM * NL; /* lines */
+            auto line_of = [&](int t, int c, float* line, float* low) {
                 const int r = t / (DIM * NL), rr = t % (DIM * NL);
                 const int d = rr / NL, J = rr % NL;
                 const float* RV = V + (size_t)(r ? s1 : s0) * SD * CH;
-                float m = 0.0f;
 #pragma unroll
-                for (int c = 0; c < CH; ++c) {
+                for (int i = 0; i < S; ++i) line[i] = RV[node_index<DIM, S>(d, J, i) * CH + c];
+#pragma unroll
+                for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
+            };
+            if constexpr (CH == 1) {
+                for (int t = gl; t < NT; t += G) {
                     float line[S], low[SL];
-#pragma unroll
-                    for (int i = 0; i < S; ++i) line[i] = RV[node_index<DIM, S>(d, J, i) * CH + c];
-#pragma unroll
-                    for (int i = 0; i < SL; ++i) low[i] = line[i * (S - 1) / (SL - 1)];
-                    float H, L;
-                    if constexpr (CH == 1) {
-                        H = RefRule<S>::scalar(line);
-                        L = RefRule<SL>::scalar(low);
-                    } else {
-                        H = RefRule<S>::rgb(line);
-                        L = RefRule<SL>::rgb(low);
-                    }
-                    const float mv = metric_value(cfg.relative, cfg.min_val_f, H, L);
-                    m = (c == 0) ? mv : vadd(m, mv);
+                    line_of(t, 0, line, low);
+                    LN[t] = metric_value(cfg.relative, cfg.min_val_f, RefRule<S>::scalar(line), RefRule<SL>::scalar(low));
                 }
-                LN[t] = m;
+            } else {
+                for (int t = gl; t < NT; t += G) {
+                    float m = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        float line[S], low[SL];
+                        line_of(t, c, line, low);
+                        const float mv =
+                            metric_value(cfg.relative, cfg.min_val_f, RefRule<S>::rgb(line), RefRule<SL>::rgb(low));
+                        m = (c == 0) ? mv : vadd(m, mv);
+                    }
+                    LN[t] = m;
+                }
             }
             __syncwarp(gmask);
+            const int nreg = decltype(nreg_c)::value;
             for (int t = gl; t < nreg * DIM; t += G) {
                 const int r = t / DIM;
                 const float folded = fold_all_errors<DIM, S>(LN + t * NL);
@@ -382,7 +408,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
             dim_out = max_dim;
         };
 
-        region_errors(1, 0, 0);
+        region_errors(std::integral_constant<int, 1>{}, 0, 0);
         if (gl == 0) {
             float e;
             int dm;
@@ -494,7 +520,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
             }
             if (gl == 0) {
                 const float pmn = RMIN[P * DIM + dd], pmx = RMAX[P * DIM + dd];
-                const float half = vdiv(vsub(pmx, pmn), 2.0f);
+                const float half = vmul(vsub(pmx, pmn), 0.5f); /* = (max - min) / 2.0, exactly */
                 const float mid = vadd(pmn, vmul(half, 1.0f));
                 float vol0 = 1.0f, vol1 = 1.0f;
 #pragma unroll
@@ -513,7 +539,7 @@ __global__ void __launch_bounds__(NC_THREADS) k_per_bin_nested(const __grid_cons
                 VOL[C1] = vol1;
             }
             __syncwarp(gmask);
-            region_errors(2, C0, C1);
+            region_errors(std::integral_constant<int, 2>{}, C0, C1);
             if (gl == 0) {
                 float e0, e1;
                 int d0, d1;

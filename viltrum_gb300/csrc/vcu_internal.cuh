@@ -239,6 +239,15 @@ struct has_cull<F, std::void_t<typename F::Cull,
                                decltype(std::declval<const F&>().cull((const float*)nullptr, (const float*)nullptr))>>
     : std::true_type {};
 
+/* integrands whose cull decision splits into independent per-term tests (cull_prepare: the box
+ * the tests read; cull_keep(t): term t of the mask's kCullWords 32-bit words; cull_from_words),
+ * so that the lanes of a group can share the terms */
+template <class F, class = void> struct has_cull_terms : std::false_type {};
+template <class F>
+struct has_cull_terms<F, std::void_t<decltype(F::kCullWords), decltype(F::kCullBox),
+                                     decltype(std::declval<const F&>().cull_keep(0, (const float*)nullptr)),
+                                     decltype(F::cull_from_words((const uint32_t*)nullptr))>> : std::true_type {};
+
 /* integrands that list the terms that can be non-zero over a box of their coordinates (cull_box,
  * lo/hi of F::DIM entries) and evaluate with only those -- two points (pair_culled) or one
  * (eval_culled) -- bit for bit what pair() / operator() return at points of the box: the per-bin

@@ -79,7 +79,8 @@ VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
      * (the exact decision does the rest).  For |h| in [2^-90, 2^90] the product by RN(1/D)
      * is close enough; outside that range (subnormal quotients, near overflow) a true division. */
     const float ah = vabs(h);
-    const float q00 = (ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f) ? vmul(h, inv_D) : vdiv(h, D);
+    float q00 = vmul(h, inv_D);
+    if (!(ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f)) q00 = vdiv(h, D);
     const float q0 = vfma(vadd(vfma(-q00, D, h), l), inv_D, q00);
     float s, e;
     two_sum(vfma(-q0, D, h), l, s, e);
@@ -96,38 +97,43 @@ VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
     return ff_div_decide(q0, s, e, D);
 }
 
+/* (p0 + 4.0*p1 + p2)/6.0 and (7.0*p0 + 32.0*p1 + 12.0*p2 + 32.0*p3 + 7.0*p4)/90.0 as the reference
+ * rounds them: error-free float-float sums, then ff_div */
+VCU_HD float ref_simpson(float p0, float p1, float p2) {
+    float h, e1, h2, e2;
+    two_sum(p0, vmul(4.0f, p1), h, e1);
+    two_sum(h, p2, h2, e2);
+    return ff_div(h2, vadd(e1, e2), 6.0f, 0.1666666716337204f /* RN(1/6) */);
+}
+VCU_HD float ref_boole(float p0, float p1, float p2, float p3, float p4) {
+    float h, l, ph, pl, e;
+    two_prod(7.0f, p0, h, l);
+    two_sum(h, vmul(32.0f, p1), h, e);
+    l = vadd(l, e);
+    two_prod(12.0f, p2, ph, pl);
+    two_sum(h, ph, h, e);
+    l = vadd(l, vadd(pl, e));
+    two_sum(h, vmul(32.0f, p3), h, e);
+    l = vadd(l, e);
+    two_prod(7.0f, p4, ph, pl);
+    two_sum(h, ph, h, e);
+    l = vadd(l, vadd(pl, e));
+    return ff_div(h, l, 90.0f, 0.011111111380159855f /* RN(1/90) */);
+}
+
 template <int S> struct RefRule;
 template <> struct RefRule<2> { /* (p0+p1)/2.0: float sum, exact halving */
     static VCU_HD float scalar(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
     static VCU_HD float rgb(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
 };
 template <> struct RefRule<3> { /* (p0 + 4.0*p1 + p2)/6.0 */
-    static VCU_HD float scalar(const float* p) {
-        float h, e1, h2, e2;
-        two_sum(p[0], vmul(4.0f, p[1]), h, e1);
-        two_sum(h, p[2], h2, e2);
-        return ff_div(h2, vadd(e1, e2), 6.0f, 0.1666666716337204f /* RN(1/6) */);
-    }
+    static VCU_HD float scalar(const float* p) { return ref_simpson(p[0], p[1], p[2]); }
     static VCU_HD float rgb(const float* p) {
         return vdiv(vadd(vadd(p[0], vmul(4.0f, p[1])), p[2]), 6.0f);
     }
 };
 template <> struct RefRule<5> { /* (7.0*p0 + 32.0*p1 + 12.0*p2 + 32.0*p3 + 7.0*p4)/90.0 */
-    static VCU_HD float scalar(const float* p) {
-        float h, l, ph, pl, e;
-        two_prod(7.0f, p[0], h, l);
-        two_sum(h, vmul(32.0f, p[1]), h, e);
-        l = vadd(l, e);
-        two_prod(12.0f, p[2], ph, pl);
-        two_sum(h, ph, h, e);
-        l = vadd(l, vadd(pl, e));
-        two_sum(h, vmul(32.0f, p[3]), h, e);
-        l = vadd(l, e);
-        two_prod(7.0f, p[4], ph, pl);
-        two_sum(h, ph, h, e);
-        l = vadd(l, vadd(pl, e));
-        return ff_div(h, l, 90.0f, 0.011111111380159855f /* RN(1/90) */);
-    }
+    static VCU_HD float scalar(const float* p) { return ref_boole(p[0], p[1], p[2], p[3], p[4]); }
     static VCU_HD float rgb(const float* p) {
         const float s = vadd(vadd(vadd(vadd(vmul(7.0f, p[0]), vmul(32.0f, p[1])), vmul(12.0f, p[2])), vmul(32.0f, p[3])),
                              vmul(7.0f, p[4]));

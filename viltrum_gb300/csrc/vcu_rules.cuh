@@ -22,7 +22,19 @@ template <int S> struct Rule;
  * through fdiv_c (the IEEE quotient, see vcu_integrands.h).  subrange01() is subrange(0, 1, p):
  * the antiderivative at 1 with the products by 1 left out, minus the one at 0, which is a zero for
  * finite coefficients -- subtracting it changes at most the sign of a zero result -- so it is
- * evaluated only when the value at 1 is not finite. */
+ * evaluated only when the value at 1 is not finite.  subrange01 divides without fdiv_c's select of
+ * the special operands (G = false): that differs from the IEEE quotient only by the sign of a zero
+ * quotient and by NaN for an infinite operand, so a finite result differs at most in the sign of a
+ * zero, and a non-finite one is recomputed with the selects. */
+template <int D, bool G> __device__ __forceinline__ float div_c(float x) {
+    if constexpr (G) {
+        return fdiv_c<D>(x);
+    } else {
+        constexpr float inv = 1.0f / (float)D;
+        const float q0 = vmul(x, inv);
+        return vfma(vfma(-q0, (float)D, x), inv, q0);
+    }
+}
 template <> struct Rule<2> { /* trapezoidal */
     static __device__ __forceinline__ float rule(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
     static __device__ __forceinline__ void coefficients(const float* p, float* c) {
@@ -70,19 +82,25 @@ template <> struct Rule<3> { /* simpson */
         r = vadd(vmul(r, t), c[0]);
         return vmul(r, t);
     }
-    static __device__ __forceinline__ float horner_int1(const float* c) {
-        return vadd(vadd(fdiv_c<3>(c[2]), vmul(c[1], 0.5f)), c[0]);
+    template <bool G = true> static __device__ __forceinline__ float horner_int1(const float* c) {
+        return vadd(vadd(div_c<3, G>(c[2]), vmul(c[1], 0.5f)), c[0]);
     }
     static __device__ __forceinline__ float subrange(float a, float b, const float* p) {
         float c[3];
         coefficients(p, c);
         return vsub(horner_int(c, b), horner_int(c, a));
     }
+    static __device__ __noinline__ float subrange01_special(float p0, float p1, float p2) {
+        const float p[3] = {p0, p1, p2};
+        float c[3];
+        coefficients(p, c);
+        return vsub(horner_int1(c), horner_int(c, 0.0f));
+    }
     static __device__ __forceinline__ float subrange01(const float* p) {
         float c[3];
         coefficients(p, c);
-        const float h1 = horner_int1(c);
-        return isfinite(h1) ? h1 : vsub(h1, horner_int(c, 0.0f));
+        const float h1 = horner_int1<false>(c);
+        return isfinite(h1) ? h1 : subrange01_special(p[0], p[1], p[2]);
     }
 };
 
@@ -91,20 +109,20 @@ template <> struct Rule<5> { /* boole */
         const float s = vadd(vadd(vmul(7.0f, vadd(p[0], p[4])), vmul(32.0f, vadd(p[1], p[3]))), vmul(12.0f, p[2]));
         return vdiv(s, 90.0f);
     }
-    static __device__ __forceinline__ void coefficients(const float* p, float* c) {
+    template <bool G = true> static __device__ __forceinline__ void coefficients(const float* p, float* c) {
         c[0] = p[0];
-        c[1] = vsub(vadd(vsub(vadd(fdiv_c<3>(vmul(-25.0f, p[0])), vmul(16.0f, p[1])), vmul(12.0f, p[2])),
-                         fdiv_c<3>(vmul(16.0f, p[3]))),
+        c[1] = vsub(vadd(vsub(vadd(div_c<3, G>(vmul(-25.0f, p[0])), vmul(16.0f, p[1])), vmul(12.0f, p[2])),
+                         div_c<3, G>(vmul(16.0f, p[3]))),
                     p[4]);
-        c[2] = vadd(vsub(vadd(vsub(fdiv_c<3>(vmul(70.0f, p[0])), fdiv_c<3>(vmul(208.0f, p[1]))), vmul(76.0f, p[2])),
-                         fdiv_c<3>(vmul(112.0f, p[3]))),
-                    fdiv_c<3>(vmul(22.0f, p[4])));
-        c[3] = vsub(vadd(vsub(vadd(fdiv_c<3>(vmul(-80.0f, p[0])), vmul(96.0f, p[1])), vmul(128.0f, p[2])),
-                         fdiv_c<3>(vmul(224.0f, p[3]))),
+        c[2] = vadd(vsub(vadd(vsub(div_c<3, G>(vmul(70.0f, p[0])), div_c<3, G>(vmul(208.0f, p[1]))), vmul(76.0f, p[2])),
+                         div_c<3, G>(vmul(112.0f, p[3]))),
+                    div_c<3, G>(vmul(22.0f, p[4])));
+        c[3] = vsub(vadd(vsub(vadd(div_c<3, G>(vmul(-80.0f, p[0])), vmul(96.0f, p[1])), vmul(128.0f, p[2])),
+                         div_c<3, G>(vmul(224.0f, p[3]))),
                     vmul(16.0f, p[4]));
-        c[4] = vadd(vsub(vadd(vsub(fdiv_c<3>(vmul(32.0f, p[0])), fdiv_c<3>(vmul(128.0f, p[1]))), vmul(64.0f, p[2])),
-                         fdiv_c<3>(vmul(128.0f, p[3]))),
-                    fdiv_c<3>(vmul(32.0f, p[4])));
+        c[4] = vadd(vsub(vadd(vsub(div_c<3, G>(vmul(32.0f, p[0])), div_c<3, G>(vmul(128.0f, p[1]))), vmul(64.0f, p[2])),
+                         div_c<3, G>(vmul(128.0f, p[3]))),
+                    div_c<3, G>(vmul(32.0f, p[4])));
     }
     static __device__ __forceinline__ float at(float t, const float* p) {
         float c[5];
@@ -121,9 +139,9 @@ template <> struct Rule<5> { /* boole */
         r = vadd(vmul(r, t), c[0]);
         return vmul(r, t);
     }
-    static __device__ __forceinline__ float horner_int1(const float* c) {
-        float r = vadd(fdiv_c<5>(c[4]), vmul(c[3], 0.25f));
-        r = vadd(r, fdiv_c<3>(c[2]));
+    template <bool G = true> static __device__ __forceinline__ float horner_int1(const float* c) {
+        float r = vadd(div_c<5, G>(c[4]), vmul(c[3], 0.25f));
+        r = vadd(r, div_c<3, G>(c[2]));
         r = vadd(r, vmul(c[1], 0.5f));
         return vadd(r, c[0]);
     }
@@ -132,11 +150,17 @@ template <> struct Rule<5> { /* boole */
         coefficients(p, c);
         return vsub(horner_int(c, b), horner_int(c, a));
     }
-    static __device__ __forceinline__ float subrange01(const float* p) {
+    static __device__ __noinline__ float subrange01_special(float p0, float p1, float p2, float p3, float p4) {
+        const float p[5] = {p0, p1, p2, p3, p4};
         float c[5];
         coefficients(p, c);
-        const float h1 = horner_int1(c);
-        return isfinite(h1) ? h1 : vsub(h1, horner_int(c, 0.0f));
+        return vsub(horner_int1(c), horner_int(c, 0.0f));
+    }
+    static __device__ __forceinline__ float subrange01(const float* p) {
+        float c[5];
+        coefficients<false>(p, c);
+        const float h1 = horner_int1<false>(c);
+        return isfinite(h1) ? h1 : subrange01_special(p[0], p[1], p[2], p[3], p[4]);
     }
 };
 
