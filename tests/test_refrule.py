@@ -84,11 +84,14 @@ int main() {
         const double ulp = std::ldexp(1.0, std::ilogb(q) - 23);
         /* the quotient a random offset away from q, or within 2^-18 ulp of a midpoint (the band
          * around it included) */
-        const int mode = (t >> 1) % 4;
+        const int mode = (t >> 1) % 6;
         double delta = off(rng);
         if (mode == 1) delta = 0.5 + std::ldexp(off(rng), -18);
         if (mode == 2) delta = -0.5 + std::ldexp(off(rng), -18);
         if (mode == 3) delta = (t & 2 ? 0.5 : -0.5) + std::ldexp(off(rng), -29);
+        if (mode == 4) delta = (t & 2) ? 0.5 : -0.5;   /* exact ties */
+        if (mode == 5) delta = 0.0;                    /* exact quotients (zeros among them) */
+        if (mode == 5 && (t & 6) == 6) q = 0.0f;
         const double target = ((double)q + delta * ulp) * (double)D;
         const float h = (float)target;
         const float l = (float)(target - (double)h);
@@ -106,8 +109,9 @@ int main() {
 
 
 def test_ff_div_common_case_matches_exact_decision():
-    """ff_div's early return (remainder well inside the half gap) gives the exact decision's result,
-    including quotients within 2^-18 and 2^-29 ulp of a rounding midpoint."""
+    """ff_div's early returns (remainder well inside the half gap, exact ties, exact quotients) give
+    the exact decision's result, including quotients within 2^-18 and 2^-29 ulp of a rounding
+    midpoint, on it, and zero."""
     with tempfile.TemporaryDirectory() as d:
         src = os.path.join(d, "f.cc")
         exe = os.path.join(d, "f")

@@ -76,23 +76,35 @@ VCU_HD float ff_div_decide(float q0, float s, float e, float D) {
  * exact fma residual and l) decides (ff_div_decide). */
 VCU_HD float ff_div(float h, float l, float D, float inv_D /* RN(1/D) */) {
     /* q00 ~ h/D, then one approximate correction step brings q0 within one float of the result
-     * (the exact decision does the rest).  For |h| in [2^-90, 2^90] the product by RN(1/D)
-     * is close enough; outside that range (subnormal quotients, near overflow) a true division. */
+     * (the exact decision does the rest).  For h = 0 or |h| in [2^-90, 2^90] the product by
+     * RN(1/D) is close enough; outside that range (subnormal quotients, near overflow) a true
+     * division. */
     const float ah = vabs(h);
     float q00 = vmul(h, inv_D);
-    if (!(ah >= 8.077935669463161e-28f && ah <= 1.2379400392853803e27f)) q00 = vdiv(h, D);
+    if (!((ah >= 8.077935669463161e-28f || ah == 0.0f) && ah <= 1.2379400392853803e27f)) q00 = vdiv(h, D);
     const float q0 = vfma(vadd(vfma(-q00, D, h), l), inv_D, q00);
     float s, e;
     two_sum(vfma(-q0, D, h), l, s, e);
-    /* Common case first: q0 normal, not a power of two (both neighbours one ulp away, so the
-     * half gaps tu = td = D ulp / 2) and |s| below tu (1 - 2^-20), with |e| <= 2^-24 |s|: then R/D
-     * is farther than 2^-21 ulp from either midpoint, outside the tie band, and ff_div_decide returns
-     * q0.  The threshold RN(D (1 - 2^-20) / 2) ulp is within 2^-24 of that bound. */
+    /* Common cases first, with ff_div_decide's results.  q0 normal, not a power of two (both
+     * neighbours one ulp away, so the half gaps tu = td = D ulp / 2):
+     *  - |s| below tu (1 - 2^-20), with |e| <= 2^-24 |s|: R/D is farther than 2^-21 ulp from either
+     *    midpoint, outside the tie band: q0.  (The threshold RN(D (1 - 2^-20) / 2) ulp is within
+     *    2^-24 of that bound.)
+     *  - R = +-tu exactly (e = 0): an exact tie, to the even neighbour -- frequent for Simpson's
+     *    (p0 + 4 p1 + p2) / 6, whose numerator often has one bit more than a multiple of 3.
+     * Any q0 with R = 0 (s = e = 0): the quotient is exact. */
     const uint32_t u = float_to_bits(q0);
     const uint32_t ex = u & 0x7f800000u;
     if ((u & 0x007fffffu) != 0u && ex >= (25u << 23) && ex < (254u << 23)) {
         const float ulp = bits_to_float(ex - (23u << 23));
-        if (vabs(s) <= vmul(ulp, vmul(D, 0.49999952316284180f /* (1 - 2^-20) / 2 */))) return q0;
+        const float as = vabs(s);
+        if (as <= vmul(ulp, vmul(D, 0.49999952316284180f /* (1 - 2^-20) / 2 */))) return q0;
+        if (e == 0.0f && as == vmul(vmul(D, 0.5f), ulp)) {
+            if ((u & 1u) == 0u) return q0;
+            return bits_to_float(((s > 0.0f) == (q0 > 0.0f)) ? u + 1u : u - 1u); /* the neighbour on R's side */
+        }
+    } else if (s == 0.0f && e == 0.0f) {
+        return q0;
     }
     return ff_div_decide(q0, s, e, D);
 }
