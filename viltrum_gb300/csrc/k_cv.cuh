@@ -11,7 +11,8 @@
  *     src/nested/regions-generator-adaptive-heap.h:18-45 builds it (same split choices: error
  *     estimates with the reference's rounding, libstdc++ heap order).  From 128 splits on, in waves
  *     (wave_launch, below): the regions of largest bottleneck error are split together, one warp per
- *     region, and the host replays the heap sequence on their errors.  Below that, or when the waves
+ *     region, the waves decided on the device, and the host replays the heap sequence on their
+ *     errors.  Below that, or when the waves
  *     give up (NaN errors, a pool overflow from masses of equal errors), k_cv_generate: ONE
  *     cooperative thread block splitting in order, the heap in shared memory (up to ~28k regions) or
  *     global memory, each split's new nodes and both children's error folds evaluated by the block
@@ -1764,13 +1765,27 @@ int tol_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g,
  * replays the reference's exact heap sequence (libstdc++ push/pop, vcu_heap.h) on the computed
  * errors, which fixes the final heap order (the order regions are integrated in) and resolves ties
  * exactly; a region that sequence pops but no wave split sends the waves further.  The result is the
- * sequential generator's, region for region and position for position. */
+ * sequential generator's, region for region and position for position.  Which regions a wave
+ * splits (and whether the waves are done) is decided on the device between waves (k_wave_decide),
+ * so waves run back to back and the host reads the loop's state once every WAVE_CHUNK waves. */
 constexpr int WAVE_WARPS = 4;
 constexpr int WAVE_SHIFT = 19;                      /* bucket = bits(b) >> 19: 4096 buckets */
 constexpr int WAVE_BUCKETS = 1 << (31 - WAVE_SHIFT);
 /* counters: */
 enum { WC_POOL = 0, WC_NEW = 1, WC_EXPAND = 2, WC_FRONT2 = 3, WC_SPLIT = 4, WC_MAXB = 5, WC_GE = 6, WC_NAN = 7,
        WC_FRONT = 8, WC_OVF = 9, WC_N = 16 };
+
+/* The wave loop's state, decided on the device between waves (k_wave_decide): the host launches
+ * waves back to back and reads it back once every WAVE_CHUNK waves. */
+struct WaveCtl {
+    uint32_t state; /* WAVE_ACTIVE, WAVE_DONE (the split set is complete), WAVE_FAIL (sequential generator) */
+    uint32_t thr;   /* this wave's bucket threshold */
+    uint32_t cur;   /* the unsplit regions' list: 0 -> the first list, 1 -> the second */
+    uint32_t waves; /* waves decided so far */
+};
+enum : uint32_t { WAVE_ACTIVE = 0, WAVE_DONE = 1, WAVE_FAIL = 2 };
+constexpr int WAVE_CHUNK = 8;
+constexpr uint32_t WAVE_NO_FORCE = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t wave_bits(float b) {
     const uint32_t u = __float_as_uint(b);
@@ -1783,34 +1798,41 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
     k_wave_eval(const TolCfg cfg, const int* __restrict__ list, const uint32_t* __restrict__ nlist,
                 const float* __restrict__ vals, const float* __restrict__ rmin, const float* __restrict__ rmax,
                 const float* __restrict__ vol, const int* __restrict__ parent, float* __restrict__ key,
-                int* __restrict__ kdim, float* __restrict__ bneck, uint32_t* __restrict__ ctr) {
+                int* __restrict__ kdim, float* __restrict__ bneck, uint32_t* __restrict__ ctr,
+                const WaveCtl* __restrict__ ctl) {
     constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM), NL = ipow(S, DIM - 1);
     __shared__ float LN[WAVE_WARPS][DIM * NL];
     __shared__ float EC[WAVE_WARPS][DIM];
+    if (ctl->state != WAVE_ACTIVE) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t w = blockIdx.x * WAVE_WARPS + warp;
-    if (w >= *nlist) return;
-    const int id = list[w];
-    float e;
-    int dm;
-    warp_heuristic<DIM, S, SL, CH>(cfg, vals + (size_t)id * SD * CH, vol[id], rmin + (size_t)id * DIM,
-                                   rmax + (size_t)id * DIM, LN[warp], EC[warp], lane, e, dm);
-    if (lane == 0) {
-        key[id] = e;
-        kdim[id] = dm;
-        const int par = parent[id];
-        const float bp = par < 0 ? e : bneck[par];
-        bneck[id] = (e < bp) ? e : bp;
-        if (isnan(e)) atomicOr(&ctr[WC_NAN], 1u);
+    const uint32_t n = *nlist;
+    for (uint32_t w = blockIdx.x * WAVE_WARPS + warp; w < n; w += gridDim.x * WAVE_WARPS) {
+        const int id = list[w];
+        float e;
+        int dm;
+        warp_heuristic<DIM, S, SL, CH>(cfg, vals + (size_t)id * SD * CH, vol[id], rmin + (size_t)id * DIM,
+                                       rmax + (size_t)id * DIM, LN[warp], EC[warp], lane, e, dm);
+        if (lane == 0) {
+            key[id] = e;
+            kdim[id] = dm;
+            const int par = parent[id];
+            const float bp = par < 0 ? e : bneck[par];
+            bneck[id] = (e < bp) ? e : bp;
+            if (isnan(e)) atomicOr(&ctr[WC_NAN], 1u);
+        }
+        __syncwarp();
     }
 }
 
 /* the largest b of the unsplit regions, and their histogram of b; the count of split regions with
  * b >= that largest b comes next (k_wave_count) */
-static __global__ void k_wave_stats(const int* __restrict__ front, const uint32_t* __restrict__ nfront,
-                                    const float* __restrict__ bneck, uint32_t* __restrict__ ctr,
-                                    uint32_t* __restrict__ hist) {
+static __global__ void k_wave_stats(const int* __restrict__ fa, const int* __restrict__ fb,
+                                    const uint32_t* __restrict__ nfront, const float* __restrict__ bneck,
+                                    uint32_t* __restrict__ ctr, uint32_t* __restrict__ hist,
+                                    const WaveCtl* __restrict__ ctl) {
     __shared__ uint32_t h[WAVE_BUCKETS];
+    if (ctl->state != WAVE_ACTIVE) return;
+    const int* __restrict__ front = ctl->cur ? fb : fa;
     for (int i = threadIdx.x; i < WAVE_BUCKETS; i += blockDim.x) h[i] = 0;
     __syncthreads();
     const uint32_t n = *nfront;
@@ -1827,7 +1849,9 @@ static __global__ void k_wave_stats(const int* __restrict__ front, const uint32_
 }
 
 static __global__ void k_wave_count(const int* __restrict__ split, const uint32_t* __restrict__ nsplit,
-                                    const float* __restrict__ bneck, uint32_t* __restrict__ ctr) {
+                                    const float* __restrict__ bneck, uint32_t* __restrict__ ctr,
+                                    const WaveCtl* __restrict__ ctl) {
+    if (ctl->state != WAVE_ACTIVE) return;
     const uint32_t n = *nsplit, m = ctr[WC_MAXB];
     uint32_t c = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -1838,9 +1862,14 @@ static __global__ void k_wave_count(const int* __restrict__ split, const uint32_
 
 /* the unsplit regions whose b lies in bucket >= thr are split this wave (and recorded as split);
  * the others stay unsplit */
-static __global__ void k_wave_select(const int* __restrict__ front, const uint32_t* __restrict__ nfront,
-                                     const float* __restrict__ bneck, uint32_t thr, int* __restrict__ expand,
-                                     int* __restrict__ front2, int* __restrict__ split, uint32_t* __restrict__ ctr) {
+static __global__ void k_wave_select(int* __restrict__ fa, int* __restrict__ fb, const uint32_t* __restrict__ nfront,
+                                     const float* __restrict__ bneck, int* __restrict__ expand,
+                                     int* __restrict__ split, uint32_t* __restrict__ ctr,
+                                     const WaveCtl* __restrict__ ctl) {
+    if (ctl->state != WAVE_ACTIVE) return;
+    const int* __restrict__ front = ctl->cur ? fb : fa;
+    int* __restrict__ front2 = ctl->cur ? fa : fb;
+    const uint32_t thr = ctl->thr;
     const uint32_t n = *nfront;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int id = front[i];
@@ -1853,6 +1882,100 @@ static __global__ void k_wave_select(const int* __restrict__ front, const uint32
     }
 }
 
+/* The host loop's decision between two waves, on the device (one block of 1024 threads): stop when
+ * the pool overflowed or an error is NaN (the sequential generator takes over), or when the split set
+ * is complete (no unsplit region, or `iters` split regions with b >= the largest unsplit b, unless a
+ * forced bucket is still above it); otherwise split the unsplit regions of the top buckets, as many
+ * as still needed -- the bucket where the count from the top reaches them -- but none more than two
+ * octaves below the largest b, nor above a forced bucket. */
+constexpr int DECIDE_THREADS = 1024;
+static __global__ void __launch_bounds__(DECIDE_THREADS)
+    k_wave_decide(uint32_t* __restrict__ ctr, const uint32_t* __restrict__ hist, WaveCtl* __restrict__ ctl,
+                  uint32_t iters, uint32_t capacity, uint32_t force) {
+    constexpr int PER = WAVE_BUCKETS / DECIDE_THREADS;
+    __shared__ uint32_t part[DECIDE_THREADS];
+    __shared__ uint32_t best;
+    if (ctl->state != WAVE_ACTIVE) return;
+    const int t = threadIdx.x;
+    const uint32_t nfront = ctr[WC_FRONT], ge = ctr[WC_GE], maxb = ctr[WC_MAXB] >> WAVE_SHIFT;
+    const bool forced = force != WAVE_NO_FORCE && maxb >= force;
+    const bool fail = ctr[WC_OVF] != 0u || ctr[WC_NAN] != 0u || ctl->waves > 100000u;
+    const bool done = nfront == 0u || (ge >= iters && !forced);
+    if (fail || done) {
+        __syncthreads();
+        if (t == 0) ctl->state = fail ? WAVE_FAIL : WAVE_DONE;
+        return;
+    }
+    const uint32_t need = ge >= iters ? 1u : iters - ge;
+    /* suffix counts: part[t] = this thread's buckets, then the count above them */
+    uint32_t local[PER], sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        local[k] = hist[t * PER + k];
+        sum += local[k];
+    }
+    part[t] = sum;
+    if (t == 0) best = 0u;
+    __syncthreads();
+    for (int off = 1; off < DECIDE_THREADS; off <<= 1) { /* inclusive suffix scan over threads */
+        const uint32_t v = (t + off < DECIDE_THREADS) ? part[t + off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t suffix = part[t] - sum; /* buckets above this thread's */
+    uint32_t cand = 0u;
+    bool found = false;
+#pragma unroll
+    for (int k = PER - 1; k >= 0; --k) {
+        suffix += local[k];
+        if (!found && suffix >= need) {
+            found = true;
+            cand = (uint32_t)(t * PER + k);
+        }
+    }
+    if (found) atomicMax(&best, cand);
+    __syncthreads();
+    if (t == 0) {
+        uint32_t thr = best; /* 0 when the unsplit regions number fewer than needed */
+        const uint32_t octave2 = 2u * (1u << (23 - WAVE_SHIFT));
+        const uint32_t floor_bkt = maxb > octave2 ? maxb - octave2 : 0u;
+        if (thr < floor_bkt) thr = floor_bkt;
+        if (forced && force < thr) thr = force;
+        ctl->thr = thr;
+        ctl->waves += 1u;
+    }
+    __syncthreads();
+    /* the regions this wave splits: the unsplit ones in buckets >= thr (the suffix count at thr) */
+    const uint32_t thr = ctl->thr;
+    uint32_t acc = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k)
+        if ((uint32_t)(t * PER + k) >= thr) acc += local[k];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __syncthreads();
+    if ((t & 31) == 0) part[t >> 5] = acc;
+    __syncthreads();
+    if (t == 0) {
+        uint64_t total = 0;
+        for (int w = 0; w < DECIDE_THREADS / 32; ++w) total += part[w];
+        if ((uint64_t)ctr[WC_POOL] + 2ull * total > capacity) {
+            ctl->state = WAVE_FAIL;
+        } else {
+            ctr[WC_NEW] = 0u;
+            ctr[WC_EXPAND] = 0u;
+            ctr[WC_FRONT2] = 0u;
+        }
+    }
+}
+
+/* after a wave: the new unsplit list becomes the current one */
+static __global__ void k_wave_swap(uint32_t* __restrict__ ctr, WaveCtl* __restrict__ ctl) {
+    if (ctl->state != WAVE_ACTIVE) return;
+    ctr[WC_FRONT] = ctr[WC_FRONT2];
+    ctl->cur ^= 1u;
+}
+
 /* split the selected regions along their heuristic dimension; the halves join the unsplit list
  * and the list whose errors are computed next */
 template <class F, int DIM, int SH>
@@ -1860,12 +1983,15 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
     k_wave_split(const __grid_constant__ F f, const int* __restrict__ expand, const uint32_t* __restrict__ nexpand,
                  const int* __restrict__ kdim, uint32_t capacity, float* __restrict__ vals, float* __restrict__ rmin,
                  float* __restrict__ rmax, float* __restrict__ vol, int* __restrict__ child, int* __restrict__ parent,
-                 int* __restrict__ fresh, int* __restrict__ front2, uint32_t* __restrict__ ctr) {
+                 int* __restrict__ fresh, int* __restrict__ fa, int* __restrict__ fb, uint32_t* __restrict__ ctr,
+                 const WaveCtl* __restrict__ ctl) {
     constexpr int S = SH, CH = F::CH, SD = ipow(S, DIM);
     __shared__ float CO[WAVE_WARPS][DIM * S], CN[WAVE_WARPS][S - 1];
+    if (ctl->state != WAVE_ACTIVE) return;
+    int* __restrict__ front2 = ctl->cur ? fa : fb;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t w = blockIdx.x * WAVE_WARPS + warp;
-    if (w >= *nexpand) return;
+    const uint32_t n = *nexpand;
+    for (uint32_t w = blockIdx.x * WAVE_WARPS + warp; w < n; w += gridDim.x * WAVE_WARPS) {
     const int id = expand[w];
     int c0 = -1;
     if (lane == 0) {
@@ -1888,9 +2014,11 @@ __global__ void __launch_bounds__(WAVE_WARPS * 32)
         }
     }
     c0 = __shfl_sync(0xffffffffu, c0, 0);
-    if (c0 < 0) return;
+    if (c0 < 0) continue;
     warp_split<F, DIM, S>(f, vals + (size_t)id * SD * CH, id, kdim[id], c0, vals, rmin, rmax, vol, CO[warp], CN[warp],
                           lane);
+    __syncwarp();
+    }
 }
 
 template <int DIM, int SH, int SL, class F>
@@ -1917,7 +2045,8 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
                  o_vol = take(cap * 4), o_key = take(cap * 4), o_kdim = take(cap * 4), o_b = take(cap * 4),
                  o_par = take(cap * 4), o_child = take(cap * 4), o_fa = take(cap * 4), o_fb = take(cap * 4),
                  o_exp = take(cap * 4), o_split = take(cap * 4), o_fresh = take(cap * 4), o_hp = take((N + 1) * 4),
-                 o_ctr = take(WC_N * 4), o_hist = take(WAVE_BUCKETS * 4), o_cnt = take(g.nbins * 4),
+                 o_ctr = take(WC_N * 4), o_ctl = take(sizeof(WaveCtl)), o_hist = take(WAVE_BUCKETS * 4),
+                 o_cnt = take(g.nbins * 4),
                  o_off = take((g.nbins + 1) * 4), o_cur = take(g.nbins * 4);
     int rc = ensure(ctx, ctx->scratch, o);
     if (rc) return rc;
@@ -1968,72 +2097,47 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
         VCU_CUDA(ctx, cudaMemcpyAsync(parent, root + 1, 4, cudaMemcpyHostToDevice, ctx->stream));
         VCU_CUDA(ctx, cudaMemcpyAsync(child, root + 2, 4, cudaMemcpyHostToDevice, ctx->stream));
     }
+    WaveCtl* ctl = reinterpret_cast<WaveCtl*>(base + o_ctl);
+    {
+        const WaveCtl c0{WAVE_ACTIVE, 0u, 0u, 0u};
+        VCU_CUDA(ctx, cudaMemcpyAsync(ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice, ctx->stream));
+    }
     k_wave_eval<F, DIM, SH, SL><<<1, WAVE_WARPS * 32, 0, ctx->stream>>>(tc, fresh, ctr + WC_NEW, vals, rmin, rmax, vol,
-                                                                      parent, key, kdim, bneck, ctr);
+                                                                      parent, key, kdim, bneck, ctr, ctl);
     launches += 2;
-    int* front = fa;
-    int* front2 = fb;
-    uint32_t nfront = 1;
-    std::vector<uint32_t> h(WAVE_BUCKETS);
     std::vector<float> hkey, hb;
     std::vector<int> hdim, hchild;
     std::vector<float> HE(N + 1);
     std::vector<int> HS(N + 1);
-    uint32_t force = 0xffffffffu; /* after an incomplete replay: split every unsplit b bucket >= force */
+    uint32_t force = WAVE_NO_FORCE; /* after an incomplete replay: split every unsplit b bucket >= force */
+    /* fixed grids (the kernels loop over their lists, whose lengths stay on the device) */
+    const unsigned gstat = (unsigned)ctx->sm_count * 4;
+    const unsigned gsplit = (unsigned)ctx->sm_count * 8, geval = (unsigned)ctx->sm_count * 16;
     for (int round = 0; round < 8; ++round) {
-        /* waves */
-        for (int wave = 0;; ++wave) {
-            if (wave > 100000) return -1;
-            VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_MAXB, 0, 8, ctx->stream));
-            VCU_CUDA(ctx, cudaMemsetAsync(hist, 0, WAVE_BUCKETS * 4, ctx->stream));
-            const unsigned sb = (unsigned)std::min<size_t>((nfront + 255) / 256, (size_t)ctx->sm_count * 4);
-            k_wave_stats<<<sb ? sb : 1, 256, 0, ctx->stream>>>(front, ctr + WC_FRONT, bneck, ctr, hist);
-            k_wave_count<<<(unsigned)ctx->sm_count * 4, 256, 0, ctx->stream>>>(split, ctr + WC_SPLIT, bneck, ctr);
-            launches += 2;
-            uint32_t hc[WC_N];
-            VCU_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
-            VCU_CUDA(ctx, cudaMemcpyAsync(h.data(), hist, WAVE_BUCKETS * 4, cudaMemcpyDeviceToHost, ctx->stream));
-            VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            if (hc[WC_OVF] || hc[WC_NAN]) return -1; /* pool too small, or NaN errors: the sequential generator */
-            nfront = hc[WC_FRONT];
-            const uint32_t ge = hc[WC_GE];
-            const uint32_t maxb = hc[WC_MAXB] >> WAVE_SHIFT;
-            if (nfront == 0) break;
-            const bool forced = force != 0xffffffffu && maxb >= force;
-            if (ge >= N && !forced) break;
-            /* split the unsplit regions of the top buckets, as many as still needed */
-            const uint32_t need = ge >= N ? 1u : (uint32_t)(N - ge);
-            uint32_t thr = 0, acc = 0;
-            for (int bkt = WAVE_BUCKETS - 1; bkt >= 0; --bkt) {
-                acc += h[bkt];
-                if (acc >= need) {
-                    thr = (uint32_t)bkt;
-                    break;
-                }
+        /* waves, WAVE_CHUNK at a time without a host round trip: the device decides between waves
+         * (k_wave_decide) and every kernel of a wave after the last returns at once */
+        for (;;) {
+            for (int wave = 0; wave < WAVE_CHUNK; ++wave) {
+                VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_MAXB, 0, 8, ctx->stream));
+                VCU_CUDA(ctx, cudaMemsetAsync(hist, 0, WAVE_BUCKETS * 4, ctx->stream));
+                k_wave_stats<<<gstat, 256, 0, ctx->stream>>>(fa, fb, ctr + WC_FRONT, bneck, ctr, hist, ctl);
+                k_wave_count<<<gstat, 256, 0, ctx->stream>>>(split, ctr + WC_SPLIT, bneck, ctr, ctl);
+                k_wave_decide<<<1, DECIDE_THREADS, 0, ctx->stream>>>(ctr, hist, ctl, (uint32_t)N, (uint32_t)cap, force);
+                k_wave_select<<<gstat, 256, 0, ctx->stream>>>(fa, fb, ctr + WC_FRONT, bneck, expand, split, ctr, ctl);
+                k_wave_split<F, DIM, SH><<<gsplit, WAVE_WARPS * 32, 0, ctx->stream>>>(
+                    f, expand, ctr + WC_EXPAND, kdim, (uint32_t)cap, vals, rmin, rmax, vol, child, parent, fresh, fa, fb,
+                    ctr, ctl);
+                k_wave_eval<F, DIM, SH, SL><<<geval, WAVE_WARPS * 32, 0, ctx->stream>>>(
+                    tc, fresh, ctr + WC_NEW, vals, rmin, rmax, vol, parent, key, kdim, bneck, ctr, ctl);
+                k_wave_swap<<<1, 1, 0, ctx->stream>>>(ctr, ctl);
+                launches += 7;
             }
-            /* and only those within a factor 4 of the largest b (two octaves of buckets): a wave splits
-             * nothing far below what the sequence is splitting now, so the tree does not grow
-             * breadth-first into regions the sequence never reaches */
-            const uint32_t floor_bkt = maxb > 2u * (1u << (23 - WAVE_SHIFT)) ? maxb - 2u * (1u << (23 - WAVE_SHIFT)) : 0u;
-            if (thr < floor_bkt) thr = floor_bkt;
-            if (forced && force < thr) thr = force;
-            acc = 0;
-            for (uint32_t bkt = thr; bkt < (uint32_t)WAVE_BUCKETS; ++bkt) acc += h[bkt];
-            if (hc[WC_POOL] + 2ull * acc > cap) return -1;
-            VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_NEW, 0, 12, ctx->stream)); /* NEW, EXPAND, FRONT2 */
-            const unsigned gb = (unsigned)((nfront + 255) / 256);
-            k_wave_select<<<gb, 256, 0, ctx->stream>>>(front, ctr + WC_FRONT, bneck, thr, expand, front2, split, ctr);
-            const unsigned wb = (unsigned)((nfront + WAVE_WARPS - 1) / WAVE_WARPS);
-            k_wave_split<F, DIM, SH><<<wb, WAVE_WARPS * 32, 0, ctx->stream>>>(
-                f, expand, ctr + WC_EXPAND, kdim, (uint32_t)cap, vals, rmin, rmax, vol, child, parent, fresh, front2, ctr);
-            const unsigned eb = (unsigned)((2 * (size_t)nfront + WAVE_WARPS - 1) / WAVE_WARPS);
-            k_wave_eval<F, DIM, SH, SL><<<eb, WAVE_WARPS * 32, 0, ctx->stream>>>(tc, fresh, ctr + WC_NEW, vals, rmin, rmax,
-                                                                               vol, parent, key, kdim, bneck, ctr);
-            VCU_CUDA(ctx, cudaMemcpyAsync(ctr + WC_FRONT, ctr + WC_FRONT2, 4, cudaMemcpyDeviceToDevice, ctx->stream));
-            launches += 3;
             VCU_CUDA(ctx, cudaGetLastError());
-            std::swap(front, front2);
-            nfront = nfront * 3; /* upper bound until the next read */
+            WaveCtl hc{};
+            VCU_CUDA(ctx, cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+            VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (hc.state == WAVE_FAIL) return -1; /* pool too small, or NaN errors: the sequential generator */
+            if (hc.state == WAVE_DONE) break;
         }
         /* replay the reference's heap sequence on the computed errors */
         uint32_t pool = 0;
@@ -2080,6 +2184,8 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
         std::memcpy(&u, &hb[missing], 4);
         if (u & 0x80000000u) u = 0;
         force = u >> WAVE_SHIFT;
+        const uint32_t active = WAVE_ACTIVE;
+        VCU_CUDA(ctx, cudaMemcpyAsync(&ctl->state, &active, 4, cudaMemcpyHostToDevice, ctx->stream));
     }
     return -1;
 }
