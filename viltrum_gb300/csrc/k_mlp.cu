@@ -22,8 +22,6 @@
  *     variate's estimate where its variance is lower.
  */
 #include <algorithm>
-#include <cstdlib>
-#include <cstring>
 
 #include "k_mlp.cuh"
 #include "k_mlp_tc.cuh"
@@ -332,18 +330,6 @@ __global__ void __launch_bounds__(TRAIN_WARPS * 32, 1)
     }
 }
 
-/* one training step's forward and backward on tcgen05 (tc::train_tiles) */
-template <int D>
-__global__ void __launch_bounds__(tc::THREADS, 1)
-    k_mlp_train_tc(const TrainCfg cfg, const char* __restrict__ packed, float* __restrict__ partial,
-                   uint32_t* __restrict__ status) {
-    tc::train_tiles<D>(cfg.u_in, cfg.y_in, cfg.npts, cfg.rounds, cfg.scale, cfg.out, packed, partial, status);
-}
-static bool use_mma_train() { /* temporary comparison switch */
-    const char* e = std::getenv("VCU_MLP_TRAIN");
-    return e && std::strcmp(e, "mma") == 0;
-}
-
 /* grad[i] = sum over blocks of partial[b][i], in block order */
 template <int D>
 __global__ void k_mlp_reduce(const float* __restrict__ partial, int nparts, float* __restrict__ grad) {
@@ -380,7 +366,6 @@ template <int D> __device__ __forceinline__ void pack_param(char* packed, int p,
             const __nv_bfloat16 b = __float2bfloat16_rn(v);
             bf[t_off(l, D) + n * (in + PAD) + k] = b;
             bf[n_off(l, D) + k * (WIDTH + PAD) + n] = b;
-            tc::pack_tc_weight<D>(packed, l, k, n, b);
             return;
         }
         if (p >= b_off(l, D) && p < b_off(l, D) + WIDTH) {
@@ -863,7 +848,7 @@ template <int D> int alloc_state(vcu_ctx* ctx, uint64_t nparts, size_t node_floa
         o = (o + bytes + 255) & ~size_t(255);
         return at;
     };
-    const size_t o_theta = a(np * 4), o_m = a(np * 4), o_v = a(np * 4), o_g = a(ng * 4), o_p = a(tc::packed_total_bytes<D>()),
+    const size_t o_theta = a(np * 4), o_m = a(np * 4), o_v = a(np * 4), o_g = a(ng * 4), o_p = a(pack_bytes(D)),
                  o_s = a(64), o_c = a(64), o_h = a(HELDOUT_BLOCKS * 8), o_pt = a(nparts * ng * 4),
                  o_n = a(node_floats * 4);
     int rc = ensure(ctx, ctx->scratch, o);
@@ -888,7 +873,7 @@ template <int D> int upload_params(vcu_ctx* ctx, const State& s, const float* th
     VCU_CUDA(ctx, cudaMemsetAsync(s.m, 0, np * 4, ctx->stream));
     VCU_CUDA(ctx, cudaMemsetAsync(s.v, 0, np * 4, ctx->stream));
     VCU_CUDA(ctx, cudaMemsetAsync(s.grad, 0, np * 4, ctx->stream));
-    VCU_CUDA(ctx, cudaMemsetAsync(s.packed, 0, tc::packed_total_bytes<D>(), ctx->stream));
+    VCU_CUDA(ctx, cudaMemsetAsync(s.packed, 0, pack_bytes(D), ctx->stream));
     VCU_CUDA(ctx, cudaMemsetAsync(s.step, 0, 64, ctx->stream));
     static const float one = 1.0f; /* the learning-rate scale starts at 1 */
     VCU_CUDA(ctx, cudaMemcpyAsync(s.step + 2, &one, 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -902,10 +887,6 @@ template <int D> int set_smem_train(vcu_ctx* ctx) {
     const int tb = train_smem_bytes<D>();
     if ((size_t)tb > ctx->smem_optin) return fail(ctx, VCU_UNSUPPORTED, "training block does not fit in shared memory");
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_train<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb));
-    if ((size_t)tc::TrainSmem<D>::BYTES > ctx->smem_optin)
-        return fail(ctx, VCU_UNSUPPORTED, "training CTA does not fit in shared memory");
-    VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_train_tc<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       tc::TrainSmem<D>::BYTES));
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_nodes<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        smem_fwd_bytes<D>()));
     VCU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_heldout<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1009,12 +990,8 @@ int learned(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g, co
         cudaGraphExec_t exec = nullptr;
         VCU_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         k_mlp_samples<F, D><<<(unsigned)((batch + 255) / 256), 256, 0, ctx->stream>>>(f, tc, batch, su, sy, s.step);
-        if (use_mma_train())
-            k_mlp_train<D><<<train_blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed,
-                                                                                                    s.partial);
-        else
-            k_mlp_train_tc<D><<<train_blocks, tc::THREADS, tc::TrainSmem<D>::BYTES, ctx->stream>>>(
-                tc, s.packed, s.partial, ctx->d_status);
+        k_mlp_train<D><<<train_blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed,
+                                                                                                s.partial);
         k_mlp_adam<D><<<(unsigned)((n_params(D) + 255) / 256), 256, 0, ctx->stream>>>(ac, s.theta, s.m, s.v, s.partial,
                                                                                        s.step, s.packed);
         k_mlp_step_inc<<<1, 1, 0, ctx->stream>>>(s.step);
@@ -1168,11 +1145,7 @@ int eval_grad(vcu_ctx* ctx, const float* theta, const float* u, const float* y, 
     tc.out = dout;
     tc.npts = (uint64_t)npts;
     tc.scale = (float)(2.0 / (double)npts);
-    if (use_mma_train())
-        k_mlp_train<D><<<blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.partial);
-    else
-        k_mlp_train_tc<D><<<blocks, tc::THREADS, tc::TrainSmem<D>::BYTES, ctx->stream>>>(tc, s.packed, s.partial,
-                                                                                          ctx->d_status);
+    k_mlp_train<D><<<blocks, TRAIN_WARPS * 32, train_smem_bytes<D>(), ctx->stream>>>(tc, s.packed, s.partial);
     ++launches;
     VCU_CUDA(ctx, cudaGetLastError());
     k_mlp_reduce<D><<<(unsigned)((n_params(D) + 255) / 256), 256, 0, ctx->stream>>>(s.partial, (int)blocks, s.grad);

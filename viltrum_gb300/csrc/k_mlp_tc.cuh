@@ -255,352 +255,6 @@ __device__ __forceinline__ void forward_points(const char* __restrict__ packed, 
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
-/* ---------------------------------------------------------------- training on tcgen05
- * One training step's forward and backward over `rounds` tiles of 128 points per CTA, two tiles at
- * a time (thread t owns row t of both), every product on the tensor cores (M = 128, N = 64, BF16
- * operands in shared memory, FP32 accumulators in TMEM):
- *   forward   z_l = a_l W_l          A = a_l [point][input], B = W_l [unit][input], both K-major
- *   backward  da_l = dz_l W_l^T      A = dz_l [point][unit] K-major, B = W_l read MN-major
- *             dW_l += a_l^T dz_l     A = a_l, B = dz_l, both read MN-major
- *             db_l += 1^T dz_l       A = ones (one 8-row group repeated: stride 0), B = dz_l MN-major
- * A K-major [row][col] tile read MN-major is the [col][row] operand, so nothing is transposed in
- * shared memory.  The dW MMA's rows past a layer's inputs read other rows of the tile and are
- * discarded.  dW_l of the four layers and db_l accumulate in TMEM over the CTA's tiles and are read
- * once at the end; the output layer's gradients are FP32 sums in shared memory.  Each phase issues
- * both tiles' MMAs and waits once.  Rounding points are the mma.sync kernels': BF16 features and
- * activations, dz rounded to BF16 before its products, FP32 accumulation.  The CTA writes its
- * gradient to partial[block] in the training kernels' order (W0..W3 rows by input, b0..b3, w4, b4). */
-constexpr int PAIR = 2; /* tiles in flight per CTA */
-template <int D> struct TrainSmem {
-    static constexpr int K0 = fin(D);
-    static constexpr int W0 = 0;                              /* [unit][input] weights, K-major */
-    static constexpr int W1 = W0 + MMA_N * K0 * 2;
-    static constexpr int W2 = W1 + MMA_N * WIDTH * 2;
-    static constexpr int W3 = W2 + MMA_N * WIDTH * 2;
-    static constexpr int F = W3 + MMA_N * WIDTH * 2;          /* features: PAIR x 128 x K0 */
-    static constexpr int H1 = F + PAIR * TILE * K0 * 2;       /* hidden activations: PAIR x 128 x 64 */
-    static constexpr int H2 = H1 + PAIR * TILE * WIDTH * 2;
-    static constexpr int H3 = H2 + PAIR * TILE * WIDTH * 2;
-    static constexpr int DZ = H3 + PAIR * TILE * WIDTH * 2;   /* dz_l (h4 before dz_3): PAIR x 128 x 64 */
-    static constexpr int ONES = DZ + PAIR * TILE * WIDTH * 2; /* 8 rows x 128 ones */
-    static constexpr int P32 = ONES + 8 * TILE * 2 + 2048;    /* bias[4][64], w4[64], b4 (after a pad) */
-    static constexpr int ACC = P32 + (5 * WIDTH + 4) * 4;     /* dw4[64], db4 */
-    static constexpr int DV = ACC + (5 * WIDTH + 4) * 4;      /* the tiles' output gradients */
-    static constexpr int MBAR = DV + PAIR * TILE * 4;
-    static constexpr int SLOT = MBAR + 8;
-    static constexpr int FLAG = SLOT + 4;
-    static constexpr int BYTES = FLAG + 4;
-    static constexpr int TCOLS = 512; /* temp 0-127 (64 per tile), dW_l at 128 + 64 l, db 384-447 */
-    static_assert(W1 % 16 == 0 && F % 16 == 0 && ONES % 16 == 0 && P32 % 16 == 0 && MBAR % 8 == 0, "alignment");
-};
-
-/* The packed parameter image carries, after its mma.sync layouts (pack_bytes), the training CTA's
- * weight operands already in the canonical layout -- TrainSmem's W0..W3, byte for byte -- so that a
- * CTA loads them with 16-byte copies. */
-template <int D> __host__ __device__ constexpr int tc_pack_off() { return ((pack_bytes(D) + 127) / 128) * 128; }
-template <int D> __host__ __device__ constexpr int tc_pack_bytes() { return TrainSmem<D>::F; }
-template <int D> __host__ __device__ constexpr int packed_total_bytes() { return tc_pack_off<D>() + tc_pack_bytes<D>(); }
-/* W_l[k][n] (input k, unit n) in the canonical section */
-template <int D> __device__ __forceinline__ void pack_tc_weight(char* packed, int l, int k, int n, __nv_bfloat16 b) {
-    using L = TrainSmem<D>;
-    const int K = layer_in(l, D);
-    const int wb = l == 0 ? L::W0 : (l == 1 ? L::W1 : (l == 2 ? L::W2 : L::W3));
-    *reinterpret_cast<__nv_bfloat16*>(packed + tc_pack_off<D>() + wb + core_off(n, k, K)) = b;
-}
-
-/* an operand for tcgen05.mma: its first matrix descriptor fields and the address step per K = 16.
- * K-major [row][K] tile: LBO 128 (K direction), SBO K/8 x 128 (8-row groups), step 256.
- * MN-major read of a K-major [K][cols] tile (the operand's M or N = cols): LBO cols/8 x 128 (the K
- * direction), SBO 128 (the M/N direction), step 2 LBO. */
-struct Operand {
-    uint32_t addr, lbo, sbo, step;
-};
-__device__ __forceinline__ Operand kmajor(uint32_t addr, int k) { return Operand{addr, 128u, (uint32_t)(k / 8) * 128u, 256u}; }
-__device__ __forceinline__ Operand mnmajor(uint32_t addr, int cols) {
-    const uint32_t lbo = (uint32_t)(cols / 8) * 128u;
-    return Operand{addr, lbo, 128u, 2u * lbo};
-}
-/* instruction descriptor with A and B MN-major (bits 15 and 16) */
-__host__ __device__ constexpr uint32_t instr_desc_mn(int m, int n, bool a_mn, bool b_mn) {
-    return instr_desc(m, n) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
-}
-/* D[128 x 64] (+)= A B^T over `steps` x 16 of K */
-__device__ __forceinline__ void mma_k(uint32_t tmem_d, const Operand& a, const Operand& b, int steps, uint32_t idesc,
-                                      bool accumulate) {
-    for (int ks = 0; ks < steps; ++ks)
-        mma_f16(tmem_d, smem_desc(a.addr + ks * a.step, a.lbo, a.sbo), smem_desc(b.addr + ks * b.step, b.lbo, b.sbo),
-                idesc, (accumulate || ks > 0) ? 1u : 0u);
-}
-__device__ __forceinline__ __nv_bfloat16 bf16_of(float v) { return __float2bfloat16_rn(v); }
-
-template <int D>
-__device__ __forceinline__ void train_tiles(const float* __restrict__ u_in, const float* __restrict__ y_in,
-                                            uint64_t npts, uint32_t rounds, float scale, float* __restrict__ out,
-                                            const char* __restrict__ packed, float* __restrict__ partial,
-                                            uint32_t* __restrict__ status) {
-    using L = TrainSmem<D>;
-    constexpr int K0 = L::K0;
-    constexpr int ACT0 = TILE * K0 * 2, ACT = TILE * WIDTH * 2; /* bytes of one tile's features / layer */
-    extern __shared__ __align__(128) char smem[];
-    const int t = threadIdx.x, warp = t >> 5;
-    {
-        const uint4* wsrc = reinterpret_cast<const uint4*>(packed + tc_pack_off<D>());
-        uint4* wdst = reinterpret_cast<uint4*>(smem);
-        for (int i = t; i < tc_pack_bytes<D>() / 16; i += THREADS) wdst[i] = wsrc[i];
-        const float* src = reinterpret_cast<const float*>(packed + fp32_off_bytes(D));
-        float* p32 = reinterpret_cast<float*>(smem + L::P32);
-        for (int i = t; i < 5 * WIDTH + 1; i += THREADS) p32[i] = src[i];
-        float* acc = reinterpret_cast<float*>(smem + L::ACC);
-        for (int i = t; i < 5 * WIDTH + 4; i += THREADS) acc[i] = 0.0f;
-        const uint32_t one2 = pack_bf16x2(1.0f, 1.0f);
-        uint4* ones = reinterpret_cast<uint4*>(smem + L::ONES);
-        for (int i = t; i < 8 * TILE * 2 / 16; i += THREADS) ones[i] = make_uint4(one2, one2, one2, one2);
-    }
-    const uint32_t mbar = smem_u32(smem + L::MBAR), slot = smem_u32(smem + L::SLOT);
-    volatile int* flag = reinterpret_cast<volatile int*>(smem + L::FLAG);
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(L::TCOLS)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        *flag = 0;
-    }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(smem + L::SLOT);
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    const uint32_t sbase = smem_u32(smem);
-    const float* bias = reinterpret_cast<const float*>(smem + L::P32);
-    const float* w4 = bias + 4 * WIDTH;
-    const float b4 = w4[WIDTH];
-    float* acc = reinterpret_cast<float*>(smem + L::ACC); /* (db[4][64]) | dw4[64] | db4 */
-    float* dv = reinterpret_cast<float*>(smem + L::DV);
-    const uint32_t id_kk = instr_desc(TILE, MMA_N), id_km = instr_desc_mn(TILE, MMA_N, false, true),
-                   id_mm = instr_desc_mn(TILE, MMA_N, true, true);
-    const Operand ones{sbase + L::ONES, 128u, 0u, 256u}; /* 128 rows of one 8-row group */
-    uint32_t phase = 0;
-    bool ok = true;
-    auto mma_done = [&]() -> bool {
-        const bool got = mbar_wait(mbar, phase);
-        phase ^= 1u;
-        if (!got) *flag = 1;
-        tc_fence_after();
-        return __syncthreads_and(got) != 0;
-    };
-    auto sync_operands = [&]() {
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-    };
-    auto act_off = [&](int l, int p) -> int { /* tile p's input of layer l */
-        return l == 0 ? L::F + p * ACT0 : (l == 1 ? L::H1 : (l == 2 ? L::H2 : L::H3)) + p * ACT;
-    };
-    auto w_off_b = [&](int l) -> int { return l == 0 ? L::W0 : (l == 1 ? L::W1 : (l == 2 ? L::W2 : L::W3)); };
-    auto write_row = [&](char* dst, const float* v) { /* row t of a K-major 128 x 64 tile */
-#pragma unroll
-        for (int kg = 0; kg < WIDTH / 8; ++kg) {
-            uint32_t w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) w[q] = pack_bf16x2(v[8 * kg + 2 * q], v[8 * kg + 2 * q + 1]);
-            *reinterpret_cast<uint4*>(dst + core_off(t, 8 * kg, WIDTH)) = make_uint4(w[0], w[1], w[2], w[3]);
-        }
-    };
-    uint32_t done = 0; /* tile pairs accumulated */
-    for (uint32_t r = 0; r < rounds && ok; r += PAIR) {
-        uint64_t ip[PAIR];
-        bool valid[PAIR];
-        float y[PAIR];
-#pragma unroll
-        for (int p = 0; p < PAIR; ++p) {
-            ip[p] = ((uint64_t)blockIdx.x * rounds + r + p) * TILE + (uint64_t)t;
-            valid[p] = r + p < rounds && ip[p] < npts;
-            y[p] = valid[p] ? y_in[ip[p]] : 0.0f;
-            float u[D];
-            for (int d = 0; d < D; ++d) u[d] = valid[p] ? u_in[ip[p] * D + d] : 0.5f;
-            float ft[K0];
-#pragma unroll
-            for (int k = 0; k < K0; ++k) ft[k] = 0.0f;
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                ft[d] = u[d];
-                float sn = sinpif(u[d]), cs = cospif(u[d]);
-#pragma unroll
-                for (int k = 0; k < BANDS; ++k) {
-                    ft[D + 12 * d + 2 * k] = sn;
-                    ft[D + 12 * d + 2 * k + 1] = cs;
-                    const float s2 = 2.0f * sn * cs, c2 = fmaf(-2.0f * sn, sn, 1.0f);
-                    sn = s2;
-                    cs = c2;
-                }
-            }
-            char* F = smem + L::F + p * ACT0;
-#pragma unroll
-            for (int kg = 0; kg < K0 / 8; ++kg) {
-                uint32_t w[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) w[q] = pack_bf16x2(ft[8 * kg + 2 * q], ft[8 * kg + 2 * q + 1]);
-                *reinterpret_cast<uint4*>(F + core_off(t, 8 * kg, K0)) = make_uint4(w[0], w[1], w[2], w[3]);
-            }
-        }
-        /* forward: relu' masks per layer and tile, two words of 32 units */
-        uint32_t mk[PAIR][4][2];
-        float g[PAIR] = {};
-        for (int l = 0; l < 4 && ok; ++l) {
-            const int K = l == 0 ? K0 : WIDTH;
-            sync_operands();
-            if (t == 0) {
-                tc_fence_after();
-#pragma unroll
-                for (int p = 0; p < PAIR; ++p)
-                    mma_k(tmem + 64 * p, kmajor(sbase + act_off(l, p), K), kmajor(sbase + w_off_b(l), K), K / 16, id_kk,
-                          false);
-                mma_commit(mbar);
-            }
-            ok = mma_done();
-            if (!ok) break;
-            const float* bl = bias + l * WIDTH;
-#pragma unroll
-            for (int p = 0; p < PAIR; ++p) {
-                float h[WIDTH];
-                tmem_ld32(tmem + lane_base + 64 * p, h);
-                tmem_ld32(tmem + lane_base + 64 * p + 32, h + 32);
-                mk[p][l][0] = mk[p][l][1] = 0u;
-#pragma unroll
-                for (int j = 0; j < WIDTH; ++j) {
-                    h[j] = __bfloat162float(bf16_of(fmaxf(h[j] + bl[j], 0.0f)));
-                    if (h[j] > 0.0f) mk[p][l][j >> 5] |= 1u << (j & 31);
-                }
-                if (l < 3) {
-                    write_row(smem + act_off(l + 1, p), h);
-                } else {
-                    float s = 0.0f;
-#pragma unroll
-                    for (int j = 0; j < WIDTH; ++j) s = fmaf(h[j], w4[j], s);
-                    g[p] = s + b4;
-                    write_row(smem + L::DZ + p * ACT, h); /* h4, for the output weights' gradient */
-                }
-            }
-            tc_fence_before();
-        }
-        if (!ok) break;
-        float d[PAIR];
-#pragma unroll
-        for (int p = 0; p < PAIR; ++p) {
-            if (out && valid[p]) out[ip[p]] = g[p];
-            d[p] = valid[p] ? (g[p] - y[p]) * scale : 0.0f;
-            dv[p * TILE + t] = d[p];
-        }
-        __syncthreads();
-        /* output layer: dw4[n] = sum d h4[n] (two threads per unit, one tile each), db4 = sum d */
-        {
-            const int n = t & (WIDTH - 1), half = t >> 6;
-            float sw = 0.0f;
-            for (int p = 0; p < PAIR; ++p) {
-                const char* H4 = smem + L::DZ + p * ACT;
-                for (int b = half * (TILE / 2); b < (half + 1) * (TILE / 2); ++b)
-                    sw = fmaf(dv[p * TILE + b],
-                              __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(H4 + core_off(b, n, WIDTH))), sw);
-            }
-            float sb = d[0] + d[1];
-            for (int o = 16; o > 0; o >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
-            __syncthreads();
-            float* tmp = dv; /* the output gradients are no longer needed */
-            if (half == 1) tmp[n] = sw;
-            if ((t & 31) == 0) tmp[WIDTH + warp] = sb;
-            __syncthreads();
-            if (half == 0) acc[4 * WIDTH + n] += sw + tmp[n];
-            if (t == 0) acc[5 * WIDTH] += ((tmp[WIDTH] + tmp[WIDTH + 1]) + tmp[WIDTH + 2]) + tmp[WIDTH + 3];
-        }
-        /* dz_3 = relu'(z_3) * d * w4, rounded to BF16 (overwrites h4) */
-        {
-            float z[PAIR][WIDTH];
-#pragma unroll
-            for (int p = 0; p < PAIR; ++p)
-#pragma unroll
-                for (int n = 0; n < WIDTH; ++n)
-                    z[p][n] = ((mk[p][3][n >> 5] >> (n & 31)) & 1u) ? __bfloat162float(bf16_of(d[p] * w4[n])) : 0.0f;
-            __syncthreads(); /* every thread has read h4 */
-#pragma unroll
-            for (int p = 0; p < PAIR; ++p) write_row(smem + L::DZ + p * ACT, z[p]);
-        }
-        for (int l = 3; l >= 0 && ok; --l) {
-            const int K = l == 0 ? K0 : WIDTH;
-            sync_operands();
-            if (t == 0) {
-                tc_fence_after();
-                const bool acc_prev = done > 0;
-#pragma unroll
-                for (int p = 0; p < PAIR; ++p) {
-                    const Operand dz = mnmajor(sbase + L::DZ + p * ACT, WIDTH);
-                    /* dW_l += a_l^T dz_l, db_l += 1^T dz_l, and (l > 0) da_l = dz_l W_l^T */
-                    mma_k(tmem + 128 + 64 * l, mnmajor(sbase + act_off(l, p), K), dz, TILE / 16, id_mm, acc_prev || p > 0);
-                    mma_k(tmem + 384, ones, dz, TILE / 16, id_km, p > 0);
-                    if (l > 0)
-                        mma_k(tmem + 64 * p, kmajor(sbase + L::DZ + p * ACT, WIDTH), mnmajor(sbase + w_off_b(l), WIDTH),
-                              WIDTH / 16, id_km, false);
-                }
-                mma_commit(mbar);
-            }
-            ok = mma_done();
-            if (!ok) break;
-            if (warp == 0) { /* row 0 of the ones product: the column sums of both tiles */
-                float db[WIDTH];
-                tmem_ld32(tmem + lane_base + 384, db);
-                tmem_ld32(tmem + lane_base + 416, db + 32);
-                if (t == 0)
-                    for (int n = 0; n < WIDTH; ++n) acc[l * WIDTH + n] += db[n];
-            }
-            if (l > 0) {
-#pragma unroll
-                for (int p = 0; p < PAIR; ++p) {
-                    /* dz_{l-1} = relu'(z_{l-1}) * (dz_l W_l^T), rounded to BF16 */
-                    float da[WIDTH];
-                    tmem_ld32(tmem + lane_base + 64 * p, da);
-                    tmem_ld32(tmem + lane_base + 64 * p + 32, da + 32);
-#pragma unroll
-                    for (int k = 0; k < WIDTH; ++k)
-                        da[k] = ((mk[p][l - 1][k >> 5] >> (k & 31)) & 1u) ? __bfloat162float(bf16_of(da[k])) : 0.0f;
-                    write_row(smem + L::DZ + p * ACT, da);
-                }
-            }
-            tc_fence_before();
-        }
-        if (!ok) break;
-        ++done;
-        __syncthreads();
-    }
-    /* the CTA's gradient: dW_l rows (inputs) from TMEM, warp w reading rows 32w..32w+31 */
-    float* dst = partial + (size_t)blockIdx.x * n_params(D);
-    __syncthreads();
-    for (int l = 0; l < 4; ++l) {
-        const int K = layer_in(l, D);
-        const int woff = l == 0 ? 0 : K0 * WIDTH + (l - 1) * WIDTH * WIDTH;
-        float v[WIDTH];
-        if (ok && done > 0) {
-            tmem_ld32(tmem + lane_base + 128 + 64 * l, v);
-            tmem_ld32(tmem + lane_base + 160 + 64 * l, v + 32);
-        } else {
-#pragma unroll
-            for (int n = 0; n < WIDTH; ++n) v[n] = 0.0f;
-        }
-        if (t < K)
-            for (int n = 0; n < WIDTH; ++n) dst[woff + t * WIDTH + n] = v[n];
-    }
-    const int nw = (K0 + 3 * WIDTH) * WIDTH;
-    for (int k = t; k < 5 * WIDTH + 1; k += THREADS) dst[nw + k] = acc[k];
-    if (*flag && t == 0) atomicOr(status, VCU_FLAG_TIMEOUT);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::TCOLS) : "memory");
-}
-
 }  // namespace tc
 }  // namespace mlp
 }  // namespace vcu
