@@ -639,6 +639,50 @@ struct MovingScene3 {
         out[1] = c1;
         out[2] = c2;
     }
+    /* two points of the box at once: eval_culled's arithmetic for each, the kept terms' loops shared */
+    VCU_HD void pair_culled(const CullBox& c, const float* x0, const float* x1, float* o0, float* o1) const {
+        float g0 = 0.0f, g1 = 0.0f;
+        uint64_t m = c.g;
+        while (m) {
+            const int i = ctz64(m);
+            m &= m - 1;
+            const float gx = g[i][0], gy = g[i][1], gs = g[i][2], ga = g[i][3];
+            const float dx0 = vsub(x0[0], gx), dy0 = vsub(x0[1], gy);
+            const float dx1 = vsub(x1[0], gx), dy1 = vsub(x1[1], gy);
+            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
+            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
+            g0 = vfma(ga, vexp_nonpos(vmul(r0, gs)), g0);
+            g1 = vfma(ga, vexp_nonpos(vmul(r1, gs)), g1);
+        }
+        float a0 = g0, a1 = g0, a2 = g0, b0 = g1, b1 = g1, b2 = g1;
+        uint32_t dm = c.d;
+        while (dm) {
+            const int i = ctz32(dm);
+            dm &= dm - 1;
+            const float cx0 = vfma(x0[2], d[i][2], d[i][0]), cy0 = vfma(x0[2], d[i][3], d[i][1]);
+            const float cx1 = vfma(x1[2], d[i][2], d[i][0]), cy1 = vfma(x1[2], d[i][3], d[i][1]);
+            const float dx0 = vsub(x0[0], cx0), dy0 = vsub(x0[1], cy0);
+            const float dx1 = vsub(x1[0], cx1), dy1 = vsub(x1[1], cy1);
+            const float r0 = vfma(dx0, dx0, vmul(dy0, dy0));
+            const float r1 = vfma(dx1, dx1, vmul(dy1, dy1));
+            if (r0 <= d[i][4]) {
+                a0 = vadd(a0, d[i][5]);
+                a1 = vadd(a1, d[i][6]);
+                a2 = vadd(a2, d[i][7]);
+            }
+            if (r1 <= d[i][4]) {
+                b0 = vadd(b0, d[i][5]);
+                b1 = vadd(b1, d[i][6]);
+                b2 = vadd(b2, d[i][7]);
+            }
+        }
+        o0[0] = a0;
+        o0[1] = a1;
+        o0[2] = a2;
+        o1[0] = b0;
+        o1[1] = b1;
+        o1[2] = b2;
+    }
     /* two points at once, each with exactly the arithmetic of operator() */
     VCU_HD void pair(const float* x0, const float* x1, float* o0, float* o1) const {
         float g0 = 0.0f, g1 = 0.0f;

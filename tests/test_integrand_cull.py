@@ -269,11 +269,15 @@ int main(int argc, char** argv) {
                         x[k] = mode == 0 ? lo[k] : mode == 1 ? hi[k]
                              : vcu::vadd(lo[k], vcu::vmul(u01(rng), vcu::vsub(hi[k], lo[k])));
                     }
-                    float a[3], r[3];
+                    float a[3], r[3], y[3], pa[3], pb[3], ry[3];
                     s.eval_culled(c, x, a);
                     s(x, r);
+                    /* a second point of the box with the first, through pair_culled */
+                    for (int k = 0; k < 3; ++k) y[k] = vcu::vadd(lo[k], vcu::vmul(u01(rng), vcu::vsub(hi[k], lo[k])));
+                    s.pair_culled(c, x, y, pa, pb);
+                    s(y, ry);
                     ++checked;
-                    if (std::memcmp(a, r, sizeof(a))) {
+                    if (std::memcmp(a, r, sizeof(a)) || std::memcmp(pa, r, sizeof(pa)) || std::memcmp(pb, ry, sizeof(pb))) {
                         std::printf("mismatch res=%d at (%a,%a,%a)\n", res, x[0], x[1], x[2]);
                         return 1;
                     }
@@ -288,9 +292,9 @@ int main(int argc, char** argv) {
 
 
 def test_moving_scene_culled_evaluation_equals_full_evaluation(tmp_path):
-    """The moving-disk scene's eval_culled (bumps culled as in the 2-D scene, disks by their centre's
-    path over the box's time interval) returns operator()'s three channels bit for bit at points of
-    the box, for bins of 1/512 to 1/8 and the whole or a quarter of the time range."""
+    """The moving-disk scene's eval_culled and pair_culled (bumps culled as in the 2-D scene, disks by
+    their centre's path over the box's time interval) return operator()'s three channels bit for bit
+    at points of the box, for bins of 1/512 to 1/8 and the whole or a quarter of the time range."""
     src = tmp_path / "mov.cc"
     src.write_text(MOVING)
     exe = tmp_path / "mov"

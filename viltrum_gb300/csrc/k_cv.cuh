@@ -854,13 +854,11 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
     for (int c = 0; c < CH; ++c) sf32[c] = cf32[c] = sa32[c] = ca32[c] = 0.0f;
     float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f, m2f32 = 0.0f;
     const uint32_t blo = (uint32_t)bin, bhi = (uint32_t)(bin >> 32);
-    for (uint64_t j = lane; j < cfg.spp && n > 0; j += 32) {
-        uint32_t chosen;
-        float x[F::DIM];
-        for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+    /* one sample's draw: its region of the bin's list, its point, the point's weight (volume(bin n
+     * region) for a uniform point, else 1/pdf) */
+    auto draw = [&](uint64_t j, uint32_t& chosen, float* x, float& sfac) {
         float a[DIM], b[DIM], A[DIM], B[DIM], v;
         bool empty;
-        float sfac; /* the point's weight: volume(bin n region) for a uniform point, else 1/pdf */
         /* region_sampling_mis's weight from the importance point's pdf (region-sampling.h:93-135);
          * also whether the uniform point is taken for a draw rr_u */
         auto mis_weight = [&](float pdf_imp, float vol, float rr_u, bool& uniform) -> float {
@@ -982,14 +980,11 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
                 }
             }
         }
+    };
+    /* one sample's polynomial value, weights and moments, in sample order */
+    auto accumulate = [&](uint32_t chosen, const float* x, const float* fv, float sfac) {
         const int id = heap_pay[lists[off + chosen]] & 0xffffff;
-        float fv[CH], gv[CH], p[DIM];
-        if constexpr (has_eval_cull<F>::value && F::DIM == DIM) {
-            if (!replay) f.eval_culled(cl, x, fv);
-            else f(x, fv);
-        } else {
-            f(x, fv);
-        }
+        float gv[CH], p[DIM];
         for (int d = 0; d < DIM; ++d) {
             const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
             p[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));
@@ -1031,7 +1026,49 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
         m2a32 = vfma(da, da2, m2a32);
         cfa32 = vfma(df, da2, cfa32);
         if (cfg.var_out) m2f32 = vfma(df, vsub(nf, mf32), m2f32);
+    };
+    bool paired = false;
+    if constexpr (has_pair_cull<F>::value && F::DIM == DIM && !PDF) {
+        if (!replay) {
+            /* a lane's samples j and j + 32 drawn, evaluated together (pair_culled: the kept terms'
+             * loops shared, two independent chains), then accumulated in order */
+            paired = true;
+            for (uint64_t j = lane; j < cfg.spp && n > 0; j += 64) {
+                const bool two = j + 32 < cfg.spp;
+                uint32_t c0, c1;
+                float x0[F::DIM], x1[F::DIM], s0, s1;
+                for (int d = 0; d < F::DIM; ++d) x0[d] = x1[d] = 0.0f;
+                draw(j, c0, x0, s0);
+                if (two) {
+                    draw(j + 32, c1, x1, s1);
+                } else {
+                    c1 = c0;
+                    s1 = s0;
+                    for (int d = 0; d < F::DIM; ++d) x1[d] = x0[d];
+                }
+                float f0[CH], f1[CH];
+                f.pair_culled(cl, x0, x1, f0, f1);
+                accumulate(c0, x0, f0, s0);
+                if (two) accumulate(c1, x1, f1, s1);
+            }
+        }
     }
+    if (!paired)
+        for (uint64_t j = lane; j < cfg.spp && n > 0; j += 32) {
+            uint32_t chosen;
+            float x[F::DIM];
+            for (int d = 0; d < F::DIM; ++d) x[d] = 0.0f;
+            float sfac;
+            draw(j, chosen, x, sfac);
+            float fv[CH];
+            if constexpr (has_eval_cull<F>::value && F::DIM == DIM) {
+                if (!replay) f.eval_culled(cl, x, fv);
+                else f(x, fv);
+            } else {
+                f(x, fv);
+            }
+            accumulate(chosen, x, fv, sfac);
+        }
     /* lanes merged in FP32: each Kahan sum as the float-float pair (sum, -compensation) added with
      * two-sum, the moments by Chan's pairwise formulas (one division per step) */
     float sfh[CH], sfl[CH], sah[CH], sal[CH];
