@@ -94,6 +94,29 @@ def test_cv_statistics_against_fp64(ctx, port):
     assert 0.7 <= ratio <= 1.4, (gpu_sq, ref_sq)
 
 
+def test_cv_occluded_scene_statistics(ctx, port):
+    """The 5-D occluded scene, whose residual evaluates its drawn points two at a time with the scene's
+    terms culled to the bin (pair_culled): with Philox draws its error against a plain Monte Carlo
+    truth (2^16 samples per bin) matches the oracle's control variates' at equal samples."""
+    params = scenes.occluded_scene5(7)
+    lo, hi = [0] * 5, [1] * 5
+    res, iters, spp = [16, 16], 255, 64
+    p = ctx.problem(scenes.OCCLUDED_SCENE5, params, lo, hi, res)
+    truth = np.empty(16 * 16, np.float32)
+    ctx.per_bin_monte_carlo(p, 1 << 16, 99, truth)
+    truth = truth.astype(np.float64)
+    gpu_sq, ref_sq = [], []
+    for seed in (1, 2, 3, 4):
+        out, _, _, st = _gpu_cv(ctx, scenes.OCCLUDED_SCENE5, params, lo, hi, res, iters, spp, seed)
+        assert st.flags == 0
+        gpu_sq.append(np.mean((out[:, 0] - truth) ** 2))
+        ref = port.control_variates(scenes.OCCLUDED_SCENE5, params, lo, hi, res,
+                                    orc.Nested.make("simpson", "trapezoidal", "size", "relative"), iters, spp, seed)
+        ref_sq.append(np.mean((ref["bins"].ravel() - truth) ** 2))
+    ratio = np.mean(gpu_sq) / np.mean(ref_sq)
+    assert 0.6 <= ratio <= 1.6, (gpu_sq, ref_sq)
+
+
 def test_cv_fullsize_matches_oracle(ctx, port):
     """The control-variate workload at its full size -- integrator_crespo2021(2^14 - 1 splits, 64
     residual samples) on the RGB moving-disk scene into 512x512 bins -- against the oracle: the same

@@ -753,7 +753,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
     /* the integrand's terms that can be non-zero in the bin (points drawn here lie in it; replayed
      * points are the caller's, so they are evaluated in full) */
     [[maybe_unused]] typename cull_box_of<F>::type cl{};
-    if constexpr (has_eval_cull<F>::value && F::DIM == DIM) {
+    if constexpr ((has_eval_cull<F>::value || has_pair_cull<F>::value) && F::DIM == DIM) {
         if (!replay) cl = f.cull_box(bmin, bmax);
     }
     auto isect = [&](int id, float* a, float* b, float* A, float* B, float& v, bool& empty) {
