@@ -90,11 +90,28 @@ template <int S> __host__ __device__ constexpr int scratch_words() {
  * from the last dimension (region.h:141-150) with subrange() in the reference's double-promoted
  * arithmetic.  Over the whole region (A = 0, B = 1 in every dimension, the usual case for a single
  * bin) the lower end of each Horner evaluation is exactly 0 and the upper end's multiplications by
- * t = 1 are exact, so only the upper end is evaluated. */
+ * t = 1 are exact, so only the upper end is evaluated: in FP32 (ref_integral01, the reference's float
+ * certified), in double only where FP32 cannot certify it (a sum on or next to a rounding boundary
+ * that is not exact, zeros, extreme magnitudes) -- the FP64 pipe runs at 1/64 of the FP32 rate. */
+static __device__ __noinline__ float integral01_double3(float c0, float c1, float c2) {
+    const float c[3] = {c0, c1, c2};
+    return __double2float_rn(horner_int_ref<3>(c, 1.0f));
+}
+static __device__ __noinline__ float integral01_double5(float c0, float c1, float c2, float c3, float c4) {
+    const float c[5] = {c0, c1, c2, c3, c4};
+    return __double2float_rn(horner_int_ref<5>(c, 1.0f));
+}
 template <int S> __device__ __forceinline__ float subrange01_ref(const float* p) {
     float c[S];
     Rule<S>::coefficients(p, c);
-    return __double2float_rn(horner_int_ref<S>(c, 1.0f));
+    if constexpr (S == 3 || S == 5) {
+        float v;
+        if (ref_integral01<S>(c, v)) return v;
+        if constexpr (S == 3) return integral01_double3(c[0], c[1], c[2]);
+        else return integral01_double5(c[0], c[1], c[2], c[3], c[4]);
+    } else {
+        return __double2float_rn(horner_int_ref<S>(c, 1.0f));
+    }
 }
 template <int DIM, int S>
 __device__ float region_integral_ref(const float* __restrict__ V, const float* A, const float* B, bool whole) {

@@ -133,6 +133,94 @@ VCU_HD float ref_boole(float p0, float p1, float p2, float p3, float p4) {
     return ff_div(h, l, 90.0f, 0.011111111380159855f /* RN(1/90) */);
 }
 
+/* sum_k c[k] / (k + 1), the integral over [0, 1] of the power-basis polynomial c[0] + c[1] t + ... of
+ * a rule of S nodes, as the reference rounds subrange(0, 1) for float coefficients: Horner steps in
+ * double ("c[k]*t/(k+1.0)" a float product divided in double), the result rounded once to float
+ * (rules.h:41-44, 96-100, 288-293; the antiderivative at 0 is a zero).  Here the terms are summed
+ * error-free as a float-float pair (h, l), the divisions by 3 and 5 as the IEEE quotient plus its exact
+ * remainder's share.  Two ways to the reference's float:
+ *  - the reference's double value and h + l both lie within ~2^-44 T of the exact sum (T: the sum of
+ *    the terms' magnitudes), so q = RN(h + l) is the reference's float whenever every value within
+ *    E = 2^-40 T of h + l rounds to q (rounding is monotone: the two ends of that interval suffice);
+ *  - where that fails because the sum sits on or next to a rounding boundary, the sum may be exact:
+ *    every term a float (zero division remainders, exact halvings), so all are multiples of the
+ *    smallest term's ulp u; with T < 2^51 u every double step of the reference is exact, and if l
+ *    also carries the error terms exactly, RN(h + l) is the reference's float (ties to even alike).
+ * Returns false otherwise -- a boundary within E of an inexact sum, a sum that cancels to below
+ * ~2^-17 T, T outside [2^-60, 2^60] or not finite -- and the caller evaluates the reference's double
+ * expression instead. */
+VCU_HD bool ref_certify(float h, float l, float T, float& out) {
+    const float q = vadd(h, l);
+    const float r = vadd(vsub(h, q), l);
+    const float E = vmul(T, 9.094947017729282e-13f); /* 2^-40 */
+    if (vadd(q, vsub(r, E)) != q || vadd(q, vadd(r, E)) != q) return false;
+    out = q;
+    return true;
+}
+VCU_HD bool ref_in_range(float T) { /* 2^-60 <= T <= 2^60 (false for NaN) */
+    return T >= 8.673617379884035e-19f && T <= 1.152921504606847e18f;
+}
+/* the exponent field of the smallest ulp among the non-zero terms (1 for subnormals; 255 if all are
+ * zero), and whether T < 2^51 times that ulp */
+VCU_HD bool ref_exact_span(const float* t, int n, float T) {
+    uint32_t ef = 255u;
+    for (int i = 0; i < n; ++i) {
+        const uint32_t e = (float_to_bits(t[i]) >> 23) & 0xffu;
+        if (float_to_bits(t[i]) << 1) ef = (e == 0u ? 1u : e) < ef ? (e == 0u ? 1u : e) : ef;
+    }
+    if (ef == 255u) return false; /* all zero: the signs of zeros are the double path's */
+    /* u = 2^(ef - 150); 2^51 u = 2^(ef - 99) as a float: exponent field ef - 99 + 127 */
+    const uint32_t bf = ef + 28u;
+    if (bf >= 255u) return false;
+    return T < bits_to_float(bf << 23);
+}
+template <int S> VCU_HD bool ref_integral01(const float* c, float& out);
+template <> VCU_HD bool ref_integral01<3>(const float* c, float& out) {
+    /* c2/3 + c1/2 + c0 */
+    const float a = fdiv_c<3>(c[2]);
+    const float ra = vfma(-a, 3.0f, c[2]); /* exact remainder */
+    const float b = vmul(c[1], 0.5f);
+    float s, e1, h, e2;
+    two_sum(a, b, s, e1);
+    two_sum(s, c[0], h, e2);
+    const float T = vadd(vadd(vabs(a), vabs(b)), vabs(c[0]));
+    if (!ref_in_range(T)) return false;
+    if (ref_certify(h, vadd(vadd(vmul(ra, 0.3333333432674408f), e1), e2), T, out)) return true;
+    float l, le;
+    two_sum(e1, e2, l, le);
+    const float terms[3] = {a, b, c[0]};
+    if (ra != 0.0f || le != 0.0f || vmul(b, 2.0f) != c[1] || !ref_exact_span(terms, 3, T)) return false;
+    out = vadd(h, l);
+    return true;
+}
+template <> VCU_HD bool ref_integral01<5>(const float* c, float& out) {
+    /* c4/5 + c3/4 + c2/3 + c1/2 + c0, summed in the reference's order */
+    const float a5 = fdiv_c<5>(c[4]);
+    const float r5 = vfma(-a5, 5.0f, c[4]);
+    const float b4 = vmul(c[3], 0.25f);
+    const float a3 = fdiv_c<3>(c[2]);
+    const float r3 = vfma(-a3, 3.0f, c[2]);
+    const float b2 = vmul(c[1], 0.5f);
+    float s, e1, e2, e3, h, e4;
+    two_sum(a5, b4, s, e1);
+    two_sum(s, a3, s, e2);
+    two_sum(s, b2, s, e3);
+    two_sum(s, c[0], h, e4);
+    const float T = vadd(vadd(vadd(vadd(vabs(a5), vabs(b4)), vabs(a3)), vabs(b2)), vabs(c[0]));
+    if (!ref_in_range(T)) return false;
+    const float l0 = vadd(vmul(r5, 0.20000000298023224f), vmul(r3, 0.3333333432674408f));
+    if (ref_certify(h, vadd(vadd(vadd(vadd(l0, e1), e2), e3), e4), T, out)) return true;
+    if (r5 != 0.0f || r3 != 0.0f || vmul(b4, 4.0f) != c[3] || vmul(b2, 2.0f) != c[1]) return false;
+    float l, le1, le2, le3;
+    two_sum(e1, e2, l, le1);
+    two_sum(l, e3, l, le2);
+    two_sum(l, e4, l, le3);
+    const float terms[5] = {a5, b4, a3, b2, c[0]};
+    if (le1 != 0.0f || le2 != 0.0f || le3 != 0.0f || !ref_exact_span(terms, 5, T)) return false;
+    out = vadd(h, l);
+    return true;
+}
+
 template <int S> struct RefRule;
 template <> struct RefRule<2> { /* (p0+p1)/2.0: float sum, exact halving */
     static VCU_HD float scalar(const float* p) { return vmul(vadd(p[0], p[1]), 0.5f); }
