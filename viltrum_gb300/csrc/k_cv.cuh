@@ -624,9 +624,41 @@ __device__ float poly_subrange(const float* V, int c, const float* A, const floa
     return buf[0];
 }
 
-/* the region polynomial at normalised position p, folding dimension 0 first (region.h:86-112) */
+/* approximation_at (region.h:86-112): the region's polynomial at the normalised point p, folded
+ * from dimension 0 with Horner's at() (rules.h:85-89, 282-286).  The first fold's S^(DIM-1) lines
+ * take their power-basis coefficients from C (k_cv_coef: the same floats at() computes from the
+ * node values), so a sample spends its arithmetic on the Horner steps. */
 template <int DIM, int S, int CH>
-__device__ float poly_at(const float* V, int c, const float* p) {
+__device__ float poly_at_coef(const float* C, int c, const float* p) {
+    constexpr int SD = ipow(S, DIM);
+    constexpr int UNROLL = SD / S <= 9 ? SD / S : 4; /* 3-D Boole: 25 lines, unrolled by 4 */
+    float buf[SD / S > 0 ? SD / S : 1];
+    int n = SD / S;
+#pragma unroll UNROLL
+    for (int i = 0; i < n; ++i) {
+        float cc[S];
+#pragma unroll
+        for (int j = 0; j < S; ++j) cc[j] = C[(i * S + j) * CH + c];
+        buf[i] = Rule<S>::horner_at(cc, p[0]);
+    }
+    for (int d = 1; d < DIM; ++d) {
+        const int m = n / S;
+        for (int i = 0; i < m; ++i) {
+            float line[S];
+#pragma unroll
+            for (int j = 0; j < S; ++j) line[j] = buf[i * S + j];
+            buf[i] = Rule<S>::at(p[d], line);
+        }
+        n = m;
+    }
+    return vmul(buf[0], 1.0f);
+}
+
+/* the same from the node values (at() forms each line's coefficients): for more than 3 dimensions,
+ * where the first fold has 81 lines, the precomputed coefficients measured no faster (2326 against
+ * 2309 ms for a 5-D scene at 1024x1024 bins and 4096 samples; 3-D RGB: 5.62 against 5.72 ms) */
+template <int DIM, int S, int CH>
+__device__ float poly_at_nodes(const float* V, int c, const float* p) {
     constexpr int SD = ipow(S, DIM);
     float buf[SD / S > 0 ? SD / S : 1];
     int n = SD / S;
@@ -647,6 +679,27 @@ __device__ float poly_at(const float* V, int c, const float* p) {
         n = m;
     }
     return vmul(buf[0], 1.0f);
+}
+template <int DIM> __host__ __device__ constexpr bool cv_coef_pass() { return DIM <= 3; }
+
+/* the first-fold coefficients of every listed region: coef[(k*SD + i*S + j)*CH + c] is coefficient j
+ * of line i (nodes i*S .. i*S+S-1 along dimension 0) of channel c of heap entry k's region */
+template <int S, int CH>
+__global__ void k_cv_coef(const int* __restrict__ heap_pay, const float* __restrict__ vals, int sd, size_t nheap,
+                          float* __restrict__ coef) {
+    const size_t lines = (size_t)(sd / S) * CH;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nheap * lines;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t k = t / lines;
+        const int r = (int)(t - k * lines), i = r / CH, c = r - i * CH;
+        const size_t id = (size_t)(heap_pay[k] & 0xffffff);
+        float line[S], cc[S];
+#pragma unroll
+        for (int j = 0; j < S; ++j) line[j] = vals[(id * sd + i * S + j) * CH + c];
+        Rule<S>::coefficients(line, cc);
+#pragma unroll
+        for (int j = 0; j < S; ++j) coef[(k * sd + i * S + j) * CH + c] = cc[j];
+    }
 }
 
 __device__ __forceinline__ float norm1(const float* v, int ch) {
@@ -692,9 +745,9 @@ template <class F, int DIM, int S, bool PDF>
 __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
     k_cv_residual(const __grid_constant__ F f, const ResCfg cfg, const uint32_t* __restrict__ offsets,
                   const uint32_t* __restrict__ lists, const int* __restrict__ heap_pay, const float* __restrict__ vals,
-                  const float* __restrict__ rmin, const float* __restrict__ rmax, const float* __restrict__ rvol,
-                  const float* __restrict__ replay, float* __restrict__ bins, float* __restrict__ approx_out,
-                  uint32_t* __restrict__ status) {
+                  const float* __restrict__ coef, const float* __restrict__ rmin, const float* __restrict__ rmax,
+                  const float* __restrict__ rvol, const float* __restrict__ replay, float* __restrict__ bins,
+                  float* __restrict__ approx_out, uint32_t* __restrict__ status) {
     constexpr int CH = F::CH;
     constexpr int SD = ipow(S, DIM);
     static_assert(!PDF || S == 3, "the pdf of a region exists for Simpson's rule only");
@@ -989,7 +1042,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
             const float rmn = rmin[(size_t)id * DIM + d], rmx = rmax[(size_t)id * DIM + d];
             p[d] = (rmn >= rmx) ? rmn : vdiv(vsub(x[d], rmn), vsub(rmx, rmn));
         }
-        for (int c = 0; c < CH; ++c) gv[c] = poly_at<DIM, S, CH>(vals + (size_t)id * SD * CH, c, p);
+        if constexpr (cv_coef_pass<DIM>()) {
+            const float* C = coef + (size_t)lists[off + chosen] * SD * CH;
+            for (int c = 0; c < CH; ++c) gv[c] = poly_at_coef<DIM, S, CH>(C, c, p);
+        } else {
+            for (int c = 0; c < CH; ++c) gv[c] = poly_at_nodes<DIM, S, CH>(vals + (size_t)id * SD * CH, c, p);
+        }
         /* sample weights: prod(res) * 1/P(region) (n for the uniform choice) * the point's weight */
         const double rrf = (cfg.rr == VCU_RR_UNIFORM) ? (double)n : cfg.rrf[off + chosen];
         float fs[CH], as[CH];
@@ -1243,11 +1301,22 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     const size_t o_cdf = align256((size_t)total * 8 + 512);
     const size_t o_rrf = align256(o_cdf + (size_t)total * 8);
     const size_t o_rerr = align256(o_rrf + (size_t)total * 8);
-    const size_t aux_bytes = importance ? o_rerr + nheap * 4 : (size_t)total * 8 + 512;
+    const size_t aux_lists = importance ? o_rerr + nheap * 4 : (size_t)total * 8 + 512;
+    /* the listed regions' first-fold coefficients, for the residual's polynomial values */
+    const bool sampled = cv_coef_pass<DIM>() && (cv.samples_per_bin > 0 || d_replay != nullptr);
+    const size_t o_coef = align256(aux_lists);
+    const size_t aux_bytes = sampled ? o_coef + nheap * (size_t)ipow(S, DIM) * F::CH * 4 : aux_lists;
     if ((rc = ensure(ctx, ctx->aux, aux_bytes))) return rc;
     uint32_t* lists_u = static_cast<uint32_t*>(ctx->aux.ptr);
     uint32_t* lists = lists_u + total + 64;
     char* aux = static_cast<char*>(ctx->aux.ptr);
+    float* coef = sampled ? reinterpret_cast<float*>(aux + o_coef) : nullptr;
+    if (sampled) {
+        const size_t nt = nheap * (size_t)ipow(S, DIM - 1) * F::CH;
+        const unsigned cblocks = (unsigned)std::min<size_t>((nt + 255) / 256, (size_t)ctx->sm_count * 16);
+        k_cv_coef<S, F::CH><<<cblocks, 256, 0, ctx->stream>>>(hp, vals, ipow(S, DIM), nheap, coef);
+        ++launches;
+    }
     k_cv_lists<<<lblocks, 256, 0, ctx->stream>>>(lc, hp, rmin, rmax, nullptr, off, cur, lists_u, 1);
     k_cv_sort<<<(unsigned)((g.nbins * 32 + 255) / 256), 256, 0, ctx->stream>>>(off, lists_u, lists, g.nbins);
     launches += 2;
@@ -1297,14 +1366,14 @@ int regions_into_bins(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinG
     if constexpr (S == 3) {
         if (pdf)
             k_cv_residual<F, DIM, S, true><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(
-                f, rcfg, off, lists, hp, vals, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
+                f, rcfg, off, lists, hp, vals, coef, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
         else
             k_cv_residual<F, DIM, S, false><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(
-                f, rcfg, off, lists, hp, vals, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
+                f, rcfg, off, lists, hp, vals, coef, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
     } else {
         if (pdf) return fail(ctx, VCU_UNSUPPORTED, "the pdf strategies need a Simpson high rule");
         k_cv_residual<F, DIM, S, false><<<rblocks, RES_WARPS * 32, 0, ctx->stream>>>(
-            f, rcfg, off, lists, hp, vals, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
+            f, rcfg, off, lists, hp, vals, coef, rmin, rmax, vol, d_replay, d_bins, d_approx, ctx->d_status);
     }
     ++launches;
     if (d_regions) {

@@ -41,10 +41,11 @@ template <> struct Rule<2> { /* trapezoidal */
         c[0] = p[0];
         c[1] = vsub(p[1], p[0]);
     }
+    static __device__ __forceinline__ float horner_at(const float* c, float t) { return vadd(vmul(c[1], t), c[0]); }
     static __device__ __forceinline__ float at(float t, const float* p) {
         float c[2];
         coefficients(p, c);
-        return vadd(vmul(c[1], t), c[0]);
+        return horner_at(c, t);
     }
     static __device__ __forceinline__ float horner_int(const float* c, float t) {
         return vmul(vadd(vmul(vmul(c[1], t), 0.5f), c[0]), t);
@@ -72,10 +73,13 @@ template <> struct Rule<3> { /* simpson */
         c[1] = vsub(vadd(vmul(-3.0f, p[0]), vmul(4.0f, p[1])), p[2]);
         c[2] = vadd(vsub(vmul(2.0f, p[0]), vmul(4.0f, p[1])), vmul(2.0f, p[2]));
     }
+    static __device__ __forceinline__ float horner_at(const float* c, float t) {
+        return vadd(vmul(vadd(vmul(c[2], t), c[1]), t), c[0]);
+    }
     static __device__ __forceinline__ float at(float t, const float* p) {
         float c[3];
         coefficients(p, c);
-        return vadd(vmul(vadd(vmul(c[2], t), c[1]), t), c[0]);
+        return horner_at(c, t);
     }
     static __device__ __forceinline__ float horner_int(const float* c, float t) {
         float r = vadd(fdiv_c<3>(vmul(c[2], t)), vmul(c[1], 0.5f));
@@ -124,13 +128,16 @@ template <> struct Rule<5> { /* boole */
                          div_c<3, G>(vmul(128.0f, p[3]))),
                     div_c<3, G>(vmul(32.0f, p[4])));
     }
-    static __device__ __forceinline__ float at(float t, const float* p) {
-        float c[5];
-        coefficients(p, c);
+    static __device__ __forceinline__ float horner_at(const float* c, float t) {
         float r = vadd(vmul(c[4], t), c[3]);
         r = vadd(vmul(r, t), c[2]);
         r = vadd(vmul(r, t), c[1]);
         return vadd(vmul(r, t), c[0]);
+    }
+    static __device__ __forceinline__ float at(float t, const float* p) {
+        float c[5];
+        coefficients(p, c);
+        return horner_at(c, t);
     }
     static __device__ __forceinline__ float horner_int(const float* c, float t) {
         float r = vadd(fdiv_c<5>(vmul(c[4], t)), vmul(c[3], 0.25f));
