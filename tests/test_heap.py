@@ -1,6 +1,6 @@
-"""The device heap (viltrum_gb300/csrc/vcu_heap.h) makes libstdc++'s choices: the two-array form
-and the packed-entry form, over one array and split between two (as the batched kernel keeps its top
-levels in shared memory).
+"""The device heap (viltrum_gb300/csrc/vcu_heap.h) makes libstdc++'s choices: the two-array form,
+the packed-entry form over one array and split between two (as the batched kernel keeps its top
+levels in shared memory), and the branch-free packed form the host replays long sequences with.
 
 A small host program drives vcu::heap_push / heap_pop and std::push_heap / std::pop_heap with
 the same random sequences (with many equal keys, which is where the two could disagree) and
@@ -23,7 +23,7 @@ int main() {
     for (int trial = 0; trial < 400; ++trial) {
         std::vector<E> ref;
         float key[128]; int pay[128]; int n = 0; int next = 0;
-        vcu::HeapEntry one[130], top[16], rest[130];
+        vcu::HeapEntry one[130], top[16], rest[130], flat[130];
         const vcu::HeapArray ha{one};
         const vcu::HeapSplit hs{top, rest, 7};
         const int levels = 1 + trial % 7;
@@ -39,16 +39,19 @@ int main() {
                 vcu::heap_push_entries(ha, n);
                 hs.set(n - 1, vcu::HeapEntry{k, next - 1});
                 vcu::heap_push_entries(hs, n);
+                vcu::heap_sift_up_packed(flat, n - 1, vcu::HeapEntry{k, next - 1});
             } else {
                 std::pop_heap(ref.begin(), ref.end(), [](const E& a, const E& b) { return a.k < b.k; });
                 ref.pop_back();
                 vcu::heap_pop(key, pay, n);
                 vcu::heap_pop_entries(ha, n);
-                vcu::heap_pop_entries(hs, n); --n;
+                vcu::heap_pop_entries(hs, n);
+                vcu::heap_pop_packed(flat, n); --n;
             }
             for (int i = 0; i < n; ++i)
                 if (ref[i].k != key[i] || ref[i].p != pay[i] || ref[i].k != ha.get(i).key || ref[i].p != ha.get(i).pay ||
-                    ref[i].k != hs.get(i).key || ref[i].p != hs.get(i).pay) {
+                    ref[i].k != hs.get(i).key || ref[i].p != hs.get(i).pay || ref[i].k != flat[i].key ||
+                    ref[i].p != flat[i].pay) {
                     std::printf("mismatch trial %d op %d\n", trial, op); return 1; }
         }
     }

@@ -2213,7 +2213,7 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
     launches += 2;
     std::vector<float> hkey, hb;
     std::vector<int> hdim, hchild;
-    std::vector<float> HE(N + 1);
+    std::vector<HeapEntry> H(N + 2);
     std::vector<int> HS(N + 1);
     uint32_t force = WAVE_NO_FORCE; /* after an incomplete replay: split every unsplit b bucket >= force */
     /* fixed grids (the kernels loop over their lists, whose lengths stay on the device) */
@@ -2258,26 +2258,22 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
         VCU_CUDA(ctx, cudaMemcpyAsync(hchild.data(), child, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
         VCU_CUDA(ctx, cudaMemcpyAsync(hb.data(), bneck, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
         VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        HE[0] = hkey[0];
-        HS[0] = 0 | (hdim[0] << 24);
+        H[0] = HeapEntry{hkey[0], 0 | (hdim[0] << 24)};
         int missing = -1;
         for (size_t it = 0; it < N; ++it) {
-            const int top = HS[0] & 0xffffff;
+            const int top = H[0].pay & 0xffffff;
             const int c = hchild[top];
             if (c < 0) {
                 missing = top;
                 break;
             }
             const int n = (int)it + 1;
-            heap_pop(HE.data(), HS.data(), n);
-            HE[n - 1] = hkey[c];
-            HS[n - 1] = c | (hdim[c] << 24);
-            heap_push(HE.data(), HS.data(), n);
-            HE[n] = hkey[c + 1];
-            HS[n] = (c + 1) | (hdim[c + 1] << 24);
-            heap_push(HE.data(), HS.data(), n + 1);
+            heap_pop_packed(H.data(), n);
+            heap_sift_up_packed(H.data(), n - 1, HeapEntry{hkey[c], c | (hdim[c] << 24)});
+            heap_sift_up_packed(H.data(), n, HeapEntry{hkey[c + 1], (c + 1) | (hdim[c + 1] << 24)});
         }
         if (missing < 0) {
+            for (size_t i = 0; i <= N; ++i) HS[i] = H[i].pay;
             VCU_CUDA(ctx, cudaMemcpyAsync(hp, HS.data(), (N + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
             return regions_into_bins<F, DIM, SH, SL>(ctx, residual_functor(f), p, g, cv, vals, rmin, rmax, vol, hp, N + 1,
                                                      reinterpret_cast<uint32_t*>(base + o_cnt),

@@ -149,4 +149,38 @@ template <class A> VCU_HEAP_HD void heap_pop_entries(const A& h, int len) {
     heap_sift_up_entries(h, hole, v);
 }
 
+/* The same two algorithms on a plain packed array, for the host's replay of long heap sequences:
+ * the larger child is chosen by arithmetic on the comparison (no branch to mispredict on random
+ * sibling orders) and an entry moves as one 8-byte copy.  Same stores, same array. */
+VCU_HEAP_HD void heap_sift_up_packed(HeapEntry* h, int hole, HeapEntry v) {
+    while (hole > 0) {
+        const int parent = (hole - 1) >> 1;
+        const HeapEntry pe = h[parent];
+        if (!(pe.key < v.key)) break;
+        h[hole] = pe;
+        hole = parent;
+    }
+    h[hole] = v;
+}
+VCU_HEAP_HD void heap_pop_packed(HeapEntry* h, int len) {
+    if (len <= 1) return;
+    const int n = len - 1;
+    const HeapEntry v = h[n];
+    h[n] = h[0];
+    int hole = 0, child = 0;
+    const int lim = (n - 1) / 2;
+    while (child < lim) {
+        child = 2 * (child + 1);
+        child -= (int)(h[child].key < h[child - 1].key);
+        h[hole] = h[child];
+        hole = child;
+    }
+    if ((n & 1) == 0 && child == (n - 2) / 2) {
+        child = 2 * (child + 1);
+        h[hole] = h[child - 1];
+        hole = child - 1;
+    }
+    heap_sift_up_packed(h, hole, v);
+}
+
 }  // namespace vcu
