@@ -2152,6 +2152,8 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
                  o_par = take(cap * 4), o_child = take(cap * 4), o_fa = take(cap * 4), o_fb = take(cap * 4),
                  o_exp = take(cap * 4), o_split = take(cap * 4), o_fresh = take(cap * 4), o_hp = take((N + 1) * 4),
                  o_ctr = take(WC_N * 4), o_ctl = take(sizeof(WaveCtl)), o_hist = take(WAVE_BUCKETS * 4),
+                 o_skey = take(cap * 4), o_sdim = take(cap * 4), o_schild = take(cap * 4),
+                 o_sctr = take(WC_N * 4 + sizeof(WaveCtl)),
                  o_cnt = take(g.nbins * 4),
                  o_off = take((g.nbins + 1) * 4), o_cur = take(g.nbins * 4);
     int rc = ensure(ctx, ctx->scratch, o);
@@ -2219,59 +2221,94 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
     /* fixed grids (the kernels loop over their lists, whose lengths stay on the device) */
     const unsigned gstat = (unsigned)ctx->sm_count * 4;
     const unsigned gsplit = (unsigned)ctx->sm_count * 8, geval = (unsigned)ctx->sm_count * 16;
-    for (int round = 0; round < 8; ++round) {
-        /* waves, WAVE_CHUNK at a time without a host round trip: the device decides between waves
-         * (k_wave_decide) and every kernel of a wave after the last returns at once */
-        for (;;) {
-            for (int wave = 0; wave < WAVE_CHUNK; ++wave) {
-                VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_MAXB, 0, 8, ctx->stream));
-                VCU_CUDA(ctx, cudaMemsetAsync(hist, 0, WAVE_BUCKETS * 4, ctx->stream));
-                k_wave_stats<<<gstat, 256, 0, ctx->stream>>>(fa, fb, ctr + WC_FRONT, bneck, ctr, hist, ctl);
-                k_wave_count<<<gstat, 256, 0, ctx->stream>>>(split, ctr + WC_SPLIT, bneck, ctr, ctl);
-                k_wave_decide<<<1, DECIDE_THREADS, 0, ctx->stream>>>(ctr, hist, ctl, (uint32_t)N, (uint32_t)cap, force);
-                k_wave_select<<<gstat, 256, 0, ctx->stream>>>(fa, fb, ctr + WC_FRONT, bneck, expand, split, ctr, ctl);
-                k_wave_split<F, DIM, SH><<<gsplit, WAVE_WARPS * 32, 0, ctx->stream>>>(
-                    f, expand, ctr + WC_EXPAND, kdim, (uint32_t)cap, vals, rmin, rmax, vol, child, parent, fresh, fa, fb,
-                    ctr, ctl);
-                k_wave_eval<F, DIM, SH, SL><<<geval, WAVE_WARPS * 32, 0, ctx->stream>>>(
-                    tc, fresh, ctr + WC_NEW, vals, rmin, rmax, vol, parent, key, kdim, bneck, ctr, ctl);
-                k_wave_swap<<<1, 1, 0, ctx->stream>>>(ctr, ctl);
-                launches += 7;
-            }
-            VCU_CUDA(ctx, cudaGetLastError());
-            WaveCtl hc{};
-            VCU_CUDA(ctx, cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
-            VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            if (hc.state == WAVE_FAIL) return -1; /* pool too small, or NaN errors: the sequential generator */
-            if (hc.state == WAVE_DONE) break;
+    auto chunk = [&]() -> int {
+        for (int wave = 0; wave < WAVE_CHUNK; ++wave) {
+            VCU_CUDA(ctx, cudaMemsetAsync(ctr + WC_MAXB, 0, 8, ctx->stream));
+            VCU_CUDA(ctx, cudaMemsetAsync(hist, 0, WAVE_BUCKETS * 4, ctx->stream));
+            k_wave_stats<<<gstat, 256, 0, ctx->stream>>>(fa, fb, ctr + WC_FRONT, bneck, ctr, hist, ctl);
+            k_wave_count<<<gstat, 256, 0, ctx->stream>>>(split, ctr + WC_SPLIT, bneck, ctr, ctl);
+            k_wave_decide<<<1, DECIDE_THREADS, 0, ctx->stream>>>(ctr, hist, ctl, (uint32_t)N, (uint32_t)cap, force);
+            k_wave_select<<<gstat, 256, 0, ctx->stream>>>(fa, fb, ctr + WC_FRONT, bneck, expand, split, ctr, ctl);
+            k_wave_split<F, DIM, SH><<<gsplit, WAVE_WARPS * 32, 0, ctx->stream>>>(
+                f, expand, ctr + WC_EXPAND, kdim, (uint32_t)cap, vals, rmin, rmax, vol, child, parent, fresh, fa, fb,
+                ctr, ctl);
+            k_wave_eval<F, DIM, SH, SL><<<geval, WAVE_WARPS * 32, 0, ctx->stream>>>(
+                tc, fresh, ctr + WC_NEW, vals, rmin, rmax, vol, parent, key, kdim, bneck, ctr, ctl);
+            k_wave_swap<<<1, 1, 0, ctx->stream>>>(ctr, ctl);
+            launches += 7;
         }
-        /* replay the reference's heap sequence on the computed errors */
-        uint32_t pool = 0;
-        VCU_CUDA(ctx, cudaMemcpyAsync(&pool, ctr + WC_POOL, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        hkey.resize(pool);
-        hdim.resize(pool);
-        hchild.resize(pool);
-        hb.resize(pool);
-        VCU_CUDA(ctx, cudaMemcpyAsync(hkey.data(), key, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        VCU_CUDA(ctx, cudaMemcpyAsync(hdim.data(), kdim, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        VCU_CUDA(ctx, cudaMemcpyAsync(hchild.data(), child, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        VCU_CUDA(ctx, cudaMemcpyAsync(hb.data(), bneck, pool * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        H[0] = HeapEntry{hkey[0], 0 | (hdim[0] << 24)};
-        int missing = -1;
-        for (size_t it = 0; it < N; ++it) {
+        VCU_CUDA(ctx, cudaGetLastError());
+        return VCU_OK;
+    };
+    /* The heap sequence is replayed on the host while the device runs the next waves: after each
+     * chunk the device copies the loop state, the errors, split dimensions and children into snapshot
+     * buffers; the next chunk is launched at once (it does nothing once the loop is done), and the
+     * copy stream brings the snapshot to the host, where the replay goes on until it meets a region
+     * no wave has split yet.  A region's children and their errors come from the same wave, and a
+     * snapshot is taken between waves, so every region the replay reads is final. */
+    float* skey = reinterpret_cast<float*>(base + o_skey);
+    int* sdim = reinterpret_cast<int*>(base + o_sdim);
+    int* schild = reinterpret_cast<int*>(base + o_schild);
+    uint32_t* sctr = reinterpret_cast<uint32_t*>(base + o_sctr);
+    WaveCtl* sctl = reinterpret_cast<WaveCtl*>(sctr + WC_N);
+    size_t done = 0; /* splits replayed */
+    bool started = false;
+    int missing = -1;
+    auto replay_more = [&]() {
+        if (!started) {
+            H[0] = HeapEntry{hkey[0], 0 | (hdim[0] << 24)};
+            started = true;
+        }
+        missing = -1;
+        while (done < N) {
             const int top = H[0].pay & 0xffffff;
             const int c = hchild[top];
             if (c < 0) {
                 missing = top;
                 break;
             }
-            const int n = (int)it + 1;
+            const int n = (int)done + 1;
             heap_pop_packed(H.data(), n);
             heap_sift_up_packed(H.data(), n - 1, HeapEntry{hkey[c], c | (hdim[c] << 24)});
             heap_sift_up_packed(H.data(), n, HeapEntry{hkey[c + 1], (c + 1) | (hdim[c + 1] << 24)});
+            ++done;
         }
+    };
+    for (int round = 0; round < 8; ++round) {
+        /* waves, WAVE_CHUNK at a time without a host round trip: the device decides between waves
+         * (k_wave_decide) and every kernel of a wave after the last returns at once */
+        if ((rc = chunk())) return rc;
+        for (;;) {
+            VCU_CUDA(ctx, cudaMemcpyAsync(sctr, ctr, WC_N * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(sctl, ctl, sizeof(WaveCtl), cudaMemcpyDeviceToDevice, ctx->stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(skey, key, cap * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(sdim, kdim, cap * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(schild, child, cap * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            VCU_CUDA(ctx, cudaEventRecord(ctx->ev_snap, ctx->stream));
+            if ((rc = chunk())) return rc;
+            VCU_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_snap, 0));
+            uint32_t hctr[WC_N];
+            WaveCtl hc{};
+            VCU_CUDA(ctx, cudaMemcpyAsync(hctr, sctr, WC_N * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(&hc, sctl, sizeof(hc), cudaMemcpyDeviceToHost, ctx->copy_stream));
+            VCU_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+            if (hc.state == WAVE_FAIL) { /* pool too small, or NaN errors: the sequential generator */
+                VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                return -1;
+            }
+            const uint32_t pool = hctr[WC_POOL] < cap ? hctr[WC_POOL] : (uint32_t)cap;
+            hkey.resize(pool);
+            hdim.resize(pool);
+            hchild.resize(pool);
+            VCU_CUDA(ctx, cudaMemcpyAsync(hkey.data(), skey, (size_t)pool * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(hdim.data(), sdim, (size_t)pool * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            VCU_CUDA(ctx, cudaMemcpyAsync(hchild.data(), schild, (size_t)pool * 4, cudaMemcpyDeviceToHost,
+                                          ctx->copy_stream));
+            VCU_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+            replay_more();
+            if (hc.state == WAVE_DONE) break;
+        }
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (missing < 0) {
             for (size_t i = 0; i <= N; ++i) HS[i] = H[i].pay;
             VCU_CUDA(ctx, cudaMemcpyAsync(hp, HS.data(), (N + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -2281,6 +2318,9 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
                                                      reinterpret_cast<uint32_t*>(base + o_cur), d_replay, d_bins,
                                                      d_approx, d_regions, launches);
         }
+        hb.resize(hkey.size());
+        VCU_CUDA(ctx, cudaMemcpyAsync(hb.data(), bneck, hb.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        VCU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         /* the sequence needs a region no wave split: split every unsplit region down to its b */
         uint32_t u;
         std::memcpy(&u, &hb[missing], 4);

@@ -210,6 +210,8 @@ extern "C" int vcu_create(vcu_ctx** out, const vcu_opts* opts) {
     if ((e = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&ctx->ev_tune[0])) != cudaSuccess) return bail(e);
     if ((e = cudaEventCreate(&ctx->ev_tune[1])) != cudaSuccess) return bail(e);
+    if ((e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&ctx->d_status, 256)) != cudaSuccess) return bail(e);
     if ((e = cudaMemset(ctx->d_status, 0, 256)) != cudaSuccess) return bail(e);
     *out = ctx;
@@ -229,6 +231,9 @@ extern "C" int vcu_destroy(vcu_ctx* ctx) {
     for (cudaEvent_t ev : ctx->ev_tune)
         if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->ev_snap) cudaEventDestroy(ctx->ev_snap);
     cudaGetLastError();
     delete ctx;
     return VCU_OK;

@@ -78,6 +78,8 @@ struct vcu_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    cudaStream_t copy_stream = nullptr; /* device-to-host copies that overlap the main stream's work */
+    cudaEvent_t ev_snap = nullptr;      /* orders them after the main stream's snapshot */
     uint32_t* d_status = nullptr; /* one word of device status flags */
     vcu_buffer out, aux, in, scratch;
     vcu_buffer batch_in, batch_pool; /* owned by the batched-integral path only */
