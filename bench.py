@@ -737,6 +737,11 @@ def profile_workload(args) -> dict:
         b = np.empty(r * r * 3, np.float32)
         nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
         call = lambda: ctx.control_variates(p, nst, (1 << 14) - 1, _lib.CvOpts(64, 3, 0, 0, 1.0), b)
+    elif w == "cv_occluded":  # the polynomial control variate of the time-to-RMSE sweep, 256 samples per bin
+        p = ctx.problem(scenes.OCCLUDED_SCENE5, scenes.occluded_scene5(SEED), [0] * 5, [1] * 5, [r, r])
+        b = np.empty(r * r, np.float32)
+        nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
+        call = lambda: ctx.control_variates(p, nst, (1 << 14) - 1, _lib.CvOpts(256, 1, 0, 0, 1.0), b)
     elif w in ("cv_importance", "cv_fubini"):
         nst = _lib.Nested(3, 2, 1, 1, 1e-5, 1e-37, 1e-37)
         if w == "cv_importance":  # rr_pdf_region + region_sampling_importance, alpha 0
@@ -782,8 +787,8 @@ def main(argv=None) -> int:
     ap.add_argument("--res", type=int, default=512, help="bins per side (512 is the benchmark workload)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' lines")
-    ap.add_argument("--workload", choices=["nested", "mc", "cv", "cv_crespo", "cv_importance", "cv_fubini", "batch",
-                             "learned"], default=None,
+    ap.add_argument("--workload", choices=["nested", "mc", "cv", "cv_crespo", "cv_occluded", "cv_importance", "cv_fubini",
+                             "batch", "learned"], default=None,
                     help="profiling aid: one small run of one workload (prints its stats, not a benchmark line)")
     args = ap.parse_args(argv)
     global RES
