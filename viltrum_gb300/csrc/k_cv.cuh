@@ -2251,29 +2251,9 @@ int wave_launch(vcu_ctx* ctx, const F& f, const vcu_problem* p, const BinGrid& g
     int* schild = reinterpret_cast<int*>(base + o_schild);
     uint32_t* sctr = reinterpret_cast<uint32_t*>(base + o_sctr);
     WaveCtl* sctl = reinterpret_cast<WaveCtl*>(sctr + WC_N);
-    size_t done = 0; /* splits replayed */
-    bool started = false;
+    HeapReplay replay{H.data()};
     int missing = -1;
-    auto replay_more = [&]() {
-        if (!started) {
-            H[0] = HeapEntry{hkey[0], 0 | (hdim[0] << 24)};
-            started = true;
-        }
-        missing = -1;
-        while (done < N) {
-            const int top = H[0].pay & 0xffffff;
-            const int c = hchild[top];
-            if (c < 0) {
-                missing = top;
-                break;
-            }
-            const int n = (int)done + 1;
-            heap_pop_packed(H.data(), n);
-            heap_sift_up_packed(H.data(), n - 1, HeapEntry{hkey[c], c | (hdim[c] << 24)});
-            heap_sift_up_packed(H.data(), n, HeapEntry{hkey[c + 1], (c + 1) | (hdim[c + 1] << 24)});
-            ++done;
-        }
-    };
+    auto replay_more = [&]() { missing = replay.run(N, hkey.data(), hdim.data(), hchild.data()); };
     for (int round = 0; round < 8; ++round) {
         /* waves, WAVE_CHUNK at a time without a host round trip: the device decides between waves
          * (k_wave_decide) and every kernel of a wave after the last returns at once */

@@ -14,6 +14,7 @@
  * Host and device compile the same code; tests/test_heap.py checks it against std::.
  */
 #pragma once
+#include <cstddef>
 
 #if defined(__CUDACC__)
 #define VCU_HEAP_HD __host__ __device__ __forceinline__
@@ -182,5 +183,35 @@ VCU_HEAP_HD void heap_pop_packed(HeapEntry* h, int len) {
     }
     heap_sift_up_packed(h, hole, v);
 }
+
+/* The reference's heap sequence over a tree of regions known in stages (the control-variate waves
+ * reveal which regions split, and into which children, a chunk of waves at a time): region x's
+ * children are child[x] and child[x] + 1 (child[x] < 0: not known yet), key[] its error, dim[] its
+ * split dimension.  run() pops the top region and pushes its two children, as
+ * regions-generator-adaptive-heap.h:25-43 does, until n_splits splits are done or the top region's
+ * children are not known yet; it returns that region (-1 when done) and resumes from there on the
+ * next call, so replaying in stages gives the array one pass over the finished tree gives. */
+struct HeapReplay {
+    HeapEntry* h;        /* n_splits + 2 entries */
+    size_t done = 0;     /* splits replayed */
+    bool started = false;
+    int run(size_t n_splits, const float* key, const int* dim, const int* child) {
+        if (!started) {
+            h[0] = HeapEntry{key[0], 0 | (dim[0] << 24)};
+            started = true;
+        }
+        while (done < n_splits) {
+            const int top = h[0].pay & 0xffffff;
+            const int c = child[top];
+            if (c < 0) return top;
+            const int n = (int)done + 1;
+            heap_pop_packed(h, n);
+            heap_sift_up_packed(h, n - 1, HeapEntry{key[c], c | (dim[c] << 24)});
+            heap_sift_up_packed(h, n, HeapEntry{key[c + 1], (c + 1) | (dim[c + 1] << 24)});
+            ++done;
+        }
+        return -1;
+    }
+};
 
 }  // namespace vcu
