@@ -12,14 +12,15 @@
  *     estimates with the reference's rounding, libstdc++ heap order).  From 128 splits on, in waves
  *     (wave_launch, below): the regions of largest bottleneck error are split together, one warp per
  *     region, the waves decided on the device, and the host replays the heap sequence on their
- *     errors.  Below that, or when the waves
+ *     errors (HeapReplay, overlapping the next waves).  Below that, or when the waves
  *     give up (NaN errors, a pool overflow from masses of equal errors), k_cv_generate: ONE
  *     cooperative thread block splitting in order, the heap in shared memory (up to ~28k regions) or
  *     global memory, each split's new nodes and both children's error folds evaluated by the block
  *     in parallel.  Node values, ranges and volumes of every region built live in a global pool (a
  *     region's slot never moves; the heap holds pool ids).
- *  2. k_cv_count / k_cv_fill / k_cv_sort: per-bin region lists.  Every region, in heap order, is
- *     appended to the bins pixels_in_region gives (src/newton-cotes/region.h:454-463, the 0.99 rule),
+ *  2. k_cv_lists (count, then fill) / k_cv_scan_* / k_cv_sort: per-bin region lists.  Every region,
+ *     in heap order, is appended to the bins pixels_in_region gives (src/newton-cotes/region.h:454-463,
+ *     the 0.99 rule),
  *     as the reference's stratification does (regions-integrator-parallel-variance-reduction.h:49-57):
  *     count per bin, exclusive scan, fill, then sort each bin's list by heap position so the order
  *     is the reference's sequential order.
@@ -29,7 +30,10 @@
  *     volume), pushes f*w and g*w (g = the region polynomial, region.h:103-112) into the
  *     cv_optimize_weight / cv_fixed_weight estimator (weight-strategy.h:7-110); sums in FP32 (Kahan
  *     per lane, float-float across lanes), moments FP32 per lane and float-float across lanes, the
- *     final recombination (sum_f - a*sum_g)/n + a*approximation in FP64.  Sample j of bin b draws from
+ *     final recombination (sum_f - a*sum_g)/n + a*approximation in float-float.  Up to 3 dimensions a
+ *     sample's polynomial starts from the first-fold coefficients k_cv_coef precomputes per listed
+ *     region; uniform points are drawn and evaluated in pairs where the integrand has a two-point culled
+ *     form.  Sample j of bin b draws from
  *     Philox4x32-10 (key = seed, counter = (j, b_lo, b_hi, 0xC0DE0000 | block)), or replays given
  *     (chosen list index, point) records.
  */
@@ -901,8 +905,8 @@ __global__ void __launch_bounds__(RES_WARPS * 32, (!PDF && DIM <= 3) ? 6 : 1)
     /* residual samples */
     /* per lane, in FP32: Kahan sums of the weighted samples, and the covariance moments of the
      * sample norms (weight-strategy.h:187-208) by Welford's update.  Across lanes the sums merge as
-     * float-float pairs (two-sum, FP32) and the moments by Chan's formulas in float-float; only the
-     * recombination is FP64 -- FP64 runs at a small fraction of the FP32 rate here */
+     * float-float pairs (two-sum, FP32) and the moments by Chan's formulas in float-float, as is the
+     * recombination -- FP64 runs at a small fraction of the FP32 rate here */
     float sf32[CH], cf32[CH], sa32[CH], ca32[CH];
     for (int c = 0; c < CH; ++c) sf32[c] = cf32[c] = sa32[c] = ca32[c] = 0.0f;
     float wn32 = 0.0f, mf32 = 0.0f, ma32 = 0.0f, m2a32 = 0.0f, cfa32 = 0.0f, m2f32 = 0.0f;
